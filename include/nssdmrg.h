@@ -1,0 +1,230 @@
+/*
+ * nssdmrg.h -- C ABI of the GB300 superblock eigensolver for nssDMRG.
+ *
+ * The reference library (Fortran, aamaricci/nssDMRG) runs its superblock
+ * eigensolve through three seams, and this ABI replaces each of them:
+ *
+ *  1. the H·v callback.  `procedure(sparse_HxV), pointer :: spHtimesV_p`
+ *     (src/DMRG_GLOBAL.f90:41-53) is pointed at spMatVec_direct_main
+ *     (src/DMRG_SUPERBLOCK_SETUP.f90:740-865), which reads the module-global
+ *     operator pool Hleft, Hright, A, B, Dls, Drs, Offset, RowOffset,
+ *     ColOffset, isb2jsb, IsHconjg (src/DMRG_GLOBAL.f90:119-124).
+ *     nss_sb_upload() takes that pool once per DMRG step; nss_hv() has the
+ *     sparse_HxV(Nloc, v, Hv) semantics.
+ *  2. the eigensolver.  sb_diag calls SciFortran sp_eigh(spHtimesV_p, ...)
+ *     (src/DMRG_SUPERBLOCK.f90:335-474); nss_eigh() replaces that call.
+ *  3. the RDM.  sb_get_rdm + blocks_matrix%eigh + the truncation choice of
+ *     renormalize_block (src/DMRG_RDM.f90:18-221, :277-294;
+ *     src/MATRIX/MATRIX_BLOCKS.f90:589-657) become nss_rdm().
+ *
+ * Every entry point returns 0 on success or a negative NSS_ERR_* code; none
+ * aborts.  nss_last_error() gives the message (the reference `stop`s with a
+ * message instead).  A context is single-caller and not re-entrant.
+ * Indices in this ABI are 0-based (the reference is 1-based).
+ */
+#ifndef NSSDMRG_H
+#define NSSDMRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSS_OK               0
+#define NSS_ERR_INVALID     -1   /* bad argument or inconsistent descriptor */
+#define NSS_ERR_CUDA        -2   /* CUDA runtime or library error */
+#define NSS_ERR_NOMEM       -3   /* allocation failed or over the HBM budget */
+#define NSS_ERR_STATE       -4   /* call out of order (e.g. nss_hv before upload) */
+#define NSS_ERR_NOCONV      -5   /* eigensolver hit its iteration cap */
+#define NSS_ERR_ASYMMETRIC  -6   /* rho not symmetric to 1e-12 (DMRG_RDM.f90:159-160) */
+#define NSS_ERR_NOCUDA      -7   /* no CUDA device */
+
+/* Precision modes for nss_eigh. */
+#define NSS_PREC_FP64        0   /* plain method: every product in FP64 */
+#define NSS_PREC_MIXED       1   /* sector GEMMs on tensor cores, FP64 Lanczos + refinement */
+
+typedef struct nss_ctx nss_ctx;
+
+/* One sparse operator block in row-list (CSR) form, 0-based.  A block with
+ * nrow == 0 is "absent" (the reference's status=.false.). */
+typedef struct {
+    int32_t nrow, ncol;
+    const int32_t *rowptr;   /* nrow+1 entries */
+    const int32_t *colidx;   /* rowptr[nrow] entries */
+    const double  *vals;     /* rowptr[nrow] entries */
+} nss_csr;
+
+/* The direct-mode operator pool, flattened.  Arrays of length nsb are per
+ * superblock sector k; arrays of length tnso*nsb are indexed it + tnso*k,
+ * the column-major order of the reference's A(it,k). */
+typedef struct {
+    int32_t nsb;              /* size(sb_sector) */
+    int32_t tnso;             /* terms per sector (3 spin, 4 Hubbard, OBC) */
+    int32_t m_left, m_right;  /* dims of the enlarged left/right blocks */
+    const int32_t *dls;       /* [nsb] Dls(k) */
+    const int32_t *drs;       /* [nsb] Drs(k) */
+    const int64_t *offset;    /* [nsb] Offset(k) */
+    const int32_t *ai;        /* [sum dls] left block states of each sector (AI), ascending */
+    const int32_t *bi;        /* [sum drs] right block states of each sector (BI), ascending */
+    const nss_csr *hleft;     /* [nsb]  Hleft(k)  Dl x Dl */
+    const nss_csr *hright;    /* [nsb]  Hright(k) Dr x Dr */
+    const nss_csr *a;         /* [tnso*nsb] A(it,k) */
+    const nss_csr *b;         /* [tnso*nsb] B(it,k) */
+    const int32_t *isb2jsb;   /* [tnso*nsb] isb2jsb(it,k), 0-based (unused when absent) */
+    const int32_t *ishconjg;  /* [tnso*nsb] IsHconjg(it,k) */
+    const int64_t *row_offset;/* [tnso*nsb] RowOffset(it,k) */
+    const int64_t *col_offset;/* [tnso*nsb] ColOffset(it,k) */
+} nss_sb_desc;
+
+/* Create a context on CUDA device `device`.  hbm_budget (bytes) caps what
+ * the context may allocate; 0 means no cap.  Returns NULL on failure; the
+ * reason is then available from nss_last_error(NULL). */
+nss_ctx    *nss_create(int device, size_t hbm_budget);
+void        nss_destroy(nss_ctx *ctx);
+const char *nss_last_error(const nss_ctx *ctx);
+
+/* Upload the superblock operator pool; replaces the Setup_SuperBlock_Direct
+ * -> spHtimesV_p assignment (src/DMRG_SUPERBLOCK.f90:553-573,
+ * src/DMRG_SUPERBLOCK_SETUP.f90:113-136).  Copies everything: the caller
+ * may free its arrays on return.  Replaces any previous superblock. */
+int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc);
+/* Free the device superblock (sb_delete_Hv, src/DMRG_SUPERBLOCK.f90:582-620). */
+int nss_sb_free(nss_ctx *ctx);
+/* Vector length of the uploaded superblock (sb_vecDim_Hv, :626-646). */
+int64_t nss_sb_dim(const nss_ctx *ctx);
+
+/* sparse_HxV: hv = H_sb v for host vectors of length n (must equal
+ * nss_sb_dim).  spMatVec_direct_main semantics: hv is overwritten. */
+int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv);
+/* Same on device pointers, ordered on the context's stream. */
+int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv);
+
+/* Lowest `neigen` eigenpairs of the uploaded H_sb (replaces sp_eigh at
+ * src/DMRG_SUPERBLOCK.f90:394-425).  nitermax caps the Krylov dimension,
+ * tol is the relative residual tolerance (lanc_tolerance), seed fixes the
+ * random start vector.  evals[neigen] receives the eigenvalues (ascending);
+ * evecs, if not NULL, receives the n x neigen eigenvectors (column-major,
+ * the reference's gs_vector); they also stay resident on the device for
+ * nss_rdm.  numop (may be NULL) receives the number of H·v products.
+ * ncv is accepted for interface parity with sp_eigh and ignored (the solver
+ * keeps the whole Krylov basis instead of restarting). */
+int nss_eigh(nss_ctx *ctx, int neigen, int nitermax, int ncv, double tol,
+             uint64_t seed, int precision, double *evals, double *evecs,
+             int *numop);
+
+/* Result of nss_rdm for one side of the superblock. */
+typedef struct {
+    int32_t nevals;        /* number of rho eigenvalues (= sum of block sizes) */
+    int32_t m_s;           /* kept states after the degeneracy extension */
+    double  trunc_err;     /* 1 - sum(lambda(1:m_s)) */
+    double  entropy;       /* -sum lambda log(lambda + 1e-32) */
+} nss_rdm_side;
+
+/* Reduced density matrices of the ground state (column 0 of the last
+ * nss_eigh, or `psi` when not NULL, length nss_sb_dim), their block
+ * eigendecomposition and the truncation choice (src/DMRG_RDM.f90:18-221,
+ * :277-294).  mstates is Mstates, deg_thr is deg_evals_threshold.  Per side
+ * (index 0 left, 1 right) the optional outputs are
+ *   lambda[side]  : nevals eigenvalues, descending, negatives clipped to 0
+ *   kept_blk[side]: m_s ints, the rho block (= superblock sector) of each
+ *                   kept column, in rank order (its QN is the block's QN)
+ *   u[side]       : m_block x m_s column-major rotation matrix (U = trRho)
+ * with m_block = m_left / m_right of the descriptor.  Any may be NULL. */
+int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
+            nss_rdm_side out[2], double *lambda_left, double *lambda_right,
+            int32_t *kept_left, int32_t *kept_right,
+            double *u_left, double *u_right);
+
+/* ---------------------------------------------------------------------------
+ * Block-level superblock setup (the enumeration and operator-pool build of
+ * sb_get_states / sb_build_dims / Setup_SuperBlock_{Spin,Fermion}_Direct,
+ * src/DMRG_SUPERBLOCK.f90:36-283 and src/DMRG_SUPERBLOCK_SETUP.f90:152-693,
+ * :1079-1122), for callers that hand over the enlarged blocks instead of a
+ * ready pool.  Operators are full block matrices in CSR form.
+ * ------------------------------------------------------------------------- */
+#define NSS_SITE_SPIN      0   /* operators S_z_n, S_p_n */
+#define NSS_SITE_FERMION   1   /* operators C_l1_s1_n, C_l1_s2_n, P_n */
+
+typedef struct {
+    int32_t dim;            /* block dimension */
+    int32_t qdim;           /* QN tuple length */
+    const double *basis;    /* [dim*qdim] QN tuple of every state (row-major) */
+    nss_csr h;              /* "H" */
+    nss_csr op[3];          /* spin: Sz, S+ ; fermion: C_up, C_dw, P */
+} nss_block_desc;
+
+/* Enumerate the superblock of target QN `target` (qdim values) and upload
+ * its operator pool.  site_type is NSS_SITE_*; hij is the Nso x Nso coupling
+ * matrix (row-major, Nso = 2), the reference's HopH. */
+int nss_sb_setup(nss_ctx *ctx, int site_type, const nss_block_desc *left,
+                 const nss_block_desc *right, const double *target,
+                 const double *hij);
+/* Sector tables of the current superblock: nsb, sector QNs (left QN, qdim
+ * each), Dls, Drs, Offset and sb_states (left*m_right + right, 0-based).
+ * Pass NULL for anything not wanted; sizes from nss_sb_counts. */
+int nss_sb_counts(const nss_ctx *ctx, int32_t *nsb, int32_t *qdim, int64_t *n);
+int nss_sb_tables(const nss_ctx *ctx, double *qns, int32_t *dls, int32_t *drs,
+                  int64_t *offset, int64_t *sb_states);
+
+/* ---------------------------------------------------------------------------
+ * DMRG driver (init_dmrg / run_DMRG / finalize_dmrg, src/DMRG_MAIN.f90:9-14,
+ * :22-72, :140-241, :262-433): OBC infinite and finite algorithms with every
+ * superblock solve on the GPU.
+ * ------------------------------------------------------------------------- */
+#define NSS_MODEL_HEISENBERG_HALF 0   /* spin_site(sun=2) */
+#define NSS_MODEL_HEISENBERG_ONE  1   /* spin_site(sun=3) */
+#define NSS_MODEL_HUBBARD         2   /* electron_site, Norb=1 */
+
+typedef struct {
+    int32_t model;          /* NSS_MODEL_* */
+    double  jz, jxy;        /* Heisenberg: Hlr = diag(jz, jxy/2) */
+    double  t, u;           /* Hubbard: Hlr = diag(-t,-t), Uloc = u */
+    int32_t hfmode;         /* Hubbard Hartree shift (HFMODE) */
+    double  dmrg_qn[2];     /* target QN in units of L (DMRG_QN, QNtype local) */
+    int32_t ldmrg;          /* Ldmrg */
+    int32_t mdmrg;          /* Mdmrg */
+    int32_t nsweep;         /* number of finite sweeps (0: infinite only) */
+    const int32_t *msweep;  /* [nsweep] states per sweep */
+    int32_t lanc_neigen;    /* default 2 */
+    int32_t lanc_niter;     /* default 512 */
+    double  lanc_tolerance; /* default 1e-12 */
+    double  deg_evals_threshold; /* default 0.1 */
+    uint64_t seed;
+    int32_t precision;      /* NSS_PREC_* */
+} nss_dmrg_params;
+
+typedef struct {
+    int32_t type;           /* 0 infinite, 1 finite */
+    int32_t left_length, right_length, current_l;
+    int64_t n;              /* superblock dimension */
+    int32_t nsb;
+    int32_t numop;
+    double  energy[2];      /* gs_energy / current_L / Norb (lanc_neigen <= 2) */
+    double  entropy_left, entropy_right;
+    double  trunc_left, trunc_right;
+    int32_t m_left, m_right;   /* block dims after the step */
+    double  ms_solve;       /* device time of nss_eigh + nss_rdm */
+} nss_step_record;
+
+typedef struct nss_dmrg nss_dmrg;
+
+nss_dmrg *nss_dmrg_create(nss_ctx *ctx, const nss_dmrg_params *p);
+void      nss_dmrg_destroy(nss_dmrg *d);
+int       nss_dmrg_infinite(nss_dmrg *d);
+int       nss_dmrg_finite(nss_dmrg *d);
+/* Run the infinite algorithm up to the last step and stop after building and
+ * uploading that step's superblock (no solve), for benchmarking. */
+int       nss_dmrg_prepare_last(nss_dmrg *d);
+/* The superblock operator pool of the step nss_dmrg_prepare_last stopped at,
+ * as the descriptor a Fortran caller would pass to nss_sb_upload (valid until
+ * the next call on d). */
+int       nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out);
+int       nss_dmrg_nrecords(const nss_dmrg *d);
+int       nss_dmrg_records(const nss_dmrg *d, nss_step_record *out, int max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSSDMRG_H */

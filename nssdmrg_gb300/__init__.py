@@ -1,0 +1,387 @@
+"""GB300-native superblock eigensolver for nssDMRG.
+
+A thin Python view of the C ABI in ``include/nssdmrg.h`` (``libnssdmrg.so``,
+built by ``nssdmrg_gb300.build``).  The names mirror the reference library's
+Fortran procedures that the ABI replaces:
+
+* ``Superblock.upload``      -- the operator pool of Setup_SuperBlock_Direct
+* ``Superblock.setup``       -- sb_get_states + sb_build_dims + Setup_SuperBlock_Direct
+* ``Superblock.spmatvec``    -- spMatVec_direct_main (the sparse_HxV callback)
+* ``Superblock.sb_diag``     -- sb_diag's Lanczos branch (replaces sp_eigh)
+* ``Superblock.sb_get_rdm``  -- sb_get_rdm + block eigh + truncation choice
+* ``DMRG``                   -- init_dmrg / run_DMRG (infinite, finite)
+
+There is no CPU fallback: every call goes to the CUDA library, and loading
+fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libnssdmrg.so"
+
+NSS_OK = 0
+NSS_ERR_INVALID = -1
+NSS_ERR_CUDA = -2
+NSS_ERR_NOMEM = -3
+NSS_ERR_STATE = -4
+NSS_ERR_NOCONV = -5
+NSS_ERR_ASYMMETRIC = -6
+NSS_PREC_FP64 = 0
+NSS_PREC_MIXED = 1
+NSS_SITE_SPIN = 0
+NSS_SITE_FERMION = 1
+MODEL_HEISENBERG_HALF = 0
+MODEL_HEISENBERG_ONE = 1
+MODEL_HUBBARD = 2
+
+
+class NssError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nssdmrg error {code}: {msg}")
+        self.code = code
+
+
+class Csr(C.Structure):
+    _fields_ = [("nrow", C.c_int32), ("ncol", C.c_int32), ("rowptr", C.POINTER(C.c_int32)),
+                ("colidx", C.POINTER(C.c_int32)), ("vals", C.POINTER(C.c_double))]
+
+
+class SbDesc(C.Structure):
+    _fields_ = [("nsb", C.c_int32), ("tnso", C.c_int32), ("m_left", C.c_int32), ("m_right", C.c_int32),
+                ("dls", C.POINTER(C.c_int32)), ("drs", C.POINTER(C.c_int32)), ("offset", C.POINTER(C.c_int64)),
+                ("ai", C.POINTER(C.c_int32)), ("bi", C.POINTER(C.c_int32)),
+                ("hleft", C.POINTER(Csr)), ("hright", C.POINTER(Csr)),
+                ("a", C.POINTER(Csr)), ("b", C.POINTER(Csr)),
+                ("isb2jsb", C.POINTER(C.c_int32)), ("ishconjg", C.POINTER(C.c_int32)),
+                ("row_offset", C.POINTER(C.c_int64)), ("col_offset", C.POINTER(C.c_int64))]
+
+
+class RdmSide(C.Structure):
+    _fields_ = [("nevals", C.c_int32), ("m_s", C.c_int32), ("trunc_err", C.c_double), ("entropy", C.c_double)]
+
+
+class BlockDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("qdim", C.c_int32), ("basis", C.POINTER(C.c_double)),
+                ("h", Csr), ("op", Csr * 3)]
+
+
+class DmrgParams(C.Structure):
+    _fields_ = [("model", C.c_int32), ("jz", C.c_double), ("jxy", C.c_double), ("t", C.c_double),
+                ("u", C.c_double), ("hfmode", C.c_int32), ("dmrg_qn", C.c_double * 2), ("ldmrg", C.c_int32),
+                ("mdmrg", C.c_int32), ("nsweep", C.c_int32), ("msweep", C.POINTER(C.c_int32)),
+                ("lanc_neigen", C.c_int32), ("lanc_niter", C.c_int32), ("lanc_tolerance", C.c_double),
+                ("deg_evals_threshold", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int32)]
+
+
+class StepRecord(C.Structure):
+    _fields_ = [("type", C.c_int32), ("left_length", C.c_int32), ("right_length", C.c_int32),
+                ("current_l", C.c_int32), ("n", C.c_int64), ("nsb", C.c_int32), ("numop", C.c_int32),
+                ("energy", C.c_double * 2), ("entropy_left", C.c_double), ("entropy_right", C.c_double),
+                ("trunc_left", C.c_double), ("trunc_right", C.c_double), ("m_left", C.c_int32),
+                ("m_right", C.c_int32), ("ms_solve", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libnssdmrg.so (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run nssdmrg_gb300.build.build() first "
+                          "(there is no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "nss_create": (P, [C.c_int, C.c_size_t]),
+        "nss_destroy": (None, [P]),
+        "nss_last_error": (C.c_char_p, [P]),
+        "nss_sb_upload": (C.c_int, [P, C.POINTER(SbDesc)]),
+        "nss_sb_free": (C.c_int, [P]),
+        "nss_sb_dim": (I64, [P]),
+        "nss_hv": (C.c_int, [P, I64, P, P]),
+        "nss_hv_device": (C.c_int, [P, I64, P, P]),
+        "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
+        "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
+        "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
+        "nss_sb_counts": (C.c_int, [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]),
+        "nss_sb_tables": (C.c_int, [P, P, P, P, P, P]),
+        "nss_dmrg_create": (P, [P, C.POINTER(DmrgParams)]),
+        "nss_dmrg_destroy": (None, [P]),
+        "nss_dmrg_infinite": (C.c_int, [P]),
+        "nss_dmrg_finite": (C.c_int, [P]),
+        "nss_dmrg_prepare_last": (C.c_int, [P]),
+        "nss_dmrg_export_superblock": (C.c_int, [P, C.POINTER(SbDesc)]),
+        "nss_dmrg_nrecords": (C.c_int, [P]),
+        "nss_dmrg_records": (C.c_int, [P, C.POINTER(StepRecord), C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class _Keep:
+    """Keeps numpy buffers alive while a ctypes descriptor points at them."""
+
+    def __init__(self):
+        self.refs = []
+
+    def arr(self, a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self.refs.append(a)
+        return a
+
+    def csr(self, m) -> Csr:
+        """scipy.sparse matrix (or None = absent block) -> nss_csr."""
+        c = Csr()
+        if m is None:
+            c.nrow = 0
+            c.ncol = 0
+            return c
+        m = m.tocsr()
+        rp = self.arr(m.indptr, np.int32)
+        ci = self.arr(m.indices, np.int32)
+        va = self.arr(m.data, np.float64)
+        c.nrow, c.ncol = m.shape
+        c.rowptr = _p(rp, C.c_int32)
+        c.colidx = _p(ci, C.c_int32)
+        c.vals = _p(va, C.c_double)
+        return c
+
+
+@dataclass
+class RdmResult:
+    m_s: tuple
+    trunc_err: tuple
+    entropy: tuple
+    lambdas: tuple       # descending eigenvalues, left and right
+    kept_blocks: tuple   # rho block (= sector) of each kept state
+    u: tuple             # rotation matrices [m_block x m_s]
+
+
+class Superblock:
+    """One GPU context holding one superblock (the reference's H*v pool)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        L = lib()
+        self._ctx = L.nss_create(device, hbm_budget)
+        if not self._ctx:
+            raise NssError(NSS_ERR_CUDA, L.nss_last_error(None).decode())
+        self._keep = None
+        self.m_left = self.m_right = 0
+
+    def close(self):
+        if self._ctx:
+            lib().nss_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != NSS_OK:
+            raise NssError(rc, lib().nss_last_error(self._ctx).decode())
+
+    @property
+    def n(self) -> int:
+        return int(lib().nss_sb_dim(self._ctx))
+
+    # -- the operator pool as the reference keeps it (DMRG_GLOBAL.f90:119-124)
+    def upload(self, dls, drs, offset, hleft, hright, terms, tnso, m_left, m_right, ai=None, bi=None):
+        """terms: list of (it, k, jsb, hconj, A, B, row_offset, col_offset)
+        with it 0-based; A/B scipy sparse matrices."""
+        keep = _Keep()
+        nsb = len(dls)
+        d = SbDesc()
+        d.nsb, d.tnso, d.m_left, d.m_right = nsb, tnso, m_left, m_right
+        dl = keep.arr(dls, np.int32)
+        dr = keep.arr(drs, np.int32)
+        off = keep.arr(offset, np.int64)
+        d.dls, d.drs, d.offset = _p(dl, C.c_int32), _p(dr, C.c_int32), _p(off, C.c_int64)
+        if ai is not None:
+            a_ = keep.arr(np.concatenate(ai), np.int32)
+            b_ = keep.arr(np.concatenate(bi), np.int32)
+            d.ai, d.bi = _p(a_, C.c_int32), _p(b_, C.c_int32)
+        hl = (Csr * nsb)(*[keep.csr(h) for h in hleft])
+        hr = (Csr * nsb)(*[keep.csr(h) for h in hright])
+        nt = max(1, tnso * nsb)
+        A = (Csr * nt)()
+        B = (Csr * nt)()
+        isb = np.full(nt, -1, np.int32)
+        hc = np.zeros(nt, np.int32)
+        ro = np.zeros(nt, np.int64)
+        co = np.zeros(nt, np.int64)
+        for (it, k, jsb, hconj, a, b, r_off, c_off) in terms:
+            idx = it + tnso * k
+            A[idx] = keep.csr(a)
+            B[idx] = keep.csr(b)
+            isb[idx], hc[idx], ro[idx], co[idx] = jsb, hconj, r_off, c_off
+        keep.refs += [hl, hr, A, B]
+        isb, hc, ro, co = (keep.arr(isb, np.int32), keep.arr(hc, np.int32), keep.arr(ro, np.int64),
+                           keep.arr(co, np.int64))
+        d.hleft = C.cast(hl, C.POINTER(Csr))
+        d.hright = C.cast(hr, C.POINTER(Csr))
+        d.a = C.cast(A, C.POINTER(Csr))
+        d.b = C.cast(B, C.POINTER(Csr))
+        d.isb2jsb, d.ishconjg = _p(isb, C.c_int32), _p(hc, C.c_int32)
+        d.row_offset, d.col_offset = _p(ro, C.c_int64), _p(co, C.c_int64)
+        self._check(lib().nss_sb_upload(self._ctx, C.byref(d)))
+        self.m_left, self.m_right = m_left, m_right
+
+    def upload_desc(self, desc: SbDesc):
+        self._check(lib().nss_sb_upload(self._ctx, C.byref(desc)))
+        self.m_left, self.m_right = desc.m_left, desc.m_right
+
+    def setup(self, site_type, left, right, target, hij):
+        """Block-level setup.  left/right: dicts with 'basis' [dim,qdim],
+        'H' and the model operators (spin: S_z_n, S_p_n; fermion: C_l1_s1_n,
+        C_l1_s2_n, P_n) as scipy sparse matrices."""
+        keep = _Keep()
+
+        def bd(blk):
+            b = BlockDesc()
+            basis = keep.arr(blk["basis"], np.float64)
+            b.dim, b.qdim = basis.shape
+            b.basis = _p(basis, C.c_double)
+            b.h = keep.csr(blk["H"])
+            keys = ("S_z_n", "S_p_n") if site_type == NSS_SITE_SPIN else ("C_l1_s1_n", "C_l1_s2_n", "P_n")
+            for i, k in enumerate(keys):
+                b.op[i] = keep.csr(blk[k])
+            return b
+
+        L, R = bd(left), bd(right)
+        t = keep.arr(target, np.float64)
+        h = keep.arr(np.asarray(hij, np.float64).reshape(-1), np.float64)
+        self._check(lib().nss_sb_setup(self._ctx, site_type, C.byref(L), C.byref(R), _ptr(t), _ptr(h)))
+        self.m_left, self.m_right = L.dim, R.dim
+
+    def tables(self):
+        """Sector tables of the last setup(): qns, Dls, Drs, Offset, sb_states."""
+        L = lib()
+        nsb, qdim, n = C.c_int32(), C.c_int32(), C.c_int64()
+        self._check(L.nss_sb_counts(self._ctx, C.byref(nsb), C.byref(qdim), C.byref(n)))
+        qns = np.zeros((nsb.value, qdim.value))
+        dls = np.zeros(nsb.value, np.int32)
+        drs = np.zeros(nsb.value, np.int32)
+        off = np.zeros(nsb.value, np.int64)
+        st = np.zeros(n.value, np.int64)
+        self._check(L.nss_sb_tables(self._ctx, _ptr(qns), _ptr(dls), _ptr(drs), _ptr(off), _ptr(st)))
+        return qns, dls, drs, off, st
+
+    # -- sparse_HxV
+    def spmatvec(self, v: np.ndarray) -> np.ndarray:
+        v = np.ascontiguousarray(v, np.float64)
+        hv = np.empty_like(v)
+        self._check(lib().nss_hv(self._ctx, v.size, _ptr(v), _ptr(hv)))
+        return hv
+
+    def sb_diag(self, neigen=1, nitermax=512, tol=1e-12, seed=1234, precision=NSS_PREC_FP64,
+                want_vectors=True, ncv=0):
+        ev = np.zeros(max(1, neigen))
+        n = self.n
+        vec = np.zeros((max(1, neigen), n)) if want_vectors else None
+        numop = C.c_int()
+        self._check(lib().nss_eigh(self._ctx, neigen, nitermax, ncv, tol, seed, precision, _ptr(ev),
+                                   _ptr(vec) if vec is not None else None, C.byref(numop)))
+        ne = min(neigen, n)
+        return ev[:ne], (vec[:ne].T if vec is not None else None), numop.value
+
+    def sb_get_rdm(self, mstates, deg_thr=0.1, psi=None, want_u=True) -> RdmResult:
+        out = (RdmSide * 2)()
+        ml, mr = self.m_left, self.m_right
+        lam_l, lam_r = np.zeros(ml), np.zeros(mr)
+        kl, kr = np.zeros(ml, np.int32), np.zeros(mr, np.int32)
+        ul = np.zeros(ml * ml) if want_u else None
+        ur = np.zeros(mr * mr) if want_u else None
+        p = np.ascontiguousarray(psi, np.float64) if psi is not None else None
+        self._check(lib().nss_rdm(self._ctx, _ptr(p) if p is not None else None, mstates, deg_thr, out,
+                                  _ptr(lam_l), _ptr(lam_r), _ptr(kl), _ptr(kr),
+                                  _ptr(ul) if want_u else None, _ptr(ur) if want_u else None))
+        ms = (out[0].m_s, out[1].m_s)
+        us = (None, None)
+        if want_u:
+            us = (ul[: ml * ms[0]].reshape(ms[0], ml).T, ur[: mr * ms[1]].reshape(ms[1], mr).T)
+        return RdmResult(ms, (out[0].trunc_err, out[1].trunc_err), (out[0].entropy, out[1].entropy),
+                         (lam_l[: out[0].nevals], lam_r[: out[1].nevals]), (kl[: ms[0]], kr[: ms[1]]), us)
+
+
+class DMRG:
+    """init_dmrg / run_DMRG with every superblock solve on the GPU."""
+
+    def __init__(self, model, ldmrg, mdmrg, msweep=(), jz=1.0, jxy=1.0, t=1.0, u=0.0, hfmode=True,
+                 dmrg_qn=(0.0, 0.0), lanc_neigen=1, lanc_niter=512, lanc_tolerance=1e-12,
+                 deg_evals_threshold=0.1, seed=1234, precision=NSS_PREC_FP64, device=0, sb=None):
+        self.sb = sb or Superblock(device)
+        p = DmrgParams()
+        p.model, p.jz, p.jxy, p.t, p.u, p.hfmode = model, jz, jxy, t, u, int(hfmode)
+        p.dmrg_qn[0] = dmrg_qn[0]
+        p.dmrg_qn[1] = dmrg_qn[1] if len(dmrg_qn) > 1 else 0.0
+        p.ldmrg, p.mdmrg = ldmrg, mdmrg
+        self._ms = np.ascontiguousarray(msweep, np.int32) if len(msweep) else np.zeros(1, np.int32)
+        p.nsweep = len(msweep)
+        p.msweep = _p(self._ms, C.c_int32)
+        p.lanc_neigen, p.lanc_niter, p.lanc_tolerance = lanc_neigen, lanc_niter, lanc_tolerance
+        p.deg_evals_threshold, p.seed, p.precision = deg_evals_threshold, seed, precision
+        self._p = p
+        self._d = lib().nss_dmrg_create(self.sb._ctx, C.byref(p))
+        if not self._d:
+            raise NssError(NSS_ERR_INVALID, lib().nss_last_error(self.sb._ctx).decode())
+
+    def close(self):
+        if getattr(self, "_d", None):
+            lib().nss_dmrg_destroy(self._d)
+            self._d = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def infinite(self):
+        self.sb._check(lib().nss_dmrg_infinite(self._d))
+        return self.records()
+
+    def finite(self):
+        self.sb._check(lib().nss_dmrg_finite(self._d))
+        return self.records()
+
+    def prepare_last(self):
+        self.sb._check(lib().nss_dmrg_prepare_last(self._d))
+
+    def export_superblock(self) -> SbDesc:
+        d = SbDesc()
+        self.sb._check(lib().nss_dmrg_export_superblock(self._d, C.byref(d)))
+        return d
+
+    def records(self):
+        L = lib()
+        n = L.nss_dmrg_nrecords(self._d)
+        arr = (StepRecord * max(1, n))()
+        L.nss_dmrg_records(self._d, arr, n)
+        out = []
+        for r in arr[:n]:
+            out.append({k: (list(getattr(r, k)) if k == "energy" else getattr(r, k)) for k, _ in StepRecord._fields_})
+        return out

@@ -1,0 +1,317 @@
+// C ABI (include/nssdmrg.h).  Every entry point catches C++ exceptions and
+// turns them into status codes; nothing here aborts the caller.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "device.cuh"
+#include "host_dmrg.hpp"
+
+struct nss_ctx {
+    nss::Ctx c;
+    std::unique_ptr<nss::SbHost> sbhost;   // set by nss_sb_setup
+    double *d_v = nullptr, *d_hv = nullptr, *d_psi = nullptr;
+    int64_t tmp_n = 0;
+};
+
+struct nss_dmrg {
+    nss_ctx *ctx = nullptr;
+    nss::Driver drv;
+    nss::SbView view;   // last exported superblock
+    std::unique_ptr<nss::SbHost> last;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(nss_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->c.err = msg;
+    else g_err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(nss_ctx *ctx, F &&f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        return fail(ctx, NSS_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(ctx, NSS_ERR_INVALID, e.what());
+    }
+}
+
+int ensure_tmp(nss_ctx *ctx, int64_t n) {
+    if (ctx->tmp_n >= n && ctx->d_v) return NSS_OK;
+    nss::ctx_free(ctx->c, ctx->d_v);
+    nss::ctx_free(ctx->c, ctx->d_hv);
+    ctx->d_v = ctx->d_hv = nullptr;
+    NSS_CUDA_TRY(ctx->c, nss::ctx_alloc(ctx->c, &ctx->d_v, (size_t)n));
+    NSS_CUDA_TRY(ctx->c, nss::ctx_alloc(ctx->c, &ctx->d_hv, (size_t)n));
+    ctx->tmp_n = n;
+    return NSS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nss_ctx *nss_create(int device, size_t hbm_budget) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_err = "nss_create: no CUDA device";
+        return nullptr;
+    }
+    if (device < 0 || device >= ndev) {
+        g_err = "nss_create: device index out of range";
+        return nullptr;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        g_err = "nss_create: cudaSetDevice failed";
+        return nullptr;
+    }
+    auto *ctx = new (std::nothrow) nss_ctx;
+    if (!ctx) {
+        g_err = "nss_create: host allocation failed";
+        return nullptr;
+    }
+    ctx->c.device = device;
+    ctx->c.budget = hbm_budget;
+    if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_err = "nss_create: stream creation failed";
+        delete ctx;
+        return nullptr;
+    }
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS || cusolverDnSetStream(h, ctx->c.stream) != CUSOLVER_STATUS_SUCCESS) {
+        g_err = "nss_create: cuSOLVER initialisation failed";
+        cudaStreamDestroy(ctx->c.stream);
+        delete ctx;
+        return nullptr;
+    }
+    ctx->c.solver = h;
+    return ctx;
+}
+
+void nss_destroy(nss_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->c.device);
+    cudaStreamSynchronize(ctx->c.stream);
+    nss::sb_release(ctx->c);
+    nss::lanczos_release(ctx->c);
+    nss::rdm_release(ctx->c);
+    nss::ctx_free(ctx->c, ctx->d_v);
+    nss::ctx_free(ctx->c, ctx->d_hv);
+    nss::ctx_free(ctx->c, ctx->d_psi);
+    if (ctx->c.solver) cusolverDnDestroy((cusolverDnHandle_t)ctx->c.solver);
+    cudaStreamDestroy(ctx->c.stream);
+    delete ctx;
+}
+
+const char *nss_last_error(const nss_ctx *ctx) { return ctx ? ctx->c.err.c_str() : g_err.c_str(); }
+
+int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->c.device);
+        ctx->sbhost.reset();
+        return nss::sb_upload(ctx->c, desc);
+    });
+}
+
+int nss_sb_free(nss_ctx *ctx) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    cudaSetDevice(ctx->c.device);
+    cudaStreamSynchronize(ctx->c.stream);
+    nss::sb_release(ctx->c);
+    ctx->sbhost.reset();
+    return NSS_OK;
+}
+
+int64_t nss_sb_dim(const nss_ctx *ctx) { return (ctx && ctx->c.sb.valid) ? ctx->c.sb.n : 0; }
+
+int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
+    if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
+    if (!d_v || !d_hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
+    cudaSetDevice(ctx->c.device);
+    return nss::hv_device(ctx->c, d_v, d_hv);
+}
+
+int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
+    if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
+    if (!v || !hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
+    cudaSetDevice(ctx->c.device);
+    int rc = ensure_tmp(ctx, n);
+    if (rc) return rc;
+    nss::Ctx &c = ctx->c;
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, v, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    rc = nss::hv_device(c, ctx->d_v, ctx->d_hv);
+    if (rc) return rc;
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(hv, ctx->d_hv, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    return NSS_OK;
+}
+
+int nss_eigh(nss_ctx *ctx, int neigen, int nitermax, int ncv, double tol, uint64_t seed, int precision,
+             double *evals, double *evecs, int *numop) {
+    (void)ncv;
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!evals) return fail(ctx, NSS_ERR_INVALID, "nss_eigh: evals is NULL");
+    if (precision != NSS_PREC_FP64 && precision != NSS_PREC_MIXED)
+        return fail(ctx, NSS_ERR_INVALID, "nss_eigh: unknown precision mode");
+    cudaSetDevice(ctx->c.device);
+    return guarded(ctx, [&] {
+        int rc = nss::lanczos_eigh(ctx->c, neigen, nitermax, tol, seed, precision, evals, numop);
+        if (rc) return rc;
+        if (evecs) {
+            nss::Ctx &c = ctx->c;
+            const int64_t n = c.sb.n;
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(evecs, c.lz.evecs, (size_t)c.lz.neigen_done * n * sizeof(double),
+                                            cudaMemcpyDeviceToHost, c.stream));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+        }
+        return NSS_OK;
+    });
+}
+
+int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rdm_side out[2],
+            double *lambda_left, double *lambda_right, int32_t *kept_left, int32_t *kept_right, double *u_left,
+            double *u_right) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!out) return fail(ctx, NSS_ERR_INVALID, "nss_rdm: out is NULL");
+    cudaSetDevice(ctx->c.device);
+    return guarded(ctx, [&] {
+        nss::Ctx &c = ctx->c;
+        if (!c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_rdm: no superblock uploaded");
+        const double *d_psi = nullptr;
+        if (psi) {
+            if (!ctx->d_psi || ctx->tmp_n < c.sb.n) {
+                int rc = ensure_tmp(ctx, c.sb.n);
+                if (rc) return rc;
+            }
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, psi, c.sb.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+            d_psi = ctx->d_v;
+        } else {
+            if (c.lz.neigen_done < 1 || c.lz.n != c.sb.n)
+                return fail(ctx, NSS_ERR_STATE, "nss_rdm: no ground state (call nss_eigh or pass psi)");
+            d_psi = c.lz.evecs;
+        }
+        return nss::rdm_run(c, d_psi, mstates, deg_thr, out, lambda_left, lambda_right, kept_left, kept_right,
+                            u_left, u_right);
+    });
+}
+
+int nss_sb_setup(nss_ctx *ctx, int site_type, const nss_block_desc *left, const nss_block_desc *right,
+                 const double *target, const double *hij) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!left || !right || !target || !hij) return fail(ctx, NSS_ERR_INVALID, "nss_sb_setup: null argument");
+    if (site_type != NSS_SITE_SPIN && site_type != NSS_SITE_FERMION)
+        return fail(ctx, NSS_ERR_INVALID, "nss_sb_setup: unknown site type");
+    cudaSetDevice(ctx->c.device);
+    return guarded(ctx, [&] {
+        const bool f = site_type == NSS_SITE_FERMION;
+        nss::Block l = nss::block_from_desc(*left, f), r = nss::block_from_desc(*right, f);
+        nss::Qn t(target, target + left->qdim);
+        auto sb = std::make_unique<nss::SbHost>(nss::sb_build(l, r, t, hij));
+        nss::SbView v;
+        nss::sb_view(*sb, v);
+        int rc = nss::sb_upload(ctx->c, &v.desc);
+        if (rc) return rc;
+        ctx->sbhost = std::move(sb);
+        return NSS_OK;
+    });
+}
+
+int nss_sb_counts(const nss_ctx *ctx, int32_t *nsb, int32_t *qdim, int64_t *n) {
+    if (!ctx || !ctx->sbhost) return NSS_ERR_STATE;
+    if (nsb) *nsb = ctx->sbhost->nsb();
+    if (qdim) *qdim = ctx->sbhost->qdim;
+    if (n) *n = ctx->sbhost->n();
+    return NSS_OK;
+}
+
+int nss_sb_tables(const nss_ctx *ctx, double *qns, int32_t *dls, int32_t *drs, int64_t *offset, int64_t *sb_states) {
+    if (!ctx || !ctx->sbhost) return NSS_ERR_STATE;
+    const nss::SbHost &s = *ctx->sbhost;
+    for (int k = 0; k < s.nsb(); ++k) {
+        if (qns)
+            for (int t = 0; t < s.qdim; ++t) qns[k * s.qdim + t] = s.qns[k][t];
+        if (dls) dls[k] = s.dls[k];
+        if (drs) drs[k] = s.drs[k];
+        if (offset) offset[k] = s.offset[k];
+    }
+    if (sb_states)
+        for (int64_t i = 0; i < s.n(); ++i) sb_states[i] = s.sb_states[i];
+    return NSS_OK;
+}
+
+nss_dmrg *nss_dmrg_create(nss_ctx *ctx, const nss_dmrg_params *p) {
+    if (!ctx || !p) {
+        g_err = "nss_dmrg_create: null argument";
+        return nullptr;
+    }
+    auto *d = new (std::nothrow) nss_dmrg;
+    if (!d) return nullptr;
+    d->ctx = ctx;
+    int rc = guarded(ctx, [&] { return d->drv.init(&ctx->c, *p); });
+    if (rc) {
+        delete d;
+        return nullptr;
+    }
+    return d;
+}
+
+void nss_dmrg_destroy(nss_dmrg *d) { delete d; }
+
+int nss_dmrg_infinite(nss_dmrg *d) {
+    if (!d) return NSS_ERR_INVALID;
+    cudaSetDevice(d->ctx->c.device);
+    return guarded(d->ctx, [&] { return d->drv.infinite(); });
+}
+
+int nss_dmrg_finite(nss_dmrg *d) {
+    if (!d) return NSS_ERR_INVALID;
+    cudaSetDevice(d->ctx->c.device);
+    return guarded(d->ctx, [&] { return d->drv.finite(); });
+}
+
+int nss_dmrg_prepare_last(nss_dmrg *d) {
+    if (!d) return NSS_ERR_INVALID;
+    cudaSetDevice(d->ctx->c.device);
+    return guarded(d->ctx, [&] {
+        d->drv.stop_before_last_solve = true;
+        int rc = d->drv.infinite();
+        d->drv.stop_before_last_solve = false;
+        if (rc) return rc;
+        if (!d->drv.stopped) return fail(d->ctx, NSS_ERR_STATE, "nss_dmrg_prepare_last: infinite run already done");
+        return NSS_OK;
+    });
+}
+
+int nss_dmrg_nrecords(const nss_dmrg *d) { return d ? (int)d->drv.records.size() : 0; }
+
+int nss_dmrg_records(const nss_dmrg *d, nss_step_record *out, int max) {
+    if (!d || !out) return NSS_ERR_INVALID;
+    int n = std::min<int>(max, (int)d->drv.records.size());
+    for (int i = 0; i < n; ++i) out[i] = d->drv.records[i];
+    return n;
+}
+
+int nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out) {
+    if (!d || !out) return NSS_ERR_INVALID;
+    if (!d->drv.last_sb) return fail(d->ctx, NSS_ERR_STATE, "nss_dmrg_export_superblock: no superblock built yet");
+    d->last = std::make_unique<nss::SbHost>(*d->drv.last_sb);
+    nss::sb_view(*d->last, d->view);
+    *out = d->view.desc;
+    return NSS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// Device context of the GB300 superblock eigensolver.
+//
+// HBM layout of one uploaded superblock (all FP64 unless noted):
+//   psi-space vectors : N doubles; sector k occupies [Offset(k), Offset(k)+Dl*Dr)
+//                       as the row-major W_k[il][ir] (ir fastest), which is the
+//                       reference's column-major Psi_k[Dr x Dl]
+//                       (src/DMRG_SUPERBLOCK_SETUP.f90:770,787).
+//   hl / hr pools     : dense row-major H_L(k) [Dl x Dl] and H_R(k) [Dr x Dr],
+//                       one after the other (sector operators are 75-95 %
+//                       filled at production bond dimensions, so dense tiles).
+//   term tables       : the A(it,k) x B(it,k) terms regrouped by the sector they
+//                       write (RowOffset), CSR pools for A and B; regrouping
+//                       lets one CTA own an output tile, so no atomics.
+//   tiles             : (sector, row0, col0) work items of the matvec kernel.
+//   Krylov basis      : nitermax+1 vectors of N doubles, vector-major.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/nssdmrg.h"
+
+namespace nss {
+
+struct DevTerm {          // one A x B term, grouped by output sector
+    int out_sec, in_sec;
+    int a_nrow, a_ncol, b_nrow, b_ncol;
+    int64_t a_rp, b_rp;   // offsets of the rowptr arrays in the pools
+};
+
+struct DevSb {
+    bool valid = false;
+    int nsb = 0, tnso = 0, m_left = 0, m_right = 0;
+    int64_t n = 0;
+    // host mirrors of the small tables
+    std::vector<int> dls, drs;
+    std::vector<int64_t> off, hl_off, hr_off;
+    std::vector<int> ai, bi, ai_off, bi_off;
+    std::vector<int> term_ptr;            // [nsb+1] into terms (by output sector)
+    std::vector<DevTerm> terms;
+    // F_HV bookkeeping: algorithmic flops of one H*v
+    double flops_dense = 0.0, flops_ab = 0.0;
+    // device arrays
+    int *d_dls = nullptr, *d_drs = nullptr;
+    int64_t *d_off = nullptr, *d_hl_off = nullptr, *d_hr_off = nullptr;
+    double *d_hl = nullptr, *d_hr = nullptr;
+    int *d_term_ptr = nullptr;
+    DevTerm *d_terms = nullptr;
+    int *d_ab_rowptr = nullptr, *d_ab_col = nullptr;
+    double *d_ab_val = nullptr;
+    int4 *d_tiles = nullptr;
+    int ntiles = 0;
+    // float copies for the mixed-precision path (built lazily)
+    float *d_hl32 = nullptr, *d_hr32 = nullptr;
+};
+
+// Device-side Lanczos state, kept resident between nss_eigh and nss_rdm.
+struct DevLanczos {
+    int cap = 0;                 // allocated Krylov vectors
+    int64_t n = 0;
+    double *V = nullptr;         // [cap][n]
+    double *w = nullptr;         // [n]
+    double *evecs = nullptr;     // [neigen][n] Ritz vectors (last solve)
+    int neigen_done = 0;
+    double *scal = nullptr;      // device scalars (see k_lanczos.cu)
+    double *part = nullptr;      // partial sums [cap+2][nblk]
+    unsigned *counter = nullptr; // last-block-done counters
+    double *alpha = nullptr, *beta = nullptr;   // [cap]
+    double *theta = nullptr, *resid = nullptr, *svec = nullptr; // tridiagonal results
+    int *flags = nullptr;        // device flags
+    int *h_flags = nullptr;      // pinned host copy
+};
+
+struct DevRdm {
+    int64_t cap_rho = 0, cap_evals = 0, cap_u = 0;
+    double *rho = nullptr;       // blocks, left then right
+    double *evals = nullptr;     // per-block eigenvalues, concatenated
+    double *sorted = nullptr;    // descending
+    int *order = nullptr;        // block-concatenated position per rank
+    double *u = nullptr;         // dense rotation matrix staging
+    double *work = nullptr;      // cuSOLVER workspace
+    int64_t lwork = 0;
+    int *info = nullptr;
+    double *scal = nullptr;
+    int *iscal = nullptr;
+};
+
+struct Ctx {
+    int device = 0;
+    size_t budget = 0, used = 0;
+    std::unordered_map<void *, size_t> sizes;   // live allocations
+    std::string err;
+    cudaStream_t stream = nullptr;
+    void *solver = nullptr;      // cusolverDnHandle_t
+    DevSb sb;
+    DevLanczos lz;
+    DevRdm rdm;
+    // last nss_eigh statistics
+    int last_numop = 0;
+    double last_ms_eigh = 0.0;
+};
+
+// Allocation through the context budget.
+template <class T>
+cudaError_t ctx_alloc(Ctx &c, T **p, size_t count) {
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    if (c.budget && c.used + bytes > c.budget) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e == cudaSuccess) {
+        c.used += bytes;
+        c.sizes[(void *)*p] = bytes;
+    }
+    return e;
+}
+void ctx_free(Ctx &c, void *p);
+
+// k_matvec.cu
+int sb_upload(Ctx &c, const nss_sb_desc *d);
+void sb_release(Ctx &c);
+int hv_device(Ctx &c, const double *d_v, double *d_hv);
+
+// k_lanczos.cu
+int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,
+                 int precision, double *evals_host, int *numop);
+void lanczos_release(Ctx &c);
+
+// k_rdm.cu
+int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2],
+            double *lam_l, double *lam_r, int32_t *kept_l, int32_t *kept_r,
+            double *u_l, double *u_r);
+void rdm_release(Ctx &c);
+
+}  // namespace nss
+
+#define NSS_CUDA_TRY(c, call)                                                   \
+    do {                                                                        \
+        cudaError_t _e = (call);                                                \
+        if (_e != cudaSuccess) {                                                \
+            (c).err = std::string(#call) + ": " + cudaGetErrorString(_e);       \
+            return _e == cudaErrorMemoryAllocation ? NSS_ERR_NOMEM : NSS_ERR_CUDA; \
+        }                                                                       \
+    } while (0)

@@ -1,0 +1,393 @@
+// Host-side DMRG driver (see host_dmrg.hpp).
+#include "host_dmrg.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <stdexcept>
+
+#include "device.cuh"
+
+namespace nss {
+
+namespace {
+
+Csr dense_csr(int n, std::initializer_list<double> v) {
+    std::vector<double> a(v);
+    return csr_from_dense(n, n, a.data());
+}
+
+}  // namespace
+
+// spin_site (src/BLOCKS/SITES.f90:281-350), zero field.
+Block spin_site(int sun) {
+    Block b;
+    b.length = 1;
+    b.qdim = 1;
+    b.fermion = false;
+    if (sun == 2) {
+        b.dim = 2;
+        b.basis = {0.5, -0.5};
+        b.ops.push_back({"H", Csr{}, "bosonic"});
+        b.ops[0].m.init(2, 2);
+        b.ops.push_back({"S_z_n", dense_csr(2, {0.5, 0, 0, -0.5}), "bosonic"});
+        b.ops.push_back({"S_p_n", dense_csr(2, {0, 1, 0, 0}), "bosonic"});
+    } else if (sun == 3) {
+        const double r2 = std::sqrt(2.0);
+        b.dim = 3;
+        b.basis = {1.0, 0.0, -1.0};
+        b.ops.push_back({"H", Csr{}, "bosonic"});
+        b.ops[0].m.init(3, 3);
+        b.ops.push_back({"S_z_n", dense_csr(3, {1, 0, 0, 0, 0, 0, 0, 0, -1}), "bosonic"});
+        b.ops.push_back({"S_p_n", dense_csr(3, {0, r2, 0, 0, 0, r2, 0, 0, 0}), "bosonic"});
+    } else {
+        throw std::runtime_error("spin_site ERROR: SU(N) value not supported");
+    }
+    return b;
+}
+
+// electron_site, Norb=1 (src/BLOCKS/SITES.f90:358-450; src/FOCK/HLOCAL.f90:
+// 312-433 local H, :587-615 C with the Jordan-Wigner sign of c() :884-896,
+// :735-781 basis QNs and parity).  Fock index m = iup + 2*idw.
+Block electron_site(double uloc, bool hfmode) {
+    Block b;
+    b.length = 1;
+    b.dim = 4;
+    b.qdim = 2;
+    b.fermion = true;
+    const int nup[4] = {0, 1, 0, 1}, ndw[4] = {0, 0, 1, 1};
+    std::vector<double> h(16, 0.0), cu(16, 0.0), cd(16, 0.0), p(16, 0.0);
+    for (int m = 0; m < 4; ++m) {
+        double e = uloc * nup[m] * ndw[m];
+        if (hfmode) e -= 0.5 * uloc * (nup[m] + ndw[m]);
+        h[m * 4 + m] = e;
+        p[m * 4 + m] = ((nup[m] + ndw[m]) % 2) ? -1.0 : 1.0;
+        b.basis.push_back(nup[m]);
+        b.basis.push_back(ndw[m]);
+    }
+    cu[0 * 4 + 1] = 1.0;    // c_up |up>    = |0>
+    cu[2 * 4 + 3] = 1.0;    // c_up |up,dw> = |dw>
+    cd[0 * 4 + 2] = 1.0;    // c_dw |dw>    = |0>
+    cd[1 * 4 + 3] = -1.0;   // c_dw |up,dw> = -|up>  (one occupied level below)
+    b.ops.push_back({"H", csr_from_dense(4, 4, h.data()), "bosonic"});
+    b.ops.push_back({"C_l1_s1_n", csr_from_dense(4, 4, cu.data()), "fermionic"});
+    b.ops.push_back({"C_l1_s2_n", csr_from_dense(4, 4, cd.data()), "fermionic"});
+    b.ops.push_back({"P_n", csr_from_dense(4, 4, p.data()), "psign"});
+    return b;
+}
+
+namespace {
+
+// connect_spin_blocks (src/DMRG_CONNECT.f90:394-454), link 'n'
+Csr connect_spin(const Block &l, const Block &r, const double *hij) {
+    const Csr &szl = l.op("S_z_n"), &spl = l.op("S_p_n");
+    const Csr &szr = r.op("S_z_n"), &spr = r.op("S_p_n");
+    Csr h2 = csr_scale(csr_kron(szl, szr), hij[0]);
+    h2 = csr_add(h2, csr_scale(csr_kron(spl, csr_transpose(spr)), hij[3]));
+    h2 = csr_add(h2, csr_scale(csr_kron(csr_transpose(spl), spr), hij[3]));
+    return h2;
+}
+
+// connect_fermion_blocks (src/DMRG_CONNECT.f90:296-389), real, Norb=1
+Csr connect_fermion(const Block &l, const Block &r, const double *hij) {
+    const Csr &pl = l.op("P_n");
+    const char *key[2] = {"C_l1_s1_n", "C_l1_s2_n"};
+    Csr h2;
+    h2.init(l.dim * r.dim, l.dim * r.dim);
+    for (int io = 0; io < 2; ++io)
+        for (int jo = 0; jo < 2; ++jo) {
+            const double t = hij[io * 2 + jo];
+            if (t == 0.0) continue;
+            const Csr &cl = l.op(key[io]), &cr = r.op(key[jo]);
+            h2 = csr_add(h2, csr_scale(csr_kron(csr_matmul(csr_transpose(cl), pl), cr), t));
+            h2 = csr_add(h2, csr_scale(csr_kron(csr_matmul(pl, cl), csr_transpose(cr)), t));
+        }
+    return h2;
+}
+
+Csr connect(const Block &l, const Block &r, const double *hij) {
+    return l.fermion ? connect_fermion(l, r, hij) : connect_spin(l, r, hij);
+}
+
+std::vector<double> outsum(const std::vector<double> &a, int na, const std::vector<double> &b, int nb, int q) {
+    std::vector<double> c((size_t)na * nb * q);
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j)
+            for (int t = 0; t < q; ++t) c[((size_t)i * nb + j) * q + t] = a[(size_t)i * q + t] + b[(size_t)j * q + t];
+    return c;
+}
+
+}  // namespace
+
+Block enlarge_block(const Block &blk, const Block &dot, char label, const double *hij) {
+    const int m = blk.dim, d = dot.dim;
+    Block out = blk;
+    Csr hb, hd, h2;
+    if (label == 'l') {
+        hb = csr_kron(blk.op("H"), csr_identity(d));
+        hd = csr_kron(csr_identity(m), dot.op("H"));
+        h2 = connect(blk, dot, hij);
+    } else {
+        hb = csr_kron(csr_identity(d), blk.op("H"));
+        hd = csr_kron(dot.op("H"), csr_identity(m));
+        h2 = connect(dot, blk, hij);
+    }
+    out.op("H") = csr_add(csr_add(hb, hd), h2);
+    // other operators in list order; P is read from the list being updated
+    // exactly as the reference loop does (src/DMRG_CONNECT.f90:117-146)
+    for (size_t i = 0; i < blk.ops.size(); ++i) {
+        const Op &o = blk.ops[i];
+        if (o.key == "H") continue;
+        const char t = o.type.empty() ? 'b' : o.type[0];
+        Csr eo;
+        if (label == 'l') {
+            eo = (t == 'b') ? csr_identity(m) : out.op("P_n");
+            out.ops[i].m = csr_kron(eo, dot.op(o.key));
+        } else {
+            eo = (t == 'p') ? out.op("P_n") : csr_identity(m);
+            out.ops[i].m = csr_kron(dot.op(o.key), eo);
+        }
+    }
+    out.length = blk.length + 1;
+    out.dim = m * d;
+    out.basis = (label == 'l') ? outsum(blk.basis, m, dot.basis, d, blk.qdim)
+                               : outsum(dot.basis, d, blk.basis, m, blk.qdim);
+    return out;
+}
+
+Block block_from_desc(const nss_block_desc &d, bool fermion) {
+    Block b;
+    b.dim = d.dim;
+    b.qdim = d.qdim;
+    b.fermion = fermion;
+    b.basis.assign(d.basis, d.basis + (size_t)d.dim * d.qdim);
+    auto mk = [&](const nss_csr &c) {
+        Csr m;
+        m.init(c.nrow, c.ncol);
+        if (c.nrow != d.dim || c.ncol != d.dim) throw std::runtime_error("block operator has wrong shape");
+        int nnz = c.rowptr[c.nrow];
+        m.rowptr.assign(c.rowptr, c.rowptr + c.nrow + 1);
+        m.col.assign(c.colidx, c.colidx + nnz);
+        m.val.assign(c.vals, c.vals + nnz);
+        return m;
+    };
+    b.ops.push_back({"H", mk(d.h), "bosonic"});
+    if (!fermion) {
+        b.ops.push_back({"S_z_n", mk(d.op[0]), "bosonic"});
+        b.ops.push_back({"S_p_n", mk(d.op[1]), "bosonic"});
+    } else {
+        b.ops.push_back({"C_l1_s1_n", mk(d.op[0]), "fermionic"});
+        b.ops.push_back({"C_l1_s2_n", mk(d.op[1]), "fermionic"});
+        b.ops.push_back({"P_n", mk(d.op[2]), "psign"});
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+int Driver::init(Ctx *c, const nss_dmrg_params &params) {
+    ctx = c;
+    p = params;
+    if (p.msweep && p.nsweep > 0) msweep.assign(p.msweep, p.msweep + p.nsweep);
+    p.msweep = nullptr;
+    if (p.lanc_neigen <= 0) p.lanc_neigen = 2;
+    if (p.lanc_niter <= 0) p.lanc_niter = 512;
+    if (p.lanc_tolerance <= 0) p.lanc_tolerance = 1e-12;
+    if (p.deg_evals_threshold <= 0) p.deg_evals_threshold = 0.1;
+    switch (p.model) {
+    case NSS_MODEL_HEISENBERG_HALF:
+        dot = spin_site(2);
+        break;
+    case NSS_MODEL_HEISENBERG_ONE:
+        dot = spin_site(3);
+        break;
+    case NSS_MODEL_HUBBARD:
+        dot = electron_site(p.u, p.hfmode != 0);
+        break;
+    default:
+        c->err = "nss_dmrg_create: unknown model";
+        return NSS_ERR_INVALID;
+    }
+    if (p.model == NSS_MODEL_HUBBARD) {
+        hij[0] = -p.t; hij[1] = 0; hij[2] = 0; hij[3] = -p.t;    // Hlr = diag(ts,ts), ts=-t
+    } else {
+        hij[0] = p.jz; hij[1] = 0; hij[2] = 0; hij[3] = p.jxy / 2.0;   // Hlr = diag(Jp, Jx/2)
+    }
+    left = dot;
+    right = dot;
+    return NSS_OK;
+}
+
+int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, bool renormalize,
+                   Block &left, Block &right, nss_step_record &rec);
+
+// step_dmrg (src/DMRG_MAIN.f90:262-433), OBC link 'n'
+int Driver::step(int type, int label, int sweep) {
+    const int mstates = (type == 0) ? p.mdmrg : msweep.at(sweep - 1);
+    left = enlarge_block(left, dot, 'l', hij);
+    right = enlarge_block(right, dot, 'r', hij);
+    const int current_l = left.length + right.length;
+    // sb_set_current_qn, QNtype local: int(target_qn * L * Norb), truncated
+    Qn target(left.qdim);
+    for (int i = 0; i < left.qdim; ++i) target[i] = std::trunc(p.dmrg_qn[i] * current_l * 1.0);
+    SbHost sb = sb_build(left, right, target, hij);
+    bool renorm;
+    if (type == 0) renorm = left.length != p.ldmrg;
+    else renorm = !(left.length == p.ldmrg + 1 && label == 1);
+    nss_step_record rec{};
+    rec.type = type;
+    rec.left_length = left.length;
+    rec.right_length = right.length;
+    rec.current_l = current_l;
+    rec.n = sb.n();
+    rec.nsb = sb.nsb();
+    if (stop_before_last_solve && type == 0 && left.length == p.ldmrg) {
+        last_sb = std::make_shared<SbHost>(std::move(sb));
+        SbView v;
+        sb_view(*last_sb, v);
+        int rc = sb_upload(*ctx, &v.desc);
+        stopped = true;
+        return rc;
+    }
+    int rc = nss_solve_step(*ctx, sb, p, mstates, renorm, left, right, rec);
+    if (rc) return rc;
+    records.push_back(rec);
+    return NSS_OK;
+}
+
+int Driver::infinite() {
+    while (left.length < p.ldmrg) {
+        int rc = step(0, 0, 0);
+        if (rc || stopped) return rc;
+    }
+    return NSS_OK;
+}
+
+// finite_DMRG (src/DMRG_MAIN.f90:168-241), OBC
+int Driver::finite() {
+    const int fN = 2 * p.ldmrg;
+    std::vector<Block> lb(fN + 2), rb(fN + 2);
+    lb[1] = left;
+    rb[1] = right;
+    while (left.length < p.ldmrg) {
+        int rc = step(0, 0, 0);
+        if (rc) return rc;
+        lb[left.length] = left;
+        rb[right.length] = right;
+    }
+    for (int im = 1; im <= (int)msweep.size(); ++im) {
+        while (left.length < fN) {
+            right = rb[fN - left.length];
+            int rc = step(1, 1, im);
+            if (rc) return rc;
+            lb[left.length] = left;
+        }
+        while (right.length < fN) {
+            left = lb[fN - right.length];
+            int rc = step(1, 2, im);
+            if (rc) return rc;
+            rb[right.length] = right;
+        }
+        while (left.length <= p.ldmrg) {
+            right = rb[fN - left.length];
+            int rc = step(1, 1, im);
+            if (rc) return rc;
+            lb[left.length] = left;
+        }
+    }
+    return NSS_OK;
+}
+
+namespace {
+
+// U (column-major m_block x m_s, dense) -> CSR, dropping exact zeros
+Csr u_to_csr(const std::vector<double> &u, int nrow, int ncol) {
+    Csr c;
+    c.init(nrow, ncol);
+    std::vector<std::vector<std::pair<int, double>>> rows(nrow);
+    for (int j = 0; j < ncol; ++j)
+        for (int i = 0; i < nrow; ++i) {
+            double v = u[(size_t)j * nrow + i];
+            if (v != 0.0) rows[i].push_back({j, v});
+        }
+    for (int i = 0; i < nrow; ++i) {
+        for (auto &e : rows[i]) {
+            c.col.push_back(e.first);
+            c.val.push_back(e.second);
+        }
+        c.rowptr[i + 1] = (int)c.col.size();
+    }
+    return c;
+}
+
+// operators_renormalization (src/DMRG_RDM.f90:355-404): O <- U^T O U, and the
+// new basis from the kept blocks' QNs (:244-251).
+void renormalize(Block &blk, const Csr &u, const std::vector<Qn> &kept_qn) {
+    const Csr ut = csr_transpose(u);
+    for (auto &o : blk.ops) o.m = csr_matmul(csr_matmul(ut, o.m), u);
+    blk.dim = u.ncol;
+    blk.basis.clear();
+    for (const Qn &q : kept_qn) blk.basis.insert(blk.basis.end(), q.begin(), q.end());
+}
+
+}  // namespace
+
+int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, bool renorm, Block &left,
+                   Block &right, nss_step_record &rec) {
+    SbView v;
+    sb_view(sb, v);
+    int rc = sb_upload(c, &v.desc);
+    if (rc) return rc;
+    const int64_t n = sb.n();
+    const int neigen = (int)std::min<int64_t>(n, p.lanc_neigen);
+    const int nitermax = (int)std::min<int64_t>(n, p.lanc_niter);
+    double ev[4] = {0, 0, 0, 0};
+    int numop = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c.stream);
+    rc = lanczos_eigh(c, neigen, nitermax, p.lanc_tolerance, p.seed, p.precision, ev, &numop);
+    if (rc) return rc;
+    nss_rdm_side side[2];
+    std::vector<double> u_l, u_r;
+    std::vector<int32_t> k_l, k_r;
+    // m_s is known only after the truncation kernel: size for the maximum
+    u_l.resize((size_t)sb.m_left * sb.m_left);
+    u_r.resize((size_t)sb.m_right * sb.m_right);
+    k_l.resize(sb.m_left);
+    k_r.resize(sb.m_right);
+    rc = rdm_run(c, c.lz.evecs, mstates, p.deg_evals_threshold, side, nullptr, nullptr,
+                 renorm ? k_l.data() : nullptr, renorm ? k_r.data() : nullptr,
+                 renorm ? u_l.data() : nullptr, renorm ? u_r.data() : nullptr);
+    if (rc) return rc;
+    cudaEventRecord(e1, c.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    rec.ms_solve = ms;
+    rec.numop = numop;
+    for (int e = 0; e < 2; ++e) rec.energy[e] = (e < neigen) ? ev[e] / rec.current_l : 0.0;
+    rec.entropy_left = side[0].entropy;
+    rec.entropy_right = side[1].entropy;
+    rec.m_left = left.dim;
+    rec.m_right = right.dim;
+    if (renorm) {
+        std::vector<Qn> ql, qr;
+        for (int j = 0; j < side[0].m_s; ++j) ql.push_back(sb.qns[k_l[j]]);
+        for (int j = 0; j < side[1].m_s; ++j) {
+            Qn q = sb.target;
+            for (size_t t = 0; t < q.size(); ++t) q[t] -= sb.qns[k_r[j]][t];
+            qr.push_back(q);
+        }
+        renormalize(left, u_to_csr(u_l, sb.m_left, side[0].m_s), ql);
+        renormalize(right, u_to_csr(u_r, sb.m_right, side[1].m_s), qr);
+        rec.trunc_left = side[0].trunc_err;
+        rec.trunc_right = side[1].trunc_err;
+        rec.m_left = left.dim;
+        rec.m_right = right.dim;
+    }
+    return NSS_OK;
+}
+
+}  // namespace nss

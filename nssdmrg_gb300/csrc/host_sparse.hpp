@@ -1,0 +1,78 @@
+// Host-side row-list sparse matrices, blocks and sector lists.
+//
+// These mirror the reference's containers: sparse_matrix / sparse_row
+// (src/MATRIX/MATRIX_SPARSE.f90:28-72), sectors_list
+// (src/LIST/LIST_SECTORS.f90:16-43) and block (src/BLOCKS/BLOCKS.f90:14-43).
+// They hold the block-level state of a DMRG run between superblock solves;
+// the superblock solve itself runs on the GPU.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace nss {
+
+// CSR matrix, 0-based.  Explicit zeros that arise from arithmetic are kept,
+// as in the reference's sparse algebra.
+struct Csr {
+    int nrow = 0, ncol = 0;
+    std::vector<int> rowptr{0};
+    std::vector<int> col;
+    std::vector<double> val;
+
+    int64_t nnz() const { return (int64_t)col.size(); }
+    void init(int r, int c) {
+        nrow = r; ncol = c;
+        rowptr.assign(r + 1, 0);
+        col.clear(); val.clear();
+    }
+};
+
+Csr csr_identity(int n);
+Csr csr_from_dense(int nrow, int ncol, const double *a /* row-major */);
+Csr csr_scale(const Csr &a, double s);
+Csr csr_add(const Csr &a, const Csr &b);           // a + b
+Csr csr_kron(const Csr &a, const Csr &b);           // sp_kron_matrix
+Csr csr_transpose(const Csr &a);                    // sp_dgr_matrix (real)
+Csr csr_matmul(const Csr &a, const Csr &b);         // sp_matmul_matrix
+// sp_filter_matrix_2: rows `rows`, columns `cols` (0-based state lists).
+Csr csr_filter(const Csr &a, const std::vector<int> &rows, const std::vector<int> &cols);
+
+// A QN tuple; compared with exact equality like the reference's real(8) tuples.
+using Qn = std::vector<double>;
+
+// sectors_list: QNs in first-occurrence order of the basis, ascending maps.
+struct Sectors {
+    std::vector<Qn> qns;
+    std::vector<std::vector<int>> maps;
+    std::map<Qn, int> index;
+    int find(const Qn &q) const {
+        auto it = index.find(q);
+        return it == index.end() ? -1 : it->second;
+    }
+};
+Sectors make_sectors(const std::vector<double> &basis, int dim, int qdim);
+
+struct Op {
+    std::string key;
+    Csr m;
+    std::string type;    // "bosonic" | "fermionic" | "psign"
+};
+
+struct Block {
+    int length = 1;
+    int dim = 1;
+    int qdim = 1;
+    bool fermion = false;
+    std::vector<double> basis;   // dim*qdim
+    std::vector<Op> ops;         // ordered as the reference's operators_list
+
+    Csr &op(const std::string &key);
+    const Csr &op(const std::string &key) const;
+    int find_op(const std::string &key) const;
+    Sectors sectors() const { return make_sectors(basis, dim, qdim); }
+};
+
+}  // namespace nss

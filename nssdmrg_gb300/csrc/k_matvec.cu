@@ -1,0 +1,290 @@
+// Superblock upload and the direct H_sb * psi product (plain FP64 path).
+//
+// Restates spMatVec_direct_main (src/DMRG_SUPERBLOCK_SETUP.f90:740-865) as one
+// kernel over output tiles.  For output sector k, with W_k the row-major
+// [Dl x Dr] view of the sector (i = ir + il*Dr + Offset, :770),
+//     Out_k = H_L(k) W_k + W_k H_R(k)^T + sum_t A_t W_q(t) B_t^T,
+// where the last sum runs over the terms whose RowOffset is sector k
+// (:808-857, regrouped by output sector so each tile has one writer).
+#include "device.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+namespace nss {
+
+void ctx_free(Ctx &c, void *p) {
+    if (!p) return;
+    auto it = c.sizes.find(p);
+    if (it != c.sizes.end()) {
+        c.used -= it->second;
+        c.sizes.erase(it);
+    }
+    cudaFree(p);
+}
+
+void sb_release(Ctx &c) {
+    DevSb &s = c.sb;
+    void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
+                    s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
+                    s.d_tiles, s.d_hl32, s.d_hr32};
+    for (void *p : ptrs) ctx_free(c, p);
+    s = DevSb{};
+}
+
+namespace {
+
+constexpr int TILE = 16;
+
+template <class T>
+int upload_vec(Ctx &c, T **dst, const std::vector<T> &src) {
+    NSS_CUDA_TRY(c, ctx_alloc(c, dst, src.size()));
+    if (!src.empty())
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T),
+                                        cudaMemcpyHostToDevice, c.stream));
+    return NSS_OK;
+}
+
+bool csr_ok(const nss_csr &m, int nrow, int ncol) {
+    if (m.nrow != nrow || m.ncol != ncol) return false;
+    if (nrow == 0) return true;
+    if (!m.rowptr || m.rowptr[0] != 0) return false;
+    int nnz = m.rowptr[nrow];
+    if (nnz < 0 || (nnz > 0 && (!m.colidx || !m.vals))) return false;
+    for (int i = 0; i < nrow; ++i)
+        if (m.rowptr[i + 1] < m.rowptr[i]) return false;
+    for (int j = 0; j < nnz; ++j)
+        if (m.colidx[j] < 0 || m.colidx[j] >= ncol) return false;
+    return true;
+}
+
+}  // namespace
+
+// Validate and copy the operator pool.  Errors mirror the reference's stop
+// conditions (wrong sizes, vecDim != m_sb) as NSS_ERR_INVALID.
+int sb_upload(Ctx &c, const nss_sb_desc *d) {
+    if (!d || d->nsb <= 0 || d->tnso < 0 || !d->dls || !d->drs || !d->offset || !d->hleft ||
+        !d->hright) {
+        c.err = "nss_sb_upload: incomplete descriptor";
+        return NSS_ERR_INVALID;
+    }
+    sb_release(c);
+    DevSb &s = c.sb;
+    s.nsb = d->nsb;
+    s.tnso = d->tnso;
+    s.m_left = d->m_left;
+    s.m_right = d->m_right;
+    s.dls.assign(d->dls, d->dls + s.nsb);
+    s.drs.assign(d->drs, d->drs + s.nsb);
+    s.off.assign(d->offset, d->offset + s.nsb);
+    int64_t pos = 0;
+    std::map<int64_t, int> sec_at;
+    for (int k = 0; k < s.nsb; ++k) {
+        if (s.dls[k] <= 0 || s.drs[k] <= 0 || s.off[k] != pos) {
+            c.err = "nss_sb_upload: sector dims/offsets inconsistent at sector " + std::to_string(k);
+            return NSS_ERR_INVALID;
+        }
+        sec_at[pos] = k;
+        pos += (int64_t)s.dls[k] * s.drs[k];
+    }
+    s.n = pos;
+    // sector block maps (for the RDM)
+    if (d->ai && d->bi) {
+        int la = 0, lb = 0;
+        for (int k = 0; k < s.nsb; ++k) {
+            s.ai_off.push_back(la);
+            s.bi_off.push_back(lb);
+            la += s.dls[k];
+            lb += s.drs[k];
+        }
+        s.ai_off.push_back(la);
+        s.bi_off.push_back(lb);
+        s.ai.assign(d->ai, d->ai + la);
+        s.bi.assign(d->bi, d->bi + lb);
+        for (int x : s.ai)
+            if (x < 0 || x >= d->m_left) { c.err = "nss_sb_upload: ai out of range"; return NSS_ERR_INVALID; }
+        for (int x : s.bi)
+            if (x < 0 || x >= d->m_right) { c.err = "nss_sb_upload: bi out of range"; return NSS_ERR_INVALID; }
+    }
+
+    // dense sector operators
+    std::vector<double> hl, hr;
+    for (int k = 0; k < s.nsb; ++k) {
+        const int dl = s.dls[k], dr = s.drs[k];
+        if (!csr_ok(d->hleft[k], dl, dl) || !csr_ok(d->hright[k], dr, dr)) {
+            c.err = "nss_sb_upload: Hleft/Hright shape or index error at sector " + std::to_string(k);
+            return NSS_ERR_INVALID;
+        }
+        s.hl_off.push_back((int64_t)hl.size());
+        s.hr_off.push_back((int64_t)hr.size());
+        size_t bl = hl.size(), br = hr.size();
+        hl.resize(bl + (size_t)dl * dl, 0.0);
+        hr.resize(br + (size_t)dr * dr, 0.0);
+        const nss_csr &L = d->hleft[k], &R = d->hright[k];
+        for (int i = 0; i < dl; ++i)
+            for (int jj = L.rowptr[i]; jj < L.rowptr[i + 1]; ++jj) hl[bl + (size_t)i * dl + L.colidx[jj]] += L.vals[jj];
+        for (int i = 0; i < dr; ++i)
+            for (int jj = R.rowptr[i]; jj < R.rowptr[i + 1]; ++jj) hr[br + (size_t)i * dr + R.colidx[jj]] += R.vals[jj];
+        s.flops_dense += 2.0 * dl * dr * ((double)dl + dr);
+    }
+    s.hl_off.push_back((int64_t)hl.size());
+    s.hr_off.push_back((int64_t)hr.size());
+
+    // A x B terms, regrouped by output sector
+    std::vector<std::vector<DevTerm>> by_out(s.nsb);
+    std::vector<int> rowptr;
+    std::vector<int> col;
+    std::vector<double> val;
+    auto push_csr = [&](const nss_csr &m) {
+        int64_t at = (int64_t)rowptr.size();
+        int base = (int)col.size();
+        for (int i = 0; i <= m.nrow; ++i) rowptr.push_back(base + m.rowptr[i]);
+        int nnz = m.rowptr[m.nrow];
+        col.insert(col.end(), m.colidx, m.colidx + nnz);
+        val.insert(val.end(), m.vals, m.vals + nnz);
+        return at;
+    };
+    const int nt = s.tnso * s.nsb;
+    for (int idx = 0; idx < nt; ++idx) {
+        const nss_csr &A = d->a[idx], &B = d->b[idx];
+        if (A.nrow == 0 || B.nrow == 0) continue;   // status=.false. -> skipped (:810)
+        auto ro = sec_at.find(d->row_offset[idx]);
+        auto co = sec_at.find(d->col_offset[idx]);
+        if (ro == sec_at.end() || co == sec_at.end()) {
+            c.err = "nss_sb_upload: Row/ColOffset not at a sector start (term " + std::to_string(idx) + ")";
+            return NSS_ERR_INVALID;
+        }
+        int o = ro->second, q = co->second;
+        if (!csr_ok(A, s.dls[o], s.dls[q]) || !csr_ok(B, s.drs[o], s.drs[q])) {
+            c.err = "nss_sb_upload: A/B shape or index error (term " + std::to_string(idx) + ")";
+            return NSS_ERR_INVALID;
+        }
+        DevTerm t;
+        t.out_sec = o;
+        t.in_sec = q;
+        t.a_nrow = A.nrow; t.a_ncol = A.ncol;
+        t.b_nrow = B.nrow; t.b_ncol = B.ncol;
+        t.a_rp = push_csr(A);
+        t.b_rp = push_csr(B);
+        by_out[o].push_back(t);
+        // the reference's loop count, src/DMRG_SUPERBLOCK_SETUP.f90:819-853
+        s.flops_ab += 2.0 * ((double)B.rowptr[B.nrow] * A.ncol + (double)A.rowptr[A.nrow] * B.nrow);
+    }
+    s.term_ptr.push_back(0);
+    for (int k = 0; k < s.nsb; ++k) {
+        for (auto &t : by_out[k]) s.terms.push_back(t);
+        s.term_ptr.push_back((int)s.terms.size());
+    }
+    // tiles
+    std::vector<int4> tiles;
+    for (int k = 0; k < s.nsb; ++k)
+        for (int r = 0; r < s.dls[k]; r += TILE)
+            for (int cc = 0; cc < s.drs[k]; cc += TILE) tiles.push_back(make_int4(k, r, cc, 0));
+    s.ntiles = (int)tiles.size();
+
+    int rc;
+    if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
+        (rc = upload_vec(c, &s.d_off, s.off)) || (rc = upload_vec(c, &s.d_hl_off, s.hl_off)) ||
+        (rc = upload_vec(c, &s.d_hr_off, s.hr_off)) || (rc = upload_vec(c, &s.d_hl, hl)) ||
+        (rc = upload_vec(c, &s.d_hr, hr)) || (rc = upload_vec(c, &s.d_term_ptr, s.term_ptr)) ||
+        (rc = upload_vec(c, &s.d_terms, s.terms)) || (rc = upload_vec(c, &s.d_ab_rowptr, rowptr)) ||
+        (rc = upload_vec(c, &s.d_ab_col, col)) || (rc = upload_vec(c, &s.d_ab_val, val)) ||
+        (rc = upload_vec(c, &s.d_tiles, tiles)))
+        return rc;
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    s.valid = true;
+    return NSS_OK;
+}
+
+// One CTA per 16x16 output tile; thread (ty,tx) owns W_k[row0+ty][col0+tx].
+// GB300 issues FP64 at about 1/64 of its FP32 rate, so this kernel is bound
+// by the FP64 pipe; the operand tiles are staged in shared memory only to
+// keep the loads coalesced.
+__global__ void __launch_bounds__(256) k_hv_fp64(
+    const double *__restrict__ v, double *__restrict__ hv, const int4 *__restrict__ tiles,
+    const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
+    const double *__restrict__ hlp, const int64_t *__restrict__ hl_off,
+    const double *__restrict__ hrp, const int64_t *__restrict__ hr_off,
+    const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
+    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const double *__restrict__ ab_val) {
+    __shared__ double sa[TILE][33];
+    __shared__ double sb[32][TILE + 1];
+    const int4 t = tiles[blockIdx.x];
+    const int k = t.x, row0 = t.y, col0 = t.z;
+    const int dl = dls[k], dr = drs[k];
+    const int64_t o = off[k];
+    const double *W = v + o;
+    const double *HL = hlp + hl_off[k];
+    const double *HR = hrp + hr_off[k];
+    const int tid = threadIdx.x, ty = tid / TILE, tx = tid % TILE;
+    const int il = row0 + ty, ir = col0 + tx;
+    double acc = 0.0;
+
+    // H_L W : sum_j HL[il][j] W[j][ir]   (the H^L x 1^R loop, :784-796)
+    for (int j0 = 0; j0 < dl; j0 += 32) {
+        for (int e = tid; e < TILE * 32; e += 256) {
+            int r = e / 32, cc = e % 32;
+            int gi = row0 + r, gj = j0 + cc;
+            sa[r][cc] = (gi < dl && gj < dl) ? HL[(int64_t)gi * dl + gj] : 0.0;
+        }
+        for (int e = tid; e < 32 * TILE; e += 256) {
+            int r = e / TILE, cc = e % TILE;
+            int gj = j0 + r, gc = col0 + cc;
+            sb[r][cc] = (gj < dl && gc < dr) ? W[(int64_t)gj * dr + gc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) acc = fma(sa[ty][j], sb[j][tx], acc);
+        __syncthreads();
+    }
+    // W H_R^T : sum_j W[il][j] HR[ir][j]   (the 1^L x H^R loop, :767-779)
+    for (int j0 = 0; j0 < dr; j0 += 32) {
+        for (int e = tid; e < TILE * 32; e += 256) {
+            int r = e / 32, cc = e % 32;
+            int gi = row0 + r, gj = j0 + cc;
+            sa[r][cc] = (gi < dl && gj < dr) ? W[(int64_t)gi * dr + gj] : 0.0;
+        }
+        for (int e = tid; e < 32 * TILE; e += 256) {
+            int r = e / TILE, cc = e % TILE;   // sb[j][x] = HR[col0+x][j0+j]
+            int gr = col0 + cc, gj = j0 + r;
+            sb[r][cc] = (gr < dr && gj < dr) ? HR[(int64_t)gr * dr + gj] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) acc = fma(sa[ty][j], sb[j][tx], acc);
+        __syncthreads();
+    }
+    if (il >= dl || ir >= dr) return;
+    // sum_t A W_q B^T : Out[ai][bi] += A[ai][aj] B[bi][bj] W_q[aj][bj] (:808-857)
+    for (int ti = term_ptr[k]; ti < term_ptr[k + 1]; ++ti) {
+        const DevTerm tm = terms[ti];
+        const double *Wq = v + off[tm.in_sec];
+        const int drq = drs[tm.in_sec];
+        const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
+        for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
+            const int aj = ab_col[ja];
+            const double av = ab_val[ja];
+            double cb = 0.0;
+            for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
+                cb = fma(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
+            acc = fma(av, cb, acc);
+        }
+    }
+    hv[o + (int64_t)il * dr + ir] = acc;
+}
+
+int hv_device(Ctx &c, const double *d_v, double *d_hv) {
+    DevSb &s = c.sb;
+    if (!s.valid) {
+        c.err = "nss_hv: no superblock uploaded";
+        return NSS_ERR_STATE;
+    }
+    k_hv_fp64<<<s.ntiles, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles, s.d_dls, s.d_drs, s.d_off, s.d_hl,
+                                              s.d_hl_off, s.d_hr, s.d_hr_off, s.d_term_ptr, s.d_terms,
+                                              s.d_ab_rowptr, s.d_ab_col, s.d_ab_val);
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    return NSS_OK;
+}
+
+}  // namespace nss

@@ -1,0 +1,334 @@
+// Reduced density matrices, their block eigendecomposition and the
+// truncation choice, on the GPU.
+//
+// sb_get_rdm / build_density_matrix (src/DMRG_RDM.f90:18-162): for every
+// superblock sector k, Psi = W_k [Dl x Dr]; rho_L(k) = Psi Psi^T and
+// rho_R(k) = Psi^T Psi, appended in sector order (left block QN q, right
+// block QN target - q).  eigh_blocks_matrix (src/MATRIX/MATRIX_BLOCKS.f90:
+// 589-657): per-block symmetric eigensolve, negative eigenvalues set to
+// tiny(1d0), then one descending order over all blocks (ascending sort then
+// reversal: among exactly equal eigenvalues the later block position comes
+// first).  renormalize_block (src/DMRG_RDM.f90:204-221): m_s =
+// min(Mstates, m_block, #lambda), extended by every later eigenvalue within
+// deg_evals_threshold (relative) of lambda(m_s); trunc = 1 - sum lambda(1:m_s);
+// U = rho%sparse(m_block, m_s) (src/MATRIX/MATRIX_BLOCKS.f90:556-576).
+// Entropy -sum lambda log(lambda + 1e-32) (src/DMRG_MAIN.f90:511-518).
+//
+// The block eigensolve is cuSOLVER dsyevd, one call per block on the
+// context stream (a library call; the sector blocks are small, < 600).
+#include "device.cuh"
+
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+namespace nss {
+
+namespace {
+
+constexpr int RT = 16;
+
+struct RhoItem {     // one 16x16 tile of one rho block
+    int side, k, r0, c0;
+};
+
+// rho_L[a][b] = sum_r W[a][r] W[b][r] ; rho_R[a][b] = sum_l W[l][a] W[l][b]
+__global__ void __launch_bounds__(256) k_rho(const double *__restrict__ psi, const RhoItem *__restrict__ items,
+                                             const int *__restrict__ dls, const int *__restrict__ drs,
+                                             const int64_t *__restrict__ off, const int64_t *__restrict__ rho_off,
+                                             int nsb, double *__restrict__ rho) {
+    __shared__ double sa[RT][33];
+    __shared__ double sb[RT][33];
+    const RhoItem it = items[blockIdx.x];
+    const int dl = dls[it.k], dr = drs[it.k];
+    const double *W = psi + off[it.k];
+    const int dim = it.side == 0 ? dl : dr;       // rho is dim x dim
+    const int kk = it.side == 0 ? dr : dl;        // contraction length
+    double *R = rho + rho_off[it.side * nsb + it.k];
+    const int tid = threadIdx.x, ty = tid / RT, tx = tid % RT;
+    double acc = 0.0;
+    for (int j0 = 0; j0 < kk; j0 += 32) {
+        for (int e = tid; e < RT * 32; e += 256) {
+            const int r = e / 32, cc = e % 32;
+            const int ga = it.r0 + r, gb = it.c0 + r, gj = j0 + cc;
+            double va = 0.0, vb = 0.0;
+            if (gj < kk) {
+                if (it.side == 0) {
+                    if (ga < dim) va = W[(int64_t)ga * dr + gj];
+                    if (gb < dim) vb = W[(int64_t)gb * dr + gj];
+                } else {
+                    if (ga < dim) va = W[(int64_t)gj * dr + ga];
+                    if (gb < dim) vb = W[(int64_t)gj * dr + gb];
+                }
+            }
+            sa[r][cc] = va;
+            sb[r][cc] = vb;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) acc = fma(sa[ty][j], sb[tx][j], acc);
+        __syncthreads();
+    }
+    const int a = it.r0 + ty, b = it.c0 + tx;
+    if (a < dim && b < dim) R[(int64_t)a * dim + b] = acc;
+}
+
+// |rho - rho^T| > 1e-12 -> error flag (build_density_matrix, :159-160)
+__global__ void k_symcheck(const double *rho, int64_t total_dummy, const int64_t *rho_off, const int *dims,
+                           int nblk, int *err) {
+    for (int q = blockIdx.x; q < nblk; q += gridDim.x) {
+        const int d = dims[q];
+        const double *R = rho + rho_off[q];
+        for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+            const int a = e / d, b = e % d;
+            if (fabs(R[(int64_t)a * d + b] - R[(int64_t)b * d + a]) > 1e-12) atomicExch(err, 1);
+        }
+    }
+    (void)total_dummy;
+}
+
+// negative eigenvalues -> tiny(1d0) (MATRIX_BLOCKS.f90:629)
+__global__ void k_clamp(double *ev, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (ev[i] < 0.0) ev[i] = DBL_MIN;
+}
+
+// Descending rank of every eigenvalue; ties: larger position first (the
+// reversal of a stable ascending order).
+__global__ void k_rank(const double *ev, int n, double *sorted, int *order) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = ev[i];
+        int r = 0;
+        for (int j = 0; j < n; ++j) {
+            const double y = ev[j];
+            r += (y > x) || (y == x && j > i);
+        }
+        sorted[r] = x;
+        order[r] = i;
+    }
+}
+
+// Truncation choice, truncation error and entropy of one side (one thread;
+// sequential sums in descending order as the reference's loops).
+__global__ void k_truncate(const double *sorted, int n, int mstates, int mblock, double thr,
+                           double *out_d /*trunc, entropy*/, int *out_i /*m_s*/) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    auto lam = [&](int i) { return sorted[i] < 0.0 ? 0.0 : sorted[i]; };
+    int ms = min(mstates, min(mblock, n));
+    if (ms < 1) ms = 1;
+    const double e_ = lam(ms - 1);
+    int ext = 0;
+    for (int i = ms; i < n; ++i) {
+        const double err = fabs(e_ - lam(i)) / e_;
+        if (err <= thr) ++ext;
+    }
+    ms += ext;
+    double s = 0.0;
+    for (int i = 0; i < ms; ++i) s += lam(i);
+    double ent = 0.0;
+    for (int i = 0; i < n; ++i) ent -= lam(i) * log(lam(i) + 1e-32);
+    out_d[0] = 1.0 - s;
+    out_d[1] = ent;
+    out_i[0] = ms;
+}
+
+// U[map_q[p], j] = evec_q[p][col(j)] ; kept_blk[j] = q  (column-major U)
+__global__ void k_umat(const double *rho /*eigenvector blocks*/, const int64_t *rho_off, const int *dims,
+                       const int *ev_off /*[nblk+1] block starts*/, int ev_base, int nblk,
+                       const int *order, int ms, const int *maps, const int *map_off, int mblock,
+                       double *u, int *kept) {
+    for (int j = blockIdx.x; j < ms; j += gridDim.x) {
+        const int pos = order[j] + ev_base;   // position in the concatenated list
+        int q = 0;
+        while (q + 1 < nblk && ev_off[q + 1] <= pos) ++q;
+        const int col = pos - ev_off[q];
+        const int d = dims[q];
+        const double *E = rho + rho_off[q];   // column-major eigenvectors (cuSOLVER)
+        for (int p = threadIdx.x; p < d; p += blockDim.x)
+            u[(int64_t)j * mblock + maps[map_off[q] + p]] = E[(int64_t)col * d + p];
+        if (threadIdx.x == 0) kept[j] = q;
+    }
+}
+
+int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
+    if (*p && cap >= need) return NSS_OK;
+    ctx_free(c, *p);
+    *p = nullptr;
+    NSS_CUDA_TRY(c, ctx_alloc(c, p, (size_t)need));
+    cap = need;
+    return NSS_OK;
+}
+
+}  // namespace
+
+void rdm_release(Ctx &c) {
+    DevRdm &r = c.rdm;
+    void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal};
+    for (void *p : ptrs) ctx_free(c, p);
+    r = DevRdm{};
+}
+
+int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2], double *lam_l,
+            double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r) {
+    DevSb &s = c.sb;
+    if (!s.valid) { c.err = "nss_rdm: no superblock uploaded"; return NSS_ERR_STATE; }
+    if (s.ai.empty() || s.bi.empty()) { c.err = "nss_rdm: descriptor had no ai/bi state maps"; return NSS_ERR_INVALID; }
+    if (mstates < 1) { c.err = "nss_rdm: Mstates must be >= 1 (Edmrg mode is not supported)"; return NSS_ERR_INVALID; }
+    cudaStream_t st = c.stream;
+    DevRdm &r = c.rdm;
+    const int nsb = s.nsb;
+    // block layout: left blocks 0..nsb-1 then right blocks
+    std::vector<int64_t> rho_off(2 * nsb + 1);
+    std::vector<int> dims(2 * nsb), ev_off(2 * nsb + 2);
+    int64_t acc = 0;
+    int eacc = 0, maxd = 1;
+    for (int side = 0; side < 2; ++side)
+        for (int k = 0; k < nsb; ++k) {
+            const int d = side == 0 ? s.dls[k] : s.drs[k];
+            const int q = side * nsb + k;
+            rho_off[q] = acc;
+            dims[q] = d;
+            ev_off[q] = eacc;
+            acc += (int64_t)d * d;
+            eacc += d;
+            maxd = std::max(maxd, d);
+        }
+    rho_off[2 * nsb] = acc;
+    ev_off[2 * nsb] = eacc;
+    const int nl = ev_off[nsb], nr = eacc - nl;
+    std::vector<RhoItem> items;
+    for (int side = 0; side < 2; ++side)
+        for (int k = 0; k < nsb; ++k) {
+            const int d = side == 0 ? s.dls[k] : s.drs[k];
+            for (int r0 = 0; r0 < d; r0 += RT)
+                for (int c0 = 0; c0 < d; c0 += RT) items.push_back({side, k, r0, c0});
+        }
+    // device scratch: rho pool, evals, sorted, order, tables
+    int rc;
+    int64_t cap_sorted = r.cap_evals;
+    if ((rc = ensure(c, &r.rho, r.cap_rho, acc))) return rc;
+    if ((rc = ensure(c, &r.evals, r.cap_evals, eacc))) return rc;
+    if (!r.sorted || cap_sorted < eacc || !r.order) {
+        ctx_free(c, r.sorted);
+        ctx_free(c, r.order);
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.sorted, (size_t)eacc));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.order, (size_t)eacc));
+    }
+    const int mblk[2] = {s.m_left, s.m_right};
+    const int64_t ucap = (int64_t)std::max(s.m_left, s.m_right) * std::max(s.m_left, s.m_right);
+    if ((rc = ensure(c, &r.u, r.cap_u, ucap))) return rc;
+    if (!r.scal) {
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.scal, 8));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.iscal, 8));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.info, 1));
+    }
+    // small tables (allocated per call; freed at the end)
+    RhoItem *d_items = nullptr;
+    int64_t *d_rho_off = nullptr;
+    int *d_dims = nullptr, *d_ev_off = nullptr, *d_maps = nullptr, *d_map_off = nullptr;
+    std::vector<int> maps(s.ai), map_off(s.ai_off);
+    for (int k = 1; k <= nsb; ++k) map_off.push_back((int)s.ai.size() + s.bi_off[k]);
+    maps.insert(maps.end(), s.bi.begin(), s.bi.end());
+    auto up = [&](auto **dst, const auto &src) -> int {
+        NSS_CUDA_TRY(c, ctx_alloc(c, dst, src.size()));
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, st));
+        return NSS_OK;
+    };
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        void *ptrs[] = {d_items, d_rho_off, d_dims, d_ev_off, d_maps, d_map_off};
+        for (void *p : ptrs) ctx_free(c, p);
+    };
+    if ((rc = up(&d_items, items)) || (rc = up(&d_rho_off, rho_off)) || (rc = up(&d_dims, dims)) ||
+        (rc = up(&d_ev_off, ev_off)) || (rc = up(&d_maps, maps)) || (rc = up(&d_map_off, map_off))) {
+        cleanup();
+        return rc;
+    }
+    k_rho<<<(int)items.size(), 256, 0, st>>>(d_psi, d_items, s.d_dls, s.d_drs, s.d_off, d_rho_off, nsb, r.rho);
+    NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
+    k_symcheck<<<std::min(2 * nsb, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, 2 * nsb, r.iscal + 7);
+    // block eigensolves
+    cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
+    int lw = 0;
+    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, maxd, r.rho, maxd,
+                                    r.evals, &lw) != CUSOLVER_STATUS_SUCCESS) {
+        cleanup();
+        c.err = "nss_rdm: cusolverDnDsyevd_bufferSize failed";
+        return NSS_ERR_CUDA;
+    }
+    if (!r.work || r.lwork < lw) {
+        ctx_free(c, r.work);
+        r.work = nullptr;
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.work, (size_t)lw));
+        r.lwork = lw;
+    }
+    for (int q = 0; q < 2 * nsb; ++q) {
+        const int d = dims[q];
+        if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, r.rho + rho_off[q], d,
+                             r.evals + ev_off[q], r.work, (int)r.lwork, r.info) != CUSOLVER_STATUS_SUCCESS) {
+            cleanup();
+            c.err = "nss_rdm: cusolverDnDsyevd failed";
+            return NSS_ERR_CUDA;
+        }
+    }
+    k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
+    // per side: rank, truncation, U
+    const int nside[2] = {nl, nr};
+    for (int side = 0; side < 2; ++side) {
+        const int n = nside[side], base = side == 0 ? 0 : nl;
+        k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base);
+        k_truncate<<<1, 32, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
+                                     r.iscal + side);
+    }
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    double hs[4];
+    int hi[8];
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(hs, r.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(hi, r.iscal, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (hi[7]) {
+        cleanup();
+        c.err = "build_density_matrix error: rho not Symmetric";
+        return NSS_ERR_ASYMMETRIC;
+    }
+    double *lam_out[2] = {lam_l, lam_r};
+    int32_t *kept_out[2] = {kept_l, kept_r};
+    double *u_out[2] = {u_l, u_r};
+    for (int side = 0; side < 2; ++side) {
+        const int n = nside[side], base = side == 0 ? 0 : nl;
+        const int ms = hi[side];
+        out[side].nevals = n;
+        out[side].m_s = ms;
+        out[side].trunc_err = hs[2 * side];
+        out[side].entropy = hs[2 * side + 1];
+        if (lam_out[side]) {
+            // lambda clipped at 0 (DMRG_RDM.f90:88,97): tiny stays as is, as the
+            // reference clips only negative values after the tiny substitution
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(lam_out[side], r.sorted + base, n * sizeof(double),
+                                            cudaMemcpyDeviceToHost, st));
+        }
+        if (u_out[side] || kept_out[side]) {
+            NSS_CUDA_TRY(c, cudaMemsetAsync(r.u, 0, (size_t)mblk[side] * ms * sizeof(double), st));
+            int *kept_buf = nullptr;
+            NSS_CUDA_TRY(c, ctx_alloc(c, &kept_buf, (size_t)std::max(ms, 1)));
+            int *d_kept = kept_buf;
+            k_umat<<<std::min(ms, 1024), 128, 0, st>>>(r.rho, d_rho_off + side * nsb, d_dims + side * nsb,
+                                                       d_ev_off + side * nsb, base, nsb, r.order + base, ms,
+                                                       d_maps, d_map_off + side * nsb, mblk[side], r.u, d_kept);
+            NSS_CUDA_TRY(c, cudaGetLastError());
+            if (u_out[side])
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(u_out[side], r.u, (size_t)mblk[side] * ms * sizeof(double),
+                                                cudaMemcpyDeviceToHost, st));
+            if (kept_out[side])
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(kept_out[side], d_kept, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+            ctx_free(c, kept_buf);
+        }
+    }
+    cleanup();
+    return NSS_OK;
+}
+
+}  // namespace nss

@@ -1,0 +1,57 @@
+"""Whole DMRG runs with every superblock solve on the GPU, against the
+reference's published trajectories and the oracle's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nss():
+    import nssdmrg_gb300 as nss
+    nss.lib()
+    return nss
+
+
+MODELS = {"heisenberg_half": 0, "heisenberg_one": 1, "hubbard": 2}
+
+
+def _run(nss, t, finite=False):
+    d = nss.DMRG(MODELS[t["model"]], t["ldmrg"], t["mdmrg"], msweep=t.get("msweep", ()),
+                 u=t.get("u", 0.0), hfmode=t.get("hfmode", True),
+                 dmrg_qn=tuple(t["dmrg_qn"]) + ((0.0,) if len(t["dmrg_qn"]) == 1 else ()),
+                 lanc_neigen=t["neigen"], lanc_tolerance=1e-12)
+    recs = d.finite() if finite else d.infinite()
+    return recs
+
+
+@pytest.mark.parametrize("key", ["spin_L40_M20", "hubbard_L40_M40", "hubbard_U2_L100_M50"])
+def test_reference_trajectory(nss, trajectories, key):
+    t = trajectories[key]
+    recs = _run(nss, t)
+    ne = t["neigen"]
+    e = np.array([r["energy"][:ne] for r in recs])
+    ref = np.array(t["energy"])[:, :ne]
+    assert e.shape == ref.shape
+    np.testing.assert_allclose(e, ref, rtol=1e-10, atol=0)
+    s = np.array([r["entropy_left"] for r in recs])
+    np.testing.assert_allclose(s[:-1], np.array(t["entropy"])[:-1], rtol=0, atol=1e-7)
+
+
+@pytest.mark.parametrize("key", ["hubbard_U4_L20_M64", "spin1_L16_M48"])
+def test_oracle_trajectory(nss, oracle_runs, key):
+    t = oracle_runs[key]
+    recs = _run(nss, t)
+    e = np.array([r["energy"][0] for r in recs])
+    np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-10, atol=0)
+    assert [r["n"] for r in recs] == t["N"]
+    np.testing.assert_allclose([r["trunc_left"] for r in recs], t["trunc"], rtol=0, atol=1e-9)
+
+
+def test_finite_sweeps_c1(nss, oracle_runs):
+    t = oracle_runs["c1_spin_L20_M64_3sweeps"]
+    recs = _run(nss, t, finite=True)
+    assert [r["left_length"] for r in recs] == t["left_length"]
+    assert [r["n"] for r in recs] == t["N"]
+    e = np.array([r["energy"][0] for r in recs])
+    np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-10, atol=0)

@@ -1,0 +1,168 @@
+"""CUDA path against the oracle on identical inputs, through the C ABI.
+
+Tolerances: H*v and rho eigenvalues are FP64 sums in a different order than
+the oracle's, bounded here at 1e-12 relative to the largest entry; energies
+at 1e-12 relative (the reference's own assertion for the spin model).
+Sector enumeration and block indexing are integer work: bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_npz
+from oracle import dmrg_oracle as O
+from tests.golden.blockio import unpack_block
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nss():
+    import nssdmrg_gb300 as nss
+    nss.lib()
+    return nss
+
+
+def _setup(z):
+    l, r = unpack_block("eleft", z), unpack_block("eright", z)
+    sb = O.sb_get_states(l, r, z["target"])
+    ds = O.setup_direct(l, r, sb, z["hij"])
+    return l, r, sb, ds
+
+
+def _upload(nss, sbo, l, r, ds):
+    terms = [(t.it - 1, t.isb, t.jsb, t.hconj, t.A, t.B, t.row_offset, t.col_offset) for t in ds.terms]
+    sbo.upload(ds.sb.Dls, ds.sb.Drs, ds.sb.Offset, ds.Hleft, ds.Hright, terms, ds.tNso, l.dim, r.dim,
+               ds.sb.AI, ds.sb.BI)
+
+
+def _blocks(blk):
+    d = {"basis": blk.basis}
+    for k, (m, _) in blk.ops.items():
+        d[k] = m
+    return d
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_hv_upload_path_matches_oracle(nss, name):
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    assert s.n == sb.N
+    hv = s.spmatvec(z["v"])
+    ref = z["hv"]
+    assert np.abs(hv - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_block_setup_enumeration_is_bit_exact(nss, name):
+    z = load_npz(name)
+    l, r = unpack_block("eleft", z), unpack_block("eright", z)
+    s = nss.Superblock()
+    st = nss.NSS_SITE_FERMION if l.sitetype == "fermion" else nss.NSS_SITE_SPIN
+    s.setup(st, _blocks(l), _blocks(r), z["target"], z["hij"])
+    qns, dls, drs, off, states = s.tables()
+    np.testing.assert_array_equal(qns, z["sb_qns"])
+    np.testing.assert_array_equal(dls, z["sb_dls"])
+    np.testing.assert_array_equal(drs, z["sb_drs"])
+    np.testing.assert_array_equal(off, z["sb_offset"])
+    np.testing.assert_array_equal(states, z["sb_states"])
+    hv = s.spmatvec(z["v"])
+    assert np.abs(hv - z["hv"]).max() <= 1e-12 * np.abs(z["hv"]).max()
+
+
+def test_hv_is_linear_and_symmetric(nss):
+    z = load_npz("c2_small.npz")
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    rng = np.random.default_rng(5)
+    u, v = rng.standard_normal(sb.N), rng.standard_normal(sb.N)
+    hu, hv = s.spmatvec(u), s.spmatvec(v)
+    huv = s.spmatvec(2.0 * u - 3.0 * v)
+    scale = np.abs(hu).max() + np.abs(hv).max()
+    assert np.abs(huv - (2.0 * hu - 3.0 * hv)).max() <= 1e-12 * scale
+    assert abs(u @ hv - v @ hu) <= 1e-11 * scale * np.sqrt(sb.N)
+
+
+@pytest.mark.parametrize("name,neigen", [("kat_spin.npz", 2), ("kat_hubbard.npz", 1)])
+def test_eigh_matches_energy_check(nss, name, neigen):
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    ev, vec, numop = s.sb_diag(neigen=neigen, tol=1e-12)
+    current_l = l.length + r.length
+    np.testing.assert_allclose(ev / current_l, z["golden_energy"], rtol=1e-12, atol=0)
+    # the Ritz vectors are normalised eigenvectors to the tolerance
+    hv = s.spmatvec(vec[:, 0])
+    assert np.linalg.norm(hv - ev[0] * vec[:, 0]) <= 1e-9 * abs(ev[0])
+    assert abs(np.linalg.norm(vec[:, 0]) - 1.0) < 1e-12
+    assert 0 < numop <= 512
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz"])
+def test_rdm_of_given_state_matches_oracle(nss, name):
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    mst = int(z["params"][1])
+    res = s.sb_get_rdm(mst, 0.1, psi=z["psi"])
+    np.testing.assert_allclose(res.lambdas[0], z["lam_left"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(res.lambdas[1], z["lam_right"], rtol=0, atol=1e-13)
+    assert list(res.m_s) == [int(x) for x in z["ms"]]
+    np.testing.assert_allclose(res.trunc_err, z["trunc"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(res.entropy, z["entropy"], rtol=1e-11, atol=0)
+    # U has orthonormal columns and spans kept blocks only
+    for side in (0, 1):
+        u = res.u[side]
+        assert np.allclose(u.T @ u, np.eye(u.shape[1]), atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_full_solve_entropy_matches_oracle(nss, name):
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    ev, vec, _ = s.sb_diag(neigen=1, tol=1e-12, want_vectors=False)
+    np.testing.assert_allclose(ev[0], z["oracle_gs_energy"][0], rtol=1e-12, atol=0)
+    res = s.sb_get_rdm(64, 0.1)
+    np.testing.assert_allclose(res.lambdas[0], z["lam_left"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(res.entropy[0], z["entropy"][0], rtol=1e-9, atol=0)
+
+
+def test_errors_are_status_codes(nss):
+    s = nss.Superblock()
+    with pytest.raises(nss.NssError) as e:
+        s.spmatvec(np.zeros(4))
+    assert e.value.code == nss.NSS_ERR_STATE
+    z = load_npz("kat_spin.npz")
+    l, r, sb, ds = _setup(z)
+    bad = list(ds.sb.Offset)
+    bad[1] += 1
+    terms = [(t.it - 1, t.isb, t.jsb, t.hconj, t.A, t.B, t.row_offset, t.col_offset) for t in ds.terms]
+    with pytest.raises(nss.NssError) as e:
+        s.upload(ds.sb.Dls, ds.sb.Drs, bad, ds.Hleft, ds.Hright, terms, ds.tNso, l.dim, r.dim)
+    assert e.value.code == nss.NSS_ERR_INVALID
+    _upload(nss, s, l, r, ds)
+    with pytest.raises(nss.NssError) as e:
+        s.spmatvec(np.zeros(sb.N + 1))
+    assert e.value.code == nss.NSS_ERR_INVALID
+
+
+def test_tiny_superblock_exhausts_krylov_space(nss):
+    """First iDMRG step: N=6; the Krylov space is the whole space."""
+    dot = O.spin_site(2)
+    l = O.enlarge_block(dot, dot, "l", O.heisenberg_hij())
+    r = O.enlarge_block(dot, dot, "r", O.heisenberg_hij())
+    sb = O.sb_get_states(l, r, np.array([0.0]))
+    ds = O.setup_direct(l, r, sb, O.heisenberg_hij())
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    ev, vec, numop = s.sb_diag(neigen=2, tol=1e-12)
+    h = O.sparse_superblock_h(l, r, sb, O.heisenberg_hij()).toarray()
+    ref = np.linalg.eigvalsh(h)[:2]
+    np.testing.assert_allclose(ev, ref, rtol=1e-12, atol=1e-12)
+    assert numop <= sb.N
