@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: the superblock eigensolve of nssDMRG on one GB300.
+
+Workload (one "step"): the last infinite-DMRG superblock of the Hubbard
+chain L=32 (Ldmrg=16), t=1, U=4 (plain U n_up n_dw, HFMODE=F), half filling
+N_up=N_dw=16, Mdmrg=256 -- the ground-state Lanczos solve (tolerance 1e-12,
+at most 512 iterations, seeded random start) followed by the reduced density
+matrices, their block eigendecomposition and the truncation choice.  The
+superblock itself is produced by running the infinite algorithm up to that
+step (untimed set-up); its inputs are synthetic only in the sense that the
+chain is generated, not read from a data set.
+
+metric: H_sb*psi TFLOP/s sustained through the whole solve, i.e. the
+algorithmic flops of one H*psi (dense sector products 2 Dl Dr (Dl+Dr) plus
+the A x B terms as the reference's loops count them) times the number of
+H*psi products, divided by the step time.  Extra keys give solves/s and
+the per-step time.
+
+--impl reference times the oracle's C restatement of the reference's CPU
+path (spMatVec_direct_main loop nest + Lanczos) on all host cores, on the
+same workload built by the CPU oracle; no GPU code runs on that arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"workload": "hubbard_L32_U4_M256_last_infinite_step", "model": "hubbard", "L": 32,
+            "ldmrg": 16, "mdmrg": 256, "U": 4.0, "t": 1.0, "hfmode": False, "filling": "half",
+            "lanc_tolerance": 1e-12, "lanc_niter": 512, "neigen": 1}
+METRIC = "H_sb·ψ TFLOP/s (superblock eigensolve + RDM)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, x in enumerate(r) if x.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------
+def build_product_workload(nss, device, precision):
+    d = nss.DMRG(nss.MODEL_HUBBARD, WORKLOAD["ldmrg"], WORKLOAD["mdmrg"], u=WORKLOAD["U"], t=WORKLOAD["t"],
+                 hfmode=WORKLOAD["hfmode"], dmrg_qn=(0.5, 0.5), lanc_neigen=1, precision=precision,
+                 device=device)
+    t0 = time.perf_counter()
+    d.prepare_last()
+    return d, time.perf_counter() - t0
+
+
+def cpu_baseline_leg(desc, n, flops_hv, budget_s=20.0):
+    """Oracle C restatement on all host cores, one full solve of the same
+    superblock (bounded: at most `budget_s` seconds of Lanczos work)."""
+    from oracle.cref import RefSuperblock, lib as reflib
+    reflib()
+    ref = RefSuperblock.from_desc_struct(desc, n)
+    cores = os.cpu_count() or 1
+    # calibrate the per-iteration cost on a short run, then size the sample
+    t0 = time.perf_counter()
+    ev, numop, rc = ref.lanczos(neigen=1, nitermax=16, tol=1e-12, seed=7, nthreads=cores)
+    per_it = (time.perf_counter() - t0) / max(numop, 1)
+    nit = int(max(16, min(WORKLOAD["lanc_niter"], budget_s / max(per_it, 1e-9) / 2)))
+    t0 = time.perf_counter()
+    ev, numop, rc = ref.lanczos(neigen=1, nitermax=nit, tol=1e-12, seed=7, nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": flops_hv * numop / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"one Lanczos solve of the same superblock (N={n}), {numop} H*psi products "
+                      f"({'converged' if rc == 0 else 'iteration-capped'}), OpenMP over sectors, "
+                      f"{dt:.2f} s", "energy": float(ev[0])}
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import nssdmrg_gb300 as nss
+    prec = nss.NSS_PREC_FP64 if args.precision == "fp64" else nss.NSS_PREC_MIXED
+    d, t_prep = build_product_workload(nss, local, prec)
+    sb = d.sb
+    n = sb.n
+    fd, fab = sb.flops()
+    f_hv = fd + fab
+    ext = torch.cuda.ExternalStream(sb.stream)
+    flush = torch.empty(int(512 * 2**20) // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def solve(seed):
+        ev, _, numop = sb.sb_diag(neigen=1, nitermax=WORKLOAD["lanc_niter"], tol=WORKLOAD["lanc_tolerance"],
+                                  seed=seed, precision=prec, want_vectors=False)
+        res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=False)
+        return ev, numop, res
+
+    for w in range(args.warmup):
+        solve(100 + w)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = sb.launches
+    times, numops, energies = [], [], []
+    torch.cuda.nvtx.range_push("bench_timed")
+    with Clocks(local) as clk:
+        for s in range(args.steps):
+            flush.zero_()                      # evict L2 between timed steps
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            ev, numop, res = solve(1000 + s)
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            numops.append(numop)
+            energies.append(float(ev[0]))
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    launches = sb.launches - launches0
+    t_total = sum(times)
+    if world > 1:
+        tt = torch.tensor([t_total], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(tt.item())
+        torch.distributed.barrier()
+    flops_total = f_hv * sum(numops) * world
+    value = flops_total / (t_total / 1e3) / 1e12
+
+    # dominant kernel: the sector H*psi kernel, timed alone on the same stream
+    v = torch.randn(n, dtype=torch.float64, device=f"cuda:{local}")
+    hv = torch.empty_like(v)
+    torch.cuda.synchronize()
+    for _ in range(5):
+        sb.hv_device(v.data_ptr(), hv.data_ptr())
+    reps = 50
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("bench_hv")
+    k0.record(ext)
+    for _ in range(reps):
+        sb.hv_device(v.data_ptr(), hv.data_ptr())
+    k1.record(ext)
+    torch.cuda.nvtx.range_pop()
+    k1.synchronize()
+    t_hv = k0.elapsed_time(k1) / reps / 1e3
+    hv_achieved = f_hv / t_hv / 1e12
+
+    # end-to-end through the C ABI with host buffers: upload the operator
+    # pool from host memory, solve, bring the RDM outputs (lambda, kept
+    # blocks, rotation matrices) back to host memory.
+    desc = d.export_superblock()
+    e2e_times = []
+    h2d = d2h = 0
+    for s in range(max(2, args.steps // 2) + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        sb.upload_desc(desc)
+        ev, _, numop = sb.sb_diag(neigen=1, nitermax=WORKLOAD["lanc_niter"], tol=WORKLOAD["lanc_tolerance"],
+                                  seed=2000 + s, precision=prec, want_vectors=False)
+        res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=True)
+        e1.record(ext)
+        e1.synchronize()
+        if s == 0:
+            continue                           # first pass re-allocates
+        e2e_times.append(e0.elapsed_time(e1))
+        h2d = sb.upload_bytes
+        d2h = 8 + sum(8 * lam.size for lam in res.lambdas) + sum(4 * k.size for k in res.kept_blocks) + \
+            sum(8 * u.size for u in res.u)
+        numops.append(numop)
+    e2e_value = f_hv * statistics.mean(numops) / (statistics.mean(e2e_times) / 1e3) / 1e12 * world
+
+    out = None
+    if rank == 0:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
+            else {}
+        fp64 = json.loads((ROOT / "profiles" / "fp64_peak.json").read_text())["dfma_gflops"] / 1e3 \
+            if (ROOT / "profiles" / "fp64_peak.json").exists() else 1.007
+        traffic = None
+        tp = ROOT / "profiles" / "roofline_traffic.json"
+        if tp.exists():
+            traffic = json.loads(tp.read_text()).get("k_hv_fp64_bytes_per_launch")
+        out = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32/f64",
+            "data": "synthetic (Hubbard chain generated by the infinite algorithm; L2 flushed between steps)",
+            "config": dict(WORKLOAD, N=n, precision=args.precision,
+                           l2="flushed between timed steps (512 MiB write)",
+                           parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "solves_per_s": 1e3 * args.steps * world / t_total,
+            "numop_mean": statistics.mean(numops[:args.steps]),
+            "flops_per_hv": f_hv, "flops_per_hv_dense": fd, "flops_per_hv_ab": fab,
+            "energy_per_site": energies[-1] / WORKLOAD["L"],
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_times)},
+            "roofline": {"kernel": "k_hv_fp64 (sector H*psi)", "bound": "fp64", "achieved": hv_achieved,
+                         "peak": fp64, "unit": "TFLOP/s", "frac": hv_achieved / fp64, "traffic": traffic,
+                         "peak_source": "DFMA microbenchmark on this pool's GB300 (profiles/fp64_peak.md); "
+                                        "MEASURED_PEAKS.json has HBM and bf16 only",
+                         "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")},
+            "setup_s": t_prep,
+        }
+        if not args.no_cpu_baseline and world == 1:
+            try:
+                out["cpu_baseline"] = cpu_baseline_leg(desc, n, f_hv)
+            except Exception as e:   # the baseline must never break the GPU line
+                out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        out["clocks"] = clk.summary()
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    from oracle import dmrg_oracle as O
+    from oracle.cref import RefSuperblock
+    obuild.build()
+    t0 = time.perf_counter()
+    p = O.Params(Ldmrg=WORKLOAD["ldmrg"], Mdmrg=WORKLOAD["mdmrg"], lanc_neigen=1, dmrg_qn=(0.5, 0.5))
+    run = O.DMRG(O.hubbard_hij(WORKLOAD["t"]), O.electron_site(WORKLOAD["U"], WORKLOAD["hfmode"]), p,
+                 keep_setups=True)
+    while run.left.length < p.Ldmrg - 1:
+        run.step("i")
+    # the last step's superblock, built by the oracle (no GPU code)
+    run.left = O.enlarge_block(run.left, run.dot, "l", run.hij)
+    run.right = O.enlarge_block(run.right, run.dot, "r", run.hij)
+    target = O.current_target_qn(p, run.left.length + run.right.length)
+    sbo = O.sb_get_states(run.left, run.right, target)
+    ds = O.setup_direct(run.left, run.right, sbo, run.hij)
+    t_prep = time.perf_counter() - t0
+    ref = RefSuperblock(ds, run.left.dim, run.right.dim)
+    f_hv = sum(2.0 * dl * dr * (dl + dr) for dl, dr in zip(sbo.Dls, sbo.Drs))
+    f_hv += sum(2.0 * (t.B.nnz * t.A.shape[1] + t.A.nnz * t.B.shape[0]) for t in ds.terms)
+    cores = os.cpu_count() or 1
+    # bounded sample per step: Lanczos capped so the whole run stays short
+    t0 = time.perf_counter()
+    ev, numop, rc = ref.lanczos(neigen=1, nitermax=16, tol=1e-12, seed=7, nthreads=cores)
+    per_it = (time.perf_counter() - t0) / max(numop, 1)
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    nit = int(max(8, min(WORKLOAD["lanc_niter"], budget / max(per_it, 1e-9) / 2)))
+    for w in range(args.warmup):
+        ref.lanczos(neigen=1, nitermax=min(nit, 16), tol=1e-12, seed=w, nthreads=cores)
+    times, numops = [], []
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        ev, numop, rc = ref.lanczos(neigen=1, nitermax=nit, tol=1e-12, seed=1000 + s, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+        numops.append(numop)
+    value = f_hv * sum(numops) / sum(times) / 1e12
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (Hubbard chain generated by the CPU oracle's infinite algorithm)",
+           "config": dict(WORKLOAD, N=sbo.N, precision="fp64", l2="n/a (CPU)", parallelism="host cores"),
+           "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                            "sample": f"per step one Lanczos solve capped at {nit} H*psi products "
+                                      f"(oracle C restatement of spMatVec_direct_main + Lanczos, OpenMP)"},
+           "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "gpu_launches": 0, "flops_per_hv": f_hv, "numop_mean": statistics.mean(numops), "setup_s": t_prep,
+           "energy_per_site": float(ev[0]) / WORKLOAD["L"]}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)

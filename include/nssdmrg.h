@@ -95,6 +95,19 @@ int nss_sb_free(nss_ctx *ctx);
 /* Vector length of the uploaded superblock (sb_vecDim_Hv, :626-646). */
 int64_t nss_sb_dim(const nss_ctx *ctx);
 
+/* Algorithmic work of one H*v on the uploaded superblock: the dense sector
+ * products 2 Dl Dr (Dl + Dr) summed over sectors, and the A x B terms counted
+ * as the reference's loops count them, 2 (nnz(B) Ncol(A) + nnz(A) Nrow(B))
+ * (src/DMRG_SUPERBLOCK_SETUP.f90:819-853).  Either pointer may be NULL. */
+int nss_sb_flops(const nss_ctx *ctx, double *dense, double *ab);
+/* Number of kernels of this library launched on the context so far (library
+ * kernels of cuSOLVER are not counted). */
+int64_t nss_kernel_launches(const nss_ctx *ctx);
+/* Bytes copied host->device by the last nss_sb_upload / nss_sb_setup. */
+int64_t nss_sb_upload_bytes(const nss_ctx *ctx);
+/* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
+void *nss_stream(const nss_ctx *ctx);
+
 /* sparse_HxV: hv = H_sb v for host vectors of length n (must equal
  * nss_sb_dim).  spMatVec_direct_main semantics: hv is overwritten. */
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv);

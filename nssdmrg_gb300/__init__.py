@@ -107,6 +107,10 @@ def lib():
         "nss_sb_upload": (C.c_int, [P, C.POINTER(SbDesc)]),
         "nss_sb_free": (C.c_int, [P]),
         "nss_sb_dim": (I64, [P]),
+        "nss_sb_flops": (C.c_int, [P, C.POINTER(D), C.POINTER(D)]),
+        "nss_kernel_launches": (I64, [P]),
+        "nss_sb_upload_bytes": (I64, [P]),
+        "nss_stream": (P, [P]),
         "nss_hv": (C.c_int, [P, I64, P, P]),
         "nss_hv_device": (C.c_int, [P, I64, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
@@ -289,6 +293,29 @@ class Superblock:
         st = np.zeros(n.value, np.int64)
         self._check(L.nss_sb_tables(self._ctx, _ptr(qns), _ptr(dls), _ptr(drs), _ptr(off), _ptr(st)))
         return qns, dls, drs, off, st
+
+    def flops(self):
+        """(dense, ab) algorithmic FLOPs of one H*v."""
+        d, a = C.c_double(), C.c_double()
+        self._check(lib().nss_sb_flops(self._ctx, C.byref(d), C.byref(a)))
+        return d.value, a.value
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
+        return int(lib().nss_stream(self._ctx) or 0)
+
+    @property
+    def upload_bytes(self) -> int:
+        return int(lib().nss_sb_upload_bytes(self._ctx))
+
+    @property
+    def launches(self) -> int:
+        return int(lib().nss_kernel_launches(self._ctx))
+
+    def hv_device(self, d_v: int, d_hv: int):
+        """H*v on device pointers (e.g. torch tensors' data_ptr())."""
+        self._check(lib().nss_hv_device(self._ctx, self.n, C.c_void_p(d_v), C.c_void_p(d_hv)))
 
     # -- sparse_HxV
     def spmatvec(self, v: np.ndarray) -> np.ndarray:

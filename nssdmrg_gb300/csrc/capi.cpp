@@ -134,6 +134,19 @@ int nss_sb_free(nss_ctx *ctx) {
 
 int64_t nss_sb_dim(const nss_ctx *ctx) { return (ctx && ctx->c.sb.valid) ? ctx->c.sb.n : 0; }
 
+int nss_sb_flops(const nss_ctx *ctx, double *dense, double *ab) {
+    if (!ctx || !ctx->c.sb.valid) return NSS_ERR_STATE;
+    if (dense) *dense = ctx->c.sb.flops_dense;
+    if (ab) *ab = ctx->c.sb.flops_ab;
+    return NSS_OK;
+}
+
+int64_t nss_kernel_launches(const nss_ctx *ctx) { return ctx ? ctx->c.launches : 0; }
+
+int64_t nss_sb_upload_bytes(const nss_ctx *ctx) { return (ctx && ctx->c.sb.valid) ? ctx->c.sb.h2d_bytes : 0; }
+
+void *nss_stream(const nss_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
 int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

@@ -43,6 +43,7 @@ struct DevSb {
     std::vector<DevTerm> terms;
     // F_HV bookkeeping: algorithmic flops of one H*v
     double flops_dense = 0.0, flops_ab = 0.0;
+    int64_t h2d_bytes = 0;
     // device arrays
     int *d_dls = nullptr, *d_drs = nullptr;
     int64_t *d_off = nullptr, *d_hl_off = nullptr, *d_hr_off = nullptr;
@@ -98,6 +99,7 @@ struct Ctx {
     DevSb sb;
     DevLanczos lz;
     DevRdm rdm;
+    int64_t launches = 0;        // kernels of this library launched
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;

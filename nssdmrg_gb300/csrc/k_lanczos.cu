@@ -227,9 +227,10 @@ __global__ void k_next(double *__restrict__ vnext, const double *__restrict__ w,
     if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_M] = j + 2;
 }
 
-// x <- x / ||x|| (one CTA per launch is enough for start vectors)
-__global__ void k_normalize(double *x, int64_t n) {
-    __shared__ double red[8];
+// x <- x / ||x|| (one CTA per launch is enough for start vectors);
+// blockDim.x <= 1024, so at most 32 warp partial sums
+__global__ void __launch_bounds__(1024) k_normalize(double *x, int64_t n) {
+    __shared__ double red[32];
     double ss = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss = fma(x[i], x[i], ss);
     ss = warp_sum(ss);
@@ -455,7 +456,9 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta, 0, (cap + 1) * sizeof(double), st));
     const int vb = 608;   // 4 CTAs per SM for elementwise kernels
     uint64_t restarts = 0;
+    ++c.launches;
     k_random<<<vb, 256, 0, st>>>(z.V, n, seed, restarts);
+    ++c.launches;
     k_normalize<<<1, 1024, 0, st>>>(z.V, n);
     int j = 0, m_done = 1, numop_ = 0;
     bool converged = false;
@@ -475,16 +478,22 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             const int m = jj + 1;
             rc = hv_device(c, z.V + (int64_t)jj * n, z.w);
             if (rc) return rc;
+            ++c.launches;
             k_alpha<<<NBLK, 256, 0, st>>>(z.V + (int64_t)jj * n, z.w, n, z.part, z.scal, z.counter, z.flags);
+            ++c.launches;
             k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m, z.w, n, z.part, h1, z.scal, z.counter, z.flags, 0, 1,
                                                  z.beta);
+            ++c.launches;
             k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m, z.w, n, h1, z.part, z.scal, z.counter, z.flags,
                                                   z.alpha, z.beta, 0);
+            ++c.launches;
             k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m, z.w, n, z.part, h2, z.scal, z.counter, z.flags, 1, 0,
                                                  z.beta);
+            ++c.launches;
             k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m, z.w, n, h2, z.part, z.scal, z.counter, z.flags,
                                                   z.alpha, z.beta, 1);
             if (m < mmax)
+                ++c.launches;
                 k_next<<<vb, 256, 0, st>>>(z.V + (int64_t)m * n, z.w, n, z.scal, z.flags, z.alpha, z.beta, jj);
         }
         NSS_CUDA_TRY(c, cudaGetLastError());
@@ -496,6 +505,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         j = ran;
         m_done = j;
         const bool full = (m_done >= mmax) || (m_done >= n);
+        ++c.launches;
         k_tridiag<<<1, 256, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
                                      z.flags, full ? 1 : 0);
         NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -507,17 +517,21 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             // invariant subspace: continue from a random vector orthogonal to V
             ++restarts;
             double *vn = z.V + (int64_t)m_done * n;
+            ++c.launches;
             k_random<<<vb, 256, 0, st>>>(vn, n, seed, restarts);
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
             for (int pass = 0; pass < 2; ++pass) {
                 NSS_CUDA_TRY(c, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
+                ++c.launches;
                 k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m_done, vn, n, z.part, h1, z.scal, z.counter, z.flags, 0,
                                                      0, z.beta);
                 // reuse k_update on the candidate vector; alpha/beta slots of
                 // m_done-1 are restored below
+                ++c.launches;
                 k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m_done, vn, n, h1, z.part, z.scal, z.counter, z.flags,
                                                       rs_alpha, rs_beta, 0);
             }
+            ++c.launches;
             k_normalize<<<1, 1024, 0, st>>>(vn, n);
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
@@ -530,8 +544,12 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         return NSS_ERR_NOCONV;
     }
     const int ne = std::min<int64_t>(neigen, m_done);
+    ++c.launches;
     k_ritz<<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(z.V, m_done, n, z.svec, sstride, ne, z.evecs);
-    for (int e = 0; e < ne; ++e) k_normalize<<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
+    for (int e = 0; e < ne; ++e) {
+        ++c.launches;
+        k_normalize<<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
+    }
     cudaEventRecord(e1, st);
     NSS_CUDA_TRY(c, cudaGetLastError());
     if (evals_host) NSS_CUDA_TRY(c, cudaMemcpyAsync(evals_host, z.theta, ne * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -40,6 +40,7 @@ constexpr int TILE = 16;
 template <class T>
 int upload_vec(Ctx &c, T **dst, const std::vector<T> &src) {
     NSS_CUDA_TRY(c, ctx_alloc(c, dst, src.size()));
+    c.sb.h2d_bytes += (int64_t)(src.size() * sizeof(T));
     if (!src.empty())
         NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T),
                                         cudaMemcpyHostToDevice, c.stream));
@@ -283,6 +284,7 @@ int hv_device(Ctx &c, const double *d_v, double *d_hv) {
     k_hv_fp64<<<s.ntiles, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles, s.d_dls, s.d_drs, s.d_off, s.d_hl,
                                               s.d_hl_off, s.d_hr, s.d_hr_off, s.d_term_ptr, s.d_terms,
                                               s.d_ab_rowptr, s.d_ab_col, s.d_ab_val);
+    c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;
 }

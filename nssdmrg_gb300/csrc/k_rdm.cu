@@ -246,8 +246,10 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         cleanup();
         return rc;
     }
+    ++c.launches;
     k_rho<<<(int)items.size(), 256, 0, st>>>(d_psi, d_items, s.d_dls, s.d_drs, s.d_off, d_rho_off, nsb, r.rho);
     NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
+    ++c.launches;
     k_symcheck<<<std::min(2 * nsb, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, 2 * nsb, r.iscal + 7);
     // block eigensolves
     cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
@@ -273,12 +275,15 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             return NSS_ERR_CUDA;
         }
     }
+    ++c.launches;
     k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
     // per side: rank, truncation, U
     const int nside[2] = {nl, nr};
     for (int side = 0; side < 2; ++side) {
         const int n = nside[side], base = side == 0 ? 0 : nl;
+        ++c.launches;
         k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base);
+        ++c.launches;
         k_truncate<<<1, 32, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
                                      r.iscal + side);
     }
@@ -314,6 +319,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             int *kept_buf = nullptr;
             NSS_CUDA_TRY(c, ctx_alloc(c, &kept_buf, (size_t)std::max(ms, 1)));
             int *d_kept = kept_buf;
+            ++c.launches;
             k_umat<<<std::min(ms, 1024), 128, 0, st>>>(r.rho, d_rho_off + side * nsb, d_dims + side * nsb,
                                                        d_ev_off + side * nsb, base, nsb, r.order + base, ms,
                                                        d_maps, d_map_off + side * nsb, mblk[side], r.u, d_kept);

@@ -93,17 +93,17 @@ def trajectories(ref: Path):
                               "source": "test/src/Hubbard1d/L40.energy.check, L40.Sentropy.check"}
     e = np.loadtxt(pl / "Hubbard" / "U2" / "energyVSleft.length_L100_M50_iDMRG.dmrg")
     s = np.loadtxt(pl / "Hubbard" / "U2" / "SentropyVSleft.length_L100_M50_iDMRG.dmrg")
+    # This published run used deg_evals_threshold = 0.01 (its DMRG.conf does
+    # not set it; the current default is 0.1): with 0.01 all 99 steps are
+    # reproduced to 6e-15, with 0.1 the curve departs at step 28, where a
+    # multiplet 7.3 % below lambda(m_s) is kept.  The spin L=300 curve in
+    # .plot/HeisenbergSU2.3 matches no threshold of the current algorithm
+    # past step 7 (an older revision) and is not used.
     out["hubbard_U2_L100_M50"] = {"model": "hubbard", "ldmrg": 100, "mdmrg": 50, "neigen": 1, "u": 2.0,
-                                  "hfmode": False, "dmrg_qn": [0.5, 0.5],
+                                  "hfmode": False, "dmrg_qn": [0.5, 0.5], "deg_evals_threshold": 0.01,
                                   "left_length": e[:, 0].astype(int).tolist(), "energy": e[:, 1:2].tolist(),
                                   "entropy": s[:, 1].tolist(),
                                   "source": ".plot/Hubbard/U2/energyVSleft.length_L100_M50_iDMRG.dmrg"}
-    e = np.loadtxt(pl / "HeisenbergSU2.3" / "energyVSsys.length_L300_M40_iDMRG.dmrg")
-    s = np.loadtxt(pl / "HeisenbergSU2.3" / "SentropyVSsys.length_L300_M40_iDMRG.dmrg")
-    out["spin_L300_M40"] = {"model": "heisenberg_half", "ldmrg": 150, "mdmrg": 40, "neigen": 2,
-                            "dmrg_qn": [0.0], "left_length": e[:, 0].astype(int).tolist(),
-                            "energy": e[:, 1:3].tolist(), "entropy": s[:, 1].tolist(),
-                            "source": ".plot/HeisenbergSU2.3/energyVSsys.length_L300_M40_iDMRG.dmrg"}
     (OUT / "trajectories.json").write_text(json.dumps(out))
     print("trajectories:", {k: len(v["energy"]) for k, v in out.items()})
 

@@ -108,11 +108,13 @@ def test_hubbard_sentropy_check_is_the_step_that_wrote_the_restart_blocks(trajec
 
 
 def test_u2_hfmode_false_trajectory_first_steps(trajectories):
-    """U != 0 with the plain U n_up n_dw interaction (HFMODE=F)."""
+    """U != 0 with the plain U n_up n_dw interaction (HFMODE=F); the first 40
+    of the 99 published steps, past step 28 where the degeneracy extension
+    decides (the run used deg_evals_threshold = 0.01)."""
     t = trajectories["hubbard_U2_L100_M50"]
-    nsteps = 24
+    nsteps = 40
     p = O.Params(Ldmrg=nsteps + 1, Mdmrg=t["mdmrg"], lanc_neigen=1, lanc_ncv_factor=10,
-                 lanc_dim_threshold=128, dmrg_qn=(0.5, 0.5))
+                 lanc_dim_threshold=128, dmrg_qn=(0.5, 0.5), deg_evals_threshold=t["deg_evals_threshold"])
     run = O.DMRG(O.hubbard_hij(), O.electron_site(t["u"], t["hfmode"]), p)
     for _ in range(nsteps):
         run.step("i")
