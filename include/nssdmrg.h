@@ -94,6 +94,8 @@ int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc);
 int nss_sb_free(nss_ctx *ctx);
 /* Vector length of the uploaded superblock (sb_vecDim_Hv, :626-646). */
 int64_t nss_sb_dim(const nss_ctx *ctx);
+/* Shape of the uploaded superblock: sectors, enlarged block dims, N. */
+int nss_sb_shape(const nss_ctx *ctx, int32_t *nsb, int32_t *m_left, int32_t *m_right, int64_t *n);
 
 /* Algorithmic work of one H*v on the uploaded superblock: the dense sector
  * products 2 Dl Dr (Dl + Dr) summed over sectors, and the A x B terms counted

@@ -107,6 +107,7 @@ def lib():
         "nss_sb_upload": (C.c_int, [P, C.POINTER(SbDesc)]),
         "nss_sb_free": (C.c_int, [P]),
         "nss_sb_dim": (I64, [P]),
+        "nss_sb_shape": (C.c_int, [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]),
         "nss_sb_flops": (C.c_int, [P, C.POINTER(D), C.POINTER(D)]),
         "nss_kernel_launches": (I64, [P]),
         "nss_sb_upload_bytes": (I64, [P]),
@@ -294,6 +295,12 @@ class Superblock:
         self._check(L.nss_sb_tables(self._ctx, _ptr(qns), _ptr(dls), _ptr(drs), _ptr(off), _ptr(st)))
         return qns, dls, drs, off, st
 
+    def shape(self):
+        """(nsb, m_left, m_right, N) of the uploaded superblock, as the library holds it."""
+        a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
+        self._check(lib().nss_sb_shape(self._ctx, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return a.value, b.value, c.value, d.value
+
     def flops(self):
         """(dense, ab) algorithmic FLOPs of one H*v."""
         d, a = C.c_double(), C.c_double()
@@ -337,7 +344,9 @@ class Superblock:
 
     def sb_get_rdm(self, mstates, deg_thr=0.1, psi=None, want_u=True) -> RdmResult:
         out = (RdmSide * 2)()
-        ml, mr = self.m_left, self.m_right
+        _, ml, mr, n = self.shape()     # output buffers sized from the uploaded superblock
+        if psi is not None and np.asarray(psi).size != n:
+            raise NssError(NSS_ERR_INVALID, "psi has the wrong length")
         lam_l, lam_r = np.zeros(ml), np.zeros(mr)
         kl, kr = np.zeros(ml, np.int32), np.zeros(mr, np.int32)
         ul = np.zeros(ml * ml) if want_u else None

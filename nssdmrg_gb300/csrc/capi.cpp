@@ -134,6 +134,15 @@ int nss_sb_free(nss_ctx *ctx) {
 
 int64_t nss_sb_dim(const nss_ctx *ctx) { return (ctx && ctx->c.sb.valid) ? ctx->c.sb.n : 0; }
 
+int nss_sb_shape(const nss_ctx *ctx, int32_t *nsb, int32_t *m_left, int32_t *m_right, int64_t *n) {
+    if (!ctx || !ctx->c.sb.valid) return NSS_ERR_STATE;
+    if (nsb) *nsb = ctx->c.sb.nsb;
+    if (m_left) *m_left = ctx->c.sb.m_left;
+    if (m_right) *m_right = ctx->c.sb.m_right;
+    if (n) *n = ctx->c.sb.n;
+    return NSS_OK;
+}
+
 int nss_sb_flops(const nss_ctx *ctx, double *dense, double *ab) {
     if (!ctx || !ctx->c.sb.valid) return NSS_ERR_STATE;
     if (dense) *dense = ctx->c.sb.flops_dense;

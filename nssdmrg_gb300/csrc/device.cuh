@@ -54,8 +54,10 @@ struct DevSb {
     double *d_ab_val = nullptr;
     int4 *d_tiles = nullptr;
     int ntiles = 0;
-    // float copies for the mixed-precision path (built lazily)
-    float *d_hl32 = nullptr, *d_hr32 = nullptr;
+    // FP32 copies for the mixed-precision path
+    float *d_hl32 = nullptr, *d_hr32 = nullptr, *d_ab_val32 = nullptr;
+    int4 *d_tiles32 = nullptr;
+    int ntiles32 = 0;
 };
 
 // Device-side Lanczos state, kept resident between nss_eigh and nss_rdm.
@@ -64,6 +66,10 @@ struct DevLanczos {
     int64_t n = 0;
     double *V = nullptr;         // [cap][n]
     double *w = nullptr;         // [n]
+    float *V32 = nullptr;        // [cap][n] mixed-precision basis (lazily)
+    float *w32 = nullptr;        // [n]
+    double last_resid[4] = {0, 0, 0, 0};   // FP64 residual norms of the last solve
+    int last_iters = 0;
     double *evecs = nullptr;     // [neigen][n] Ritz vectors (last solve)
     int neigen_done = 0;
     double *scal = nullptr;      // device scalars (see k_lanczos.cu)
@@ -124,6 +130,7 @@ void ctx_free(Ctx &c, void *p);
 int sb_upload(Ctx &c, const nss_sb_desc *d);
 void sb_release(Ctx &c);
 int hv_device(Ctx &c, const double *d_v, double *d_hv);
+int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv);
 
 // k_lanczos.cu
 int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,

@@ -24,6 +24,17 @@
 // grow by ||H||/beta per step; the recurrence-first order keeps it at 1e-15.
 // Every kernel reads the device stop flag first, so the host can enqueue a
 // whole chunk of iterations ahead of the convergence test.
+//
+// Precision modes.  The kernels are templates over the type T of the Krylov
+// vectors.  T = double is the plain method: FP64 everywhere.  T = float is
+// the mixed method: H*psi in FP32 (k_hv_fp32), the basis and the projections
+// in FP32 with FP64 block partial sums, while alpha/beta, the tridiagonal
+// eigensolve and the Ritz vector stay FP64; it runs to a relative residual
+// of MIXED_TOL, and the energy is then refined in FP64 as the Rayleigh
+// quotient psi.H.psi of the FP64 Ritz vector with the FP64 H*psi (error
+// quadratic in the vector error: |dE|/|E| ~ 1e-13 at MIXED_TOL = 1e-7),
+// whose FP64 residual ||H psi - E psi|| is reported.  On GB300 the FP64
+// pipe runs at 1/64 of the FP32 one, which is what the mixed method buys.
 #include "device.cuh"
 
 #include <cmath>
@@ -38,13 +49,15 @@ namespace {
 constexpr int NBLK = 304;         // 2 CTAs per SM on the 152-SM GB300
 constexpr int CHECK = 8;          // convergence test period (iterations)
 constexpr int SUB = 1024;         // rows staged per shared-memory sub-chunk
+constexpr double MIXED_TOL = 1e-7;
 
 // device scalar slots (Ctx::lz.scal)
 enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NSCAL = 4 };
 // device flag slots (Ctx::lz.flags)
 enum { F_STOP = 0, F_PASS2 = 1, F_M = 2, F_CONV = 3, F_BREAK = 4, F_NFLAGS = 8 };
 
-__device__ __forceinline__ double warp_sum(double x) {
+template <class T>
+__device__ __forceinline__ T warp_sum(T x) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     return x;
 }
@@ -57,31 +70,44 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 }
 
 // uniform(-1,1) start vector from a counter-based hash of (seed, stream, i)
-__global__ void k_random(double *x, int64_t n, uint64_t seed, uint64_t stream) {
+template <class T>
+__global__ void k_random(T *x, int64_t n, uint64_t seed, uint64_t stream) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t r = splitmix64(seed ^ splitmix64(stream * 0x632BE59BD9B4E019ull + (uint64_t)i));
-        x[i] = 2.0 * ((double)(r >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+        x[i] = (T)(2.0 * ((double)(r >> 11) * (1.0 / 9007199254740992.0)) - 1.0);
     }
 }
 
-// h[l] = V[l] . w for l < m, and h[m] = w . w (written to scal[slot_ww]).
-// Grid-wide reduction by the last CTA to finish.
-// With threeterm != 0 the recurrence step w -= alpha v_{m-1} + beta v_{m-2}
-// (alpha from scal[S_ALPHA], beta = betas[m-2]) is applied to w first and
-// the updated w is written back.
-__global__ void __launch_bounds__(256) k_dots(const double *__restrict__ V, int m, double *__restrict__ w,
-                                              int64_t n, double *__restrict__ part, double *__restrict__ h,
+// Last-CTA-done grid reduction helper: every CTA writes its partials, the
+// last one to arrive sees all of them.
+__device__ __forceinline__ bool last_block(unsigned *counter) {
+    __shared__ unsigned last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) __threadfence();
+    return last != 0;
+}
+
+// h[l] = V[l] . w for l < m, and scal[S_WW] = w . w.  With threeterm != 0
+// the recurrence step w -= alpha v_{m-1} + beta v_{m-2} (alpha from
+// scal[S_ALPHA], beta = betas[m-2]) is applied to w first and the updated w
+// is written back.  Per-thread sums in T, block and grid sums in FP64.
+template <class T>
+__global__ void __launch_bounds__(256) k_dots(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n,
+                                              double *__restrict__ part, double *__restrict__ h,
                                               double *__restrict__ scal, unsigned *counter, const int *flags,
                                               int pass2, int threeterm, const double *__restrict__ betas) {
     if (flags[F_STOP] || (pass2 && !flags[F_PASS2])) return;
-    const double a3 = threeterm ? scal[S_ALPHA] : 0.0;
-    const double b3 = (threeterm && m >= 2) ? betas[m - 2] : 0.0;
-    const double *vj = V + (int64_t)(m - 1) * n;
-    const double *vjm = (m >= 2) ? V + (int64_t)(m - 2) * n : V;
     extern __shared__ double sm[];
-    double *ws = sm;             // [SUB]
-    double *acc = sm + SUB;      // [m+1]
+    double *acc = sm;                      // [m+1]
+    T *ws = (T *)(sm + (m + 2));           // [SUB]
+    const T a3 = threeterm ? (T)scal[S_ALPHA] : (T)0;
+    const T b3 = (threeterm && m >= 2) ? (T)betas[m - 2] : (T)0;
+    const T *vj = V + (int64_t)(m - 1) * n;
+    const T *vjm = (m >= 2) ? V + (int64_t)(m - 2) * n : V;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int l = tid; l <= m; l += 256) acc[l] = 0.0;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -91,7 +117,7 @@ __global__ void __launch_bounds__(256) k_dots(const double *__restrict__ V, int 
         __syncthreads();
         if (threeterm) {
             for (int e = tid; e < len; e += 256) {
-                double x = w[s0 + e] - a3 * vj[s0 + e];
+                T x = w[s0 + e] - a3 * vj[s0 + e];
                 if (m >= 2) x -= b3 * vjm[s0 + e];
                 ws[e] = x;
                 w[s0 + e] = x;
@@ -101,28 +127,24 @@ __global__ void __launch_bounds__(256) k_dots(const double *__restrict__ V, int 
         }
         __syncthreads();
         for (int l = warp; l <= m; l += 8) {
-            const double *vl = (l < m) ? V + (int64_t)l * n + s0 : nullptr;
-            double p = 0.0;
-            if (l < m)
-                for (int e = lane; e < len; e += 32) p = fma(vl[e], ws[e], p);
-            else
-                for (int e = lane; e < len; e += 32) p = fma(ws[e], ws[e], p);
-            p = warp_sum(p);
-            if (lane == 0) acc[l] += p;
+            T p = (T)0;
+            if (l < m) {
+                const T *vl = V + (int64_t)l * n + s0;
+                for (int e = lane; e < len; e += 32) p += vl[e] * ws[e];
+            } else {
+                for (int e = lane; e < len; e += 32) p += ws[e] * ws[e];
+            }
+            const double pd = warp_sum<double>((double)p);
+            if (lane == 0) acc[l] += pd;
         }
     }
     __syncthreads();
     for (int l = tid; l <= m; l += 256) part[(int64_t)l * gridDim.x + blockIdx.x] = acc[l];
-    __threadfence();
-    __shared__ unsigned last;
-    if (tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
+    if (!last_block(counter)) return;
     for (int l = warp; l <= m; l += 8) {
         double p = 0.0;
         for (int b = lane; b < (int)gridDim.x; b += 32) p += part[(int64_t)l * gridDim.x + b];
-        p = warp_sum(p);
+        p = warp_sum<double>(p);
         if (lane == 0) {
             if (l < m) h[l] = p;
             else scal[S_WW] = p;
@@ -132,29 +154,25 @@ __global__ void __launch_bounds__(256) k_dots(const double *__restrict__ V, int 
 }
 
 // alpha = v . w  (grid reduction by the last CTA) -> scal[S_ALPHA]
-__global__ void __launch_bounds__(256) k_alpha(const double *__restrict__ v, const double *__restrict__ w, int64_t n,
+template <class T>
+__global__ void __launch_bounds__(256) k_alpha(const T *__restrict__ v, const T *__restrict__ w, int64_t n,
                                                double *__restrict__ part, double *__restrict__ scal,
                                                unsigned *counter, const int *flags) {
     if (flags[F_STOP]) return;
     const int tid = threadIdx.x;
-    double p = 0.0;
+    T p = (T)0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p = fma(v[i], w[i], p);
-    p = warp_sum(p);
+        p += v[i] * w[i];
+    const double pd = warp_sum<double>((double)p);
     __shared__ double red[8];
-    if ((tid & 31) == 0) red[tid >> 5] = p;
+    if ((tid & 31) == 0) red[tid >> 5] = pd;
     __syncthreads();
     if (tid == 0) {
         double t = 0.0;
         for (int q = 0; q < 8; ++q) t += red[q];
         part[blockIdx.x] = t;
     }
-    __threadfence();
-    __shared__ unsigned last;
-    if (tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!last || tid != 0) return;
-    __threadfence();
+    if (!last_block(counter) || tid != 0) return;
     double t = 0.0;
     for (int b = 0; b < (int)gridDim.x; ++b) t += part[b];
     scal[S_ALPHA] = t;
@@ -162,45 +180,42 @@ __global__ void __launch_bounds__(256) k_alpha(const double *__restrict__ v, con
 }
 
 // w -= V_m h ; beta^2 = w.w ; the last CTA records alpha_j and beta_j.
-__global__ void __launch_bounds__(256) k_update(const double *__restrict__ V, int m, double *__restrict__ w,
-                                                int64_t n, const double *__restrict__ h, double *__restrict__ part,
+template <class T>
+__global__ void __launch_bounds__(256) k_update(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n,
+                                                const double *__restrict__ h, double *__restrict__ part,
                                                 double *__restrict__ scal, unsigned *counter, int *flags,
                                                 double *alpha, double *beta, int pass2) {
     if (flags[F_STOP] || (pass2 && !flags[F_PASS2])) return;
-    extern __shared__ double hs[];
+    extern __shared__ double hsd[];
+    T *hs = (T *)hsd;
     const int tid = threadIdx.x;
-    for (int l = tid; l < m; l += 256) hs[l] = h[l];
+    for (int l = tid; l < m; l += 256) hs[l] = (T)h[l];
     __syncthreads();
-    double ss = 0.0;
+    T ss = (T)0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double x = w[i];
-        for (int l = 0; l < m; ++l) x = fma(-V[(int64_t)l * n + i], hs[l], x);
+        T x = w[i];
+        for (int l = 0; l < m; ++l) x -= V[(int64_t)l * n + i] * hs[l];
         w[i] = x;
-        ss = fma(x, x, ss);
+        ss += x * x;
     }
-    ss = warp_sum(ss);
+    const double sd = warp_sum<double>((double)ss);
     __shared__ double red[8];
-    if ((tid & 31) == 0) red[tid >> 5] = ss;
+    if ((tid & 31) == 0) red[tid >> 5] = sd;
     __syncthreads();
     if (tid == 0) {
         double t = 0.0;
         for (int q = 0; q < 8; ++q) t += red[q];
         part[blockIdx.x] = t;
     }
-    __threadfence();
-    __shared__ unsigned last;
-    if (tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!last || tid != 0) return;
-    __threadfence();
+    if (!last_block(counter) || tid != 0) return;
     double bb = 0.0;
     for (int b = 0; b < (int)gridDim.x; ++b) bb += part[b];
     const int j = m - 1;
     if (!pass2) {
-        alpha[j] = scal[S_ALPHA] + hs[j];
+        alpha[j] = scal[S_ALPHA] + h[j];
         flags[F_PASS2] = (bb < 0.5 * scal[S_WW]) ? 1 : 0;
     } else {
-        alpha[j] += hs[j];
+        alpha[j] += h[j];
     }
     scal[S_BB] = bb;
     beta[j] = sqrt(bb);
@@ -208,11 +223,11 @@ __global__ void __launch_bounds__(256) k_update(const double *__restrict__ V, in
 }
 
 // v_{j+1} = w / beta_j, or flag a breakdown (invariant subspace).
-__global__ void k_next(double *__restrict__ vnext, const double *__restrict__ w, int64_t n, const double *scal,
-                       int *flags, const double *alpha, const double *beta, int j) {
+template <class T>
+__global__ void k_next(T *__restrict__ vnext, const T *__restrict__ w, int64_t n, int *flags,
+                       const double *alpha, const double *beta, int j) {
     if (flags[F_STOP]) return;
     const double b = beta[j];
-    // breakdown: beta below roundoff of the projected step
     const double scale = fmax(fabs(alpha[j]), j > 0 ? beta[j - 1] : 0.0);
     if (!(b > 1e-13 * fmax(scale, 1e-300))) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -221,7 +236,7 @@ __global__ void k_next(double *__restrict__ vnext, const double *__restrict__ w,
         }
         return;
     }
-    const double inv = 1.0 / b;
+    const T inv = (T)(1.0 / b);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         vnext[i] = w[i] * inv;
     if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_M] = j + 2;
@@ -229,17 +244,18 @@ __global__ void k_next(double *__restrict__ vnext, const double *__restrict__ w,
 
 // x <- x / ||x|| (one CTA per launch is enough for start vectors);
 // blockDim.x <= 1024, so at most 32 warp partial sums
-__global__ void __launch_bounds__(1024) k_normalize(double *x, int64_t n) {
+template <class T>
+__global__ void __launch_bounds__(1024) k_normalize(T *x, int64_t n) {
     __shared__ double red[32];
     double ss = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss = fma(x[i], x[i], ss);
-    ss = warp_sum(ss);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss += (double)x[i] * (double)x[i];
+    ss = warp_sum<double>(ss);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
     __syncthreads();
     double t = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
     const double inv = 1.0 / sqrt(t);
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] *= inv;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = (T)((double)x[i] * inv);
 }
 
 // Number of eigenvalues of T_m below x (Sturm count of the leading
@@ -376,8 +392,9 @@ __global__ void __launch_bounds__(256) k_tridiag(const double *alpha, const doub
     }
 }
 
-// Ritz vectors: out[e] = sum_l V[l] s_e[l]
-__global__ void __launch_bounds__(256) k_ritz(const double *__restrict__ V, int m, int64_t n,
+// Ritz vectors: out[e] = sum_l V[l] s_e[l]   (FP64 accumulation, FP64 out)
+template <class T>
+__global__ void __launch_bounds__(256) k_ritz(const T *__restrict__ V, int m, int64_t n,
                                               const double *__restrict__ svec, int sstride, int ne,
                                               double *__restrict__ out) {
     extern __shared__ double ss[];   // [ne][m]
@@ -386,27 +403,89 @@ __global__ void __launch_bounds__(256) k_ritz(const double *__restrict__ V, int 
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double acc[4] = {0, 0, 0, 0};
         for (int l = 0; l < m; ++l) {
-            const double v = V[(int64_t)l * n + i];
+            const double v = (double)V[(int64_t)l * n + i];
             for (int e = 0; e < ne && e < 4; ++e) acc[e] = fma(v, ss[e * m + l], acc[e]);
         }
         for (int e = 0; e < ne && e < 4; ++e) out[(int64_t)e * n + i] = acc[e];
     }
 }
 
+// FP64 refinement: r[0] = psi.w, r[1] = w.w, r[2] = psi.psi (grid reduction)
+__global__ void __launch_bounds__(256) k_rq(const double *__restrict__ psi, const double *__restrict__ w, int64_t n,
+                                            double *__restrict__ part, double *__restrict__ r, unsigned *counter) {
+    const int tid = threadIdx.x;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        a = fma(psi[i], w[i], a);
+        b = fma(w[i], w[i], b);
+        c = fma(psi[i], psi[i], c);
+    }
+    a = warp_sum<double>(a);
+    b = warp_sum<double>(b);
+    c = warp_sum<double>(c);
+    __shared__ double red[3][8];
+    if ((tid & 31) == 0) { red[0][tid >> 5] = a; red[1][tid >> 5] = b; red[2][tid >> 5] = c; }
+    __syncthreads();
+    if (tid < 3) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += red[tid][q];
+        part[(int64_t)tid * gridDim.x + blockIdx.x] = t;
+    }
+    if (!last_block(counter)) return;
+    if (tid < 3) {
+        double t = 0.0;
+        for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[(int64_t)tid * gridDim.x + bb];
+        r[tid] = t;
+    }
+    if (tid == 0) *counter = 0u;
+}
+
+// ||w - theta psi||^2 (grid reduction); theta = r[0]/r[2]
+__global__ void __launch_bounds__(256) k_resid(const double *__restrict__ psi, const double *__restrict__ w, int64_t n,
+                                               double *__restrict__ part, double *__restrict__ r, unsigned *counter) {
+    const int tid = threadIdx.x;
+    const double th = r[0] / r[2];
+    double a = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double d = w[i] - th * psi[i];
+        a = fma(d, d, a);
+    }
+    a = warp_sum<double>(a);
+    __shared__ double red[8];
+    if ((tid & 31) == 0) red[tid >> 5] = a;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += red[q];
+        part[blockIdx.x] = t;
+    }
+    if (!last_block(counter) || tid != 0) return;
+    double t = 0.0;
+    for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[bb];
+    r[3] = t;
+    *counter = 0u;
+}
+
 // per-eigenvector scratch row: s[m] followed by three factor bands of m
 inline int svec_stride(int cap) { return 4 * (cap + 1); }
 
-int ensure_lanczos(Ctx &c, int64_t n, int cap, int neigen) {
+int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     DevLanczos &z = c.lz;
-    if (z.V && z.n == n && z.cap >= cap) return NSS_OK;
+    if (z.V && z.n == n && z.cap >= cap && (!mixed || z.V32)) return NSS_OK;
     lanczos_release(c);
     z.n = n;
     z.cap = cap;
-    NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)(cap + 1) * n));
+    if (mixed) {
+        NSS_CUDA_TRY(c, ctx_alloc(c, &z.V32, (size_t)(cap + 1) * n));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &z.w32, (size_t)n));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)n));   // FP64 refinement scratch
+    } else {
+        NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)(cap + 1) * n));
+    }
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.w, (size_t)n));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));
     // scalars, two projection-coefficient vectors, restart scratch alpha/beta
-    NSS_CUDA_TRY(c, ctx_alloc(c, &z.scal, (size_t)S_NSCAL + 4 * (cap + 2)));
+    NSS_CUDA_TRY(c, ctx_alloc(c, &z.scal, (size_t)S_NSCAL + 4 * (cap + 2) + 8));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.part, (size_t)(cap + 2) * NBLK));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.counter, 4));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.alpha, (size_t)cap + 1));
@@ -417,7 +496,117 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, int neigen) {
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.flags, F_NFLAGS));
     NSS_CUDA_TRY(c, cudaMallocHost((void **)&z.h_flags, F_NFLAGS * sizeof(int)));
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.counter, 0, 4 * sizeof(unsigned), c.stream));
-    (void)neigen;
+    return NSS_OK;
+}
+
+template <class T>
+int hv_t(Ctx &c, const T *v, T *hv);
+template <>
+int hv_t<double>(Ctx &c, const double *v, double *hv) { return hv_device(c, v, hv); }
+template <>
+int hv_t<float>(Ctx &c, const float *v, float *hv) { return hv_device_fp32(c, v, hv); }
+
+// The Lanczos iterations on a basis of type T; leaves theta (Ritz values),
+// svec (their T-eigenvectors) and the Ritz vectors (FP64) in c.lz.
+template <class T>
+int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t seed, int *numop_out,
+                int *m_out) {
+    DevLanczos &z = c.lz;
+    const int64_t n = c.sb.n;
+    const int cap = z.cap;
+    double *h1 = z.scal + S_NSCAL, *h2 = h1 + (cap + 2);
+    double *rs_alpha = h2 + (cap + 2), *rs_beta = rs_alpha + (cap + 2);
+    const int sstride = svec_stride(cap);
+    cudaStream_t st = c.stream;
+    NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+    NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta, 0, (cap + 1) * sizeof(double), st));
+    const int vb = 608;   // 4 CTAs per SM for elementwise kernels
+    uint64_t restarts = 0;
+    ++c.launches;
+    k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
+    ++c.launches;
+    k_normalize<T><<<1, 1024, 0, st>>>(V, n);
+    int j = 0, m_done = 1, numop_ = 0, rc = NSS_OK;
+    bool converged = false;
+    const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
+    const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
+    if (dots_smem > 48 * 1024)
+        cudaFuncSetAttribute(k_dots<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
+    if (upd_smem > 48 * 1024)
+        cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+    while (!converged) {
+        const int jend = std::min(mmax, j + CHECK);
+        for (int jj = j; jj < jend; ++jj) {
+            const int m = jj + 1;
+            rc = hv_t<T>(c, V + (int64_t)jj * n, w);
+            if (rc) return rc;
+            c.launches += 5;
+            k_alpha<T><<<NBLK, 256, 0, st>>>(V + (int64_t)jj * n, w, n, z.part, z.scal, z.counter, z.flags);
+            k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m, w, n, z.part, h1, z.scal, z.counter, z.flags, 0, 1,
+                                                    z.beta);
+            k_update<T><<<NBLK, 256, upd_smem, st>>>(V, m, w, n, h1, z.part, z.scal, z.counter, z.flags,
+                                                     z.alpha, z.beta, 0);
+            k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m, w, n, z.part, h2, z.scal, z.counter, z.flags, 1, 0,
+                                                    z.beta);
+            k_update<T><<<NBLK, 256, upd_smem, st>>>(V, m, w, n, h2, z.part, z.scal, z.counter, z.flags,
+                                                     z.alpha, z.beta, 1);
+            if (m < mmax) {
+                ++c.launches;
+                k_next<T><<<vb, 256, 0, st>>>(V + (int64_t)m * n, w, n, z.flags, z.alpha, z.beta, jj);
+            }
+        }
+        NSS_CUDA_TRY(c, cudaGetLastError());
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        // iterations that ran: up to the breakdown step, or the whole chunk
+        const int ran = z.h_flags[F_STOP] == 2 ? z.h_flags[F_BREAK] : jend;
+        numop_ += ran - j;
+        j = ran;
+        m_done = j;
+        const bool full = (m_done >= mmax) || (m_done >= n);
+        ++c.launches;
+        k_tridiag<<<1, 256, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
+                                     z.flags, full ? 1 : 0);
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        const int conv = z.h_flags[F_CONV];
+        if (conv >= neigen || m_done >= n) { converged = true; break; }
+        if (m_done >= mmax) break;
+        if (z.h_flags[F_STOP] == 2) {
+            // invariant subspace: continue from a random vector orthogonal to V
+            ++restarts;
+            T *vn = V + (int64_t)m_done * n;
+            ++c.launches;
+            k_random<T><<<vb, 256, 0, st>>>(vn, n, seed, restarts);
+            NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+            for (int pass = 0; pass < 2; ++pass) {
+                NSS_CUDA_TRY(c, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
+                c.launches += 2;
+                k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m_done, vn, n, z.part, h1, z.scal, z.counter, z.flags,
+                                                        0, 0, z.beta);
+                k_update<T><<<NBLK, 256, upd_smem, st>>>(V, m_done, vn, n, h1, z.part, z.scal, z.counter, z.flags,
+                                                         rs_alpha, rs_beta, 0);
+            }
+            ++c.launches;
+            k_normalize<T><<<1, 1024, 0, st>>>(vn, n);
+            NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
+            NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+        }
+    }
+    *numop_out = numop_;
+    *m_out = m_done;
+    if (!converged) {
+        c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(mmax) + " iterations";
+        return NSS_ERR_NOCONV;
+    }
+    const int ne = (int)std::min<int64_t>(neigen, m_done);
+    ++c.launches;
+    k_ritz<T><<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(V, m_done, n, z.svec, sstride, ne, z.evecs);
+    for (int e = 0; e < ne; ++e) {
+        ++c.launches;
+        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
+    }
+    NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;
 }
 
@@ -425,7 +614,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, int neigen) {
 
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
-    void *ptrs[] = {z.V, z.w, z.evecs, z.scal, z.part, z.counter, z.alpha, z.beta,
+    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.evecs, z.scal, z.part, z.counter, z.alpha, z.beta,
                     z.theta, z.resid, z.svec, z.flags};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
@@ -443,123 +632,54 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     int mmax = (int)std::min<int64_t>(n, nitermax);
     if (mmax < neigen) mmax = neigen;
     if (tol <= 0.0) tol = 1e-15;
-    (void)precision;
-    int rc = ensure_lanczos(c, n, mmax + 1, neigen);
+    const bool mixed = precision == NSS_PREC_MIXED;
+    int rc = ensure_lanczos(c, n, mmax + 1, mixed);
     if (rc) return rc;
     DevLanczos &z = c.lz;
-    const int cap = z.cap;
-    double *h1 = z.scal + S_NSCAL, *h2 = h1 + (cap + 2);
-    double *rs_alpha = h2 + (cap + 2), *rs_beta = rs_alpha + (cap + 2);
-    const int sstride = svec_stride(cap);
     cudaStream_t st = c.stream;
-    NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-    NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta, 0, (cap + 1) * sizeof(double), st));
-    const int vb = 608;   // 4 CTAs per SM for elementwise kernels
-    uint64_t restarts = 0;
-    ++c.launches;
-    k_random<<<vb, 256, 0, st>>>(z.V, n, seed, restarts);
-    ++c.launches;
-    k_normalize<<<1, 1024, 0, st>>>(z.V, n);
-    int j = 0, m_done = 1, numop_ = 0;
-    bool converged = false;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    const size_t dots_smem = (SUB + cap + 2) * sizeof(double);
-    const size_t upd_smem = (cap + 2) * sizeof(double);
-    if (dots_smem > 48 * 1024)
-        cudaFuncSetAttribute(k_dots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
-    if (upd_smem > 48 * 1024)
-        cudaFuncSetAttribute(k_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
-    while (!converged) {
-        const int jend = std::min(mmax, j + CHECK);
-        for (int jj = j; jj < jend; ++jj) {
-            const int m = jj + 1;
-            rc = hv_device(c, z.V + (int64_t)jj * n, z.w);
-            if (rc) return rc;
-            ++c.launches;
-            k_alpha<<<NBLK, 256, 0, st>>>(z.V + (int64_t)jj * n, z.w, n, z.part, z.scal, z.counter, z.flags);
-            ++c.launches;
-            k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m, z.w, n, z.part, h1, z.scal, z.counter, z.flags, 0, 1,
-                                                 z.beta);
-            ++c.launches;
-            k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m, z.w, n, h1, z.part, z.scal, z.counter, z.flags,
-                                                  z.alpha, z.beta, 0);
-            ++c.launches;
-            k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m, z.w, n, z.part, h2, z.scal, z.counter, z.flags, 1, 0,
-                                                 z.beta);
-            ++c.launches;
-            k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m, z.w, n, h2, z.part, z.scal, z.counter, z.flags,
-                                                  z.alpha, z.beta, 1);
-            if (m < mmax)
-                ++c.launches;
-                k_next<<<vb, 256, 0, st>>>(z.V + (int64_t)m * n, z.w, n, z.scal, z.flags, z.alpha, z.beta, jj);
-        }
-        NSS_CUDA_TRY(c, cudaGetLastError());
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
-        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-        // iterations that ran: up to the breakdown step, or the whole chunk
-        int ran = z.h_flags[F_STOP] == 2 ? z.h_flags[F_BREAK] : jend;
-        numop_ += ran - j;
-        j = ran;
-        m_done = j;
-        const bool full = (m_done >= mmax) || (m_done >= n);
-        ++c.launches;
-        k_tridiag<<<1, 256, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
-                                     z.flags, full ? 1 : 0);
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
-        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-        const int conv = z.h_flags[F_CONV];
-        if (conv >= neigen || m_done >= n) { converged = true; break; }
-        if (m_done >= mmax) break;
-        if (z.h_flags[F_STOP] == 2) {
-            // invariant subspace: continue from a random vector orthogonal to V
-            ++restarts;
-            double *vn = z.V + (int64_t)m_done * n;
-            ++c.launches;
-            k_random<<<vb, 256, 0, st>>>(vn, n, seed, restarts);
-            NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-            for (int pass = 0; pass < 2; ++pass) {
-                NSS_CUDA_TRY(c, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
-                ++c.launches;
-                k_dots<<<NBLK, 256, dots_smem, st>>>(z.V, m_done, vn, n, z.part, h1, z.scal, z.counter, z.flags, 0,
-                                                     0, z.beta);
-                // reuse k_update on the candidate vector; alpha/beta slots of
-                // m_done-1 are restored below
-                ++c.launches;
-                k_update<<<NBLK, 256, upd_smem, st>>>(z.V, m_done, vn, n, h1, z.part, z.scal, z.counter, z.flags,
-                                                      rs_alpha, rs_beta, 0);
-            }
-            ++c.launches;
-            k_normalize<<<1, 1024, 0, st>>>(vn, n);
-            NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
-            NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-        }
+    int numop_ = 0, m_done = 0;
+    if (!mixed) {
+        rc = run_lanczos<double>(c, z.V, z.w, neigen, mmax, tol, seed, &numop_, &m_done);
+    } else {
+        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, MIXED_TOL), seed, &numop_, &m_done);
     }
-    if (!converged) {
-        c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(nitermax) + " iterations";
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        return NSS_ERR_NOCONV;
-    }
-    const int ne = std::min<int64_t>(neigen, m_done);
-    ++c.launches;
-    k_ritz<<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(z.V, m_done, n, z.svec, sstride, ne, z.evecs);
-    for (int e = 0; e < ne; ++e) {
-        ++c.launches;
-        k_normalize<<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
+    const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
+    if (!rc && mixed) {
+        // FP64 refinement of each eigenvalue: theta = psi.H.psi / psi.psi with
+        // the FP64 H*psi, and the FP64 residual ||H psi - theta psi||.
+        double *r = z.scal + S_NSCAL + 4 * (z.cap + 2);   // 8 refinement slots
+        for (int e = 0; e < ne; ++e) {
+            const double *psi = z.evecs + (int64_t)e * n;
+            rc = hv_device(c, psi, z.w);
+            ++numop_;
+            if (rc) break;
+            c.launches += 2;
+            k_rq<<<NBLK, 256, 0, st>>>(psi, z.w, n, z.part, r, z.counter);
+            k_resid<<<NBLK, 256, 0, st>>>(psi, z.w, n, z.part, r, z.counter);
+            double hr[4];
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(hr, r, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+            const double th = hr[0] / hr[2];
+            z.last_resid[e] = std::sqrt(std::max(hr[3], 0.0));
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta + e, &th, sizeof(double), cudaMemcpyHostToDevice, st));
+        }
     }
     cudaEventRecord(e1, st);
-    NSS_CUDA_TRY(c, cudaGetLastError());
-    if (evals_host) NSS_CUDA_TRY(c, cudaMemcpyAsync(evals_host, z.theta, ne * sizeof(double), cudaMemcpyDeviceToHost, st));
-    NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+    cudaError_t ce = cudaStreamSynchronize(st);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
+    if (evals_host) NSS_CUDA_TRY(c, cudaMemcpy(evals_host, z.theta, ne * sizeof(double), cudaMemcpyDeviceToHost));
     c.last_ms_eigh = ms;
     c.last_numop = numop_;
+    z.last_iters = m_done;
     z.neigen_done = ne;
     if (numop) *numop = numop_;
     return NSS_OK;

@@ -28,7 +28,7 @@ void sb_release(Ctx &c) {
     DevSb &s = c.sb;
     void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
                     s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
-                    s.d_tiles, s.d_hl32, s.d_hr32};
+                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32};
     for (void *p : ptrs) ctx_free(c, p);
     s = DevSb{};
 }
@@ -36,6 +36,7 @@ void sb_release(Ctx &c) {
 namespace {
 
 constexpr int TILE = 16;
+constexpr int TILE32 = 32;
 
 template <class T>
 int upload_vec(Ctx &c, T **dst, const std::vector<T> &src) {
@@ -184,7 +185,18 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
             for (int cc = 0; cc < s.drs[k]; cc += TILE) tiles.push_back(make_int4(k, r, cc, 0));
     s.ntiles = (int)tiles.size();
 
+    // FP32 copies for the mixed path, and its 32x32 tiles
+    std::vector<float> hl32(hl.begin(), hl.end()), hr32(hr.begin(), hr.end()), val32(val.begin(), val.end());
+    std::vector<int4> tiles32;
+    for (int k = 0; k < s.nsb; ++k)
+        for (int r = 0; r < s.dls[k]; r += TILE32)
+            for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
+    s.ntiles32 = (int)tiles32.size();
+
     int rc;
+    if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
+        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_tiles32, tiles32)))
+        return rc;
     if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
         (rc = upload_vec(c, &s.d_off, s.off)) || (rc = upload_vec(c, &s.d_hl_off, s.hl_off)) ||
         (rc = upload_vec(c, &s.d_hr_off, s.hr_off)) || (rc = upload_vec(c, &s.d_hl, hl)) ||
@@ -273,6 +285,103 @@ __global__ void __launch_bounds__(256) k_hv_fp64(
         }
     }
     hv[o + (int64_t)il * dr + ir] = acc;
+}
+
+// FP32 variant for the mixed-precision Lanczos phase: 32x32 output tiles,
+// each thread owns rows {ty, ty+16} x cols {tx, tx+16}; FP32 operands and
+// accumulation (GB300 issues FP32 FMAs 64x faster than FP64 ones).
+__global__ void __launch_bounds__(256) k_hv_fp32(
+    const float *__restrict__ v, float *__restrict__ hv, const int4 *__restrict__ tiles,
+    const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
+    const float *__restrict__ hlp, const int64_t *__restrict__ hl_off,
+    const float *__restrict__ hrp, const int64_t *__restrict__ hr_off,
+    const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
+    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val) {
+    __shared__ float sa[TILE32][33];
+    __shared__ float sb[32][TILE32 + 1];
+    const int4 t = tiles[blockIdx.x];
+    const int k = t.x, row0 = t.y, col0 = t.z;
+    const int dl = dls[k], dr = drs[k];
+    const int64_t o = off[k];
+    const float *W = v + o;
+    const float *HL = hlp + hl_off[k];
+    const float *HR = hrp + hr_off[k];
+    const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
+    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    // H_L W
+    for (int j0 = 0; j0 < dl; j0 += 32) {
+        for (int e = tid; e < TILE32 * 32; e += 256) {
+            const int r = e / 32, cc = e % 32;
+            const int gi = row0 + r, gj = j0 + cc;
+            sa[r][cc] = (gi < dl && gj < dl) ? HL[(int64_t)gi * dl + gj] : 0.f;
+            const int gj2 = j0 + r, gc = col0 + cc;
+            sb[r][cc] = (gj2 < dl && gc < dr) ? W[(int64_t)gj2 * dr + gc] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+            const float a0 = sa[ty][j], a1 = sa[ty + 16][j], b0 = sb[j][tx], b1 = sb[j][tx + 16];
+            acc[0][0] = fmaf(a0, b0, acc[0][0]);
+            acc[0][1] = fmaf(a0, b1, acc[0][1]);
+            acc[1][0] = fmaf(a1, b0, acc[1][0]);
+            acc[1][1] = fmaf(a1, b1, acc[1][1]);
+        }
+        __syncthreads();
+    }
+    // W H_R^T
+    for (int j0 = 0; j0 < dr; j0 += 32) {
+        for (int e = tid; e < TILE32 * 32; e += 256) {
+            const int r = e / 32, cc = e % 32;
+            const int gi = row0 + r, gj = j0 + cc;
+            sa[r][cc] = (gi < dl && gj < dr) ? W[(int64_t)gi * dr + gj] : 0.f;
+            const int gr = col0 + r;                 // sb[j][x] = HR[col0+x][j0+j]
+            sb[cc][r] = (gr < dr && gj < dr) ? HR[(int64_t)gr * dr + gj] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+            const float a0 = sa[ty][j], a1 = sa[ty + 16][j], b0 = sb[j][tx], b1 = sb[j][tx + 16];
+            acc[0][0] = fmaf(a0, b0, acc[0][0]);
+            acc[0][1] = fmaf(a0, b1, acc[0][1]);
+            acc[1][0] = fmaf(a1, b0, acc[1][0]);
+            acc[1][1] = fmaf(a1, b1, acc[1][1]);
+        }
+        __syncthreads();
+    }
+    for (int rr = 0; rr < 2; ++rr)
+        for (int cc = 0; cc < 2; ++cc) {
+            const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+            if (il >= dl || ir >= dr) continue;
+            float a = acc[rr][cc];
+            for (int ti = term_ptr[k]; ti < term_ptr[k + 1]; ++ti) {
+                const DevTerm tm = terms[ti];
+                const float *Wq = v + off[tm.in_sec];
+                const int drq = drs[tm.in_sec];
+                const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
+                for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
+                    const int aj = ab_col[ja];
+                    float cb = 0.f;
+                    for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
+                        cb = fmaf(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
+                    a = fmaf(ab_val[ja], cb, a);
+                }
+            }
+            hv[o + (int64_t)il * dr + ir] = a;
+        }
+}
+
+int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv) {
+    DevSb &s = c.sb;
+    if (!s.valid) {
+        c.err = "nss_hv: no superblock uploaded";
+        return NSS_ERR_STATE;
+    }
+    k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
+                                                s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms,
+                                                s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32);
+    c.launches += 1;
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    return NSS_OK;
 }
 
 int hv_device(Ctx &c, const double *d_v, double *d_hv) {

@@ -36,7 +36,10 @@ def test_reference_trajectory(nss, trajectories, key):
     assert e.shape == ref.shape
     np.testing.assert_allclose(e, ref, rtol=1e-10, atol=0)
     s = np.array([r["entropy_left"] for r in recs])
-    np.testing.assert_allclose(s[:-1], np.array(t["entropy"])[:-1], rtol=0, atol=1e-7)
+    ref_s = np.array(t["entropy"])
+    # the published entropy files end one row early or repeat the last row
+    nrow = min(len(s), len(ref_s)) - 1
+    np.testing.assert_allclose(s[:nrow], ref_s[:nrow], rtol=0, atol=1e-7)
 
 
 @pytest.mark.parametrize("key", ["hubbard_U4_L20_M64", "spin1_L16_M48"])
@@ -59,5 +62,16 @@ def test_finite_sweeps_c1(nss, oracle_runs):
     recs = _run(nss, t, finite=True)
     assert [r["left_length"] for r in recs] == t["left_length"]
     assert [r["n"] for r in recs][:5] == t["N"][:5]
+    e = np.array([r["energy"][0] for r in recs])
+    np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-10, atol=0)
+
+
+def test_mixed_precision_trajectory(nss, trajectories):
+    """Whole iDMRG run with the mixed method: every energy within 1e-10 of
+    the reference's published trajectory."""
+    t = trajectories["hubbard_L40_M40"]
+    d = nss.DMRG(MODELS[t["model"]], t["ldmrg"], t["mdmrg"], u=t["u"], hfmode=t["hfmode"],
+                 dmrg_qn=tuple(t["dmrg_qn"]), lanc_neigen=1, precision=nss.NSS_PREC_MIXED)
+    recs = d.infinite()
     e = np.array([r["energy"][0] for r in recs])
     np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-10, atol=0)

@@ -166,3 +166,21 @@ def test_tiny_superblock_exhausts_krylov_space(nss):
     ref = np.linalg.eigvalsh(h)[:2]
     np.testing.assert_allclose(ev, ref, rtol=1e-12, atol=1e-12)
     assert numop <= sb.N
+
+
+@pytest.mark.parametrize("name,neigen", [("kat_spin.npz", 2), ("kat_hubbard.npz", 1), ("c2_small.npz", 1)])
+def test_mixed_precision_energy_within_1e10(nss, name, neigen):
+    """Mixed method: FP32 H*psi and Krylov basis, FP64 alpha/beta, FP64
+    Rayleigh-quotient refinement; |dE|/|E| <= 1e-10 against the FP64 oracle."""
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    ev, vec, numop = s.sb_diag(neigen=neigen, tol=1e-12, precision=nss.NSS_PREC_MIXED)
+    ref = z["oracle_gs_energy"][:neigen]
+    np.testing.assert_allclose(ev, ref, rtol=1e-10, atol=0)
+    # the refined Ritz vector is an eigenvector to FP32-level accuracy
+    hv = s.spmatvec(vec[:, 0])
+    assert np.linalg.norm(hv - ev[0] * vec[:, 0]) <= 1e-5 * abs(ev[0])
+    res = s.sb_get_rdm(64, 0.1)
+    assert abs(res.entropy[0] - z["entropy"][0]) <= 1e-5 * abs(z["entropy"][0])
