@@ -48,8 +48,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="headline path; the other one is timed alongside for comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="for profiler captures: time the headline path only, no clock sampler, no "
+                         "compute-rate probe, no e2e, no CPU baseline (no child processes)")
     return ap.parse_args()
 
 
@@ -68,12 +72,15 @@ class Clocks:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, enabled: bool = True):
         self.device = device
+        self.enabled = enabled
         self.proc = None
         self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
 
     def __enter__(self):
+        if not self.enabled:
+            return self
         try:
             self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
@@ -94,6 +101,8 @@ class Clocks:
             self.f.close()
 
     def summary(self):
+        if not self.enabled:
+            return None
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
@@ -111,6 +120,23 @@ class Clocks:
         reasons = sorted({names[i] for _, _, r in rows for i, x in enumerate(r) if x.lower() == "active"})
         return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
                 "samples": len(rows), "reasons": reasons}
+
+
+def measure_core_peaks():
+    """FP64 (DFMA) and FP32 (FFMA) whole-GPU rates in TFLOP/s, measured now by
+    the package's microbenchmark (MEASURED_PEAKS.json holds only the HBM
+    copy and bf16 tensor rates)."""
+    exe = ROOT / "nssdmrg_gb300" / "_build" / "peaks"
+    try:
+        from nssdmrg_gb300.build import build_peaks
+        exe = build_peaks()
+        line = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.strip().splitlines()[-1]
+        j = json.loads(line)
+        return j["dfma_gflops"] / 1e3, j["ffma_gflops"] / 1e3, \
+            "DFMA / FFMA rates measured in this run by nssdmrg_gb300/peaks.cu (whole GPU)"
+    except Exception as e:  # keep the line; say what was used
+        return 1.007, 73.7, f"fallback: earlier peaks.cu measurement on this pool ({str(e)[:60]})"
+    # (a measured FFMA rate is the FP32 kernels' denominator)
 
 
 # ---------------------------------------------------------------------------
@@ -162,51 +188,73 @@ def run_gpu(args):
     ext = torch.cuda.ExternalStream(sb.stream)
     flush = torch.empty(int(512 * 2**20) // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    def solve(seed):
+    def solve(seed, p):
         ev, _, numop = sb.sb_diag(neigen=1, nitermax=WORKLOAD["lanc_niter"], tol=WORKLOAD["lanc_tolerance"],
-                                  seed=seed, precision=prec, want_vectors=False)
+                                  seed=seed, precision=p, want_vectors=False)
         res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=False)
         return ev, numop, res
 
-    for w in range(args.warmup):
-        solve(100 + w)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    launches0 = sb.launches
-    times, numops, energies = [], [], []
-    torch.cuda.nvtx.range_push("bench_timed")
-    with Clocks(local) as clk:
-        for s in range(args.steps):
-            flush.zero_()                      # evict L2 between timed steps
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(ext)
-            ev, numop, res = solve(1000 + s)
-            e1.record(ext)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-            numops.append(numop)
-            energies.append(float(ev[0]))
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
-    launches = sb.launches - launches0
-    t_total = sum(times)
-    if world > 1:
-        tt = torch.tensor([t_total], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-        torch.distributed.barrier()
-    flops_total = f_hv * sum(numops) * world
-    value = flops_total / (t_total / 1e3) / 1e12
+    def time_path(p, steps, sample_clocks):
+        for w in range(args.warmup):
+            solve(100 + w, p)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        l0 = sb.launches
+        times, numops, energies, ents = [], [], [], []
+        torch.cuda.nvtx.range_push("bench_timed")
+        with Clocks(local, enabled=sample_clocks) as clk:
+            for s in range(steps):
+                flush.zero_()                      # evict L2 between timed steps
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                ev, numop, res = solve(1000 + s, p)
+                e1.record(ext)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+                numops.append(numop)
+                energies.append(float(ev[0]))
+                ents.append(res.entropy[0])
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        t_total = sum(times)
+        if world > 1:
+            tt = torch.tensor([t_total], device=f"cuda:{local}")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_total = float(tt.item())
+            torch.distributed.barrier()
+        return {"t_total": t_total, "numops": numops, "energies": energies, "entropy": ents,
+                "launches": sb.launches - l0, "clocks": clk.summary(),
+                "value": f_hv * sum(numops) * world / (t_total / 1e3) / 1e12,
+                "ms_per_step": t_total / steps, "solves_per_s": 1e3 * steps * world / t_total}
 
-    # dominant kernel: the sector H*psi kernel, timed alone on the same stream
-    v = torch.randn(n, dtype=torch.float64, device=f"cuda:{local}")
+    other = nss.NSS_PREC_FP64 if prec == nss.NSS_PREC_MIXED else nss.NSS_PREC_MIXED
+    head = time_path(prec, args.steps, not args.profile)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "ms_per_step": head["ms_per_step"],
+                              "numop_mean": statistics.mean(head["numops"])}))
+        return None
+    comp = time_path(other, args.steps, False)
+    value = head["value"]
+    t_total = head["t_total"]
+    numops = list(head["numops"])
+    energies = head["energies"]
+    launches = head["launches"]
+    clk_summary = head["clocks"]
+
+    # dominant kernel of the headline path: its sector H*psi kernel, timed
+    # alone on the library's stream (FP64: k_hv_fp64; mixed: the FP32 one)
+    mixed = prec == nss.NSS_PREC_MIXED
+    dt = torch.float32 if mixed else torch.float64
+    v = torch.randn(n, dtype=dt, device=f"cuda:{local}")
     hv = torch.empty_like(v)
+    hv_call = sb.hv_device_f32 if mixed else sb.hv_device
     torch.cuda.synchronize()
     for _ in range(5):
-        sb.hv_device(v.data_ptr(), hv.data_ptr())
+        hv_call(v.data_ptr(), hv.data_ptr())
     reps = 50
     k0 = torch.cuda.Event(enable_timing=True)
     k1 = torch.cuda.Event(enable_timing=True)
@@ -215,7 +263,7 @@ def run_gpu(args):
     torch.cuda.nvtx.range_push("bench_hv")
     k0.record(ext)
     for _ in range(reps):
-        sb.hv_device(v.data_ptr(), hv.data_ptr())
+        hv_call(v.data_ptr(), hv.data_ptr())
     k1.record(ext)
     torch.cuda.nvtx.range_pop()
     k1.synchronize()
@@ -253,31 +301,41 @@ def run_gpu(args):
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
             else {}
-        fp64 = json.loads((ROOT / "profiles" / "fp64_peak.json").read_text())["dfma_gflops"] / 1e3 \
-            if (ROOT / "profiles" / "fp64_peak.json").exists() else 1.007
+        fp64, fp32, peak_src = measure_core_peaks()
+        kname = "k_hv_fp32" if mixed else "k_hv_fp64"
+        peak = fp32 if mixed else fp64
         traffic = None
         tp = ROOT / "profiles" / "roofline_traffic.json"
         if tp.exists():
-            traffic = json.loads(tp.read_text()).get("k_hv_fp64_bytes_per_launch")
+            traffic = json.loads(tp.read_text()).get(f"{kname}_bytes_per_launch")
+        # same superblock, same seed: the two paths' energies
+        de = abs(head["energies"][0] - comp["energies"][0]) / abs(comp["energies"][0])
         out = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32/f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)" if mixed else "f64",
             "data": "synthetic (Hubbard chain generated by the infinite algorithm; L2 flushed between steps)",
             "config": dict(WORKLOAD, N=n, precision=args.precision,
                            l2="flushed between timed steps (512 MiB write)",
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
-            "solves_per_s": 1e3 * args.steps * world / t_total,
+            "solves_per_s": head["solves_per_s"],
             "numop_mean": statistics.mean(numops[:args.steps]),
+            ("fp64" if mixed else "mixed"): {"value": comp["value"], "ms_per_step": comp["ms_per_step"],
+                                             "solves_per_s": comp["solves_per_s"],
+                                             "numop_mean": statistics.mean(comp["numops"]),
+                                             "energy_per_site": comp["energies"][-1] / WORKLOAD["L"]},
+            "speedup_vs_other_path": comp["ms_per_step"] / head["ms_per_step"],
+            "dE_rel_mixed_vs_fp64": de,
+            "d_entropy_rel_mixed_vs_fp64": abs(head["entropy"][0] - comp["entropy"][0]) / abs(comp["entropy"][0]),
             "flops_per_hv": f_hv, "flops_per_hv_dense": fd, "flops_per_hv_ab": fab,
             "energy_per_site": energies[-1] / WORKLOAD["L"],
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_times)},
-            "roofline": {"kernel": "k_hv_fp64 (sector H*psi)", "bound": "fp64", "achieved": hv_achieved,
-                         "peak": fp64, "unit": "TFLOP/s", "frac": hv_achieved / fp64, "traffic": traffic,
-                         "peak_source": "DFMA microbenchmark on this pool's GB300 (profiles/fp64_peak.md); "
-                                        "MEASURED_PEAKS.json has HBM and bf16 only",
+            "roofline": {"kernel": f"{kname} (sector H*psi)", "bound": "fp32" if mixed else "fp64",
+                         "achieved": hv_achieved, "peak": peak, "unit": "TFLOP/s", "frac": hv_achieved / peak,
+                         "traffic": traffic,
+                         "peak_source": peak_src,
                          "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")},
             "setup_s": t_prep,
         }
@@ -286,7 +344,7 @@ def run_gpu(args):
                 out["cpu_baseline"] = cpu_baseline_leg(desc, n, f_hv)
             except Exception as e:   # the baseline must never break the GPU line
                 out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
-        out["clocks"] = clk.summary()
+        out["clocks"] = clk_summary
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -115,6 +115,8 @@ void *nss_stream(const nss_ctx *ctx);
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv);
 /* Same on device pointers, ordered on the context's stream. */
 int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv);
+/* The FP32 product of the mixed-precision path, on device pointers. */
+int nss_hv_device_f32(nss_ctx *ctx, int64_t n, const float *d_v, float *d_hv);
 
 /* Lowest `neigen` eigenpairs of the uploaded H_sb (replaces sp_eigh at
  * src/DMRG_SUPERBLOCK.f90:394-425).  nitermax caps the Krylov dimension,

@@ -114,6 +114,7 @@ def lib():
         "nss_stream": (P, [P]),
         "nss_hv": (C.c_int, [P, I64, P, P]),
         "nss_hv_device": (C.c_int, [P, I64, P, P]),
+        "nss_hv_device_f32": (C.c_int, [P, I64, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
@@ -323,6 +324,10 @@ class Superblock:
     def hv_device(self, d_v: int, d_hv: int):
         """H*v on device pointers (e.g. torch tensors' data_ptr())."""
         self._check(lib().nss_hv_device(self._ctx, self.n, C.c_void_p(d_v), C.c_void_p(d_hv)))
+
+    def hv_device_f32(self, d_v: int, d_hv: int):
+        """The mixed path's FP32 H*v on device pointers."""
+        self._check(lib().nss_hv_device_f32(self._ctx, self.n, C.c_void_p(d_v), C.c_void_p(d_hv)))
 
     # -- sparse_HxV
     def spmatvec(self, v: np.ndarray) -> np.ndarray:

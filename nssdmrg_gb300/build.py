@@ -63,5 +63,20 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     return LIB
 
 
+def build_peaks(verbose: bool = False) -> Path:
+    """Compile the compute-rate microbenchmark (peaks.cu) next to the objects."""
+    BUILD.mkdir(exist_ok=True)
+    exe = BUILD / "peaks"
+    src = HERE / "peaks.cu"
+    if exe.exists() and exe.stat().st_mtime >= src.stat().st_mtime:
+        return exe
+    r = subprocess.run([nvcc(), *ARCH, "-O3", "-o", str(exe), str(src)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on peaks.cu:\n{r.stderr}")
+    if verbose:
+        print(f"built {exe}")
+    return exe
+
+
 if __name__ == "__main__":
     build(verbose=True, extra=sys.argv[1:])

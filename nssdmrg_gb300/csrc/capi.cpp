@@ -165,6 +165,15 @@ int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv) {
     return nss::hv_device(ctx->c, d_v, d_hv);
 }
 
+int nss_hv_device_f32(nss_ctx *ctx, int64_t n, const float *d_v, float *d_hv) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
+    if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
+    if (!d_v || !d_hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
+    cudaSetDevice(ctx->c.device);
+    return nss::hv_device_fp32(ctx->c, d_v, d_hv);
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

@@ -88,9 +88,12 @@ struct DevRdm {
     double *sorted = nullptr;    // descending
     int *order = nullptr;        // block-concatenated position per rank
     double *u = nullptr;         // dense rotation matrix staging
-    double *work = nullptr;      // cuSOLVER workspace
+    double *work = nullptr;      // cuSOLVER workspaces, one per side stream
     int64_t lwork = 0;
-    int *info = nullptr;
+    int *info = nullptr;         // one per side stream
+    static constexpr int NSIDE = 8;
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
     double *scal = nullptr;
     int *iscal = nullptr;
 };

@@ -278,17 +278,16 @@ __device__ int sturm_count(const double *alpha, const double *beta, int m, doubl
     return cnt;
 }
 
-// Eigenvalues theta[0..ne) of T_m by 64-way multisection (one 64-thread group
-// per eigenvalue), eigenvectors s by inverse iteration, residual estimates
-// beta_{m-1} |s_{m-1}| and the convergence flag.
-__global__ void __launch_bounds__(256) k_tridiag(const double *alpha, const double *beta, int m, int ne,
+// Eigenvalues theta[0..ne) of T_m by 32-way multisection, one warp per
+// eigenvalue (a round costs one Sturm count per lane; GB300's FP64 pipe is
+// narrow, so fewer concurrent counts and more rounds is the faster trade),
+// eigenvectors s by inverse iteration, residual estimates beta_{m-1} |s_{m-1}|
+// and the convergence flag.
+__global__ void __launch_bounds__(128) k_tridiag(const double *alpha, const double *beta, int m, int ne,
                                                  double tol, double *theta, double *resid, double *svec,
                                                  int sstride, int *flags, int final_pass) {
     __shared__ double lo_s, hi_s;
-    __shared__ double xs[4][65];
-    __shared__ int cs[4][65];
-    __shared__ double ab[4][2];
-    const int tid = threadIdx.x, grp = tid >> 6, g = tid & 63;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         double lo = 1e300, hi = -1e300;
         for (int i = 0; i < m; ++i) {
@@ -301,32 +300,26 @@ __global__ void __launch_bounds__(256) k_tridiag(const double *alpha, const doub
         hi_s = hi + pad;
     }
     __syncthreads();
-    for (int e0 = 0; e0 < ne; e0 += 4) {
-        const int e = e0 + grp;
-        const bool active = e < ne && e < m;
-        if (g == 0) { ab[grp][0] = lo_s; ab[grp][1] = hi_s; }
-        __syncthreads();
-        for (int round = 0; round < 12; ++round) {
-            double a = ab[grp][0], b = ab[grp][1];
-            bool done = !(b - a > 4e-16 * fmax(fabs(a), fabs(b)) + 1e-300);
-            if (active && !done) {
-                double x = a + (b - a) * (double)(g + 1) / 65.0;
-                xs[grp][g] = x;
-                cs[grp][g] = sturm_count(alpha, beta, m, x);
-            }
-            __syncthreads();
-            if (active && !done && g == 0) {
-                // first point whose count exceeds e brackets eigenvalue e
-                int t = 0;
-                while (t < 64 && cs[grp][t] <= e) ++t;
-                ab[grp][0] = (t == 0) ? a : xs[grp][t - 1];
-                ab[grp][1] = (t == 64) ? b : xs[grp][t];
-            }
-            __syncthreads();
+    const int e = warp;
+    if (e < ne && e < m) {
+        double a = lo_s, b = hi_s;
+        for (int round = 0; round < 24; ++round) {
+            if (!(b - a > 4e-16 * fmax(fabs(a), fabs(b)) + 1e-300)) break;
+            const double x = a + (b - a) * (double)(lane + 1) / 33.0;
+            const int cnt = sturm_count(alpha, beta, m, x);
+            const unsigned over = __ballot_sync(0xffffffffu, cnt > e);
+            // first point whose count exceeds e brackets eigenvalue e
+            const int t = over ? __ffs(over) - 1 : 32;
+            const double xt = __shfl_sync(0xffffffffu, x, t < 32 ? t : 31);
+            const double xp = __shfl_sync(0xffffffffu, x, t > 0 ? t - 1 : 0);
+            const double na = (t == 0) ? a : xp;
+            const double nb = (t == 32) ? b : xt;
+            a = na;
+            b = nb;
         }
-        if (active && g == 0) theta[e] = 0.5 * (ab[grp][0] + ab[grp][1]);
-        __syncthreads();
+        if (lane == 0) theta[e] = 0.5 * (a + b);
     }
+    __syncthreads();
     // inverse iteration, one thread per eigenvalue: (T - shift I) y = s, solved
     // by Gaussian elimination with partial pivoting (the LAPACK dgtsv scheme);
     // the factor bands live in the eigenvector's scratch row (stride 4*m+).
@@ -565,7 +558,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         m_done = j;
         const bool full = (m_done >= mmax) || (m_done >= n);
         ++c.launches;
-        k_tridiag<<<1, 256, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
+        k_tridiag<<<1, 128, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
                                      z.flags, full ? 1 : 0);
         NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
         NSS_CUDA_TRY(c, cudaStreamSynchronize(st));

@@ -110,28 +110,53 @@ __global__ void k_rank(const double *ev, int n, double *sorted, int *order) {
     }
 }
 
-// Truncation choice, truncation error and entropy of one side (one thread;
-// sequential sums in descending order as the reference's loops).
-__global__ void k_truncate(const double *sorted, int n, int mstates, int mblock, double thr,
-                           double *out_d /*trunc, entropy*/, int *out_i /*m_s*/) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    auto lam = [&](int i) { return sorted[i] < 0.0 ? 0.0 : sorted[i]; };
+// Truncation choice, truncation error and entropy of one side, one CTA of
+// 1024 threads: the degeneracy extension is a count over the tail, the sums
+// are block reductions (the reference sums sequentially; the orders differ by
+// rounding only).
+__global__ void __launch_bounds__(1024) k_truncate(const double *sorted, int n, int mstates, int mblock, double thr,
+                                                   double *out_d /*trunc, entropy*/, int *out_i /*m_s*/) {
+    __shared__ double red_s[32], red_e[32];
+    __shared__ int red_c[32];
+    __shared__ int ms_s;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int ms = min(mstates, min(mblock, n));
     if (ms < 1) ms = 1;
-    const double e_ = lam(ms - 1);
-    int ext = 0;
-    for (int i = ms; i < n; ++i) {
-        const double err = fabs(e_ - lam(i)) / e_;
-        if (err <= thr) ++ext;
+    const double e_ = sorted[ms - 1] < 0.0 ? 0.0 : sorted[ms - 1];
+    int cnt = 0;
+    for (int i = ms + tid; i < n; i += blockDim.x) {
+        const double li = sorted[i] < 0.0 ? 0.0 : sorted[i];
+        if (fabs(e_ - li) / e_ <= thr) ++cnt;
     }
-    ms += ext;
-    double s = 0.0;
-    for (int i = 0; i < ms; ++i) s += lam(i);
-    double ent = 0.0;
-    for (int i = 0; i < n; ++i) ent -= lam(i) * log(lam(i) + 1e-32);
-    out_d[0] = 1.0 - s;
-    out_d[1] = ent;
-    out_i[0] = ms;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) red_c[warp] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+        int t = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red_c[q];
+        ms_s = ms + t;
+    }
+    __syncthreads();
+    const int msf = ms_s;
+    double sk = 0.0, ent = 0.0;
+    for (int i = tid; i < n; i += blockDim.x) {
+        const double li = sorted[i] < 0.0 ? 0.0 : sorted[i];
+        if (i < msf) sk += li;
+        ent -= li * log(li + 1e-32);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sk += __shfl_xor_sync(0xffffffffu, sk, o);
+        ent += __shfl_xor_sync(0xffffffffu, ent, o);
+    }
+    if (lane == 0) { red_s[warp] = sk; red_e[warp] = ent; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += red_s[q]; b += red_e[q]; }
+        out_d[0] = 1.0 - a;
+        out_d[1] = b;
+        out_i[0] = msf;
+    }
 }
 
 // U[map_q[p], j] = evec_q[p][col(j)] ; kept_blk[j] = q  (column-major U)
@@ -167,6 +192,11 @@ void rdm_release(Ctx &c) {
     DevRdm &r = c.rdm;
     void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal};
     for (void *p : ptrs) ctx_free(c, p);
+    for (int i = 0; i < DevRdm::NSIDE; ++i) {
+        if (r.side[i]) cudaStreamDestroy(r.side[i]);
+        if (r.ev_join[i]) cudaEventDestroy(r.ev_join[i]);
+    }
+    if (r.ev_fork) cudaEventDestroy(r.ev_fork);
     r = DevRdm{};
 }
 
@@ -222,7 +252,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     if (!r.scal) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.scal, 8));
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.iscal, 8));
-        NSS_CUDA_TRY(c, ctx_alloc(c, &r.info, 1));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.info, DevRdm::NSIDE));
     }
     // small tables (allocated per call; freed at the end)
     RhoItem *d_items = nullptr;
@@ -263,17 +293,40 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     if (!r.work || r.lwork < lw) {
         ctx_free(c, r.work);
         r.work = nullptr;
-        NSS_CUDA_TRY(c, ctx_alloc(c, &r.work, (size_t)lw));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.work, (size_t)lw * DevRdm::NSIDE));
         r.lwork = lw;
     }
-    for (int q = 0; q < 2 * nsb; ++q) {
+    if (!r.ev_fork) {
+        NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
+        for (int i = 0; i < DevRdm::NSIDE; ++i) {
+            NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&r.side[i], cudaStreamNonBlocking));
+            NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
+        }
+    }
+    // The blocks are independent and each dsyevd is a chain of small kernels,
+    // so they run on NSIDE streams at once (largest first, round robin).
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
+    for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
+    std::vector<int> by_size(2 * nsb);
+    for (int q = 0; q < 2 * nsb; ++q) by_size[q] = q;
+    std::sort(by_size.begin(), by_size.end(), [&](int a, int b) { return dims[a] > dims[b]; });
+    for (int i = 0; i < 2 * nsb; ++i) {
+        const int q = by_size[i], sid = i % DevRdm::NSIDE;
         const int d = dims[q];
+        cusolverDnSetStream(h, r.side[sid]);
         if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, r.rho + rho_off[q], d,
-                             r.evals + ev_off[q], r.work, (int)r.lwork, r.info) != CUSOLVER_STATUS_SUCCESS) {
+                             r.evals + ev_off[q], r.work + (size_t)sid * r.lwork, (int)r.lwork, r.info + sid) !=
+            CUSOLVER_STATUS_SUCCESS) {
+            cusolverDnSetStream(h, st);
             cleanup();
             c.err = "nss_rdm: cusolverDnDsyevd failed";
             return NSS_ERR_CUDA;
         }
+    }
+    cusolverDnSetStream(h, st);
+    for (int i = 0; i < DevRdm::NSIDE; ++i) {
+        NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
+        NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
     }
     ++c.launches;
     k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
@@ -284,7 +337,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         ++c.launches;
         k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base);
         ++c.launches;
-        k_truncate<<<1, 32, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
+        k_truncate<<<1, 1024, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
                                      r.iscal + side);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());
