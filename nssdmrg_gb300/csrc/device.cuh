@@ -56,8 +56,11 @@ struct DevSb {
     int ntiles = 0;
     // FP32 copies for the mixed-precision path
     float *d_hl32 = nullptr, *d_hr32 = nullptr, *d_ab_val32 = nullptr;
-    int4 *d_tiles32 = nullptr;
+    int4 *d_tiles32 = nullptr;         // CUDA-core FP32 tiles (small sectors)
     int ntiles32 = 0;
+    int4 *d_tiles_tc = nullptr;        // tensor-core tiles (sectors with Dl >= TC_MIN_DL)
+    int ntiles_tc = 0;
+    int *d_tc_err = nullptr;           // set when a tensor-core wait ran out
 };
 
 // Device-side Lanczos state, kept resident between nss_eigh and nss_rdm.
@@ -134,6 +137,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d);
 void sb_release(Ctx &c);
 int hv_device(Ctx &c, const double *d_v, double *d_hv);
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv);
+int hv_device_tc(Ctx &c, const float *d_v, float *d_hv);
+// sectors with at least this many left states take the tensor-core kernel
+// in the mixed path (0 disables it: env NSS_TC=0)
+extern int g_tc_min_dl;
 
 // k_lanczos.cu
 int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,

@@ -9,7 +9,7 @@
 // 2^-21 relative accuracy, i.e. FP32-class H*psi.  Operands are staged by the
 // CTA's threads into shared memory in the no-swizzle K-major canonical
 // layout (8-row x 16-byte core matrices; LBO = next core along K = 128 B,
-// SBO = next 8-row group = 4 cores = 512 B for a 32-wide K chunk), one
+// SBO = next 8-row group = 8 cores = 1024 B for a 32-wide K chunk), one
 // thread issues the MMAs, tcgen05.commit signals an mbarrier, and after the
 // K loops the 4 warps read their 32 TMEM lanes each (tcgen05.ld 32x32b) and
 // add the A x B terms of the sector on the CUDA cores in FP32.
@@ -37,7 +37,7 @@ constexpr uint32_t MAX_SPIN = 1u << 24;
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-    // no swizzle, K-major: LBO = 128 B (core to core along K), SBO = 512 B
+    // no swizzle, K-major: LBO = 128 B (core to core along K), SBO = 1024 B
     uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
     d |= (uint64_t)(128 >> 4) << 16;
     d |= (uint64_t)((TC_K / 4) * 128 >> 4) << 32;
@@ -226,6 +226,22 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NCOLS));
+}
+
+int hv_device_tc(Ctx &c, const float *d_v, float *d_hv) {
+    DevSb &s = c.sb;
+    if (s.ntiles_tc == 0) return NSS_OK;
+    static bool attr_set = false;
+    if (!attr_set) {
+        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_hv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr_set = true;
+    }
+    k_hv_tc<<<s.ntiles_tc, TC_THREADS, TC_SMEM, c.stream>>>(
+        d_v, d_hv, s.d_tiles_tc, s.d_dls, s.d_drs, s.d_off, s.d_hl32, s.d_hl_off, s.d_hr32, s.d_hr_off,
+        s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32, s.d_tc_err);
+    c.launches += 1;
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    return NSS_OK;
 }
 
 }  // namespace nss

@@ -669,6 +669,14 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     cudaEventDestroy(e1);
     if (rc) return rc;
     if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
+    if (mixed && c.sb.d_tc_err) {
+        int tc_err = 0;
+        NSS_CUDA_TRY(c, cudaMemcpy(&tc_err, c.sb.d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (tc_err) {
+            c.err = "nss_eigh: a tensor-core pipeline wait timed out (results discarded)";
+            return NSS_ERR_CUDA;
+        }
+    }
     if (evals_host) NSS_CUDA_TRY(c, cudaMemcpy(evals_host, z.theta, ne * sizeof(double), cudaMemcpyDeviceToHost));
     c.last_ms_eigh = ms;
     c.last_numop = numop_;

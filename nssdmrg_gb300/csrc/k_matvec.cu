@@ -9,10 +9,16 @@
 #include "device.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 
 namespace nss {
+
+int g_tc_min_dl = [] {
+    const char *e = std::getenv("NSS_TC");
+    return (e && e[0] == '0') ? 0 : 64;
+}();
 
 void ctx_free(Ctx &c, void *p) {
     if (!p) return;
@@ -28,7 +34,7 @@ void sb_release(Ctx &c) {
     DevSb &s = c.sb;
     void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
                     s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
-                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32};
+                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err};
     for (void *p : ptrs) ctx_free(c, p);
     s = DevSb{};
 }
@@ -37,6 +43,7 @@ namespace {
 
 constexpr int TILE = 16;
 constexpr int TILE32 = 32;
+constexpr int TC_ROWS = 128, TC_COLS = 64;   // k_hv_tc tile
 
 template <class T>
 int upload_vec(Ctx &c, T **dst, const std::vector<T> &src) {
@@ -187,15 +194,24 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
 
     // FP32 copies for the mixed path, and its 32x32 tiles
     std::vector<float> hl32(hl.begin(), hl.end()), hr32(hr.begin(), hr.end()), val32(val.begin(), val.end());
-    std::vector<int4> tiles32;
-    for (int k = 0; k < s.nsb; ++k)
-        for (int r = 0; r < s.dls[k]; r += TILE32)
-            for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
+    std::vector<int4> tiles32, tiles_tc;
+    for (int k = 0; k < s.nsb; ++k) {
+        if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
+            for (int r = 0; r < s.dls[k]; r += TC_ROWS)
+                for (int cc = 0; cc < s.drs[k]; cc += TC_COLS) tiles_tc.push_back(make_int4(k, r, cc, 0));
+        } else {
+            for (int r = 0; r < s.dls[k]; r += TILE32)
+                for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
+        }
+    }
     s.ntiles32 = (int)tiles32.size();
+    s.ntiles_tc = (int)tiles_tc.size();
+    std::vector<int> tc_err(1, 0);
 
     int rc;
     if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
-        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_tiles32, tiles32)))
+        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_tiles32, tiles32)) ||
+        (rc = upload_vec(c, &s.d_tiles_tc, tiles_tc)) || (rc = upload_vec(c, &s.d_tc_err, tc_err)))
         return rc;
     if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
         (rc = upload_vec(c, &s.d_off, s.off)) || (rc = upload_vec(c, &s.d_hl_off, s.hl_off)) ||
@@ -376,12 +392,14 @@ int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv) {
         c.err = "nss_hv: no superblock uploaded";
         return NSS_ERR_STATE;
     }
-    k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
-                                                s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms,
-                                                s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32);
-    c.launches += 1;
-    NSS_CUDA_TRY(c, cudaGetLastError());
-    return NSS_OK;
+    if (s.ntiles32 > 0) {
+        k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
+                                                    s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms,
+                                                    s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32);
+        c.launches += 1;
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
+    return hv_device_tc(c, d_v, d_hv);
 }
 
 int hv_device(Ctx &c, const double *d_v, double *d_hv) {

@@ -184,3 +184,35 @@ def test_mixed_precision_energy_within_1e10(nss, name, neigen):
     assert np.linalg.norm(hv - ev[0] * vec[:, 0]) <= 1e-5 * abs(ev[0])
     res = s.sb_get_rdm(64, 0.1)
     assert abs(res.entropy[0] - z["entropy"][0]) <= 1e-5 * abs(z["entropy"][0])
+
+
+@pytest.fixture(scope="module")
+def c2_superblock(nss):
+    """Last infinite step of the Hubbard L=32, U=4, M=256 chain (the
+    benchmark superblock: N=65 900, sectors up to 120 x 120)."""
+    d = nss.DMRG(nss.MODEL_HUBBARD, 16, 256, u=4.0, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1)
+    d.prepare_last()
+    return d
+
+
+def test_fp32_and_tensor_core_products_match_fp64(nss, c2_superblock):
+    """The mixed path's product (tcgen05 3xTF32 tiles for sectors with
+    Dl >= 64, FP32 CUDA-core tiles for the rest) against the FP64 product on
+    the same superblock: FP32-class accuracy, 2e-6 of the largest entry."""
+    import torch
+    sb = c2_superblock.sb
+    n = sb.n
+    g = torch.Generator(device="cuda").manual_seed(3)
+    v64 = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    v32 = v64.float()
+    h64 = torch.empty_like(v64)
+    h32 = torch.empty_like(v32)
+    sb.hv_device(v64.data_ptr(), h64.data_ptr())
+    sb.hv_device_f32(v32.data_ptr(), h32.data_ptr())
+    torch.cuda.synchronize()
+    err = (h32.double() - h64).abs().max().item() / h64.abs().max().item()
+    assert err <= 2e-6, err
+    # the mixed solve on this superblock: |dE|/|E| <= 1e-10 against FP64
+    e64, _, _ = sb.sb_diag(neigen=1, tol=1e-12, want_vectors=False)
+    emx, _, _ = sb.sb_diag(neigen=1, tol=1e-12, want_vectors=False, precision=nss.NSS_PREC_MIXED)
+    assert abs(emx[0] - e64[0]) <= 1e-10 * abs(e64[0])
