@@ -67,7 +67,8 @@ struct DevSb {
 struct DevLanczos {
     int cap = 0;                 // allocated Krylov vectors
     int64_t n = 0;
-    double *V = nullptr;         // [cap][n]
+    double *V = nullptr;         // [cap+1][n] when full64, else one n-vector of scratch
+    bool full64 = false;         // V holds a whole FP64 Krylov basis
     double *w = nullptr;         // [n]
     float *V32 = nullptr;        // [cap][n] mixed-precision basis (lazily)
     float *w32 = nullptr;        // [n]
@@ -141,6 +142,9 @@ int hv_device_tc(Ctx &c, const float *d_v, float *d_hv);
 // sectors with at least this many left states take the tensor-core kernel
 // in the mixed path (0 disables it: env NSS_TC=0)
 extern int g_tc_min_dl;
+
+// k_noalloc.cu
+int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy);
 
 // k_lanczos.cu
 int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,

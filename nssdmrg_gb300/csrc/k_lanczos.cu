@@ -464,7 +464,9 @@ inline int svec_stride(int cap) { return 4 * (cap + 1); }
 
 int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     DevLanczos &z = c.lz;
-    if (z.V && z.n == n && z.cap >= cap && (!mixed || z.V32)) return NSS_OK;
+    // reuse only buffers shaped for this mode: the FP64 method needs a whole
+    // FP64 basis in V, the mixed one an FP32 basis in V32
+    if (z.V && z.n == n && z.cap >= cap && (mixed ? (z.V32 != nullptr) : z.full64)) return NSS_OK;
     lanczos_release(c);
     z.n = n;
     z.cap = cap;
@@ -472,8 +474,10 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V32, (size_t)(cap + 1) * n));
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.w32, (size_t)n));
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)n));   // FP64 refinement scratch
+        z.full64 = false;
     } else {
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)(cap + 1) * n));
+        z.full64 = true;
     }
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.w, (size_t)n));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));

@@ -216,3 +216,17 @@ def test_fp32_and_tensor_core_products_match_fp64(nss, c2_superblock):
     e64, _, _ = sb.sb_diag(neigen=1, tol=1e-12, want_vectors=False)
     emx, _, _ = sb.sb_diag(neigen=1, tol=1e-12, want_vectors=False, precision=nss.NSS_PREC_MIXED)
     assert abs(emx[0] - e64[0]) <= 1e-10 * abs(e64[0])
+
+
+def test_precision_modes_alternate_on_one_context(nss):
+    """FP64 and mixed solves share a context's buffers; switching back and
+    forth must re-shape them (the FP64 basis is larger than the mixed
+    path's FP64 scratch)."""
+    z = load_npz("c2_small.npz")
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    ref = z["oracle_gs_energy"][0]
+    for prec in (nss.NSS_PREC_MIXED, nss.NSS_PREC_FP64, nss.NSS_PREC_MIXED, nss.NSS_PREC_FP64):
+        ev, _, _ = s.sb_diag(neigen=1, tol=1e-12, want_vectors=False, precision=prec)
+        assert abs(ev[0] - ref) <= 1e-10 * abs(ref)
