@@ -154,6 +154,18 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
             int32_t *kept_left, int32_t *kept_right,
             double *u_left, double *u_right);
 
+/* Energy <psi|H|psi> / <psi|psi> of a device vector d_psi (length n =
+ * nss_sb_dim) on the uploaded superblock, written to *energy (host), without
+ * allocating any memory.  No counterpart in the reference: it is for callers
+ * that cannot allocate device memory when they need an energy (a host code
+ * whose device heap belongs to another allocator, a context whose HBM budget
+ * is spent, code about to be captured into a CUDA graph).  Its scratch is a
+ * static device array of 32768 16x16-tile partial sums (512 KiB per GPU that
+ * loads the library, held until exit); larger superblocks are rejected with
+ * NSS_ERR_INVALID.  The first call on a device looks up that array and must
+ * come before any stream capture; calls that overlap on the GPU race. */
+int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy);
+
 /* ---------------------------------------------------------------------------
  * Block-level superblock setup (the enumeration and operator-pool build of
  * sb_get_states / sb_build_dims / Setup_SuperBlock_{Spin,Fermion}_Direct,

@@ -115,6 +115,7 @@ def lib():
         "nss_hv": (C.c_int, [P, I64, P, P]),
         "nss_hv_device": (C.c_int, [P, I64, P, P]),
         "nss_hv_device_f32": (C.c_int, [P, I64, P, P]),
+        "nss_sb_energy_noalloc": (C.c_int, [P, I64, P, C.POINTER(D)]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
@@ -324,6 +325,13 @@ class Superblock:
     def hv_device(self, d_v: int, d_hv: int):
         """H*v on device pointers (e.g. torch tensors' data_ptr())."""
         self._check(lib().nss_hv_device(self._ctx, self.n, C.c_void_p(d_v), C.c_void_p(d_hv)))
+
+    def energy_noalloc(self, d_psi: int) -> float:
+        """<psi|H|psi>/<psi|psi> of a device vector, allocating nothing (for
+        callers that cannot allocate device memory at that point)."""
+        e = C.c_double()
+        self._check(lib().nss_sb_energy_noalloc(self._ctx, self.n, C.c_void_p(d_psi), C.byref(e)))
+        return e.value
 
     def hv_device_f32(self, d_v: int, d_hv: int):
         """The mixed path's FP32 H*v on device pointers."""

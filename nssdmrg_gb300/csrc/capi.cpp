@@ -174,6 +174,12 @@ int nss_hv_device_f32(nss_ctx *ctx, int64_t n, const float *d_v, float *d_hv) {
     return nss::hv_device_fp32(ctx->c, d_v, d_hv);
 }
 
+int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    cudaSetDevice(ctx->c.device);
+    return nss::sb_energy_noalloc(ctx->c, n, d_psi, energy);
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
