@@ -56,6 +56,8 @@ struct DevSb {
     int ntiles = 0;
     // FP32 copies for the mixed-precision path
     float *d_hl32 = nullptr, *d_hr32 = nullptr, *d_ab_val32 = nullptr;
+    int *d_ab_rowptr32 = nullptr, *d_ab_col32 = nullptr;   // pruned FP32 A/B pool
+    DevTerm *d_terms32 = nullptr;                            // terms indexing that pool
     int4 *d_tiles32 = nullptr;         // CUDA-core FP32 tiles (small sectors)
     int ntiles32 = 0;
     int4 *d_tiles_tc = nullptr;        // tensor-core tiles (sectors with Dl >= TC_MIN_DL)

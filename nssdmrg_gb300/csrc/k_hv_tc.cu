@@ -83,30 +83,50 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 // Stage one K chunk: A rows [row0, row0+128) x [j0, j0+32) and B rows (the
 // output columns) [col0, col0+BN) x [j0, j0+32), split into TF32 hi/lo.
 // phase 0: A = HL[il][j], B[n][j] = W[j][ir];  phase 1: A = W[il][j], B = HR[ir][j]
+// All of a thread's global loads are issued before any conversion so that
+// they are in flight together.
 __device__ __forceinline__ void tc_stage(float *st, int phase, const float *W, const float *H, int dl, int dr,
                                          int row0, int col0, int j0) {
     float *ahi = st, *alo = st + A_FLOATS, *bhi = st + 2 * A_FLOATS, *blo = bhi + B_FLOATS;
     const int kmax = phase == 0 ? dl : dr;
+    constexpr int NA = A_FLOATS / TC_THREADS, NB = B_FLOATS / TC_THREADS;
+    float xa[NA], xb[NB];
     // lane -> (row & 7, k & 3) so a warp writes 128 contiguous bytes
-    for (int e = threadIdx.x; e < A_FLOATS; e += TC_THREADS) {
+#pragma unroll
+    for (int it = 0; it < NA; ++it) {
+        const int e = threadIdx.x + it * TC_THREADS;
         const int lane = e & 31, grp = e >> 5;             // grp = (row>>3)*(TC_K/4) + (k>>2)
         const int row = (grp / (TC_K / 4)) * 8 + (lane >> 2), k = (grp % (TC_K / 4)) * 4 + (lane & 3);
         const int gi = row0 + row, gj = j0 + k;
-        float x = 0.f;
-        if (gi < dl && gj < kmax) x = phase == 0 ? H[(int64_t)gi * dl + gj] : W[(int64_t)gi * dr + gj];
-        const float h = tf32_round(x);
-        ahi[canon(row, k)] = h;
-        alo[canon(row, k)] = x - h;
+        xa[it] = 0.f;
+        if (gi < dl && gj < kmax) xa[it] = phase == 0 ? H[(int64_t)gi * dl + gj] : W[(int64_t)gi * dr + gj];
     }
-    for (int e = threadIdx.x; e < B_FLOATS; e += TC_THREADS) {
+#pragma unroll
+    for (int it = 0; it < NB; ++it) {
+        const int e = threadIdx.x + it * TC_THREADS;
         const int lane = e & 31, grp = e >> 5;
         const int n = (grp / (TC_K / 4)) * 8 + (lane >> 2), k = (grp % (TC_K / 4)) * 4 + (lane & 3);
         const int gc = col0 + n, gj = j0 + k;
-        float x = 0.f;
-        if (gc < dr && gj < kmax) x = phase == 0 ? W[(int64_t)gj * dr + gc] : H[(int64_t)gc * dr + gj];
-        const float h = tf32_round(x);
+        xb[it] = 0.f;
+        if (gc < dr && gj < kmax) xb[it] = phase == 0 ? W[(int64_t)gj * dr + gc] : H[(int64_t)gc * dr + gj];
+    }
+#pragma unroll
+    for (int it = 0; it < NA; ++it) {
+        const int e = threadIdx.x + it * TC_THREADS;
+        const int lane = e & 31, grp = e >> 5;
+        const int row = (grp / (TC_K / 4)) * 8 + (lane >> 2), k = (grp % (TC_K / 4)) * 4 + (lane & 3);
+        const float h = tf32_round(xa[it]);
+        ahi[canon(row, k)] = h;
+        alo[canon(row, k)] = xa[it] - h;
+    }
+#pragma unroll
+    for (int it = 0; it < NB; ++it) {
+        const int e = threadIdx.x + it * TC_THREADS;
+        const int lane = e & 31, grp = e >> 5;
+        const int n = (grp / (TC_K / 4)) * 8 + (lane >> 2), k = (grp % (TC_K / 4)) * 4 + (lane & 3);
+        const float h = tf32_round(xb[it]);
         bhi[canon(n, k)] = h;
-        blo[canon(n, k)] = x - h;
+        blo[canon(n, k)] = xb[it] - h;
     }
 }
 
@@ -190,8 +210,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // Epilogue, in two passes.  (1) Each warp moves its 32 TMEM lanes (rows)
+    // into shared memory (row stride 65 floats: conflict-free), the MMAs being
+    // complete so the stage buffers are free.  (2) Lanes run along columns:
+    // the A x B gathers W_q[aj][bj(ir)] and the stores to H psi are coalesced.
     const int w = tid >> 5, lane = tid & 31;
-    const int il = row0 + 32 * w + lane;
+    float *Dsm = stage[0];                          // 128 x 65 floats < one stage
     if (ok_s) {
         for (int c0 = 0; c0 < TC_BN; c0 += 8) {
             uint32_t r[8];
@@ -200,26 +224,34 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
                            "=r"(r[7])
                          : "r"(tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)c0));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (il < dl) {
-                for (int j = 0; j < 8; ++j) {
-                    const int ir = col0 + c0 + j;
-                    if (ir >= dr) continue;
-                    float a = __uint_as_float(r[j]);
-                    for (int ti = term_ptr[k]; ti < term_ptr[k + 1]; ++ti) {
-                        const DevTerm tm = terms[ti];
-                        const float *Wq = v + off[tm.in_sec];
-                        const int drq = drs[tm.in_sec];
-                        const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
-                        for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
-                            const int aj = ab_col[ja];
-                            float cb = 0.f;
-                            for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
-                                cb = fmaf(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
-                            a = fmaf(ab_val[ja], cb, a);
-                        }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) Dsm[(32 * w + lane) * (TC_BN + 1) + c0 + j] = __uint_as_float(r[j]);
+        }
+    }
+    __syncthreads();
+    if (ok_s) {
+        const int t0 = term_ptr[k], t1 = term_ptr[k + 1];
+        for (int rr = w; rr < TC_M; rr += TC_THREADS / 32) {
+            const int il = row0 + rr;
+            if (il >= dl) break;
+            for (int cc = lane; cc < TC_BN; cc += 32) {
+                const int ir = col0 + cc;
+                if (ir >= dr) continue;
+                float a = Dsm[rr * (TC_BN + 1) + cc];
+                for (int ti = t0; ti < t1; ++ti) {
+                    const DevTerm tm = terms[ti];
+                    const float *Wq = v + off[tm.in_sec];
+                    const int drq = drs[tm.in_sec];
+                    const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
+                    for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
+                        const int aj = ab_col[ja];
+                        float cb = 0.f;
+                        for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
+                            cb = fmaf(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
+                        a = fmaf(ab_val[ja], cb, a);
                     }
-                    hv[off[k] + (int64_t)il * dr + ir] = a;
                 }
+                hv[off[k] + (int64_t)il * dr + ir] = a;
             }
         }
     }
@@ -238,7 +270,7 @@ int hv_device_tc(Ctx &c, const float *d_v, float *d_hv) {
     }
     k_hv_tc<<<s.ntiles_tc, TC_THREADS, TC_SMEM, c.stream>>>(
         d_v, d_hv, s.d_tiles_tc, s.d_dls, s.d_drs, s.d_off, s.d_hl32, s.d_hl_off, s.d_hr32, s.d_hr_off,
-        s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32, s.d_tc_err);
+        s.d_term_ptr, s.d_terms32, s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, s.d_tc_err);
     c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;

@@ -239,7 +239,6 @@ __global__ void k_next(T *__restrict__ vnext, const T *__restrict__ w, int64_t n
     const T inv = (T)(1.0 / b);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         vnext[i] = w[i] * inv;
-    if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_M] = j + 2;
 }
 
 // x <- x / ||x|| (one CTA per launch is enough for start vectors);
@@ -283,9 +282,16 @@ __device__ int sturm_count(const double *alpha, const double *beta, int m, doubl
 // narrow, so fewer concurrent counts and more rounds is the faster trade),
 // eigenvectors s by inverse iteration, residual estimates beta_{m-1} |s_{m-1}|
 // and the convergence flag.
-__global__ void __launch_bounds__(128) k_tridiag(const double *alpha, const double *beta, int m, int ne,
+// m_arg is the basis size the chunk would reach; after a breakdown the
+// kernel uses the breakdown step instead, and once a solve has converged
+// (stop flag 1) later calls leave theta and s untouched.  It records the m it
+// used (F_M) and sets the stop flag: 1 converged or Krylov space exhausted
+// (m = n), 3 iteration cap reached.
+__global__ void __launch_bounds__(128) k_tridiag(const double *alpha, const double *beta, int m_arg, int ne,
                                                  double tol, double *theta, double *resid, double *svec,
-                                                 int sstride, int *flags, int final_pass) {
+                                                 int sstride, int *flags, int mmax, int64_t nvec) {
+    if (flags[F_STOP] == 1 || flags[F_STOP] == 3) return;
+    const int m = (flags[F_STOP] == 2) ? flags[F_BREAK] : m_arg;
     __shared__ double lo_s, hi_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
@@ -381,7 +387,9 @@ __global__ void __launch_bounds__(128) k_tridiag(const double *alpha, const doub
         for (int e = 0; e < ne && e < m; ++e)
             if (resid[e] <= tol * fmax(fabs(theta[e]), 1e-300)) ++conv;
         flags[F_CONV] = conv;
-        if (!final_pass && conv >= ne) flags[F_STOP] = 1;
+        flags[F_M] = m;
+        if (conv >= min(ne, m) || (int64_t)m >= nvec) flags[F_STOP] = 1;
+        else if (m >= mmax) flags[F_STOP] = 3;
     }
 }
 
@@ -491,7 +499,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.resid, 8));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.svec, (size_t)4 * svec_stride(cap)));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.flags, F_NFLAGS));
-    NSS_CUDA_TRY(c, cudaMallocHost((void **)&z.h_flags, F_NFLAGS * sizeof(int)));
+    NSS_CUDA_TRY(c, cudaMallocHost((void **)&z.h_flags, 2 * F_NFLAGS * sizeof(int)));
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.counter, 0, 4 * sizeof(unsigned), c.stream));
     return NSS_OK;
 }
@@ -523,7 +531,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
     ++c.launches;
     k_normalize<T><<<1, 1024, 0, st>>>(V, n);
-    int j = 0, m_done = 1, numop_ = 0, rc = NSS_OK;
+    int m_done = 1, numop_ = 0, rc = NSS_OK;
     bool converged = false;
     const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
     const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
@@ -531,12 +539,19 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         cudaFuncSetAttribute(k_dots<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
     if (upd_smem > 48 * 1024)
         cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
-    while (!converged) {
-        const int jend = std::min(mmax, j + CHECK);
-        for (int jj = j; jj < jend; ++jj) {
+    // Chunks of CHECK iterations, each followed by the convergence test and
+    // a copy of the flags into one of two pinned slots; one chunk runs ahead
+    // of the host's read of the previous one, so the stream never idles.
+    // Kernels of a chunk enqueued after convergence exit at once (stop flag).
+    cudaEvent_t evs[2];
+    cudaEventCreateWithFlags(&evs[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
+    auto enqueue_chunk = [&](int j0, int slot) -> int {
+        const int jend = std::min(mmax, j0 + CHECK);
+        for (int jj = j0; jj < jend; ++jj) {
             const int m = jj + 1;
-            rc = hv_t<T>(c, V + (int64_t)jj * n, w);
-            if (rc) return rc;
+            int r2 = hv_t<T>(c, V + (int64_t)jj * n, w);
+            if (r2) return -1;
             c.launches += 5;
             k_alpha<T><<<NBLK, 256, 0, st>>>(V + (int64_t)jj * n, w, n, z.part, z.scal, z.counter, z.flags);
             k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m, w, n, z.part, h1, z.scal, z.counter, z.flags, 0, 1,
@@ -552,25 +567,29 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
                 k_next<T><<<vb, 256, 0, st>>>(V + (int64_t)m * n, w, n, z.flags, z.alpha, z.beta, jj);
             }
         }
-        NSS_CUDA_TRY(c, cudaGetLastError());
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
-        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-        // iterations that ran: up to the breakdown step, or the whole chunk
-        const int ran = z.h_flags[F_STOP] == 2 ? z.h_flags[F_BREAK] : jend;
-        numop_ += ran - j;
-        j = ran;
-        m_done = j;
-        const bool full = (m_done >= mmax) || (m_done >= n);
         ++c.launches;
-        k_tridiag<<<1, 128, 0, st>>>(z.alpha, z.beta, m_done, neigen, tol, z.theta, z.resid, z.svec, sstride,
-                                     z.flags, full ? 1 : 0);
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.h_flags, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st));
-        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-        const int conv = z.h_flags[F_CONV];
-        if (conv >= neigen || m_done >= n) { converged = true; break; }
-        if (m_done >= mmax) break;
-        if (z.h_flags[F_STOP] == 2) {
-            // invariant subspace: continue from a random vector orthogonal to V
+        k_tridiag<<<1, 128, 0, st>>>(z.alpha, z.beta, jend, neigen, tol, z.theta, z.resid, z.svec, sstride,
+                                     z.flags, mmax, n);
+        cudaMemcpyAsync(z.h_flags + slot * F_NFLAGS, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(evs[slot], st);
+        return jend;
+    };
+    int slot = 0;
+    int pend_end = enqueue_chunk(0, slot);
+    bool capped = false;
+    while (pend_end >= 0) {
+        const int next_end = (pend_end < mmax) ? enqueue_chunk(pend_end, slot ^ 1) : -2;
+        if (next_end == -1) { rc = NSS_ERR_CUDA; break; }
+        cudaError_t ce = cudaEventSynchronize(evs[slot]);
+        if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); rc = NSS_ERR_CUDA; break; }
+        const int *f = z.h_flags + slot * F_NFLAGS;
+        m_done = f[F_M];
+        if (f[F_STOP] == 1) { converged = true; break; }
+        if (f[F_STOP] == 3) { capped = true; break; }
+        if (f[F_STOP] == 2) {
+            // invariant subspace without convergence: continue from a random
+            // vector orthogonal to V (the chunk run ahead has already exited)
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
             ++restarts;
             T *vn = V + (int64_t)m_done * n;
             ++c.launches;
@@ -588,8 +607,20 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             k_normalize<T><<<1, 1024, 0, st>>>(vn, n);
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+            slot = 0;
+            pend_end = enqueue_chunk(m_done, slot);
+            continue;
         }
+        if (next_end < 0) { capped = true; break; }
+        slot ^= 1;
+        pend_end = next_end;
     }
+    cudaStreamSynchronize(st);
+    cudaEventDestroy(evs[0]);
+    cudaEventDestroy(evs[1]);
+    if (rc) return rc;
+    (void)capped;
+    numop_ = m_done;
     *numop_out = numop_;
     *m_out = m_done;
     if (!converged) {

@@ -9,6 +9,7 @@
 #include "device.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -34,7 +35,8 @@ void sb_release(Ctx &c) {
     DevSb &s = c.sb;
     void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
                     s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
-                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err};
+                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err,
+                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32};
     for (void *p : ptrs) ctx_free(c, p);
     s = DevSb{};
 }
@@ -192,8 +194,36 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
             for (int cc = 0; cc < s.drs[k]; cc += TILE) tiles.push_back(make_int4(k, r, cc, 0));
     s.ntiles = (int)tiles.size();
 
-    // FP32 copies for the mixed path, and its 32x32 tiles
-    std::vector<float> hl32(hl.begin(), hl.end()), hr32(hr.begin(), hr.end()), val32(val.begin(), val.end());
+    // FP32 copies for the mixed path, and its 32x32 tiles.  The FP32 A/B
+    // pool drops entries below 1e-12 of the largest entry of their matrix:
+    // the renormalised sign operator P carries rounding-level off-diagonal
+    // entries (up to 33 per row at m=256) whose contribution (~1e-17 of the
+    // result) is far below FP32 rounding, while each of them costs a gather.
+    // The FP64 pool keeps every entry, as the reference does.
+    std::vector<float> hl32(hl.begin(), hl.end()), hr32(hr.begin(), hr.end());
+    std::vector<int> rowptr32, col32;
+    std::vector<float> val32;
+    std::vector<DevTerm> terms32 = s.terms;
+    for (DevTerm &t : terms32) {
+        for (int which = 0; which < 2; ++which) {
+            const int64_t rp = which == 0 ? t.a_rp : t.b_rp;
+            const int nrow = which == 0 ? t.a_nrow : t.b_nrow;
+            double mx = 0.0;
+            for (int jj = rowptr[rp]; jj < rowptr[rp + nrow]; ++jj) mx = std::max(mx, std::fabs(val[jj]));
+            const int64_t at = (int64_t)rowptr32.size();
+            rowptr32.push_back((int)col32.size());
+            for (int i = 0; i < nrow; ++i) {
+                for (int jj = rowptr[rp + i]; jj < rowptr[rp + i + 1]; ++jj)
+                    if (std::fabs(val[jj]) > 1e-12 * mx) {
+                        col32.push_back(col[jj]);
+                        val32.push_back((float)val[jj]);
+                    }
+                rowptr32.push_back((int)col32.size());
+            }
+            if (which == 0) t.a_rp = at;
+            else t.b_rp = at;
+        }
+    }
     std::vector<int4> tiles32, tiles_tc;
     for (int k = 0; k < s.nsb; ++k) {
         if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
@@ -210,7 +240,9 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
 
     int rc;
     if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
-        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_tiles32, tiles32)) ||
+        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_ab_rowptr32, rowptr32)) ||
+        (rc = upload_vec(c, &s.d_ab_col32, col32)) || (rc = upload_vec(c, &s.d_terms32, terms32)) ||
+        (rc = upload_vec(c, &s.d_tiles32, tiles32)) ||
         (rc = upload_vec(c, &s.d_tiles_tc, tiles_tc)) || (rc = upload_vec(c, &s.d_tc_err, tc_err)))
         return rc;
     if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
@@ -394,8 +426,8 @@ int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv) {
     }
     if (s.ntiles32 > 0) {
         k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
-                                                    s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms,
-                                                    s.d_ab_rowptr, s.d_ab_col, s.d_ab_val32);
+                                                    s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms32,
+                                                    s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32);
         c.launches += 1;
         NSS_CUDA_TRY(c, cudaGetLastError());
     }
