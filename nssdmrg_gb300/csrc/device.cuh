@@ -138,9 +138,10 @@ void ctx_free(Ctx &c, void *p);
 // k_matvec.cu
 int sb_upload(Ctx &c, const nss_sb_desc *d);
 void sb_release(Ctx &c);
-int hv_device(Ctx &c, const double *d_v, double *d_hv);
-int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv);
-int hv_device_tc(Ctx &c, const float *d_v, float *d_hv);
+// `stop` (may be null): a device flag; the kernels return at once when set
+int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop = nullptr);
+int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
+int hv_device_tc(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
 // sectors with at least this many left states take the tensor-core kernel
 // in the mixed path (0 disables it: env NSS_TC=0)
 extern int g_tc_min_dl;

@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     const float *__restrict__ hrp, const int64_t *__restrict__ hr_off,
     const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
     const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val,
-    int *err) {
+    int *err, const int *stop) {
+    if (stop && *stop) return;   // before any TMEM allocation: uniform exit
     extern __shared__ __align__(1024) uint8_t smem[];
     float *stage[2] = {(float *)smem, (float *)smem + STAGE_FLOATS};
     __shared__ __align__(8) uint64_t mbar[2];
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_NCOLS));
 }
 
-int hv_device_tc(Ctx &c, const float *d_v, float *d_hv) {
+int hv_device_tc(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
     DevSb &s = c.sb;
     if (s.ntiles_tc == 0) return NSS_OK;
     static bool attr_set = false;
@@ -270,7 +271,7 @@ int hv_device_tc(Ctx &c, const float *d_v, float *d_hv) {
     }
     k_hv_tc<<<s.ntiles_tc, TC_THREADS, TC_SMEM, c.stream>>>(
         d_v, d_hv, s.d_tiles_tc, s.d_dls, s.d_drs, s.d_off, s.d_hl32, s.d_hl_off, s.d_hr32, s.d_hr_off,
-        s.d_term_ptr, s.d_terms32, s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, s.d_tc_err);
+        s.d_term_ptr, s.d_terms32, s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, s.d_tc_err, stop);
     c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;

@@ -505,11 +505,11 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
 }
 
 template <class T>
-int hv_t(Ctx &c, const T *v, T *hv);
+int hv_t(Ctx &c, const T *v, T *hv, const int *stop);
 template <>
-int hv_t<double>(Ctx &c, const double *v, double *hv) { return hv_device(c, v, hv); }
+int hv_t<double>(Ctx &c, const double *v, double *hv, const int *stop) { return hv_device(c, v, hv, stop); }
 template <>
-int hv_t<float>(Ctx &c, const float *v, float *hv) { return hv_device_fp32(c, v, hv); }
+int hv_t<float>(Ctx &c, const float *v, float *hv, const int *stop) { return hv_device_fp32(c, v, hv, stop); }
 
 // The Lanczos iterations on a basis of type T; leaves theta (Ritz values),
 // svec (their T-eigenvectors) and the Ritz vectors (FP64) in c.lz.
@@ -550,7 +550,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         const int jend = std::min(mmax, j0 + CHECK);
         for (int jj = j0; jj < jend; ++jj) {
             const int m = jj + 1;
-            int r2 = hv_t<T>(c, V + (int64_t)jj * n, w);
+            int r2 = hv_t<T>(c, V + (int64_t)jj * n, w, z.flags + F_STOP);
             if (r2) return -1;
             c.launches += 5;
             k_alpha<T><<<NBLK, 256, 0, st>>>(V + (int64_t)jj * n, w, n, z.part, z.scal, z.counter, z.flags);

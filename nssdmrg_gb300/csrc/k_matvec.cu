@@ -268,7 +268,9 @@ __global__ void __launch_bounds__(256) k_hv_fp64(
     const double *__restrict__ hlp, const int64_t *__restrict__ hl_off,
     const double *__restrict__ hrp, const int64_t *__restrict__ hr_off,
     const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
-    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const double *__restrict__ ab_val) {
+    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const double *__restrict__ ab_val,
+    const int *stop) {
+    if (stop && *stop) return;   // the Lanczos loop has already finished
     __shared__ double sa[TILE][33];
     __shared__ double sb[32][TILE + 1];
     const int4 t = tiles[blockIdx.x];
@@ -344,7 +346,9 @@ __global__ void __launch_bounds__(256) k_hv_fp32(
     const float *__restrict__ hlp, const int64_t *__restrict__ hl_off,
     const float *__restrict__ hrp, const int64_t *__restrict__ hr_off,
     const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
-    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val) {
+    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val,
+    const int *stop) {
+    if (stop && *stop) return;   // the Lanczos loop has already finished
     __shared__ float sa[TILE32][33];
     __shared__ float sb[32][TILE32 + 1];
     const int4 t = tiles[blockIdx.x];
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(256) k_hv_fp32(
         }
 }
 
-int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv) {
+int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
     DevSb &s = c.sb;
     if (!s.valid) {
         c.err = "nss_hv: no superblock uploaded";
@@ -427,14 +431,14 @@ int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv) {
     if (s.ntiles32 > 0) {
         k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
                                                     s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms32,
-                                                    s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32);
+                                                    s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, stop);
         c.launches += 1;
         NSS_CUDA_TRY(c, cudaGetLastError());
     }
-    return hv_device_tc(c, d_v, d_hv);
+    return hv_device_tc(c, d_v, d_hv, stop);
 }
 
-int hv_device(Ctx &c, const double *d_v, double *d_hv) {
+int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop) {
     DevSb &s = c.sb;
     if (!s.valid) {
         c.err = "nss_hv: no superblock uploaded";
@@ -442,7 +446,7 @@ int hv_device(Ctx &c, const double *d_v, double *d_hv) {
     }
     k_hv_fp64<<<s.ntiles, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles, s.d_dls, s.d_drs, s.d_off, s.d_hl,
                                               s.d_hl_off, s.d_hr, s.d_hr_off, s.d_term_ptr, s.d_terms,
-                                              s.d_ab_rowptr, s.d_ab_col, s.d_ab_val);
+                                              s.d_ab_rowptr, s.d_ab_col, s.d_ab_val, stop);
     c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;
