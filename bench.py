@@ -188,9 +188,11 @@ def run_gpu(args):
     ext = torch.cuda.ExternalStream(sb.stream)
     flush = torch.empty(int(512 * 2**20) // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    def solve(seed, p):
+    def solve(seed, p, mid=None):
         ev, _, numop = sb.sb_diag(neigen=1, nitermax=WORKLOAD["lanc_niter"], tol=WORKLOAD["lanc_tolerance"],
                                   seed=seed, precision=p, want_vectors=False)
+        if mid is not None:
+            mid.record(ext)
         res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=False)
         return ev, numop, res
 
@@ -201,19 +203,21 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
         l0 = sb.launches
-        times, numops, energies, ents = [], [], [], []
+        times, numops, energies, ents, t_eigh = [], [], [], [], []
         torch.cuda.nvtx.range_push("bench_timed")
         with Clocks(local, enabled=sample_clocks) as clk:
             for s in range(steps):
                 flush.zero_()                      # evict L2 between timed steps
                 torch.cuda.synchronize()
                 e0 = torch.cuda.Event(enable_timing=True)
+                em = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(ext)
-                ev, numop, res = solve(1000 + s, p)
+                ev, numop, res = solve(1000 + s, p, em)
                 e1.record(ext)
                 e1.synchronize()
                 times.append(e0.elapsed_time(e1))
+                t_eigh.append(e0.elapsed_time(em))
                 numops.append(numop)
                 energies.append(float(ev[0]))
                 ents.append(res.entropy[0])
@@ -228,7 +232,8 @@ def run_gpu(args):
         return {"t_total": t_total, "numops": numops, "energies": energies, "entropy": ents,
                 "launches": sb.launches - l0, "clocks": clk.summary(),
                 "value": f_hv * sum(numops) * world / (t_total / 1e3) / 1e12,
-                "ms_per_step": t_total / steps, "solves_per_s": 1e3 * steps * world / t_total}
+                "ms_per_step": t_total / steps, "solves_per_s": 1e3 * steps * world / t_total,
+                "ms_eigh": statistics.mean(t_eigh), "ms_rdm": (t_total - sum(t_eigh)) / steps}
 
     other = nss.NSS_PREC_FP64 if prec == nss.NSS_PREC_MIXED else nss.NSS_PREC_MIXED
     head = time_path(prec, args.steps, not args.profile)
@@ -267,6 +272,7 @@ def run_gpu(args):
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile_run": True, "ms_per_step": head["ms_per_step"],
+                              "ms_eigensolve": head["ms_eigh"], "ms_rdm": head["ms_rdm"],
                               "numop_mean": statistics.mean(head["numops"]), "ms_per_hv": t_hv * 1e3}))
         return None
 
@@ -319,9 +325,11 @@ def run_gpu(args):
                            l2="flushed between timed steps (512 MiB write)",
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
             "solves_per_s": head["solves_per_s"],
+            "ms_eigensolve": head["ms_eigh"], "ms_rdm": head["ms_rdm"],
             "numop_mean": statistics.mean(numops[:args.steps]),
             ("fp64" if mixed else "mixed"): {"value": comp["value"], "ms_per_step": comp["ms_per_step"],
                                              "solves_per_s": comp["solves_per_s"],
+                                             "ms_eigensolve": comp["ms_eigh"], "ms_rdm": comp["ms_rdm"],
                                              "numop_mean": statistics.mean(comp["numops"]),
                                              "energy_per_site": comp["energies"][-1] / WORKLOAD["L"]},
             "speedup_vs_other_path": comp["ms_per_step"] / head["ms_per_step"],

@@ -166,6 +166,16 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
  * come before any stream capture; calls that overlap on the GPU race. */
 int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy);
 
+/* Lowest ne eigenpairs of the symmetric tridiagonal matrix with diagonal
+ * a[0..m) and off-diagonal b[0..m-1), computed on the host CPU: the solver
+ * nss_eigh runs on the Lanczos matrix T_m while the GPU works on the next
+ * iterations (the reference hands T_m to ARPACK on the host,
+ * src/DMRG_SUPERBLOCK.f90:412-425).  Outputs theta[ne] ascending, s[ne*m]
+ * unit eigenvectors (row e = vector e, largest component positive) and
+ * resid[ne] = |b_last * s_e[m-1]|.  Needs no context and no GPU. */
+int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b_last,
+                       double *theta, double *s, double *resid);
+
 /* ---------------------------------------------------------------------------
  * Block-level superblock setup (the enumeration and operator-pool build of
  * sb_get_states / sb_build_dims / Setup_SuperBlock_{Spin,Fermion}_Direct,

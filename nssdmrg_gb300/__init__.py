@@ -116,6 +116,7 @@ def lib():
         "nss_hv_device": (C.c_int, [P, I64, P, P]),
         "nss_hv_device_f32": (C.c_int, [P, I64, P, P]),
         "nss_sb_energy_noalloc": (C.c_int, [P, I64, P, C.POINTER(D)]),
+        "nss_tridiag_lowest": (C.c_int, [C.c_int, P, P, C.c_int, D, P, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
@@ -144,6 +145,23 @@ def _ptr(a: np.ndarray):
 
 def _p(a: np.ndarray, t):
     return a.ctypes.data_as(C.POINTER(t))
+
+
+def tridiag_lowest(a, b, ne: int = 1, b_last: float = 0.0):
+    """Lowest `ne` eigenpairs of the symmetric tridiagonal matrix (diagonal a,
+    off-diagonal b) with the host solver nss_eigh uses on the Lanczos matrix.
+    Returns (theta[ne], s[ne, m], resid[ne]), resid = |b_last * s[:, -1]|."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    m = a.size
+    theta = np.zeros(ne)
+    s = np.zeros((ne, m))
+    resid = np.zeros(ne)
+    rc = lib().nss_tridiag_lowest(m, _ptr(a), _ptr(b) if b.size else None, ne, float(b_last), _ptr(theta),
+                                  _ptr(s), _ptr(resid))
+    if rc != 0:
+        raise NssError(rc, lib().nss_last_error(None).decode())
+    return theta, s, resid
 
 
 class _Keep:

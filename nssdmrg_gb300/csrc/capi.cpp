@@ -6,9 +6,11 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "device.cuh"
 #include "host_dmrg.hpp"
+#include "host_tridiag.hpp"
 
 struct nss_ctx {
     nss::Ctx c;
@@ -178,6 +180,17 @@ int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     cudaSetDevice(ctx->c.device);
     return nss::sb_energy_noalloc(ctx->c, n, d_psi, energy);
+}
+
+int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b_last, double *theta, double *s,
+                       double *resid) {
+    if (m <= 0 || ne <= 0 || ne > m || !a || (m > 1 && !b) || !theta || !s || !resid) {
+        g_err = "nss_tridiag_lowest: need 0 < ne <= m and non-NULL arrays";
+        return NSS_ERR_INVALID;
+    }
+    std::vector<double> work;
+    nss::tridiag_lowest(a, b, m, ne, b_last, theta, s, resid, nullptr, work);
+    return NSS_OK;
 }
 
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {

@@ -79,12 +79,17 @@ struct DevLanczos {
     double *evecs = nullptr;     // [neigen][n] Ritz vectors (last solve)
     int neigen_done = 0;
     double *scal = nullptr;      // device scalars (see k_lanczos.cu)
-    double *part = nullptr;      // partial sums [cap+2][nblk]
+    double *part = nullptr;      // per-CTA partial sums
     unsigned *counter = nullptr; // last-block-done counters
     double *alpha = nullptr, *beta = nullptr;   // [cap]
     double *theta = nullptr, *resid = nullptr, *svec = nullptr; // tridiagonal results
     int *flags = nullptr;        // device flags
-    int *h_flags = nullptr;      // pinned host copy
+    int *h_flags = nullptr;      // host-mapped flag mirror + the host's stop request
+    double *h_ab = nullptr;      // host-mapped mirror of alpha [cap+1], beta [cap+1]
+    int *d_h_flags = nullptr;    // device addresses of the two mapped buffers
+    double *d_h_ab = nullptr;
+    int orth_grid = 0;           // CTAs of the cooperative orthogonalisation kernel
+    size_t orth_smem = 0;        // its dynamic shared memory
 };
 
 struct DevRdm {

@@ -12,7 +12,9 @@
 // SBO = next 8-row group = 8 cores = 1024 B for a 32-wide K chunk), one
 // thread issues the MMAs, tcgen05.commit signals an mbarrier, and after the
 // K loops the 4 warps read their 32 TMEM lanes each (tcgen05.ld 32x32b) and
-// add the A x B terms of the sector on the CUDA cores in FP32.
+// add the dense products to the A x B terms of the sector, which k_hv_fp32
+// ("terms only" tiles, launched just before on the same stream) has written
+// to H psi.
 //
 // Two shared-memory stages: the threads stage chunk i+1 while the tensor
 // core works on chunk i.  Every mbarrier wait is bounded; a wait that runs
@@ -134,10 +136,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     const float *__restrict__ v, float *__restrict__ hv, const int4 *__restrict__ tiles,
     const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
     const float *__restrict__ hlp, const int64_t *__restrict__ hl_off,
-    const float *__restrict__ hrp, const int64_t *__restrict__ hr_off,
-    const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
-    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val,
-    int *err, const int *stop) {
+    const float *__restrict__ hrp, const int64_t *__restrict__ hr_off, int *err, const int *stop) {
     if (stop && *stop) return;   // before any TMEM allocation: uniform exit
     extern __shared__ __align__(1024) uint8_t smem[];
     float *stage[2] = {(float *)smem, (float *)smem + STAGE_FLOATS};
@@ -213,8 +212,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // Epilogue, in two passes.  (1) Each warp moves its 32 TMEM lanes (rows)
     // into shared memory (row stride 65 floats: conflict-free), the MMAs being
-    // complete so the stage buffers are free.  (2) Lanes run along columns:
-    // the A x B gathers W_q[aj][bj(ir)] and the stores to H psi are coalesced.
+    // complete so the stage buffers are free.  (2) Lanes run along columns, so
+    // the read-add-store of H psi (which holds the A x B terms) is coalesced.
     const int w = tid >> 5, lane = tid & 31;
     float *Dsm = stage[0];                          // 128 x 65 floats < one stage
     if (ok_s) {
@@ -231,28 +230,15 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     }
     __syncthreads();
     if (ok_s) {
-        const int t0 = term_ptr[k], t1 = term_ptr[k + 1];
+        float *out = hv + off[k];
         for (int rr = w; rr < TC_M; rr += TC_THREADS / 32) {
             const int il = row0 + rr;
             if (il >= dl) break;
             for (int cc = lane; cc < TC_BN; cc += 32) {
                 const int ir = col0 + cc;
                 if (ir >= dr) continue;
-                float a = Dsm[rr * (TC_BN + 1) + cc];
-                for (int ti = t0; ti < t1; ++ti) {
-                    const DevTerm tm = terms[ti];
-                    const float *Wq = v + off[tm.in_sec];
-                    const int drq = drs[tm.in_sec];
-                    const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
-                    for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
-                        const int aj = ab_col[ja];
-                        float cb = 0.f;
-                        for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
-                            cb = fmaf(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
-                        a = fmaf(ab_val[ja], cb, a);
-                    }
-                }
-                hv[off[k] + (int64_t)il * dr + ir] = a;
+                const int64_t idx = (int64_t)il * dr + ir;
+                out[idx] = Dsm[rr * (TC_BN + 1) + cc] + out[idx];
             }
         }
     }
@@ -271,7 +257,7 @@ int hv_device_tc(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
     }
     k_hv_tc<<<s.ntiles_tc, TC_THREADS, TC_SMEM, c.stream>>>(
         d_v, d_hv, s.d_tiles_tc, s.d_dls, s.d_drs, s.d_off, s.d_hl32, s.d_hl_off, s.d_hr32, s.d_hr_off,
-        s.d_term_ptr, s.d_terms32, s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, s.d_tc_err, stop);
+        s.d_tc_err, stop);
     c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;

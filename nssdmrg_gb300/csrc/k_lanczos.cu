@@ -1,4 +1,5 @@
-// Lanczos eigensolver for the lowest eigenpairs of H_sb, entirely on the GPU.
+// Lanczos eigensolver for the lowest eigenpairs of H_sb, on the GPU with the
+// small tridiagonal problem on the host.
 //
 // Replaces SciFortran sp_eigh (ARPACK, called at src/DMRG_SUPERBLOCK.f90:
 // 394-425) for the direct mode.  Algorithm: Lanczos with full
@@ -6,37 +7,50 @@
 // Gram-Schmidt projection of the (small) residual against the whole basis,
 // and a second projection only when that one removes more than half of the
 // residual -- the whole Krylov basis kept resident in HBM (no restarts), and a
-// convergence test every CHECK steps on the tridiagonal matrix T on the
-// device: residual beta_m |s_m| <= tol |theta| for each wanted Ritz pair,
-// the ARPACK criterion.  Breakdown (beta ~ 0, invariant subspace) restarts
-// with a fresh random vector orthogonal to the basis.  Eigenvectors are
-// gauge-dependent, so parity with the reference is on eigenvalues and on
-// what the RDM derives from them.
+// convergence test every CHECK steps on the tridiagonal matrix T_m:
+// residual beta_m |s_m| <= tol |theta| for each wanted Ritz pair, the ARPACK
+// criterion.  Breakdown (beta ~ 0, invariant subspace) restarts with a fresh
+// random vector orthogonal to the basis.  Eigenvectors are gauge-dependent,
+// so parity with the reference is on eigenvalues and on what the RDM derives
+// from them.
 //
-// Per iteration j (m = j+1 basis vectors):
-//   k_hv          w = H v_j
-//   k_alpha       alpha = v_j . w
-//   k_dots        w -= alpha v_j + beta_{j-1} v_{j-1};  h = V_m^T w, ww = w.w
-//   k_update      w -= V_m h, beta^2 = w.w, alpha_j = alpha + h_j
-//   k_dots/k_update again only if beta^2 < ww/2 (device flag)
-//   k_next        v_{j+1} = w / beta
+// Per iteration j (m = j+1 basis vectors) two kinds of launch:
+//   sector H*psi   w = H v_j                      (k_hv_* kernels)
+//   k_orth         one cooperative launch, one CTA per SM, each CTA owning a
+//                  contiguous slice of the rows; grid barriers separate
+//                    alpha = v_j . w
+//                    w -= alpha v_j + beta_{j-1} v_{j-1};  h = V_m^T w, ww = w.w
+//                    w -= V_m h, beta^2 = w.w  (again if beta^2 < ww/2)
+//                    v_{j+1} = w / beta, or the breakdown flag
 // Projecting the raw H v_j instead (one pass) lets the orthogonality error
 // grow by ||H||/beta per step; the recurrence-first order keeps it at 1e-15.
-// Every kernel reads the device stop flag first, so the host can enqueue a
-// whole chunk of iterations ahead of the convergence test.
+// Every grid-level sum is reduced by every CTA in the same fixed order, so
+// all CTAs hold bitwise identical scalars and take the same branches.
+//
+// The tridiagonal problem (m <= a few hundred) is a chain of dependent FP64
+// operations, which GB300's narrow FP64 pipe runs slowly on one SM; it is
+// solved on the host (host_tridiag.cpp) from alpha/beta that k_orth writes
+// into host-mapped memory, while the GPU already runs the next CHECK
+// iterations.  On convergence the host raises a stop request in host-mapped
+// memory; the next k_orth publishes it as the device stop flag, and every
+// kernel still queued returns at once.  The decision depends only on the
+// checked chunk, so results do not depend on that timing.
 //
 // Precision modes.  The kernels are templates over the type T of the Krylov
 // vectors.  T = double is the plain method: FP64 everywhere.  T = float is
-// the mixed method: H*psi in FP32 (k_hv_fp32), the basis and the projections
-// in FP32 with FP64 block partial sums, while alpha/beta, the tridiagonal
-// eigensolve and the Ritz vector stay FP64; it runs to a relative residual
-// of MIXED_TOL, and the energy is then refined in FP64 as the Rayleigh
-// quotient psi.H.psi of the FP64 Ritz vector with the FP64 H*psi (error
-// quadratic in the vector error: |dE|/|E| ~ 1e-13 at MIXED_TOL = 1e-7),
-// whose FP64 residual ||H psi - E psi|| is reported.  On GB300 the FP64
-// pipe runs at 1/64 of the FP32 one, which is what the mixed method buys.
+// the mixed method: H*psi in FP32 (k_hv_fp32 / k_hv_tc), the basis and the
+// projections in FP32 with FP64 block partial sums, while alpha/beta, the
+// tridiagonal eigensolve and the Ritz vector stay FP64; it runs to a relative
+// residual of MIXED_TOL, and the energy is then refined in FP64 as the
+// Rayleigh quotient psi.H.psi of the FP64 Ritz vector with the FP64 H*psi
+// (error quadratic in the vector error: |dE|/|E| ~ 1e-13 at MIXED_TOL =
+// 1e-7), whose FP64 residual ||H psi - E psi|| is reported.  On GB300 the
+// FP64 pipe runs at 1/64 of the FP32 one, which is what the mixed method buys.
 #include "device.cuh"
+#include "host_tridiag.hpp"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -46,15 +60,19 @@ namespace nss {
 
 namespace {
 
-constexpr int NBLK = 304;         // 2 CTAs per SM on the 152-SM GB300
-constexpr int CHECK = 8;          // convergence test period (iterations)
+constexpr int NBLK = 304;         // grid of the restart-path reductions
+constexpr int CHECK = 4;          // convergence test period (iterations)
 constexpr int SUB = 1024;         // rows staged per shared-memory sub-chunk
 constexpr double MIXED_TOL = 1e-7;
+constexpr int ORTH_THREADS = 512;
+constexpr int ORTH_WARPS = ORTH_THREADS / 32;
+constexpr uint32_t BAR_SPIN = 1u << 24;   // grid-barrier poll limit (~1 s)
 
 // device scalar slots (Ctx::lz.scal)
 enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NSCAL = 4 };
-// device flag slots (Ctx::lz.flags)
-enum { F_STOP = 0, F_PASS2 = 1, F_M = 2, F_CONV = 3, F_BREAK = 4, F_NFLAGS = 8 };
+// device flag slots (Ctx::lz.flags); the host-mapped mirror uses the same
+// indices and one more word, F_NFLAGS, for the host's stop request
+enum { F_STOP = 0, F_PASS2 = 1, F_M = 2, F_CONV = 3, F_BREAK = 4, F_HOST = 5, F_ERR = 6, F_NFLAGS = 8 };
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T x) {
@@ -91,6 +109,7 @@ __device__ __forceinline__ bool last_block(unsigned *counter) {
     return last != 0;
 }
 
+// Restart path only (a fresh start vector orthogonalised against the basis):
 // h[l] = V[l] . w for l < m, and scal[S_WW] = w . w.  With threeterm != 0
 // the recurrence step w -= alpha v_{m-1} + beta v_{m-2} (alpha from
 // scal[S_ALPHA], beta = betas[m-2]) is applied to w first and the updated w
@@ -153,32 +172,6 @@ __global__ void __launch_bounds__(256) k_dots(const T *__restrict__ V, int m, T 
     if (tid == 0) *counter = 0u;
 }
 
-// alpha = v . w  (grid reduction by the last CTA) -> scal[S_ALPHA]
-template <class T>
-__global__ void __launch_bounds__(256) k_alpha(const T *__restrict__ v, const T *__restrict__ w, int64_t n,
-                                               double *__restrict__ part, double *__restrict__ scal,
-                                               unsigned *counter, const int *flags) {
-    if (flags[F_STOP]) return;
-    const int tid = threadIdx.x;
-    T p = (T)0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p += v[i] * w[i];
-    const double pd = warp_sum<double>((double)p);
-    __shared__ double red[8];
-    if ((tid & 31) == 0) red[tid >> 5] = pd;
-    __syncthreads();
-    if (tid == 0) {
-        double t = 0.0;
-        for (int q = 0; q < 8; ++q) t += red[q];
-        part[blockIdx.x] = t;
-    }
-    if (!last_block(counter) || tid != 0) return;
-    double t = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) t += part[b];
-    scal[S_ALPHA] = t;
-    *counter = 0u;
-}
-
 // w -= V_m h ; beta^2 = w.w ; the last CTA records alpha_j and beta_j.
 template <class T>
 __global__ void __launch_bounds__(256) k_update(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n,
@@ -222,25 +215,6 @@ __global__ void __launch_bounds__(256) k_update(const T *__restrict__ V, int m, 
     *counter = 0u;
 }
 
-// v_{j+1} = w / beta_j, or flag a breakdown (invariant subspace).
-template <class T>
-__global__ void k_next(T *__restrict__ vnext, const T *__restrict__ w, int64_t n, int *flags,
-                       const double *alpha, const double *beta, int j) {
-    if (flags[F_STOP]) return;
-    const double b = beta[j];
-    const double scale = fmax(fabs(alpha[j]), j > 0 ? beta[j - 1] : 0.0);
-    if (!(b > 1e-13 * fmax(scale, 1e-300))) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            flags[F_BREAK] = j + 1;
-            flags[F_STOP] = 2;
-        }
-        return;
-    }
-    const T inv = (T)(1.0 / b);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        vnext[i] = w[i] * inv;
-}
-
 // x <- x / ||x|| (one CTA per launch is enough for start vectors);
 // blockDim.x <= 1024, so at most 32 warp partial sums
 template <class T>
@@ -257,139 +231,292 @@ __global__ void __launch_bounds__(1024) k_normalize(T *x, int64_t n) {
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = (T)((double)x[i] * inv);
 }
 
-// Number of eigenvalues of T_m below x (Sturm count of the leading
-// principal minors, division-free with exact power-of-two rescaling).
-__device__ int sturm_count(const double *alpha, const double *beta, int m, double x) {
-    double p0 = 1.0, p1 = alpha[0] - x;
-    int cnt = (p1 < 0.0) ? 1 : 0;
-    for (int i = 1; i < m; ++i) {
-        const double b = beta[i - 1];
-        double p2 = (alpha[i] - x) * p1 - b * b * p0;
-        // a zero minor takes the sign opposite to its predecessor
-        if (p2 == 0.0) p2 = -copysign(1e-300, p1);
-        if ((p2 < 0.0) != (p1 < 0.0)) ++cnt;
-        p0 = p1;
-        p1 = p2;
-        const double a = fmax(fabs(p0), fabs(p1));
-        if (a > 0x1p+600) { p0 *= 0x1p-600; p1 *= 0x1p-600; }
-        else if (a < 0x1p-600) { p0 *= 0x1p+600; p1 *= 0x1p+600; }
+// ---------------------------------------------------------------------------
+// Fused orthogonalisation step (cooperative launch).
+
+struct OrthArgs {
+    void *V, *w;                 // T*: basis [cap+1][n], work vector [n]
+    int64_t n;
+    int j, mmax, pstride;        // step, iteration cap, column stride of partials
+    double *alpha, *beta;        // device tridiagonal coefficients
+    double *part;                // per-CTA partials (five regions)
+    unsigned *bar;               // grid barrier: arrival count, generation
+    int *flags;                  // device flags
+    double *h_alpha, *h_beta;    // host-mapped mirrors of alpha, beta
+    int *h_flags;                // host-mapped flag mirror + stop request
+};
+
+// Grid-wide barrier for a cooperative launch (all CTAs resident).  Bounded:
+// a wait that runs out sets flags[F_ERR] and every later barrier returns
+// false at once, so the kernel always ends.
+__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int good = 1;
+        volatile unsigned *gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            uint32_t it = 0;
+            while (*gen == g) {
+                if (*(volatile int *)err) { good = 0; break; }
+                if (++it > BAR_SPIN) { atomicExch(err, 1); good = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good;
     }
-    return cnt;
+    __syncthreads();
+    return ok != 0;
 }
 
-// Eigenvalues theta[0..ne) of T_m by 32-way multisection, one warp per
-// eigenvalue (a round costs one Sturm count per lane; GB300's FP64 pipe is
-// narrow, so fewer concurrent counts and more rounds is the faster trade),
-// eigenvectors s by inverse iteration, residual estimates beta_{m-1} |s_{m-1}|
-// and the convergence flag.
-// m_arg is the basis size the chunk would reach; after a breakdown the
-// kernel uses the breakdown step instead, and once a solve has converged
-// (stop flag 1) later calls leave theta and s untouched.  It records the m it
-// used (F_M) and sets the stop flag: 1 converged or Krylov space exhausted
-// (m = n), 3 iteration cap reached.
-__global__ void __launch_bounds__(128) k_tridiag(const double *alpha, const double *beta, int m_arg, int ne,
-                                                 double tol, double *theta, double *resid, double *svec,
-                                                 int sstride, int *flags, int mmax, int64_t nvec) {
-    if (flags[F_STOP] == 1 || flags[F_STOP] == 3) return;
-    const int m = (flags[F_STOP] == 2) ? flags[F_BREAK] : m_arg;
-    __shared__ double lo_s, hi_s;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
-        double lo = 1e300, hi = -1e300;
-        for (int i = 0; i < m; ++i) {
-            double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i < m - 1 ? fabs(beta[i]) : 0.0);
-            lo = fmin(lo, alpha[i] - r);
-            hi = fmax(hi, alpha[i] + r);
-        }
-        double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
-        lo_s = lo - pad;
-        hi_s = hi + pad;
+// CTA sum (512 threads), valid in thread 0
+__device__ __forceinline__ double block_sum(double v, double *scr) {
+    v = warp_sum<double>(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) scr[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < ORTH_WARPS ? scr[threadIdx.x] : 0.0;
+        t = warp_sum<double>(t);
+    }
+    return t;
+}
+
+// sum of the G per-CTA partials p[0..G), same order in every CTA
+__device__ __forceinline__ double grid_total(const double *p, int G, double *bcast) {
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int b = threadIdx.x; b < G; b += 32) t += __ldcg(p + b);
+        t = warp_sum<double>(t);
+        if (threadIdx.x == 0) *bcast = t;
     }
     __syncthreads();
-    const int e = warp;
-    if (e < ne && e < m) {
-        double a = lo_s, b = hi_s;
-        for (int round = 0; round < 24; ++round) {
-            if (!(b - a > 4e-16 * fmax(fabs(a), fabs(b)) + 1e-300)) break;
-            const double x = a + (b - a) * (double)(lane + 1) / 33.0;
-            const int cnt = sturm_count(alpha, beta, m, x);
-            const unsigned over = __ballot_sync(0xffffffffu, cnt > e);
-            // first point whose count exceeds e brackets eigenvalue e
-            const int t = over ? __ffs(over) - 1 : 32;
-            const double xt = __shfl_sync(0xffffffffu, x, t < 32 ? t : 31);
-            const double xp = __shfl_sync(0xffffffffu, x, t > 0 ? t - 1 : 0);
-            const double na = (t == 0) ? a : xp;
-            const double nb = (t == 32) ? b : xt;
-            a = na;
-            b = nb;
+    return *bcast;
+}
+
+// hs[l] = sum_b p[l*G + b] for l < ncol (four columns per warp in flight)
+__device__ __forceinline__ void grid_columns(const double *p, int G, int ncol, double *hs) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int l0 = warp; l0 < ncol; l0 += 4 * ORTH_WARPS) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int l = l0 + u * ORTH_WARPS;
+            if (l < ncol)
+                for (int b = lane; b < G; b += 32) t[u] += __ldcg(p + (int64_t)l * G + b);
         }
-        if (lane == 0) theta[e] = 0.5 * (a + b);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double s = warp_sum<double>(t[u]);
+            const int l = l0 + u * ORTH_WARPS;
+            if (lane == 0 && l < ncol) hs[l] = s;
+        }
     }
-    __syncthreads();
-    // inverse iteration, one thread per eigenvalue: (T - shift I) y = s, solved
-    // by Gaussian elimination with partial pivoting (the LAPACK dgtsv scheme);
-    // the factor bands live in the eigenvector's scratch row (stride 4*m+).
-    if (tid < ne && tid < m) {
-        const int e = tid;
-        double *s = svec + (int64_t)e * sstride;
-        double *D = s + m, *DU = s + 2 * m, *DL = s + 3 * m;
-        const double th = theta[e];
-        const double shift = th + 1e-14 * fmax(fabs(th), 1.0);
-        for (int i = 0; i < m; ++i) s[i] = 1.0 + 0.01 * (double)((i * 7 + e * 3) % 11);
-        for (int it = 0; it < 3; ++it) {
-            for (int i = 0; i < m; ++i) {
-                D[i] = alpha[i] - shift;
-                DU[i] = (i < m - 1) ? beta[i] : 0.0;
-                DL[i] = (i < m - 1) ? beta[i] : 0.0;
+}
+
+// Reduce CW per-lane values over the 32 lanes of a warp at once (butterfly
+// with exchange: 31 shuffles for all CW columns); lane L ends with the sum of
+// column L % CW in d[0].
+template <int CW>
+__device__ __forceinline__ double multi_reduce(double (&d)[CW], int lane) {
+    if (CW < 32) {
+#pragma unroll
+        for (int s = 16; s >= CW; s >>= 1)
+#pragma unroll
+            for (int c = 0; c < CW; ++c) d[c] += __shfl_xor_sync(0xffffffffu, d[c], s);
+    }
+#pragma unroll
+    for (int s = CW / 2; s >= 1; s >>= 1) {
+        const bool upper = (lane & s) != 0;
+#pragma unroll
+        for (int c = 0; c < s; ++c) {
+            const double send = upper ? d[c] : d[c + s];
+            const double keep = upper ? d[c + s] : d[c];
+            d[c] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+        }
+    }
+    return d[0];
+}
+
+// CTA partials of h[l] = V[l] . w (l < m) over rows [i0, i1), plus w.w as
+// column m when `ww`; written to out[l*G] (out = region + blockIdx.x).  Work
+// items are (CW-column group, row quarter); a lane runs down the rows of its
+// item accumulating CW columns in registers, then one multi_reduce.
+template <class T, int CW>
+__device__ __forceinline__ void cta_dots(const T *__restrict__ V, int m, const T *__restrict__ w, int64_t n,
+                                         int64_t i0, int64_t i1, bool ww, double *red, double *out, int G) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncol = m + (ww ? 1 : 0);
+    const int ng = (ncol + CW - 1) / CW;
+    const int nq = ng >= ORTH_WARPS ? 1 : ORTH_WARPS / ng;
+    const int rs = ng * CW;
+    const int64_t len = i1 - i0, qlen = (len + nq - 1) / nq;
+    for (int item = warp; item < ng * nq; item += ORTH_WARPS) {
+        const int g = item % ng, q = item / ng, l0 = g * CW;
+        const int64_t r0 = i0 + (int64_t)q * qlen, r1 = min(i1, r0 + qlen);
+        T acc[CW];
+#pragma unroll
+        for (int c = 0; c < CW; ++c) acc[c] = (T)0;
+        if (l0 + CW <= m) {
+            for (int64_t r = r0 + lane; r < r1; r += 32) {
+                const T wv = w[r];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) acc[c] += V[(int64_t)(l0 + c) * n + r] * wv;
             }
-            for (int i = 0; i < m - 1; ++i) {
-                if (fabs(D[i]) >= fabs(DL[i])) {
-                    if (D[i] == 0.0) D[i] = 1e-300;
-                    const double f = DL[i] / D[i];
-                    D[i + 1] -= f * DU[i];
-                    s[i + 1] -= f * s[i];
-                    DL[i] = 0.0;
-                } else {
-                    const double f = D[i] / DL[i];
-                    D[i] = DL[i];
-                    const double tmp = D[i + 1];
-                    D[i + 1] = DU[i] - f * tmp;
-                    if (i < m - 2) {
-                        DL[i] = DU[i + 1];
-                        DU[i + 1] = -f * DL[i];
-                    } else {
-                        DL[i] = 0.0;
-                    }
-                    DU[i] = tmp;
-                    const double b0 = s[i];
-                    s[i] = s[i + 1];
-                    s[i + 1] = b0 - f * s[i + 1];
+        } else {
+            for (int64_t r = r0 + lane; r < r1; r += 32) {
+                const T wv = w[r];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) {
+                    const int l = l0 + c;
+                    if (l < m) acc[c] += V[(int64_t)l * n + r] * wv;
+                    else if (ww && l == m) acc[c] += wv * wv;
                 }
             }
-            if (D[m - 1] == 0.0) D[m - 1] = 1e-300;
-            s[m - 1] /= D[m - 1];
-            if (m > 1) s[m - 2] = (s[m - 2] - DU[m - 2] * s[m - 1]) / D[m - 2];
-            for (int i = m - 3; i >= 0; --i) s[i] = (s[i] - DU[i] * s[i + 1] - DL[i] * s[i + 2]) / D[i];
-            double nrm = 0.0;
-            for (int i = 0; i < m; ++i) nrm = fma(s[i], s[i], nrm);
-            nrm = 1.0 / sqrt(nrm);
-            for (int i = 0; i < m; ++i) s[i] *= nrm;
         }
-        // sign convention: largest component positive
-        double big = 0.0;
-        for (int i = 0; i < m; ++i) if (fabs(s[i]) > fabs(big)) big = s[i];
-        if (big < 0.0) for (int i = 0; i < m; ++i) s[i] = -s[i];
-        resid[e] = fabs(beta[m - 1] * s[m - 1]);
+        double d[CW];
+#pragma unroll
+        for (int c = 0; c < CW; ++c) d[c] = (double)acc[c];
+        const double s = multi_reduce<CW>(d, lane);
+        if (lane < CW && l0 + lane < ncol) red[q * rs + l0 + lane] = s;
     }
     __syncthreads();
-    if (tid == 0) {
-        int conv = 0;
-        for (int e = 0; e < ne && e < m; ++e)
-            if (resid[e] <= tol * fmax(fabs(theta[e]), 1e-300)) ++conv;
-        flags[F_CONV] = conv;
-        flags[F_M] = m;
-        if (conv >= min(ne, m) || (int64_t)m >= nvec) flags[F_STOP] = 1;
-        else if (m >= mmax) flags[F_STOP] = 3;
+    for (int l = threadIdx.x; l < ncol; l += ORTH_THREADS) {
+        double s = 0.0;
+        for (int q = 0; q < nq; ++q) s += red[q * rs + l];
+        out[(int64_t)l * G] = s;
+    }
+}
+
+// w -= V_m h over rows [i0, i1); returns the CTA's w.w (valid in thread 0)
+template <class T>
+__device__ __forceinline__ double cta_update(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n,
+                                             int64_t i0, int64_t i1, const double *hs, T *hT, double *scr) {
+    for (int l = threadIdx.x; l < m; l += ORTH_THREADS) hT[l] = (T)hs[l];
+    __syncthreads();
+    T ss = (T)0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += ORTH_THREADS) {
+        T x = w[i];
+#pragma unroll 16
+        for (int l = 0; l < m; ++l) x -= V[(int64_t)l * n + i] * hT[l];
+        w[i] = x;
+        ss += x * x;
+    }
+    return block_sum((double)ss, scr);
+}
+
+template <class T>
+struct OrthCW { static constexpr int value = sizeof(T) == 4 ? 32 : 16; };
+
+__host__ __device__ inline int orth_redsz(int pstride, int cw) {
+    return ORTH_WARPS * cw > pstride + cw ? ORTH_WARPS * cw : pstride + cw;
+}
+
+// shared memory of k_orth, in doubles: hs, red, hT, scratch
+inline size_t orth_smem(int pstride, int cw) {
+    return (size_t)(pstride + orth_redsz(pstride, cw) + pstride + 64) * sizeof(double);
+}
+
+template <class T, int CW>
+__global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
+    int *flags = a.flags;
+    if (*(volatile int *)&flags[F_STOP]) return;     // set before this launch: uniform
+    extern __shared__ double osm[];
+    const int ps = a.pstride;
+    double *hs = osm;
+    double *red = hs + ps;
+    T *hT = (T *)(red + orth_redsz(ps, CW));
+    double *scr = red + orth_redsz(ps, CW) + ps;     // [0,16) block sums, [32] broadcast
+    const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x;
+    const int64_t n = a.n;
+    const int64_t chunk = (n + G - 1) / G;
+    const int64_t i0 = min(n, (int64_t)blk * chunk), i1 = min(n, i0 + chunk);
+    T *V = (T *)a.V, *w = (T *)a.w;
+    const int j = a.j, m = j + 1;
+    const T *vj = V + (int64_t)j * n;
+    const T *vjm = V + (int64_t)(j > 0 ? j - 1 : 0) * n;
+    double *pA = a.part, *pH = pA + G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G, *pB2 = pH2 + (int64_t)ps * G;
+    int *err = flags + F_ERR;
+
+    // the host's stop request, published by CTA 0 before the first barrier
+    if (blk == 0 && tid == 0) flags[F_HOST] = *(volatile const int *)(a.h_flags + F_NFLAGS);
+    {   // alpha = v_j . w
+        T p = (T)0;
+        for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) p += vj[i] * w[i];
+        const double t = block_sum((double)p, scr);
+        if (tid == 0) pA[blk] = t;
+    }
+    if (!grid_sync(a.bar, err)) return;
+    if (__ldcg(&flags[F_HOST])) {
+        if (blk == 0 && tid == 0) flags[F_STOP] = 1;
+        return;
+    }
+    const double alpha0 = grid_total(pA, G, scr + 32);
+    {   // three-term step, then h = V_m^T w and ww = w.w
+        const T a3 = (T)alpha0;
+        const T b3 = j > 0 ? (T)a.beta[j - 1] : (T)0;
+        for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+            T x = w[i] - a3 * vj[i];
+            if (j > 0) x -= b3 * vjm[i];
+            w[i] = x;
+        }
+        __syncthreads();
+        cta_dots<T, CW>(V, m, w, n, i0, i1, true, red, pH + blk, G);
+    }
+    if (!grid_sync(a.bar, err)) return;
+    grid_columns(pH, G, m + 1, hs);
+    __syncthreads();
+    const double ww = hs[m];
+    double hj = hs[j];
+    {
+        const double t = cta_update<T>(V, m, w, n, i0, i1, hs, hT, scr);
+        if (tid == 0) pB[blk] = t;
+    }
+    if (!grid_sync(a.bar, err)) return;
+    double bb = grid_total(pB, G, scr + 32);
+    if (bb < 0.5 * ww) {   // second projection (same decision in every CTA)
+        cta_dots<T, CW>(V, m, w, n, i0, i1, false, red, pH2 + blk, G);
+        if (!grid_sync(a.bar, err)) return;
+        grid_columns(pH2, G, m, hs);
+        __syncthreads();
+        hj += hs[j];
+        const double t = cta_update<T>(V, m, w, n, i0, i1, hs, hT, scr);
+        if (tid == 0) pB2[blk] = t;
+        if (!grid_sync(a.bar, err)) return;
+        bb = grid_total(pB2, G, scr + 32);
+    }
+    const double alpha_j = alpha0 + hj;
+    const double beta_j = sqrt(bb);
+    bool brk = false;
+    if (m < a.mmax) {
+        const double scale = fmax(fabs(alpha_j), j > 0 ? a.beta[j - 1] : 0.0);
+        brk = !(beta_j > 1e-13 * fmax(scale, 1e-300));
+        if (!brk) {
+            const T inv = (T)(1.0 / beta_j);
+            T *vn = V + (int64_t)m * n;
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) vn[i] = w[i] * inv;
+        }
+    }
+    if (blk == 0 && tid == 0) {
+        a.alpha[j] = alpha_j;
+        a.beta[j] = beta_j;
+        a.h_alpha[j] = alpha_j;
+        a.h_beta[j] = beta_j;
+        if (brk) {
+            flags[F_BREAK] = m;
+            flags[F_STOP] = 2;
+            a.h_flags[F_BREAK] = m;
+            a.h_flags[F_STOP] = 2;
+        }
+        __threadfence_system();
     }
 }
 
@@ -467,7 +594,7 @@ __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ psi, c
     *counter = 0u;
 }
 
-// per-eigenvector scratch row: s[m] followed by three factor bands of m
+// per-eigenvector scratch row of svec
 inline int svec_stride(int cap) { return 4 * (cap + 1); }
 
 int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
@@ -487,11 +614,29 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)(cap + 1) * n));
         z.full64 = true;
     }
+    int dev = 0, nsm = 0;
+    NSS_CUDA_TRY(c, cudaGetDevice(&dev));
+    NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int pstride = cap + 2;
+    const int cw = mixed ? OrthCW<float>::value : OrthCW<double>::value;
+    const size_t smem = orth_smem(pstride, cw);
+    const void *fn = mixed ? (const void *)k_orth<float, OrthCW<float>::value>
+                           : (const void *)k_orth<double, OrthCW<double>::value>;
+    if (smem > 48 * 1024) NSS_CUDA_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, ORTH_THREADS, smem));
+    if (occ < 1) {
+        c.err = "nss_eigh: Krylov basis too large for the orthogonalisation kernel's shared memory";
+        return NSS_ERR_INVALID;
+    }
+    z.orth_grid = nsm;      // one CTA per SM, all resident (cooperative launch)
+    z.orth_smem = smem;
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.w, (size_t)n));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));
-    // scalars, two projection-coefficient vectors, restart scratch alpha/beta
+    // scalars, projection coefficients, restart scratch alpha/beta, refinement
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.scal, (size_t)S_NSCAL + 4 * (cap + 2) + 8));
-    NSS_CUDA_TRY(c, ctx_alloc(c, &z.part, (size_t)(cap + 2) * NBLK));
+    const size_t part = std::max((size_t)(cap + 2) * NBLK, (size_t)(2 * pstride + 3) * (size_t)nsm);
+    NSS_CUDA_TRY(c, ctx_alloc(c, &z.part, part));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.counter, 4));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.alpha, (size_t)cap + 1));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.beta, (size_t)cap + 1));
@@ -499,7 +644,11 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.resid, 8));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.svec, (size_t)4 * svec_stride(cap)));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.flags, F_NFLAGS));
-    NSS_CUDA_TRY(c, cudaMallocHost((void **)&z.h_flags, 2 * F_NFLAGS * sizeof(int)));
+    // host-mapped mirrors: alpha, beta; flags + the host's stop request
+    NSS_CUDA_TRY(c, cudaHostAlloc((void **)&z.h_ab, 2 * (size_t)(cap + 1) * sizeof(double), cudaHostAllocMapped));
+    NSS_CUDA_TRY(c, cudaHostAlloc((void **)&z.h_flags, (F_NFLAGS + 8) * sizeof(int), cudaHostAllocMapped));
+    NSS_CUDA_TRY(c, cudaHostGetDevicePointer((void **)&z.d_h_ab, z.h_ab, 0));
+    NSS_CUDA_TRY(c, cudaHostGetDevicePointer((void **)&z.d_h_flags, z.h_flags, 0));
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.counter, 0, 4 * sizeof(unsigned), c.stream));
     return NSS_OK;
 }
@@ -512,81 +661,109 @@ template <>
 int hv_t<float>(Ctx &c, const float *v, float *hv, const int *stop) { return hv_device_fp32(c, v, hv, stop); }
 
 // The Lanczos iterations on a basis of type T; leaves theta (Ritz values),
-// svec (their T-eigenvectors) and the Ritz vectors (FP64) in c.lz.
+// svec (their T_m eigenvectors, stride m) and the Ritz vectors (FP64) in c.lz.
 template <class T>
 int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t seed, int *numop_out,
                 int *m_out) {
     DevLanczos &z = c.lz;
     const int64_t n = c.sb.n;
     const int cap = z.cap;
-    double *h1 = z.scal + S_NSCAL, *h2 = h1 + (cap + 2);
-    double *rs_alpha = h2 + (cap + 2), *rs_beta = rs_alpha + (cap + 2);
-    const int sstride = svec_stride(cap);
+    double *h1 = z.scal + S_NSCAL;
+    double *rs_alpha = h1 + 2 * (cap + 2), *rs_beta = rs_alpha + (cap + 2);
     cudaStream_t st = c.stream;
+    volatile int *hf = z.h_flags;
+    double *ha = z.h_ab, *hb = z.h_ab + (cap + 1);
+    // no kernel of this context is running: the previous solve synchronised
+    for (int i = 0; i < F_NFLAGS + 8; ++i) hf[i] = 0;
+    for (int i = 0; i <= cap; ++i) ha[i] = hb[i] = 0.0;
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta, 0, (cap + 1) * sizeof(double), st));
+    NSS_CUDA_TRY(c, cudaMemsetAsync(z.counter, 0, 4 * sizeof(unsigned), st));
     const int vb = 608;   // 4 CTAs per SM for elementwise kernels
     uint64_t restarts = 0;
     ++c.launches;
     k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
     ++c.launches;
     k_normalize<T><<<1, 1024, 0, st>>>(V, n);
-    int m_done = 1, numop_ = 0, rc = NSS_OK;
-    bool converged = false;
     const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
     const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
     if (dots_smem > 48 * 1024)
         cudaFuncSetAttribute(k_dots<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
     if (upd_smem > 48 * 1024)
         cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
-    // Chunks of CHECK iterations, each followed by the convergence test and
-    // a copy of the flags into one of two pinned slots; one chunk runs ahead
-    // of the host's read of the previous one, so the stream never idles.
-    // Kernels of a chunk enqueued after convergence exit at once (stop flag).
+    constexpr int CW = OrthCW<T>::value;
+    OrthArgs oa;
+    oa.V = V;
+    oa.w = w;
+    oa.n = n;
+    oa.j = 0;
+    oa.mmax = mmax;
+    oa.pstride = cap + 2;
+    oa.alpha = z.alpha;
+    oa.beta = z.beta;
+    oa.part = z.part;
+    oa.bar = z.counter + 2;
+    oa.flags = z.flags;
+    oa.h_alpha = z.d_h_ab;
+    oa.h_beta = z.d_h_ab + (cap + 1);
+    oa.h_flags = z.d_h_flags;
+    // Chunks of CHECK iterations, each ending with an event; the host checks
+    // chunk k on T_m while the GPU runs chunk k+1.
     cudaEvent_t evs[2];
     cudaEventCreateWithFlags(&evs[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
     auto enqueue_chunk = [&](int j0, int slot) -> int {
         const int jend = std::min(mmax, j0 + CHECK);
         for (int jj = j0; jj < jend; ++jj) {
-            const int m = jj + 1;
-            int r2 = hv_t<T>(c, V + (int64_t)jj * n, w, z.flags + F_STOP);
-            if (r2) return -1;
-            c.launches += 5;
-            k_alpha<T><<<NBLK, 256, 0, st>>>(V + (int64_t)jj * n, w, n, z.part, z.scal, z.counter, z.flags);
-            k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m, w, n, z.part, h1, z.scal, z.counter, z.flags, 0, 1,
-                                                    z.beta);
-            k_update<T><<<NBLK, 256, upd_smem, st>>>(V, m, w, n, h1, z.part, z.scal, z.counter, z.flags,
-                                                     z.alpha, z.beta, 0);
-            k_dots<T><<<NBLK, 256, dots_smem, st>>>(V, m, w, n, z.part, h2, z.scal, z.counter, z.flags, 1, 0,
-                                                    z.beta);
-            k_update<T><<<NBLK, 256, upd_smem, st>>>(V, m, w, n, h2, z.part, z.scal, z.counter, z.flags,
-                                                     z.alpha, z.beta, 1);
-            if (m < mmax) {
-                ++c.launches;
-                k_next<T><<<vb, 256, 0, st>>>(V + (int64_t)m * n, w, n, z.flags, z.alpha, z.beta, jj);
+            if (hv_t<T>(c, V + (int64_t)jj * n, w, z.flags + F_STOP)) return -1;
+            oa.j = jj;
+            void *args[] = {&oa};
+            cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_orth<T, CW>, dim3(z.orth_grid),
+                                                        dim3(ORTH_THREADS), args, z.orth_smem, st);
+            ++c.launches;
+            if (e != cudaSuccess) {
+                c.err = std::string("nss_eigh: cooperative launch failed: ") + cudaGetErrorString(e);
+                return -1;
             }
         }
-        ++c.launches;
-        k_tridiag<<<1, 128, 0, st>>>(z.alpha, z.beta, jend, neigen, tol, z.theta, z.resid, z.svec, sstride,
-                                     z.flags, mmax, n);
-        cudaMemcpyAsync(z.h_flags + slot * F_NFLAGS, z.flags, F_NFLAGS * sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaEventRecord(evs[slot], st);
         return jend;
     };
+    std::vector<double> theta(4, 0.0), resid(4, 0.0), upper(4, 0.0), svec, work;
+    bool have_upper = false;
+    int m_done = 1, rc = NSS_OK, ne_done = 1;
+    bool converged = false;
     int slot = 0;
     int pend_end = enqueue_chunk(0, slot);
-    bool capped = false;
+    if (pend_end < 0) rc = NSS_ERR_CUDA;
     while (pend_end >= 0) {
         const int next_end = (pend_end < mmax) ? enqueue_chunk(pend_end, slot ^ 1) : -2;
         if (next_end == -1) { rc = NSS_ERR_CUDA; break; }
         cudaError_t ce = cudaEventSynchronize(evs[slot]);
         if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); rc = NSS_ERR_CUDA; break; }
-        const int *f = z.h_flags + slot * F_NFLAGS;
-        m_done = f[F_M];
-        if (f[F_STOP] == 1) { converged = true; break; }
-        if (f[F_STOP] == 3) { capped = true; break; }
-        if (f[F_STOP] == 2) {
+        // a breakdown inside this chunk ends it early; one flagged by the
+        // chunk running ahead belongs to the next check
+        int m = pend_end;
+        const bool brk = hf[F_STOP] == 2 && hf[F_BREAK] <= pend_end;
+        if (brk) m = hf[F_BREAK];
+        const int ne = std::min(neigen, m);
+        svec.resize((size_t)ne * m);
+        tridiag_lowest(ha, hb, m, ne, hb[m - 1], theta.data(), svec.data(), resid.data(),
+                       (have_upper && ne == neigen) ? upper.data() : nullptr, work);
+        for (int e = 0; e < ne; ++e) upper[e] = theta[e];
+        have_upper = ne == neigen;
+        int conv = 0;
+        for (int e = 0; e < ne; ++e)
+            if (resid[e] <= tol * std::max(std::fabs(theta[e]), 1e-300)) ++conv;
+        m_done = m;
+        ne_done = ne;
+        if (conv >= ne || (int64_t)m >= n) {
+            hf[F_NFLAGS] = 1;                        // stop request for the queued kernels
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            converged = true;
+            break;
+        }
+        if (brk) {
             // invariant subspace without convergence: continue from a random
             // vector orthogonal to V (the chunk run ahead has already exited)
             NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
@@ -607,34 +784,50 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             k_normalize<T><<<1, 1024, 0, st>>>(vn, n);
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+            hb[m_done - 1] = 0.0;
+            hf[F_STOP] = 0;
+            hf[F_BREAK] = 0;
             slot = 0;
             pend_end = enqueue_chunk(m_done, slot);
+            if (pend_end < 0) { rc = NSS_ERR_CUDA; break; }
             continue;
         }
-        if (next_end < 0) { capped = true; break; }
+        if (next_end < 0) break;   // iteration cap reached without convergence
         slot ^= 1;
         pend_end = next_end;
     }
-    cudaStreamSynchronize(st);
+    cudaError_t ce = cudaStreamSynchronize(st);
     cudaEventDestroy(evs[0]);
     cudaEventDestroy(evs[1]);
     if (rc) return rc;
-    (void)capped;
-    numop_ = m_done;
-    *numop_out = numop_;
+    if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
+    int dflags[F_NFLAGS];
+    NSS_CUDA_TRY(c, cudaMemcpy(dflags, z.flags, sizeof(dflags), cudaMemcpyDeviceToHost));
+    if (dflags[F_ERR]) {
+        c.err = "nss_eigh: a grid barrier of the orthogonalisation kernel timed out (results discarded)";
+        return NSS_ERR_CUDA;
+    }
+    *numop_out = m_done;
     *m_out = m_done;
     if (!converged) {
         c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(mmax) + " iterations";
         return NSS_ERR_NOCONV;
     }
-    const int ne = (int)std::min<int64_t>(neigen, m_done);
+    const int ne = ne_done;
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta, theta.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(z.resid, resid.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(z.svec, svec.data(), (size_t)ne * m_done * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
     ++c.launches;
-    k_ritz<T><<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(V, m_done, n, z.svec, sstride, ne, z.evecs);
+    k_ritz<T><<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(V, m_done, n, z.svec, m_done, ne, z.evecs);
     for (int e = 0; e < ne; ++e) {
         ++c.launches;
         k_normalize<double><<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());
+    // the pageable sources above are consumed before this returns
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
     return NSS_OK;
 }
 
@@ -646,6 +839,7 @@ void lanczos_release(Ctx &c) {
                     z.theta, z.resid, z.svec, z.flags};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
+    if (z.h_ab) cudaFreeHost(z.h_ab);
     z = DevLanczos{};
 }
 

@@ -224,11 +224,21 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
             else t.b_rp = at;
         }
     }
+    // Sectors on the tensor-core kernel get their A x B terms from "terms
+    // only" CUDA-core tiles (w = 1), listed first: k_hv_fp32 writes those
+    // terms to H psi and k_hv_tc, launched after it, adds its dense products.
     std::vector<int4> tiles32, tiles_tc;
     for (int k = 0; k < s.nsb; ++k) {
         if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
             for (int r = 0; r < s.dls[k]; r += TC_ROWS)
                 for (int cc = 0; cc < s.drs[k]; cc += TC_COLS) tiles_tc.push_back(make_int4(k, r, cc, 0));
+            for (int r = 0; r < s.dls[k]; r += TILE32)
+                for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 1));
+        }
+    }
+    for (int k = 0; k < s.nsb; ++k) {
+        if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
+            continue;
         } else {
             for (int r = 0; r < s.dls[k]; r += TILE32)
                 for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
@@ -360,8 +370,10 @@ __global__ void __launch_bounds__(256) k_hv_fp32(
     const float *HR = hrp + hr_off[k];
     const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
     float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    // a "terms only" tile (t.w = 1) skips the two dense products
+    const int kdl = (t.w & 1) ? 0 : dl, kdr = (t.w & 1) ? 0 : dr;
     // H_L W
-    for (int j0 = 0; j0 < dl; j0 += 32) {
+    for (int j0 = 0; j0 < kdl; j0 += 32) {
         for (int e = tid; e < TILE32 * 32; e += 256) {
             const int r = e / 32, cc = e % 32;
             const int gi = row0 + r, gj = j0 + cc;
@@ -381,7 +393,7 @@ __global__ void __launch_bounds__(256) k_hv_fp32(
         __syncthreads();
     }
     // W H_R^T
-    for (int j0 = 0; j0 < dr; j0 += 32) {
+    for (int j0 = 0; j0 < kdr; j0 += 32) {
         for (int e = tid; e < TILE32 * 32; e += 256) {
             const int r = e / 32, cc = e % 32;
             const int gi = row0 + r, gj = j0 + cc;

@@ -18,6 +18,8 @@
 // context stream (a library call; the sector blocks are small, < 600).
 #include "device.cuh"
 
+#include <cstdlib>
+
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -177,6 +179,137 @@ __global__ void k_umat(const double *rho /*eigenvector blocks*/, const int64_t *
     }
 }
 
+// Batched cyclic Jacobi eigensolver for the small rho blocks (n <= JAC_MAX):
+// one CTA per block, the block and its eigenvectors in shared memory.  Each
+// sweep visits all n(n-1)/2 pairs in n-1 rounds of n/2 disjoint rotations
+// (round-robin tournament), so a round's rotations are applied in parallel:
+// rows of A, then columns of A and of V.  Sweeps stop when the off-diagonal
+// Frobenius norm is below 1e-15 of the whole norm (quadratic convergence, a
+// handful of sweeps), at most JAC_SWEEPS.  Output as cuSOLVER's: eigenvalues
+// ascending, eigenvectors as the columns of a column-major block.
+constexpr int JAC_MAX = 64, JAC_SWEEPS = 24;
+
+// blocks up to this size take k_jacobi (env NSS_JACOBI_MAX, 0..JAC_MAX; 0
+// sends every block to the library eigensolver)
+int jacobi_max() {
+    static const int v = [] {
+        const char *e = std::getenv("NSS_JACOBI_MAX");
+        if (!e) return JAC_MAX;
+        const int x = std::atoi(e);
+        return x < 0 ? 0 : (x > JAC_MAX ? JAC_MAX : x);
+    }();
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_jacobi(double *rho, const int64_t *__restrict__ rho_off,
+                                                const int *__restrict__ dims, const int *__restrict__ ev_off,
+                                                const int *__restrict__ blocks, double *evals) {
+    extern __shared__ double jac_smem[];            // A and V: 2 x JAC_MAX x (JAC_MAX+1)
+    double(*A)[JAC_MAX + 1] = reinterpret_cast<double(*)[JAC_MAX + 1]>(jac_smem);
+    double(*V)[JAC_MAX + 1] = reinterpret_cast<double(*)[JAC_MAX + 1]>(jac_smem + JAC_MAX * (JAC_MAX + 1));
+    __shared__ double cs[JAC_MAX / 2][2];
+    __shared__ int pr[JAC_MAX / 2][2];
+    __shared__ double red[8][2];
+    __shared__ int perm[JAC_MAX];
+    const int q = blocks[blockIdx.x];
+    const int n = dims[q];
+    double *R = rho + rho_off[q];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        A[i][j] = R[e];
+        V[i][j] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    const int ne = n + (n & 1);          // even number of players (one dummy if n is odd)
+    for (int sweep = 0; sweep < JAC_SWEEPS && n > 1; ++sweep) {
+        // off-diagonal and total squared norms
+        double off = 0.0, tot = 0.0;
+        for (int e = tid; e < n * n; e += blockDim.x) {
+            const int i = e / n, j = e % n;
+            const double x = A[i][j] * A[i][j];
+            tot += x;
+            if (i != j) off += x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        }
+        if ((tid & 31) == 0) { red[tid >> 5][0] = off; red[tid >> 5][1] = tot; }
+        __syncthreads();
+        double offs = 0.0, tots = 0.0;
+        for (int w = 0; w < 8; ++w) { offs += red[w][0]; tots += red[w][1]; }
+        __syncthreads();
+        if (!(offs > 1e-30 * tots)) break;
+        for (int round = 0; round < ne - 1; ++round) {
+            // round-robin pairing: player 0 fixed, the others rotate
+            if (tid < ne / 2) {
+                const int a0 = (tid == 0) ? 0 : 1 + (tid - 1 + round) % (ne - 1);
+                const int b0 = 1 + (ne - 2 - tid + round) % (ne - 1);
+                int p = min(a0, b0), r = max(a0, b0);
+                double c = 1.0, sn = 0.0;
+                if (r < n && p != r) {
+                    const double apq = A[p][r];
+                    if (apq != 0.0) {
+                        const double th = (A[r][r] - A[p][p]) / (2.0 * apq);
+                        // t = tan of the rotation angle; 1/(2 th) where th*th would overflow
+                        const double t = fabs(th) > 1e150 ? 0.5 / th
+                                                          : (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                        c = 1.0 / sqrt(t * t + 1.0);
+                        sn = t * c;
+                    }
+                } else {
+                    p = r = -1;
+                }
+                pr[tid][0] = p;
+                pr[tid][1] = r;
+                cs[tid][0] = c;
+                cs[tid][1] = sn;
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int e = tid; e < (ne / 2) * n; e += blockDim.x) {
+                const int k = e / n, col = e % n;
+                const int p = pr[k][0], r = pr[k][1];
+                if (p < 0) continue;
+                const double c = cs[k][0], sn = cs[k][1];
+                const double ap = A[p][col], ar = A[r][col];
+                A[p][col] = c * ap - sn * ar;
+                A[r][col] = sn * ap + c * ar;
+            }
+            __syncthreads();
+            // columns: A <- A J and V <- V J
+            for (int e = tid; e < (ne / 2) * n; e += blockDim.x) {
+                const int k = e / n, row = e % n;
+                const int p = pr[k][0], r = pr[k][1];
+                if (p < 0) continue;
+                const double c = cs[k][0], sn = cs[k][1];
+                const double ap = A[row][p], ar = A[row][r];
+                A[row][p] = c * ap - sn * ar;
+                A[row][r] = sn * ap + c * ar;
+                const double vp = V[row][p], vr = V[row][r];
+                V[row][p] = c * vp - sn * vr;
+                V[row][r] = sn * vp + c * vr;
+            }
+            __syncthreads();
+        }
+    }
+    // ascending order of the eigenvalues (ties: lower index first)
+    for (int i = tid; i < n; i += blockDim.x) {
+        const double x = A[i][i];
+        int rnk = 0;
+        for (int j = 0; j < n; ++j) rnk += (A[j][j] < x) || (A[j][j] == x && j < i);
+        perm[rnk] = i;
+    }
+    __syncthreads();
+    double *ev = evals + ev_off[q];
+    for (int e = tid; e < n * n; e += blockDim.x) {
+        const int col = e / n, row = e % n;         // column-major output
+        R[e] = V[row][perm[col]];
+        if (row == 0) ev[col] = A[perm[col]][perm[col]];
+    }
+}
+
 int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
     if (*p && cap >= need) return NSS_OK;
     ctx_free(c, *p);
@@ -266,9 +399,10 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, st));
         return NSS_OK;
     };
+    int *jac_tmp = nullptr;
     auto cleanup = [&]() {
         cudaStreamSynchronize(st);
-        void *ptrs[] = {d_items, d_rho_off, d_dims, d_ev_off, d_maps, d_map_off};
+        void *ptrs[] = {d_items, d_rho_off, d_dims, d_ev_off, d_maps, d_map_off, jac_tmp};
         for (void *p : ptrs) ctx_free(c, p);
     };
     if ((rc = up(&d_items, items)) || (rc = up(&d_rho_off, rho_off)) || (rc = up(&d_dims, dims)) ||
@@ -307,10 +441,22 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // so they run on NSIDE streams at once (largest first, round robin).
     NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
     for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
-    std::vector<int> by_size(2 * nsb);
-    for (int q = 0; q < 2 * nsb; ++q) by_size[q] = q;
+    // small blocks: one batched Jacobi launch on the main stream, concurrent
+    // with the library eigensolves of the large blocks on the side streams
+    std::vector<int> small, by_size;
+    const int jmax = jacobi_max();
+    for (int q = 0; q < 2 * nsb; ++q) (dims[q] <= jmax ? small : by_size).push_back(q);
+    if (!small.empty()) {
+        NSS_CUDA_TRY(c, ctx_alloc(c, &jac_tmp, small.size()));
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(jac_tmp, small.data(), small.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        constexpr int jac_smem = 2 * JAC_MAX * (JAC_MAX + 1) * (int)sizeof(double);
+        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, jac_smem));
+        ++c.launches;
+        k_jacobi<<<(int)small.size(), 256, jac_smem, st>>>(r.rho, d_rho_off, d_dims, d_ev_off, jac_tmp, r.evals);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
     std::sort(by_size.begin(), by_size.end(), [&](int a, int b) { return dims[a] > dims[b]; });
-    for (int i = 0; i < 2 * nsb; ++i) {
+    for (int i = 0; i < (int)by_size.size(); ++i) {
         const int q = by_size[i], sid = i % DevRdm::NSIDE;
         const int d = dims[q];
         cusolverDnSetStream(h, r.side[sid]);
