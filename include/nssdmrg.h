@@ -176,6 +176,15 @@ int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *
 int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b_last,
                        double *theta, double *s, double *resid);
 
+/* Lowest eigenpair of the (k+1)x(k+1) matrix [[theta0, m^T], [m, T]] with T
+ * tridiagonal (diagonal a[0..k), off-diagonal b[0..k-1)), on the host: the
+ * small problem of the FP64-anchored refinement that nss_eigh's mixed
+ * precision runs after its FP32 phase (no counterpart in the reference,
+ * whose Lanczos is FP64 throughout).  Outputs *lam, c[k+1] (unit norm,
+ * c[0] > 0) and *resid = |b_last * c[k]|.  Needs no context and no GPU. */
+int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, const double *b, double b_last,
+                     double *lam, double *c, double *resid);
+
 /* ---------------------------------------------------------------------------
  * Block-level superblock setup (the enumeration and operator-pool build of
  * sb_get_states / sb_build_dims / Setup_SuperBlock_{Spin,Fermion}_Direct,

@@ -117,6 +117,7 @@ def lib():
         "nss_hv_device_f32": (C.c_int, [P, I64, P, P]),
         "nss_sb_energy_noalloc": (C.c_int, [P, I64, P, C.POINTER(D)]),
         "nss_tridiag_lowest": (C.c_int, [C.c_int, P, P, C.c_int, D, P, P, P]),
+        "nss_arrow_lowest": (C.c_int, [C.c_int, D, P, P, P, D, C.POINTER(D), P, C.POINTER(D)]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
@@ -162,6 +163,23 @@ def tridiag_lowest(a, b, ne: int = 1, b_last: float = 0.0):
     if rc != 0:
         raise NssError(rc, lib().nss_last_error(None).decode())
     return theta, s, resid
+
+
+def arrow_lowest(theta0: float, m, a, b, b_last: float = 0.0):
+    """Lowest eigenpair of [[theta0, m^T], [m, tridiag(a, b)]] with the host
+    solver of the mixed-precision refinement.  Returns (lam, c, resid)."""
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    k = a.size
+    lam = C.c_double(0.0)
+    res = C.c_double(0.0)
+    c = np.zeros(k + 1)
+    rc = lib().nss_arrow_lowest(k, float(theta0), _ptr(m) if k else None, _ptr(a) if k else None,
+                                _ptr(b) if b.size else None, float(b_last), C.byref(lam), _ptr(c), C.byref(res))
+    if rc != 0:
+        raise NssError(rc, lib().nss_last_error(None).decode())
+    return lam.value, c, res.value
 
 
 class _Keep:

@@ -193,6 +193,20 @@ int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b
     return NSS_OK;
 }
 
+int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, const double *b, double b_last,
+                     double *lam, double *c, double *resid) {
+    if (k < 0 || (k > 0 && (!m || !a || (k > 1 && !b))) || !lam || !c || !resid) {
+        g_err = "nss_arrow_lowest: need k >= 0 and non-NULL arrays";
+        return NSS_ERR_INVALID;
+    }
+    std::vector<double> work;
+    if (!nss::arrow_lowest(theta0, m, a, b, k, b_last, lam, c, resid, work)) {
+        g_err = "nss_arrow_lowest: no root below the tridiagonal spectrum";
+        return NSS_ERR_NOCONV;
+    }
+    return NSS_OK;
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

@@ -85,7 +85,8 @@ struct DevLanczos {
     double *theta = nullptr, *resid = nullptr, *svec = nullptr; // tridiagonal results
     int *flags = nullptr;        // device flags
     int *h_flags = nullptr;      // host-mapped flag mirror + the host's stop request
-    double *h_ab = nullptr;      // host-mapped mirror of alpha [cap+1], beta [cap+1]
+    double *h_ab = nullptr;      // host-mapped mirror of alpha, beta, anchor couplings ([cap+1] each)
+    double last_anchor_theta = 0.0;
     int *d_h_flags = nullptr;    // device addresses of the two mapped buffers
     double *d_h_ab = nullptr;
     int orth_grid = 0;           // CTAs of the cooperative orthogonalisation kernel

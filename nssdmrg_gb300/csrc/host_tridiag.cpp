@@ -238,3 +238,94 @@ void tridiag_lowest(const double *a, const double *b, int m, int ne, double b_la
 }
 
 }  // namespace nss
+
+namespace nss {
+
+namespace {
+
+// y = (T - lam I)^{-1} m for T - lam I positive definite (LDL^T, no pivoting);
+// returns false when a pivot is not positive (lam not below lambda_min(T))
+bool spd_solve(const double *a, const double *b, int k, double lam, const double *m, double *y, double *d) {
+    for (int i = 0; i < k; ++i) {
+        double di = a[i] - lam;
+        if (i > 0) di -= b[i - 1] * b[i - 1] / d[i - 1];
+        if (!(di > 0.0)) return false;
+        d[i] = di;
+    }
+    // forward: z_i = m_i - (b_{i-1}/d_{i-1}) z_{i-1}
+    for (int i = 0; i < k; ++i) y[i] = m[i] - (i > 0 ? b[i - 1] / d[i - 1] * y[i - 1] : 0.0);
+    // diagonal and backward: y_i = z_i/d_i - (b_i/d_i) y_{i+1}
+    for (int i = k - 1; i >= 0; --i) y[i] = y[i] / d[i] - (i + 1 < k ? b[i] / d[i] * y[i + 1] : 0.0);
+    return true;
+}
+
+}  // namespace
+
+bool arrow_lowest(double theta0, const double *m, const double *a, const double *b, int k, double b_last,
+                  double *lam, double *c, double *resid, std::vector<double> &work) {
+    c[0] = 1.0;
+    if (k <= 0) {
+        *lam = theta0;
+        *resid = 0.0;
+        return true;
+    }
+    work.resize((size_t)4 * k + 16);
+    double *y = work.data(), *d = y + k, *tw = d + k;
+    // upper end of the bracket: min(theta0, lambda_min(T)), the latter by
+    // the tridiagonal solver (its eigenvector scratch in tw)
+    double tmin = 0.0, tres = 0.0;
+    std::vector<double> w2;
+    std::vector<double> s1((size_t)k);
+    tridiag_lowest(a, b, k, 1, 0.0, &tmin, s1.data(), &tres, nullptr, w2);
+    double hi = std::min(theta0, tmin);
+    // lower end: Gershgorin bound of M
+    double msum = 0.0;
+    for (int i = 0; i < k; ++i) msum += std::fabs(m[i]);
+    double lo = theta0 - msum;
+    for (int i = 0; i < k; ++i) {
+        const double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < k ? std::fabs(b[i]) : 0.0) + std::fabs(m[i]);
+        lo = std::min(lo, a[i] - r);
+    }
+    const double scale = std::max({std::fabs(lo), std::fabs(hi), DBL_MIN});
+    lo -= 4.0 * EPS * scale;
+    // step just below hi so that T - lam I stays definite
+    double x = hi - std::max(1e-12 * scale, 4.0 * EPS * scale);
+    if (x <= lo) x = 0.5 * (lo + hi);
+    (void)tw;
+    bool ok = false;
+    for (int it = 0; it < 200; ++it) {
+        if (!spd_solve(a, b, k, x, m, y, d)) {   // above lambda_min(T): move down
+            hi = x;
+            x = 0.5 * (lo + hi);
+            continue;
+        }
+        double my = 0.0, yy = 0.0;
+        for (int i = 0; i < k; ++i) {
+            my += m[i] * y[i];
+            yy += y[i] * y[i];
+        }
+        const double f = theta0 - x - my;
+        if (f > 0.0) lo = x;
+        else hi = x;
+        const double step = f / (1.0 + yy);      // Newton: f' = -(1 + y.y)
+        double xn = x + step;
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const double dx = std::fabs(xn - x);
+        x = xn;
+        if (dx <= 2.0 * EPS * std::fabs(x) || hi - lo <= 4.0 * EPS * std::fabs(x)) {
+            ok = spd_solve(a, b, k, x, m, y, d);
+            break;
+        }
+    }
+    if (!ok) return false;
+    double nn = 1.0;
+    for (int i = 0; i < k; ++i) nn += y[i] * y[i];
+    const double inv = 1.0 / std::sqrt(nn);
+    c[0] = inv;
+    for (int i = 0; i < k; ++i) c[i + 1] = -y[i] * inv;
+    *lam = x;
+    *resid = std::fabs(b_last * c[k]);
+    return true;
+}
+
+}  // namespace nss

@@ -26,4 +26,17 @@ namespace nss {
 void tridiag_lowest(const double *a, const double *b, int m, int ne, double b_last, double *theta,
                     double *s, double *resid, const double *upper, std::vector<double> &work);
 
+// Lowest eigenpair of the (k+1) x (k+1) "arrowhead + tridiagonal" matrix
+//     M = [ theta0  m^T ]
+//         [ m       T   ]     T = tridiag(a[0..k), b[0..k-1))
+// that the anchored refinement of the mixed-precision Lanczos produces (row 0
+// is the FP64 anchor vector, rows 1.. its FP32 Krylov complement).  The root
+// lam < min(theta0, lambda_min(T)) of the secular equation
+//     f(lam) = theta0 - lam - m^T (T - lam)^{-1} m = 0
+// by safeguarded Newton (T - lam I is positive definite there, so LDL^T
+// needs no pivoting); c[0] = 1, c[1..] = -(T - lam)^{-1} m, normalised.
+// resid = |b_last * c[k]|.  Returns false when no root is bracketed.
+bool arrow_lowest(double theta0, const double *m, const double *a, const double *b, int k, double b_last,
+                  double *lam, double *c, double *resid, std::vector<double> &work);
+
 }  // namespace nss

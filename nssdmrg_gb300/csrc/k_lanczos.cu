@@ -244,7 +244,15 @@ struct OrthArgs {
     int *flags;                  // device flags
     double *h_alpha, *h_beta;    // host-mapped mirrors of alpha, beta
     int *h_flags;                // host-mapped flag mirror + stop request
+    // anchored refinement (anc_u == nullptr: plain Lanczos): the Krylov
+    // vectors are kept orthogonal to the FP64 anchor u and to ndefl FP64
+    // vectors defl[k*n..]; m_j = r . v_j (r = H u - theta0 u) goes to h_m[j]
+    const double *anc_u, *anc_r, *defl;
+    int ndefl;
+    double *h_m;
 };
+
+constexpr int PA_COLS = 8;       // per-CTA values of the first phase (alpha, u.w, r.v, y_k.w)
 
 // Grid-wide barrier for a cooperative launch (all CTAs resident).  Bounded:
 // a wait that runs out sets flags[F_ERR] and every later barrier returns
@@ -443,16 +451,38 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     const int j = a.j, m = j + 1;
     const T *vj = V + (int64_t)j * n;
     const T *vjm = V + (int64_t)(j > 0 ? j - 1 : 0) * n;
-    double *pA = a.part, *pH = pA + G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G, *pB2 = pH2 + (int64_t)ps * G;
+    double *pA = a.part, *pH = pA + PA_COLS * G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G,
+           *pB2 = pH2 + (int64_t)ps * G;
     int *err = flags + F_ERR;
+    const bool anc = a.anc_u != nullptr;
+    const int nd = anc ? a.ndefl : 0;
 
     // the host's stop request, published by CTA 0 before the first barrier
     if (blk == 0 && tid == 0) flags[F_HOST] = *(volatile const int *)(a.h_flags + F_NFLAGS);
-    {   // alpha = v_j . w
+    {   // alpha = v_j . w; anchored also u.w, r.v_j and y_k.w
         T p = (T)0;
-        for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) p += vj[i] * w[i];
-        const double t = block_sum((double)p, scr);
+        double pu = 0.0, pr = 0.0, py[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+            const T wi = w[i], vi = vj[i];
+            p += vi * wi;
+            if (anc) {
+                pu += a.anc_u[i] * (double)wi;
+                pr += a.anc_r[i] * (double)vi;
+                for (int k = 0; k < nd; ++k) py[k] += a.defl[(int64_t)k * n + i] * (double)wi;
+            }
+        }
+        double t = block_sum((double)p, scr);
         if (tid == 0) pA[blk] = t;
+        if (anc) {
+            t = block_sum(pu, scr);
+            if (tid == 0) pA[G + blk] = t;
+            t = block_sum(pr, scr);
+            if (tid == 0) pA[2 * G + blk] = t;
+            for (int k = 0; k < nd; ++k) {
+                t = block_sum(py[k], scr);
+                if (tid == 0) pA[(3 + k) * G + blk] = t;
+            }
+        }
     }
     if (!grid_sync(a.bar, err)) return;
     if (__ldcg(&flags[F_HOST])) {
@@ -460,12 +490,24 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         return;
     }
     const double alpha0 = grid_total(pA, G, scr + 32);
-    {   // three-term step, then h = V_m^T w and ww = w.w
+    double cu = 0.0, cy[4] = {0.0, 0.0, 0.0, 0.0};
+    if (anc) {
+        cu = grid_total(pA + G, G, scr + 33);
+        const double cr = grid_total(pA + 2 * G, G, scr + 34);
+        for (int k = 0; k < nd; ++k) cy[k] = grid_total(pA + (3 + k) * G, G, scr + 35 + k);
+        if (blk == 0 && tid == 0) a.h_m[j] = cr;
+    }
+    {   // three-term step (and the anchor projections), then h = V_m^T w and ww = w.w
         const T a3 = (T)alpha0;
         const T b3 = j > 0 ? (T)a.beta[j - 1] : (T)0;
         for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
             T x = w[i] - a3 * vj[i];
             if (j > 0) x -= b3 * vjm[i];
+            if (anc) {
+                double q = cu * a.anc_u[i];
+                for (int k = 0; k < nd; ++k) q += cy[k] * a.defl[(int64_t)k * n + i];
+                x -= (T)q;
+            }
             w[i] = x;
         }
         __syncthreads();
@@ -594,6 +636,40 @@ __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ psi, c
     *counter = 0u;
 }
 
+// Anchor residual: w <- w - theta0 psi with theta0 = r[0]/r[2] (from k_rq),
+// and r[4] = ||w||^2 (grid reduction)
+__global__ void __launch_bounds__(256) k_anchor_r(const double *__restrict__ psi, double *__restrict__ w, int64_t n,
+                                                  double *__restrict__ part, double *__restrict__ r, unsigned *counter) {
+    const int tid = threadIdx.x;
+    const double th = r[0] / r[2];
+    double a = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double d = w[i] - th * psi[i];
+        w[i] = d;
+        a = fma(d, d, a);
+    }
+    a = warp_sum<double>(a);
+    __shared__ double red[8];
+    if ((tid & 31) == 0) red[tid >> 5] = a;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += red[q];
+        part[blockIdx.x] = t;
+    }
+    if (!last_block(counter) || tid != 0) return;
+    double t = 0.0;
+    for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[bb];
+    r[4] = t;
+    *counter = 0u;
+}
+
+// out = (float)(x * s)
+__global__ void k_to32(float *__restrict__ out, const double *__restrict__ x, double s, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)(x[i] * s);
+}
+
 // per-eigenvector scratch row of svec
 inline int svec_stride(int cap) { return 4 * (cap + 1); }
 
@@ -635,7 +711,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));
     // scalars, projection coefficients, restart scratch alpha/beta, refinement
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.scal, (size_t)S_NSCAL + 4 * (cap + 2) + 8));
-    const size_t part = std::max((size_t)(cap + 2) * NBLK, (size_t)(2 * pstride + 3) * (size_t)nsm);
+    const size_t part = std::max((size_t)(cap + 2) * NBLK, (size_t)(2 * pstride + PA_COLS + 2) * (size_t)nsm);
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.part, part));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.counter, 4));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.alpha, (size_t)cap + 1));
@@ -644,8 +720,8 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.resid, 8));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.svec, (size_t)4 * svec_stride(cap)));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.flags, F_NFLAGS));
-    // host-mapped mirrors: alpha, beta; flags + the host's stop request
-    NSS_CUDA_TRY(c, cudaHostAlloc((void **)&z.h_ab, 2 * (size_t)(cap + 1) * sizeof(double), cudaHostAllocMapped));
+    // host-mapped mirrors: alpha, beta, anchor couplings m; flags + the host's stop request
+    NSS_CUDA_TRY(c, cudaHostAlloc((void **)&z.h_ab, 3 * (size_t)(cap + 1) * sizeof(double), cudaHostAllocMapped));
     NSS_CUDA_TRY(c, cudaHostAlloc((void **)&z.h_flags, (F_NFLAGS + 8) * sizeof(int), cudaHostAllocMapped));
     NSS_CUDA_TRY(c, cudaHostGetDevicePointer((void **)&z.d_h_ab, z.h_ab, 0));
     NSS_CUDA_TRY(c, cudaHostGetDevicePointer((void **)&z.d_h_flags, z.h_flags, 0));
@@ -660,11 +736,37 @@ int hv_t<double>(Ctx &c, const double *v, double *hv, const int *stop) { return 
 template <>
 int hv_t<float>(Ctx &c, const float *v, float *hv, const int *stop) { return hv_device_fp32(c, v, hv, stop); }
 
+// Anchored refinement of one eigenvector (mixed precision, second phase):
+// the FP64 anchor u with theta0 = u.H.u and r = H u - theta0 u; the caller
+// has put r/|r| (FP32) into V[0].  The result c0 u + sum_l c_l V[l] goes to
+// `out` (may alias u).
+struct AnchorSpec {
+    const double *u, *r, *defl;
+    int ndefl;
+    double theta0;
+    double *out;
+};
+
+// out = c[0] u + sum_l c[l+1] V[l]   (FP64 accumulation)
+template <class T>
+__global__ void __launch_bounds__(256) k_ritz_anchor(const T *__restrict__ V, int m, int64_t n,
+                                                     const double *__restrict__ cvec, const double *u, double *out) {
+    extern __shared__ double cs[];   // [m+1]
+    for (int t = threadIdx.x; t <= m; t += blockDim.x) cs[t] = cvec[t];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = cs[0] * u[i];
+        for (int l = 0; l < m; ++l) acc = fma((double)V[(int64_t)l * n + i], cs[l + 1], acc);
+        out[i] = acc;
+    }
+}
+
 // The Lanczos iterations on a basis of type T; leaves theta (Ritz values),
 // svec (their T_m eigenvectors, stride m) and the Ritz vectors (FP64) in c.lz.
+// With `anc` it runs the anchored refinement instead (one eigenvector).
 template <class T>
 int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t seed, int *numop_out,
-                int *m_out) {
+                int *m_out, const AnchorSpec *anc = nullptr) {
     DevLanczos &z = c.lz;
     const int64_t n = c.sb.n;
     const int cap = z.cap;
@@ -681,10 +783,14 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     NSS_CUDA_TRY(c, cudaMemsetAsync(z.counter, 0, 4 * sizeof(unsigned), st));
     const int vb = 608;   // 4 CTAs per SM for elementwise kernels
     uint64_t restarts = 0;
-    ++c.launches;
-    k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
-    ++c.launches;
-    k_normalize<T><<<1, 1024, 0, st>>>(V, n);
+    if (anc) {
+        neigen = 1;
+    } else {
+        ++c.launches;
+        k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
+        ++c.launches;
+        k_normalize<T><<<1, 1024, 0, st>>>(V, n);
+    }
     const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
     const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
     if (dots_smem > 48 * 1024)
@@ -707,6 +813,13 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     oa.h_alpha = z.d_h_ab;
     oa.h_beta = z.d_h_ab + (cap + 1);
     oa.h_flags = z.d_h_flags;
+    oa.anc_u = anc ? anc->u : nullptr;
+    oa.anc_r = anc ? anc->r : nullptr;
+    oa.defl = anc ? anc->defl : nullptr;
+    oa.ndefl = anc ? anc->ndefl : 0;
+    oa.h_m = z.d_h_ab + 2 * (cap + 1);
+    const double *hm = z.h_ab + 2 * (cap + 1);
+    std::vector<double> cvec;
     // Chunks of CHECK iterations, each ending with an event; the host checks
     // chunk k on T_m while the GPU runs chunk k+1.
     cudaEvent_t evs[2];
@@ -747,14 +860,25 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         const bool brk = hf[F_STOP] == 2 && hf[F_BREAK] <= pend_end;
         if (brk) m = hf[F_BREAK];
         const int ne = std::min(neigen, m);
-        svec.resize((size_t)ne * m);
-        tridiag_lowest(ha, hb, m, ne, hb[m - 1], theta.data(), svec.data(), resid.data(),
-                       (have_upper && ne == neigen) ? upper.data() : nullptr, work);
-        for (int e = 0; e < ne; ++e) upper[e] = theta[e];
-        have_upper = ne == neigen;
         int conv = 0;
-        for (int e = 0; e < ne; ++e)
-            if (resid[e] <= tol * std::max(std::fabs(theta[e]), 1e-300)) ++conv;
+        if (anc) {
+            // lowest eigenpair of [[theta0, m^T], [m, T_m]]
+            cvec.resize((size_t)m + 1);
+            double lam = 0.0, res = 0.0;
+            if (arrow_lowest(anc->theta0, hm, ha, hb, m, hb[m - 1], &lam, cvec.data(), &res, work)) {
+                theta[0] = lam;
+                resid[0] = res;
+                if (res <= tol * std::max(std::fabs(lam), 1e-300) || brk) conv = 1;
+            }
+        } else {
+            svec.resize((size_t)ne * m);
+            tridiag_lowest(ha, hb, m, ne, hb[m - 1], theta.data(), svec.data(), resid.data(),
+                           (have_upper && ne == neigen) ? upper.data() : nullptr, work);
+            for (int e = 0; e < ne; ++e) upper[e] = theta[e];
+            have_upper = ne == neigen;
+            for (int e = 0; e < ne; ++e)
+                if (resid[e] <= tol * std::max(std::fabs(theta[e]), 1e-300)) ++conv;
+        }
         m_done = m;
         ne_done = ne;
         if (conv >= ne || (int64_t)m >= n) {
@@ -814,6 +938,20 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(mmax) + " iterations";
         return NSS_ERR_NOCONV;
     }
+    if (anc) {
+        if (cvec.size() != (size_t)m_done + 1) {
+            c.err = "nss_eigh: the anchored refinement found no eigenpair";
+            return NSS_ERR_NOCONV;
+        }
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(z.svec, cvec.data(), cvec.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        c.launches += 2;
+        k_ritz_anchor<T><<<NBLK, 256, cvec.size() * sizeof(double), st>>>(V, m_done, n, z.svec, anc->u, anc->out);
+        k_normalize<double><<<1, 1024, 0, st>>>(anc->out, n);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        z.last_anchor_theta = theta[0];
+        return NSS_OK;
+    }
     const int ne = ne_done;
     NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta, theta.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
     NSS_CUDA_TRY(c, cudaMemcpyAsync(z.resid, resid.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -871,7 +1009,66 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     }
     const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
     if (!rc && mixed) {
-        // FP64 refinement of each eigenvalue: theta = psi.H.psi / psi.psi with
+        // Anchored refinement of each Ritz vector: FP64 anchor u (deflated
+        // against the vectors already refined), r = H u - theta0 u in FP64,
+        // then FP32 Lanczos on the complement of u started from r/|r|, with
+        // the couplings u.H.v = r.v in FP64; the small matrix is solved on the
+        // host.  The FP32 errors then only touch the correction (|r|/gap), so
+        // the vector comes out at FP64 quality.
+        double *r = z.scal + S_NSCAL + 4 * (z.cap + 2);   // 8 refinement slots
+        double *h1 = z.scal + S_NSCAL;
+        double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
+        const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(double);
+        const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
+        if (dots_smem > 48 * 1024)
+            cudaFuncSetAttribute(k_dots<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
+        if (upd_smem > 48 * 1024)
+            cudaFuncSetAttribute(k_update<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+        // w -= Y (Y^T w) against the e vectors already refined; returns via scal[S_BB]
+        auto deflate = [&](double *vec, int e) -> int {
+            NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+            NSS_CUDA_TRY(c, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
+            c.launches += 2;
+            k_dots<double><<<NBLK, 256, dots_smem, st>>>(z.evecs, e, vec, n, z.part, h1, z.scal, z.counter, z.flags,
+                                                         0, 0, z.beta);
+            k_update<double><<<NBLK, 256, upd_smem, st>>>(z.evecs, e, vec, n, h1, z.part, z.scal, z.counter, z.flags,
+                                                          rs_alpha, rs_beta, 0);
+            return NSS_OK;
+        };
+        for (int e = 0; e < ne && !rc; ++e) {
+            double *u = z.evecs + (int64_t)e * n;
+            if (e > 0) {
+                if ((rc = deflate(u, e))) break;
+                ++c.launches;
+                k_normalize<double><<<1, 1024, 0, st>>>(u, n);
+            }
+            if ((rc = hv_device(c, u, z.w))) break;
+            ++numop_;
+            c.launches += 2;
+            k_rq<<<NBLK, 256, 0, st>>>(u, z.w, n, z.part, r, z.counter);
+            k_anchor_r<<<NBLK, 256, 0, st>>>(u, z.w, n, z.part, r, z.counter);
+            double hr[8];
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(hr, r, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+            const double theta0 = hr[0] / hr[2];
+            double rr = hr[4];
+            if (e > 0) {
+                if ((rc = deflate(z.w, e))) break;
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(&rr, z.scal + S_BB, sizeof(double), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+            }
+            const double beta0 = std::sqrt(std::max(rr, 0.0));
+            if (!(beta0 > tol * std::fabs(theta0))) continue;   // the anchor is converged already
+            ++c.launches;
+            k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, n);
+            AnchorSpec as{u, z.w, z.evecs, e, theta0, u};
+            int it2 = 0, m2 = 0;
+            rc = run_lanczos<float>(c, z.V32, z.w32, 1, mmax, tol, seed, &it2, &m2, &as);
+            numop_ += it2;
+        }
+    }
+    if (!rc && mixed) {
+        // FP64 energy of each eigenvector: theta = psi.H.psi / psi.psi with
         // the FP64 H*psi, and the FP64 residual ||H psi - theta psi||.
         double *r = z.scal + S_NSCAL + 4 * (z.cap + 2);   // 8 refinement slots
         for (int e = 0; e < ne; ++e) {

@@ -82,3 +82,48 @@ def test_scaled_extremes():
 def test_invalid_arguments():
     with pytest.raises(nss.NssError):
         nss.tridiag_lowest(np.zeros(3), np.zeros(2), ne=4)
+
+
+def _arrow_dense(theta0, m, a, b):
+    k = a.size
+    M = np.zeros((k + 1, k + 1))
+    M[0, 0] = theta0
+    M[0, 1:] = m
+    M[1:, 0] = m
+    M[1:, 1:] = np.diag(a) + np.diag(b, 1) + np.diag(b, -1)
+    return M
+
+
+@pytest.mark.parametrize("k", [0, 1, 5, 60, 200])
+def test_arrowhead_refinement_matrix(k):
+    """The small problem of the anchored refinement: an FP64 anchor (row 0)
+    close to the ground state, coupled by a small m to its Krylov
+    complement."""
+    rng = np.random.default_rng(k + 11)
+    theta0 = -20.0
+    a = rng.uniform(-15.0, 5.0, k)
+    b = np.abs(rng.standard_normal(max(k - 1, 0)))
+    m = rng.standard_normal(k) * 1e-6
+    if k:
+        m[0] = 3e-6
+    lam, c, resid = nss.arrow_lowest(theta0, m, a, b, 0.25)
+    M = _arrow_dense(theta0, m, a, b)
+    w, v = np.linalg.eigh(M)
+    assert lam == pytest.approx(w[0], rel=1e-15, abs=1e-14)
+    ref = v[:, 0] * np.sign(v[0, 0])
+    assert np.abs(c - ref).max() < 1e-12
+    assert abs(np.linalg.norm(c) - 1.0) < 1e-14
+    if k:
+        assert resid == pytest.approx(0.25 * abs(c[-1]), rel=1e-14, abs=1e-300)
+
+
+def test_arrowhead_strong_coupling():
+    rng = np.random.default_rng(5)
+    k = 40
+    a = rng.uniform(-2.0, 2.0, k)
+    b = np.abs(rng.standard_normal(k - 1))
+    m = rng.standard_normal(k)
+    lam, c, _ = nss.arrow_lowest(0.5, m, a, b)
+    w, v = np.linalg.eigh(_arrow_dense(0.5, m, a, b))
+    assert lam == pytest.approx(w[0], rel=1e-13)
+    assert np.abs(np.abs(c) - np.abs(v[:, 0])).max() < 1e-10
