@@ -74,6 +74,7 @@ struct DevLanczos {
     double *w = nullptr;         // [n]
     float *V32 = nullptr;        // [cap][n] mixed-precision basis (lazily)
     float *w32 = nullptr;        // [n]
+    float *anc32 = nullptr;      // [6][n] FP32 anchor, residual, deflation vectors (mixed)
     double last_resid[4] = {0, 0, 0, 0};   // FP64 residual norms of the last solve
     int last_iters = 0;
     double *evecs = nullptr;     // [neigen][n] Ritz vectors (last solve)
@@ -108,6 +109,11 @@ struct DevRdm {
     cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
     double *scal = nullptr;
     int *iscal = nullptr;
+    double *bat = nullptr;       // batched eigensolve pool: padded blocks, eigenvalues, workspaces
+    int64_t cap_bat = 0;
+    int *bat_info = nullptr;
+    int64_t cap_bat_info = 0;
+    void *params = nullptr;      // cusolverDnParams_t
 };
 
 struct Ctx {

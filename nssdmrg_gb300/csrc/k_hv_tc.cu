@@ -230,15 +230,30 @@ __global__ void __launch_bounds__(TC_THREADS) k_hv_tc(
     }
     __syncthreads();
     if (ok_s) {
+        // warp w owns rows w, w+4, ..., lanes columns lane and lane+32; the
+        // terms already in H psi are read eight rows at a time, so those loads
+        // are in flight together
         float *out = hv + off[k];
-        for (int rr = w; rr < TC_M; rr += TC_THREADS / 32) {
-            const int il = row0 + rr;
-            if (il >= dl) break;
-            for (int cc = lane; cc < TC_BN; cc += 32) {
-                const int ir = col0 + cc;
-                if (ir >= dr) continue;
-                const int64_t idx = (int64_t)il * dr + ir;
-                out[idx] = Dsm[rr * (TC_BN + 1) + cc] + out[idx];
+        constexpr int RB = 8;
+        for (int r0 = w; r0 < TC_M; r0 += 4 * RB) {
+            float x[RB][2];
+#pragma unroll
+            for (int q = 0; q < RB; ++q) {
+                const int il = row0 + r0 + 4 * q;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int ir = col0 + lane + 32 * h;
+                    x[q][h] = (il < dl && ir < dr) ? __ldcg(out + (int64_t)il * dr + ir) : 0.f;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < RB; ++q) {
+                const int rr = r0 + 4 * q, il = row0 + rr;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int cc = lane + 32 * h, ir = col0 + cc;
+                    if (il < dl && ir < dr) out[(int64_t)il * dr + ir] = Dsm[rr * (TC_BN + 1) + cc] + x[q][h];
+                }
             }
         }
     }

@@ -53,6 +53,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -64,6 +65,18 @@ constexpr int NBLK = 304;         // grid of the restart-path reductions
 constexpr int CHECK = 4;          // convergence test period (iterations)
 constexpr int SUB = 1024;         // rows staged per shared-memory sub-chunk
 constexpr double MIXED_TOL = 1e-7;
+
+// residual target of the FP32 phase (env NSS_MIXED_TOL overrides, clamped to
+// [1e-9, 1e-2]); the anchored FP64 phase then takes the vector to `tol`
+double mixed_tol() {
+    static const double v = [] {
+        const char *e = std::getenv("NSS_MIXED_TOL");
+        if (!e) return MIXED_TOL;
+        const double x = std::atof(e);
+        return x < 1e-9 ? 1e-9 : (x > 1e-2 ? 1e-2 : x);
+    }();
+    return v;
+}
 constexpr int ORTH_THREADS = 512;
 constexpr int ORTH_WARPS = ORTH_THREADS / 32;
 constexpr uint32_t BAR_SPIN = 1u << 24;   // grid-barrier poll limit (~1 s)
@@ -233,21 +246,28 @@ __global__ void __launch_bounds__(1024) k_normalize(T *x, int64_t n) {
 
 // ---------------------------------------------------------------------------
 // Fused orthogonalisation step (cooperative launch).
+//
+// Reductions are carried out in the basis type T: FP32 for the mixed
+// method, FP64 for the plain one.  On GB300 an FP64 add or FMA occupies a
+// warp's share of the FP64 pipe for 64 cycles (a division ~650), so FP64
+// reduction trees inside the FP32 method would cost more than the FP32
+// vector work they sum; FP32 sums are as accurate as the FP32 vectors and
+// the FP32 products they add up.
 
 struct OrthArgs {
     void *V, *w;                 // T*: basis [cap+1][n], work vector [n]
     int64_t n;
     int j, mmax, pstride;        // step, iteration cap, column stride of partials
     double *alpha, *beta;        // device tridiagonal coefficients
-    double *part;                // per-CTA partials (five regions)
+    void *part;                  // T*: per-CTA partials (five regions)
     unsigned *bar;               // grid barrier: arrival count, generation
     int *flags;                  // device flags
     double *h_alpha, *h_beta;    // host-mapped mirrors of alpha, beta
     int *h_flags;                // host-mapped flag mirror + stop request
-    // anchored refinement (anc_u == nullptr: plain Lanczos): the Krylov
-    // vectors are kept orthogonal to the FP64 anchor u and to ndefl FP64
+    // anchored refinement (anc_u == nullptr: plain Lanczos), T* vectors: the
+    // Krylov vectors are kept orthogonal to the anchor u and to ndefl
     // vectors defl[k*n..]; m_j = r . v_j (r = H u - theta0 u) goes to h_m[j]
-    const double *anc_u, *anc_r, *defl;
+    const void *anc_u, *anc_r, *defl;
     int ndefl;
     double *h_m;
 };
@@ -274,7 +294,7 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, int *err) {
             while (*gen == g) {
                 if (*(volatile int *)err) { good = 0; break; }
                 if (++it > BAR_SPIN) { atomicExch(err, 1); good = 0; break; }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __threadfence();
@@ -284,37 +304,47 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, int *err) {
     return ok != 0;
 }
 
-// CTA sum (512 threads), valid in thread 0
-__device__ __forceinline__ double block_sum(double v, double *scr) {
-    v = warp_sum<double>(v);
+// CTA sums of NV values at once (512 threads), valid in thread 0
+template <class R, int NV>
+__device__ __forceinline__ void block_sums(R (&v)[NV], R *scr) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = warp_sum<R>(v[q]);
     __syncthreads();
-    if ((threadIdx.x & 31) == 0) scr[threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) scr[q * ORTH_WARPS + (threadIdx.x >> 5)] = v[q];
     __syncthreads();
-    double t = 0.0;
     if (threadIdx.x < 32) {
-        t = threadIdx.x < ORTH_WARPS ? scr[threadIdx.x] : 0.0;
-        t = warp_sum<double>(t);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            R t = threadIdx.x < ORTH_WARPS ? scr[q * ORTH_WARPS + threadIdx.x] : (R)0;
+            v[q] = warp_sum<R>(t);
+        }
     }
-    return t;
 }
 
-// sum of the G per-CTA partials p[0..G), same order in every CTA
-__device__ __forceinline__ double grid_total(const double *p, int G, double *bcast) {
-    if (threadIdx.x < 32) {
-        double t = 0.0;
-        for (int b = threadIdx.x; b < G; b += 32) t += __ldcg(p + b);
-        t = warp_sum<double>(t);
-        if (threadIdx.x == 0) *bcast = t;
+// sums of the G per-CTA partials of NV columns p[q*G + b], same order in
+// every CTA; warp q reduces column q, results broadcast through bc[]
+template <class R, int NV>
+__device__ __forceinline__ void grid_totals(const R *p, int G, R *bc, R (&out)[NV]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < NV) {
+        R t = (R)0;
+        for (int b = lane; b < G; b += 32) t += __ldcg(p + (int64_t)warp * G + b);
+        t = warp_sum<R>(t);
+        if (lane == 0) bc[warp] = t;
     }
     __syncthreads();
-    return *bcast;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) out[q] = bc[q];
 }
 
 // hs[l] = sum_b p[l*G + b] for l < ncol (four columns per warp in flight)
-__device__ __forceinline__ void grid_columns(const double *p, int G, int ncol, double *hs) {
+template <class R>
+__device__ __forceinline__ void grid_columns(const R *p, int G, int ncol, R *hs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int l0 = warp; l0 < ncol; l0 += 4 * ORTH_WARPS) {
-        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        R t[4] = {(R)0, (R)0, (R)0, (R)0};
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int l = l0 + u * ORTH_WARPS;
@@ -323,7 +353,7 @@ __device__ __forceinline__ void grid_columns(const double *p, int G, int ncol, d
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const double s = warp_sum<double>(t[u]);
+            const R s = warp_sum<R>(t[u]);
             const int l = l0 + u * ORTH_WARPS;
             if (lane == 0 && l < ncol) hs[l] = s;
         }
@@ -333,8 +363,8 @@ __device__ __forceinline__ void grid_columns(const double *p, int G, int ncol, d
 // Reduce CW per-lane values over the 32 lanes of a warp at once (butterfly
 // with exchange: 31 shuffles for all CW columns); lane L ends with the sum of
 // column L % CW in d[0].
-template <int CW>
-__device__ __forceinline__ double multi_reduce(double (&d)[CW], int lane) {
+template <class R, int CW>
+__device__ __forceinline__ R multi_reduce(R (&d)[CW], int lane) {
     if (CW < 32) {
 #pragma unroll
         for (int s = 16; s >= CW; s >>= 1)
@@ -346,8 +376,8 @@ __device__ __forceinline__ double multi_reduce(double (&d)[CW], int lane) {
         const bool upper = (lane & s) != 0;
 #pragma unroll
         for (int c = 0; c < s; ++c) {
-            const double send = upper ? d[c] : d[c + s];
-            const double keep = upper ? d[c + s] : d[c];
+            const R send = upper ? d[c] : d[c + s];
+            const R keep = upper ? d[c + s] : d[c];
             d[c] = keep + __shfl_xor_sync(0xffffffffu, send, s);
         }
     }
@@ -360,7 +390,7 @@ __device__ __forceinline__ double multi_reduce(double (&d)[CW], int lane) {
 // item accumulating CW columns in registers, then one multi_reduce.
 template <class T, int CW>
 __device__ __forceinline__ void cta_dots(const T *__restrict__ V, int m, const T *__restrict__ w, int64_t n,
-                                         int64_t i0, int64_t i1, bool ww, double *red, double *out, int G) {
+                                         int64_t i0, int64_t i1, bool ww, T *red, T *out, int G) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ncol = m + (ww ? 1 : 0);
     const int ng = (ncol + CW - 1) / CW;
@@ -376,8 +406,9 @@ __device__ __forceinline__ void cta_dots(const T *__restrict__ V, int m, const T
         if (l0 + CW <= m) {
             for (int64_t r = r0 + lane; r < r1; r += 32) {
                 const T wv = w[r];
+                const T *vr = V + (int64_t)l0 * n + r;
 #pragma unroll
-                for (int c = 0; c < CW; ++c) acc[c] += V[(int64_t)(l0 + c) * n + r] * wv;
+                for (int c = 0; c < CW; ++c) acc[c] += vr[(int64_t)c * n] * wv;
             }
         } else {
             for (int64_t r = r0 + lane; r < r1; r += 32) {
@@ -390,35 +421,30 @@ __device__ __forceinline__ void cta_dots(const T *__restrict__ V, int m, const T
                 }
             }
         }
-        double d[CW];
-#pragma unroll
-        for (int c = 0; c < CW; ++c) d[c] = (double)acc[c];
-        const double s = multi_reduce<CW>(d, lane);
+        const T s = multi_reduce<T, CW>(acc, lane);
         if (lane < CW && l0 + lane < ncol) red[q * rs + l0 + lane] = s;
     }
     __syncthreads();
     for (int l = threadIdx.x; l < ncol; l += ORTH_THREADS) {
-        double s = 0.0;
+        T s = (T)0;
         for (int q = 0; q < nq; ++q) s += red[q * rs + l];
         out[(int64_t)l * G] = s;
     }
 }
 
-// w -= V_m h over rows [i0, i1); returns the CTA's w.w (valid in thread 0)
+// w -= V_m h over rows [i0, i1); returns this thread's share of w.w
 template <class T>
-__device__ __forceinline__ double cta_update(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n,
-                                             int64_t i0, int64_t i1, const double *hs, T *hT, double *scr) {
-    for (int l = threadIdx.x; l < m; l += ORTH_THREADS) hT[l] = (T)hs[l];
-    __syncthreads();
+__device__ __forceinline__ T cta_update(const T *__restrict__ V, int m, T *__restrict__ w, int64_t n, int64_t i0,
+                                        int64_t i1, const T *hs) {
     T ss = (T)0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += ORTH_THREADS) {
         T x = w[i];
-#pragma unroll 16
-        for (int l = 0; l < m; ++l) x -= V[(int64_t)l * n + i] * hT[l];
+#pragma unroll 32
+        for (int l = 0; l < m; ++l) x -= V[(int64_t)l * n + i] * hs[l];
         w[i] = x;
         ss += x * x;
     }
-    return block_sum((double)ss, scr);
+    return ss;
 }
 
 template <class T>
@@ -428,21 +454,22 @@ __host__ __device__ inline int orth_redsz(int pstride, int cw) {
     return ORTH_WARPS * cw > pstride + cw ? ORTH_WARPS * cw : pstride + cw;
 }
 
-// shared memory of k_orth, in doubles: hs, red, hT, scratch
-inline size_t orth_smem(int pstride, int cw) {
-    return (size_t)(pstride + orth_redsz(pstride, cw) + pstride + 64) * sizeof(double);
+// shared memory of k_orth, in elements of T: hs, red, scratch
+inline size_t orth_smem(int pstride, int cw, size_t tsize) {
+    return (size_t)(pstride + orth_redsz(pstride, cw) + 8 * ORTH_WARPS + 16) * tsize;
 }
 
 template <class T, int CW>
 __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     int *flags = a.flags;
     if (*(volatile int *)&flags[F_STOP]) return;     // set before this launch: uniform
-    extern __shared__ double osm[];
+    extern __shared__ __align__(16) unsigned char osm_raw[];
+    T *osm = (T *)osm_raw;
     const int ps = a.pstride;
-    double *hs = osm;
-    double *red = hs + ps;
-    T *hT = (T *)(red + orth_redsz(ps, CW));
-    double *scr = red + orth_redsz(ps, CW) + ps;     // [0,16) block sums, [32] broadcast
+    T *hs = osm;
+    T *red = hs + ps;
+    T *scr = red + orth_redsz(ps, CW);               // [8 x 16] block sums, then [16] broadcasts
+    T *bc = scr + 8 * ORTH_WARPS;
     const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x;
     const int64_t n = a.n;
     const int64_t chunk = (n + G - 1) / G;
@@ -451,62 +478,70 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     const int j = a.j, m = j + 1;
     const T *vj = V + (int64_t)j * n;
     const T *vjm = V + (int64_t)(j > 0 ? j - 1 : 0) * n;
-    double *pA = a.part, *pH = pA + PA_COLS * G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G,
-           *pB2 = pH2 + (int64_t)ps * G;
+    T *pA = (T *)a.part, *pH = pA + PA_COLS * G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G,
+      *pB2 = pH2 + (int64_t)ps * G;
     int *err = flags + F_ERR;
-    const bool anc = a.anc_u != nullptr;
+    const T *au = (const T *)a.anc_u, *ar = (const T *)a.anc_r, *ay = (const T *)a.defl;
+    const bool anc = au != nullptr;
     const int nd = anc ? a.ndefl : 0;
 
-    // the host's stop request, published by CTA 0 before the first barrier
-    if (blk == 0 && tid == 0) flags[F_HOST] = *(volatile const int *)(a.h_flags + F_NFLAGS);
-    {   // alpha = v_j . w; anchored also u.w, r.v_j and y_k.w
-        T p = (T)0;
-        double pu = 0.0, pr = 0.0, py[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
-            const T wi = w[i], vi = vj[i];
-            p += vi * wi;
-            if (anc) {
-                pu += a.anc_u[i] * (double)wi;
-                pr += a.anc_r[i] * (double)vi;
-                for (int k = 0; k < nd; ++k) py[k] += a.defl[(int64_t)k * n + i] * (double)wi;
-            }
-        }
-        double t = block_sum((double)p, scr);
-        if (tid == 0) pA[blk] = t;
+    // the host's stop request (host memory: issued first, consumed just
+    // before the first barrier so the read overlaps the first phase)
+    int host_stop = 0;
+    if (blk == 0 && tid == 0) host_stop = *(volatile const int *)(a.h_flags + F_NFLAGS);
+    // alpha = v_j . w; anchored also u.w, r.v_j and y_k.w
+    T av[PA_COLS];
+#pragma unroll
+    for (int q = 0; q < PA_COLS; ++q) av[q] = (T)0;
+    for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+        const T wi = w[i], vi = vj[i];
+        av[0] += vi * wi;
         if (anc) {
-            t = block_sum(pu, scr);
-            if (tid == 0) pA[G + blk] = t;
-            t = block_sum(pr, scr);
-            if (tid == 0) pA[2 * G + blk] = t;
-            for (int k = 0; k < nd; ++k) {
-                t = block_sum(py[k], scr);
-                if (tid == 0) pA[(3 + k) * G + blk] = t;
-            }
+            av[1] += au[i] * wi;
+            av[2] += ar[i] * vi;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < nd) av[3 + k] += ay[(int64_t)k * n + i] * wi;
         }
     }
+    if (anc) {
+        block_sums<T, PA_COLS>(av, scr);
+        if (tid == 0)
+#pragma unroll
+            for (int q = 0; q < PA_COLS; ++q) pA[q * G + blk] = av[q];
+    } else {
+        T a1[1] = {av[0]};
+        block_sums<T, 1>(a1, scr);
+        if (tid == 0) pA[blk] = a1[0];
+    }
+    if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
     if (!grid_sync(a.bar, err)) return;
     if (__ldcg(&flags[F_HOST])) {
         if (blk == 0 && tid == 0) flags[F_STOP] = 1;
         return;
     }
-    const double alpha0 = grid_total(pA, G, scr + 32);
-    double cu = 0.0, cy[4] = {0.0, 0.0, 0.0, 0.0};
+    T tot[PA_COLS];
     if (anc) {
-        cu = grid_total(pA + G, G, scr + 33);
-        const double cr = grid_total(pA + 2 * G, G, scr + 34);
-        for (int k = 0; k < nd; ++k) cy[k] = grid_total(pA + (3 + k) * G, G, scr + 35 + k);
-        if (blk == 0 && tid == 0) a.h_m[j] = cr;
+        grid_totals<T, PA_COLS>(pA, G, bc, tot);
+        if (blk == 0 && tid == 0) a.h_m[j] = (double)tot[2];
+    } else {
+        T t1[1];
+        grid_totals<T, 1>(pA, G, bc, t1);
+#pragma unroll
+        for (int q = 0; q < PA_COLS; ++q) tot[q] = (T)0;
+        tot[0] = t1[0];
     }
+    const T alpha0 = tot[0];
     {   // three-term step (and the anchor projections), then h = V_m^T w and ww = w.w
-        const T a3 = (T)alpha0;
         const T b3 = j > 0 ? (T)a.beta[j - 1] : (T)0;
         for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
-            T x = w[i] - a3 * vj[i];
+            T x = w[i] - alpha0 * vj[i];
             if (j > 0) x -= b3 * vjm[i];
             if (anc) {
-                double q = cu * a.anc_u[i];
-                for (int k = 0; k < nd; ++k) q += cy[k] * a.defl[(int64_t)k * n + i];
-                x -= (T)q;
+                x -= tot[1] * au[i];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k < nd) x -= tot[3 + k] * ay[(int64_t)k * n + i];
             }
             w[i] = x;
         }
@@ -514,44 +549,47 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         cta_dots<T, CW>(V, m, w, n, i0, i1, true, red, pH + blk, G);
     }
     if (!grid_sync(a.bar, err)) return;
-    grid_columns(pH, G, m + 1, hs);
+    grid_columns<T>(pH, G, m + 1, hs);
     __syncthreads();
-    const double ww = hs[m];
-    double hj = hs[j];
+    const T ww = hs[m];
+    T hj = hs[j];
     {
-        const double t = cta_update<T>(V, m, w, n, i0, i1, hs, hT, scr);
-        if (tid == 0) pB[blk] = t;
+        T s1[1] = {cta_update<T>(V, m, w, n, i0, i1, hs)};
+        block_sums<T, 1>(s1, scr);
+        if (tid == 0) pB[blk] = s1[0];
     }
     if (!grid_sync(a.bar, err)) return;
-    double bb = grid_total(pB, G, scr + 32);
-    if (bb < 0.5 * ww) {   // second projection (same decision in every CTA)
+    T bb[1];
+    grid_totals<T, 1>(pB, G, bc + 8, bb);
+    if (bb[0] < (T)0.5 * ww) {   // second projection (same decision in every CTA)
         cta_dots<T, CW>(V, m, w, n, i0, i1, false, red, pH2 + blk, G);
         if (!grid_sync(a.bar, err)) return;
-        grid_columns(pH2, G, m, hs);
+        grid_columns<T>(pH2, G, m, hs);
         __syncthreads();
         hj += hs[j];
-        const double t = cta_update<T>(V, m, w, n, i0, i1, hs, hT, scr);
-        if (tid == 0) pB2[blk] = t;
+        T s1[1] = {cta_update<T>(V, m, w, n, i0, i1, hs)};
+        block_sums<T, 1>(s1, scr);
+        if (tid == 0) pB2[blk] = s1[0];
         if (!grid_sync(a.bar, err)) return;
-        bb = grid_total(pB2, G, scr + 32);
+        grid_totals<T, 1>(pB2, G, bc + 9, bb);
     }
-    const double alpha_j = alpha0 + hj;
-    const double beta_j = sqrt(bb);
+    const T alpha_j = alpha0 + hj;
+    const T beta_j = sqrt(bb[0]);
     bool brk = false;
     if (m < a.mmax) {
-        const double scale = fmax(fabs(alpha_j), j > 0 ? a.beta[j - 1] : 0.0);
-        brk = !(beta_j > 1e-13 * fmax(scale, 1e-300));
+        const T scale = fmax(fabs(alpha_j), j > 0 ? (T)a.beta[j - 1] : (T)0);
+        brk = !(beta_j > (T)1e-13 * fmax(scale, (T)1e-30));
         if (!brk) {
-            const T inv = (T)(1.0 / beta_j);
+            const T inv = (T)1 / beta_j;
             T *vn = V + (int64_t)m * n;
             for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) vn[i] = w[i] * inv;
         }
     }
     if (blk == 0 && tid == 0) {
-        a.alpha[j] = alpha_j;
-        a.beta[j] = beta_j;
-        a.h_alpha[j] = alpha_j;
-        a.h_beta[j] = beta_j;
+        a.alpha[j] = (double)alpha_j;
+        a.beta[j] = (double)beta_j;
+        a.h_alpha[j] = (double)alpha_j;
+        a.h_beta[j] = (double)beta_j;
         if (brk) {
             flags[F_BREAK] = m;
             flags[F_STOP] = 2;
@@ -684,6 +722,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     if (mixed) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V32, (size_t)(cap + 1) * n));
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.w32, (size_t)n));
+        NSS_CUDA_TRY(c, ctx_alloc(c, &z.anc32, (size_t)6 * n));   // FP32 anchor, residual, deflation set
         NSS_CUDA_TRY(c, ctx_alloc(c, &z.V, (size_t)n));   // FP64 refinement scratch
         z.full64 = false;
     } else {
@@ -695,7 +734,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int pstride = cap + 2;
     const int cw = mixed ? OrthCW<float>::value : OrthCW<double>::value;
-    const size_t smem = orth_smem(pstride, cw);
+    const size_t smem = orth_smem(pstride, cw, mixed ? sizeof(float) : sizeof(double));
     const void *fn = mixed ? (const void *)k_orth<float, OrthCW<float>::value>
                            : (const void *)k_orth<double, OrthCW<double>::value>;
     if (smem > 48 * 1024) NSS_CUDA_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -741,7 +780,8 @@ int hv_t<float>(Ctx &c, const float *v, float *hv, const int *stop) { return hv_
 // has put r/|r| (FP32) into V[0].  The result c0 u + sum_l c_l V[l] goes to
 // `out` (may alias u).
 struct AnchorSpec {
-    const double *u, *r, *defl;
+    const double *u;             // FP64 anchor (the combination uses it)
+    const float *u32, *r32, *defl32;   // FP32 copies for the projections in k_orth
     int ndefl;
     double theta0;
     double *out;
@@ -813,9 +853,9 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     oa.h_alpha = z.d_h_ab;
     oa.h_beta = z.d_h_ab + (cap + 1);
     oa.h_flags = z.d_h_flags;
-    oa.anc_u = anc ? anc->u : nullptr;
-    oa.anc_r = anc ? anc->r : nullptr;
-    oa.defl = anc ? anc->defl : nullptr;
+    oa.anc_u = anc ? (const void *)anc->u32 : nullptr;
+    oa.anc_r = anc ? (const void *)anc->r32 : nullptr;
+    oa.defl = anc ? (const void *)anc->defl32 : nullptr;
     oa.ndefl = anc ? anc->ndefl : 0;
     oa.h_m = z.d_h_ab + 2 * (cap + 1);
     const double *hm = z.h_ab + 2 * (cap + 1);
@@ -973,7 +1013,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
-    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.evecs, z.scal, z.part, z.counter, z.alpha, z.beta,
+    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.evecs, z.scal, z.part, z.counter, z.alpha, z.beta,
                     z.theta, z.resid, z.svec, z.flags};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
@@ -1005,7 +1045,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     if (!mixed) {
         rc = run_lanczos<double>(c, z.V, z.w, neigen, mmax, tol, seed, &numop_, &m_done);
     } else {
-        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, MIXED_TOL), seed, &numop_, &m_done);
+        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done);
     }
     const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
     if (!rc && mixed) {
@@ -1059,9 +1099,14 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             }
             const double beta0 = std::sqrt(std::max(rr, 0.0));
             if (!(beta0 > tol * std::fabs(theta0))) continue;   // the anchor is converged already
-            ++c.launches;
+            // FP32 start vector r/|r| and FP32 copies of u, r and the deflation set
+            float *u32 = z.anc32, *r32 = z.anc32 + n, *y32 = z.anc32 + 2 * n;
+            c.launches += 3 + e;
             k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, n);
-            AnchorSpec as{u, z.w, z.evecs, e, theta0, u};
+            k_to32<<<608, 256, 0, st>>>(u32, u, 1.0, n);
+            k_to32<<<608, 256, 0, st>>>(r32, z.w, 1.0, n);
+            for (int f = 0; f < e; ++f) k_to32<<<608, 256, 0, st>>>(y32 + (int64_t)f * n, z.evecs + (int64_t)f * n, 1.0, n);
+            AnchorSpec as{u, u32, r32, y32, e, theta0, u};
             int it2 = 0, m2 = 0;
             rc = run_lanczos<float>(c, z.V32, z.w32, 1, mmax, tol, seed, &it2, &m2, &as);
             numop_ += it2;

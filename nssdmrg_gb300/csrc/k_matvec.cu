@@ -272,6 +272,87 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
 // GB300 issues FP64 at about 1/64 of its FP32 rate, so this kernel is bound
 // by the FP64 pipe; the operand tiles are staged in shared memory only to
 // keep the loads coalesced.
+// A x B terms of one output tile, staged.  The block operators of the two
+// sites at the centre bond have at most one stored element per row (the
+// enlarged blocks are block (x) site), so for each term of the output sector
+// the tile's rows of A and columns of B are staged in shared memory as
+// (column, value) pairs, and each output then needs only independent
+// gathers W_q[aj][bj], in flight together.  A row with more than one element
+// sends that batch of terms to the general CSR loop.
+constexpr int AB_MAXT = 16;
+
+template <class V, int TR, int TC>
+struct AbStage {
+    int ac[AB_MAXT][TR], bc[AB_MAXT][TC];
+    V av[AB_MAXT][TR], bv[AB_MAXT][TC];
+    const V *wq[AB_MAXT];
+    int drq[AB_MAXT];
+    int multi;
+};
+
+// stage terms [tb, tb+nt) for rows row0.. and columns col0..; ends with a barrier
+template <class V, int TR, int TC>
+__device__ __forceinline__ void ab_stage(AbStage<V, TR, TC> &S, const V *__restrict__ v, int tb, int nt, int row0,
+                                         int col0, int dl, int dr, const int *__restrict__ drs,
+                                         const int64_t *__restrict__ off, const DevTerm *__restrict__ terms,
+                                         const int *__restrict__ ab_rp, const int *__restrict__ ab_col,
+                                         const V *__restrict__ ab_val) {
+    if (threadIdx.x == 0) S.multi = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt * (TR + TC); e += blockDim.x) {
+        const int tt = e / (TR + TC), r = e % (TR + TC);
+        const DevTerm tm = terms[tb + tt];
+        int c = -1;
+        V x = (V)0;
+        if (r < TR) {
+            const int il = row0 + r;
+            if (il < dl) {
+                const int p0 = ab_rp[tm.a_rp + il], p1 = ab_rp[tm.a_rp + il + 1];
+                if (p1 > p0) { c = ab_col[p0]; x = ab_val[p0]; }
+                if (p1 - p0 > 1) S.multi = 1;
+            }
+            S.ac[tt][r] = c;
+            S.av[tt][r] = x;
+        } else {
+            const int ir = col0 + (r - TR);
+            if (ir < dr) {
+                const int p0 = ab_rp[tm.b_rp + ir], p1 = ab_rp[tm.b_rp + ir + 1];
+                if (p1 > p0) { c = ab_col[p0]; x = ab_val[p0]; }
+                if (p1 - p0 > 1) S.multi = 1;
+            }
+            S.bc[tt][r - TR] = c;
+            S.bv[tt][r - TR] = x;
+            if (r == TR) {
+                S.wq[tt] = v + off[tm.in_sec];
+                S.drq[tt] = drs[tm.in_sec];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// general loop for output (il, ir) over terms [tb, tb+nt): the reference's
+// sum over the stored elements of A and B
+template <class V>
+__device__ __forceinline__ V ab_csr(V acc, const V *__restrict__ v, int tb, int nt, int il, int ir,
+                                    const int *__restrict__ drs, const int64_t *__restrict__ off,
+                                    const DevTerm *__restrict__ terms, const int *__restrict__ ab_rp,
+                                    const int *__restrict__ ab_col, const V *__restrict__ ab_val) {
+    for (int ti = tb; ti < tb + nt; ++ti) {
+        const DevTerm tm = terms[ti];
+        const V *Wq = v + off[tm.in_sec];
+        const int drq = drs[tm.in_sec];
+        const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
+        for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
+            const int aj = ab_col[ja];
+            V cb = (V)0;
+            for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb) cb = fma(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
+            acc = fma(ab_val[ja], cb, acc);
+        }
+    }
+    return acc;
+}
+
 __global__ void __launch_bounds__(256) k_hv_fp64(
     const double *__restrict__ v, double *__restrict__ hv, const int4 *__restrict__ tiles,
     const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
@@ -328,23 +409,26 @@ __global__ void __launch_bounds__(256) k_hv_fp64(
         for (int j = 0; j < 32; ++j) acc = fma(sa[ty][j], sb[j][tx], acc);
         __syncthreads();
     }
-    if (il >= dl || ir >= dr) return;
     // sum_t A W_q B^T : Out[ai][bi] += A[ai][aj] B[bi][bj] W_q[aj][bj] (:808-857)
-    for (int ti = term_ptr[k]; ti < term_ptr[k + 1]; ++ti) {
-        const DevTerm tm = terms[ti];
-        const double *Wq = v + off[tm.in_sec];
-        const int drq = drs[tm.in_sec];
-        const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
-        for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
-            const int aj = ab_col[ja];
-            const double av = ab_val[ja];
-            double cb = 0.0;
-            for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
-                cb = fma(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
-            acc = fma(av, cb, acc);
+    __shared__ AbStage<double, TILE, TILE> S;
+    const bool in = il < dl && ir < dr;
+    for (int tb = term_ptr[k]; tb < term_ptr[k + 1]; tb += AB_MAXT) {
+        const int nt = min(AB_MAXT, term_ptr[k + 1] - tb);
+        ab_stage<double, TILE, TILE>(S, v, tb, nt, row0, col0, dl, dr, drs, off, terms, ab_rp, ab_col, ab_val);
+        if (in) {
+            if (!S.multi) {
+                for (int tt = 0; tt < nt; ++tt) {
+                    const int aj = S.ac[tt][ty], bj = S.bc[tt][tx];
+                    if (aj >= 0 && bj >= 0)
+                        acc = fma(S.av[tt][ty] * S.bv[tt][tx], S.wq[tt][(int64_t)aj * S.drq[tt] + bj], acc);
+                }
+            } else {
+                acc = ab_csr<double>(acc, v, tb, nt, il, ir, drs, off, terms, ab_rp, ab_col, ab_val);
+            }
         }
+        __syncthreads();
     }
-    hv[o + (int64_t)il * dr + ir] = acc;
+    if (in) hv[o + (int64_t)il * dr + ir] = acc;
 }
 
 // FP32 variant for the mixed-precision Lanczos phase: 32x32 output tiles,
@@ -412,25 +496,40 @@ __global__ void __launch_bounds__(256) k_hv_fp32(
         }
         __syncthreads();
     }
+    // A x B terms, staged per batch of terms (see ab_stage)
+    __shared__ AbStage<float, TILE32, TILE32> S;
+    for (int tb = term_ptr[k]; tb < term_ptr[k + 1]; tb += AB_MAXT) {
+        const int nt = min(AB_MAXT, term_ptr[k + 1] - tb);
+        ab_stage<float, TILE32, TILE32>(S, v, tb, nt, row0, col0, dl, dr, drs, off, terms, ab_rp, ab_col, ab_val);
+        if (!S.multi) {
+            for (int tt = 0; tt < nt; ++tt) {
+                const float *Wq = S.wq[tt];
+                const int drq = S.drq[tt];
+#pragma unroll
+                for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const int aj = S.ac[tt][ty + 16 * rr], bj = S.bc[tt][tx + 16 * cc];
+                        if (aj >= 0 && bj >= 0)
+                            acc[rr][cc] = fmaf(S.av[tt][ty + 16 * rr] * S.bv[tt][tx + 16 * cc],
+                                               Wq[(int64_t)aj * drq + bj], acc[rr][cc]);
+                    }
+            }
+        } else {
+            for (int rr = 0; rr < 2; ++rr)
+                for (int cc = 0; cc < 2; ++cc) {
+                    const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+                    if (il < dl && ir < dr)
+                        acc[rr][cc] = ab_csr<float>(acc[rr][cc], v, tb, nt, il, ir, drs, off, terms, ab_rp, ab_col,
+                                                    ab_val);
+                }
+        }
+        __syncthreads();
+    }
     for (int rr = 0; rr < 2; ++rr)
         for (int cc = 0; cc < 2; ++cc) {
             const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
-            if (il >= dl || ir >= dr) continue;
-            float a = acc[rr][cc];
-            for (int ti = term_ptr[k]; ti < term_ptr[k + 1]; ++ti) {
-                const DevTerm tm = terms[ti];
-                const float *Wq = v + off[tm.in_sec];
-                const int drq = drs[tm.in_sec];
-                const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
-                for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
-                    const int aj = ab_col[ja];
-                    float cb = 0.f;
-                    for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb)
-                        cb = fmaf(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
-                    a = fmaf(ab_val[ja], cb, a);
-                }
-            }
-            hv[o + (int64_t)il * dr + ir] = a;
+            if (il < dl && ir < dr) hv[o + (int64_t)il * dr + ir] = acc[rr][cc];
         }
 }
 

@@ -23,6 +23,8 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <functional>
+#include <map>
 #include <cfloat>
 #include <cmath>
 
@@ -188,13 +190,14 @@ __global__ void k_umat(const double *rho /*eigenvector blocks*/, const int64_t *
 // handful of sweeps), at most JAC_SWEEPS.  Output as cuSOLVER's: eigenvalues
 // ascending, eigenvectors as the columns of a column-major block.
 constexpr int JAC_MAX = 64, JAC_SWEEPS = 24;
+constexpr int JAC_DEFAULT = 32;
 
-// blocks up to this size take k_jacobi (env NSS_JACOBI_MAX, 0..JAC_MAX; 0
-// sends every block to the library eigensolver)
+// blocks up to this size take k_jacobi (env NSS_JACOBI_MAX, 0..JAC_MAX, default
+// 32; 0 sends every block to the batched library eigensolver)
 int jacobi_max() {
     static const int v = [] {
         const char *e = std::getenv("NSS_JACOBI_MAX");
-        if (!e) return JAC_MAX;
+        if (!e) return JAC_DEFAULT;
         const int x = std::atoi(e);
         return x < 0 ? 0 : (x > JAC_MAX ? JAC_MAX : x);
     }();
@@ -310,6 +313,50 @@ __global__ void __launch_bounds__(256) k_jacobi(double *rho, const int64_t *__re
     }
 }
 
+// Embed block q = list[b] (d x d) in the N x N column-major matrix A_b of a
+// batched eigensolve: the extra diagonal entries are -(1 + i/N) * tr(rho_q)
+// (tr >= every eigenvalue of the positive semidefinite block), so the
+// padding eigenvalues come first in ascending order and the block's
+// eigenvectors have no component outside its d rows.
+__global__ void __launch_bounds__(256) k_pack(const double *__restrict__ rho, const int64_t *__restrict__ rho_off,
+                                              const int *__restrict__ dims, const int *__restrict__ list, int N,
+                                              double *__restrict__ A) {
+    const int b = blockIdx.x, q = list[b], d = dims[q];
+    const double *R = rho + rho_off[q];
+    double *Ab = A + (int64_t)b * N * N;
+    __shared__ double tr;
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < d; i += 32) t += fabs(R[(int64_t)i * d + i]);
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) tr = fmax(t, 1e-200);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+        const int col = e / N, row = e % N;
+        double x = 0.0;
+        if (row < d && col < d) x = R[(int64_t)col * d + row];
+        else if (row == col) x = -(1.0 + (double)(row - d) * (1.0 / 64.0)) * tr;
+        Ab[e] = x;
+    }
+}
+
+// Back from the batched layout: the last d eigenpairs of A_b are the block's
+// (ascending), eigenvector rows 0..d-1, column-major d x d into the block slot.
+__global__ void __launch_bounds__(256) k_unpack(const double *__restrict__ A, const double *__restrict__ Wb, int N,
+                                                const int *__restrict__ list, const int *__restrict__ dims,
+                                                const int64_t *__restrict__ rho_off, const int *__restrict__ ev_off,
+                                                double *__restrict__ rho, double *__restrict__ evals) {
+    const int b = blockIdx.x, q = list[b], d = dims[q], sh = N - d;
+    const double *Ab = A + (int64_t)b * N * N;
+    double *R = rho + rho_off[q];
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+        const int col = e / d, row = e % d;
+        R[e] = Ab[(int64_t)(sh + col) * N + row];
+    }
+    for (int i = threadIdx.x; i < d; i += blockDim.x) evals[ev_off[q] + i] = Wb[(int64_t)b * N + sh + i];
+}
+
 int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
     if (*p && cap >= need) return NSS_OK;
     ctx_free(c, *p);
@@ -323,13 +370,14 @@ int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
 
 void rdm_release(Ctx &c) {
     DevRdm &r = c.rdm;
-    void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal};
+    void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal, r.bat, r.bat_info};
     for (void *p : ptrs) ctx_free(c, p);
     for (int i = 0; i < DevRdm::NSIDE; ++i) {
         if (r.side[i]) cudaStreamDestroy(r.side[i]);
         if (r.ev_join[i]) cudaEventDestroy(r.ev_join[i]);
     }
     if (r.ev_fork) cudaEventDestroy(r.ev_fork);
+    if (r.params) cusolverDnDestroyParams((cusolverDnParams_t)r.params);
     r = DevRdm{};
 }
 
@@ -415,21 +463,14 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
     ++c.launches;
     k_symcheck<<<std::min(2 * nsb, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, 2 * nsb, r.iscal + 7);
-    // block eigensolves
+    // Block eigensolves.  Small blocks: one k_jacobi launch on the main
+    // stream.  The others: one batched library eigensolve per padded size
+    // class N = 32*ceil(d/32) (each block embedded in an N x N matrix whose
+    // extra diagonal lies below its spectrum), the classes on side streams.
+    // A batched call costs about one single-matrix call on this GPU (the
+    // FP64 chains of one matrix run on one SM), so this replaces 2*nsb
+    // dependent chains by a handful.
     cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
-    int lw = 0;
-    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, maxd, r.rho, maxd,
-                                    r.evals, &lw) != CUSOLVER_STATUS_SUCCESS) {
-        cleanup();
-        c.err = "nss_rdm: cusolverDnDsyevd_bufferSize failed";
-        return NSS_ERR_CUDA;
-    }
-    if (!r.work || r.lwork < lw) {
-        ctx_free(c, r.work);
-        r.work = nullptr;
-        NSS_CUDA_TRY(c, ctx_alloc(c, &r.work, (size_t)lw * DevRdm::NSIDE));
-        r.lwork = lw;
-    }
     if (!r.ev_fork) {
         NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
         for (int i = 0; i < DevRdm::NSIDE; ++i) {
@@ -437,39 +478,97 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
         }
     }
-    // The blocks are independent and each dsyevd is a chain of small kernels,
-    // so they run on NSIDE streams at once (largest first, round robin).
+    if (!r.params) {
+        cusolverDnParams_t prm = nullptr;
+        if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) {
+            cleanup();
+            c.err = "nss_rdm: cusolverDnCreateParams failed";
+            return NSS_ERR_CUDA;
+        }
+        r.params = prm;
+    }
+    std::vector<int> small, large;
+    const int jmax = jacobi_max();
+    for (int q = 0; q < 2 * nsb; ++q) (dims[q] <= jmax ? small : large).push_back(q);
+    // size classes, largest first
+    std::map<int, std::vector<int>, std::greater<int>> classes;
+    for (int q : large) classes[32 * ((dims[q] + 31) / 32)].push_back(q);
+    struct Cls {
+        int N, batch;
+        int64_t a_off, w_off, ws_off, list_off;
+        size_t ws;
+        std::vector<char> hws;
+    };
+    std::vector<Cls> cls;
+    std::vector<int> lists(small);
+    int64_t pool = 0;
+    for (auto &kv : classes) {
+        Cls cl;
+        cl.N = kv.first;
+        cl.batch = (int)kv.second.size();
+        cl.list_off = (int64_t)lists.size();
+        lists.insert(lists.end(), kv.second.begin(), kv.second.end());
+        size_t wd = 0, wh = 0;
+        if (cusolverDnXsyevBatched_bufferSize(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
+                                              CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, r.rho, cl.N, CUDA_R_64F,
+                                              r.evals, CUDA_R_64F, &wd, &wh, cl.batch) != CUSOLVER_STATUS_SUCCESS) {
+            cleanup();
+            c.err = "nss_rdm: cusolverDnXsyevBatched_bufferSize failed";
+            return NSS_ERR_CUDA;
+        }
+        cl.ws = wd;
+        cl.hws.resize(wh + 16);
+        cl.a_off = pool;
+        pool += (int64_t)cl.batch * cl.N * cl.N;
+        cl.w_off = pool;
+        pool += (int64_t)cl.batch * cl.N;
+        cl.ws_off = pool;
+        pool += (int64_t)(wd + 7) / 8 + 32;
+        cls.push_back(std::move(cl));
+    }
+    if ((rc = ensure(c, &r.bat, r.cap_bat, std::max<int64_t>(pool, 1)))) { cleanup(); return rc; }
+    if (!r.bat_info || r.cap_bat_info < (int64_t)large.size() + 1) {
+        ctx_free(c, r.bat_info);
+        r.bat_info = nullptr;
+        NSS_CUDA_TRY(c, ctx_alloc(c, &r.bat_info, large.size() + 1));
+        r.cap_bat_info = (int64_t)large.size() + 1;
+    }
+    if (!lists.empty()) {
+        NSS_CUDA_TRY(c, ctx_alloc(c, &jac_tmp, lists.size()));
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(jac_tmp, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    }
     NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
     for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
-    // small blocks: one batched Jacobi launch on the main stream, concurrent
-    // with the library eigensolves of the large blocks on the side streams
-    std::vector<int> small, by_size;
-    const int jmax = jacobi_max();
-    for (int q = 0; q < 2 * nsb; ++q) (dims[q] <= jmax ? small : by_size).push_back(q);
+    int info_off = 0;
+    for (size_t ci = 0; ci < cls.size(); ++ci) {
+        Cls &cl = cls[ci];
+        cudaStream_t ss = r.side[ci % DevRdm::NSIDE];
+        double *A = r.bat + cl.a_off, *W = r.bat + cl.w_off, *ws = r.bat + cl.ws_off;
+        c.launches += 2;
+        k_pack<<<cl.batch, 256, 0, ss>>>(r.rho, d_rho_off, d_dims, jac_tmp + cl.list_off, cl.N, A);
+        cusolverDnSetStream(h, ss);
+        const cusolverStatus_t cs = cusolverDnXsyevBatched(
+            h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, A,
+            cl.N, CUDA_R_64F, W, CUDA_R_64F, ws, cl.ws, cl.hws.data(), cl.hws.size() - 16, r.bat_info + info_off,
+            cl.batch);
+        cusolverDnSetStream(h, st);
+        if (cs != CUSOLVER_STATUS_SUCCESS) {
+            cleanup();
+            c.err = "nss_rdm: cusolverDnXsyevBatched failed";
+            return NSS_ERR_CUDA;
+        }
+        k_unpack<<<cl.batch, 256, 0, ss>>>(A, W, cl.N, jac_tmp + cl.list_off, d_dims, d_rho_off, d_ev_off, r.rho,
+                                           r.evals);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+        info_off += cl.batch;
+    }
     if (!small.empty()) {
-        NSS_CUDA_TRY(c, ctx_alloc(c, &jac_tmp, small.size()));
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(jac_tmp, small.data(), small.size() * sizeof(int), cudaMemcpyHostToDevice, st));
         constexpr int jac_smem = 2 * JAC_MAX * (JAC_MAX + 1) * (int)sizeof(double);
         NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, jac_smem));
         ++c.launches;
         k_jacobi<<<(int)small.size(), 256, jac_smem, st>>>(r.rho, d_rho_off, d_dims, d_ev_off, jac_tmp, r.evals);
         NSS_CUDA_TRY(c, cudaGetLastError());
     }
-    std::sort(by_size.begin(), by_size.end(), [&](int a, int b) { return dims[a] > dims[b]; });
-    for (int i = 0; i < (int)by_size.size(); ++i) {
-        const int q = by_size[i], sid = i % DevRdm::NSIDE;
-        const int d = dims[q];
-        cusolverDnSetStream(h, r.side[sid]);
-        if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, r.rho + rho_off[q], d,
-                             r.evals + ev_off[q], r.work + (size_t)sid * r.lwork, (int)r.lwork, r.info + sid) !=
-            CUSOLVER_STATUS_SUCCESS) {
-            cusolverDnSetStream(h, st);
-            cleanup();
-            c.err = "nss_rdm: cusolverDnDsyevd failed";
-            return NSS_ERR_CUDA;
-        }
-    }
-    cusolverDnSetStream(h, st);
     for (int i = 0; i < DevRdm::NSIDE; ++i) {
         NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
         NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
