@@ -122,6 +122,9 @@ class Clocks:
                 "samples": len(rows), "reasons": reasons}
 
 
+CORE_PROBE: dict = {}
+
+
 def measure_core_peaks():
     """FP64 (DFMA) and FP32 (FFMA) whole-GPU rates in TFLOP/s, measured now by
     the package's microbenchmark (MEASURED_PEAKS.json holds only the HBM
@@ -132,6 +135,8 @@ def measure_core_peaks():
         exe = build_peaks()
         line = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.strip().splitlines()[-1]
         j = json.loads(line)
+        CORE_PROBE.update({k: j[k] for k in ("dfma_gflops", "dmma_gflops", "ffma_gflops", "dfma_chain_cycles",
+                                             "ddiv_chain_cycles", "ffma_chain_cycles", "chain_lanes") if k in j})
         return j["dfma_gflops"] / 1e3, j["ffma_gflops"] / 1e3, \
             "DFMA / FFMA rates measured in this run by nssdmrg_gb300/peaks.cu (whole GPU)"
     except Exception as e:  # keep the line; say what was used
@@ -345,6 +350,7 @@ def run_gpu(args):
                          "traffic": traffic,
                          "peak_source": peak_src,
                          "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")},
+            "core_probe": CORE_PROBE,
             "setup_s": t_prep,
         }
         if not args.no_cpu_baseline and world == 1:

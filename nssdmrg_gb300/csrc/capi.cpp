@@ -82,6 +82,7 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
         return nullptr;
     }
     ctx->c.device = device;
+    ctx->c.tc_min_dl = nss::tc_min_dl_default();
     ctx->c.budget = hbm_budget;
     if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_err = "nss_create: stream creation failed";

@@ -92,6 +92,9 @@ struct DevLanczos {
     double *d_h_ab = nullptr;
     int orth_grid = 0;           // CTAs of the cooperative orthogonalisation kernel
     size_t orth_smem = 0;        // its dynamic shared memory
+    float *wbuf32 = nullptr;     // [2][n] work vectors of the persistent chunk kernel
+    size_t chunk_smem = 0;
+    bool chunk_ok = false;       // the chunk kernel fits (one CTA per SM)
 };
 
 struct DevRdm {
@@ -127,6 +130,7 @@ struct Ctx {
     DevLanczos lz;
     DevRdm rdm;
     int64_t launches = 0;        // kernels of this library launched
+    int tc_min_dl = 256;         // tensor-core sector threshold (see tc_min_dl_default)
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
@@ -154,9 +158,12 @@ void sb_release(Ctx &c);
 int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop = nullptr);
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
 int hv_device_tc(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
+struct Hv32Ops;
+Hv32Ops hv32_ops(const DevSb &s);
 // sectors with at least this many left states take the tensor-core kernel
-// in the mixed path (0 disables it: env NSS_TC=0)
-extern int g_tc_min_dl;
+// in the mixed path; a context takes env NSS_TC_MIN_DL at creation (default
+// 256: below that the FP32 CUDA-core tiles are faster on GB300; 0 disables)
+int tc_min_dl_default();
 
 // k_noalloc.cu
 int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy);

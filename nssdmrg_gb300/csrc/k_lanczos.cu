@@ -48,6 +48,7 @@
 // FP64 pipe runs at 1/64 of the FP32 one, which is what the mixed method buys.
 #include "device.cuh"
 #include "host_tridiag.hpp"
+#include "hv_tile.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -600,6 +601,222 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent chunk kernel of the mixed method (FP32 basis, all sectors on
+// FP32 CUDA-core tiles): one cooperative launch runs iterations
+// [j0, jend), each as
+//   H*psi          the 32x32 sector tiles shared out over the CTAs, two tiles
+//                  per CTA at a time (two 256-thread groups, named barriers);
+//                  the input is the previous w'' scaled by 1/beta, the alpha
+//                  partials come out of the tile epilogues
+//   barrier
+//   three-term step and CGS dots over the CTA's rows, with the anchored
+//   refinement's extra columns (u.w, r.v_j, y_k.w)
+//   barrier, column sums, update w -= V h, beta^2 partials
+//   barrier, (second projection when needed), next step
+// so an iteration costs three grid barriers and no launch.  V rows are only
+// touched by the CTA that owns them; the work vectors alternate between
+// two buffers so that the tiles reading w''_{j-1} (all rows) never race with
+// the writes of H v_j.  The normalisation v_j = w''_{j-1} / beta_{j-1} is
+// written into V[j] by the owner CTA in iteration j.
+
+struct ChunkArgs {
+    OrthArgs o;                  // V, n, mmax, pstride, alpha/beta, part, bar, flags, mirrors, anchors
+    float *buf[2];               // w buffers, iteration j reads buf[j & 1], writes buf[(j+1) & 1]
+    int j0, jend;
+    int first_from_v;            // iteration j0 reads V[j0] itself (start or restart)
+    const int4 *tiles;
+    int ntiles;
+    Hv32Ops op;
+};
+
+constexpr int CHUNK_EXTRA = 8;   // extra partial columns of the anchored refinement
+
+inline size_t chunk_smem(int pstride) {
+    return 2 * sizeof(Tile32Smem) + orth_smem(pstride, OrthCW<float>::value, sizeof(float));
+}
+
+__global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
+    constexpr int CW = OrthCW<float>::value;
+    int *flags = a.o.flags;
+    if (*(volatile int *)&flags[F_STOP]) return;     // set before this launch: uniform
+    extern __shared__ __align__(16) unsigned char chunk_raw[];
+    Tile32Smem *tsm = (Tile32Smem *)chunk_raw;
+    float *osm = (float *)(chunk_raw + 2 * sizeof(Tile32Smem));
+    const int ps = a.o.pstride;
+    float *hs = osm;
+    float *red = hs + ps;
+    float *scr = red + orth_redsz(ps, CW);
+    float *bc = scr + 8 * ORTH_WARPS;
+    const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x, grp = tid >> 8, lt = tid & 255;
+    const int64_t n = a.o.n;
+    const int64_t chunk = (n + G - 1) / G;
+    const int64_t i0 = min(n, (int64_t)blk * chunk), i1 = min(n, i0 + chunk);
+    float *V = (float *)a.o.V;
+    float *pA = (float *)a.o.part, *pH = pA + PA_COLS * G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G,
+          *pB2 = pH2 + (int64_t)ps * G;
+    int *err = flags + F_ERR;
+    const float *au = (const float *)a.o.anc_u, *ar = (const float *)a.o.anc_r, *ay = (const float *)a.o.defl;
+    const bool anc = au != nullptr;
+    const int nd = anc ? a.o.ndefl : 0;
+    const int nx = anc ? 3 + nd : 0;                 // extra columns: u.w, r.v_j, y_k.w
+    float beta_prev = a.j0 > 0 ? (float)a.o.beta[a.j0 - 1] : 0.f;
+    for (int jj = a.j0; jj < a.jend; ++jj) {
+        const int m = jj + 1;
+        const bool first = jj == a.j0 && a.first_from_v;
+        const float *x = first ? V + (int64_t)jj * n : a.buf[jj & 1];
+        const float sc = first ? 1.f : 1.f / beta_prev;
+        float *y = a.buf[(jj + 1) & 1];
+        int host_stop = 0;
+        if (blk == 0 && tid == 0) host_stop = *(volatile const int *)(a.o.h_flags + F_NFLAGS);
+        // H v_j into y, alpha partials from the tiles
+        float ap = 0.f;
+        for (int ti = 2 * blk + grp; ti < a.ntiles; ti += 2 * G)
+            ap += hv32_tile(a.tiles[ti], x, y, a.op, tsm[grp], lt, GroupSync{1 + grp}, sc);
+        {
+            float a1[1] = {ap};
+            block_sums<float, 1>(a1, scr);
+            if (tid == 0) pA[blk] = a1[0];
+        }
+        if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
+        if (!grid_sync(a.o.bar, err)) return;
+        if (__ldcg(&flags[F_HOST])) {
+            if (blk == 0 && tid == 0) flags[F_STOP] = 1;
+            return;
+        }
+        float alpha0;
+        {
+            float t1[1];
+            grid_totals<float, 1>(pA, G, bc, t1);
+            alpha0 = t1[0];
+        }
+        // v_j into V (own rows), three-term step, anchor extras
+        float ex[CHUNK_EXTRA];
+#pragma unroll
+        for (int q = 0; q < CHUNK_EXTRA; ++q) ex[q] = 0.f;
+        {
+            float *vj = V + (int64_t)jj * n;
+            const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                const float v = x[i] * sc;
+                if (!first) vj[i] = v;
+                float w = y[i] - alpha0 * v;
+                if (jj > 0) w -= beta_prev * vjm[i];
+                y[i] = w;
+                if (anc) {
+                    ex[0] += au[i] * w;
+                    ex[1] += ar[i] * v;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < nd) ex[2 + k] += ay[(int64_t)k * n + i] * w;
+                }
+            }
+        }
+        __syncthreads();
+        cta_dots<float, CW>(V, m, y, n, i0, i1, true, red, pH + blk, G);
+        if (anc) {
+            block_sums<float, CHUNK_EXTRA>(ex, scr);
+            if (tid == 0) {
+                pH[(int64_t)(m + 1) * G + blk] = ex[0];
+                pH[(int64_t)(m + 2) * G + blk] = ex[1];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k < nd) pH[(int64_t)(m + 3 + k) * G + blk] = ex[2 + k];
+            }
+        }
+        if (!grid_sync(a.o.bar, err)) return;
+        grid_columns<float>(pH, G, m + 1 + nx, hs);
+        __syncthreads();
+        const float ww = hs[m];
+        float hj = hs[jj];
+        if (anc && blk == 0 && tid == 0) a.o.h_m[jj] = (double)hs[m + 2];
+        // w -= V h (+ the anchor and deflation components)
+        auto update = [&](int xoff) -> float {
+            float ss = 0.f;
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                float w = y[i];
+#pragma unroll 32
+                for (int l = 0; l < m; ++l) w -= V[(int64_t)l * n + i] * hs[l];
+                if (anc) {
+                    w -= hs[xoff] * au[i];
+                    for (int k = 0; k < nd; ++k) w -= hs[xoff + 2 + k] * ay[(int64_t)k * n + i];
+                }
+                y[i] = w;
+                ss += w * w;
+            }
+            return ss;
+        };
+        {
+            float s1[1] = {update(m + 1)};
+            block_sums<float, 1>(s1, scr);
+            if (tid == 0) pB[blk] = s1[0];
+        }
+        if (!grid_sync(a.o.bar, err)) return;
+        float bb;
+        {
+            float t1[1];
+            grid_totals<float, 1>(pB, G, bc + 8, t1);
+            bb = t1[0];
+        }
+        if (bb < 0.5f * ww) {   // second projection (same decision in every CTA)
+            cta_dots<float, CW>(V, m, y, n, i0, i1, false, red, pH2 + blk, G);
+            if (anc) {
+#pragma unroll
+                for (int q = 0; q < CHUNK_EXTRA; ++q) ex[q] = 0.f;
+                for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                    const float w = y[i];
+                    ex[0] += au[i] * w;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < nd) ex[2 + k] += ay[(int64_t)k * n + i] * w;
+                }
+                block_sums<float, CHUNK_EXTRA>(ex, scr);
+                if (tid == 0) {
+                    pH2[(int64_t)m * G + blk] = ex[0];
+                    pH2[(int64_t)(m + 1) * G + blk] = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < nd) pH2[(int64_t)(m + 2 + k) * G + blk] = ex[2 + k];
+                }
+            }
+            if (!grid_sync(a.o.bar, err)) return;
+            grid_columns<float>(pH2, G, m + (anc ? 2 + nd : 0), hs);
+            __syncthreads();
+            hj += hs[jj];
+            float s1[1] = {update(m)};
+            block_sums<float, 1>(s1, scr);
+            if (tid == 0) pB2[blk] = s1[0];
+            if (!grid_sync(a.o.bar, err)) return;
+            float t1[1];
+            grid_totals<float, 1>(pB2, G, bc + 9, t1);
+            bb = t1[0];
+        }
+        const float alpha_j = alpha0 + hj;
+        const float beta_j = sqrtf(bb);
+        bool brk = false;
+        if (m < a.o.mmax) {
+            const float scale = fmaxf(fabsf(alpha_j), jj > 0 ? beta_prev : 0.f);
+            brk = !(beta_j > 1e-13f * fmaxf(scale, 1e-30f));
+        }
+        if (blk == 0 && tid == 0) {
+            a.o.alpha[jj] = (double)alpha_j;
+            a.o.beta[jj] = (double)beta_j;
+            a.o.h_alpha[jj] = (double)alpha_j;
+            a.o.h_beta[jj] = (double)beta_j;
+            if (brk) {
+                flags[F_BREAK] = m;
+                flags[F_STOP] = 2;
+                a.o.h_flags[F_BREAK] = m;
+                a.o.h_flags[F_STOP] = 2;
+            }
+            __threadfence_system();
+        }
+        if (brk) return;
+        beta_prev = beta_j;
+        __syncthreads();
+    }
+}
+
 // Ritz vectors: out[e] = sum_l V[l] s_e[l]   (FP64 accumulation, FP64 out)
 template <class T>
 __global__ void __launch_bounds__(256) k_ritz(const T *__restrict__ V, int m, int64_t n,
@@ -732,7 +949,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     int dev = 0, nsm = 0;
     NSS_CUDA_TRY(c, cudaGetDevice(&dev));
     NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int pstride = cap + 2;
+    const int pstride = cap + 8;   // m+1 columns plus the anchored refinement's extras
     const int cw = mixed ? OrthCW<float>::value : OrthCW<double>::value;
     const size_t smem = orth_smem(pstride, cw, mixed ? sizeof(float) : sizeof(double));
     const void *fn = mixed ? (const void *)k_orth<float, OrthCW<float>::value>
@@ -746,6 +963,20 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     }
     z.orth_grid = nsm;      // one CTA per SM, all resident (cooperative launch)
     z.orth_smem = smem;
+    z.chunk_ok = false;
+    if (mixed) {
+        // the persistent chunk kernel of the mixed method
+        const size_t csm = chunk_smem(pstride);
+        NSS_CUDA_TRY(c, cudaFuncSetAttribute((const void *)k_chunk32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)csm));
+        int occ2 = 0;
+        NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS, csm));
+        if (occ2 >= 1) {
+            NSS_CUDA_TRY(c, ctx_alloc(c, &z.wbuf32, (size_t)2 * n));
+            z.chunk_smem = csm;
+            z.chunk_ok = true;
+        }
+    }
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.w, (size_t)n));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));
     // scalars, projection coefficients, restart scratch alpha/beta, refinement
@@ -844,7 +1075,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     oa.n = n;
     oa.j = 0;
     oa.mmax = mmax;
-    oa.pstride = cap + 2;
+    oa.pstride = cap + 8;
     oa.alpha = z.alpha;
     oa.beta = z.beta;
     oa.part = z.part;
@@ -865,8 +1096,34 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaEvent_t evs[2];
     cudaEventCreateWithFlags(&evs[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
+    // mixed method without tensor-core sectors: one persistent launch per chunk
+    const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.ntiles_tc == 0;
+    bool from_v = true;   // the next chunk starts from V[j0] (start, restart)
     auto enqueue_chunk = [&](int j0, int slot) -> int {
         const int jend = std::min(mmax, j0 + CHECK);
+        if (use_chunk && jend > j0) {
+            ChunkArgs ca;
+            ca.o = oa;
+            ca.buf[0] = z.wbuf32;
+            ca.buf[1] = z.wbuf32 + n;
+            ca.j0 = j0;
+            ca.jend = jend;
+            ca.first_from_v = from_v ? 1 : 0;
+            ca.tiles = c.sb.d_tiles32;
+            ca.ntiles = c.sb.ntiles32;
+            ca.op = hv32_ops(c.sb);
+            from_v = false;
+            void *args[] = {&ca};
+            cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_chunk32, dim3(z.orth_grid),
+                                                        dim3(ORTH_THREADS), args, z.chunk_smem, st);
+            ++c.launches;
+            if (e != cudaSuccess) {
+                c.err = std::string("nss_eigh: cooperative launch failed: ") + cudaGetErrorString(e);
+                return -1;
+            }
+            cudaEventRecord(evs[slot], st);
+            return jend;
+        }
         for (int jj = j0; jj < jend; ++jj) {
             if (hv_t<T>(c, V + (int64_t)jj * n, w, z.flags + F_STOP)) return -1;
             oa.j = jj;
@@ -952,6 +1209,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             hb[m_done - 1] = 0.0;
             hf[F_STOP] = 0;
             hf[F_BREAK] = 0;
+            from_v = true;
             slot = 0;
             pend_end = enqueue_chunk(m_done, slot);
             if (pend_end < 0) { rc = NSS_ERR_CUDA; break; }
@@ -1013,8 +1271,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
-    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.evecs, z.scal, z.part, z.counter, z.alpha, z.beta,
-                    z.theta, z.resid, z.svec, z.flags};
+    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.evecs, z.scal, z.part, z.counter, z.alpha,
+                    z.beta, z.theta, z.resid, z.svec, z.flags};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
     if (z.h_ab) cudaFreeHost(z.h_ab);

@@ -7,6 +7,7 @@
 // where the last sum runs over the terms whose RowOffset is sector k
 // (:808-857, regrouped by output sector so each tile has one writer).
 #include "device.cuh"
+#include "hv_tile.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -16,10 +17,12 @@
 
 namespace nss {
 
-int g_tc_min_dl = [] {
-    const char *e = std::getenv("NSS_TC");
-    return (e && e[0] == '0') ? 0 : 64;
-}();
+int tc_min_dl_default() {
+    const char *e = std::getenv("NSS_TC_MIN_DL");
+    if (!e) return 256;
+    const int x = std::atoi(e);
+    return x < 0 ? 0 : x;
+}
 
 void ctx_free(Ctx &c, void *p) {
     if (!p) return;
@@ -229,7 +232,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     // terms to H psi and k_hv_tc, launched after it, adds its dense products.
     std::vector<int4> tiles32, tiles_tc;
     for (int k = 0; k < s.nsb; ++k) {
-        if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
+        if (c.tc_min_dl > 0 && s.dls[k] >= c.tc_min_dl) {
             for (int r = 0; r < s.dls[k]; r += TC_ROWS)
                 for (int cc = 0; cc < s.drs[k]; cc += TC_COLS) tiles_tc.push_back(make_int4(k, r, cc, 0));
             for (int r = 0; r < s.dls[k]; r += TILE32)
@@ -237,7 +240,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
         }
     }
     for (int k = 0; k < s.nsb; ++k) {
-        if (g_tc_min_dl > 0 && s.dls[k] >= g_tc_min_dl) {
+        if (c.tc_min_dl > 0 && s.dls[k] >= c.tc_min_dl) {
             continue;
         } else {
             for (int r = 0; r < s.dls[k]; r += TILE32)
@@ -272,87 +275,6 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
 // GB300 issues FP64 at about 1/64 of its FP32 rate, so this kernel is bound
 // by the FP64 pipe; the operand tiles are staged in shared memory only to
 // keep the loads coalesced.
-// A x B terms of one output tile, staged.  The block operators of the two
-// sites at the centre bond have at most one stored element per row (the
-// enlarged blocks are block (x) site), so for each term of the output sector
-// the tile's rows of A and columns of B are staged in shared memory as
-// (column, value) pairs, and each output then needs only independent
-// gathers W_q[aj][bj], in flight together.  A row with more than one element
-// sends that batch of terms to the general CSR loop.
-constexpr int AB_MAXT = 16;
-
-template <class V, int TR, int TC>
-struct AbStage {
-    int ac[AB_MAXT][TR], bc[AB_MAXT][TC];
-    V av[AB_MAXT][TR], bv[AB_MAXT][TC];
-    const V *wq[AB_MAXT];
-    int drq[AB_MAXT];
-    int multi;
-};
-
-// stage terms [tb, tb+nt) for rows row0.. and columns col0..; ends with a barrier
-template <class V, int TR, int TC>
-__device__ __forceinline__ void ab_stage(AbStage<V, TR, TC> &S, const V *__restrict__ v, int tb, int nt, int row0,
-                                         int col0, int dl, int dr, const int *__restrict__ drs,
-                                         const int64_t *__restrict__ off, const DevTerm *__restrict__ terms,
-                                         const int *__restrict__ ab_rp, const int *__restrict__ ab_col,
-                                         const V *__restrict__ ab_val) {
-    if (threadIdx.x == 0) S.multi = 0;
-    __syncthreads();
-    for (int e = threadIdx.x; e < nt * (TR + TC); e += blockDim.x) {
-        const int tt = e / (TR + TC), r = e % (TR + TC);
-        const DevTerm tm = terms[tb + tt];
-        int c = -1;
-        V x = (V)0;
-        if (r < TR) {
-            const int il = row0 + r;
-            if (il < dl) {
-                const int p0 = ab_rp[tm.a_rp + il], p1 = ab_rp[tm.a_rp + il + 1];
-                if (p1 > p0) { c = ab_col[p0]; x = ab_val[p0]; }
-                if (p1 - p0 > 1) S.multi = 1;
-            }
-            S.ac[tt][r] = c;
-            S.av[tt][r] = x;
-        } else {
-            const int ir = col0 + (r - TR);
-            if (ir < dr) {
-                const int p0 = ab_rp[tm.b_rp + ir], p1 = ab_rp[tm.b_rp + ir + 1];
-                if (p1 > p0) { c = ab_col[p0]; x = ab_val[p0]; }
-                if (p1 - p0 > 1) S.multi = 1;
-            }
-            S.bc[tt][r - TR] = c;
-            S.bv[tt][r - TR] = x;
-            if (r == TR) {
-                S.wq[tt] = v + off[tm.in_sec];
-                S.drq[tt] = drs[tm.in_sec];
-            }
-        }
-    }
-    __syncthreads();
-}
-
-// general loop for output (il, ir) over terms [tb, tb+nt): the reference's
-// sum over the stored elements of A and B
-template <class V>
-__device__ __forceinline__ V ab_csr(V acc, const V *__restrict__ v, int tb, int nt, int il, int ir,
-                                    const int *__restrict__ drs, const int64_t *__restrict__ off,
-                                    const DevTerm *__restrict__ terms, const int *__restrict__ ab_rp,
-                                    const int *__restrict__ ab_col, const V *__restrict__ ab_val) {
-    for (int ti = tb; ti < tb + nt; ++ti) {
-        const DevTerm tm = terms[ti];
-        const V *Wq = v + off[tm.in_sec];
-        const int drq = drs[tm.in_sec];
-        const int *arp = ab_rp + tm.a_rp, *brp = ab_rp + tm.b_rp;
-        for (int ja = arp[il]; ja < arp[il + 1]; ++ja) {
-            const int aj = ab_col[ja];
-            V cb = (V)0;
-            for (int jb = brp[ir]; jb < brp[ir + 1]; ++jb) cb = fma(ab_val[jb], Wq[(int64_t)aj * drq + ab_col[jb]], cb);
-            acc = fma(ab_val[ja], cb, acc);
-        }
-    }
-    return acc;
-}
-
 __global__ void __launch_bounds__(256) k_hv_fp64(
     const double *__restrict__ v, double *__restrict__ hv, const int4 *__restrict__ tiles,
     const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
@@ -414,7 +336,8 @@ __global__ void __launch_bounds__(256) k_hv_fp64(
     const bool in = il < dl && ir < dr;
     for (int tb = term_ptr[k]; tb < term_ptr[k + 1]; tb += AB_MAXT) {
         const int nt = min(AB_MAXT, term_ptr[k + 1] - tb);
-        ab_stage<double, TILE, TILE>(S, v, tb, nt, row0, col0, dl, dr, drs, off, terms, ab_rp, ab_col, ab_val);
+        ab_stage<double, TILE, TILE>(S, v, tb, nt, row0, col0, dl, dr, drs, off, terms, ab_rp, ab_col, ab_val,
+                                     threadIdx.x, blockDim.x, CtaSync{});
         if (in) {
             if (!S.multi) {
                 for (int tt = 0; tt < nt; ++tt) {
@@ -434,103 +357,28 @@ __global__ void __launch_bounds__(256) k_hv_fp64(
 // FP32 variant for the mixed-precision Lanczos phase: 32x32 output tiles,
 // each thread owns rows {ty, ty+16} x cols {tx, tx+16}; FP32 operands and
 // accumulation (GB300 issues FP32 FMAs 64x faster than FP64 ones).
-__global__ void __launch_bounds__(256) k_hv_fp32(
-    const float *__restrict__ v, float *__restrict__ hv, const int4 *__restrict__ tiles,
-    const int *__restrict__ dls, const int *__restrict__ drs, const int64_t *__restrict__ off,
-    const float *__restrict__ hlp, const int64_t *__restrict__ hl_off,
-    const float *__restrict__ hrp, const int64_t *__restrict__ hr_off,
-    const int *__restrict__ term_ptr, const DevTerm *__restrict__ terms,
-    const int *__restrict__ ab_rp, const int *__restrict__ ab_col, const float *__restrict__ ab_val,
-    const int *stop) {
+__global__ void __launch_bounds__(256) k_hv_fp32(const float *__restrict__ v, float *__restrict__ hv,
+                                                 const int4 *__restrict__ tiles, Hv32Ops op, const int *stop) {
     if (stop && *stop) return;   // the Lanczos loop has already finished
-    __shared__ float sa[TILE32][33];
-    __shared__ float sb[32][TILE32 + 1];
-    const int4 t = tiles[blockIdx.x];
-    const int k = t.x, row0 = t.y, col0 = t.z;
-    const int dl = dls[k], dr = drs[k];
-    const int64_t o = off[k];
-    const float *W = v + o;
-    const float *HL = hlp + hl_off[k];
-    const float *HR = hrp + hr_off[k];
-    const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
-    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-    // a "terms only" tile (t.w = 1) skips the two dense products
-    const int kdl = (t.w & 1) ? 0 : dl, kdr = (t.w & 1) ? 0 : dr;
-    // H_L W
-    for (int j0 = 0; j0 < kdl; j0 += 32) {
-        for (int e = tid; e < TILE32 * 32; e += 256) {
-            const int r = e / 32, cc = e % 32;
-            const int gi = row0 + r, gj = j0 + cc;
-            sa[r][cc] = (gi < dl && gj < dl) ? HL[(int64_t)gi * dl + gj] : 0.f;
-            const int gj2 = j0 + r, gc = col0 + cc;
-            sb[r][cc] = (gj2 < dl && gc < dr) ? W[(int64_t)gj2 * dr + gc] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int j = 0; j < 32; ++j) {
-            const float a0 = sa[ty][j], a1 = sa[ty + 16][j], b0 = sb[j][tx], b1 = sb[j][tx + 16];
-            acc[0][0] = fmaf(a0, b0, acc[0][0]);
-            acc[0][1] = fmaf(a0, b1, acc[0][1]);
-            acc[1][0] = fmaf(a1, b0, acc[1][0]);
-            acc[1][1] = fmaf(a1, b1, acc[1][1]);
-        }
-        __syncthreads();
-    }
-    // W H_R^T
-    for (int j0 = 0; j0 < kdr; j0 += 32) {
-        for (int e = tid; e < TILE32 * 32; e += 256) {
-            const int r = e / 32, cc = e % 32;
-            const int gi = row0 + r, gj = j0 + cc;
-            sa[r][cc] = (gi < dl && gj < dr) ? W[(int64_t)gi * dr + gj] : 0.f;
-            const int gr = col0 + r;                 // sb[j][x] = HR[col0+x][j0+j]
-            sb[cc][r] = (gr < dr && gj < dr) ? HR[(int64_t)gr * dr + gj] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int j = 0; j < 32; ++j) {
-            const float a0 = sa[ty][j], a1 = sa[ty + 16][j], b0 = sb[j][tx], b1 = sb[j][tx + 16];
-            acc[0][0] = fmaf(a0, b0, acc[0][0]);
-            acc[0][1] = fmaf(a0, b1, acc[0][1]);
-            acc[1][0] = fmaf(a1, b0, acc[1][0]);
-            acc[1][1] = fmaf(a1, b1, acc[1][1]);
-        }
-        __syncthreads();
-    }
-    // A x B terms, staged per batch of terms (see ab_stage)
-    __shared__ AbStage<float, TILE32, TILE32> S;
-    for (int tb = term_ptr[k]; tb < term_ptr[k + 1]; tb += AB_MAXT) {
-        const int nt = min(AB_MAXT, term_ptr[k + 1] - tb);
-        ab_stage<float, TILE32, TILE32>(S, v, tb, nt, row0, col0, dl, dr, drs, off, terms, ab_rp, ab_col, ab_val);
-        if (!S.multi) {
-            for (int tt = 0; tt < nt; ++tt) {
-                const float *Wq = S.wq[tt];
-                const int drq = S.drq[tt];
-#pragma unroll
-                for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-                    for (int cc = 0; cc < 2; ++cc) {
-                        const int aj = S.ac[tt][ty + 16 * rr], bj = S.bc[tt][tx + 16 * cc];
-                        if (aj >= 0 && bj >= 0)
-                            acc[rr][cc] = fmaf(S.av[tt][ty + 16 * rr] * S.bv[tt][tx + 16 * cc],
-                                               Wq[(int64_t)aj * drq + bj], acc[rr][cc]);
-                    }
-            }
-        } else {
-            for (int rr = 0; rr < 2; ++rr)
-                for (int cc = 0; cc < 2; ++cc) {
-                    const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
-                    if (il < dl && ir < dr)
-                        acc[rr][cc] = ab_csr<float>(acc[rr][cc], v, tb, nt, il, ir, drs, off, terms, ab_rp, ab_col,
-                                                    ab_val);
-                }
-        }
-        __syncthreads();
-    }
-    for (int rr = 0; rr < 2; ++rr)
-        for (int cc = 0; cc < 2; ++cc) {
-            const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
-            if (il < dl && ir < dr) hv[o + (int64_t)il * dr + ir] = acc[rr][cc];
-        }
+    __shared__ Tile32Smem sm;
+    hv32_tile(tiles[blockIdx.x], v, hv, op, sm, threadIdx.x, CtaSync{}, 1.0f);
+}
+
+Hv32Ops hv32_ops(const DevSb &s) {
+    Hv32Ops op;
+    op.dls = s.d_dls;
+    op.drs = s.d_drs;
+    op.off = s.d_off;
+    op.hl = s.d_hl32;
+    op.hl_off = s.d_hl_off;
+    op.hr = s.d_hr32;
+    op.hr_off = s.d_hr_off;
+    op.term_ptr = s.d_term_ptr;
+    op.terms = s.d_terms32;
+    op.ab_rp = s.d_ab_rowptr32;
+    op.ab_col = s.d_ab_col32;
+    op.ab_val = s.d_ab_val32;
+    return op;
 }
 
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
@@ -540,9 +388,7 @@ int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
         return NSS_ERR_STATE;
     }
     if (s.ntiles32 > 0) {
-        k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, s.d_dls, s.d_drs, s.d_off, s.d_hl32,
-                                                    s.d_hl_off, s.d_hr32, s.d_hr_off, s.d_term_ptr, s.d_terms32,
-                                                    s.d_ab_rowptr32, s.d_ab_col32, s.d_ab_val32, stop);
+        k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, hv32_ops(s), stop);
         c.launches += 1;
         NSS_CUDA_TRY(c, cudaGetLastError());
     }

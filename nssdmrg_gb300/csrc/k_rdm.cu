@@ -100,16 +100,30 @@ __global__ void k_clamp(double *ev, int n) {
 }
 
 // Descending rank of every eigenvalue; ties: larger position first (the
-// reversal of a stable ascending order).
-__global__ void k_rank(const double *ev, int n, double *sorted, int *order) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double x = ev[i];
-        int r = 0;
-        for (int j = 0; j < n; ++j) {
-            const double y = ev[j];
-            r += (y > x) || (y == x && j > i);
-        }
-        sorted[r] = x;
+// reversal of a stable ascending order).  After k_clamp the values are >= 0,
+// whose IEEE bit patterns order like the values, so the n^2 comparisons are
+// integer compares (an FP64 compare costs a 64-cycle slot of GB300's FP64
+// pipe); -0.0 is read as +0.0.  Keys are staged through shared memory.
+__device__ __forceinline__ long long rank_key(double x) { return x == 0.0 ? 0ll : __double_as_longlong(x); }
+
+__global__ void __launch_bounds__(256) k_rank(const double *ev, int n, double *sorted, int *order) {
+    __shared__ long long ks[1024];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long xi = i < n ? rank_key(ev[i]) : 0ll;
+    int r = 0;
+    for (int j0 = 0; j0 < n; j0 += 1024) {
+        const int jn = min(1024, n - j0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < jn; t += blockDim.x) ks[t] = rank_key(ev[j0 + t]);
+        __syncthreads();
+        if (i < n)
+            for (int t = 0; t < jn; ++t) {
+                const long long y = ks[t];
+                r += (y > xi) || (y == xi && j0 + t > i);
+            }
+    }
+    if (i < n) {
+        sorted[r] = ev[i];
         order[r] = i;
     }
 }

@@ -1,7 +1,9 @@
 // Compute-rate microbenchmark: FP64 FMA (DFMA), FP64 MMA (mma.sync m8n8k4)
-// and FP32 FMA (FFMA) throughput of the whole GPU.  GB300's HBM and bf16
-// tensor peaks are measured elsewhere; these are the denominators of the
-// FP64 and FP32 CUDA-core kernels' rooflines.  Prints one JSON line.
+// and FP32 FMA (FFMA) throughput of the whole GPU, plus the latency of
+// dependent FP64 FMA / FP64 division / FP32 FMA chains in one warp (clock64).
+// GB300's HBM and bf16 tensor peaks are measured elsewhere; these are the
+// denominators of the FP64 and FP32 CUDA-core kernels' rooflines and the
+// facts behind keeping serial FP64 chains off the GPU.  Prints one JSON line.
 #include <cstdio>
 #include <cuda_runtime.h>
 #include <cmath>
@@ -34,6 +36,28 @@ __global__ void dmma_k(double* out, int iters){
     } }
   out[blockIdx.x*blockDim.x+threadIdx.x]=d0+d1+e0+e1+f0+f1+g0+g1;
 }
+// dependent chains, one warp: cycles per operation
+#define LAT_N 2048
+__global__ void lat_k(double* dout, float* fout, long long* cyc, int active){
+  double x = threadIdx.x*1e-3 + 1.0, y = threadIdx.x*1e-3 + 1.5; float f = threadIdx.x*1e-3f + 1.0f;
+  long long t0 = clock64();
+  if (threadIdx.x < active) {
+#pragma unroll 16
+    for (int i = 0; i < LAT_N; ++i) x = fma(x, 0.999, 1e-3);
+  }
+  long long t1 = clock64();
+  if (threadIdx.x < active) {
+    for (int i = 0; i < LAT_N / 8; ++i) y = 0.75 / y + 0.5;
+  }
+  long long t2 = clock64();
+  if (threadIdx.x < active) {
+#pragma unroll 16
+    for (int i = 0; i < LAT_N; ++i) f = fmaf(f, 0.999f, 1e-3f);
+  }
+  long long t3 = clock64();
+  dout[threadIdx.x] = x + y; fout[threadIdx.x] = f;
+  if (threadIdx.x == 0) { cyc[0] = t1 - t0; cyc[1] = t2 - t1; cyc[2] = t3 - t2; }
+}
 int main(){
   int nsm; cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
   cudaDeviceProp pr; cudaGetDeviceProperties(&pr,0);
@@ -52,9 +76,17 @@ int main(){
   // per warp per mma: 8*8*4*2 = 512 flops
   best_m = fmax(best_m, 512.0*(n/32)*(it/4)*16*4/ms/1e6);
   }
+  long long* dcyc; cudaMalloc(&dcyc, 4*sizeof(long long)); long long hc[3] = {0, 0, 0}; double lat[2][3];
+  for (int a = 0; a < 2; ++a) {
+    for (int rep = 0; rep < 2; ++rep) lat_k<<<1, 32>>>(dout, fout, dcyc, a == 0 ? 1 : 32);
+    cudaMemcpy(hc, dcyc, 3*sizeof(long long), cudaMemcpyDeviceToHost);
+    lat[a][0] = (double)hc[0] / LAT_N; lat[a][1] = (double)hc[1] / (LAT_N / 8); lat[a][2] = (double)hc[2] / LAT_N;
+  }
   cudaError_t e = cudaGetLastError();
   printf("{\"device\": \"%s\", \"sm\": \"%d.%d\", \"sms\": %d, \"dfma_gflops\": %.1f, \"dmma_gflops\": %.1f, "
-         "\"ffma_gflops\": %.1f, \"status\": \"%s\"}\n", pr.name, pr.major, pr.minor, nsm, best_d, best_m, best_f,
-         cudaGetErrorString(e));
+         "\"ffma_gflops\": %.1f, \"dfma_chain_cycles\": [%.1f, %.1f], \"ddiv_chain_cycles\": [%.1f, %.1f], "
+         "\"ffma_chain_cycles\": [%.1f, %.1f], \"chain_lanes\": [1, 32], \"status\": \"%s\"}\n",
+         pr.name, pr.major, pr.minor, nsm, best_d, best_m, best_f, lat[0][0], lat[1][0], lat[0][1], lat[1][1],
+         lat[0][2], lat[1][2], cudaGetErrorString(e));
   return e == cudaSuccess ? 0 : 1;
 }

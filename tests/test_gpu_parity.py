@@ -189,8 +189,19 @@ def test_mixed_precision_energy_within_1e10(nss, name, neigen):
 @pytest.fixture(scope="module")
 def c2_superblock(nss):
     """Last infinite step of the Hubbard L=32, U=4, M=256 chain (the
-    benchmark superblock: N=65 900, sectors up to 120 x 120)."""
-    d = nss.DMRG(nss.MODEL_HUBBARD, 16, 256, u=4.0, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1)
+    benchmark superblock: N=65 900, sectors up to 120 x 120).  Its context
+    sends sectors with Dl >= 64 to the tensor-core kernel (the default
+    threshold, 256, would leave it unused at this size)."""
+    import os
+    old = os.environ.get("NSS_TC_MIN_DL")
+    os.environ["NSS_TC_MIN_DL"] = "64"
+    try:
+        d = nss.DMRG(nss.MODEL_HUBBARD, 16, 256, u=4.0, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1)
+    finally:
+        if old is None:
+            del os.environ["NSS_TC_MIN_DL"]
+        else:
+            os.environ["NSS_TC_MIN_DL"] = old
     d.prepare_last()
     return d
 
