@@ -234,3 +234,123 @@ __device__ __forceinline__ float hv32_tile(int4 t, const float *__restrict__ v, 
 }
 
 }  // namespace nss
+
+namespace nss {
+
+// Work items of the persistent kernel's H*psi phase.  An item is a 32x32
+// output tile (x = sector, y = row0, z = col0) and a part (w):
+//   HV_FULL   H_L W + W H_R^T + A x B terms       -> slot 0
+//   HV_LEFT   H_L W                               -> slot 1
+//   HV_RIGHT  W H_R^T + A x B terms               -> slot 0
+// Sectors whose tiles have long K loops (Dl or Dr > 64) are split into a
+// LEFT and a RIGHT item so the two halves run on different SMs; the result
+// is slot 0 + slot 1 (regions of slot 1 that no item writes stay zero).
+enum { HV_FULL = 0, HV_LEFT = 1, HV_RIGHT = 2 };
+constexpr int HV_KMAX = 128;     // K extent staged at once
+
+struct Item32Smem {
+    float sa[32][HV_KMAX + 1];   // A rows x K
+    float sb[HV_KMAX][33];       // K x B columns
+    AbStage<float, 32, 32> S;
+};
+
+// One item by 256 threads (lt = thread index in the group): each thread owns
+// rows {ty, ty+16} x columns {tx, tx+16}.  A whole K range (up to HV_KMAX) is
+// staged at once, so a phase costs one load latency instead of one per 32 K.
+// The outputs times `scale` go to slot[0] or slot[1]; returns this thread's
+// share of sum_i (v[i] scale) (out[i] scale) over its outputs.
+template <class Sync>
+__device__ __forceinline__ float hv32_item(int4 t, const float *__restrict__ v, float *__restrict__ slot0,
+                                           float *__restrict__ slot1, const Hv32Ops &op, Item32Smem &sm, int lt,
+                                           Sync sync, float scale) {
+    const int k = t.x, row0 = t.y, col0 = t.z, part = t.w;
+    const int dl = op.dls[k], dr = op.drs[k];
+    const int64_t o = op.off[k];
+    const float *W = v + o;
+    const int ty = lt / 16, tx = lt % 16;
+    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int ph = 0; ph < 2; ++ph) {
+        if ((ph == 0 && part == HV_RIGHT) || (ph == 1 && part == HV_LEFT)) continue;
+        const int K = ph == 0 ? dl : dr;
+        const float *H = ph == 0 ? op.hl + op.hl_off[k] : op.hr + op.hr_off[k];
+        for (int kb = 0; kb < K; kb += HV_KMAX) {
+            const int kn = min(HV_KMAX, K - kb);
+            for (int e = lt; e < 32 * kn; e += 256) {
+                const int r = e / kn, c = e % kn;       // A[r][c], K index kb + c
+                const int gi = row0 + r, gj = kb + c;
+                float x = 0.f;
+                if (gi < dl) x = ph == 0 ? H[(int64_t)gi * dl + gj] : W[(int64_t)gi * dr + gj];
+                sm.sa[r][c] = x;
+            }
+            for (int e = lt; e < 32 * kn; e += 256) {
+                float x = 0.f;
+                if (ph == 0) {                           // B[c][xx] = W[kb+c][col0+xx]
+                    const int c = e / 32, xx = e % 32, gc = col0 + xx;
+                    if (gc < dr) x = W[(int64_t)(kb + c) * dr + gc];
+                    sm.sb[c][xx] = x;
+                } else {                                 // B[c][xx] = HR[col0+xx][kb+c]
+                    const int xx = e / kn, c = e % kn, gr = col0 + xx;
+                    if (gr < dr) x = H[(int64_t)gr * dr + kb + c];
+                    sm.sb[c][xx] = x;
+                }
+            }
+            sync();
+#pragma unroll 8
+            for (int j = 0; j < kn; ++j) {
+                const float a0 = sm.sa[ty][j], a1 = sm.sa[ty + 16][j], b0 = sm.sb[j][tx], b1 = sm.sb[j][tx + 16];
+                acc[0][0] = fmaf(a0, b0, acc[0][0]);
+                acc[0][1] = fmaf(a0, b1, acc[0][1]);
+                acc[1][0] = fmaf(a1, b0, acc[1][0]);
+                acc[1][1] = fmaf(a1, b1, acc[1][1]);
+            }
+            sync();
+        }
+    }
+    if (part != HV_LEFT) {
+        AbStage<float, 32, 32> &S = sm.S;
+        for (int tb = op.term_ptr[k]; tb < op.term_ptr[k + 1]; tb += AB_MAXT) {
+            const int nt = min(AB_MAXT, op.term_ptr[k + 1] - tb);
+            ab_stage<float, 32, 32>(S, v, tb, nt, row0, col0, dl, dr, op.drs, op.off, op.terms, op.ab_rp,
+                                    op.ab_col, op.ab_val, lt, 256, sync);
+            if (!S.multi) {
+                for (int tt = 0; tt < nt; ++tt) {
+                    const float *Wq = S.wq[tt];
+                    const int drq = S.drq[tt];
+#pragma unroll
+                    for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+                        for (int cc = 0; cc < 2; ++cc) {
+                            const int aj = S.ac[tt][ty + 16 * rr], bj = S.bc[tt][tx + 16 * cc];
+                            if (aj >= 0 && bj >= 0)
+                                acc[rr][cc] = fmaf(S.av[tt][ty + 16 * rr] * S.bv[tt][tx + 16 * cc],
+                                                   Wq[(int64_t)aj * drq + bj], acc[rr][cc]);
+                        }
+                }
+            } else {
+                for (int rr = 0; rr < 2; ++rr)
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+                        if (il < dl && ir < dr)
+                            acc[rr][cc] = ab_csr<float>(acc[rr][cc], v, tb, nt, il, ir, op.drs, op.off, op.terms,
+                                                        op.ab_rp, op.ab_col, op.ab_val);
+                    }
+            }
+            sync();
+        }
+    }
+    float *out = (part == HV_LEFT ? slot1 : slot0) + o;
+    float p = 0.f;
+    for (int rr = 0; rr < 2; ++rr)
+        for (int cc = 0; cc < 2; ++cc) {
+            const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+            if (il < dl && ir < dr) {
+                const int64_t idx = (int64_t)il * dr + ir;
+                const float y = acc[rr][cc] * scale;
+                out[idx] = y;
+                p = fmaf(W[idx] * scale, y, p);
+            }
+        }
+    return p;
+}
+
+}  // namespace nss

@@ -80,7 +80,7 @@ double mixed_tol() {
 }
 constexpr int ORTH_THREADS = 512;
 constexpr int ORTH_WARPS = ORTH_THREADS / 32;
-constexpr uint32_t BAR_SPIN = 1u << 24;   // grid-barrier poll limit (~1 s)
+constexpr uint32_t BAR_SPIN = 1u << 22;   // grid-barrier poll limit (~2 s of L2 round trips)
 
 // device scalar slots (Ctx::lz.scal)
 enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NSCAL = 4 };
@@ -275,34 +275,49 @@ struct OrthArgs {
 
 constexpr int PA_COLS = 8;       // per-CTA values of the first phase (alpha, u.w, r.v, y_k.w)
 
-// Grid-wide barrier for a cooperative launch (all CTAs resident).  Bounded:
-// a wait that runs out sets flags[F_ERR] and every later barrier returns
-// false at once, so the kernel always ends.
-__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err) {
+// Grid-wide barrier for a cooperative launch (all CTAs resident).  The
+// arrival counter only grows during a launch: barrier e of the launch waits
+// for e*G arrivals (`epoch`, kept by each CTA), so there is no reset on the
+// critical path; grid_exit zeroes the counter when the last CTA leaves.
+// Bounded: a wait that runs out sets flags[F_ERR] and every later barrier
+// returns false at once, so the kernel always ends.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned &epoch, int *err) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int good = 1;
-        volatile unsigned *gen = bar + 1;
-        const unsigned g = *gen;
+        epoch += gridDim.x;
         __threadfence();
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            uint32_t it = 0;
-            while (*gen == g) {
+        atomicAdd(bar, 1u);
+        uint32_t it = 0;
+        while (ld_acquire_u32(bar) < epoch) {
+            if ((++it & 255u) == 0) {
                 if (*(volatile int *)err) { good = 0; break; }
-                if (++it > BAR_SPIN) { atomicExch(err, 1); good = 0; break; }
-                __nanosleep(32);
+                if (it > BAR_SPIN) { atomicExch(err, 1); good = 0; break; }
             }
         }
-        __threadfence();
         ok = good;
     }
     __syncthreads();
     return ok != 0;
+}
+
+// every CTA calls this once when it leaves a launch that may use grid_sync
+__device__ __forceinline__ void grid_exit(unsigned *bar) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(bar + 1, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            atomicExch(bar + 1, 0u);
+        }
+    }
 }
 
 // CTA sums of NV values at once (512 threads), valid in thread 0
@@ -463,7 +478,11 @@ inline size_t orth_smem(int pstride, int cw, size_t tsize) {
 template <class T, int CW>
 __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     int *flags = a.flags;
-    if (*(volatile int *)&flags[F_STOP]) return;     // set before this launch: uniform
+    unsigned epoch = 0;
+    if (*(volatile int *)&flags[F_STOP]) {           // set before this launch: uniform
+        grid_exit(a.bar);
+        return;
+    }
     extern __shared__ __align__(16) unsigned char osm_raw[];
     T *osm = (T *)osm_raw;
     const int ps = a.pstride;
@@ -516,9 +535,10 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         if (tid == 0) pA[blk] = a1[0];
     }
     if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
-    if (!grid_sync(a.bar, err)) return;
+    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
     if (__ldcg(&flags[F_HOST])) {
         if (blk == 0 && tid == 0) flags[F_STOP] = 1;
+        grid_exit(a.bar);
         return;
     }
     T tot[PA_COLS];
@@ -549,7 +569,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         __syncthreads();
         cta_dots<T, CW>(V, m, w, n, i0, i1, true, red, pH + blk, G);
     }
-    if (!grid_sync(a.bar, err)) return;
+    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
     grid_columns<T>(pH, G, m + 1, hs);
     __syncthreads();
     const T ww = hs[m];
@@ -559,19 +579,19 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         block_sums<T, 1>(s1, scr);
         if (tid == 0) pB[blk] = s1[0];
     }
-    if (!grid_sync(a.bar, err)) return;
+    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
     T bb[1];
     grid_totals<T, 1>(pB, G, bc + 8, bb);
     if (bb[0] < (T)0.5 * ww) {   // second projection (same decision in every CTA)
         cta_dots<T, CW>(V, m, w, n, i0, i1, false, red, pH2 + blk, G);
-        if (!grid_sync(a.bar, err)) return;
+        if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
         grid_columns<T>(pH2, G, m, hs);
         __syncthreads();
         hj += hs[j];
         T s1[1] = {cta_update<T>(V, m, w, n, i0, i1, hs)};
         block_sums<T, 1>(s1, scr);
         if (tid == 0) pB2[blk] = s1[0];
-        if (!grid_sync(a.bar, err)) return;
+        if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
         grid_totals<T, 1>(pB2, G, bc + 9, bb);
     }
     const T alpha_j = alpha0 + hj;
@@ -599,50 +619,62 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         }
         __threadfence_system();
     }
+    grid_exit(a.bar);
 }
 
 // ---------------------------------------------------------------------------
 // Persistent chunk kernel of the mixed method (FP32 basis, all sectors on
 // FP32 CUDA-core tiles): one cooperative launch runs iterations
 // [j0, jend), each as
-//   H*psi          the 32x32 sector tiles shared out over the CTAs, two tiles
-//                  per CTA at a time (two 256-thread groups, named barriers);
-//                  the input is the previous w'' scaled by 1/beta, the alpha
-//                  partials come out of the tile epilogues
+//   H*psi          work items (32x32 tiles, the long ones split into an H_L
+//                  and an H_R + A x B part written to two slot vectors)
+//                  shared out over the CTAs, two items per CTA at a time (two
+//                  256-thread groups, named barriers); the input is the
+//                  previous w'' scaled by 1/beta, the alpha partials come out
+//                  of the item epilogues
 //   barrier
-//   three-term step and CGS dots over the CTA's rows, with the anchored
-//   refinement's extra columns (u.w, r.v_j, y_k.w)
+//   three-term step on the CTA's rows (w = slot0 + slot1 - alpha v_j -
+//   beta v_{j-1}) and the CGS dots, with the anchored refinement's extra
+//   columns (u.w, r.v_j, y_k.w)
 //   barrier, column sums, update w -= V h, beta^2 partials
 //   barrier, (second projection when needed), next step
 // so an iteration costs three grid barriers and no launch.  V rows are only
-// touched by the CTA that owns them; the work vectors alternate between
-// two buffers so that the tiles reading w''_{j-1} (all rows) never race with
-// the writes of H v_j.  The normalisation v_j = w''_{j-1} / beta_{j-1} is
-// written into V[j] by the owner CTA in iteration j.
+// touched by the CTA that owns them; the work vectors alternate between two
+// buffers so that the items reading w''_{j-1} (all rows) never race with the
+// writes of w''_j.  The normalisation v_j = w''_{j-1} / beta_{j-1} is written
+// into V[j] by the owner CTA in iteration j.  alpha, beta, the anchor
+// couplings and the flags reach the host-visible arrays when the launch ends.
 
 struct ChunkArgs {
     OrthArgs o;                  // V, n, mmax, pstride, alpha/beta, part, bar, flags, mirrors, anchors
     float *buf[2];               // w buffers, iteration j reads buf[j & 1], writes buf[(j+1) & 1]
+    float *slot[2];              // H v_j parts
     int j0, jend;
     int first_from_v;            // iteration j0 reads V[j0] itself (start or restart)
-    const int4 *tiles;
-    int ntiles;
+    const int4 *items;
+    int nitems;
     Hv32Ops op;
 };
 
 constexpr int CHUNK_EXTRA = 8;   // extra partial columns of the anchored refinement
+constexpr int CHUNK_MAXIT = 16;  // iterations per launch (>= CHECK)
 
 inline size_t chunk_smem(int pstride) {
-    return 2 * sizeof(Tile32Smem) + orth_smem(pstride, OrthCW<float>::value, sizeof(float));
+    return 2 * sizeof(Item32Smem) + orth_smem(pstride, OrthCW<float>::value, sizeof(float));
 }
 
 __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
     constexpr int CW = OrthCW<float>::value;
     int *flags = a.o.flags;
-    if (*(volatile int *)&flags[F_STOP]) return;     // set before this launch: uniform
+    unsigned epoch = 0;
+    if (*(volatile int *)&flags[F_STOP]) {           // set before this launch: uniform
+        grid_exit(a.o.bar);
+        return;
+    }
     extern __shared__ __align__(16) unsigned char chunk_raw[];
-    Tile32Smem *tsm = (Tile32Smem *)chunk_raw;
-    float *osm = (float *)(chunk_raw + 2 * sizeof(Tile32Smem));
+    Item32Smem *ism = (Item32Smem *)chunk_raw;
+    float *osm = (float *)(chunk_raw + 2 * sizeof(Item32Smem));
+    __shared__ float rec_a[CHUNK_MAXIT], rec_b[CHUNK_MAXIT], rec_m[CHUNK_MAXIT];
     const int ps = a.o.pstride;
     float *hs = osm;
     float *red = hs + ps;
@@ -661,6 +693,28 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
     const int nd = anc ? a.o.ndefl : 0;
     const int nx = anc ? 3 + nd : 0;                 // extra columns: u.w, r.v_j, y_k.w
     float beta_prev = a.j0 > 0 ? (float)a.o.beta[a.j0 - 1] : 0.f;
+    int done = 0, brk_m = 0;
+    // CTA 0 publishes the completed iterations (device arrays, host mirrors)
+    auto publish = [&]() {
+        if (blk == 0 && tid == 0) {
+            for (int q = 0; q < done; ++q) {
+                const int j = a.j0 + q;
+                a.o.alpha[j] = (double)rec_a[q];
+                a.o.beta[j] = (double)rec_b[q];
+                a.o.h_alpha[j] = (double)rec_a[q];
+                a.o.h_beta[j] = (double)rec_b[q];
+                if (anc) a.o.h_m[j] = (double)rec_m[q];
+            }
+            if (brk_m) {
+                flags[F_BREAK] = brk_m;
+                flags[F_STOP] = 2;
+                a.o.h_flags[F_BREAK] = brk_m;
+                a.o.h_flags[F_STOP] = 2;
+            }
+            __threadfence_system();
+        }
+        grid_exit(a.o.bar);
+    };
     for (int jj = a.j0; jj < a.jend; ++jj) {
         const int m = jj + 1;
         const bool first = jj == a.j0 && a.first_from_v;
@@ -669,19 +723,20 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         float *y = a.buf[(jj + 1) & 1];
         int host_stop = 0;
         if (blk == 0 && tid == 0) host_stop = *(volatile const int *)(a.o.h_flags + F_NFLAGS);
-        // H v_j into y, alpha partials from the tiles
+        // H v_j into the slots, alpha partials from the items
         float ap = 0.f;
-        for (int ti = 2 * blk + grp; ti < a.ntiles; ti += 2 * G)
-            ap += hv32_tile(a.tiles[ti], x, y, a.op, tsm[grp], lt, GroupSync{1 + grp}, sc);
+        for (int ti = 2 * blk + grp; ti < a.nitems; ti += 2 * G)
+            ap += hv32_item(a.items[ti], x, a.slot[0], a.slot[1], a.op, ism[grp], lt, GroupSync{1 + grp}, sc);
         {
             float a1[1] = {ap};
             block_sums<float, 1>(a1, scr);
             if (tid == 0) pA[blk] = a1[0];
         }
         if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
-        if (!grid_sync(a.o.bar, err)) return;
+        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
         if (__ldcg(&flags[F_HOST])) {
             if (blk == 0 && tid == 0) flags[F_STOP] = 1;
+            publish();
             return;
         }
         float alpha0;
@@ -697,10 +752,11 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         {
             float *vj = V + (int64_t)jj * n;
             const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
+            const float *s0 = a.slot[0], *s1 = a.slot[1];
             for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
                 const float v = x[i] * sc;
                 if (!first) vj[i] = v;
-                float w = y[i] - alpha0 * v;
+                float w = (s0[i] + s1[i]) - alpha0 * v;
                 if (jj > 0) w -= beta_prev * vjm[i];
                 y[i] = w;
                 if (anc) {
@@ -724,12 +780,12 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
                     if (k < nd) pH[(int64_t)(m + 3 + k) * G + blk] = ex[2 + k];
             }
         }
-        if (!grid_sync(a.o.bar, err)) return;
+        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
         grid_columns<float>(pH, G, m + 1 + nx, hs);
         __syncthreads();
         const float ww = hs[m];
         float hj = hs[jj];
-        if (anc && blk == 0 && tid == 0) a.o.h_m[jj] = (double)hs[m + 2];
+        const float mj = anc ? hs[m + 2] : 0.f;
         // w -= V h (+ the anchor and deflation components)
         auto update = [&](int xoff) -> float {
             float ss = 0.f;
@@ -751,7 +807,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             block_sums<float, 1>(s1, scr);
             if (tid == 0) pB[blk] = s1[0];
         }
-        if (!grid_sync(a.o.bar, err)) return;
+        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
         float bb;
         {
             float t1[1];
@@ -779,14 +835,14 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
                         if (k < nd) pH2[(int64_t)(m + 2 + k) * G + blk] = ex[2 + k];
                 }
             }
-            if (!grid_sync(a.o.bar, err)) return;
+            if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
             grid_columns<float>(pH2, G, m + (anc ? 2 + nd : 0), hs);
             __syncthreads();
             hj += hs[jj];
             float s1[1] = {update(m)};
             block_sums<float, 1>(s1, scr);
             if (tid == 0) pB2[blk] = s1[0];
-            if (!grid_sync(a.o.bar, err)) return;
+            if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
             float t1[1];
             grid_totals<float, 1>(pB2, G, bc + 9, t1);
             bb = t1[0];
@@ -799,22 +855,20 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             brk = !(beta_j > 1e-13f * fmaxf(scale, 1e-30f));
         }
         if (blk == 0 && tid == 0) {
-            a.o.alpha[jj] = (double)alpha_j;
-            a.o.beta[jj] = (double)beta_j;
-            a.o.h_alpha[jj] = (double)alpha_j;
-            a.o.h_beta[jj] = (double)beta_j;
-            if (brk) {
-                flags[F_BREAK] = m;
-                flags[F_STOP] = 2;
-                a.o.h_flags[F_BREAK] = m;
-                a.o.h_flags[F_STOP] = 2;
-            }
-            __threadfence_system();
+            rec_a[done] = alpha_j;
+            rec_b[done] = beta_j;
+            rec_m[done] = mj;
         }
-        if (brk) return;
+        ++done;
+        if (brk) {
+            brk_m = m;
+            publish();
+            return;
+        }
         beta_prev = beta_j;
         __syncthreads();
     }
+    publish();
 }
 
 // Ritz vectors: out[e] = sum_l V[l] s_e[l]   (FP64 accumulation, FP64 out)
@@ -973,6 +1027,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
         NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS, csm));
         if (occ2 >= 1) {
             NSS_CUDA_TRY(c, ctx_alloc(c, &z.wbuf32, (size_t)2 * n));
+            NSS_CUDA_TRY(c, ctx_alloc(c, &z.slot32, (size_t)2 * n));
             z.chunk_smem = csm;
             z.chunk_ok = true;
         }
@@ -1098,6 +1153,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
     // mixed method without tensor-core sectors: one persistent launch per chunk
     const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.ntiles_tc == 0;
+    if (use_chunk)   // slot 1 regions that no item writes must read as zero
+        NSS_CUDA_TRY(c, cudaMemsetAsync(z.slot32 + n, 0, (size_t)n * sizeof(float), st));
     bool from_v = true;   // the next chunk starts from V[j0] (start, restart)
     auto enqueue_chunk = [&](int j0, int slot) -> int {
         const int jend = std::min(mmax, j0 + CHECK);
@@ -1109,8 +1166,10 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             ca.j0 = j0;
             ca.jend = jend;
             ca.first_from_v = from_v ? 1 : 0;
-            ca.tiles = c.sb.d_tiles32;
-            ca.ntiles = c.sb.ntiles32;
+            ca.slot[0] = z.slot32;
+            ca.slot[1] = z.slot32 + n;
+            ca.items = c.sb.d_items32;
+            ca.nitems = c.sb.nitems32;
             ca.op = hv32_ops(c.sb);
             from_v = false;
             void *args[] = {&ca};
@@ -1271,8 +1330,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
-    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.evecs, z.scal, z.part, z.counter, z.alpha,
-                    z.beta, z.theta, z.resid, z.svec, z.flags};
+    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.slot32, z.evecs, z.scal, z.part, z.counter,
+                    z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
     if (z.h_ab) cudaFreeHost(z.h_ab);

@@ -39,7 +39,7 @@ void sb_release(Ctx &c) {
     void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
                     s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
                     s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err,
-                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32};
+                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32, s.d_items32};
     for (void *p : ptrs) ctx_free(c, p);
     s = DevSb{};
 }
@@ -247,6 +247,30 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
                 for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
         }
     }
+    // work items of the persistent kernel: 32x32 tiles of every sector,
+    // split into an H_L part and an H_R + A x B part when a K loop is long
+    std::vector<int4> items32;
+    for (int k = 0; k < s.nsb; ++k) {
+        const bool split = std::max(s.dls[k], s.drs[k]) > 64;
+        for (int r = 0; r < s.dls[k]; r += TILE32)
+            for (int cc = 0; cc < s.drs[k]; cc += TILE32) {
+                if (split) {
+                    items32.push_back(make_int4(k, r, cc, HV_LEFT));
+                    items32.push_back(make_int4(k, r, cc, HV_RIGHT));
+                } else {
+                    items32.push_back(make_int4(k, r, cc, HV_FULL));
+                }
+            }
+    }
+    // longest first, so the split halves start at once
+    std::stable_sort(items32.begin(), items32.end(), [&](const int4 &x, const int4 &y) {
+        auto cost = [&](const int4 &t) {
+            const int dl = s.dls[t.x], dr = s.drs[t.x];
+            return t.w == HV_LEFT ? dl : (t.w == HV_RIGHT ? dr + 32 : dl + dr + 32);
+        };
+        return cost(x) > cost(y);
+    });
+    s.nitems32 = (int)items32.size();
     s.ntiles32 = (int)tiles32.size();
     s.ntiles_tc = (int)tiles_tc.size();
     std::vector<int> tc_err(1, 0);
@@ -255,7 +279,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
         (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_ab_rowptr32, rowptr32)) ||
         (rc = upload_vec(c, &s.d_ab_col32, col32)) || (rc = upload_vec(c, &s.d_terms32, terms32)) ||
-        (rc = upload_vec(c, &s.d_tiles32, tiles32)) ||
+        (rc = upload_vec(c, &s.d_tiles32, tiles32)) || (rc = upload_vec(c, &s.d_items32, items32)) ||
         (rc = upload_vec(c, &s.d_tiles_tc, tiles_tc)) || (rc = upload_vec(c, &s.d_tc_err, tc_err)))
         return rc;
     if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
