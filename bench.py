@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="headline path; the other one is timed alongside for comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurement")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -173,6 +174,43 @@ def cpu_baseline_leg(desc, n, flops_hv, budget_s=20.0):
             "sample": f"one Lanczos solve of the same superblock (N={n}), {numop} H*psi products "
                       f"({'converged' if rc == 0 else 'iteration-capped'}), OpenMP over sectors, "
                       f"{dt:.2f} s", "energy": float(ev[0])}
+
+
+SWEEP_CASE = {"workload": "heisenberg_half_L20_M64_3sweeps", "model": "heisenberg_half", "L": 20, "ldmrg": 10,
+              "mdmrg": 64, "msweep": [64, 64, 64], "lanc_tolerance": 1e-12, "lanc_niter": 200}
+
+
+def measure_sweeps(nss, device):
+    """Finite-algorithm throughput on the spin-1/2 Heisenberg chain L=20,
+    M=64, three sweeps (the first benchmark configuration): sweeps/s of the
+    finite part (total time minus the infinite growth, each timed on its own
+    run), for both precisions, and |dE| of the final energies."""
+    out = {"config": SWEEP_CASE}
+    res = {}
+    for name, prec in (("mixed", nss.NSS_PREC_MIXED), ("fp64", nss.NSS_PREC_FP64)):
+        def make():
+            return nss.DMRG(nss.MODEL_HEISENBERG_HALF, SWEEP_CASE["ldmrg"], SWEEP_CASE["mdmrg"],
+                            msweep=SWEEP_CASE["msweep"], dmrg_qn=(0.0,), lanc_neigen=1,
+                            lanc_niter=SWEEP_CASE["lanc_niter"], lanc_tolerance=SWEEP_CASE["lanc_tolerance"],
+                            precision=prec, device=device)
+        make().finite()                      # warm-up (allocations, first-touch)
+        t0 = time.perf_counter()
+        d_inf = make()
+        d_inf.infinite()
+        t_inf = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        d = make()
+        recs = d.finite()
+        t_all = time.perf_counter() - t0
+        t_sw = max(t_all - t_inf, 1e-9)
+        nsw = len(SWEEP_CASE["msweep"])
+        res[name] = {"sweeps_per_s": nsw / t_sw, "s_total": t_all, "s_infinite": t_inf,
+                     "steps": len(recs), "energy_final": recs[-1]["energy"][0]}
+    out.update(res)
+    out["speedup_mixed_vs_fp64"] = res["mixed"]["sweeps_per_s"] / res["fp64"]["sweeps_per_s"]
+    out["dE_rel_mixed_vs_fp64"] = abs(res["mixed"]["energy_final"] - res["fp64"]["energy_final"]) / \
+        abs(res["fp64"]["energy_final"])
+    return out
 
 
 def run_gpu(args):
@@ -308,6 +346,8 @@ def run_gpu(args):
         numops.append(numop)
     e2e_value = f_hv * statistics.mean(numops) / (statistics.mean(e2e_times) / 1e3) / 1e12 * world
 
+    sweeps = measure_sweeps(nss, local) if not args.no_sweeps else None
+
     out = None
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
@@ -351,6 +391,7 @@ def run_gpu(args):
                          "peak_source": peak_src,
                          "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")},
             "core_probe": CORE_PROBE,
+            "sweeps": sweeps,
             "setup_s": t_prep,
         }
         if not args.no_cpu_baseline and world == 1:

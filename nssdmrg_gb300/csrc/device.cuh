@@ -60,8 +60,11 @@ struct DevSb {
     DevTerm *d_terms32 = nullptr;                            // terms indexing that pool
     int4 *d_tiles32 = nullptr;         // CUDA-core FP32 tiles (small sectors)
     int ntiles32 = 0;
-    int4 *d_items32 = nullptr;         // work items of the persistent mixed kernel
+    struct ItemRec *d_items32 = nullptr;   // work items of the persistent mixed kernel
     int nitems32 = 0;
+    int *d_item_ell = nullptr;         // per item: offset of its A x B table (-1: CSR loop)
+    int2 *d_ell = nullptr;             // the tables
+    int4 *d_term_hdr = nullptr;        // per FP32 term: input-sector offset (lo, hi), its Dr
     int4 *d_tiles_tc = nullptr;        // tensor-core tiles (sectors with Dl >= TC_MIN_DL)
     int ntiles_tc = 0;
     int *d_tc_err = nullptr;           // set when a tensor-core wait ran out
@@ -95,7 +98,7 @@ struct DevLanczos {
     int orth_grid = 0;           // CTAs of the cooperative orthogonalisation kernel
     size_t orth_smem = 0;        // its dynamic shared memory
     float *wbuf32 = nullptr;     // [2][n] work vectors of the persistent chunk kernel
-    float *slot32 = nullptr;     // [2][n] H*psi parts of the persistent chunk kernel
+    float *slot32 = nullptr;     // [3][n] H*psi parts of the persistent chunk kernel
     size_t chunk_smem = 0;
     bool chunk_ok = false;       // the chunk kernel fits (one CTA per SM)
 };

@@ -128,6 +128,11 @@ struct Hv32Ops {
     const DevTerm *terms;
     const int *ab_rp, *ab_col;
     const float *ab_val;
+    // per work item of the persistent kernel: offset of its A x B table in
+    // `ell` (-1: a row with several elements, use the CSR loop)
+    const int *item_ell;
+    const int2 *ell;             // (column, value bits) of A rows / B columns
+    const int4 *term_hdr;        // per term: offset of its input sector (lo, hi), its Dr
 };
 
 // One 32x32 FP32 output tile t = (sector, row0, col0, flags) by 256 threads
@@ -241,95 +246,225 @@ namespace nss {
 // output tile (x = sector, y = row0, z = col0) and a part (w):
 //   HV_FULL   H_L W + W H_R^T + A x B terms       -> slot 0
 //   HV_LEFT   H_L W                               -> slot 1
-//   HV_RIGHT  W H_R^T + A x B terms               -> slot 0
-// Sectors whose tiles have long K loops (Dl or Dr > 64) are split into a
-// LEFT and a RIGHT item so the two halves run on different SMs; the result
-// is slot 0 + slot 1 (regions of slot 1 that no item writes stay zero).
-enum { HV_FULL = 0, HV_LEFT = 1, HV_RIGHT = 2 };
-constexpr int HV_KMAX = 128;     // K extent staged at once
+//   HV_RIGHT  W H_R^T                             -> slot 2
+//   HV_TERMS  A x B terms                         -> slot 0
+// Sectors whose tiles have long K loops (Dl or Dr > 64) are split into the
+// last three so the parts run on different SMs; the result is slot 0 +
+// slot 1 + slot 2 (regions of slots 1 and 2 that no item writes stay zero).
+enum { HV_FULL = 0, HV_LEFT = 1, HV_RIGHT = 2, HV_TERMS = 3 };
+constexpr int HV_KMAX = 128;            // K extent staged at once
+constexpr int SA_LD = HV_KMAX + 4;      // A rows: float4 reads along K
+constexpr int SB_LD = 34;               // B rows: float2 reads along the columns
 
-struct Item32Smem {
-    float sa[32][HV_KMAX + 1];   // A rows x K
-    float sb[HV_KMAX][33];       // K x B columns
+// A work item with everything it needs to start its operand loads, so that
+// these depend on one load only: (sector, row0, col0, part), (Dl, Dr, first
+// term, end term), (sector offset lo/hi, A x B table offset, 0), (H_L and
+// H_R offsets lo/hi).
+struct ItemRec {
+    int4 a, b, c, d;
+};
+
+__device__ __forceinline__ int64_t lohi(int lo, int hi) { return (int64_t)(unsigned)lo | ((int64_t)hi << 32); }
+
+struct __align__(16) Item32Smem {
+    float sa[32][SA_LD];                // A rows x K
+    float sb[HV_KMAX][SB_LD];           // K x B columns
     AbStage<float, 32, 32> S;
 };
 
+// K loop over staged operands: sa[r][k0..k0+kn4) x sb[k0..k0+kn4)[cols]
+__device__ __forceinline__ void item_mma(const Item32Smem &sm, int k0, int kn4, int ty, int tx, float (&acc)[2][2]) {
+#pragma unroll 2
+    for (int j = k0; j < k0 + kn4; j += 4) {
+        const float4 a0 = *reinterpret_cast<const float4 *>(&sm.sa[ty][j]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&sm.sa[ty + 16][j]);
+        const float av0[4] = {a0.x, a0.y, a0.z, a0.w}, av1[4] = {a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 b = *reinterpret_cast<const float2 *>(&sm.sb[j + q][2 * tx]);
+            acc[0][0] = fmaf(av0[q], b.x, acc[0][0]);
+            acc[0][1] = fmaf(av0[q], b.y, acc[0][1]);
+            acc[1][0] = fmaf(av1[q], b.x, acc[1][0]);
+            acc[1][1] = fmaf(av1[q], b.y, acc[1][1]);
+        }
+    }
+}
+
+// Staged operands of one phase into columns [k0, k0 + ext) of sa / rows of
+// sb: A[r][c] and B[c][x] of H_L W (ph 0) or W H_R^T (ph 1), K range
+// [kb, kb + kn), zero beyond kn; EXT (64 or 128) is the staged extent, so a
+// thread loads EXT/8 elements per operand, all in flight before the stores.
+template <int EXT>
+__device__ __forceinline__ void item_load(int ph, const float *__restrict__ H, const float *__restrict__ W, int dl,
+                                          int dr, int row0, int col0, int kb, int kn, int lt, float *ra, float *rb) {
+    constexpr int PER = 32 * EXT / 256;
+    constexpr int SH = EXT == 64 ? 6 : 7;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int e = lt + q * 256;
+        const int r = e >> SH, c = e & (EXT - 1);
+        const int gi = row0 + r;
+        float x = 0.f;
+        if (gi < dl && c < kn) x = ph == 0 ? H[(int64_t)gi * dl + kb + c] : W[(int64_t)gi * dr + kb + c];
+        ra[q] = x;
+        float y = 0.f;
+        if (ph == 0) {
+            const int c2 = e >> 5, xx = e & 31, gc = col0 + xx;
+            if (gc < dr && c2 < kn) y = W[(int64_t)(kb + c2) * dr + gc];
+        } else {
+            const int xx = e >> SH, gr = col0 + xx;
+            if (gr < dr && c < kn) y = H[(int64_t)gr * dr + kb + c];
+        }
+        rb[q] = y;
+    }
+}
+
+template <int EXT>
+__device__ __forceinline__ void item_store(Item32Smem &sm, int ph, int k0, int kn4, int lt, const float *ra,
+                                           const float *rb) {
+    constexpr int PER = 32 * EXT / 256;
+    constexpr int SH = EXT == 64 ? 6 : 7;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int e = lt + q * 256;
+        const int r = e >> SH, c = e & (EXT - 1);
+        if (c < kn4) sm.sa[r][k0 + c] = ra[q];
+        if (ph == 0) {
+            const int c2 = e >> 5, xx = e & 31;
+            if (c2 < kn4) sm.sb[k0 + c2][xx] = rb[q];
+        } else {
+            const int xx = e >> SH;
+            if (c < kn4) sm.sb[k0 + c][xx] = rb[q];
+        }
+    }
+}
+
 // One item by 256 threads (lt = thread index in the group): each thread owns
-// rows {ty, ty+16} x columns {tx, tx+16}.  A whole K range (up to HV_KMAX) is
-// staged at once, so a phase costs one load latency instead of one per 32 K.
-// The outputs times `scale` go to slot[0] or slot[1]; returns this thread's
-// share of sum_i (v[i] scale) (out[i] scale) over its outputs.
+// rows {ty, ty+16} x columns {2tx, 2tx+1}, so a K step of four costs two
+// float4 and four float2 shared-memory reads for sixteen FMAs.  The staged
+// operands are loaded with every load of a thread in flight before its
+// stores: a FULL item (both K <= 64) stages both products in one round (H_L
+// part in columns 0..63, H_R part in 64..127), a LEFT / RIGHT item its K
+// range (<= HV_KMAX) in one round per 128.  The A x B tables (and the
+// per-term offsets) are read in the same round.  The outputs times `scale`
+// go to the item's slot; returns this thread's share of sum_i (v[i] scale)
+// (out[i] scale) over its outputs.
 template <class Sync>
-__device__ __forceinline__ float hv32_item(int4 t, const float *__restrict__ v, float *__restrict__ slot0,
-                                           float *__restrict__ slot1, const Hv32Ops &op, Item32Smem &sm, int lt,
-                                           Sync sync, float scale) {
-    const int k = t.x, row0 = t.y, col0 = t.z, part = t.w;
-    const int dl = op.dls[k], dr = op.drs[k];
-    const int64_t o = op.off[k];
+__device__ __forceinline__ float hv32_item(const ItemRec &it, const float *__restrict__ v, float *const *slots,
+                                           const Hv32Ops &op, Item32Smem &sm, int lt, Sync sync, float scale) {
+    const int row0 = it.a.y, col0 = it.a.z, part = it.a.w;
+    const int dl = it.b.x, dr = it.b.y, t0 = it.b.z, t1 = it.b.w;
+    const int64_t o = lohi(it.c.x, it.c.y);
     const float *W = v + o;
+    const float *HLk = op.hl + lohi(it.d.x, it.d.y), *HRk = op.hr + lohi(it.d.z, it.d.w);
     const int ty = lt / 16, tx = lt % 16;
     float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-    for (int ph = 0; ph < 2; ++ph) {
-        if ((ph == 0 && part == HV_RIGHT) || (ph == 1 && part == HV_LEFT)) continue;
+    const bool terms = part == HV_FULL || part == HV_TERMS;
+    const int eo = terms ? it.c.z : -1;
+    constexpr int NE = AB_MAXT * 64 / 256;
+    int2 ee[NE];
+    int4 hd = make_int4(0, 0, 0, 0);
+    const int nt0 = min(AB_MAXT, t1 - t0);
+    // first batch of the A x B table, issued with the operand loads
+    auto ell_load = [&](int tb, int nt) {
+        const int2 *src = op.ell + eo + (int64_t)(tb - t0) * 64;
+#pragma unroll
+        for (int q = 0; q < NE; ++q) {
+            const int e = lt + q * 256;
+            ee[q] = e < nt * 64 ? src[e] : make_int2(-1, 0);
+        }
+        if (lt < nt) hd = op.term_hdr[tb + lt];
+    };
+    if (eo >= 0 && nt0 > 0) ell_load(t0, nt0);
+    if (part == HV_FULL) {
+        float ra[8], rb[8];
+        item_load<64>(0, HLk, W, dl, dr, row0, col0, 0, dl, lt, ra, rb);
+        float rc[8], rd[8];
+        item_load<64>(1, HRk, W, dl, dr, row0, col0, 0, dr, lt, rc, rd);
+        const int kl4 = (dl + 3) & ~3, kr4 = (dr + 3) & ~3;
+        item_store<64>(sm, 0, 0, kl4, lt, ra, rb);
+        item_store<64>(sm, 1, 64, kr4, lt, rc, rd);
+        sync();
+        item_mma(sm, 0, kl4, ty, tx, acc);
+        item_mma(sm, 64, kr4, ty, tx, acc);
+        sync();
+    } else if (part == HV_LEFT || part == HV_RIGHT) {
+        const int ph = part == HV_LEFT ? 0 : 1;
         const int K = ph == 0 ? dl : dr;
-        const float *H = ph == 0 ? op.hl + op.hl_off[k] : op.hr + op.hr_off[k];
+        const float *H = ph == 0 ? HLk : HRk;
         for (int kb = 0; kb < K; kb += HV_KMAX) {
-            const int kn = min(HV_KMAX, K - kb);
-            for (int e = lt; e < 32 * kn; e += 256) {
-                const int r = e / kn, c = e % kn;       // A[r][c], K index kb + c
-                const int gi = row0 + r, gj = kb + c;
-                float x = 0.f;
-                if (gi < dl) x = ph == 0 ? H[(int64_t)gi * dl + gj] : W[(int64_t)gi * dr + gj];
-                sm.sa[r][c] = x;
-            }
-            for (int e = lt; e < 32 * kn; e += 256) {
-                float x = 0.f;
-                if (ph == 0) {                           // B[c][xx] = W[kb+c][col0+xx]
-                    const int c = e / 32, xx = e % 32, gc = col0 + xx;
-                    if (gc < dr) x = W[(int64_t)(kb + c) * dr + gc];
-                    sm.sb[c][xx] = x;
-                } else {                                 // B[c][xx] = HR[col0+xx][kb+c]
-                    const int xx = e / kn, c = e % kn, gr = col0 + xx;
-                    if (gr < dr) x = H[(int64_t)gr * dr + kb + c];
-                    sm.sb[c][xx] = x;
-                }
-            }
+            const int kn = min(HV_KMAX, K - kb), kn4 = (kn + 3) & ~3;
+            float ra[16], rb[16];
+            item_load<HV_KMAX>(ph, H, W, dl, dr, row0, col0, kb, kn, lt, ra, rb);
+            item_store<HV_KMAX>(sm, ph, 0, kn4, lt, ra, rb);
             sync();
-#pragma unroll 8
-            for (int j = 0; j < kn; ++j) {
-                const float a0 = sm.sa[ty][j], a1 = sm.sa[ty + 16][j], b0 = sm.sb[j][tx], b1 = sm.sb[j][tx + 16];
-                acc[0][0] = fmaf(a0, b0, acc[0][0]);
-                acc[0][1] = fmaf(a0, b1, acc[0][1]);
-                acc[1][0] = fmaf(a1, b0, acc[1][0]);
-                acc[1][1] = fmaf(a1, b1, acc[1][1]);
-            }
+            item_mma(sm, 0, kn4, ty, tx, acc);
             sync();
         }
     }
-    if (part != HV_LEFT) {
+    if (terms) {
         AbStage<float, 32, 32> &S = sm.S;
-        for (int tb = op.term_ptr[k]; tb < op.term_ptr[k + 1]; tb += AB_MAXT) {
-            const int nt = min(AB_MAXT, op.term_ptr[k + 1] - tb);
-            ab_stage<float, 32, 32>(S, v, tb, nt, row0, col0, dl, dr, op.drs, op.off, op.terms, op.ab_rp,
-                                    op.ab_col, op.ab_val, lt, 256, sync);
-            if (!S.multi) {
-                for (int tt = 0; tt < nt; ++tt) {
-                    const float *Wq = S.wq[tt];
-                    const int drq = S.drq[tt];
+        for (int tb = t0; tb < t1; tb += AB_MAXT) {
+            const int nt = min(AB_MAXT, t1 - tb);
+            bool multi = false;
+            if (eo >= 0) {
+                if (tb != t0) ell_load(tb, nt);
+                if (lt < nt) {
+                    S.wq[lt] = v + ((int64_t)(unsigned)hd.x | ((int64_t)hd.y << 32));
+                    S.drq[lt] = hd.z;
+                }
 #pragma unroll
-                    for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-                        for (int cc = 0; cc < 2; ++cc) {
-                            const int aj = S.ac[tt][ty + 16 * rr], bj = S.bc[tt][tx + 16 * cc];
-                            if (aj >= 0 && bj >= 0)
-                                acc[rr][cc] = fmaf(S.av[tt][ty + 16 * rr] * S.bv[tt][tx + 16 * cc],
-                                                   Wq[(int64_t)aj * drq + bj], acc[rr][cc]);
+                for (int q = 0; q < NE; ++q) {
+                    const int e = lt + q * 256;
+                    if (e < nt * 64) {
+                        const int tt = e >> 6, r = e & 63;
+                        if (r < 32) {
+                            S.ac[tt][r] = ee[q].x;
+                            S.av[tt][r] = __int_as_float(ee[q].y);
+                        } else {
+                            S.bc[tt][r - 32] = ee[q].x;
+                            S.bv[tt][r - 32] = __int_as_float(ee[q].y);
                         }
+                    }
+                }
+                sync();
+            } else {
+                ab_stage<float, 32, 32>(S, v, tb, nt, row0, col0, dl, dr, op.drs, op.off, op.terms, op.ab_rp,
+                                        op.ab_col, op.ab_val, lt, 256, sync);
+                multi = S.multi != 0;
+            }
+            if (!multi) {
+                // the gathers of eight terms issued before their FMAs
+                for (int t8 = 0; t8 < nt; t8 += 8) {
+                    float g[8][2][2], f[8][2][2];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int tt = t8 + u;
+                        const bool on = tt < nt;
+                        const float *Wq = on ? S.wq[tt] : nullptr;
+                        const int drq = on ? S.drq[tt] : 0;
+#pragma unroll
+                        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+                            for (int cc = 0; cc < 2; ++cc) {
+                                const int aj = on ? S.ac[tt][ty + 16 * rr] : -1;
+                                const int bj = on ? S.bc[tt][2 * tx + cc] : -1;
+                                const bool hit = aj >= 0 && bj >= 0;
+                                f[u][rr][cc] = hit ? S.av[tt][ty + 16 * rr] * S.bv[tt][2 * tx + cc] : 0.f;
+                                g[u][rr][cc] = hit ? Wq[(int64_t)aj * drq + bj] : 0.f;
+                            }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+#pragma unroll
+                        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+                            for (int cc = 0; cc < 2; ++cc) acc[rr][cc] = fmaf(f[u][rr][cc], g[u][rr][cc], acc[rr][cc]);
                 }
             } else {
                 for (int rr = 0; rr < 2; ++rr)
                     for (int cc = 0; cc < 2; ++cc) {
-                        const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+                        const int il = row0 + ty + 16 * rr, ir = col0 + 2 * tx + cc;
                         if (il < dl && ir < dr)
                             acc[rr][cc] = ab_csr<float>(acc[rr][cc], v, tb, nt, il, ir, op.drs, op.off, op.terms,
                                                         op.ab_rp, op.ab_col, op.ab_val);
@@ -338,16 +473,16 @@ __device__ __forceinline__ float hv32_item(int4 t, const float *__restrict__ v, 
             sync();
         }
     }
-    float *out = (part == HV_LEFT ? slot1 : slot0) + o;
+    float *out = slots[part == HV_LEFT ? 1 : (part == HV_RIGHT ? 2 : 0)] + o;
     float p = 0.f;
     for (int rr = 0; rr < 2; ++rr)
         for (int cc = 0; cc < 2; ++cc) {
-            const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
+            const int il = row0 + ty + 16 * rr, ir = col0 + 2 * tx + cc;
             if (il < dl && ir < dr) {
-                const int64_t idx = (int64_t)il * dr + ir;
+                const int64_t idx2 = (int64_t)il * dr + ir;
                 const float y = acc[rr][cc] * scale;
-                out[idx] = y;
-                p = fmaf(W[idx] * scale, y, p);
+                out[idx2] = y;
+                p = fmaf(W[idx2] * scale, y, p);
             }
         }
     return p;

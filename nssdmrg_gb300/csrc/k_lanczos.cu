@@ -648,10 +648,10 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
 struct ChunkArgs {
     OrthArgs o;                  // V, n, mmax, pstride, alpha/beta, part, bar, flags, mirrors, anchors
     float *buf[2];               // w buffers, iteration j reads buf[j & 1], writes buf[(j+1) & 1]
-    float *slot[2];              // H v_j parts
+    float *slot[3];              // H v_j parts
     int j0, jend;
     int first_from_v;            // iteration j0 reads V[j0] itself (start or restart)
-    const int4 *items;
+    const ItemRec *items;
     int nitems;
     Hv32Ops op;
 };
@@ -726,7 +726,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         // H v_j into the slots, alpha partials from the items
         float ap = 0.f;
         for (int ti = 2 * blk + grp; ti < a.nitems; ti += 2 * G)
-            ap += hv32_item(a.items[ti], x, a.slot[0], a.slot[1], a.op, ism[grp], lt, GroupSync{1 + grp}, sc);
+            ap += hv32_item(a.items[ti], x, a.slot, a.op, ism[grp], lt, GroupSync{1 + grp}, sc);
         {
             float a1[1] = {ap};
             block_sums<float, 1>(a1, scr);
@@ -752,11 +752,11 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         {
             float *vj = V + (int64_t)jj * n;
             const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
-            const float *s0 = a.slot[0], *s1 = a.slot[1];
+            const float *s0 = a.slot[0], *s1 = a.slot[1], *s2 = a.slot[2];
             for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
                 const float v = x[i] * sc;
                 if (!first) vj[i] = v;
-                float w = (s0[i] + s1[i]) - alpha0 * v;
+                float w = (s0[i] + s1[i] + s2[i]) - alpha0 * v;
                 if (jj > 0) w -= beta_prev * vjm[i];
                 y[i] = w;
                 if (anc) {
@@ -1027,7 +1027,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
         NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS, csm));
         if (occ2 >= 1) {
             NSS_CUDA_TRY(c, ctx_alloc(c, &z.wbuf32, (size_t)2 * n));
-            NSS_CUDA_TRY(c, ctx_alloc(c, &z.slot32, (size_t)2 * n));
+            NSS_CUDA_TRY(c, ctx_alloc(c, &z.slot32, (size_t)3 * n));
             z.chunk_smem = csm;
             z.chunk_ok = true;
         }
@@ -1153,8 +1153,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
     // mixed method without tensor-core sectors: one persistent launch per chunk
     const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.ntiles_tc == 0;
-    if (use_chunk)   // slot 1 regions that no item writes must read as zero
-        NSS_CUDA_TRY(c, cudaMemsetAsync(z.slot32 + n, 0, (size_t)n * sizeof(float), st));
+    if (use_chunk)   // slot 1 and 2 regions that no item writes must read as zero
+        NSS_CUDA_TRY(c, cudaMemsetAsync(z.slot32 + n, 0, (size_t)2 * n * sizeof(float), st));
     bool from_v = true;   // the next chunk starts from V[j0] (start, restart)
     auto enqueue_chunk = [&](int j0, int slot) -> int {
         const int jend = std::min(mmax, j0 + CHECK);
@@ -1168,6 +1168,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             ca.first_from_v = from_v ? 1 : 0;
             ca.slot[0] = z.slot32;
             ca.slot[1] = z.slot32 + n;
+            ca.slot[2] = z.slot32 + 2 * n;
             ca.items = c.sb.d_items32;
             ca.nitems = c.sb.nitems32;
             ca.op = hv32_ops(c.sb);

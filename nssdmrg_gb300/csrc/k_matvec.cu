@@ -39,7 +39,8 @@ void sb_release(Ctx &c) {
     void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
                     s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
                     s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err,
-                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32, s.d_items32};
+                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32, s.d_items32, s.d_item_ell, s.d_ell,
+                    s.d_term_hdr};
     for (void *p : ptrs) ctx_free(c, p);
     s = DevSb{};
 }
@@ -248,7 +249,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
         }
     }
     // work items of the persistent kernel: 32x32 tiles of every sector,
-    // split into an H_L part and an H_R + A x B part when a K loop is long
+    // split into H_L, H_R and A x B parts when a K loop is long
     std::vector<int4> items32;
     for (int k = 0; k < s.nsb; ++k) {
         const bool split = std::max(s.dls[k], s.drs[k]) > 64;
@@ -257,6 +258,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
                 if (split) {
                     items32.push_back(make_int4(k, r, cc, HV_LEFT));
                     items32.push_back(make_int4(k, r, cc, HV_RIGHT));
+                    if (s.term_ptr[k + 1] > s.term_ptr[k]) items32.push_back(make_int4(k, r, cc, HV_TERMS));
                 } else {
                     items32.push_back(make_int4(k, r, cc, HV_FULL));
                 }
@@ -266,10 +268,65 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     std::stable_sort(items32.begin(), items32.end(), [&](const int4 &x, const int4 &y) {
         auto cost = [&](const int4 &t) {
             const int dl = s.dls[t.x], dr = s.drs[t.x];
-            return t.w == HV_LEFT ? dl : (t.w == HV_RIGHT ? dr + 32 : dl + dr + 32);
+            return t.w == HV_LEFT ? dl : (t.w == HV_RIGHT ? dr : (t.w == HV_TERMS ? 48 : dl + dr + 48));
         };
         return cost(x) > cost(y);
     });
+    // A x B tables of the items that carry terms: for each term of the
+    // sector, the (column, value) of the tile's 32 rows of A and 32 columns
+    // of B in the FP32 pool (-1: empty row); items with a row of several
+    // elements keep -1 and use the CSR loop
+    std::vector<int> item_ell(items32.size(), -1);
+    std::vector<int2> ell;
+    for (size_t ii = 0; ii < items32.size(); ++ii) {
+        const int4 it = items32[ii];
+        if (it.w != HV_FULL && it.w != HV_TERMS) continue;
+        const int k = it.x, dl = s.dls[k], dr = s.drs[k];
+        const size_t base = ell.size();
+        bool ok = true;
+        for (int ti = s.term_ptr[k]; ti < s.term_ptr[k + 1] && ok; ++ti) {
+            const DevTerm &tm = terms32[ti];
+            for (int side = 0; side < 2 && ok; ++side) {
+                const int64_t rp = side == 0 ? tm.a_rp : tm.b_rp;
+                const int lim = side == 0 ? dl : dr, first = side == 0 ? it.y : it.z;
+                for (int r = 0; r < 32; ++r) {
+                    const int g = first + r;
+                    int2 e = make_int2(-1, 0);
+                    if (g < lim) {
+                        const int p0 = rowptr32[rp + g], p1 = rowptr32[rp + g + 1];
+                        if (p1 - p0 > 1) { ok = false; break; }
+                        if (p1 > p0) {
+                            float fv = val32[p0];
+                            int bits;
+                            std::memcpy(&bits, &fv, sizeof(bits));
+                            e = make_int2(col32[p0], bits);
+                        }
+                    }
+                    ell.push_back(e);
+                }
+            }
+        }
+        if (ok) item_ell[ii] = (int)base;
+        else ell.resize(base);
+    }
+    if (ell.empty()) ell.push_back(make_int2(-1, 0));
+    std::vector<int4> term_hdr(std::max<size_t>(terms32.size(), 1), make_int4(0, 0, 0, 0));
+    for (size_t ti = 0; ti < terms32.size(); ++ti) {
+        const int64_t of = s.off[terms32[ti].in_sec];
+        term_hdr[ti] = make_int4((int)(uint32_t)(of & 0xffffffff), (int)(of >> 32), s.drs[terms32[ti].in_sec], 0);
+    }
+    std::vector<ItemRec> recs(items32.size());
+    for (size_t ii = 0; ii < items32.size(); ++ii) {
+        const int4 it = items32[ii];
+        const int k = it.x;
+        const int64_t of = s.off[k], hlo = s.hl_off[k], hro = s.hr_off[k];
+        auto lo = [](int64_t x) { return (int)(uint32_t)(x & 0xffffffff); };
+        auto hi = [](int64_t x) { return (int)(x >> 32); };
+        recs[ii].a = it;
+        recs[ii].b = make_int4(s.dls[k], s.drs[k], s.term_ptr[k], s.term_ptr[k + 1]);
+        recs[ii].c = make_int4(lo(of), hi(of), item_ell[ii], 0);
+        recs[ii].d = make_int4(lo(hlo), hi(hlo), lo(hro), hi(hro));
+    }
     s.nitems32 = (int)items32.size();
     s.ntiles32 = (int)tiles32.size();
     s.ntiles_tc = (int)tiles_tc.size();
@@ -279,7 +336,9 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
         (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_ab_rowptr32, rowptr32)) ||
         (rc = upload_vec(c, &s.d_ab_col32, col32)) || (rc = upload_vec(c, &s.d_terms32, terms32)) ||
-        (rc = upload_vec(c, &s.d_tiles32, tiles32)) || (rc = upload_vec(c, &s.d_items32, items32)) ||
+        (rc = upload_vec(c, &s.d_tiles32, tiles32)) || (rc = upload_vec(c, &s.d_items32, recs)) ||
+        (rc = upload_vec(c, &s.d_item_ell, item_ell)) || (rc = upload_vec(c, &s.d_ell, ell)) ||
+        (rc = upload_vec(c, &s.d_term_hdr, term_hdr)) ||
         (rc = upload_vec(c, &s.d_tiles_tc, tiles_tc)) || (rc = upload_vec(c, &s.d_tc_err, tc_err)))
         return rc;
     if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
@@ -402,6 +461,9 @@ Hv32Ops hv32_ops(const DevSb &s) {
     op.ab_rp = s.d_ab_rowptr32;
     op.ab_col = s.d_ab_col32;
     op.ab_val = s.d_ab_val32;
+    op.item_ell = s.d_item_ell;
+    op.ell = s.d_ell;
+    op.term_hdr = s.d_term_hdr;
     return op;
 }
 
