@@ -52,6 +52,7 @@ def parse():
                     help="headline path; the other one is timed alongside for comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -213,6 +214,65 @@ def measure_sweeps(nss, device):
     return out
 
 
+BATCH_CASE = {"workload": "hubbard_batch_64", "instances": 64, "distinct": 8, "seed": 42, "U": [0.0, 8.0],
+              "L": [16, 24, 32, 48], "m": [64, 128, 256, 384], "t": 1.0, "filling": "half",
+              "lanc_tolerance": 1e-12, "lanc_niter": 256}
+
+
+def measure_batch(nss, device):
+    """Batched solves (the fourth benchmark configuration, scaled as noted):
+    Hubbard superblocks at the last infinite step, U ~ Uniform[0,8], L and m
+    drawn from the listed sets with a fixed seed; `distinct` superblocks are
+    generated and each is uploaded into instances/distinct contexts (every
+    instance is its own solve with its own start vector).  Solves/s of one
+    nss_eigh_batch call against the same solves one by one (mixed and FP64),
+    and the largest |dE| between the batched and the single results."""
+    rng = np.random.default_rng(BATCH_CASE["seed"])
+    descs, drivers, meta = [], [], []
+    t0 = time.perf_counter()
+    for k in range(BATCH_CASE["distinct"]):
+        L = int(rng.choice(BATCH_CASE["L"]))
+        m = int(rng.choice(BATCH_CASE["m"]))
+        u = float(rng.uniform(*BATCH_CASE["U"]))
+        d = nss.DMRG(nss.MODEL_HUBBARD, L // 2, m, u=u, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1,
+                     device=device)
+        d.prepare_last()
+        drivers.append(d)
+        descs.append(d.export_superblock())
+        meta.append({"L": L, "m": m, "U": round(u, 4), "N": int(d.sb.n)})
+    t_gen = time.perf_counter() - t0
+    reps = BATCH_CASE["instances"] // BATCH_CASE["distinct"]
+    sbs = []
+    for k in range(BATCH_CASE["distinct"]):
+        for r in range(reps):
+            s = nss.Superblock(device)
+            s.upload_desc(descs[k])
+            sbs.append(s)
+    tol, nit = BATCH_CASE["lanc_tolerance"], BATCH_CASE["lanc_niter"]
+    seeds = np.arange(1, len(sbs) + 1, dtype=np.uint64)
+    nss.eigh_batch(sbs[:2], nitermax=nit, tol=tol)            # warm-up
+    t0 = time.perf_counter()
+    eb, nops = nss.eigh_batch(sbs, nitermax=nit, tol=tol, seeds=seeds)
+    t_batch = time.perf_counter() - t0
+    single = {}
+    for name, prec in (("mixed", nss.NSS_PREC_MIXED), ("fp64", nss.NSS_PREC_FP64)):
+        es = []
+        t0 = time.perf_counter()
+        for i, s in enumerate(sbs):
+            ev, _, _ = s.sb_diag(neigen=1, nitermax=nit, tol=tol, seed=int(seeds[i]), precision=prec,
+                                 want_vectors=False)
+            es.append(ev[0])
+        single[name] = (time.perf_counter() - t0, np.array(es))
+    n = len(sbs)
+    de = float(np.max(np.abs(eb - single["fp64"][1]) / np.abs(single["fp64"][1])))
+    return {"config": BATCH_CASE, "superblocks": meta, "generate_s": t_gen,
+            "batched": {"solves_per_s": n / t_batch, "s": t_batch, "matvecs_mean": float(np.mean(nops))},
+            "one_by_one_mixed": {"solves_per_s": n / single["mixed"][0], "s": single["mixed"][0]},
+            "one_by_one_fp64": {"solves_per_s": n / single["fp64"][0], "s": single["fp64"][0]},
+            "speedup_batched_vs_fp64": single["fp64"][0] / t_batch,
+            "dE_rel_batched_vs_fp64_max": de}
+
+
 def run_gpu(args):
     import torch
 
@@ -347,6 +407,7 @@ def run_gpu(args):
     e2e_value = f_hv * statistics.mean(numops) / (statistics.mean(e2e_times) / 1e3) / 1e12 * world
 
     sweeps = measure_sweeps(nss, local) if not args.no_sweeps else None
+    batch = measure_batch(nss, local) if not args.no_batch else None
 
     out = None
     if rank == 0:
@@ -392,6 +453,7 @@ def run_gpu(args):
                          "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")},
             "core_probe": CORE_PROBE,
             "sweeps": sweeps,
+            "batch": batch,
             "setup_s": t_prep,
         }
         if not args.no_cpu_baseline and world == 1:

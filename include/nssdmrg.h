@@ -139,6 +139,19 @@ typedef struct {
     double  entropy;       /* -sum lambda log(lambda + 1e-32) */
 } nss_rdm_side;
 
+/* Batched ground states: nb independent superblocks, one context each (all
+ * on one device, each with a superblock uploaded), solved together with the
+ * mixed method (precision NSS_PREC_MIXED semantics, one eigenpair) by one
+ * persistent cooperative launch per group of iterations, the H*psi work
+ * items of all solves shared out over the whole GPU.  evals[b] receives the
+ * FP64 energy of solve b, numops[b] its H*psi count; each context keeps its
+ * ground state for nss_rdm.  No counterpart in the reference (it solves one
+ * superblock at a time); each result equals the one nss_eigh gives for that
+ * context alone to within the solver tolerance.  Superblocks with
+ * tensor-core sectors (NSS_TC_MIN_DL) are rejected. */
+int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const uint64_t *seeds,
+                   double *evals, int *numops);
+
 /* Reduced density matrices of the ground state (column 0 of the last
  * nss_eigh, or `psi` when not NULL, length nss_sb_dim), their block
  * eigendecomposition and the truncation choice (src/DMRG_RDM.f90:18-221,

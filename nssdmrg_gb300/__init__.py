@@ -120,6 +120,7 @@ def lib():
         "nss_arrow_lowest": (C.c_int, [C.c_int, D, P, P, P, D, C.POINTER(D), P, C.POINTER(D)]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
+        "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
         "nss_sb_counts": (C.c_int, [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]),
         "nss_sb_tables": (C.c_int, [P, P, P, P, P, P]),
@@ -180,6 +181,21 @@ def arrow_lowest(theta0: float, m, a, b, b_last: float = 0.0):
     if rc != 0:
         raise NssError(rc, lib().nss_last_error(None).decode())
     return lam.value, c, res.value
+
+
+def eigh_batch(superblocks, nitermax: int = 512, tol: float = 1e-12, seeds=None):
+    """Ground states of several Superblocks (one context each) solved together
+    by the batched persistent kernel (mixed precision).  Returns (energies,
+    numops); each Superblock keeps its ground state for sb_get_rdm."""
+    nb = len(superblocks)
+    ctxs = (C.c_void_p * nb)(*[sb._ctx for sb in superblocks])
+    sd = np.ascontiguousarray(seeds if seeds is not None else np.arange(1, nb + 1), dtype=np.uint64)
+    ev = np.zeros(nb)
+    nops = np.zeros(nb, dtype=np.int32)
+    rc = lib().nss_eigh_batch(ctxs, nb, int(nitermax), float(tol), _ptr(sd), _ptr(ev), _ptr(nops))
+    if rc != 0:
+        raise NssError(rc, lib().nss_last_error(superblocks[0]._ctx).decode())
+    return ev, nops
 
 
 class _Keep:

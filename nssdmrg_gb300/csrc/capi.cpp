@@ -247,6 +247,26 @@ int nss_eigh(nss_ctx *ctx, int neigen, int nitermax, int ncv, double tol, uint64
     });
 }
 
+int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const uint64_t *seeds, double *evals,
+                   int *numops) {
+    if (!ctxs || nb < 1 || !ctxs[0]) {
+        g_err = "nss_eigh_batch: need at least one context";
+        return NSS_ERR_INVALID;
+    }
+    for (int b = 0; b < nb; ++b)
+        if (!ctxs[b]) {
+            g_err = "nss_eigh_batch: NULL context";
+            return NSS_ERR_INVALID;
+        }
+    nss_ctx *c0 = ctxs[0];
+    return guarded(c0, [&] {
+        cudaSetDevice(c0->c.device);
+        std::vector<nss::Ctx *> cs((size_t)nb);
+        for (int b = 0; b < nb; ++b) cs[b] = &ctxs[b]->c;
+        return nss::lanczos_eigh_batch(cs.data(), nb, nitermax, tol, seeds, evals, numops);
+    });
+}
+
 int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rdm_side out[2],
             double *lambda_left, double *lambda_right, int32_t *kept_left, int32_t *kept_right, double *u_left,
             double *u_right) {

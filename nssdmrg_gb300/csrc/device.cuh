@@ -62,6 +62,7 @@ struct DevSb {
     int ntiles32 = 0;
     struct ItemRec *d_items32 = nullptr;   // work items of the persistent mixed kernel
     int nitems32 = 0;
+    std::vector<int> item_cost;        // host: relative cost of each item (batch ordering)
     int *d_item_ell = nullptr;         // per item: offset of its A x B table (-1: CSR loop)
     int2 *d_ell = nullptr;             // the tables
     int4 *d_term_hdr = nullptr;        // per FP32 term: input-sector offset (lo, hi), its Dr
@@ -101,6 +102,8 @@ struct DevLanczos {
     float *slot32 = nullptr;     // [3][n] H*psi parts of the persistent chunk kernel
     size_t chunk_smem = 0;
     bool chunk_ok = false;       // the chunk kernel fits (one CTA per SM)
+    float *pitem = nullptr;      // per-item alpha partials of the batched kernel
+    int cap_pitem = 0;
 };
 
 struct DevRdm {
@@ -177,6 +180,10 @@ int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy);
 // k_lanczos.cu
 int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,
                  int precision, double *evals_host, int *numop);
+// several mixed-precision ground-state solves, one context each, advanced
+// together by the batched persistent kernel; cs[0]'s stream runs them
+int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const uint64_t *seeds,
+                       double *evals_host, int *numops);
 void lanczos_release(Ctx &c);
 
 // k_rdm.cu

@@ -871,6 +871,304 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
     publish();
 }
 
+// ---------------------------------------------------------------------------
+// Batched persistent kernel: several independent mixed-precision solves (one
+// context each) advance together, one launch per chunk of iterations.  The
+// H*psi work items of all solves are shared out over all CTAs (longest
+// first); each solve's rows belong to its own range of CTAs, which run its
+// three-term step, projections and updates.  The grid barriers are global,
+// so every CTA takes the same barrier sequence: the per-solve decisions that
+// change it (second projection, breakdown, end of the chunk) are recomputed
+// by every CTA from the solves' partial sums, in the same order, so all CTAs
+// agree.  Solves stop within a launch only at their chunk end or at a
+// breakdown; the host checks convergence between launches.
+
+struct BatchSolve {
+    ChunkArgs c;                 // per-solve arguments (c.o.bar unused)
+    float *pitem;                // [c.nitems] alpha partials of the solve's items
+    int cta0, ncta;              // CTAs owning the solve's rows
+    int active;                  // takes part in this launch
+    int pad;
+};
+
+struct BatchArgs {
+    const BatchSolve *s;
+    int ns;
+    int nitems;                  // items of all active solves
+    const int2 *gitems;          // (solve, item) in processing order
+    float *st;                   // [4 ns] per-solve scalars published inside an iteration
+    unsigned *bar;               // global barrier
+    int *err;
+    int steps;                   // iterations of this launch
+};
+
+constexpr int BATCH_MAX = 160;   // solves per launch (each needs a CTA)
+
+__global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
+    constexpr int CW = OrthCW<float>::value;
+    extern __shared__ __align__(16) unsigned char batch_raw[];
+    Item32Smem *ism = (Item32Smem *)batch_raw;
+    float *osm = (float *)(batch_raw + 2 * sizeof(Item32Smem));
+    __shared__ float rec_a[CHUNK_MAXIT], rec_b[CHUNK_MAXIT], rec_m[CHUNK_MAXIT];
+    __shared__ float bprev[BATCH_MAX], balpha[BATCH_MAX], bbb[BATCH_MAX];
+    __shared__ int alive[BATCH_MAX], p2[BATCH_MAX], brkm[BATCH_MAX];
+    __shared__ int my_s, any_p2;
+    const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x, grp = tid >> 8, lt = tid & 255;
+    const int ns = B.ns;
+    unsigned epoch = 0;
+    if (tid == 0) {
+        my_s = -1;
+        for (int s = 0; s < ns; ++s)
+            if (B.s[s].active && blk >= B.s[s].cta0 && blk < B.s[s].cta0 + B.s[s].ncta) my_s = s;
+    }
+    for (int s = tid; s < ns; s += ORTH_THREADS) {
+        const BatchSolve &S = B.s[s];
+        const int j0 = S.c.j0;
+        alive[s] = S.active && !*(volatile int *)&S.c.o.flags[F_STOP] && S.c.jend > j0;
+        bprev[s] = j0 > 0 ? (float)S.c.o.beta[j0 - 1] : 0.f;
+        brkm[s] = 0;
+    }
+    __syncthreads();
+    const int me = my_s;
+    // this CTA's own solve (if any)
+    const BatchSolve *Mp = me >= 0 ? &B.s[me] : nullptr;
+    const int Gs = Mp ? Mp->ncta : 1, lb = Mp ? blk - Mp->cta0 : 0;
+    const int ps = Mp ? Mp->c.o.pstride : 8;
+    float *hs = osm;
+    float *red = hs + ps;
+    float *scr = red + orth_redsz(ps, CW);
+    float *bc = scr + 8 * ORTH_WARPS;
+    const int64_t n = Mp ? Mp->c.o.n : 0;
+    const int64_t chunk = (n + Gs - 1) / Gs;
+    const int64_t i0 = min(n, (int64_t)lb * chunk), i1 = min(n, i0 + chunk);
+    float *V = Mp ? (float *)Mp->c.o.V : nullptr;
+    float *pA = Mp ? (float *)Mp->c.o.part : nullptr;
+    float *pH = pA + PA_COLS * Gs, *pB = pH + (int64_t)ps * Gs, *pH2 = pB + Gs, *pB2 = pH2 + (int64_t)ps * Gs;
+    const float *au = Mp ? (const float *)Mp->c.o.anc_u : nullptr;
+    const float *ar = Mp ? (const float *)Mp->c.o.anc_r : nullptr;
+    const float *ay = Mp ? (const float *)Mp->c.o.defl : nullptr;
+    const bool anc = au != nullptr;
+    const int nd = anc ? Mp->c.o.ndefl : 0;
+    const int nx = anc ? 3 + nd : 0;
+    int done = 0;
+    for (int step = 0; step < B.steps; ++step) {
+        // ---- H*psi of every running solve, all items over all CTAs
+        for (int gi = 2 * blk + grp; gi < B.nitems; gi += 2 * G) {
+            const int2 g = B.gitems[gi];
+            const BatchSolve &S = B.s[g.x];
+            const int tj = S.c.j0 + step;
+            if (!alive[g.x] || tj >= S.c.jend) continue;
+            const bool first = tj == S.c.j0 && S.c.first_from_v;
+            const float *x = first ? (const float *)S.c.o.V + (int64_t)tj * S.c.o.n : S.c.buf[tj & 1];
+            const float sc = first ? 1.f : 1.f / bprev[g.x];
+            float ap = hv32_item(S.c.items[g.y], x, S.c.slot, S.c.op, ism[grp], lt, GroupSync{1 + grp}, sc);
+            // group sum of the alpha partial (named barrier of the group)
+            ap = warp_sum<float>(ap);
+            if ((lt & 31) == 0) scr[grp * 8 + (lt >> 5)] = ap;
+            GroupSync{1 + grp}();
+            if (lt == 0) {
+                float t = 0.f;
+                for (int q = 0; q < 8; ++q) t += scr[grp * 8 + q];
+                S.pitem[g.y] = t;
+            }
+            GroupSync{1 + grp}();
+        }
+        if (!grid_sync(B.bar, epoch, B.err)) break;
+        const bool run = me >= 0 && alive[me] && Mp->c.j0 + step < Mp->c.jend;
+        const int jj = Mp ? Mp->c.j0 + step : 0, m = jj + 1;
+        const bool first = run && jj == Mp->c.j0 && Mp->c.first_from_v;
+        const float *x = run ? (first ? V + (int64_t)jj * n : Mp->c.buf[jj & 1]) : nullptr;
+        const float sc = first ? 1.f : (me >= 0 ? 1.f / bprev[me] : 1.f);
+        float *y = run ? Mp->c.buf[(jj + 1) & 1] : nullptr;
+        float ex[CHUNK_EXTRA];
+#pragma unroll
+        for (int q = 0; q < CHUNK_EXTRA; ++q) ex[q] = 0.f;
+        float alpha0 = 0.f;
+        if (run) {
+            {   // alpha from the item partials, fixed order
+                float t = 0.f;
+                if (tid < 32) {
+                    for (int q = tid; q < Mp->c.nitems; q += 32) t += __ldcg(Mp->pitem + q);
+                    t = warp_sum<float>(t);
+                    if (tid == 0) bc[0] = t;
+                }
+                __syncthreads();
+                alpha0 = bc[0];
+            }
+            float *vj = V + (int64_t)jj * n;
+            const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
+            const float *s0 = Mp->c.slot[0], *s1 = Mp->c.slot[1], *s2 = Mp->c.slot[2];
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                const float v = x[i] * sc;
+                if (!first) vj[i] = v;
+                float w = (s0[i] + s1[i] + s2[i]) - alpha0 * v;
+                if (jj > 0) w -= bprev[me] * vjm[i];
+                y[i] = w;
+                if (anc) {
+                    ex[0] += au[i] * w;
+                    ex[1] += ar[i] * v;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < nd) ex[2 + k] += ay[(int64_t)k * n + i] * w;
+                }
+            }
+            __syncthreads();
+            cta_dots<float, CW>(V, m, y, n, i0, i1, true, red, pH + lb, Gs);
+            if (anc) {
+                block_sums<float, CHUNK_EXTRA>(ex, scr);
+                if (tid == 0) {
+                    pH[(int64_t)(m + 1) * Gs + lb] = ex[0];
+                    pH[(int64_t)(m + 2) * Gs + lb] = ex[1];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < nd) pH[(int64_t)(m + 3 + k) * Gs + lb] = ex[2 + k];
+                }
+            }
+        }
+        if (!grid_sync(B.bar, epoch, B.err)) break;
+        float hj = 0.f, mj = 0.f;
+        auto update = [&](int xoff) -> float {
+            float ss = 0.f;
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                float w = y[i];
+#pragma unroll 32
+                for (int l = 0; l < m; ++l) w -= V[(int64_t)l * n + i] * hs[l];
+                if (anc) {
+                    w -= hs[xoff] * au[i];
+                    for (int k = 0; k < nd; ++k) w -= hs[xoff + 2 + k] * ay[(int64_t)k * n + i];
+                }
+                y[i] = w;
+                ss += w * w;
+            }
+            return ss;
+        };
+        if (run) {
+            grid_columns<float>(pH, Gs, m + 1 + nx, hs);
+            __syncthreads();
+            hj = hs[jj];
+            mj = anc ? hs[m + 2] : 0.f;
+            if (lb == 0 && tid == 0) {
+                B.st[4 * me + 0] = alpha0 + hj;
+                B.st[4 * me + 1] = hs[m];
+                B.st[4 * me + 2] = 0.f;
+            }
+            float s1[1] = {update(m + 1)};
+            block_sums<float, 1>(s1, scr);
+            if (tid == 0) pB[lb] = s1[0];
+        }
+        if (!grid_sync(B.bar, epoch, B.err)) break;
+        // every CTA: beta^2 and the second-projection decision of every solve
+        if (tid == 0) any_p2 = 0;
+        __syncthreads();
+        for (int s = tid; s < ns; s += ORTH_THREADS) {
+            const BatchSolve &S = B.s[s];
+            p2[s] = 0;
+            if (!alive[s] || S.c.j0 + step >= S.c.jend) continue;
+            const float *pBs = (const float *)S.c.o.part + (PA_COLS + (int64_t)S.c.o.pstride) * S.ncta;
+            float t = 0.f;
+            for (int b = 0; b < S.ncta; ++b) t += __ldcg(pBs + b);
+            bbb[s] = t;
+            balpha[s] = __ldcg(B.st + 4 * s + 0);
+            if (t < 0.5f * __ldcg(B.st + 4 * s + 1)) {
+                p2[s] = 1;
+                any_p2 = 1;
+            }
+        }
+        __syncthreads();
+        if (any_p2) {
+            const bool mine = run && p2[me];
+            if (mine) {
+                cta_dots<float, CW>(V, m, y, n, i0, i1, false, red, pH2 + lb, Gs);
+                if (anc) {
+#pragma unroll
+                    for (int q = 0; q < CHUNK_EXTRA; ++q) ex[q] = 0.f;
+                    for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                        const float w = y[i];
+                        ex[0] += au[i] * w;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k < nd) ex[2 + k] += ay[(int64_t)k * n + i] * w;
+                    }
+                    block_sums<float, CHUNK_EXTRA>(ex, scr);
+                    if (tid == 0) {
+                        pH2[(int64_t)m * Gs + lb] = ex[0];
+                        pH2[(int64_t)(m + 1) * Gs + lb] = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k < nd) pH2[(int64_t)(m + 2 + k) * Gs + lb] = ex[2 + k];
+                    }
+                }
+            }
+            if (!grid_sync(B.bar, epoch, B.err)) break;
+            if (mine) {
+                grid_columns<float>(pH2, Gs, m + (anc ? 2 + nd : 0), hs);
+                __syncthreads();
+                if (lb == 0 && tid == 0) B.st[4 * me + 2] = hs[jj];
+                float s1[1] = {update(m)};
+                block_sums<float, 1>(s1, scr);
+                if (tid == 0) pB2[lb] = s1[0];
+            }
+            if (!grid_sync(B.bar, epoch, B.err)) break;
+            for (int s = tid; s < ns; s += ORTH_THREADS) {
+                if (!p2[s]) continue;
+                const BatchSolve &S = B.s[s];
+                const float *pB2s = (const float *)S.c.o.part + (PA_COLS + 2 * (int64_t)S.c.o.pstride + 1) * S.ncta;
+                float t = 0.f;
+                for (int b = 0; b < S.ncta; ++b) t += __ldcg(pB2s + b);
+                bbb[s] = t;
+                balpha[s] += __ldcg(B.st + 4 * s + 2);
+            }
+            __syncthreads();
+        }
+        // every CTA: beta, breakdown, next scale of every solve that ran
+        for (int s = tid; s < ns; s += ORTH_THREADS) {
+            const BatchSolve &S = B.s[s];
+            if (!alive[s] || S.c.j0 + step >= S.c.jend) continue;
+            const float beta = sqrtf(bbb[s]);
+            const int ms = S.c.j0 + step + 1;
+            if (ms < S.c.o.mmax) {
+                const float scale = fmaxf(fabsf(balpha[s]), S.c.j0 + step > 0 ? bprev[s] : 0.f);
+                if (!(beta > 1e-13f * fmaxf(scale, 1e-30f))) {
+                    brkm[s] = ms;
+                    alive[s] = 0;
+                }
+            }
+            bprev[s] = beta;
+        }
+        __syncthreads();
+        if (run) {
+            if (lb == 0 && tid == 0) {
+                rec_a[done] = balpha[me];
+                rec_b[done] = bprev[me];
+                rec_m[done] = mj;
+            }
+            ++done;
+        }
+    }
+    // publish the completed iterations of the own solve
+    if (me >= 0 && lb == 0 && tid == 0) {
+        const ChunkArgs &a = Mp->c;
+        for (int q = 0; q < done; ++q) {
+            const int j = a.j0 + q;
+            a.o.alpha[j] = (double)rec_a[q];
+            a.o.beta[j] = (double)rec_b[q];
+            a.o.h_alpha[j] = (double)rec_a[q];
+            a.o.h_beta[j] = (double)rec_b[q];
+            if (anc) a.o.h_m[j] = (double)rec_m[q];
+        }
+        if (brkm[me]) {
+            a.o.flags[F_BREAK] = brkm[me];
+            a.o.flags[F_STOP] = 2;
+            a.o.h_flags[F_BREAK] = brkm[me];
+            a.o.h_flags[F_STOP] = 2;
+        }
+        __threadfence_system();
+    }
+    grid_exit(B.bar);
+}
+
+inline size_t batch_smem(int pstride_max) { return chunk_smem(pstride_max); }
+
 // Ritz vectors: out[e] = sum_l V[l] s_e[l]   (FP64 accumulation, FP64 out)
 template <class T>
 __global__ void __launch_bounds__(256) k_ritz(const T *__restrict__ V, int m, int64_t n,
@@ -1332,7 +1630,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
     void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.slot32, z.evecs, z.scal, z.part, z.counter,
-                    z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags};
+                    z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags, z.pitem};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
     if (z.h_ab) cudaFreeHost(z.h_ab);
@@ -1473,6 +1771,364 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     z.neigen_done = ne;
     if (numop) *numop = numop_;
     return NSS_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batched ground-state solves (mixed precision): every context keeps its own
+// superblock, Krylov basis and host mirrors; one cooperative launch of
+// k_batch32 per round runs CHECK iterations of every solve still going, then
+// the host checks each solve (tridiagonal or anchored problem) and moves it
+// through FP32 Lanczos -> anchored refinement -> FP64 energy, exactly as
+// lanczos_eigh does for one context.
+namespace {
+
+struct BatchState {
+    Ctx *c = nullptr;
+    int64_t n = 0;
+    int mmax = 0, phase = 1, j0 = 0, m_done = 0, numop = 0, rc = 0;
+    bool from_v = true, have_upper = false;
+    double tol = 0.0, theta0 = 0.0, result = 0.0;
+    uint64_t seed = 0, restarts = 0;
+    std::vector<double> theta, resid, upper, svec, work, cvec;
+    AnchorSpec as{};
+};
+
+}  // namespace
+
+int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const uint64_t *seeds,
+                       double *evals_host, int *numops) {
+    if (nb < 1 || nb > BATCH_MAX) {
+        cs[0]->err = "nss_eigh_batch: between 1 and " + std::to_string(BATCH_MAX) + " solves per batch";
+        return NSS_ERR_INVALID;
+    }
+    Ctx &c0 = *cs[0];
+    cudaStream_t st = c0.stream;
+    if (tol <= 0.0) tol = 1e-15;
+    if (nitermax <= 0) nitermax = 512;
+    std::vector<BatchState> S(nb);
+    int rc = NSS_OK;
+    for (int b = 0; b < nb; ++b) {
+        Ctx &c = *cs[b];
+        if (c.device != c0.device) { c0.err = "nss_eigh_batch: all contexts must use one device"; return NSS_ERR_INVALID; }
+        if (!c.sb.valid) { c0.err = "nss_eigh_batch: a context has no superblock"; return NSS_ERR_STATE; }
+        if (c.sb.ntiles_tc != 0) {
+            c0.err = "nss_eigh_batch: superblocks with tensor-core sectors are solved one by one (nss_eigh)";
+            return NSS_ERR_INVALID;
+        }
+        BatchState &B = S[b];
+        B.c = &c;
+        B.n = c.sb.n;
+        B.mmax = (int)std::min<int64_t>(B.n, nitermax);
+        B.tol = std::max(tol, mixed_tol());
+        B.seed = seeds ? seeds[b] : 1234;
+        B.theta.assign(4, 0.0);
+        B.resid.assign(4, 0.0);
+        B.upper.assign(4, 0.0);
+        if ((rc = ensure_lanczos(c, B.n, B.mmax + 1, true))) { c0.err = c.err; return rc; }
+        DevLanczos &z = c.lz;
+        if (!z.chunk_ok) { c0.err = "nss_eigh_batch: the persistent kernel does not fit this Krylov basis"; return NSS_ERR_INVALID; }
+        if (!z.pitem || z.cap_pitem < c.sb.nitems32) {
+            ctx_free(c, z.pitem);
+            z.pitem = nullptr;
+            NSS_CUDA_TRY(c, ctx_alloc(c, &z.pitem, (size_t)std::max(c.sb.nitems32, 1)));
+            z.cap_pitem = c.sb.nitems32;
+        }
+    }
+    const int G = c0.lz.orth_grid;
+    if (nb > G) { c0.err = "nss_eigh_batch: more solves than CTAs of the persistent kernel"; return NSS_ERR_INVALID; }
+    // per-solve start: mirrors, flags, random start vector
+    auto start_run = [&](BatchState &B) -> int {
+        Ctx &c = *B.c;
+        DevLanczos &z = c.lz;
+        volatile int *hf = z.h_flags;
+        for (int i = 0; i < F_NFLAGS + 8; ++i) hf[i] = 0;
+        for (int i = 0; i < 3 * (z.cap + 1); ++i) z.h_ab[i] = 0.0;
+        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta, 0, (z.cap + 1) * sizeof(double), st));
+        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.slot32 + B.n, 0, (size_t)2 * B.n * sizeof(float), st));
+        B.j0 = 0;
+        B.from_v = true;
+        B.have_upper = false;
+        return NSS_OK;
+    };
+    for (auto &B : S) {
+        Ctx &c = *B.c;
+        if ((rc = start_run(B))) return rc;
+        c0.launches += 2;
+        k_random<float><<<608, 256, 0, st>>>(c.lz.V32, B.n, B.seed, 0);
+        k_normalize<float><<<1, 1024, 0, st>>>(c.lz.V32, B.n);
+    }
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(c0.lz.counter, 0, 4 * sizeof(unsigned), st));
+    // device argument arrays (per call)
+    BatchSolve *d_solves = nullptr;
+    int2 *d_gitems = nullptr;
+    float *d_st = nullptr;
+    int tot_items = 0;
+    for (auto &B : S) tot_items += B.c->sb.nitems32;
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_solves, (size_t)nb));
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_gitems, (size_t)std::max(tot_items, 1)));
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_st, (size_t)4 * nb));
+    BatchSolve *h_solves = nullptr;
+    int2 *h_gitems = nullptr;
+    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&h_solves, sizeof(BatchSolve) * nb));
+    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&h_gitems, sizeof(int2) * std::max(tot_items, 1)));
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        ctx_free(c0, d_solves);
+        ctx_free(c0, d_gitems);
+        ctx_free(c0, d_st);
+        cudaFreeHost(h_solves);
+        cudaFreeHost(h_gitems);
+    };
+    auto fail = [&](int code) { cleanup(); return code; };
+    size_t smem_max = 0;
+    for (auto &B : S) smem_max = std::max(smem_max, B.c->lz.chunk_smem);
+    NSS_CUDA_TRY(c0, cudaFuncSetAttribute((const void *)k_batch32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_max));
+    double *r = c0.lz.scal + S_NSCAL + 4 * (c0.lz.cap + 2);   // refinement slots (context 0's scratch)
+    for (int round = 0; round < 100000; ++round) {
+        std::vector<int> act;
+        for (int b = 0; b < nb; ++b)
+            if ((S[b].phase == 1 || S[b].phase == 2) && S[b].rc == 0) act.push_back(b);
+        if (act.empty()) break;
+        // CTAs in proportion to the superblock sizes, at least one each
+        const int na = (int)act.size();
+        double ntot = 0.0;
+        for (int b : act) ntot += (double)S[b].n;
+        std::vector<int> ncta(na, 1);
+        int left = G - na;
+        for (int q = 0; q < na && left > 0; ++q) {
+            const int extra = std::min(left, (int)((double)(G - na) * S[act[q]].n / ntot));
+            ncta[q] += extra;
+            left -= extra;
+        }
+        int cta = 0, ng = 0;
+        std::vector<std::pair<int, int2>> order;
+        for (int q = 0; q < na; ++q) {
+            BatchState &B = S[act[q]];
+            Ctx &c = *B.c;
+            DevLanczos &z = c.lz;
+            BatchSolve bs{};
+            ChunkArgs &ca = bs.c;
+            OrthArgs &oa = ca.o;
+            oa.V = z.V32;
+            oa.w = z.w32;
+            oa.n = B.n;
+            oa.j = B.j0;
+            oa.mmax = B.mmax;
+            oa.pstride = z.cap + 8;
+            oa.alpha = z.alpha;
+            oa.beta = z.beta;
+            oa.part = z.part;
+            oa.bar = nullptr;
+            oa.flags = z.flags;
+            oa.h_alpha = z.d_h_ab;
+            oa.h_beta = z.d_h_ab + (z.cap + 1);
+            oa.h_flags = z.d_h_flags;
+            oa.h_m = z.d_h_ab + 2 * (z.cap + 1);
+            const bool anc = B.phase == 2;
+            oa.anc_u = anc ? (const void *)B.as.u32 : nullptr;
+            oa.anc_r = anc ? (const void *)B.as.r32 : nullptr;
+            oa.defl = anc ? (const void *)B.as.defl32 : nullptr;
+            oa.ndefl = 0;
+            ca.buf[0] = z.wbuf32;
+            ca.buf[1] = z.wbuf32 + B.n;
+            ca.slot[0] = z.slot32;
+            ca.slot[1] = z.slot32 + B.n;
+            ca.slot[2] = z.slot32 + 2 * B.n;
+            ca.j0 = B.j0;
+            ca.jend = std::min(B.mmax, B.j0 + CHECK);
+            ca.first_from_v = B.from_v ? 1 : 0;
+            ca.items = c.sb.d_items32;
+            ca.nitems = c.sb.nitems32;
+            ca.op = hv32_ops(c.sb);
+            bs.pitem = z.pitem;
+            bs.cta0 = cta;
+            bs.ncta = ncta[q];
+            bs.active = 1;
+            cta += ncta[q];
+            h_solves[q] = bs;
+            for (int li = 0; li < c.sb.nitems32; ++li) order.push_back({c.sb.item_cost[li], make_int2(q, li)});
+            B.from_v = false;
+        }
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::pair<int, int2> &x, const std::pair<int, int2> &y) { return x.first > y.first; });
+        for (auto &o : order) h_gitems[ng++] = o.second;
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(d_solves, h_solves, sizeof(BatchSolve) * na, cudaMemcpyHostToDevice, st));
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(d_gitems, h_gitems, sizeof(int2) * std::max(ng, 1), cudaMemcpyHostToDevice, st));
+        BatchArgs ba;
+        ba.s = d_solves;
+        ba.ns = na;
+        ba.nitems = ng;
+        ba.gitems = d_gitems;
+        ba.st = d_st;
+        ba.bar = c0.lz.counter + 2;
+        ba.err = c0.lz.flags + F_ERR;
+        ba.steps = CHECK;
+        void *args[] = {&ba};
+        cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_batch32, dim3(G), dim3(ORTH_THREADS), args,
+                                                    smem_max, st);
+        ++c0.launches;
+        if (e != cudaSuccess) {
+            c0.err = std::string("nss_eigh_batch: cooperative launch failed: ") + cudaGetErrorString(e);
+            return fail(NSS_ERR_CUDA);
+        }
+        cudaError_t ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) { c0.err = cudaGetErrorString(ce); return fail(NSS_ERR_CUDA); }
+        int err_flag = 0;
+        NSS_CUDA_TRY(c0, cudaMemcpy(&err_flag, c0.lz.flags + F_ERR, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err_flag) {
+            c0.err = "nss_eigh_batch: a grid barrier timed out (results discarded)";
+            return fail(NSS_ERR_CUDA);
+        }
+        // host checks and phase changes
+        for (int q = 0; q < na; ++q) {
+            BatchState &B = S[act[q]];
+            Ctx &c = *B.c;
+            DevLanczos &z = c.lz;
+            volatile int *hf = z.h_flags;
+            const double *ha = z.h_ab, *hb = z.h_ab + (z.cap + 1), *hm = z.h_ab + 2 * (z.cap + 1);
+            const int jend = std::min(B.mmax, B.j0 + CHECK);
+            int m = jend;
+            const bool brk = hf[F_STOP] == 2 && hf[F_BREAK] <= jend;
+            if (brk) m = hf[F_BREAK];
+            bool conv = false;
+            if (B.phase == 1) {
+                B.svec.resize((size_t)m);
+                tridiag_lowest(ha, hb, m, 1, hb[m - 1], B.theta.data(), B.svec.data(), B.resid.data(),
+                               B.have_upper ? B.upper.data() : nullptr, B.work);
+                B.upper[0] = B.theta[0];
+                B.have_upper = true;
+                conv = B.resid[0] <= B.tol * std::max(std::fabs(B.theta[0]), 1e-300) || (int64_t)m >= B.n;
+            } else {
+                B.cvec.resize((size_t)m + 1);
+                double lam = 0.0, res = 0.0;
+                if (arrow_lowest(B.theta0, hm, ha, hb, m, hb[m - 1], &lam, B.cvec.data(), &res, B.work))
+                    conv = res <= tol * std::max(std::fabs(lam), 1e-300) || brk;
+                else
+                    B.cvec.clear();
+            }
+            B.m_done = m;
+            if (!conv) {
+                if (brk && B.phase == 1) {
+                    // invariant subspace without convergence: restart from a random
+                    // vector orthogonal to the basis (as lanczos_eigh)
+                    ++B.restarts;
+                    float *vn = z.V32 + (int64_t)m * B.n;
+                    const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(float);
+                    const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
+                    double *h1 = z.scal + S_NSCAL;
+                    double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
+                    c0.launches += 6;
+                    k_random<float><<<608, 256, 0, st>>>(vn, B.n, B.seed, B.restarts);
+                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+                    for (int pass = 0; pass < 2; ++pass) {
+                        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
+                        k_dots<float><<<NBLK, 256, dots_smem, st>>>(z.V32, m, vn, B.n, z.part, h1, z.scal, z.counter,
+                                                                    z.flags, 0, 0, z.beta);
+                        k_update<float><<<NBLK, 256, upd_smem, st>>>(z.V32, m, vn, B.n, h1, z.part, z.scal,
+                                                                     z.counter, z.flags, rs_alpha, rs_beta, 0);
+                    }
+                    k_normalize<float><<<1, 1024, 0, st>>>(vn, B.n);
+                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta + (m - 1), 0, sizeof(double), st));
+                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+                    NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
+                    z.h_ab[(z.cap + 1) + m - 1] = 0.0;
+                    hf[F_STOP] = 0;
+                    hf[F_BREAK] = 0;
+                    B.j0 = m;
+                    B.from_v = true;
+                } else if (m >= B.mmax) {
+                    c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(B.mmax) + " iterations";
+                    B.rc = NSS_ERR_NOCONV;
+                } else {
+                    B.j0 = jend;
+                }
+                continue;
+            }
+            B.numop += m;
+            if (B.phase == 1) {
+                // FP32 phase done: Ritz vector, then the anchored refinement
+                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.svec.data(), (size_t)m * sizeof(double),
+                                                 cudaMemcpyHostToDevice, st));
+                c0.launches += 2;
+                k_ritz<float><<<NBLK, 256, (size_t)m * sizeof(double), st>>>(z.V32, m, B.n, z.svec, m, 1, z.evecs);
+                k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+                const cudaStream_t keep = c.stream;
+                c.stream = st;
+                int r2 = hv_device(c, z.evecs, z.w);
+                c.stream = keep;
+                if (r2) { c0.err = c.err; return fail(r2); }
+                ++B.numop;
+                c0.launches += 2;
+                k_rq<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+                k_anchor_r<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+                double hr[8];
+                NSS_CUDA_TRY(c0, cudaMemcpyAsync(hr, r, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
+                B.theta0 = hr[0] / hr[2];
+                const double beta0 = std::sqrt(std::max(hr[4], 0.0));
+                if (!(beta0 > tol * std::fabs(B.theta0))) {
+                    B.phase = 3;
+                } else {
+                    float *u32 = z.anc32, *r32 = z.anc32 + B.n;
+                    c0.launches += 3;
+                    k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, B.n);
+                    k_to32<<<608, 256, 0, st>>>(u32, z.evecs, 1.0, B.n);
+                    k_to32<<<608, 256, 0, st>>>(r32, z.w, 1.0, B.n);
+                    B.as = AnchorSpec{z.evecs, u32, r32, z.anc32 + 2 * B.n, 0, B.theta0, z.evecs};
+                    if ((rc = start_run(B))) return fail(rc);
+                    B.phase = 2;
+                }
+            } else {
+                // anchored phase done: the combined vector
+                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.cvec.data(), B.cvec.size() * sizeof(double),
+                                                 cudaMemcpyHostToDevice, st));
+                c0.launches += 2;
+                k_ritz_anchor<float><<<NBLK, 256, B.cvec.size() * sizeof(double), st>>>(z.V32, m, B.n, z.svec, z.evecs,
+                                                                                        z.evecs);
+                k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+                B.phase = 3;
+            }
+            if (B.phase == 3) {
+                // FP64 energy of the vector
+                const cudaStream_t keep = c.stream;
+                c.stream = st;
+                int r2 = hv_device(c, z.evecs, z.w);
+                c.stream = keep;
+                if (r2) { c0.err = c.err; return fail(r2); }
+                ++B.numop;
+                c0.launches += 2;
+                k_rq<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+                k_resid<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+                double hr[4];
+                NSS_CUDA_TRY(c0, cudaMemcpyAsync(hr, r, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
+                B.result = hr[0] / hr[2];
+                z.last_resid[0] = std::sqrt(std::max(hr[3], 0.0));
+                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.theta, &B.result, sizeof(double), cudaMemcpyHostToDevice, st));
+                z.last_iters = B.m_done;
+                z.neigen_done = 1;
+                c.last_numop = B.numop;
+                B.phase = 4;
+            }
+        }
+    }
+    cleanup();
+    int first_rc = NSS_OK;
+    for (int b = 0; b < nb; ++b) {
+        if (evals_host) evals_host[b] = S[b].result;
+        if (numops) numops[b] = S[b].numop;
+        if (S[b].rc && !first_rc) {
+            first_rc = S[b].rc;
+            c0.err = S[b].c->err;
+        } else if (S[b].phase != 4 && !S[b].rc && !first_rc) {
+            first_rc = NSS_ERR_NOCONV;
+            c0.err = "nss_eigh_batch: a solve did not finish";
+        }
+    }
+    return first_rc;
 }
 
 }  // namespace nss

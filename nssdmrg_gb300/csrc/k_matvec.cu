@@ -328,6 +328,12 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
         recs[ii].d = make_int4(lo(hlo), hi(hlo), lo(hro), hi(hro));
     }
     s.nitems32 = (int)items32.size();
+    s.item_cost.resize(items32.size());
+    for (size_t ii = 0; ii < items32.size(); ++ii) {
+        const int4 t = items32[ii];
+        const int dl = s.dls[t.x], dr = s.drs[t.x];
+        s.item_cost[ii] = t.w == HV_LEFT ? dl : (t.w == HV_RIGHT ? dr : (t.w == HV_TERMS ? 48 : dl + dr + 48));
+    }
     s.ntiles32 = (int)tiles32.size();
     s.ntiles_tc = (int)tiles_tc.size();
     std::vector<int> tc_err(1, 0);
