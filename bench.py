@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -273,6 +274,81 @@ def measure_batch(nss, device):
             "dE_rel_batched_vs_fp64_max": de}
 
 
+SERVE_CASE = {"workload": "serving_mix", "rates": [20.0, 100.0, 400.0], "requests_per_rate": 150, "slots": 32,
+              "seed": 7, "templates": 8, "lanc_tolerance": 1e-12, "lanc_niter": 256}
+
+
+def measure_serving(nss, device):
+    """Continuous batching under a Poisson request stream (the fifth
+    benchmark configuration, scaled as noted): each request is one
+    ground-state solve of a superblock drawn from a pool of templates, half
+    spin-1/2 Heisenberg (J ~ U[0.5, 1.5]) and half Hubbard (U ~ U[0, 8]),
+    L and m drawn per template; requests arrive at rate lambda, are
+    admitted into free context slots (superblock upload included in the
+    latency) and join the batch engine between rounds.  p50/p99 of
+    arrival-to-result latency and the completion rate per lambda; every
+    result is checked against the template's own FP64 solve."""
+    rng = np.random.default_rng(SERVE_CASE["seed"])
+    tol, nit = SERVE_CASE["lanc_tolerance"], SERVE_CASE["lanc_niter"]
+    templates, drivers = [], []
+    for k in range(SERVE_CASE["templates"]):
+        if k % 2 == 0:
+            jv = float(rng.uniform(0.5, 1.5))
+            L, m = int(rng.choice([16, 24, 32])), int(rng.choice([64, 128]))
+            d = nss.DMRG(nss.MODEL_HEISENBERG_HALF, L // 2, m, jz=jv, jxy=jv, dmrg_qn=(0.0,), lanc_neigen=1,
+                         device=device)
+            meta = {"model": "heisenberg_half", "J": round(jv, 4), "L": L, "m": m}
+        else:
+            u = float(rng.uniform(0.0, 8.0))
+            L, m = int(rng.choice([16, 24])), int(rng.choice([64, 128]))
+            d = nss.DMRG(nss.MODEL_HUBBARD, L // 2, m, u=u, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1,
+                         device=device)
+            meta = {"model": "hubbard", "U": round(u, 4), "L": L, "m": m}
+        d.prepare_last()
+        ev, _, _ = d.sb.sb_diag(neigen=1, nitermax=nit, tol=tol, want_vectors=False)
+        meta["N"] = int(d.sb.n)
+        drivers.append(d)
+        templates.append((d.export_superblock(), float(ev[0]), meta))
+    slots = [nss.Superblock(device) for _ in range(SERVE_CASE["slots"])]
+    eng = nss.BatchEngine(slots[0])
+    out = {"config": SERVE_CASE, "templates": [t[2] for t in templates], "rates": []}
+    for lam in SERVE_CASE["rates"]:
+        nreq = SERVE_CASE["requests_per_rate"]
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, nreq))
+        kinds = rng.integers(0, len(templates), nreq)
+        free = list(range(len(slots)))
+        inflight = {}          # engine id -> (request, slot)
+        lat, dev, occ = [], 0.0, []
+        nxt = 0
+        t0 = time.perf_counter()
+        while len(lat) < nreq:
+            now = time.perf_counter() - t0
+            while nxt < nreq and arrivals[nxt] <= now and free:
+                sl = free.pop()
+                desc, _, _ = templates[kinds[nxt]]
+                slots[sl].upload_desc(desc)
+                eid = eng.add(slots[sl], seed=1000 + nxt, nitermax=nit, tol=tol)
+                inflight[eid] = (nxt, sl)
+                nxt += 1
+            if eng.inflight:
+                occ.append(eng.inflight)
+                for eid, e, _ in eng.step():
+                    req, sl = inflight.pop(abs(eid))
+                    lat.append(time.perf_counter() - t0 - arrivals[req])
+                    ref = templates[kinds[req]][1]
+                    dev = max(dev, abs(e - ref) / abs(ref)) if eid > 0 else float("inf")
+                    free.append(sl)
+            elif nxt < nreq:
+                time.sleep(max(0.0, min(0.002, arrivals[nxt] - (time.perf_counter() - t0))))
+        span = time.perf_counter() - t0
+        lat = np.array(lat) * 1e3
+        out["rates"].append({"lambda_req_per_s": lam, "requests": nreq, "completed_per_s": nreq / span,
+                             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                             "mean_inflight": float(np.mean(occ)) if occ else 0.0, "dE_rel_max_vs_alone_fp64": dev})
+    eng.close()
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -408,6 +484,7 @@ def run_gpu(args):
 
     sweeps = measure_sweeps(nss, local) if not args.no_sweeps else None
     batch = measure_batch(nss, local) if not args.no_batch else None
+    serving = measure_serving(nss, local) if not args.no_serving else None
 
     out = None
     if rank == 0:
@@ -454,6 +531,7 @@ def run_gpu(args):
             "core_probe": CORE_PROBE,
             "sweeps": sweeps,
             "batch": batch,
+            "serving": serving,
             "setup_s": t_prep,
         }
         if not args.no_cpu_baseline and world == 1:

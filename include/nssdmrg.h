@@ -152,6 +152,22 @@ typedef struct {
 int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const uint64_t *seeds,
                    double *evals, int *numops);
 
+/* Continuous batching (serving): a batch engine runs rounds of the batched
+ * persistent kernel over the solves in flight; solves join between rounds
+ * (nss_batch_add: the context must hold an uploaded superblock) and leave
+ * when done (nss_batch_step reports up to max_done of them: ids[q] is the id
+ * nss_batch_add returned, negative when that solve failed; energies[q] its
+ * FP64 energy; the context keeps the ground state for nss_rdm).  `host`
+ * provides the device, the stream and the barrier; it may also be one of
+ * the solving contexts.  At most one batch per host context.  No
+ * counterpart in the reference. */
+typedef struct nss_batch nss_batch;
+nss_batch *nss_batch_create(nss_ctx *host);
+int nss_batch_add(nss_batch *b, nss_ctx *ctx, uint64_t seed, int nitermax, double tol, int *id);
+int nss_batch_step(nss_batch *b, int max_done, int *ndone, int *ids, double *energies, int *numops);
+int nss_batch_inflight(const nss_batch *b);
+void nss_batch_destroy(nss_batch *b);
+
 /* Reduced density matrices of the ground state (column 0 of the last
  * nss_eigh, or `psi` when not NULL, length nss_sb_dim), their block
  * eigendecomposition and the truncation choice (src/DMRG_RDM.f90:18-221,

@@ -121,6 +121,11 @@ def lib():
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
+        "nss_batch_create": (P, [P]),
+        "nss_batch_add": (C.c_int, [P, P, C.c_uint64, C.c_int, D, C.POINTER(C.c_int)]),
+        "nss_batch_step": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P, P, P]),
+        "nss_batch_inflight": (C.c_int, [P]),
+        "nss_batch_destroy": (None, [P]),
         "nss_sb_setup": (C.c_int, [P, C.c_int, C.POINTER(BlockDesc), C.POINTER(BlockDesc), P, P]),
         "nss_sb_counts": (C.c_int, [P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I64)]),
         "nss_sb_tables": (C.c_int, [P, P, P, P, P, P]),
@@ -196,6 +201,52 @@ def eigh_batch(superblocks, nitermax: int = 512, tol: float = 1e-12, seeds=None)
     if rc != 0:
         raise NssError(rc, lib().nss_last_error(superblocks[0]._ctx).decode())
     return ev, nops
+
+
+class BatchEngine:
+    """Continuous batching of ground-state solves (mixed precision): add()
+    a Superblock (its context must hold the superblock) between step()
+    calls; each step() runs one round of the batched persistent kernel and
+    returns the solves that finished: [(id, energy, numop)], id < 0 on
+    failure."""
+
+    def __init__(self, host: "Superblock"):
+        self.host = host
+        self._b = lib().nss_batch_create(host._ctx)
+        if not self._b:
+            raise NssError(NSS_ERR_INVALID, lib().nss_last_error(host._ctx).decode())
+
+    def add(self, sb: "Superblock", seed: int = 1234, nitermax: int = 512, tol: float = 1e-12) -> int:
+        i = C.c_int(0)
+        rc = lib().nss_batch_add(self._b, sb._ctx, int(seed), int(nitermax), float(tol), C.byref(i))
+        if rc != 0:
+            raise NssError(rc, lib().nss_last_error(self.host._ctx).decode())
+        return i.value
+
+    def step(self, max_done: int = 256):
+        nd = C.c_int(0)
+        ids = np.zeros(max_done, dtype=np.int32)
+        en = np.zeros(max_done)
+        nops = np.zeros(max_done, dtype=np.int32)
+        rc = lib().nss_batch_step(self._b, max_done, C.byref(nd), _ptr(ids), _ptr(en), _ptr(nops))
+        if rc != 0:
+            raise NssError(rc, lib().nss_last_error(self.host._ctx).decode())
+        return [(int(ids[q]), float(en[q]), int(nops[q])) for q in range(nd.value)]
+
+    @property
+    def inflight(self) -> int:
+        return lib().nss_batch_inflight(self._b)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().nss_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _Keep:

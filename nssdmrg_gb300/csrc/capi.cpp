@@ -267,6 +267,61 @@ int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const
     });
 }
 
+struct nss_batch {
+    nss_ctx *host = nullptr;
+    nss::BatchEngine *eng = nullptr;
+};
+
+nss_batch *nss_batch_create(nss_ctx *host) {
+    if (!host) {
+        g_err = "nss_batch_create: NULL host context";
+        return nullptr;
+    }
+    try {
+        cudaSetDevice(host->c.device);
+        nss::BatchEngine *e = nss::batch_create(host->c);
+        if (!e) return nullptr;
+        nss_batch *b = new nss_batch();
+        b->host = host;
+        b->eng = e;
+        return b;
+    } catch (const std::exception &ex) {
+        host->c.err = std::string("nss_batch_create: ") + ex.what();
+        return nullptr;
+    }
+}
+
+int nss_batch_add(nss_batch *b, nss_ctx *ctx, uint64_t seed, int nitermax, double tol, int *id) {
+    if (!b || !ctx) {
+        g_err = "nss_batch_add: NULL argument";
+        return NSS_ERR_INVALID;
+    }
+    return guarded(b->host, [&] {
+        cudaSetDevice(b->host->c.device);
+        return nss::batch_add(b->eng, ctx->c, seed, nitermax, tol, id);
+    });
+}
+
+int nss_batch_step(nss_batch *b, int max_done, int *ndone, int *ids, double *energies, int *numops) {
+    if (!b) {
+        g_err = "nss_batch_step: NULL batch";
+        return NSS_ERR_INVALID;
+    }
+    return guarded(b->host, [&] {
+        cudaSetDevice(b->host->c.device);
+        return nss::batch_step(b->eng, max_done, ndone, ids, energies, numops);
+    });
+}
+
+int nss_batch_inflight(const nss_batch *b) { return b ? nss::batch_inflight(b->eng) : 0; }
+
+void nss_batch_destroy(nss_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->host->c.device);
+    nss::batch_destroy(b->eng);
+    delete b;
+}
+
 int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rdm_side out[2],
             double *lambda_left, double *lambda_right, int32_t *kept_left, int32_t *kept_right, double *u_left,
             double *u_right) {

@@ -184,6 +184,14 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed,
 // together by the batched persistent kernel; cs[0]'s stream runs them
 int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const uint64_t *seeds,
                        double *evals_host, int *numops);
+// continuous batching: solves join with batch_add and leave through
+// batch_step (one round per call) when done
+struct BatchEngine;
+BatchEngine *batch_create(Ctx &c0);
+void batch_destroy(BatchEngine *e);
+int batch_add(BatchEngine *e, Ctx &c, uint64_t seed, int nitermax, double tol, int *id);
+int batch_step(BatchEngine *e, int max_done, int *ndone, int *ids, double *energies, int *numops);
+int batch_inflight(const BatchEngine *e);
 void lanczos_release(Ctx &c);
 
 // k_rdm.cu

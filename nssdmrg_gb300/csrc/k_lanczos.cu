@@ -1775,20 +1775,25 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
 
 
 // ---------------------------------------------------------------------------
-// Batched ground-state solves (mixed precision): every context keeps its own
-// superblock, Krylov basis and host mirrors; one cooperative launch of
-// k_batch32 per round runs CHECK iterations of every solve still going, then
+// Batch engine (mixed precision): every solve keeps its own context
+// (superblock, Krylov basis, host mirrors); one cooperative launch of
+// k_batch32 per round runs CHECK iterations of every solve in flight, then
 // the host checks each solve (tridiagonal or anchored problem) and moves it
-// through FP32 Lanczos -> anchored refinement -> FP64 energy, exactly as
-// lanczos_eigh does for one context.
+// through FP32 Lanczos -> anchored refinement -> FP64 energy, as
+// lanczos_eigh does for one context.  Solves can join between rounds
+// (continuous batching: nss_batch_add) and leave when done (nss_batch_step
+// reports them).  The per-round follow-up work of all solves (Ritz vectors,
+// FP64 products, restarts) is queued back to back with one synchronisation.
+
 namespace {
 
 struct BatchState {
     Ctx *c = nullptr;
+    int id = 0;
     int64_t n = 0;
     int mmax = 0, phase = 1, j0 = 0, m_done = 0, numop = 0, rc = 0;
     bool from_v = true, have_upper = false;
-    double tol = 0.0, theta0 = 0.0, result = 0.0;
+    double tol = 0.0, tol_final = 0.0, theta0 = 0.0, result = 0.0;
     uint64_t seed = 0, restarts = 0;
     std::vector<double> theta, resid, upper, svec, work, cvec;
     AnchorSpec as{};
@@ -1796,119 +1801,151 @@ struct BatchState {
 
 }  // namespace
 
-int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const uint64_t *seeds,
-                       double *evals_host, int *numops) {
-    if (nb < 1 || nb > BATCH_MAX) {
-        cs[0]->err = "nss_eigh_batch: between 1 and " + std::to_string(BATCH_MAX) + " solves per batch";
+struct BatchEngine {
+    Ctx *c0 = nullptr;           // owns the stream, the barrier and the argument buffers
+    std::vector<BatchState> solves;
+    int next_id = 1;
+    BatchSolve *d_solves = nullptr, *h_solves = nullptr;
+    int2 *d_gitems = nullptr, *h_gitems = nullptr;
+    int cap_items = 0;
+    float *d_st = nullptr;
+    double *h_res = nullptr;     // [BATCH_MAX][8] pinned refinement results
+    size_t smem_set = 0;
+    ~BatchEngine() {
+        if (!c0) return;
+        cudaStreamSynchronize(c0->stream);
+        ctx_free(*c0, d_solves);
+        ctx_free(*c0, d_gitems);
+        ctx_free(*c0, d_st);
+        if (h_solves) cudaFreeHost(h_solves);
+        if (h_gitems) cudaFreeHost(h_gitems);
+        if (h_res) cudaFreeHost(h_res);
+    }
+};
+
+namespace {
+
+int engine_init(BatchEngine &E, Ctx &c0) {
+    E.c0 = &c0;
+    // the barrier, error word and refinement scratch live in c0's Lanczos state
+    if (!c0.lz.flags) {
+        int rc = ensure_lanczos(c0, std::max<int64_t>(c0.sb.valid ? c0.sb.n : 1, 1), 8, true);
+        if (rc) return rc;
+    }
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_solves, (size_t)BATCH_MAX));
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_st, (size_t)4 * BATCH_MAX));
+    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&E.h_solves, sizeof(BatchSolve) * BATCH_MAX));
+    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&E.h_res, sizeof(double) * 8 * BATCH_MAX));
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(c0.lz.counter, 0, 4 * sizeof(unsigned), c0.stream));
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(c0.lz.flags, 0, F_NFLAGS * sizeof(int), c0.stream));
+    return NSS_OK;
+}
+
+int engine_start_run(BatchEngine &E, BatchState &B) {
+    Ctx &c0 = *E.c0;
+    DevLanczos &z = B.c->lz;
+    volatile int *hf = z.h_flags;
+    for (int i = 0; i < F_NFLAGS + 8; ++i) hf[i] = 0;
+    for (int i = 0; i < 3 * (z.cap + 1); ++i) z.h_ab[i] = 0.0;
+    cudaStream_t st = c0.stream;
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta, 0, (z.cap + 1) * sizeof(double), st));
+    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.slot32 + B.n, 0, (size_t)2 * B.n * sizeof(float), st));
+    B.j0 = 0;
+    B.from_v = true;
+    B.have_upper = false;
+    return NSS_OK;
+}
+
+int engine_add(BatchEngine &E, Ctx &c, uint64_t seed, int nitermax, double tol, int *id) {
+    Ctx &c0 = *E.c0;
+    if ((int)E.solves.size() >= std::min(BATCH_MAX, c0.lz.orth_grid)) {
+        c0.err = "nss_batch_add: the batch is full";
         return NSS_ERR_INVALID;
     }
-    Ctx &c0 = *cs[0];
-    cudaStream_t st = c0.stream;
+    if (c.device != c0.device) { c0.err = "nss_batch_add: the context is on another device"; return NSS_ERR_INVALID; }
+    if (!c.sb.valid) { c0.err = "nss_batch_add: the context has no superblock"; return NSS_ERR_STATE; }
+    if (c.sb.ntiles_tc != 0) {
+        c0.err = "nss_batch_add: superblocks with tensor-core sectors are solved one by one (nss_eigh)";
+        return NSS_ERR_INVALID;
+    }
+    for (auto &S : E.solves)
+        if (S.c == &c) { c0.err = "nss_batch_add: the context is already in the batch"; return NSS_ERR_INVALID; }
     if (tol <= 0.0) tol = 1e-15;
     if (nitermax <= 0) nitermax = 512;
-    std::vector<BatchState> S(nb);
-    int rc = NSS_OK;
-    for (int b = 0; b < nb; ++b) {
-        Ctx &c = *cs[b];
-        if (c.device != c0.device) { c0.err = "nss_eigh_batch: all contexts must use one device"; return NSS_ERR_INVALID; }
-        if (!c.sb.valid) { c0.err = "nss_eigh_batch: a context has no superblock"; return NSS_ERR_STATE; }
-        if (c.sb.ntiles_tc != 0) {
-            c0.err = "nss_eigh_batch: superblocks with tensor-core sectors are solved one by one (nss_eigh)";
-            return NSS_ERR_INVALID;
-        }
-        BatchState &B = S[b];
-        B.c = &c;
-        B.n = c.sb.n;
-        B.mmax = (int)std::min<int64_t>(B.n, nitermax);
-        B.tol = std::max(tol, mixed_tol());
-        B.seed = seeds ? seeds[b] : 1234;
-        B.theta.assign(4, 0.0);
-        B.resid.assign(4, 0.0);
-        B.upper.assign(4, 0.0);
-        if ((rc = ensure_lanczos(c, B.n, B.mmax + 1, true))) { c0.err = c.err; return rc; }
-        DevLanczos &z = c.lz;
-        if (!z.chunk_ok) { c0.err = "nss_eigh_batch: the persistent kernel does not fit this Krylov basis"; return NSS_ERR_INVALID; }
-        if (!z.pitem || z.cap_pitem < c.sb.nitems32) {
-            ctx_free(c, z.pitem);
-            z.pitem = nullptr;
-            NSS_CUDA_TRY(c, ctx_alloc(c, &z.pitem, (size_t)std::max(c.sb.nitems32, 1)));
-            z.cap_pitem = c.sb.nitems32;
-        }
+    BatchState B;
+    B.c = &c;
+    B.id = E.next_id++;
+    B.n = c.sb.n;
+    B.mmax = (int)std::min<int64_t>(B.n, nitermax);
+    B.tol = std::max(tol, mixed_tol());
+    B.tol_final = tol;
+    B.seed = seed;
+    B.theta.assign(4, 0.0);
+    B.resid.assign(4, 0.0);
+    B.upper.assign(4, 0.0);
+    int rc = ensure_lanczos(c, B.n, B.mmax + 1, true);
+    if (rc) { c0.err = c.err; return rc; }
+    DevLanczos &z = c.lz;
+    if (!z.chunk_ok) { c0.err = "nss_batch_add: the persistent kernel does not fit this Krylov basis"; return NSS_ERR_INVALID; }
+    if (!z.pitem || z.cap_pitem < c.sb.nitems32) {
+        ctx_free(c, z.pitem);
+        z.pitem = nullptr;
+        NSS_CUDA_TRY(c0, ctx_alloc(c, &z.pitem, (size_t)std::max(c.sb.nitems32, 1)));
+        z.cap_pitem = c.sb.nitems32;
     }
+    if ((rc = engine_start_run(E, B))) return rc;
+    cudaStream_t st = c0.stream;
+    c0.launches += 2;
+    k_random<float><<<608, 256, 0, st>>>(z.V32, B.n, B.seed, 0);
+    k_normalize<float><<<1, 1024, 0, st>>>(z.V32, B.n);
+    NSS_CUDA_TRY(c0, cudaGetLastError());
+    if (id) *id = B.id;
+    E.solves.push_back(std::move(B));
+    return NSS_OK;
+}
+
+// One round: a launch over every solve in flight, the host checks, the
+// follow-up work.  Finished solves are removed and reported.
+int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *energies, int *numops) {
+    Ctx &c0 = *E.c0;
+    cudaStream_t st = c0.stream;
+    if (ndone) *ndone = 0;
     const int G = c0.lz.orth_grid;
-    if (nb > G) { c0.err = "nss_eigh_batch: more solves than CTAs of the persistent kernel"; return NSS_ERR_INVALID; }
-    // per-solve start: mirrors, flags, random start vector
-    auto start_run = [&](BatchState &B) -> int {
-        Ctx &c = *B.c;
-        DevLanczos &z = c.lz;
-        volatile int *hf = z.h_flags;
-        for (int i = 0; i < F_NFLAGS + 8; ++i) hf[i] = 0;
-        for (int i = 0; i < 3 * (z.cap + 1); ++i) z.h_ab[i] = 0.0;
-        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta, 0, (z.cap + 1) * sizeof(double), st));
-        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.slot32 + B.n, 0, (size_t)2 * B.n * sizeof(float), st));
-        B.j0 = 0;
-        B.from_v = true;
-        B.have_upper = false;
-        return NSS_OK;
-    };
-    for (auto &B : S) {
-        Ctx &c = *B.c;
-        if ((rc = start_run(B))) return rc;
-        c0.launches += 2;
-        k_random<float><<<608, 256, 0, st>>>(c.lz.V32, B.n, B.seed, 0);
-        k_normalize<float><<<1, 1024, 0, st>>>(c.lz.V32, B.n);
-    }
-    NSS_CUDA_TRY(c0, cudaMemsetAsync(c0.lz.counter, 0, 4 * sizeof(unsigned), st));
-    // device argument arrays (per call)
-    BatchSolve *d_solves = nullptr;
-    int2 *d_gitems = nullptr;
-    float *d_st = nullptr;
-    int tot_items = 0;
-    for (auto &B : S) tot_items += B.c->sb.nitems32;
-    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_solves, (size_t)nb));
-    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_gitems, (size_t)std::max(tot_items, 1)));
-    NSS_CUDA_TRY(c0, ctx_alloc(c0, &d_st, (size_t)4 * nb));
-    BatchSolve *h_solves = nullptr;
-    int2 *h_gitems = nullptr;
-    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&h_solves, sizeof(BatchSolve) * nb));
-    NSS_CUDA_TRY(c0, cudaMallocHost((void **)&h_gitems, sizeof(int2) * std::max(tot_items, 1)));
-    auto cleanup = [&]() {
-        cudaStreamSynchronize(st);
-        ctx_free(c0, d_solves);
-        ctx_free(c0, d_gitems);
-        ctx_free(c0, d_st);
-        cudaFreeHost(h_solves);
-        cudaFreeHost(h_gitems);
-    };
-    auto fail = [&](int code) { cleanup(); return code; };
-    size_t smem_max = 0;
-    for (auto &B : S) smem_max = std::max(smem_max, B.c->lz.chunk_smem);
-    NSS_CUDA_TRY(c0, cudaFuncSetAttribute((const void *)k_batch32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem_max));
-    double *r = c0.lz.scal + S_NSCAL + 4 * (c0.lz.cap + 2);   // refinement slots (context 0's scratch)
-    for (int round = 0; round < 100000; ++round) {
-        std::vector<int> act;
-        for (int b = 0; b < nb; ++b)
-            if ((S[b].phase == 1 || S[b].phase == 2) && S[b].rc == 0) act.push_back(b);
-        if (act.empty()) break;
-        // CTAs in proportion to the superblock sizes, at least one each
-        const int na = (int)act.size();
+    std::vector<int> act;
+    for (int b = 0; b < (int)E.solves.size(); ++b)
+        if ((E.solves[b].phase == 1 || E.solves[b].phase == 2) && E.solves[b].rc == 0) act.push_back(b);
+    const int na = (int)act.size();
+    if (na > 0) {
         double ntot = 0.0;
-        for (int b : act) ntot += (double)S[b].n;
+        for (int b : act) ntot += (double)E.solves[b].n;
         std::vector<int> ncta(na, 1);
         int left = G - na;
         for (int q = 0; q < na && left > 0; ++q) {
-            const int extra = std::min(left, (int)((double)(G - na) * S[act[q]].n / ntot));
+            const int extra = std::min(left, (int)((double)(G - na) * E.solves[act[q]].n / ntot));
             ncta[q] += extra;
             left -= extra;
         }
+        int tot_items = 0;
+        for (int b : act) tot_items += E.solves[b].c->sb.nitems32;
+        if (tot_items > E.cap_items) {
+            ctx_free(c0, E.d_gitems);
+            E.d_gitems = nullptr;
+            if (E.h_gitems) cudaFreeHost(E.h_gitems);
+            E.h_gitems = nullptr;
+            NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_gitems, (size_t)tot_items));
+            NSS_CUDA_TRY(c0, cudaMallocHost((void **)&E.h_gitems, sizeof(int2) * tot_items));
+            E.cap_items = tot_items;
+        }
         int cta = 0, ng = 0;
+        size_t smem_max = 0;
         std::vector<std::pair<int, int2>> order;
+        order.reserve(tot_items);
         for (int q = 0; q < na; ++q) {
-            BatchState &B = S[act[q]];
+            BatchState &B = E.solves[act[q]];
             Ctx &c = *B.c;
             DevLanczos &z = c.lz;
+            smem_max = std::max(smem_max, z.chunk_smem);
             BatchSolve bs{};
             ChunkArgs &ca = bs.c;
             OrthArgs &oa = ca.o;
@@ -1948,184 +1985,268 @@ int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const u
             bs.ncta = ncta[q];
             bs.active = 1;
             cta += ncta[q];
-            h_solves[q] = bs;
+            E.h_solves[q] = bs;
             for (int li = 0; li < c.sb.nitems32; ++li) order.push_back({c.sb.item_cost[li], make_int2(q, li)});
             B.from_v = false;
         }
         std::stable_sort(order.begin(), order.end(),
                          [](const std::pair<int, int2> &x, const std::pair<int, int2> &y) { return x.first > y.first; });
-        for (auto &o : order) h_gitems[ng++] = o.second;
-        NSS_CUDA_TRY(c0, cudaMemcpyAsync(d_solves, h_solves, sizeof(BatchSolve) * na, cudaMemcpyHostToDevice, st));
-        NSS_CUDA_TRY(c0, cudaMemcpyAsync(d_gitems, h_gitems, sizeof(int2) * std::max(ng, 1), cudaMemcpyHostToDevice, st));
+        for (auto &o : order) E.h_gitems[ng++] = o.second;
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(E.d_solves, E.h_solves, sizeof(BatchSolve) * na, cudaMemcpyHostToDevice, st));
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(E.d_gitems, E.h_gitems, sizeof(int2) * std::max(ng, 1), cudaMemcpyHostToDevice,
+                                         st));
+        if (smem_max > E.smem_set) {
+            NSS_CUDA_TRY(c0, cudaFuncSetAttribute((const void *)k_batch32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)smem_max));
+            E.smem_set = smem_max;
+        }
         BatchArgs ba;
-        ba.s = d_solves;
+        ba.s = E.d_solves;
         ba.ns = na;
         ba.nitems = ng;
-        ba.gitems = d_gitems;
-        ba.st = d_st;
+        ba.gitems = E.d_gitems;
+        ba.st = E.d_st;
         ba.bar = c0.lz.counter + 2;
         ba.err = c0.lz.flags + F_ERR;
         ba.steps = CHECK;
         void *args[] = {&ba};
         cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_batch32, dim3(G), dim3(ORTH_THREADS), args,
-                                                    smem_max, st);
+                                                    E.smem_set, st);
         ++c0.launches;
         if (e != cudaSuccess) {
-            c0.err = std::string("nss_eigh_batch: cooperative launch failed: ") + cudaGetErrorString(e);
-            return fail(NSS_ERR_CUDA);
+            c0.err = std::string("nss_batch: cooperative launch failed: ") + cudaGetErrorString(e);
+            return NSS_ERR_CUDA;
         }
         cudaError_t ce = cudaStreamSynchronize(st);
-        if (ce != cudaSuccess) { c0.err = cudaGetErrorString(ce); return fail(NSS_ERR_CUDA); }
+        if (ce != cudaSuccess) { c0.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
         int err_flag = 0;
         NSS_CUDA_TRY(c0, cudaMemcpy(&err_flag, c0.lz.flags + F_ERR, sizeof(int), cudaMemcpyDeviceToHost));
         if (err_flag) {
-            c0.err = "nss_eigh_batch: a grid barrier timed out (results discarded)";
-            return fail(NSS_ERR_CUDA);
-        }
-        // host checks and phase changes
-        for (int q = 0; q < na; ++q) {
-            BatchState &B = S[act[q]];
-            Ctx &c = *B.c;
-            DevLanczos &z = c.lz;
-            volatile int *hf = z.h_flags;
-            const double *ha = z.h_ab, *hb = z.h_ab + (z.cap + 1), *hm = z.h_ab + 2 * (z.cap + 1);
-            const int jend = std::min(B.mmax, B.j0 + CHECK);
-            int m = jend;
-            const bool brk = hf[F_STOP] == 2 && hf[F_BREAK] <= jend;
-            if (brk) m = hf[F_BREAK];
-            bool conv = false;
-            if (B.phase == 1) {
-                B.svec.resize((size_t)m);
-                tridiag_lowest(ha, hb, m, 1, hb[m - 1], B.theta.data(), B.svec.data(), B.resid.data(),
-                               B.have_upper ? B.upper.data() : nullptr, B.work);
-                B.upper[0] = B.theta[0];
-                B.have_upper = true;
-                conv = B.resid[0] <= B.tol * std::max(std::fabs(B.theta[0]), 1e-300) || (int64_t)m >= B.n;
-            } else {
-                B.cvec.resize((size_t)m + 1);
-                double lam = 0.0, res = 0.0;
-                if (arrow_lowest(B.theta0, hm, ha, hb, m, hb[m - 1], &lam, B.cvec.data(), &res, B.work))
-                    conv = res <= tol * std::max(std::fabs(lam), 1e-300) || brk;
-                else
-                    B.cvec.clear();
-            }
-            B.m_done = m;
-            if (!conv) {
-                if (brk && B.phase == 1) {
-                    // invariant subspace without convergence: restart from a random
-                    // vector orthogonal to the basis (as lanczos_eigh)
-                    ++B.restarts;
-                    float *vn = z.V32 + (int64_t)m * B.n;
-                    const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(float);
-                    const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
-                    double *h1 = z.scal + S_NSCAL;
-                    double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
-                    c0.launches += 6;
-                    k_random<float><<<608, 256, 0, st>>>(vn, B.n, B.seed, B.restarts);
-                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-                    for (int pass = 0; pass < 2; ++pass) {
-                        NSS_CUDA_TRY(c0, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
-                        k_dots<float><<<NBLK, 256, dots_smem, st>>>(z.V32, m, vn, B.n, z.part, h1, z.scal, z.counter,
-                                                                    z.flags, 0, 0, z.beta);
-                        k_update<float><<<NBLK, 256, upd_smem, st>>>(z.V32, m, vn, B.n, h1, z.part, z.scal,
-                                                                     z.counter, z.flags, rs_alpha, rs_beta, 0);
-                    }
-                    k_normalize<float><<<1, 1024, 0, st>>>(vn, B.n);
-                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta + (m - 1), 0, sizeof(double), st));
-                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
-                    NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
-                    z.h_ab[(z.cap + 1) + m - 1] = 0.0;
-                    hf[F_STOP] = 0;
-                    hf[F_BREAK] = 0;
-                    B.j0 = m;
-                    B.from_v = true;
-                } else if (m >= B.mmax) {
-                    c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(B.mmax) + " iterations";
-                    B.rc = NSS_ERR_NOCONV;
-                } else {
-                    B.j0 = jend;
-                }
-                continue;
-            }
-            B.numop += m;
-            if (B.phase == 1) {
-                // FP32 phase done: Ritz vector, then the anchored refinement
-                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.svec.data(), (size_t)m * sizeof(double),
-                                                 cudaMemcpyHostToDevice, st));
-                c0.launches += 2;
-                k_ritz<float><<<NBLK, 256, (size_t)m * sizeof(double), st>>>(z.V32, m, B.n, z.svec, m, 1, z.evecs);
-                k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
-                const cudaStream_t keep = c.stream;
-                c.stream = st;
-                int r2 = hv_device(c, z.evecs, z.w);
-                c.stream = keep;
-                if (r2) { c0.err = c.err; return fail(r2); }
-                ++B.numop;
-                c0.launches += 2;
-                k_rq<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
-                k_anchor_r<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
-                double hr[8];
-                NSS_CUDA_TRY(c0, cudaMemcpyAsync(hr, r, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
-                NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
-                B.theta0 = hr[0] / hr[2];
-                const double beta0 = std::sqrt(std::max(hr[4], 0.0));
-                if (!(beta0 > tol * std::fabs(B.theta0))) {
-                    B.phase = 3;
-                } else {
-                    float *u32 = z.anc32, *r32 = z.anc32 + B.n;
-                    c0.launches += 3;
-                    k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, B.n);
-                    k_to32<<<608, 256, 0, st>>>(u32, z.evecs, 1.0, B.n);
-                    k_to32<<<608, 256, 0, st>>>(r32, z.w, 1.0, B.n);
-                    B.as = AnchorSpec{z.evecs, u32, r32, z.anc32 + 2 * B.n, 0, B.theta0, z.evecs};
-                    if ((rc = start_run(B))) return fail(rc);
-                    B.phase = 2;
-                }
-            } else {
-                // anchored phase done: the combined vector
-                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.cvec.data(), B.cvec.size() * sizeof(double),
-                                                 cudaMemcpyHostToDevice, st));
-                c0.launches += 2;
-                k_ritz_anchor<float><<<NBLK, 256, B.cvec.size() * sizeof(double), st>>>(z.V32, m, B.n, z.svec, z.evecs,
-                                                                                        z.evecs);
-                k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
-                B.phase = 3;
-            }
-            if (B.phase == 3) {
-                // FP64 energy of the vector
-                const cudaStream_t keep = c.stream;
-                c.stream = st;
-                int r2 = hv_device(c, z.evecs, z.w);
-                c.stream = keep;
-                if (r2) { c0.err = c.err; return fail(r2); }
-                ++B.numop;
-                c0.launches += 2;
-                k_rq<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
-                k_resid<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
-                double hr[4];
-                NSS_CUDA_TRY(c0, cudaMemcpyAsync(hr, r, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
-                NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
-                B.result = hr[0] / hr[2];
-                z.last_resid[0] = std::sqrt(std::max(hr[3], 0.0));
-                NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.theta, &B.result, sizeof(double), cudaMemcpyHostToDevice, st));
-                z.last_iters = B.m_done;
-                z.neigen_done = 1;
-                c.last_numop = B.numop;
-                B.phase = 4;
-            }
+            c0.err = "nss_batch: a grid barrier timed out (results discarded)";
+            return NSS_ERR_CUDA;
         }
     }
-    cleanup();
+    // host checks
+    std::vector<int> p1, p2, p3;
+    for (int b : act) {
+        BatchState &B = E.solves[b];
+        Ctx &c = *B.c;
+        DevLanczos &z = c.lz;
+        volatile int *hf = z.h_flags;
+        const double *ha = z.h_ab, *hb = z.h_ab + (z.cap + 1), *hm = z.h_ab + 2 * (z.cap + 1);
+        const int jend = std::min(B.mmax, B.j0 + CHECK);
+        int m = jend;
+        const bool brk = hf[F_STOP] == 2 && hf[F_BREAK] <= jend;
+        if (brk) m = hf[F_BREAK];
+        bool conv = false;
+        if (B.phase == 1) {
+            B.svec.resize((size_t)m);
+            tridiag_lowest(ha, hb, m, 1, hb[m - 1], B.theta.data(), B.svec.data(), B.resid.data(),
+                           B.have_upper ? B.upper.data() : nullptr, B.work);
+            B.upper[0] = B.theta[0];
+            B.have_upper = true;
+            conv = B.resid[0] <= B.tol * std::max(std::fabs(B.theta[0]), 1e-300) || (int64_t)m >= B.n;
+        } else {
+            B.cvec.resize((size_t)m + 1);
+            double lam = 0.0, res = 0.0;
+            if (arrow_lowest(B.theta0, hm, ha, hb, m, hb[m - 1], &lam, B.cvec.data(), &res, B.work))
+                conv = res <= B.tol_final * std::max(std::fabs(lam), 1e-300) || brk;
+            else
+                B.cvec.clear();
+        }
+        B.m_done = m;
+        if (!conv) {
+            if (brk && B.phase == 1) {
+                // invariant subspace without convergence: restart from a random
+                // vector orthogonal to the basis
+                ++B.restarts;
+                float *vn = z.V32 + (int64_t)m * B.n;
+                const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(float);
+                const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
+                if (dots_smem > 48 * 1024)
+                    cudaFuncSetAttribute(k_dots<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
+                if (upd_smem > 48 * 1024)
+                    cudaFuncSetAttribute(k_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+                double *h1 = z.scal + S_NSCAL;
+                double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
+                c0.launches += 6;
+                k_random<float><<<608, 256, 0, st>>>(vn, B.n, B.seed, B.restarts);
+                NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+                for (int pass = 0; pass < 2; ++pass) {
+                    NSS_CUDA_TRY(c0, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
+                    k_dots<float><<<NBLK, 256, dots_smem, st>>>(z.V32, m, vn, B.n, z.part, h1, z.scal, z.counter,
+                                                                z.flags, 0, 0, z.beta);
+                    k_update<float><<<NBLK, 256, upd_smem, st>>>(z.V32, m, vn, B.n, h1, z.part, z.scal, z.counter,
+                                                                 z.flags, rs_alpha, rs_beta, 0);
+                }
+                k_normalize<float><<<1, 1024, 0, st>>>(vn, B.n);
+                NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta + (m - 1), 0, sizeof(double), st));
+                NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
+                z.h_ab[(z.cap + 1) + m - 1] = 0.0;
+                hf[F_STOP] = 0;
+                hf[F_BREAK] = 0;
+                B.j0 = m;
+                B.from_v = true;
+            } else if (m >= B.mmax) {
+                c.err = "nss_eigh: no convergence within nitermax=" + std::to_string(B.mmax) + " iterations";
+                B.rc = NSS_ERR_NOCONV;
+            } else {
+                B.j0 = jend;
+            }
+            continue;
+        }
+        B.numop += m;
+        (B.phase == 1 ? p1 : p2).push_back(b);
+    }
+    for (int b = 0; b < (int)E.solves.size(); ++b)
+        if (E.solves[b].phase == 3) p3.push_back(b);
+    // follow-up work, queued back to back: refinement results land in h_res
+    double *r = c0.lz.scal + S_NSCAL + 4 * (c0.lz.cap + 2);
+    auto fp64_energy = [&](BatchState &B, int slot, bool anchor) -> int {
+        Ctx &c = *B.c;
+        DevLanczos &z = c.lz;
+        const cudaStream_t keep = c.stream;
+        c.stream = st;
+        int r2 = hv_device(c, z.evecs, z.w);
+        c.stream = keep;
+        if (r2) { c0.err = c.err; return r2; }
+        ++B.numop;
+        c0.launches += 2;
+        k_rq<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+        if (anchor) k_anchor_r<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+        else k_resid<<<NBLK, 256, 0, st>>>(z.evecs, z.w, B.n, z.part, r, c0.lz.counter);
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(E.h_res + 8 * slot, r, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        return NSS_OK;
+    };
+    int rc = NSS_OK;
+    for (int b : p1) {
+        BatchState &B = E.solves[b];
+        DevLanczos &z = B.c->lz;
+        const int m = B.m_done;
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.svec.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st));
+        c0.launches += 2;
+        k_ritz<float><<<NBLK, 256, (size_t)m * sizeof(double), st>>>(z.V32, m, B.n, z.svec, m, 1, z.evecs);
+        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+        if ((rc = fp64_energy(B, b, true))) return rc;
+    }
+    for (int b : p2) {
+        BatchState &B = E.solves[b];
+        DevLanczos &z = B.c->lz;
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.cvec.data(), B.cvec.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                         st));
+        c0.launches += 2;
+        k_ritz_anchor<float><<<NBLK, 256, B.cvec.size() * sizeof(double), st>>>(z.V32, B.m_done, B.n, z.svec, z.evecs,
+                                                                                z.evecs);
+        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+        if ((rc = fp64_energy(B, b, false))) return rc;
+    }
+    for (int b : p3)
+        if ((rc = fp64_energy(E.solves[b], b, false))) return rc;
+    NSS_CUDA_TRY(c0, cudaStreamSynchronize(st));
+    auto finish = [&](BatchState &B, int slot) -> int {
+        const double *hr = E.h_res + 8 * slot;
+        B.result = hr[0] / hr[2];
+        DevLanczos &z = B.c->lz;
+        z.last_resid[0] = std::sqrt(std::max(hr[3], 0.0));
+        NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.theta, &B.result, sizeof(double), cudaMemcpyHostToDevice, st));
+        z.last_iters = B.m_done;
+        z.neigen_done = 1;
+        B.c->last_numop = B.numop;
+        B.phase = 4;
+        return NSS_OK;
+    };
+    for (int b : p1) {
+        BatchState &B = E.solves[b];
+        DevLanczos &z = B.c->lz;
+        const double *hr = E.h_res + 8 * b;
+        B.theta0 = hr[0] / hr[2];
+        const double beta0 = std::sqrt(std::max(hr[4], 0.0));
+        if (!(beta0 > B.tol_final * std::fabs(B.theta0))) {
+            B.phase = 3;   // the FP32 vector is converged already: its FP64 energy next round
+            continue;
+        }
+        float *u32 = z.anc32, *r32 = z.anc32 + B.n;
+        c0.launches += 3;
+        k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, B.n);
+        k_to32<<<608, 256, 0, st>>>(u32, z.evecs, 1.0, B.n);
+        k_to32<<<608, 256, 0, st>>>(r32, z.w, 1.0, B.n);
+        B.as = AnchorSpec{z.evecs, u32, r32, z.anc32 + 2 * B.n, 0, B.theta0, z.evecs};
+        if ((rc = engine_start_run(E, B))) return rc;
+        B.phase = 2;
+    }
+    for (int b : p2)
+        if ((rc = finish(E.solves[b], b))) return rc;
+    for (int b : p3)
+        if ((rc = finish(E.solves[b], b))) return rc;
+    // report and remove the finished solves
+    int nd = 0;
+    std::vector<BatchState> keep;
+    for (auto &B : E.solves) {
+        if ((B.phase == 4 || B.rc) && nd < max_done) {
+            if (ids) ids[nd] = B.rc ? -B.id : B.id;
+            if (energies) energies[nd] = B.result;
+            if (numops) numops[nd] = B.numop;
+            ++nd;
+        } else {
+            keep.push_back(std::move(B));
+        }
+    }
+    E.solves = std::move(keep);
+    if (ndone) *ndone = nd;
+    return NSS_OK;
+}
+
+}  // namespace
+
+BatchEngine *batch_create(Ctx &c0) {
+    BatchEngine *E = new BatchEngine();
+    if (engine_init(*E, c0)) {
+        delete E;
+        return nullptr;
+    }
+    return E;
+}
+
+void batch_destroy(BatchEngine *E) { delete E; }
+
+int batch_add(BatchEngine *E, Ctx &c, uint64_t seed, int nitermax, double tol, int *id) {
+    return engine_add(*E, c, seed, nitermax, tol, id);
+}
+
+int batch_step(BatchEngine *E, int max_done, int *ndone, int *ids, double *energies, int *numops) {
+    return engine_step(*E, max_done, ndone, ids, energies, numops);
+}
+
+int batch_inflight(const BatchEngine *E) { return (int)E->solves.size(); }
+
+int lanczos_eigh_batch(Ctx *const *cs, int nb, int nitermax, double tol, const uint64_t *seeds,
+                       double *evals_host, int *numops) {
+    if (nb < 1 || nb > BATCH_MAX) {
+        cs[0]->err = "nss_eigh_batch: between 1 and " + std::to_string(BATCH_MAX) + " solves per batch";
+        return NSS_ERR_INVALID;
+    }
+    BatchEngine E;
+    int rc = engine_init(E, *cs[0]);
+    if (rc) return rc;
+    std::vector<int> ids(nb);
+    for (int b = 0; b < nb; ++b)
+        if ((rc = engine_add(E, *cs[b], seeds ? seeds[b] : 1234, nitermax, tol, &ids[b]))) return rc;
+    std::vector<int> did(nb), nop(nb);
+    std::vector<double> en(nb);
     int first_rc = NSS_OK;
-    for (int b = 0; b < nb; ++b) {
-        if (evals_host) evals_host[b] = S[b].result;
-        if (numops) numops[b] = S[b].numop;
-        if (S[b].rc && !first_rc) {
-            first_rc = S[b].rc;
-            c0.err = S[b].c->err;
-        } else if (S[b].phase != 4 && !S[b].rc && !first_rc) {
-            first_rc = NSS_ERR_NOCONV;
-            c0.err = "nss_eigh_batch: a solve did not finish";
+    for (int round = 0; round < 1000000 && !E.solves.empty(); ++round) {
+        int nd = 0;
+        if ((rc = engine_step(E, nb, &nd, did.data(), en.data(), nop.data()))) return rc;
+        for (int q = 0; q < nd; ++q) {
+            const int id = did[q] < 0 ? -did[q] : did[q];
+            const int b = (int)(std::find(ids.begin(), ids.end(), id) - ids.begin());
+            if (b >= nb) continue;
+            if (evals_host) evals_host[b] = en[q];
+            if (numops) numops[b] = nop[q];
+            if (did[q] < 0 && !first_rc) {
+                first_rc = NSS_ERR_NOCONV;
+                cs[0]->err = cs[b]->err;
+            }
         }
     }
     return first_rc;

@@ -84,3 +84,33 @@ def test_batch_one_and_repeat(nss, superblocks):
     ev, _, _ = sbs[0].sb_diag(neigen=1, tol=1e-12, want_vectors=False)
     np.testing.assert_allclose(e1, ev[:1], rtol=1e-10)
     np.testing.assert_allclose(e2, ev[:1], rtol=1e-10)
+
+
+def test_continuous_batching(nss, superblocks):
+    """Solves join the engine while others are in flight and leave when
+    done; every result equals the context's own solve."""
+    sbs, _ = superblocks
+    ref = []
+    for s in sbs:
+        ev, _, _ = s.sb_diag(neigen=1, tol=1e-12, want_vectors=False)
+        ref.append(ev[0])
+    eng = nss.BatchEngine(sbs[0])
+    ids = {}
+    ids[eng.add(sbs[0], seed=11)] = 0
+    ids[eng.add(sbs[3], seed=12)] = 3
+    got = {}
+    pending = [1, 2, 4, 5, 6]
+    rounds = 0
+    while eng.inflight or pending:
+        if pending and rounds % 3 == 1:
+            k = pending.pop(0)
+            ids[eng.add(sbs[k], seed=20 + k)] = k
+        for i, e, nop in eng.step():
+            assert i > 0 and nop > 0
+            got[ids[i]] = e
+        rounds += 1
+        assert rounds < 10000
+    eng.close()
+    assert sorted(got) == list(range(len(sbs)))
+    for k, e in got.items():
+        assert abs(e - ref[k]) <= 1e-10 * abs(ref[k]), (k, e, ref[k])
