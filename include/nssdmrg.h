@@ -183,6 +183,15 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
             int32_t *kept_left, int32_t *kept_right,
             double *u_left, double *u_right);
 
+/* Timing of the mixed method's persistent Lanczos kernel: with `enable`
+ * set, each launch in later nss_eigh calls is bracketed by CUDA events on
+ * the context stream; nss_chunk_stats returns, for the last nss_eigh, the
+ * summed launch time (ms), the launches and the iterations they completed,
+ * and the sum over those iterations of the basis size m (the orthogonalised
+ * columns, for the bytes each iteration reads). */
+int nss_time_chunks(nss_ctx *ctx, int enable);
+int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iters, double *cols);
+
 /* Energy <psi|H|psi> / <psi|psi> of a device vector d_psi (length n =
  * nss_sb_dim) on the uploaded superblock, written to *energy (host), without
  * allocating any memory.  No counterpart in the reference: it is for callers

@@ -121,6 +121,8 @@ def lib():
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
+        "nss_time_chunks": (C.c_int, [P, C.c_int]),
+        "nss_chunk_stats": (C.c_int, [P, C.POINTER(D), C.POINTER(C.c_int), C.POINTER(I64), C.POINTER(D)]),
         "nss_batch_create": (P, [P]),
         "nss_batch_add": (C.c_int, [P, P, C.c_uint64, C.c_int, D, C.POINTER(C.c_int)]),
         "nss_batch_step": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P, P, P]),
@@ -359,6 +361,17 @@ class Superblock:
         d.row_offset, d.col_offset = _p(ro, C.c_int64), _p(co, C.c_int64)
         self._check(lib().nss_sb_upload(self._ctx, C.byref(d)))
         self.m_left, self.m_right = m_left, m_right
+
+    def time_chunks(self, enable: bool = True):
+        """CUDA-event timing of the persistent Lanczos kernel in later solves."""
+        self._check(lib().nss_time_chunks(self._ctx, int(enable)))
+
+    def chunk_stats(self):
+        """(ms, launches, iterations, sum of m) of the persistent kernel in
+        the last solve (with time_chunks enabled)."""
+        ms, nl, it, cols = C.c_double(), C.c_int(), C.c_int64(), C.c_double()
+        self._check(lib().nss_chunk_stats(self._ctx, C.byref(ms), C.byref(nl), C.byref(it), C.byref(cols)))
+        return ms.value, nl.value, it.value, cols.value
 
     def upload_desc(self, desc: SbDesc):
         self._check(lib().nss_sb_upload(self._ctx, C.byref(desc)))

@@ -208,6 +208,21 @@ int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, con
     return NSS_OK;
 }
 
+int nss_time_chunks(nss_ctx *ctx, int enable) {
+    if (!ctx) return NSS_ERR_INVALID;
+    ctx->c.time_chunks = enable != 0;
+    return NSS_OK;
+}
+
+int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iters, double *cols) {
+    if (!ctx) return NSS_ERR_INVALID;
+    if (ms) *ms = ctx->c.chunk_ms;
+    if (launches) *launches = ctx->c.chunk_launches;
+    if (iters) *iters = ctx->c.chunk_iters;
+    if (cols) *cols = ctx->c.chunk_cols;
+    return NSS_OK;
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

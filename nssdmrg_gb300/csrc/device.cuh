@@ -143,6 +143,12 @@ struct Ctx {
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
+    // optional CUDA-event timing of the persistent chunk kernel (last solve)
+    bool time_chunks = false;
+    double chunk_ms = 0.0;       // summed launch durations
+    int chunk_launches = 0;
+    int64_t chunk_iters = 0;     // iterations those launches completed
+    double chunk_cols = 0.0;     // sum over those iterations of the basis size m
 };
 
 // Allocation through the context budget.

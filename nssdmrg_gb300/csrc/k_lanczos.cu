@@ -1451,6 +1451,11 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
     // mixed method without tensor-core sectors: one persistent launch per chunk
     const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.ntiles_tc == 0;
+    struct ChunkTiming {
+        cudaEvent_t a, b;
+        int j0, jend;
+    };
+    std::vector<ChunkTiming> ctime;
     if (use_chunk)   // slot 1 and 2 regions that no item writes must read as zero
         NSS_CUDA_TRY(c, cudaMemsetAsync(z.slot32 + n, 0, (size_t)2 * n * sizeof(float), st));
     bool from_v = true;   // the next chunk starts from V[j0] (start, restart)
@@ -1472,8 +1477,18 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             ca.op = hv32_ops(c.sb);
             from_v = false;
             void *args[] = {&ca};
+            ChunkTiming ct{nullptr, nullptr, j0, jend};
+            if (c.time_chunks) {
+                cudaEventCreate(&ct.a);
+                cudaEventCreate(&ct.b);
+                cudaEventRecord(ct.a, st);
+            }
             cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_chunk32, dim3(z.orth_grid),
                                                         dim3(ORTH_THREADS), args, z.chunk_smem, st);
+            if (c.time_chunks) {
+                cudaEventRecord(ct.b, st);
+                ctime.push_back(ct);
+            }
             ++c.launches;
             if (e != cudaSuccess) {
                 c.err = std::string("nss_eigh: cooperative launch failed: ") + cudaGetErrorString(e);
@@ -1580,6 +1595,20 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaError_t ce = cudaStreamSynchronize(st);
     cudaEventDestroy(evs[0]);
     cudaEventDestroy(evs[1]);
+    for (const ChunkTiming &ct : ctime) {
+        // launches that completed iterations of the basis the solve kept
+        if (ce == cudaSuccess && ct.j0 < m_done) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ct.a, ct.b);
+            const int je = std::min(ct.jend, m_done);
+            c.chunk_ms += ms;
+            ++c.chunk_launches;
+            c.chunk_iters += je - ct.j0;
+            for (int jj = ct.j0; jj < je; ++jj) c.chunk_cols += jj + 1;
+        }
+        cudaEventDestroy(ct.a);
+        cudaEventDestroy(ct.b);
+    }
     if (rc) return rc;
     if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
     int dflags[F_NFLAGS];
@@ -1652,6 +1681,10 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     int rc = ensure_lanczos(c, n, mmax + 1, mixed);
     if (rc) return rc;
     DevLanczos &z = c.lz;
+    c.chunk_ms = 0.0;
+    c.chunk_launches = 0;
+    c.chunk_iters = 0;
+    c.chunk_cols = 0.0;
     cudaStream_t st = c.stream;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
