@@ -208,8 +208,21 @@ def measure_sweeps(nss, device):
         t_all = time.perf_counter() - t0
         t_sw = max(t_all - t_inf, 1e-9)
         nsw = len(SWEEP_CASE["msweep"])
+        fin = [r for r in recs if r["type"] != 0]
         res[name] = {"sweeps_per_s": nsw / t_sw, "s_total": t_all, "s_infinite": t_inf,
-                     "steps": len(recs), "energy_final": recs[-1]["energy"][0]}
+                     "steps": len(recs), "energy_final": recs[-1]["energy"][0],
+                     "finite_step_ms": {"step": statistics.mean(r["ms_step"] for r in fin),
+                                        "eigensolve": statistics.mean(r["ms_eigh"] for r in fin),
+                                        "rdm": statistics.mean(r["ms_solve"] - r["ms_eigh"] for r in fin),
+                                        "host": statistics.mean(r["ms_step"] - r["ms_solve"] for r in fin),
+                                        "host_build": statistics.mean(r["ms_build"] for r in fin),
+                                        "host_renorm": statistics.mean(r["ms_renorm"] for r in fin),
+                                        "nnz_u": statistics.mean(r["nnz_u"] for r in fin),
+                                        "nnz_ops": statistics.mean(r["nnz_ops"] for r in fin),
+                                        "rdm_fallback_blocks": sum(r["rdm_fallback_blocks"] for r in fin),
+                                        "rdm_own_blocks": sum(r["rdm_own_blocks"] for r in fin),
+                                        "numop": statistics.mean(r["numop"] for r in fin),
+                                        "N_max": max(r["n"] for r in fin)}}
     out.update(res)
     out["speedup_mixed_vs_fp64"] = res["mixed"]["sweeps_per_s"] / res["fp64"]["sweeps_per_s"]
     out["dE_rel_mixed_vs_fp64"] = abs(res["mixed"]["energy_final"] - res["fp64"]["energy_final"]) / \
@@ -374,7 +387,9 @@ def run_gpu(args):
                                   seed=seed, precision=p, want_vectors=False)
         if mid is not None:
             mid.record(ext)
-        res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=False)
+        # the full RDM step of a DMRG iteration: eigenvalues, truncation and
+        # the kept eigenvectors (rotation matrices U, copied to the host)
+        res = sb.sb_get_rdm(WORKLOAD["mdmrg"], 0.1, want_u=True)
         return ev, numop, res
 
     def time_path(p, steps, sample_clocks):

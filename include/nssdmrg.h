@@ -183,6 +183,15 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
             int32_t *kept_left, int32_t *kept_right,
             double *u_left, double *u_right);
 
+/* Eigensolver statistics of the last nss_rdm: rho blocks diagonalised by the
+ * library's own FP64 eigensolver (Householder tridiagonalisation, bisection,
+ * twisted-factorisation vectors of the kept states), blocks sent to the
+ * Jacobi / batched cuSOLVER path (larger than 160, or env
+ * NSS_RDM_EIG=library), and own blocks whose kept vectors were recomputed by
+ * that path (close relative eigenvalue gaps).  No counterpart in the
+ * reference (LAPACK dsyev per block, src/MATRIX/MATRIX_BLOCKS.f90:589-657). */
+int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int *fallback_blocks);
+
 /* Timing of the mixed method's persistent Lanczos kernel: with `enable`
  * set, each launch in later nss_eigh calls is bracketed by CUDA events on
  * the context stream; nss_chunk_stats returns, for the last nss_eigh, the
@@ -292,6 +301,16 @@ typedef struct {
     double  trunc_left, trunc_right;
     int32_t m_left, m_right;   /* block dims after the step */
     double  ms_solve;       /* device time of nss_eigh + nss_rdm */
+    double  ms_eigh;        /* device time of nss_eigh alone */
+    double  ms_step;        /* host wall time of the whole step (block build,
+                               superblock upload, solve, renormalisation) */
+    double  ms_build;       /* host time of the block enlargement and the
+                               superblock build */
+    double  ms_renorm;      /* host time of the operator renormalisation */
+    int64_t nnz_u;          /* nonzeros of the two rotation matrices */
+    int64_t nnz_ops;        /* nonzeros of the renormalised block operators */
+    int32_t rdm_own_blocks;     /* rho blocks on the own eigensolver ... */
+    int32_t rdm_fallback_blocks;/* ... and those whose kept vectors the library recomputed */
 } nss_step_record;
 
 typedef struct nss_dmrg nss_dmrg;

@@ -84,7 +84,10 @@ class StepRecord(C.Structure):
                 ("current_l", C.c_int32), ("n", C.c_int64), ("nsb", C.c_int32), ("numop", C.c_int32),
                 ("energy", C.c_double * 2), ("entropy_left", C.c_double), ("entropy_right", C.c_double),
                 ("trunc_left", C.c_double), ("trunc_right", C.c_double), ("m_left", C.c_int32),
-                ("m_right", C.c_int32), ("ms_solve", C.c_double)]
+                ("m_right", C.c_int32), ("ms_solve", C.c_double), ("ms_eigh", C.c_double),
+                ("ms_step", C.c_double), ("ms_build", C.c_double), ("ms_renorm", C.c_double),
+                ("nnz_u", C.c_int64), ("nnz_ops", C.c_int64), ("rdm_own_blocks", C.c_int32),
+                ("rdm_fallback_blocks", C.c_int32)]
 
 
 _lib = None
@@ -137,6 +140,7 @@ def lib():
         "nss_dmrg_finite": (C.c_int, [P]),
         "nss_dmrg_prepare_last": (C.c_int, [P]),
         "nss_dmrg_export_superblock": (C.c_int, [P, C.POINTER(SbDesc)]),
+        "nss_rdm_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "nss_dmrg_nrecords": (C.c_int, [P]),
         "nss_dmrg_records": (C.c_int, [P, C.POINTER(StepRecord), C.c_int]),
     }
@@ -372,6 +376,13 @@ class Superblock:
         ms, nl, it, cols = C.c_double(), C.c_int(), C.c_int64(), C.c_double()
         self._check(lib().nss_chunk_stats(self._ctx, C.byref(ms), C.byref(nl), C.byref(it), C.byref(cols)))
         return ms.value, nl.value, it.value, cols.value
+
+    def rdm_stats(self):
+        """(own-eigensolver blocks, library blocks, own blocks recomputed by
+        the library) of the last sb_get_rdm."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().nss_rdm_stats(self._ctx, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def upload_desc(self, desc: SbDesc):
         self._check(lib().nss_sb_upload(self._ctx, C.byref(desc)))

@@ -223,6 +223,14 @@ int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iter
     return NSS_OK;
 }
 
+int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int *fallback_blocks) {
+    if (!ctx) return NSS_ERR_INVALID;
+    if (own_blocks) *own_blocks = ctx->c.rdm_own_blocks;
+    if (library_blocks) *library_blocks = ctx->c.rdm_lib_blocks;
+    if (fallback_blocks) *fallback_blocks = ctx->c.rdm_fallback_blocks;
+    return NSS_OK;
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

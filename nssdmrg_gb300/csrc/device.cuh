@@ -126,6 +126,16 @@ struct DevRdm {
     int *bat_info = nullptr;
     int64_t cap_bat_info = 0;
     void *params = nullptr;      // cusolverDnParams_t
+    double *vec = nullptr;       // eigenvector blocks, column-major, rho layout
+    int64_t cap_vec = 0;
+    double *syd = nullptr;       // own eigensolver: reflectors, T, tau, L D L^T, scale, shift
+    int64_t cap_syd = 0;
+    int *syi = nullptr;          // own eigensolver: per-block flags
+    int64_t cap_syi = 0;
+    unsigned char *tab = nullptr;    // per-call tables (device) ...
+    int64_t cap_tab = 0;
+    unsigned char *htab = nullptr;   // ... and their pinned host staging
+    int64_t cap_htab = 0;
 };
 
 struct Ctx {
@@ -149,6 +159,9 @@ struct Ctx {
     int chunk_launches = 0;
     int64_t chunk_iters = 0;     // iterations those launches completed
     double chunk_cols = 0.0;     // sum over those iterations of the basis size m
+    // last nss_rdm: blocks on the own eigensolver, on the library, and own
+    // blocks whose vectors were recomputed by the library
+    int rdm_own_blocks = 0, rdm_lib_blocks = 0, rdm_fallback_blocks = 0;
 };
 
 // Allocation through the context budget.
@@ -199,6 +212,19 @@ int batch_add(BatchEngine *e, Ctx &c, uint64_t seed, int nitermax, double tol, i
 int batch_step(BatchEngine *e, int max_done, int *ndone, int *ids, double *energies, int *numops);
 int batch_inflight(const BatchEngine *e);
 void lanczos_release(Ctx &c);
+
+// k_syev.cu: FP64 eigensolver of the rho blocks (blocks up to SYEV_MAX)
+constexpr int SYEV_MAX = 160;
+int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
+             int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, cudaStream_t st);
+int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
+                const double *te, double *evals, double *ldd, double *ldl, double *bscale, double *bsig,
+                int *flags, int *sub, cudaStream_t st);
+int syev_vec(const int *order, const int *rank, int ev_base, int ms, int nblk, const int *ev_off, const int *dims,
+             const int64_t *rho_off, const int *bmode, const int *sub, const double *evals, const double *ldd,
+             const double *ldl, const double *bscale, const double *bsig, const double *tau, const double *refl,
+             const int *perm, int *flags, double *vec, cudaStream_t st);
+int syev_eigs_per_cta();
 
 // k_rdm.cu
 int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2],

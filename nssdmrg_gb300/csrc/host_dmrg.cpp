@@ -221,6 +221,7 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
 
 // step_dmrg (src/DMRG_MAIN.f90:262-433), OBC link 'n'
 int Driver::step(int type, int label, int sweep) {
+    const auto t_step = std::chrono::steady_clock::now();
     const int mstates = (type == 0) ? p.mdmrg : msweep.at(sweep - 1);
     left = enlarge_block(left, dot, 'l', hij);
     right = enlarge_block(right, dot, 'r', hij);
@@ -247,8 +248,10 @@ int Driver::step(int type, int label, int sweep) {
         stopped = true;
         return rc;
     }
+    rec.ms_build = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     int rc = nss_solve_step(*ctx, sb, p, mstates, renorm, left, right, rec);
     if (rc) return rc;
+    rec.ms_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     records.push_back(rec);
     return NSS_OK;
 }
@@ -341,12 +344,14 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     const int nitermax = (int)std::min<int64_t>(n, p.lanc_niter);
     double ev[4] = {0, 0, 0, 0};
     int numop = 0;
-    cudaEvent_t e0, e1;
+    cudaEvent_t e0, e1, em;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    cudaEventCreate(&em);
     cudaEventRecord(e0, c.stream);
     rc = lanczos_eigh(c, neigen, nitermax, p.lanc_tolerance, p.seed, p.precision, ev, &numop);
     if (rc) return rc;
+    cudaEventRecord(em, c.stream);
     nss_rdm_side side[2];
     std::vector<double> u_l, u_r;
     std::vector<int32_t> k_l, k_r;
@@ -361,11 +366,16 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     if (rc) return rc;
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
-    float ms = 0.f;
+    float ms = 0.f, ms_e = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventElapsedTime(&ms_e, e0, em);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaEventDestroy(em);
     rec.ms_solve = ms;
+    rec.ms_eigh = ms_e;
+    rec.rdm_own_blocks = c.rdm_own_blocks;
+    rec.rdm_fallback_blocks = c.rdm_fallback_blocks;
     rec.numop = numop;
     for (int e = 0; e < 2; ++e) rec.energy[e] = (e < neigen) ? ev[e] / rec.current_l : 0.0;
     rec.entropy_left = side[0].entropy;
@@ -380,8 +390,15 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             for (size_t t = 0; t < q.size(); ++t) q[t] -= sb.qns[k_r[j]][t];
             qr.push_back(q);
         }
-        renormalize(left, u_to_csr(u_l, sb.m_left, side[0].m_s), ql);
-        renormalize(right, u_to_csr(u_r, sb.m_right, side[1].m_s), qr);
+        const auto t_r = std::chrono::steady_clock::now();
+        const Csr cul = u_to_csr(u_l, sb.m_left, side[0].m_s), cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
+        renormalize(left, cul, ql);
+        renormalize(right, cur, qr);
+        rec.nnz_u = cul.nnz() + cur.nnz();
+        rec.nnz_ops = 0;
+        for (const auto &o : left.ops) rec.nnz_ops += o.m.nnz();
+        for (const auto &o : right.ops) rec.nnz_ops += o.m.nnz();
+        rec.ms_renorm = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_r).count();
         rec.trunc_left = side[0].trunc_err;
         rec.trunc_right = side[1].trunc_err;
         rec.m_left = left.dim;

@@ -19,6 +19,7 @@
 #include "device.cuh"
 
 #include <cstdlib>
+#include <cstring>
 
 #include <cusolverDn.h>
 
@@ -106,7 +107,8 @@ __global__ void k_clamp(double *ev, int n) {
 // pipe); -0.0 is read as +0.0.  Keys are staged through shared memory.
 __device__ __forceinline__ long long rank_key(double x) { return x == 0.0 ? 0ll : __double_as_longlong(x); }
 
-__global__ void __launch_bounds__(256) k_rank(const double *ev, int n, double *sorted, int *order) {
+__global__ void __launch_bounds__(256) k_rank(const double *ev, int n, double *sorted, int *order,
+                                              int *rank_of /* may be null */) {
     __shared__ long long ks[1024];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const long long xi = i < n ? rank_key(ev[i]) : 0ll;
@@ -125,6 +127,7 @@ __global__ void __launch_bounds__(256) k_rank(const double *ev, int n, double *s
     if (i < n) {
         sorted[r] = ev[i];
         order[r] = i;
+        if (rank_of) rank_of[i] = r;
     }
 }
 
@@ -218,9 +221,10 @@ int jacobi_max() {
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_jacobi(double *rho, const int64_t *__restrict__ rho_off,
+__global__ void __launch_bounds__(256) k_jacobi(const double *rho, const int64_t *__restrict__ rho_off,
                                                 const int *__restrict__ dims, const int *__restrict__ ev_off,
-                                                const int *__restrict__ blocks, double *evals) {
+                                                const int *__restrict__ blocks, double *vec_out,
+                                                double *evals /* may be null: vectors only */) {
     extern __shared__ double jac_smem[];            // A and V: 2 x JAC_MAX x (JAC_MAX+1)
     double(*A)[JAC_MAX + 1] = reinterpret_cast<double(*)[JAC_MAX + 1]>(jac_smem);
     double(*V)[JAC_MAX + 1] = reinterpret_cast<double(*)[JAC_MAX + 1]>(jac_smem + JAC_MAX * (JAC_MAX + 1));
@@ -230,7 +234,8 @@ __global__ void __launch_bounds__(256) k_jacobi(double *rho, const int64_t *__re
     __shared__ int perm[JAC_MAX];
     const int q = blocks[blockIdx.x];
     const int n = dims[q];
-    double *R = rho + rho_off[q];
+    const double *R = rho + rho_off[q];
+    double *Vout = vec_out + rho_off[q];
     const int tid = threadIdx.x;
     for (int e = tid; e < n * n; e += blockDim.x) {
         const int i = e / n, j = e % n;
@@ -319,11 +324,10 @@ __global__ void __launch_bounds__(256) k_jacobi(double *rho, const int64_t *__re
         perm[rnk] = i;
     }
     __syncthreads();
-    double *ev = evals + ev_off[q];
     for (int e = tid; e < n * n; e += blockDim.x) {
         const int col = e / n, row = e % n;         // column-major output
-        R[e] = V[row][perm[col]];
-        if (row == 0) ev[col] = A[perm[col]][perm[col]];
+        Vout[e] = V[row][perm[col]];
+        if (row == 0 && evals) evals[ev_off[q] + col] = A[perm[col]][perm[col]];
     }
 }
 
@@ -360,22 +364,60 @@ __global__ void __launch_bounds__(256) k_pack(const double *__restrict__ rho, co
 __global__ void __launch_bounds__(256) k_unpack(const double *__restrict__ A, const double *__restrict__ Wb, int N,
                                                 const int *__restrict__ list, const int *__restrict__ dims,
                                                 const int64_t *__restrict__ rho_off, const int *__restrict__ ev_off,
-                                                double *__restrict__ rho, double *__restrict__ evals) {
+                                                double *__restrict__ vec_out, double *__restrict__ evals) {
     const int b = blockIdx.x, q = list[b], d = dims[q], sh = N - d;
     const double *Ab = A + (int64_t)b * N * N;
-    double *R = rho + rho_off[q];
+    double *R = vec_out + rho_off[q];
     for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
         const int col = e / d, row = e % d;
         R[e] = Ab[(int64_t)(sh + col) * N + row];
     }
-    for (int i = threadIdx.x; i < d; i += blockDim.x) evals[ev_off[q] + i] = Wb[(int64_t)b * N + sh + i];
+    if (evals)
+        for (int i = threadIdx.x; i < d; i += blockDim.x) evals[ev_off[q] + i] = Wb[(int64_t)b * N + sh + i];
 }
 
-int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
+// Library vectors of the blocks whose own-path vectors were rejected: the
+// library orders a block's eigenpairs ascending over the whole block, the
+// own path ascending within each unreduced part of its tridiagonal form, so
+// column col of the output takes the library column whose rank matches the
+// rank of evals[col] in the block (ties by position).
+__global__ void __launch_bounds__(256) k_fbperm(const int *__restrict__ list, const int *__restrict__ dims,
+                                              const int *__restrict__ ev_off, const int64_t *__restrict__ rho_off,
+                                              const double *__restrict__ evals, const double *__restrict__ src,
+                                              double *__restrict__ dst) {
+    __shared__ int perm[SYEV_MAX];
+    const int q = list[blockIdx.x], n = dims[q];
+    const double *ev = evals + ev_off[q];
+    for (int col = threadIdx.x; col < n; col += blockDim.x) {
+        const double x = ev[col];
+        int rk = 0;
+        for (int i = 0; i < n; ++i) rk += (ev[i] < x) || (ev[i] == x && i < col);
+        perm[col] = rk;
+    }
+    __syncthreads();
+    const double *S = src + rho_off[q];
+    double *D = dst + rho_off[q];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int col = e / n, row = e - col * n;
+        D[e] = S[(int64_t)perm[col] * n + row];
+    }
+}
+
+// rho-block eigensolver: blocks up to SYEV_MAX take the eigensolver of
+// k_syev.cu, larger ones k_jacobi / the batched library eigensolve (which
+// also recomputes the vectors of blocks the former marks).  Env
+// NSS_RDM_EIG=library sends every block to the library path.
+bool rdm_own_eigensolver() {
+    const char *e = std::getenv("NSS_RDM_EIG");
+    return !(e && std::string(e) == "library");
+}
+
+template <class T>
+int ensure_n(Ctx &c, T **p, int64_t &cap, int64_t need) {
     if (*p && cap >= need) return NSS_OK;
     ctx_free(c, *p);
     *p = nullptr;
-    NSS_CUDA_TRY(c, ctx_alloc(c, p, (size_t)need));
+    NSS_CUDA_TRY(c, ctx_alloc(c, p, (size_t)std::max<int64_t>(need, 1)));
     cap = need;
     return NSS_OK;
 }
@@ -384,8 +426,10 @@ int ensure(Ctx &c, double **p, int64_t &cap, int64_t need) {
 
 void rdm_release(Ctx &c) {
     DevRdm &r = c.rdm;
-    void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal, r.bat, r.bat_info};
+    void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal, r.bat, r.bat_info,
+                    r.vec, r.syd, r.syi, r.tab};
     for (void *p : ptrs) ctx_free(c, p);
+    if (r.htab) cudaFreeHost(r.htab);
     for (int i = 0; i < DevRdm::NSIDE; ++i) {
         if (r.side[i]) cudaStreamDestroy(r.side[i]);
         if (r.ev_join[i]) cudaEventDestroy(r.ev_join[i]);
@@ -403,12 +447,12 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     if (mstates < 1) { c.err = "nss_rdm: Mstates must be >= 1 (Edmrg mode is not supported)"; return NSS_ERR_INVALID; }
     cudaStream_t st = c.stream;
     DevRdm &r = c.rdm;
-    const int nsb = s.nsb;
+    const int nsb = s.nsb, nblk = 2 * nsb;
     // block layout: left blocks 0..nsb-1 then right blocks
-    std::vector<int64_t> rho_off(2 * nsb + 1);
-    std::vector<int> dims(2 * nsb), ev_off(2 * nsb + 2);
+    std::vector<int64_t> rho_off(nblk + 1);
+    std::vector<int> dims(nblk), ev_off(nblk + 2);
     int64_t acc = 0;
-    int eacc = 0, maxd = 1;
+    int eacc = 0;
     for (int side = 0; side < 2; ++side)
         for (int k = 0; k < nsb; ++k) {
             const int d = side == 0 ? s.dls[k] : s.drs[k];
@@ -418,10 +462,9 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             ev_off[q] = eacc;
             acc += (int64_t)d * d;
             eacc += d;
-            maxd = std::max(maxd, d);
         }
-    rho_off[2 * nsb] = acc;
-    ev_off[2 * nsb] = eacc;
+    rho_off[nblk] = acc;
+    ev_off[nblk] = eacc;
     const int nl = ev_off[nsb], nr = eacc - nl;
     std::vector<RhoItem> items;
     for (int side = 0; side < 2; ++side)
@@ -430,163 +473,232 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             for (int r0 = 0; r0 < d; r0 += RT)
                 for (int c0 = 0; c0 < d; c0 += RT) items.push_back({side, k, r0, c0});
         }
-    // device scratch: rho pool, evals, sorted, order, tables
+    // eigensolver path of each block
+    const bool own_path = rdm_own_eigensolver();
+    const int jmax = jacobi_max();
+    std::vector<int> own, small, large;
+    int maxn_own = 1;
+    for (int q = 0; q < nblk; ++q) {
+        if (own_path && dims[q] <= SYEV_MAX) {
+            own.push_back(q);
+            maxn_own = std::max(maxn_own, dims[q]);
+        } else if (dims[q] <= jmax) {
+            small.push_back(q);
+        } else {
+            large.push_back(q);
+        }
+    }
+    std::vector<int2> bis;
+    const int epc = syev_eigs_per_cta();
+    for (int q : own)
+        for (int k0 = 0; k0 < dims[q]; k0 += epc) bis.push_back(make_int2(q, k0));
+    std::vector<int> bmode(nblk, 1);
+    for (int q : own) bmode[q] = 0;
+    std::vector<int> maps(s.ai), map_off(s.ai_off);
+    for (int k = 1; k <= nsb; ++k) map_off.push_back((int)s.ai.size() + s.bi_off[k]);
+    maps.insert(maps.end(), s.bi.begin(), s.bi.end());
+    const int mblk[2] = {s.m_left, s.m_right};
+    const int kmax = std::max(1, std::max(s.m_left, s.m_right));
+    // device scratch (grow-only)
     int rc;
     int64_t cap_sorted = r.cap_evals;
-    if ((rc = ensure(c, &r.rho, r.cap_rho, acc))) return rc;
-    if ((rc = ensure(c, &r.evals, r.cap_evals, eacc))) return rc;
+    if ((rc = ensure_n(c, &r.rho, r.cap_rho, acc))) return rc;
+    if ((rc = ensure_n(c, &r.vec, r.cap_vec, acc))) return rc;
+    if ((rc = ensure_n(c, &r.evals, r.cap_evals, eacc))) return rc;
     if (!r.sorted || cap_sorted < eacc || !r.order) {
         ctx_free(c, r.sorted);
         ctx_free(c, r.order);
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.sorted, (size_t)eacc));
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.order, (size_t)eacc));
     }
-    const int mblk[2] = {s.m_left, s.m_right};
-    const int64_t ucap = (int64_t)std::max(s.m_left, s.m_right) * std::max(s.m_left, s.m_right);
-    if ((rc = ensure(c, &r.u, r.cap_u, ucap))) return rc;
+    const int64_t ucap = (int64_t)kmax * kmax;
+    if ((rc = ensure_n(c, &r.u, r.cap_u, ucap))) return rc;
     if (!r.scal) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.scal, 8));
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.iscal, 8));
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.info, DevRdm::NSIDE));
     }
-    // small tables (allocated per call; freed at the end)
-    RhoItem *d_items = nullptr;
-    int64_t *d_rho_off = nullptr;
-    int *d_dims = nullptr, *d_ev_off = nullptr, *d_maps = nullptr, *d_map_off = nullptr;
-    std::vector<int> maps(s.ai), map_off(s.ai_off);
-    for (int k = 1; k <= nsb; ++k) map_off.push_back((int)s.ai.size() + s.bi_off[k]);
-    maps.insert(maps.end(), s.bi.begin(), s.bi.end());
-    auto up = [&](auto **dst, const auto &src) -> int {
-        NSS_CUDA_TRY(c, ctx_alloc(c, dst, src.size()));
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, st));
-        return NSS_OK;
+    // own eigensolver: reflectors (rho layout), T, tau, L D L^T (eigenvalue
+    // layout), per-block scale and shift; per-block flags
+    const int64_t syd_need = own.empty() ? 1 : acc + 5 * (int64_t)eacc + 2 * nblk;
+    if ((rc = ensure_n(c, &r.syd, r.cap_syd, syd_need))) return rc;
+    if ((rc = ensure_n(c, &r.syi, r.cap_syi, nblk + 3 * (int64_t)eacc))) return rc;
+    double *refl = r.syd, *td = refl + acc, *te = td + eacc, *tau = te + eacc, *ldd = tau + eacc,
+           *ldl = ldd + eacc, *bscale = ldl + eacc, *bsig = bscale + nblk;
+    int *flags = r.syi, *sub = flags + nblk, *rnk = sub + eacc, *perm = rnk + eacc;
+    // the call's tables: packed into one pinned staging buffer, one copy
+    size_t tot = 0;
+    auto slot = [&](size_t bytes) {
+        const size_t o = (tot + 15) & ~size_t(15);
+        tot = o + bytes;
+        return o;
     };
-    int *jac_tmp = nullptr;
+    const size_t o_items = slot(items.size() * sizeof(RhoItem)), o_rho_off = slot(rho_off.size() * sizeof(int64_t)),
+                 o_dims = slot(dims.size() * sizeof(int)), o_ev_off = slot(ev_off.size() * sizeof(int)),
+                 o_maps = slot(maps.size() * sizeof(int)), o_map_off = slot(map_off.size() * sizeof(int)),
+                 o_own = slot(own.size() * sizeof(int)), o_bis = slot(bis.size() * sizeof(int2)),
+                 o_bmode = slot(bmode.size() * sizeof(int)), o_kept = slot(2 * (size_t)kmax * sizeof(int));
+    if (!r.htab || r.cap_htab < (int64_t)tot) {
+        if (r.htab) cudaFreeHost(r.htab);
+        r.htab = nullptr;
+        NSS_CUDA_TRY(c, cudaHostAlloc((void **)&r.htab, tot, cudaHostAllocDefault));
+        r.cap_htab = (int64_t)tot;
+    }
+    if ((rc = ensure_n(c, &r.tab, r.cap_tab, (int64_t)tot))) return rc;
+    auto put = [&](size_t o, const auto &v) {
+        if (!v.empty()) std::memcpy(r.htab + o, v.data(), v.size() * sizeof(v[0]));
+    };
+    put(o_items, items);
+    put(o_rho_off, rho_off);
+    put(o_dims, dims);
+    put(o_ev_off, ev_off);
+    put(o_maps, maps);
+    put(o_map_off, map_off);
+    put(o_own, own);
+    put(o_bis, bis);
+    put(o_bmode, bmode);
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(r.tab, r.htab, o_kept, cudaMemcpyHostToDevice, st));
+    const RhoItem *d_items = (const RhoItem *)(r.tab + o_items);
+    const int64_t *d_rho_off = (const int64_t *)(r.tab + o_rho_off);
+    const int *d_dims = (const int *)(r.tab + o_dims), *d_ev_off = (const int *)(r.tab + o_ev_off),
+              *d_maps = (const int *)(r.tab + o_maps), *d_map_off = (const int *)(r.tab + o_map_off),
+              *d_own = (const int *)(r.tab + o_own), *d_bmode = (const int *)(r.tab + o_bmode);
+    const int2 *d_bis = (const int2 *)(r.tab + o_bis);
+    int *d_kept = (int *)(r.tab + o_kept);
+    std::vector<void *> temps;
     auto cleanup = [&]() {
         cudaStreamSynchronize(st);
-        void *ptrs[] = {d_items, d_rho_off, d_dims, d_ev_off, d_maps, d_map_off, jac_tmp};
-        for (void *p : ptrs) ctx_free(c, p);
+        for (void *p : temps) ctx_free(c, p);
     };
-    if ((rc = up(&d_items, items)) || (rc = up(&d_rho_off, rho_off)) || (rc = up(&d_dims, dims)) ||
-        (rc = up(&d_ev_off, ev_off)) || (rc = up(&d_maps, maps)) || (rc = up(&d_map_off, map_off))) {
-        cleanup();
-        return rc;
-    }
     ++c.launches;
     k_rho<<<(int)items.size(), 256, 0, st>>>(d_psi, d_items, s.d_dls, s.d_drs, s.d_off, d_rho_off, nsb, r.rho);
     NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
     ++c.launches;
-    k_symcheck<<<std::min(2 * nsb, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, 2 * nsb, r.iscal + 7);
-    // Block eigensolves.  Small blocks: one k_jacobi launch on the main
-    // stream.  The others: one batched library eigensolve per padded size
-    // class N = 32*ceil(d/32) (each block embedded in an N x N matrix whose
-    // extra diagonal lies below its spectrum), the classes on side streams.
-    // A batched call costs about one single-matrix call on this GPU (the
-    // FP64 chains of one matrix run on one SM), so this replaces 2*nsb
-    // dependent chains by a handful.
-    cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
-    if (!r.ev_fork) {
-        NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
-        for (int i = 0; i < DevRdm::NSIDE; ++i) {
-            NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&r.side[i], cudaStreamNonBlocking));
-            NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
-        }
-    }
-    if (!r.params) {
-        cusolverDnParams_t prm = nullptr;
-        if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) {
-            cleanup();
-            c.err = "nss_rdm: cusolverDnCreateParams failed";
-            return NSS_ERR_CUDA;
-        }
-        r.params = prm;
-    }
-    std::vector<int> small, large;
-    const int jmax = jacobi_max();
-    for (int q = 0; q < 2 * nsb; ++q) (dims[q] <= jmax ? small : large).push_back(q);
-    // size classes, largest first
-    std::map<int, std::vector<int>, std::greater<int>> classes;
-    for (int q : large) classes[32 * ((dims[q] + 31) / 32)].push_back(q);
-    struct Cls {
-        int N, batch;
-        int64_t a_off, w_off, ws_off, list_off;
-        size_t ws;
-        std::vector<char> hws;
-    };
-    std::vector<Cls> cls;
-    std::vector<int> lists(small);
-    int64_t pool = 0;
-    for (auto &kv : classes) {
-        Cls cl;
-        cl.N = kv.first;
-        cl.batch = (int)kv.second.size();
-        cl.list_off = (int64_t)lists.size();
-        lists.insert(lists.end(), kv.second.begin(), kv.second.end());
-        size_t wd = 0, wh = 0;
-        if (cusolverDnXsyevBatched_bufferSize(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
-                                              CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, r.rho, cl.N, CUDA_R_64F,
-                                              r.evals, CUDA_R_64F, &wd, &wh, cl.batch) != CUSOLVER_STATUS_SUCCESS) {
-            cleanup();
-            c.err = "nss_rdm: cusolverDnXsyevBatched_bufferSize failed";
-            return NSS_ERR_CUDA;
-        }
-        cl.ws = wd;
-        cl.hws.resize(wh + 16);
-        cl.a_off = pool;
-        pool += (int64_t)cl.batch * cl.N * cl.N;
-        cl.w_off = pool;
-        pool += (int64_t)cl.batch * cl.N;
-        cl.ws_off = pool;
-        pool += (int64_t)(wd + 7) / 8 + 32;
-        cls.push_back(std::move(cl));
-    }
-    if ((rc = ensure(c, &r.bat, r.cap_bat, std::max<int64_t>(pool, 1)))) { cleanup(); return rc; }
-    if (!r.bat_info || r.cap_bat_info < (int64_t)large.size() + 1) {
-        ctx_free(c, r.bat_info);
-        r.bat_info = nullptr;
-        NSS_CUDA_TRY(c, ctx_alloc(c, &r.bat_info, large.size() + 1));
-        r.cap_bat_info = (int64_t)large.size() + 1;
-    }
-    if (!lists.empty()) {
-        NSS_CUDA_TRY(c, ctx_alloc(c, &jac_tmp, lists.size()));
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(jac_tmp, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    }
-    NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
-    for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
-    int info_off = 0;
-    for (size_t ci = 0; ci < cls.size(); ++ci) {
-        Cls &cl = cls[ci];
-        cudaStream_t ss = r.side[ci % DevRdm::NSIDE];
-        double *A = r.bat + cl.a_off, *W = r.bat + cl.w_off, *ws = r.bat + cl.ws_off;
+    k_symcheck<<<std::min(nblk, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, nblk, r.iscal + 7);
+    if (!own.empty()) {
+        NSS_CUDA_TRY(c, cudaMemsetAsync(flags, 0, nblk * sizeof(int), st));
         c.launches += 2;
-        k_pack<<<cl.batch, 256, 0, ss>>>(r.rho, d_rho_off, d_dims, jac_tmp + cl.list_off, cl.N, A);
-        cusolverDnSetStream(h, ss);
-        const cusolverStatus_t cs = cusolverDnXsyevBatched(
-            h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, A,
-            cl.N, CUDA_R_64F, W, CUDA_R_64F, ws, cl.ws, cl.hws.data(), cl.hws.size() - 16, r.bat_info + info_off,
-            cl.batch);
-        cusolverDnSetStream(h, st);
-        if (cs != CUSOLVER_STATUS_SUCCESS) {
+        int e = syev_trd(r.rho, d_rho_off, d_dims, d_ev_off, d_own, (int)own.size(), maxn_own, refl, td, te, tau,
+                         perm, st);
+        if (!e) e = syev_bisect(d_dims, d_ev_off, d_bis, (int)bis.size(), td, te, r.evals, ldd, ldl, bscale, bsig,
+                                flags, sub, st);
+        if (e) {
             cleanup();
-            c.err = "nss_rdm: cusolverDnXsyevBatched failed";
+            c.err = std::string("nss_rdm: eigensolver launch failed: ") + cudaGetErrorString((cudaError_t)e);
             return NSS_ERR_CUDA;
         }
-        k_unpack<<<cl.batch, 256, 0, ss>>>(A, W, cl.N, jac_tmp + cl.list_off, d_dims, d_rho_off, d_ev_off, r.rho,
-                                           r.evals);
-        NSS_CUDA_TRY(c, cudaGetLastError());
-        info_off += cl.batch;
     }
-    if (!small.empty()) {
-        constexpr int jac_smem = 2 * JAC_MAX * (JAC_MAX + 1) * (int)sizeof(double);
-        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, jac_smem));
-        ++c.launches;
-        k_jacobi<<<(int)small.size(), 256, jac_smem, st>>>(r.rho, d_rho_off, d_dims, d_ev_off, jac_tmp, r.evals);
-        NSS_CUDA_TRY(c, cudaGetLastError());
+    // Library eigensolves of a list of blocks, vectors into r.vec (and the
+    // eigenvalues when write_evals): blocks up to the Jacobi size in one
+    // k_jacobi launch on the main stream, the others one batched library
+    // eigensolve per padded size class N = 32*ceil(d/32) (each block embedded
+    // in an N x N matrix whose extra diagonal lies below its spectrum), the
+    // classes on side streams.
+    cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
+    auto lib_eigh = [&](const std::vector<int> &sm, const std::vector<int> &lg, bool write_evals,
+                        double *vec_out) -> int {
+        if (sm.empty() && lg.empty()) return NSS_OK;
+        if (!r.ev_fork) {
+            NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
+            for (int i = 0; i < DevRdm::NSIDE; ++i) {
+                NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&r.side[i], cudaStreamNonBlocking));
+                NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
+            }
+        }
+        if (!r.params) {
+            cusolverDnParams_t prm = nullptr;
+            if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) {
+                c.err = "nss_rdm: cusolverDnCreateParams failed";
+                return NSS_ERR_CUDA;
+            }
+            r.params = prm;
+        }
+        std::map<int, std::vector<int>, std::greater<int>> classes;
+        for (int q : lg) classes[32 * ((dims[q] + 31) / 32)].push_back(q);
+        struct Cls {
+            int N, batch;
+            int64_t a_off, w_off, ws_off, list_off;
+            size_t ws;
+            std::vector<char> hws;
+        };
+        std::vector<Cls> cls;
+        std::vector<int> lists(sm);
+        int64_t pool = 0;
+        for (auto &kv : classes) {
+            Cls cl;
+            cl.N = kv.first;
+            cl.batch = (int)kv.second.size();
+            cl.list_off = (int64_t)lists.size();
+            lists.insert(lists.end(), kv.second.begin(), kv.second.end());
+            size_t wd = 0, wh = 0;
+            if (cusolverDnXsyevBatched_bufferSize(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
+                                                  CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, r.rho, cl.N, CUDA_R_64F,
+                                                  r.evals, CUDA_R_64F, &wd, &wh, cl.batch) != CUSOLVER_STATUS_SUCCESS) {
+                c.err = "nss_rdm: cusolverDnXsyevBatched_bufferSize failed";
+                return NSS_ERR_CUDA;
+            }
+            cl.ws = wd;
+            cl.hws.resize(wh + 16);
+            cl.a_off = pool;
+            pool += (int64_t)cl.batch * cl.N * cl.N;
+            cl.w_off = pool;
+            pool += (int64_t)cl.batch * cl.N;
+            cl.ws_off = pool;
+            pool += (int64_t)(wd + 7) / 8 + 32;
+            cls.push_back(std::move(cl));
+        }
+        if ((rc = ensure_n(c, &r.bat, r.cap_bat, std::max<int64_t>(pool, 1)))) return rc;
+        if ((rc = ensure_n(c, &r.bat_info, r.cap_bat_info, (int64_t)lg.size() + 1))) return rc;
+        int *d_list = nullptr;
+        NSS_CUDA_TRY(c, ctx_alloc(c, &d_list, lists.size()));
+        temps.push_back(d_list);
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(d_list, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
+        for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
+        double *ev_out = write_evals ? r.evals : nullptr;
+        int info_off = 0;
+        for (size_t ci = 0; ci < cls.size(); ++ci) {
+            Cls &cl = cls[ci];
+            cudaStream_t ss = r.side[ci % DevRdm::NSIDE];
+            double *A = r.bat + cl.a_off, *W = r.bat + cl.w_off, *ws = r.bat + cl.ws_off;
+            c.launches += 2;
+            k_pack<<<cl.batch, 256, 0, ss>>>(r.rho, d_rho_off, d_dims, d_list + cl.list_off, cl.N, A);
+            cusolverDnSetStream(h, ss);
+            const cusolverStatus_t cs = cusolverDnXsyevBatched(
+                h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F,
+                A, cl.N, CUDA_R_64F, W, CUDA_R_64F, ws, cl.ws, cl.hws.data(), cl.hws.size() - 16,
+                r.bat_info + info_off, cl.batch);
+            cusolverDnSetStream(h, st);
+            if (cs != CUSOLVER_STATUS_SUCCESS) {
+                c.err = "nss_rdm: cusolverDnXsyevBatched failed";
+                return NSS_ERR_CUDA;
+            }
+            k_unpack<<<cl.batch, 256, 0, ss>>>(A, W, cl.N, d_list + cl.list_off, d_dims, d_rho_off, d_ev_off,
+                                               vec_out, ev_out);
+            NSS_CUDA_TRY(c, cudaGetLastError());
+            info_off += cl.batch;
+        }
+        if (!sm.empty()) {
+            constexpr int jac_smem = 2 * JAC_MAX * (JAC_MAX + 1) * (int)sizeof(double);
+            NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, jac_smem));
+            ++c.launches;
+            k_jacobi<<<(int)sm.size(), 256, jac_smem, st>>>(r.rho, d_rho_off, d_dims, d_ev_off, d_list, vec_out,
+                                                            ev_out);
+            NSS_CUDA_TRY(c, cudaGetLastError());
+        }
+        for (int i = 0; i < DevRdm::NSIDE; ++i) {
+            NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
+            NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
+        }
+        return NSS_OK;
+    };
+    if ((rc = lib_eigh(small, large, true, r.vec))) {
+        cleanup();
+        return rc;
     }
-    for (int i = 0; i < DevRdm::NSIDE; ++i) {
-        NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
-        NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
-    }
+    c.rdm_own_blocks = (int)own.size();
+    c.rdm_lib_blocks = (int)(small.size() + large.size());
+    c.rdm_fallback_blocks = 0;
     ++c.launches;
     k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
     // per side: rank, truncation, U
@@ -594,7 +706,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     for (int side = 0; side < 2; ++side) {
         const int n = nside[side], base = side == 0 ? 0 : nl;
         ++c.launches;
-        k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base);
+        k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base,
+                                                own.empty() ? nullptr : rnk + base);
         ++c.launches;
         k_truncate<<<1, 1024, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
                                      r.iscal + side);
@@ -615,9 +728,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     double *u_out[2] = {u_l, u_r};
     for (int side = 0; side < 2; ++side) {
         const int n = nside[side], base = side == 0 ? 0 : nl;
-        const int ms = hi[side];
         out[side].nevals = n;
-        out[side].m_s = ms;
+        out[side].m_s = hi[side];
         out[side].trunc_err = hs[2 * side];
         out[side].entropy = hs[2 * side + 1];
         if (lam_out[side]) {
@@ -626,23 +738,65 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             NSS_CUDA_TRY(c, cudaMemcpyAsync(lam_out[side], r.sorted + base, n * sizeof(double),
                                             cudaMemcpyDeviceToHost, st));
         }
+    }
+    // kept eigenvectors of the own path's blocks; marked blocks again
+    // through the library
+    if (!own.empty() && (u_l || u_r)) {
+        for (int side = 0; side < 2; ++side) {
+            if (!u_out[side]) continue;
+            const int base = side == 0 ? 0 : nl, o = side * nsb;
+            ++c.launches;
+            const int e = syev_vec(r.order + base, rnk, base, hi[side], nsb, d_ev_off + o, d_dims + o,
+                                   d_rho_off + o, d_bmode + o, sub, r.evals, ldd, ldl, bscale + o, bsig + o, tau,
+                                   refl, perm, flags + o, r.vec, st);
+            if (e) {
+                cleanup();
+                c.err = std::string("nss_rdm: eigenvector launch failed: ") + cudaGetErrorString((cudaError_t)e);
+                return NSS_ERR_CUDA;
+            }
+        }
+        std::vector<int> hflags(nblk);
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(hflags.data(), flags, nblk * sizeof(int), cudaMemcpyDeviceToHost, st));
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        std::vector<int> fs, fl;
+        for (int q : own)
+            if (hflags[q] & 2) (dims[q] <= jmax ? fs : fl).push_back(q);
+        c.rdm_fallback_blocks = (int)(fs.size() + fl.size());
+        if (c.rdm_fallback_blocks) {
+            // library vectors into the blocks' rho slots (consumed by then),
+            // then matched to the own path's eigenvalue order in r.vec
+            if ((rc = lib_eigh(fs, fl, false, r.rho))) {
+                cleanup();
+                return rc;
+            }
+            std::vector<int> fb(fs);
+            fb.insert(fb.end(), fl.begin(), fl.end());
+            int *d_fb = nullptr;
+            NSS_CUDA_TRY(c, ctx_alloc(c, &d_fb, fb.size()));
+            temps.push_back(d_fb);
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(d_fb, fb.data(), fb.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+            ++c.launches;
+            k_fbperm<<<(int)fb.size(), 256, 0, st>>>(d_fb, d_dims, d_ev_off, d_rho_off, r.evals, r.rho, r.vec);
+            NSS_CUDA_TRY(c, cudaGetLastError());
+        }
+    }
+    for (int side = 0; side < 2; ++side) {
+        const int base = side == 0 ? 0 : nl;
+        const int ms = hi[side];
         if (u_out[side] || kept_out[side]) {
             NSS_CUDA_TRY(c, cudaMemsetAsync(r.u, 0, (size_t)mblk[side] * ms * sizeof(double), st));
-            int *kept_buf = nullptr;
-            NSS_CUDA_TRY(c, ctx_alloc(c, &kept_buf, (size_t)std::max(ms, 1)));
-            int *d_kept = kept_buf;
+            int *dk = d_kept + side * kmax;
             ++c.launches;
-            k_umat<<<std::min(ms, 1024), 128, 0, st>>>(r.rho, d_rho_off + side * nsb, d_dims + side * nsb,
+            k_umat<<<std::min(ms, 1024), 128, 0, st>>>(r.vec, d_rho_off + side * nsb, d_dims + side * nsb,
                                                        d_ev_off + side * nsb, base, nsb, r.order + base, ms,
-                                                       d_maps, d_map_off + side * nsb, mblk[side], r.u, d_kept);
+                                                       d_maps, d_map_off + side * nsb, mblk[side], r.u, dk);
             NSS_CUDA_TRY(c, cudaGetLastError());
             if (u_out[side])
                 NSS_CUDA_TRY(c, cudaMemcpyAsync(u_out[side], r.u, (size_t)mblk[side] * ms * sizeof(double),
                                                 cudaMemcpyDeviceToHost, st));
             if (kept_out[side])
-                NSS_CUDA_TRY(c, cudaMemcpyAsync(kept_out[side], d_kept, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
-            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-            ctx_free(c, kept_buf);
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(kept_out[side], dk, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
+            if (u_out[side] && side == 0) NSS_CUDA_TRY(c, cudaStreamSynchronize(st));   // r.u is reused
         }
     }
     cleanup();

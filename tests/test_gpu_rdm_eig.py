@@ -1,0 +1,159 @@
+"""The library's own FP64 block eigensolver of the reduced density matrices
+(Householder tridiagonalisation, Sturm bisection, twisted-factorisation
+vectors of the kept states) against numpy's eigh on the same blocks and
+against the Jacobi / batched-cuSOLVER path (env NSS_RDM_EIG=library), through
+the C ABI.
+
+Tolerances: eigenvalues at 1e-13 absolute (rho has unit trace, so this is
+~500 ulps of the largest eigenvalue; both paths are backward stable with
+errors of a few n * eps); kept vectors orthonormal to 1e-12; the kept
+subspace (projector U U^T) equal to the library path's within
+100 eps ||rho|| / gap, gap the smallest distance between a kept and a
+discarded eigenvalue of one block: any backward-stable eigensolver fixes
+the kept space only to eps ||rho|| / gap (Davis-Kahan); truncation error and
+entropy as the oracle tests.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_npz
+from test_gpu_parity import _setup, _upload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nss():
+    import nssdmrg_gb300 as nss
+    nss.lib()
+    return nss
+
+
+def _rdm(s, mst, psi, library):
+    old = os.environ.get("NSS_RDM_EIG")
+    try:
+        if library:
+            os.environ["NSS_RDM_EIG"] = "library"
+        else:
+            os.environ.pop("NSS_RDM_EIG", None)
+        res = s.sb_get_rdm(mst, 0.1, psi=psi)
+        return res, s.rdm_stats()
+    finally:
+        if old is None:
+            os.environ.pop("NSS_RDM_EIG", None)
+        else:
+            os.environ["NSS_RDM_EIG"] = old
+
+
+def _blocks_of(psi, dls, drs, off):
+    out = [[], []]
+    for k in range(len(dls)):
+        W = psi[off[k]:off[k] + dls[k] * drs[k]].reshape(dls[k], drs[k])
+        out[0].append(W @ W.T)
+        out[1].append(W.T @ W)
+    return out
+
+
+def _edge_gap(blocks, ms):
+    """Smallest gap between a kept and a discarded eigenvalue of one block
+    when the ms largest eigenvalues over all blocks are kept."""
+    allw = sorted(((w, b) for b, blk in enumerate(blocks) for w in np.linalg.eigvalsh(blk)), key=lambda t: -t[0])
+    kept, disc = allw[:ms], allw[ms:]
+    lo = {}
+    for w, b in kept:
+        lo[b] = min(lo.get(b, np.inf), w)
+    g = np.inf
+    for w, b in disc:
+        if b in lo:
+            g = min(g, lo[b] - w)
+    return g, allw[0][0]
+
+
+def _check_against(res_own, res_lib, blocks):
+    for side in (0, 1):
+        np.testing.assert_allclose(res_own.lambdas[side], res_lib.lambdas[side], rtol=0, atol=1e-13)
+        assert res_own.m_s[side] == res_lib.m_s[side]
+        assert abs(res_own.trunc_err[side] - res_lib.trunc_err[side]) <= 1e-13
+        assert abs(res_own.entropy[side] - res_lib.entropy[side]) <= 1e-11 * abs(res_lib.entropy[side]) + 1e-14
+        u, ul = res_own.u[side], res_lib.u[side]
+        assert np.abs(u.T @ u - np.eye(u.shape[1])).max() <= 1e-12
+        kb, kbl = np.asarray(res_own.kept_blocks[side]), np.asarray(res_lib.kept_blocks[side])
+        assert sorted(kb.tolist()) == sorted(kbl.tolist())
+        # per kept block: the kept columns span the same subspace, and each
+        # column is an eigenvector of the block (residual vs the block rho)
+        gap, lmax = _edge_gap(blocks[side], res_own.m_s[side])
+        tol = max(1e-12, 100 * 2.0**-52 * lmax / gap)
+        assert np.abs(u @ u.T - ul @ ul.T).max() <= tol, (gap, tol)
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_own_eigensolver_matches_library_and_numpy(nss, name):
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    mst = int(z["params"][1]) if "params" in z else 128
+    own, st_own = _rdm(s, mst, z["psi"], library=False)
+    lib, st_lib = _rdm(s, mst, z["psi"], library=True)
+    assert st_own[0] > 0 and st_own[1] == 0, st_own
+    assert st_lib[0] == 0 and st_lib[1] > 0, st_lib
+    blocks = _blocks_of(z["psi"], z["sb_dls"], z["sb_drs"], z["sb_offset"])
+    _check_against(own, lib, blocks)
+    # eigenvalues against numpy on the same blocks
+    for side in (0, 1):
+        ref = np.sort(np.concatenate([np.linalg.eigvalsh(b) for b in blocks[side]]))[::-1]
+        ref = np.where(ref < 0, 0.0, ref)
+        np.testing.assert_allclose(own.lambdas[side], ref, rtol=0, atol=1e-13)
+
+
+def _synthetic_psi(dls, drs, off, n, rng, mode):
+    """psi whose sector blocks have prescribed singular values: exact pairs
+    (degenerate rho eigenvalues), pairs split at 1e-7 relative (a relative
+    cluster) or a graded spectrum with random factors."""
+    psi = np.zeros(n)
+    for k in range(len(dls)):
+        dl, dr = int(dls[k]), int(drs[k])
+        kk = min(dl, dr)
+        U, _ = np.linalg.qr(rng.standard_normal((dl, dl)))
+        V, _ = np.linalg.qr(rng.standard_normal((dr, dr)))
+        base = np.exp(-0.35 * np.arange(kk)) * (1.0 + 0.3 * rng.random(kk))
+        if mode == "pairs":
+            base[1::2] = base[0::2][: len(base[1::2])]
+        elif mode == "near_pairs":
+            base[1::2] = base[0::2][: len(base[1::2])] * (1.0 + 1e-7)
+        W = (U[:, :kk] * base) @ V[:, :kk].T
+        psi[off[k]:off[k] + dl * dr] = W.ravel()
+    return psi / np.linalg.norm(psi)
+
+
+@pytest.mark.parametrize("mode", ["graded", "pairs", "near_pairs"])
+def test_own_eigensolver_degenerate_spectra(nss, mode):
+    z = load_npz("c2_small.npz")
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    rng = np.random.default_rng({"graded": 1, "pairs": 2, "near_pairs": 3}[mode])
+    psi = _synthetic_psi(z["sb_dls"], z["sb_drs"], z["sb_offset"], len(z["psi"]), rng, mode)
+    own, st_own = _rdm(s, 96, psi, library=False)
+    lib, _ = _rdm(s, 96, psi, library=True)
+    assert st_own[0] > 0
+    _check_against(own, lib, _blocks_of(psi, z["sb_dls"], z["sb_drs"], z["sb_offset"]))
+
+
+def test_own_eigensolver_rank_deficient_blocks_fall_back(nss):
+    """Keeping every state of rank-deficient blocks asks for vectors of
+    numerically zero eigenvalues, which the own path leaves to the library:
+    the result must still be an orthonormal eigenbasis."""
+    z = load_npz("kat_spin.npz")
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    own, st_own = _rdm(s, 10_000, z["psi"], library=False)
+    lib, _ = _rdm(s, 10_000, z["psi"], library=True)
+    for side in (0, 1):
+        u = own.u[side]
+        assert np.abs(u.T @ u - np.eye(u.shape[1])).max() <= 1e-12
+        np.testing.assert_allclose(own.lambdas[side], lib.lambdas[side], rtol=0, atol=1e-13)
+        assert own.m_s[side] == lib.m_s[side]
