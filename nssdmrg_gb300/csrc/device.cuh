@@ -136,6 +136,8 @@ struct DevRdm {
     int64_t cap_tab = 0;
     unsigned char *htab = nullptr;   // ... and their pinned host staging
     int64_t cap_htab = 0;
+    double *hu = nullptr;            // pinned staging of the compact kept columns
+    int64_t cap_hu = 0;
 };
 
 struct Ctx {
@@ -220,10 +222,12 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
                 const double *te, double *evals, double *ldd, double *ldl, double *bscale, double *bsig,
                 int *flags, int *sub, cudaStream_t st);
-int syev_vec(const int *order, const int *rank, int ev_base, int ms, int nblk, const int *ev_off, const int *dims,
-             const int64_t *rho_off, const int *bmode, const int *sub, const double *evals, const double *ldd,
-             const double *ldl, const double *bscale, const double *bsig, const double *tau, const double *refl,
-             const int *perm, int *flags, double *vec, cudaStream_t st);
+// kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions
+// start at nl): k_vec + the cluster Gram-Schmidt, two launches
+int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
+             const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
+             const double *ldd, const double *ldl, const double *bscale, const double *bsig, const double *tau,
+             const double *refl, const int *perm, int *flags, double *vec, cudaStream_t st);
 int syev_eigs_per_cta();
 
 // k_rdm.cu
@@ -238,7 +242,8 @@ void rdm_release(Ctx &c);
     do {                                                                        \
         cudaError_t _e = (call);                                                \
         if (_e != cudaSuccess) {                                                \
-            (c).err = std::string(#call) + ": " + cudaGetErrorString(_e);       \
+            (c).err = std::string(#call) + " (" + __FILE__ + ":" + std::to_string(__LINE__) + "): " + \
+                      cudaGetErrorString(_e);                                   \
             return _e == cudaErrorMemoryAllocation ? NSS_ERR_NOMEM : NSS_ERR_CUDA; \
         }                                                                       \
     } while (0)

@@ -180,21 +180,58 @@ __global__ void __launch_bounds__(1024) k_truncate(const double *sorted, int n, 
     }
 }
 
-// U[map_q[p], j] = evec_q[p][col(j)] ; kept_blk[j] = q  (column-major U)
-__global__ void k_umat(const double *rho /*eigenvector blocks*/, const int64_t *rho_off, const int *dims,
-                       const int *ev_off /*[nblk+1] block starts*/, int ev_base, int nblk,
-                       const int *order, int ms, const int *maps, const int *map_off, int mblock,
-                       double *u, int *kept) {
-    for (int j = blockIdx.x; j < ms; j += gridDim.x) {
-        const int pos = order[j] + ev_base;   // position in the concatenated list
-        int q = 0;
-        while (q + 1 < nblk && ev_off[q + 1] <= pos) ++q;
-        const int col = pos - ev_off[q];
-        const int d = dims[q];
-        const double *E = rho + rho_off[q];   // column-major eigenvectors (cuSOLVER)
-        for (int p = threadIdx.x; p < d; p += blockDim.x)
-            u[(int64_t)j * mblock + maps[map_off[q] + p]] = E[(int64_t)col * d + p];
-        if (threadIdx.x == 0) kept[j] = q;
+// Compact form of the kept columns of one side (U without its zero rows):
+// kept[j] = block of column j (side-local), uoff[j] = start of its n_q
+// values in ucomp, ucomp[uoff[j] + p] = row p of the eigenvector.  One CTA:
+// an exclusive scan of n_q over j, then the copies.
+__global__ void __launch_bounds__(1024) k_ucompact(const double *__restrict__ vec, const int64_t *__restrict__ rho_off,
+                                                  const int *__restrict__ dims, const int *__restrict__ ev_off,
+                                                  int ev_base, int nblk, const int *__restrict__ order, int ms,
+                                                  int *__restrict__ kept, int *__restrict__ uoff,
+                                                  double *__restrict__ ucomp) {
+    __shared__ int wsum_s[32];
+    __shared__ int carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (int j0 = 0; j0 < ms; j0 += 1024) {
+        const int j = j0 + tid;
+        int nq = 0;
+        if (j < ms) {
+            const int pos = order[j] + ev_base;
+            int q = 0;
+            while (q + 1 < nblk && ev_off[q + 1] <= pos) ++q;
+            nq = dims[q];
+            kept[j] = q;
+        }
+        int x = nq;                                  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum_s[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int t = wsum_s[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            wsum_s[lane] = t;                        // inclusive over warps
+        }
+        __syncthreads();
+        const int base = carry_s + (warp > 0 ? wsum_s[warp - 1] : 0);
+        if (j < ms) uoff[j] = base + x - nq;
+        __syncthreads();
+        if (tid == 0) carry_s += wsum_s[31];
+        __syncthreads();
+    }
+    for (int j = warp; j < ms; j += 32) {
+        const int q = kept[j];
+        const int pos = order[j] + ev_base, col = pos - ev_off[q], nq = dims[q];
+        const double *E = vec + rho_off[q] + (int64_t)col * nq;
+        double *D = ucomp + uoff[j];
+        for (int p = lane; p < nq; p += 32) D[p] = E[p];
     }
 }
 
@@ -430,6 +467,7 @@ void rdm_release(Ctx &c) {
                     r.vec, r.syd, r.syi, r.tab};
     for (void *p : ptrs) ctx_free(c, p);
     if (r.htab) cudaFreeHost(r.htab);
+    if (r.hu) cudaFreeHost(r.hu);
     for (int i = 0; i < DevRdm::NSIDE; ++i) {
         if (r.side[i]) cudaStreamDestroy(r.side[i]);
         if (r.ev_join[i]) cudaEventDestroy(r.ev_join[i]);
@@ -511,7 +549,9 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.sorted, (size_t)eacc));
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.order, (size_t)eacc));
     }
-    const int64_t ucap = (int64_t)kmax * kmax;
+    int maxd = 1;
+    for (int d : dims) maxd = std::max(maxd, d);
+    const int64_t ucap = 2 * (int64_t)kmax * maxd;   // compact kept columns of both sides
     if ((rc = ensure_n(c, &r.u, r.cap_u, ucap))) return rc;
     if (!r.scal) {
         NSS_CUDA_TRY(c, ctx_alloc(c, &r.scal, 8));
@@ -537,7 +577,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
                  o_dims = slot(dims.size() * sizeof(int)), o_ev_off = slot(ev_off.size() * sizeof(int)),
                  o_maps = slot(maps.size() * sizeof(int)), o_map_off = slot(map_off.size() * sizeof(int)),
                  o_own = slot(own.size() * sizeof(int)), o_bis = slot(bis.size() * sizeof(int2)),
-                 o_bmode = slot(bmode.size() * sizeof(int)), o_kept = slot(2 * (size_t)kmax * sizeof(int));
+                 o_bmode = slot(bmode.size() * sizeof(int)), o_kept = slot(4 * (size_t)kmax * sizeof(int));
     if (!r.htab || r.cap_htab < (int64_t)tot) {
         if (r.htab) cudaFreeHost(r.htab);
         r.htab = nullptr;
@@ -742,18 +782,14 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // kept eigenvectors of the own path's blocks; marked blocks again
     // through the library
     if (!own.empty() && (u_l || u_r)) {
-        for (int side = 0; side < 2; ++side) {
-            if (!u_out[side]) continue;
-            const int base = side == 0 ? 0 : nl, o = side * nsb;
-            ++c.launches;
-            const int e = syev_vec(r.order + base, rnk, base, hi[side], nsb, d_ev_off + o, d_dims + o,
-                                   d_rho_off + o, d_bmode + o, sub, r.evals, ldd, ldl, bscale + o, bsig + o, tau,
-                                   refl, perm, flags + o, r.vec, st);
-            if (e) {
-                cleanup();
-                c.err = std::string("nss_rdm: eigenvector launch failed: ") + cudaGetErrorString((cudaError_t)e);
-                return NSS_ERR_CUDA;
-            }
+        const int msv[2] = {u_l ? hi[0] : 0, u_r ? hi[1] : 0};
+        c.launches += 2;
+        const int e = syev_vec(r.order, rnk, msv, nl, nsb, d_ev_off, d_dims, d_rho_off, d_bmode, sub, r.evals, ldd,
+                               ldl, bscale, bsig, tau, refl, perm, flags, r.vec, st);
+        if (e) {
+            cleanup();
+            c.err = std::string("nss_rdm: eigenvector launch failed: ") + cudaGetErrorString((cudaError_t)e);
+            return NSS_ERR_CUDA;
         }
         std::vector<int> hflags(nblk);
         NSS_CUDA_TRY(c, cudaMemcpyAsync(hflags.data(), flags, nblk * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -780,23 +816,65 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             NSS_CUDA_TRY(c, cudaGetLastError());
         }
     }
+    // kept columns, compact (no zero rows) -> pinned staging -> the dense
+    // m_block x m_s host matrices (zero rows outside each column's block)
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    int64_t hneed = 0;
+    for (int side = 0; side < 2; ++side) hneed += (int64_t)hi[side] * (maxd + 2);
+    if (!r.hu || r.cap_hu < hneed) {
+        if (r.hu) NSS_CUDA_TRY(c, cudaFreeHost(r.hu));
+        r.hu = nullptr;
+        NSS_CUDA_TRY(c, cudaHostAlloc((void **)&r.hu, (size_t)std::max<int64_t>(hneed, 1) * sizeof(double),
+                                      cudaHostAllocDefault));
+        r.cap_hu = hneed;
+    }
+    double *hval[2];
+    int *hkept[2], *hoff[2];
+    {
+        double *hp = r.hu;
+        for (int side = 0; side < 2; ++side) {
+            hval[side] = hp;
+            hp += (int64_t)hi[side] * maxd;
+        }
+        int *ip = (int *)hp;
+        for (int side = 0; side < 2; ++side) {
+            hkept[side] = ip;
+            hoff[side] = ip + hi[side];
+            ip += 2 * (int64_t)hi[side];
+        }
+    }
+    bool any = false;
     for (int side = 0; side < 2; ++side) {
         const int base = side == 0 ? 0 : nl;
         const int ms = hi[side];
-        if (u_out[side] || kept_out[side]) {
-            NSS_CUDA_TRY(c, cudaMemsetAsync(r.u, 0, (size_t)mblk[side] * ms * sizeof(double), st));
-            int *dk = d_kept + side * kmax;
-            ++c.launches;
-            k_umat<<<std::min(ms, 1024), 128, 0, st>>>(r.vec, d_rho_off + side * nsb, d_dims + side * nsb,
-                                                       d_ev_off + side * nsb, base, nsb, r.order + base, ms,
-                                                       d_maps, d_map_off + side * nsb, mblk[side], r.u, dk);
-            NSS_CUDA_TRY(c, cudaGetLastError());
-            if (u_out[side])
-                NSS_CUDA_TRY(c, cudaMemcpyAsync(u_out[side], r.u, (size_t)mblk[side] * ms * sizeof(double),
-                                                cudaMemcpyDeviceToHost, st));
-            if (kept_out[side])
-                NSS_CUDA_TRY(c, cudaMemcpyAsync(kept_out[side], dk, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
-            if (u_out[side] && side == 0) NSS_CUDA_TRY(c, cudaStreamSynchronize(st));   // r.u is reused
+        if (!(u_out[side] || kept_out[side])) continue;
+        any = true;
+        int *dk = d_kept + side * 2 * kmax, *doff = dk + kmax;
+        double *du = r.u + (int64_t)side * kmax * maxd;
+        ++c.launches;
+        k_ucompact<<<1, 1024, 0, st>>>(r.vec, d_rho_off + side * nsb, d_dims + side * nsb, d_ev_off + side * nsb,
+                                       base, nsb, r.order + base, ms, dk, doff, du);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(hkept[side], dk, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(hoff[side], doff, ms * sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (u_out[side])
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(hval[side], du, (size_t)ms * maxd * sizeof(double),
+                                            cudaMemcpyDeviceToHost, st));
+    }
+    if (any) NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+    for (int side = 0; side < 2; ++side) {
+        const int ms = hi[side];
+        if (kept_out[side])
+            for (int j = 0; j < ms; ++j) kept_out[side][j] = hkept[side][j];
+        if (!u_out[side]) continue;
+        double *U = u_out[side];
+        std::memset(U, 0, (size_t)mblk[side] * ms * sizeof(double));
+        for (int j = 0; j < ms; ++j) {
+            const int q = side * nsb + hkept[side][j], nq = dims[q];
+            const int *mp = maps.data() + map_off[q];
+            const double *src = hval[side] + hoff[side][j];
+            double *dst = U + (int64_t)j * mblk[side];
+            for (int p = 0; p < nq; ++p) dst[mp[p]] = src[p];
         }
     }
     cleanup();

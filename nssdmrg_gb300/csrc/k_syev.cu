@@ -165,16 +165,29 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         }
         __syncthreads();
         if (t == 0.0) continue;                      // uniform: t is shared
-        // p = t A v over the trailing block (symmetric reads of the lower triangle)
-        for (int i = warp; i < m; i += NW) {
-            const int r = k + 1 + i;
-            double acc = 0.0;
-            for (int j = lane; j < m; j += 32) {
-                const int c = k + 1 + j;
-                acc = fma(j <= i ? A[r * ld + c] : A[c * ld + r], v[j], acc);
+        // p = t A v over the trailing block (symmetric reads of the lower
+        // triangle): four threads per row, each with two accumulators, so the
+        // whole CTA streams FMAs instead of one warp reduction per row
+        for (int i0 = 0; i0 < m; i0 += TRD_THREADS / 4) {
+            const int i = i0 + (tid >> 2), qd = tid & 3;
+            double a0 = 0.0, a1 = 0.0;
+            if (i < m) {
+                const int r = k + 1 + i;
+                int j = qd;
+                for (; j + 4 < m; j += 8) {
+                    const int c0 = k + 1 + j, c1 = c0 + 4;
+                    a0 = fma(A[j <= i ? r * ld + c0 : c0 * ld + r], v[j], a0);
+                    a1 = fma(A[j + 4 <= i ? r * ld + c1 : c1 * ld + r], v[j + 4], a1);
+                }
+                if (j < m) {
+                    const int c0 = k + 1 + j;
+                    a0 = fma(A[j <= i ? r * ld + c0 : c0 * ld + r], v[j], a0);
+                }
             }
-            acc = wsum(acc);
-            if (lane == 0) w[i] = t * acc;
+            double acc = a0 + a1;
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            if (i < m && qd == 0) w[i] = t * acc;
         }
         __syncthreads();
         if (warp == 0) {
@@ -242,6 +255,33 @@ __device__ __forceinline__ int sturm_count(const double *a, const double *bb, in
     return cnt;
 }
 
+// The same count in FP32 (rescaled every 4 steps), for bracketing.
+__device__ __forceinline__ int sturm_count32(const float *a, const float *bb, int n, float s) {
+    float pm = 0.0f, pc = 1.0f;
+    int cnt = 0;
+    for (int i = 0; i < n; ++i) {
+        const float t = bb[i] * pm;
+        float pn = fmaf(a[i] - s, pc, -t);
+        int bn = __float_as_int(pn);
+        if ((bn << 1) == 0) {
+            pn = -pc * 0x1p-50f;
+            bn = __float_as_int(pn);
+        }
+        cnt += (int)((unsigned)(bn ^ __float_as_int(pc)) >> 31);
+        pm = pc;
+        pc = pn;
+        if ((i & 3) == 3) {
+            const int eb = max((__float_as_int(pm) >> 23) & 0xff, (__float_as_int(pc) >> 23) & 0xff);
+            if (eb > 0) {
+                const float f = __int_as_float((254 - eb) << 23);
+                pm *= f;
+                pc *= f;
+            }
+        }
+    }
+    return cnt;
+}
+
 // Eigenvalues BIS_EPC * chunk ... of one block.  items[b] = (block, first
 // eigenvalue index).  Writes evals (ascending, unscaled); the chunk-0 CTA
 // also writes the block's scale, sigma0 and L D L^T (scaled) and sets bit 0
@@ -298,32 +338,90 @@ __global__ void __launch_bounds__(BIS_THREADS)
     for (int i = tid; i < n; i += BIS_THREADS) sbb[i] = i > 0 ? sb[i - 1] * sb[i - 1] : 0.0;
     __syncthreads();
     if (warp < 4) {
-        const int g = lane >> 4, j = lane & 15;
-        const int k = k0 + warp * 2 + g;
-        const bool active = k < n && k < k0 + BIS_EPC;
-        // unreduced block [r0, r1) holding row k; the eigenvalue is its (k - r0)-th
+        // phase A, FP32: 16 shifts per eigenvalue, 5 rounds (~20 bits); two
+        // eigenvalues per warp.  Only brackets the eigenvalue: an FP32 count
+        // is exact for a matrix within ~2^-21 of the scaled T, so the bracket
+        // is widened by 2^-16 and checked with FP64 counts in phase B.
+        __shared__ float fa[SYEV_MAX], fbb[SYEV_MAX];
+        __shared__ double blo[BIS_EPC], bhi[BIS_EPC];
+        __shared__ int bk[BIS_EPC][3];               // r0, r1, exact (1 x 1 block)
+        for (int i = tid; i < n; i += 128) {
+            fa[i] = (float)sa[i];
+            fbb[i] = (float)sbb[i];
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        {
+            const int g = lane >> 4, j = lane & 15, e = warp * 2 + g;
+            const int k = k0 + e;
+            const bool active = k < n && e < BIS_EPC;
+            int r0 = 0, r1 = 0;
+            if (active) {                            // unreduced block [r0, r1) holding row k
+                r0 = k;
+                while (r0 > 0 && sb[r0 - 1] != 0.0) --r0;
+                r1 = k + 1;
+                while (r1 < n && sb[r1 - 1] != 0.0) ++r1;
+            }
+            const int kl = k - r0;
+            float lo = -1.0f, hi = 1.0f;
+            bool done = !active || r1 - r0 <= 1;
+            for (int round = 0; round < 5 && __any_sync(0xffffffffu, !done); ++round) {
+                const float h = (hi - lo) * (1.0f / 17.0f);
+                const int c = sturm_count32(fa + r0, fbb + r0, r1 - r0, lo + (float)(j + 1) * h);
+                const unsigned gm = (__ballot_sync(0xffffffffu, c > kl) >> (16 * g)) & 0xffffu;
+                if (!done) {
+                    if (gm == 0) {
+                        lo = lo + 16.0f * h;
+                    } else {
+                        const int jj = __ffs(gm) - 1;
+                        const float nh = lo + (float)(jj + 1) * h;
+                        if (jj > 0) lo = lo + (float)jj * h;
+                        hi = nh;
+                    }
+                }
+            }
+            if (active && j == 0) {
+                bk[e][0] = r0;
+                bk[e][1] = r1;
+                bk[e][2] = r1 - r0 == 1;
+                blo[e] = r1 - r0 == 1 ? sa[k] : fmax(-1.0, (double)lo - 0x1p-16);
+                bhi[e] = r1 - r0 == 1 ? sa[k] : fmin(1.0, (double)hi + 0x1p-16);
+            }
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (warp >= 2) return;
+        // phase B, FP64: 8 shifts per eigenvalue (~3.2 bits a round), four
+        // eigenvalues per warp; the first round checks the FP32 bracket
+        const int g = lane >> 3, j = lane & 7, e = warp * 4 + g;
+        const int k = k0 + e;
+        const bool active = k < n && e < BIS_EPC;
         int r0 = 0, r1 = 0;
+        double lo = -1.0, hi = 1.0;
+        bool done = !active;
         if (active) {
-            r0 = k;
-            while (r0 > 0 && sb[r0 - 1] != 0.0) --r0;
-            r1 = k + 1;
-            while (r1 < n && sb[r1 - 1] != 0.0) ++r1;
+            r0 = bk[e][0];
+            r1 = bk[e][1];
+            lo = blo[e];
+            hi = bhi[e];
+            done = bk[e][2] != 0;
         }
         const int kl = k - r0;
-        double lo = -1.0, hi = 1.0;
-        // a 1 x 1 unreduced block (the split-off noise rows of a rank-deficient
-        // block, mostly) is its own eigenvalue, exactly
-        bool done = !active || r1 - r0 == 1;
-        if (active && r1 - r0 == 1) lo = hi = sa[k];
+        {
+            const int c = sturm_count(sa + r0, sbb + r0, r1 - r0, j == 0 ? lo : hi);
+            const unsigned m8 = (__ballot_sync(0xffffffffu, c > kl) >> (8 * g)) & 0xffu;
+            // lane 0 of the group holds count(lo) > kl (bad), lane 1 count(hi) > kl (good)
+            if (!done && ((m8 & 1u) || !(m8 & 2u))) {
+                lo = -1.0;
+                hi = 1.0;
+            }
+        }
         for (int round = 0; round < 64 && __any_sync(0xffffffffu, !done); ++round) {
-            const double h = (hi - lo) * (1.0 / 17.0);
+            const double h = (hi - lo) * (1.0 / 9.0);
             const int c = sturm_count(sa + r0, sbb + r0, r1 - r0, lo + (double)(j + 1) * h);
-            const unsigned bal = __ballot_sync(0xffffffffu, c > kl);
-            const unsigned gm = (bal >> (16 * g)) & 0xffffu;
+            const unsigned gm = (__ballot_sync(0xffffffffu, c > kl) >> (8 * g)) & 0xffu;
             if (!done) {
                 const double wold = hi - lo;
                 if (gm == 0) {
-                    lo = lo + 16.0 * h;
+                    lo = lo + 8.0 * h;
                 } else {
                     const int jj = __ffs(gm) - 1;
                     const double nh = lo + (double)(jj + 1) * h;
@@ -357,72 +455,106 @@ __global__ void __launch_bounds__(BIS_THREADS)
     }
 }
 
-// One warp per kept eigenvalue j < ms of one side: order[j] + ev_base is its
-// position in the block-concatenated eigenvalue list, rank[pos] its rank
-// within the side.
-// Blocks of the library path (bmode != 0) already hold their vectors.  The
-// kept eigenvalues of one relative cluster are done by the warp of the
-// cluster's first kept member, in ascending order, each orthogonalised
-// against the ones before it.  Output: column col of the block's
-// column-major slot in vec.  Failure sets bit 1 of flags[q].
-constexpr int VEC_MAXCL = 16;
+// 1/x from the hardware approximation (rcp.approx.ftz.f64) refined by two
+// Newton-Raphson steps r <- r + r (1 - x r) (each squares the relative
+// error): ~1 ulp, in ~5 dependent FP64 operations where a correctly rounded
+// division costs ~650 cycles on this GPU.  Used in the dependent chains of
+// the qd transforms, whose error analysis needs only a small relative error
+// per operation.  x is normal and nonzero there (|x| >= PIVMIN).
+__device__ __forceinline__ double rcp_nr(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
 
-__global__ void __launch_bounds__(VEC_WARPS * 32)
-    k_vec(const int *__restrict__ order, const int *__restrict__ rank, int ev_base, int ms, int nblk,
-          const int *__restrict__ ev_off, const int *__restrict__ dims, const int64_t *__restrict__ rho_off,
-          const int *__restrict__ bmode, const int *__restrict__ sub, const double *__restrict__ evals,
-          const double *__restrict__ ldd, const double *__restrict__ ldl, const double *__restrict__ bscale,
-          const double *__restrict__ bsig, const double *__restrict__ tau, const double *__restrict__ refl,
-          const int *__restrict__ perm, int *__restrict__ flags, double *__restrict__ vec) {
+// Where a kept eigenvalue of one side lives: j < ms of side s maps to
+// position order[j] + ev_base of the block-concatenated eigenvalue list;
+// the side's block tables start at block o.
+struct VecSide {
+    const int *order;
+    int ev_base, ms, o;
+};
+
+struct VecArgs {
+    VecSide side[2];
+    int nsb;
+    const int *rank;             // rank within its side of every position
+    const int *ev_off, *dims, *bmode, *sub, *perm;
+    const int64_t *rho_off;
+    const double *evals, *ldd, *ldl, *bscale, *bsig, *tau, *refl;
+    int *flags;
+    double *vec;
+};
+
+// (q, col) of kept eigenvalue j of the concatenated left + right list
+__device__ __forceinline__ bool vec_locate(const VecArgs &a, int j, int &side, int &q, int &col) {
+    side = j < a.side[0].ms ? 0 : 1;
+    const int jj = side == 0 ? j : j - a.side[0].ms;
+    if (jj >= a.side[side].ms) return false;
+    const VecSide &sd = a.side[side];
+    const int pos = sd.order[jj] + sd.ev_base;
+    int k = 0;
+    while (k + 1 < a.nsb && a.ev_off[sd.o + k + 1] <= pos) ++k;
+    q = sd.o + k;
+    col = pos - a.ev_off[q];
+    return true;
+}
+
+// relative cluster [c0, c1] of column col within its unreduced block
+struct VecCluster {
+    int r0, r1, c0, c1;
+};
+
+__device__ __forceinline__ VecCluster vec_cluster(const VecArgs &a, int q, int col) {
+    const int eo = a.ev_off[q];
+    const double scale = a.bscale[q], sig0 = a.bsig[q];
+    const int sr = a.sub[eo + col];
+    VecCluster c{sr & 0xffff, sr >> 16, col, col};
+    auto lamS = [&](int x) { return a.evals[eo + x] * scale - sig0; };
+    auto linked = [&](int x) {
+        if (x + 1 >= c.r1) return false;
+        const double u = lamS(x), w = lamS(x + 1);
+        return w - u < RELGAP_MIN * fmax(u, w);
+    };
+    while (c.c0 > c.r0 && linked(c.c0 - 1)) --c.c0;
+    while (linked(c.c1)) ++c.c1;
+    return c;
+}
+
+// One warp per kept eigenvalue (both sides in one launch).  Blocks of the
+// library path (bmode != 0) already hold their vectors.  The vector is
+// written to column col of the block's column-major slot in vec, rows in the
+// block's own order; failure sets bit 1 of flags[q].
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec(VecArgs a) {
     __shared__ double sm[VEC_WARPS][7][SYEV_MAX];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = blockIdx.x * VEC_WARPS + warp;
-    if (j >= ms) return;
-    const int pos = order[j] + ev_base;
-    int q = 0;
-    while (q + 1 < nblk && ev_off[q + 1] <= pos) ++q;
-    const int n = dims[q], eo = ev_off[q], col = pos - eo;
-    if (bmode[q] != 0) return;
-    double *X = vec + rho_off[q];
+    int side, q, col;
+    if (!vec_locate(a, j, side, q, col)) return;
+    if (a.bmode[q] != 0) return;
+    const int n = a.dims[q], eo = a.ev_off[q];
+    double *X = a.vec + a.rho_off[q];
     if (n == 1) {
         if (lane == 0) X[0] = 1.0;
         return;
     }
-    const double scale = bscale[q], sig0 = bsig[q];
-    const int sr = sub[eo + col], r0 = sr & 0xffff, r1 = sr >> 16;
-    auto lamS = [&](int c) { return evals[eo + c] * scale - sig0; };
-    auto linked = [&](int c) {      // c and c + 1 in one relative cluster
-        if (c + 1 >= r1) return false;
-        const double x = lamS(c), y = lamS(c + 1);
-        return y - x < RELGAP_MIN * fmax(x, y);
-    };
-    auto kept = [&](int c) { return rank[eo + c] < ms; };
-    int c0 = col;
-    while (c0 > r0 && linked(c0 - 1)) --c0;
-    int c1 = col;
-    while (linked(c1)) ++c1;
-    for (int c = c0; c < col; ++c)
-        if (kept(c)) return;                         // an earlier kept member leads
     double *dD = sm[warp][0], *dL = sm[warp][1], *lp = sm[warp][2], *um = sm[warp][3], *ss = sm[warp][4],
            *pp = sm[warp][5], *z = sm[warp][6];
-    bool ok = (flags[q] & 1) == 0;
-    int nm = 0;
-    for (int c = col; c <= c1; ++c) nm += kept(c);
-    ok = ok && nm <= VEC_MAXCL;
-    for (int i = lane; i < n; i += 32) {
-        dD[i] = ldd[eo + i];
-        dL[i] = ldl[eo + i];
-    }
-    __syncwarp();
-    const double *Vq = refl + rho_off[q];
-    for (int c = col; ok && c <= c1; ++c) {
-        if (!kept(c)) continue;
-        const double lam0 = lamS(c);
-        const double gap = fmin(c > r0 ? lam0 - lamS(c - 1) : INFINITY, c + 1 < r1 ? lamS(c + 1) - lam0 : INFINITY);
-        if (!(gap > 32.0 * 0x1p-52)) {
-            ok = false;
-            break;
+    const double scale = a.bscale[q], sig0 = a.bsig[q];
+    const int sr = a.sub[eo + col], r0 = sr & 0xffff, r1 = sr >> 16;
+    auto lamS = [&](int c) { return a.evals[eo + c] * scale - sig0; };
+    const double lam0 = lamS(col);
+    const double gap = fmin(col > r0 ? lam0 - lamS(col - 1) : INFINITY, col + 1 < r1 ? lamS(col + 1) - lam0 : INFINITY);
+    bool ok = (a.flags[q] & 1) == 0 && gap > 32.0 * 0x1p-52;
+    if (ok) {
+        for (int i = lane; i < n; i += 32) {
+            dD[i] = a.ldd[eo + i];
+            dL[i] = a.ldl[eo + i];
         }
+        __syncwarp();
         double lam = lam0, ztz = 1.0;
         bool conv = false;
         for (int itr = 0; itr < 8; ++itr) {
@@ -432,7 +564,7 @@ __global__ void __launch_bounds__(VEC_WARPS * 32)
                     ss[i] = s;
                     double dp = dD[i] + s;
                     if (fabs(dp) < PIVMIN) dp = -PIVMIN;
-                    const double l = dD[i] * dL[i] / dp;
+                    const double l = dD[i] * dL[i] * rcp_nr(dp);
                     lp[i] = l;
                     s = l * dL[i] * s - lam;
                 }
@@ -443,7 +575,7 @@ __global__ void __launch_bounds__(VEC_WARPS * 32)
                     pp[i + 1] = p;
                     double dm = dD[i] * dL[i] * dL[i] + p;
                     if (fabs(dm) < PIVMIN) dm = -PIVMIN;
-                    const double t = dD[i] / dm;
+                    const double t = dD[i] * rcp_nr(dm);
                     um[i] = dL[i] * t;
                     p = p * t - lam;
                 }
@@ -501,47 +633,79 @@ __global__ void __launch_bounds__(VEC_WARPS * 32)
             if (!(fabs(lam - lam0) <= 0.25 * gap)) break;
             __syncwarp();
         }
-        if (!conv) {
-            ok = false;
-            break;
-        }
-        const double inv = 1.0 / sqrt(ztz);
-        for (int k = lane; k < n; k += 32) z[k] *= inv;
-        __syncwarp();
-        // x = H_0 H_1 ... H_{n-3} z
-        for (int k = n - 3; k >= 0; --k) {
-            const double t = tau[eo + k];
-            if (t == 0.0) continue;
-            const double *vk = Vq + (int64_t)k * n;
-            double d = 0.0;
-            for (int i = k + 1 + lane; i < n; i += 32) d = fma(vk[i], z[i], d);
-            d = t * wsum(d);
-            for (int i = k + 1 + lane; i < n; i += 32) z[i] = fma(-d, vk[i], z[i]);
+        ok = conv;
+        if (ok) {
+            const double inv = 1.0 / sqrt(ztz);
+            for (int k = lane; k < n; k += 32) z[k] *= inv;
             __syncwarp();
+            // x = H_0 H_1 ... H_{n-3} z
+            const double *Vq = a.refl + a.rho_off[q];
+            for (int k = n - 3; k >= 0; --k) {
+                const double t = a.tau[eo + k];
+                if (t == 0.0) continue;
+                const double *vk = Vq + (int64_t)k * n;
+                double d = 0.0;
+                for (int i = k + 1 + lane; i < n; i += 32) d = fma(vk[i], z[i], d);
+                d = t * wsum(d);
+                for (int i = k + 1 + lane; i < n; i += 32) z[i] = fma(-d, vk[i], z[i]);
+                __syncwarp();
+            }
+            double *Xc = X + (int64_t)col * n;
+            for (int i = lane; i < n; i += 32) Xc[a.perm[eo + i]] = z[i];
         }
-        // Gram-Schmidt against the cluster's kept vectors done before (rows
-        // of X in the block's own order: row perm[i] holds z[i])
+    }
+    if (!ok && lane == 0) atomicOr(&a.flags[q], 2);
+}
+
+// Gram-Schmidt within relative clusters of kept eigenvalues: each member's
+// twisted vector lies in the cluster's invariant subspace up to
+// eps / (gap to the rest), so orthogonalising the cluster's kept vectors in
+// ascending order gives an orthonormal basis of it.  One warp per kept
+// eigenvalue; the warp of the first kept member does the cluster.
+constexpr int VEC_MAXCL = 16;
+
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_gs(VecArgs a) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * VEC_WARPS + warp;
+    int side, q, col;
+    if (!vec_locate(a, j, side, q, col)) return;
+    if (a.bmode[q] != 0 || (a.flags[q] & 2)) return;
+    const int n = a.dims[q], eo = a.ev_off[q];
+    if (n == 1) return;
+    const int ms = a.side[side].ms;
+    auto kept = [&](int c) { return a.rank[eo + c] < ms; };
+    const VecCluster cl = vec_cluster(a, q, col);
+    for (int c = cl.c0; c < col; ++c)
+        if (kept(c)) return;                         // an earlier kept member leads
+    int nm = 0;
+    for (int c = col; c <= cl.c1; ++c) nm += kept(c);
+    if (nm < 2) return;
+    bool ok = nm <= VEC_MAXCL;
+    double *X = a.vec + a.rho_off[q];
+    for (int c = col + 1; ok && c <= cl.c1; ++c) {
+        if (!kept(c)) continue;
+        double *Z = X + (int64_t)c * n;
         for (int cp = col; cp < c; ++cp) {
             if (!kept(cp)) continue;
             const double *Y = X + (int64_t)cp * n;
             double d = 0.0;
-            for (int i = lane; i < n; i += 32) d = fma(Y[perm[eo + i]], z[i], d);
+            for (int i = lane; i < n; i += 32) d = fma(Y[i], Z[i], d);
             d = wsum(d);
-            for (int i = lane; i < n; i += 32) z[i] = fma(-d, Y[perm[eo + i]], z[i]);
+            for (int i = lane; i < n; i += 32) Z[i] = fma(-d, Y[i], Z[i]);
             __syncwarp();
         }
         double nz = 0.0;
-        for (int i = lane; i < n; i += 32) nz = fma(z[i], z[i], nz);
+        for (int i = lane; i < n; i += 32) nz = fma(Z[i], Z[i], nz);
         nz = sqrt(wsum(nz));
         if (!(nz >= 0.5)) {
             ok = false;
             break;
         }
-        double *Xc = X + (int64_t)c * n;
-        for (int i = lane; i < n; i += 32) Xc[perm[eo + i]] = z[i] / nz;
+        const double inv = 1.0 / nz;
+        for (int i = lane; i < n; i += 32) Z[i] *= inv;
         __syncwarp();
     }
-    if (!ok && lane == 0) atomicOr(&flags[q], 2);
+    if (!ok && lane == 0) atomicOr(&a.flags[q], 2);
 }
 
 }  // namespace
@@ -565,14 +729,35 @@ int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitem
     return (int)cudaGetLastError();
 }
 
-int syev_vec(const int *order, const int *rank, int ev_base, int ms, int nblk, const int *ev_off, const int *dims,
-             const int64_t *rho_off, const int *bmode, const int *sub, const double *evals, const double *ldd,
-             const double *ldl, const double *bscale, const double *bsig, const double *tau, const double *refl,
-             const int *perm, int *flags, double *vec, cudaStream_t st) {
-    if (ms <= 0) return 0;
-    k_vec<<<(ms + VEC_WARPS - 1) / VEC_WARPS, VEC_WARPS * 32, 0, st>>>(order, rank, ev_base, ms, nblk, ev_off,
-                                                                        dims, rho_off, bmode, sub, evals, ldd, ldl,
-                                                                        bscale, bsig, tau, refl, perm, flags, vec);
+int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
+             const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
+             const double *ldd, const double *ldl, const double *bscale, const double *bsig, const double *tau,
+             const double *refl, const int *perm, int *flags, double *vec, cudaStream_t st) {
+    VecArgs a;
+    a.side[0] = VecSide{order, 0, ms[0], 0};
+    a.side[1] = VecSide{order + nl, nl, ms[1], nsb};
+    a.nsb = nsb;
+    a.rank = rank;
+    a.ev_off = ev_off;
+    a.dims = dims;
+    a.bmode = bmode;
+    a.sub = sub;
+    a.perm = perm;
+    a.rho_off = rho_off;
+    a.evals = evals;
+    a.ldd = ldd;
+    a.ldl = ldl;
+    a.bscale = bscale;
+    a.bsig = bsig;
+    a.tau = tau;
+    a.refl = refl;
+    a.flags = flags;
+    a.vec = vec;
+    const int tot = ms[0] + ms[1];
+    if (tot <= 0) return 0;
+    const int grid = (tot + VEC_WARPS - 1) / VEC_WARPS;
+    k_vec<<<grid, VEC_WARPS * 32, 0, st>>>(a);
+    k_vec_gs<<<grid, VEC_WARPS * 32, 0, st>>>(a);
     return (int)cudaGetLastError();
 }
 
