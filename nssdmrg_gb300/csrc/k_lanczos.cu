@@ -83,7 +83,7 @@ constexpr int ORTH_WARPS = ORTH_THREADS / 32;
 constexpr uint32_t BAR_SPIN = 1u << 22;   // grid-barrier poll limit (~2 s of L2 round trips)
 
 // device scalar slots (Ctx::lz.scal)
-enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NSCAL = 4 };
+enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NRM = 3, S_NSCAL = 4 };
 // device flag slots (Ctx::lz.flags); the host-mapped mirror uses the same
 // indices and one more word, F_NFLAGS, for the host's stop request
 enum { F_STOP = 0, F_PASS2 = 1, F_M = 2, F_CONV = 3, F_BREAK = 4, F_HOST = 5, F_ERR = 6, F_NFLAGS = 8 };
@@ -121,6 +121,22 @@ __device__ __forceinline__ bool last_block(unsigned *counter) {
     __syncthreads();
     if (last) __threadfence();
     return last != 0;
+}
+
+// Sum of the G per-CTA partials, by every thread of the last CTA (256
+// threads): a serial loop over ~300 FP64 adds would cost ~20k cycles of
+// dependent 64-cycle latency on this GPU.
+__device__ __forceinline__ double lastblock_sum(const double *part, int G) {
+    __shared__ double red_lb[8];
+    double p = 0.0;
+    for (int b = threadIdx.x; b < G; b += blockDim.x) p += part[b];
+    p = warp_sum<double>(p);
+    if ((threadIdx.x & 31) == 0) red_lb[threadIdx.x >> 5] = p;
+    __syncthreads();
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red_lb[q];
+    __syncthreads();
+    return t;
 }
 
 // Restart path only (a fresh start vector orthogonalised against the basis):
@@ -214,9 +230,9 @@ __global__ void __launch_bounds__(256) k_update(const T *__restrict__ V, int m, 
         for (int q = 0; q < 8; ++q) t += red[q];
         part[blockIdx.x] = t;
     }
-    if (!last_block(counter) || tid != 0) return;
-    double bb = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) bb += part[b];
+    if (!last_block(counter)) return;
+    const double bb = lastblock_sum(part, gridDim.x);
+    if (tid != 0) return;
     const int j = m - 1;
     if (!pass2) {
         alpha[j] = scal[S_ALPHA] + h[j];
@@ -229,20 +245,38 @@ __global__ void __launch_bounds__(256) k_update(const T *__restrict__ V, int m, 
     *counter = 0u;
 }
 
-// x <- x / ||x|| (one CTA per launch is enough for start vectors);
-// blockDim.x <= 1024, so at most 32 warp partial sums
+// x <- x / ||x|| over the whole GPU: k_sumsq (FP64 partial sums, the last
+// CTA writes 1 / ||x||), then k_scale.
 template <class T>
-__global__ void __launch_bounds__(1024) k_normalize(T *x, int64_t n) {
-    __shared__ double red[32];
-    double ss = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ss += (double)x[i] * (double)x[i];
-    ss = warp_sum<double>(ss);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+__global__ void __launch_bounds__(256) k_sumsq(const T *__restrict__ x, int64_t n, double *__restrict__ part,
+                                               double *__restrict__ inv, unsigned *counter) {
+    const int tid = threadIdx.x;
+    double a = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = (double)x[i];
+        a = fma(v, v, a);
+    }
+    a = warp_sum<double>(a);
+    __shared__ double red[8];
+    if ((tid & 31) == 0) red[tid >> 5] = a;
     __syncthreads();
-    double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
-    const double inv = 1.0 / sqrt(t);
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = (T)((double)x[i] * inv);
+    if (tid == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += red[q];
+        part[blockIdx.x] = t;
+    }
+    if (!last_block(counter)) return;
+    const double t = lastblock_sum(part, gridDim.x);
+    if (tid != 0) return;
+    *inv = 1.0 / sqrt(t);
+    *counter = 0u;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_scale(T *__restrict__ x, int64_t n, const double *__restrict__ inv) {
+    const double f = *inv;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = (T)((double)x[i] * f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1209,10 +1243,9 @@ __global__ void __launch_bounds__(256) k_rq(const double *__restrict__ psi, cons
         part[(int64_t)tid * gridDim.x + blockIdx.x] = t;
     }
     if (!last_block(counter)) return;
-    if (tid < 3) {
-        double t = 0.0;
-        for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[(int64_t)tid * gridDim.x + bb];
-        r[tid] = t;
+    for (int q = 0; q < 3; ++q) {
+        const double t = lastblock_sum(part + (int64_t)q * gridDim.x, gridDim.x);
+        if (tid == 0) r[q] = t;
     }
     if (tid == 0) *counter = 0u;
 }
@@ -1236,9 +1269,9 @@ __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ psi, c
         for (int q = 0; q < 8; ++q) t += red[q];
         part[blockIdx.x] = t;
     }
-    if (!last_block(counter) || tid != 0) return;
-    double t = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[bb];
+    if (!last_block(counter)) return;
+    const double t = lastblock_sum(part, gridDim.x);
+    if (tid != 0) return;
     r[3] = t;
     *counter = 0u;
 }
@@ -1264,9 +1297,9 @@ __global__ void __launch_bounds__(256) k_anchor_r(const double *__restrict__ psi
         for (int q = 0; q < 8; ++q) t += red[q];
         part[blockIdx.x] = t;
     }
-    if (!last_block(counter) || tid != 0) return;
-    double t = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb) t += part[bb];
+    if (!last_block(counter)) return;
+    const double t = lastblock_sum(part, gridDim.x);
+    if (tid != 0) return;
     r[4] = t;
     *counter = 0u;
 }
@@ -1275,6 +1308,14 @@ __global__ void __launch_bounds__(256) k_anchor_r(const double *__restrict__ psi
 __global__ void k_to32(float *__restrict__ out, const double *__restrict__ x, double s, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (float)(x[i] * s);
+}
+
+// x <- x / ||x|| on stream st (two launches)
+template <class T>
+void normalize_dev(DevLanczos &z, T *x, int64_t n, cudaStream_t st, int64_t &launches) {
+    k_sumsq<T><<<NBLK, 256, 0, st>>>(x, n, z.part, z.scal + S_NRM, z.counter);
+    k_scale<T><<<NBLK, 256, 0, st>>>(x, n, z.scal + S_NRM);
+    launches += 1;   // the caller counted one launch for the normalisation
 }
 
 // per-eigenvector scratch row of svec
@@ -1413,7 +1454,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         ++c.launches;
         k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
         ++c.launches;
-        k_normalize<T><<<1, 1024, 0, st>>>(V, n);
+        normalize_dev<T>(z, V, n, st, c.launches);
     }
     const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
     const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
@@ -1575,7 +1616,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
                                                          rs_alpha, rs_beta, 0);
             }
             ++c.launches;
-            k_normalize<T><<<1, 1024, 0, st>>>(vn, n);
+            normalize_dev<T>(z, vn, n, st, c.launches);
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.beta + (m_done - 1), 0, sizeof(double), st));
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
             NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
@@ -1631,7 +1672,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         NSS_CUDA_TRY(c, cudaMemcpyAsync(z.svec, cvec.data(), cvec.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         c.launches += 2;
         k_ritz_anchor<T><<<NBLK, 256, cvec.size() * sizeof(double), st>>>(V, m_done, n, z.svec, anc->u, anc->out);
-        k_normalize<double><<<1, 1024, 0, st>>>(anc->out, n);
+        normalize_dev<double>(z, anc->out, n, st, c.launches);
         NSS_CUDA_TRY(c, cudaGetLastError());
         NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
         z.last_anchor_theta = theta[0];
@@ -1646,7 +1687,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     k_ritz<T><<<NBLK, 256, (size_t)ne * m_done * sizeof(double), st>>>(V, m_done, n, z.svec, m_done, ne, z.evecs);
     for (int e = 0; e < ne; ++e) {
         ++c.launches;
-        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs + (int64_t)e * n, n);
+        normalize_dev<double>(z, z.evecs + (int64_t)e * n, n, st, c.launches);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());
     // the pageable sources above are consumed before this returns
@@ -1729,7 +1770,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             if (e > 0) {
                 if ((rc = deflate(u, e))) break;
                 ++c.launches;
-                k_normalize<double><<<1, 1024, 0, st>>>(u, n);
+                normalize_dev<double>(z, u, n, st, c.launches);
             }
             if ((rc = hv_device(c, u, z.w))) break;
             ++numop_;
@@ -1931,7 +1972,7 @@ int engine_add(BatchEngine &E, Ctx &c, uint64_t seed, int nitermax, double tol, 
     cudaStream_t st = c0.stream;
     c0.launches += 2;
     k_random<float><<<608, 256, 0, st>>>(z.V32, B.n, B.seed, 0);
-    k_normalize<float><<<1, 1024, 0, st>>>(z.V32, B.n);
+    normalize_dev<float>(z, z.V32, B.n, st, c0.launches);
     NSS_CUDA_TRY(c0, cudaGetLastError());
     if (id) *id = B.id;
     E.solves.push_back(std::move(B));
@@ -2112,7 +2153,7 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
                     k_update<float><<<NBLK, 256, upd_smem, st>>>(z.V32, m, vn, B.n, h1, z.part, z.scal, z.counter,
                                                                  z.flags, rs_alpha, rs_beta, 0);
                 }
-                k_normalize<float><<<1, 1024, 0, st>>>(vn, B.n);
+                normalize_dev<float>(z, vn, B.n, st, c0.launches);
                 NSS_CUDA_TRY(c0, cudaMemsetAsync(z.beta + (m - 1), 0, sizeof(double), st));
                 NSS_CUDA_TRY(c0, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
                 z.h_ab[(z.cap + 1) + m - 1] = 0.0;
@@ -2159,7 +2200,7 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
         NSS_CUDA_TRY(c0, cudaMemcpyAsync(z.svec, B.svec.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st));
         c0.launches += 2;
         k_ritz<float><<<NBLK, 256, (size_t)m * sizeof(double), st>>>(z.V32, m, B.n, z.svec, m, 1, z.evecs);
-        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+        normalize_dev<double>(z, z.evecs, B.n, st, c0.launches);
         if ((rc = fp64_energy(B, b, true))) return rc;
     }
     for (int b : p2) {
@@ -2170,7 +2211,7 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
         c0.launches += 2;
         k_ritz_anchor<float><<<NBLK, 256, B.cvec.size() * sizeof(double), st>>>(z.V32, B.m_done, B.n, z.svec, z.evecs,
                                                                                 z.evecs);
-        k_normalize<double><<<1, 1024, 0, st>>>(z.evecs, B.n);
+        normalize_dev<double>(z, z.evecs, B.n, st, c0.launches);
         if ((rc = fp64_energy(B, b, false))) return rc;
     }
     for (int b : p3)
