@@ -137,6 +137,9 @@ typedef struct {
     int32_t m_s;           /* kept states after the degeneracy extension */
     double  trunc_err;     /* 1 - sum(lambda(1:m_s)) */
     double  entropy;       /* -sum lambda log(lambda + 1e-32) */
+    double  s_number;      /* S_N = -sum_q P_q log(P_q + 1e-32), P_q = sum of block q's lambda */
+    double  s_config;      /* S_c = -sum_q P_q S_q, S_q = sum_i (l_i/P_q) log(l_i/P_q + 1e-32)
+                              (write_entanglement, src/DMRG_MAIN.f90:523-561) */
 } nss_rdm_side;
 
 /* Batched ground states: nb independent superblocks, one context each (all
@@ -311,6 +314,7 @@ typedef struct {
     int64_t nnz_ops;        /* nonzeros of the renormalised block operators */
     int32_t rdm_own_blocks;     /* rho blocks on the own eigensolver ... */
     int32_t rdm_fallback_blocks;/* ... and those whose kept vectors the library recomputed */
+    double  sn_left, sc_left, sn_right, sc_right;   /* S_N, S_c per side (SN_ScVSblock.length) */
 } nss_step_record;
 
 typedef struct nss_dmrg nss_dmrg;

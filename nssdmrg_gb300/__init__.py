@@ -63,7 +63,8 @@ class SbDesc(C.Structure):
 
 
 class RdmSide(C.Structure):
-    _fields_ = [("nevals", C.c_int32), ("m_s", C.c_int32), ("trunc_err", C.c_double), ("entropy", C.c_double)]
+    _fields_ = [("nevals", C.c_int32), ("m_s", C.c_int32), ("trunc_err", C.c_double), ("entropy", C.c_double),
+                ("s_number", C.c_double), ("s_config", C.c_double)]
 
 
 class BlockDesc(C.Structure):
@@ -87,7 +88,8 @@ class StepRecord(C.Structure):
                 ("m_right", C.c_int32), ("ms_solve", C.c_double), ("ms_eigh", C.c_double),
                 ("ms_step", C.c_double), ("ms_build", C.c_double), ("ms_renorm", C.c_double),
                 ("nnz_u", C.c_int64), ("nnz_ops", C.c_int64), ("rdm_own_blocks", C.c_int32),
-                ("rdm_fallback_blocks", C.c_int32)]
+                ("rdm_fallback_blocks", C.c_int32), ("sn_left", C.c_double), ("sc_left", C.c_double),
+                ("sn_right", C.c_double), ("sc_right", C.c_double)]
 
 
 _lib = None
@@ -292,6 +294,8 @@ class RdmResult:
     lambdas: tuple       # descending eigenvalues, left and right
     kept_blocks: tuple   # rho block (= sector) of each kept state
     u: tuple             # rotation matrices [m_block x m_s]
+    s_number: tuple = (0.0, 0.0)   # S_N per side (number entropy over QN blocks)
+    s_config: tuple = (0.0, 0.0)   # S_c per side (configurational entropy)
 
 
 class Superblock:
@@ -500,7 +504,8 @@ class Superblock:
         if want_u:
             us = (ul[: ml * ms[0]].reshape(ms[0], ml).T, ur[: mr * ms[1]].reshape(ms[1], mr).T)
         return RdmResult(ms, (out[0].trunc_err, out[1].trunc_err), (out[0].entropy, out[1].entropy),
-                         (lam_l[: out[0].nevals], lam_r[: out[1].nevals]), (kl[: ms[0]], kr[: ms[1]]), us)
+                         (lam_l[: out[0].nevals], lam_r[: out[1].nevals]), (kl[: ms[0]], kr[: ms[1]]), us,
+                         (out[0].s_number, out[1].s_number), (out[0].s_config, out[1].s_config))
 
 
 class DMRG:

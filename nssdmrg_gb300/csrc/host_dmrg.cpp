@@ -380,6 +380,10 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     for (int e = 0; e < 2; ++e) rec.energy[e] = (e < neigen) ? ev[e] / rec.current_l : 0.0;
     rec.entropy_left = side[0].entropy;
     rec.entropy_right = side[1].entropy;
+    rec.sn_left = side[0].s_number;
+    rec.sc_left = side[0].s_config;
+    rec.sn_right = side[1].s_number;
+    rec.sc_right = side[1].s_config;
     rec.m_left = left.dim;
     rec.m_right = right.dim;
     if (renorm) {

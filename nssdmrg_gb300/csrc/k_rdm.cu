@@ -35,6 +35,11 @@ namespace {
 
 constexpr int RT = 16;
 
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 struct RhoItem {     // one 16x16 tile of one rho block
     int side, k, r0, c0;
 };
@@ -177,6 +182,46 @@ __global__ void __launch_bounds__(1024) k_truncate(const double *sorted, int n, 
         out_d[0] = 1.0 - a;
         out_d[1] = b;
         out_i[0] = msf;
+    }
+}
+
+// write_entanglement's S_N and S_c (src/DMRG_MAIN.f90:523-561), one CTA per
+// side over its rho blocks (the tiny-clamped eigenvalues of each block):
+// P_q = sum lambda, S_q = sum (lambda/P_q) log(lambda/P_q + 1e-32),
+// S_N = -sum_q P_q log(P_q + 1e-32), S_c = -sum_q P_q S_q.  out[2 side] =
+// S_N, out[2 side + 1] = S_c.
+__global__ void __launch_bounds__(256) k_qn_entropy(const double *__restrict__ evals, const int *__restrict__ ev_off,
+                                                    int nsb, double *__restrict__ out) {
+    __shared__ double red[2][8];
+    const int side = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double sn = 0.0, sc = 0.0;
+    for (int k = warp; k < nsb; k += 8) {
+        const int b0 = ev_off[side * nsb + k], b1 = ev_off[side * nsb + k + 1];
+        double p = 0.0;
+        for (int i = b0 + lane; i < b1; i += 32) p += evals[i];
+        p = warp_sum_d(p);
+        double sq = 0.0;
+        for (int i = b0 + lane; i < b1; i += 32) {
+            const double o = evals[i] / p;
+            sq += o * log(o + 1e-32);
+        }
+        sq = warp_sum_d(sq);
+        sn -= p * log(p + 1e-32);
+        sc -= p * sq;
+    }
+    if (lane == 0) {
+        red[0][warp] = sn;
+        red[1][warp] = sc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            a += red[0][w];
+            b += red[1][w];
+        }
+        out[2 * side] = a;
+        out[2 * side + 1] = b;
     }
 }
 
@@ -741,6 +786,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     c.rdm_fallback_blocks = 0;
     ++c.launches;
     k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
+    ++c.launches;
+    k_qn_entropy<<<2, 256, 0, st>>>(r.evals, d_ev_off, nsb, r.scal + 4);
     // per side: rank, truncation, U
     const int nside[2] = {nl, nr};
     for (int side = 0; side < 2; ++side) {
@@ -753,9 +800,9 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
                                      r.iscal + side);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());
-    double hs[4];
+    double hs[8];
     int hi[8];
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(hs, r.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(hs, r.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
     NSS_CUDA_TRY(c, cudaMemcpyAsync(hi, r.iscal, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
     NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
     if (hi[7]) {
@@ -772,6 +819,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         out[side].m_s = hi[side];
         out[side].trunc_err = hs[2 * side];
         out[side].entropy = hs[2 * side + 1];
+        out[side].s_number = hs[4 + 2 * side];
+        out[side].s_config = hs[4 + 2 * side + 1];
         if (lam_out[side]) {
             // lambda clipped at 0 (DMRG_RDM.f90:88,97): tiny stays as is, as the
             // reference clips only negative values after the tiny substitution

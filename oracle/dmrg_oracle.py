@@ -633,6 +633,22 @@ def entropy(lam: np.ndarray) -> float:
     return float(-np.sum(lam * np.log(lam + 1e-32)))
 
 
+def qn_entropies(rho: RhoBlocks) -> tuple[float, float]:
+    """write_entanglement (src/DMRG_MAIN.f90:523-561): the entropy split over
+    the QN blocks of rho, P_q = sum of block q's (tiny-clamped) eigenvalues,
+    S_q = sum_i (l_i/P_q) log(l_i/P_q + 1e-32); returns
+    S_N = -sum_q P_q log(P_q + 1e-32) and S_c = -sum_q P_q S_q."""
+    sn = sc = 0.0
+    for e in rho.evals:
+        p = float(np.sum(e))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            o = e / p
+            sq = float(np.sum(o * np.log(o + 1e-32)))
+        sn -= p * np.log(p + 1e-32)
+        sc -= p * sq
+    return float(sn), float(sc)
+
+
 # ----------------------------------------------------------------------------
 # DMRG driver (src/DMRG_MAIN.f90)
 # ----------------------------------------------------------------------------

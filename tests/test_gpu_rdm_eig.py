@@ -157,3 +157,24 @@ def test_own_eigensolver_rank_deficient_blocks_fall_back(nss):
         assert np.abs(u.T @ u - np.eye(u.shape[1])).max() <= 1e-12
         np.testing.assert_allclose(own.lambdas[side], lib.lambdas[side], rtol=0, atol=1e-13)
         assert own.m_s[side] == lib.m_s[side]
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_qn_entropy_split_matches_oracle(nss, name):
+    """S_N and S_c (write_entanglement, src/DMRG_MAIN.f90:523-561) from the
+    device eigenvalues against the oracle's restatement on numpy's
+    eigenvalues of the same blocks, at the entropy's 1e-11 relative."""
+    from oracle import dmrg_oracle as O
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    mst = int(z["params"][1]) if "params" in z else 128
+    res = s.sb_get_rdm(mst, 0.1, psi=z["psi"], want_u=False)
+    blocks = _blocks_of(z["psi"], z["sb_dls"], z["sb_drs"], z["sb_offset"])
+    for side in (0, 1):
+        rho = O.eigh_blocks([((k,), np.arange(b.shape[0]), b) for k, b in enumerate(blocks[side])])
+        sn, sc = O.qn_entropies(rho)
+        assert abs(res.s_number[side] - sn) <= 1e-11 * abs(sn) + 1e-14, (side, res.s_number[side], sn)
+        assert abs(res.s_config[side] - sc) <= 1e-11 * abs(sc) + 1e-14, (side, res.s_config[side], sc)
+        assert abs(res.s_number[side] + res.s_config[side] - res.entropy[side]) <= 1e-12

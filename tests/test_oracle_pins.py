@@ -186,3 +186,23 @@ def test_electron_site_signs():
     assert np.allclose(cd @ cd.T + cd.T @ cd, np.eye(4))
     assert np.allclose(p, np.diag([1, -1, -1, 1]))
     assert np.allclose(np.diag(s.op("H").toarray()), [0, 0, 0, 4.0])
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+def test_qn_entropy_split_adds_up(name):
+    """write_entanglement's S_N + S_c equals the von Neumann entropy of the
+    same blocks (an identity of the restatement, src/DMRG_MAIN.f90:510-561),
+    and a single block has S_N = 0."""
+    z = load_npz(name)
+    psi, dls, drs, off = z["psi"], z["sb_dls"], z["sb_drs"], z["sb_offset"]
+    blocks = []
+    for k in range(len(dls)):
+        w = psi[off[k]:off[k] + dls[k] * drs[k]].reshape(dls[k], drs[k])
+        blocks.append(((k,), np.arange(dls[k]), w @ w.T))
+    rho = O.eigh_blocks(blocks)
+    sn, sc = O.qn_entropies(rho)
+    s = O.entropy(rho.evalues)
+    assert abs((sn + sc) - s) <= 1e-12 * max(1.0, abs(s))
+    one = O.eigh_blocks([((0,), np.arange(4), np.diag([0.5, 0.3, 0.2, 0.0]))])
+    sn1, sc1 = O.qn_entropies(one)
+    assert abs(sn1) < 1e-15 and abs(sc1 - O.entropy(one.evalues)) < 1e-15
