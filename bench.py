@@ -51,7 +51,9 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="headline path; the other one is timed alongside for comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurement")
+    ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurements")
+    ap.add_argument("--large-sweeps", type=int, default=1,
+                    help="finite sweeps timed on the spin-1 L=64 m=512 chain (0 skips it)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--profile", action="store_true",
@@ -183,33 +185,41 @@ CHECK_ITERS = 4       # iterations per launch of the persistent kernel (the libr
 SWEEP_CASE = {"workload": "heisenberg_half_L20_M64_3sweeps", "model": "heisenberg_half", "L": 20, "ldmrg": 10,
               "mdmrg": 64, "msweep": [64, 64, 64], "lanc_tolerance": 1e-12, "lanc_niter": 200}
 
+# the third configuration: spin-1 chain L=64, m=512 (4 sweeps in the
+# configuration; `--large-sweeps` sets how many are timed, default 1)
+SWEEP_CASE_LARGE = {"workload": "heisenberg_one_L64_M512", "model": "heisenberg_one", "L": 64, "ldmrg": 32,
+                    "mdmrg": 512, "lanc_tolerance": 1e-12, "lanc_niter": 200}
 
-def measure_sweeps(nss, device):
-    """Finite-algorithm throughput on the spin-1/2 Heisenberg chain L=20,
-    M=64, three sweeps (the first benchmark configuration): sweeps/s of the
-    finite part (total time minus the infinite growth, each timed on its own
-    run), for both precisions, and |dE| of the final energies."""
-    out = {"config": SWEEP_CASE}
+
+def measure_sweeps(nss, device, case=None, warm=True):
+    """Finite-algorithm throughput: sweeps/s of the finite part (total time
+    minus the infinite growth, each timed on its own run), for both
+    precisions, and |dE| of the final energies.  Default case: the spin-1/2
+    Heisenberg chain L=20, M=64, three sweeps (the first benchmark
+    configuration)."""
+    case = case or SWEEP_CASE
+    out = {"config": case}
     res = {}
+    model = nss.MODEL_HEISENBERG_ONE if case["model"] == "heisenberg_one" else nss.MODEL_HEISENBERG_HALF
     for name, prec in (("mixed", nss.NSS_PREC_MIXED), ("fp64", nss.NSS_PREC_FP64)):
         def make():
-            return nss.DMRG(nss.MODEL_HEISENBERG_HALF, SWEEP_CASE["ldmrg"], SWEEP_CASE["mdmrg"],
-                            msweep=SWEEP_CASE["msweep"], dmrg_qn=(0.0,), lanc_neigen=1,
-                            lanc_niter=SWEEP_CASE["lanc_niter"], lanc_tolerance=SWEEP_CASE["lanc_tolerance"],
+            return nss.DMRG(model, case["ldmrg"], case["mdmrg"],
+                            msweep=case["msweep"], dmrg_qn=(0.0,), lanc_neigen=1,
+                            lanc_niter=case["lanc_niter"], lanc_tolerance=case["lanc_tolerance"],
                             precision=prec, device=device)
-        make().finite()                      # warm-up (allocations, first-touch)
-        t0 = time.perf_counter()
-        d_inf = make()
-        d_inf.infinite()
-        t_inf = time.perf_counter() - t0
+        if warm:
+            make().finite()                  # warm-up (allocations, first-touch)
         t0 = time.perf_counter()
         d = make()
         recs = d.finite()
         t_all = time.perf_counter() - t0
-        t_sw = max(t_all - t_inf, 1e-9)
-        nsw = len(SWEEP_CASE["msweep"])
+        # the finite part: host wall time of its steps (block build, upload,
+        # solve, RDM, renormalisation), as the driver records them
         fin = [r for r in recs if r["type"] != 0]
-        res[name] = {"sweeps_per_s": nsw / t_sw, "s_total": t_all, "s_infinite": t_inf,
+        t_sw = max(sum(r["ms_step"] for r in fin) / 1e3, 1e-9)
+        t_inf = sum(r["ms_step"] for r in recs if r["type"] == 0) / 1e3
+        nsw = len(case["msweep"])
+        res[name] = {"sweeps_per_s": nsw / t_sw, "s_total": t_all, "s_infinite": t_inf, "s_finite": t_sw,
                      "steps": len(recs), "energy_final": recs[-1]["energy"][0],
                      "finite_step_ms": {"step": statistics.mean(r["ms_step"] for r in fin),
                                         "eigensolve": statistics.mean(r["ms_eigh"] for r in fin),
@@ -529,6 +539,11 @@ def run_gpu(args):
     e2e_value = f_hv * statistics.mean(numops) / (statistics.mean(e2e_times) / 1e3) / 1e12 * world
 
     sweeps = measure_sweeps(nss, local) if not args.no_sweeps else None
+    sweeps_large = None
+    if not args.no_sweeps and args.large_sweeps > 0:
+        case = dict(SWEEP_CASE_LARGE, msweep=[SWEEP_CASE_LARGE["mdmrg"]] * args.large_sweeps)
+        case["workload"] = f"heisenberg_one_L64_M512_{args.large_sweeps}sweeps"
+        sweeps_large = measure_sweeps(nss, local, case, warm=False)
     batch = measure_batch(nss, local) if not args.no_batch else None
     serving = measure_serving(nss, local) if not args.no_serving else None
 
@@ -589,6 +604,7 @@ def run_gpu(args):
                           "ms_per_launch": t_hv * 1e3, "hbm_peak_gbs": peaks.get("hbm_gbs")}),
             "core_probe": CORE_PROBE,
             "sweeps": sweeps,
+            "sweeps_large": sweeps_large,
             "batch": batch,
             "serving": serving,
             "setup_s": t_prep,

@@ -107,6 +107,7 @@ void nss_destroy(nss_ctx *ctx) {
     nss::sb_release(ctx->c);
     nss::lanczos_release(ctx->c);
     nss::rdm_release(ctx->c);
+    nss::renorm_release(ctx->c);
     nss::ctx_free(ctx->c, ctx->d_v);
     nss::ctx_free(ctx->c, ctx->d_hv);
     nss::ctx_free(ctx->c, ctx->d_psi);

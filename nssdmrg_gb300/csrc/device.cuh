@@ -140,6 +140,30 @@ struct DevRdm {
     int64_t cap_hu = 0;
 };
 
+// Operator renormalisation on the device (k_renorm.cu): grow-only buffers
+struct DevRenorm {
+    void *blas = nullptr;        // cublasHandle_t
+    double *ublk = nullptr, *dblk = nullptr, *tbuf = nullptr, *rbuf = nullptr;
+    int64_t cap_ublk = 0, cap_dblk = 0, cap_tbuf = 0, cap_rbuf = 0;
+    int *itab = nullptr;
+    int64_t cap_itab = 0;
+    double *hblk = nullptr, *hres = nullptr;     // pinned staging
+    int64_t cap_hblk = 0, cap_hres = 0;
+    int *hitab = nullptr;
+    int64_t cap_hitab = 0;
+};
+
+// Kept columns of one side after nss_rdm, for the device renormalisation:
+// column j belongs to side-local rho block q[j]; its n_q values (block rows,
+// no zero rows) start at off[j] in the device buffer dcomp, valid until the
+// next RDM call on the context.  dims/maps/map_off: the side's blocks and
+// their enlarged-block states.
+struct KeptLayout {
+    int ms = 0;
+    std::vector<int> q, off, dims, maps, map_off;
+    const double *dcomp = nullptr;
+};
+
 struct Ctx {
     int device = 0;
     size_t budget = 0, used = 0;
@@ -150,6 +174,7 @@ struct Ctx {
     DevSb sb;
     DevLanczos lz;
     DevRdm rdm;
+    DevRenorm ren;
     int64_t launches = 0;        // kernels of this library launched
     int tc_min_dl = 256;         // tensor-core sector threshold (see tc_min_dl_default)
     // last nss_eigh statistics
@@ -231,10 +256,17 @@ int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb
 int syev_eigs_per_cta();
 
 // k_rdm.cu
+// kl (may be null): per side, the kept columns left on the device
 int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2],
             double *lam_l, double *lam_r, int32_t *kept_l, int32_t *kept_r,
-            double *u_l, double *u_r);
+            double *u_l, double *u_r, KeptLayout *kl = nullptr);
 void rdm_release(Ctx &c);
+
+// k_renorm.cu: blk's operators <- U^T O U for the kept columns kl, blk's
+// basis <- kept_qn (one QN tuple per kept column)
+struct Block;
+int renorm_device(Ctx &c, const KeptLayout &kl, Block &blk, const std::vector<std::vector<double>> &kept_qn);
+void renorm_release(Ctx &c);
 
 }  // namespace nss
 

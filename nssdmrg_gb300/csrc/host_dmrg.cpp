@@ -2,6 +2,7 @@
 #include "host_dmrg.hpp"
 
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <stdexcept>
 
@@ -360,9 +361,18 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     u_r.resize((size_t)sb.m_right * sb.m_right);
     k_l.resize(sb.m_left);
     k_r.resize(sb.m_right);
+    // operator renormalisation: QN-block GEMMs on the device for blocks of
+    // at least 256 states (below that the host's sparse products are as
+    // fast as the transfers); env NSS_RENORM=host / device forces one
+    const char *rh = std::getenv("NSS_RENORM");
+    const bool force_host = rh && std::string(rh) == "host", force_dev = rh && std::string(rh) == "device";
+    const bool dev_renorm =
+        renorm && !force_host && (force_dev || std::max(sb.m_left, sb.m_right) >= 256);
+    KeptLayout kl[2];
     rc = rdm_run(c, c.lz.evecs, mstates, p.deg_evals_threshold, side, nullptr, nullptr,
                  renorm ? k_l.data() : nullptr, renorm ? k_r.data() : nullptr,
-                 renorm ? u_l.data() : nullptr, renorm ? u_r.data() : nullptr);
+                 (renorm && !dev_renorm) ? u_l.data() : nullptr, (renorm && !dev_renorm) ? u_r.data() : nullptr,
+                 dev_renorm ? kl : nullptr);
     if (rc) return rc;
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
@@ -395,10 +405,17 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             qr.push_back(q);
         }
         const auto t_r = std::chrono::steady_clock::now();
-        const Csr cul = u_to_csr(u_l, sb.m_left, side[0].m_s), cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
-        renormalize(left, cul, ql);
-        renormalize(right, cur, qr);
-        rec.nnz_u = cul.nnz() + cur.nnz();
+        if (dev_renorm) {
+            if ((rc = renorm_device(c, kl[0], left, ql)) || (rc = renorm_device(c, kl[1], right, qr))) return rc;
+            rec.nnz_u = 0;
+            for (int s2 = 0; s2 < 2; ++s2)
+                for (int j = 0; j < kl[s2].ms; ++j) rec.nnz_u += kl[s2].dims[kl[s2].q[j]];
+        } else {
+            const Csr cul = u_to_csr(u_l, sb.m_left, side[0].m_s), cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
+            renormalize(left, cul, ql);
+            renormalize(right, cur, qr);
+            rec.nnz_u = cul.nnz() + cur.nnz();
+        }
         rec.nnz_ops = 0;
         for (const auto &o : left.ops) rec.nnz_ops += o.m.nnz();
         for (const auto &o : right.ops) rec.nnz_ops += o.m.nnz();

@@ -523,7 +523,7 @@ void rdm_release(Ctx &c) {
 }
 
 int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2], double *lam_l,
-            double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r) {
+            double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r, KeptLayout *kl) {
     DevSb &s = c.sb;
     if (!s.valid) { c.err = "nss_rdm: no superblock uploaded"; return NSS_ERR_STATE; }
     if (s.ai.empty() || s.bi.empty()) { c.err = "nss_rdm: descriptor had no ai/bi state maps"; return NSS_ERR_INVALID; }
@@ -830,8 +830,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     }
     // kept eigenvectors of the own path's blocks; marked blocks again
     // through the library
-    if (!own.empty() && (u_l || u_r)) {
-        const int msv[2] = {u_l ? hi[0] : 0, u_r ? hi[1] : 0};
+    if (!own.empty() && (u_l || u_r || kl)) {
+        const int msv[2] = {(u_l || kl) ? hi[0] : 0, (u_r || kl) ? hi[1] : 0};
         c.launches += 2;
         const int e = syev_vec(r.order, rnk, msv, nl, nsb, d_ev_off, d_dims, d_rho_off, d_bmode, sub, r.evals, ldd,
                                ldl, bscale, bsig, tau, refl, perm, flags, r.vec, st);
@@ -896,7 +896,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     for (int side = 0; side < 2; ++side) {
         const int base = side == 0 ? 0 : nl;
         const int ms = hi[side];
-        if (!(u_out[side] || kept_out[side])) continue;
+        if (!(u_out[side] || kept_out[side] || kl)) continue;
         any = true;
         int *dk = d_kept + side * 2 * kmax, *doff = dk + kmax;
         double *du = r.u + (int64_t)side * kmax * maxd;
@@ -911,6 +911,22 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
                                             cudaMemcpyDeviceToHost, st));
     }
     if (any) NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (kl)
+        for (int side = 0; side < 2; ++side) {
+            KeptLayout &L = kl[side];
+            const int ms = hi[side], o = side * nsb;
+            L.ms = ms;
+            L.q.assign(hkept[side], hkept[side] + ms);
+            L.off.assign(hoff[side], hoff[side] + ms);
+            L.dims.assign(dims.begin() + o, dims.begin() + o + nsb);
+            L.map_off.assign(nsb, 0);
+            L.maps.clear();
+            for (int k = 0; k < nsb; ++k) {
+                L.map_off[k] = (int)L.maps.size();
+                L.maps.insert(L.maps.end(), maps.begin() + map_off[o + k], maps.begin() + map_off[o + k] + dims[o + k]);
+            }
+            L.dcomp = r.u + (int64_t)side * kmax * maxd;
+        }
     for (int side = 0; side < 2; ++side) {
         const int ms = hi[side];
         if (kept_out[side])

@@ -78,3 +78,33 @@ def test_mixed_precision_trajectory(nss, trajectories):
     recs = d.infinite()
     e = np.array([r["energy"][0] for r in recs])
     np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("model,ldmrg,mdmrg,qn,u", [(0, 10, 64, (0.0, 0.0), 0.0), (2, 12, 64, (0.5, 0.5), 4.0),
+                                                 (1, 10, 48, (0.0, 0.0), 0.0)])
+def test_device_renormalisation_matches_host(nss, model, ldmrg, mdmrg, qn, u):
+    """Operator renormalisation U^T O U as QN-block GEMMs on the GPU against
+    the host's sparse products (env NSS_RENORM=device / host) on the same run: the
+    operators differ by rounding only, so the energies agree to 1e-11 (the
+    kept dimensions may not: where the truncation cut falls among
+    eigenvalues of 1e-15..1e-18, rounding decides it)."""
+    import os
+
+    def run(host):
+        old = os.environ.get("NSS_RENORM")
+        try:
+            os.environ["NSS_RENORM"] = "host" if host else "device"
+            d = nss.DMRG(model, ldmrg, mdmrg, msweep=(mdmrg,), u=u, hfmode=False, dmrg_qn=qn, lanc_neigen=1,
+                         lanc_tolerance=1e-12)
+            return d.finite()
+        finally:
+            if old is None:
+                os.environ.pop("NSS_RENORM", None)
+            else:
+                os.environ["NSS_RENORM"] = old
+
+    dev, host = run(False), run(True)
+    assert len(dev) == len(host)
+    e_d = np.array([r["energy"][0] for r in dev])
+    e_h = np.array([r["energy"][0] for r in host])
+    np.testing.assert_allclose(e_d, e_h, rtol=1e-11, atol=0)
