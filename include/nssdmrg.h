@@ -195,6 +195,13 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
  * reference (LAPACK dsyev per block, src/MATRIX/MATRIX_BLOCKS.f90:589-657). */
 int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int *fallback_blocks);
 
+/* Why blocks fell back to the library path, counted over the context's life:
+ * out[0] L D L^T not positive definite, out[1] a kept eigenvalue within 32 eps
+ * of a neighbour, out[2] the Rayleigh iteration did not settle, out[3] a
+ * Gram-Schmidt remainder below 1/2, out[4] a relative cluster with more than
+ * 16 kept members.  No counterpart in the reference. */
+int nss_rdm_fallback_reasons(const nss_ctx *ctx, int64_t out[5]);
+
 /* Timing of the mixed method's persistent Lanczos kernel: with `enable`
  * set, each launch in later nss_eigh calls is bracketed by CUDA events on
  * the context stream; nss_chunk_stats returns, for the last nss_eigh, the

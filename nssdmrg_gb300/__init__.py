@@ -143,6 +143,7 @@ def lib():
         "nss_dmrg_prepare_last": (C.c_int, [P]),
         "nss_dmrg_export_superblock": (C.c_int, [P, C.POINTER(SbDesc)]),
         "nss_rdm_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "nss_rdm_fallback_reasons": (C.c_int, [P, C.POINTER(C.c_int64)]),
         "nss_dmrg_nrecords": (C.c_int, [P]),
         "nss_dmrg_records": (C.c_int, [P, C.POINTER(StepRecord), C.c_int]),
     }
@@ -387,6 +388,14 @@ class Superblock:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         self._check(lib().nss_rdm_stats(self._ctx, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def rdm_fallback_reasons(self):
+        """Counts of own-path blocks sent back to the library, by reason:
+        (not positive definite, gap < 32 eps, Rayleigh iteration unsettled,
+        Gram-Schmidt remainder < 1/2, cluster too large)."""
+        out = (C.c_int64 * 5)()
+        self._check(lib().nss_rdm_fallback_reasons(self._ctx, out))
+        return tuple(out)
 
     def upload_desc(self, desc: SbDesc):
         self._check(lib().nss_sb_upload(self._ctx, C.byref(desc)))

@@ -232,6 +232,12 @@ int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int 
     return NSS_OK;
 }
 
+int nss_rdm_fallback_reasons(const nss_ctx *ctx, int64_t out[5]) {
+    if (!ctx || !out) return NSS_ERR_INVALID;
+    for (int b = 0; b < 5; ++b) out[b] = ctx->c.rdm_fail_why[b];
+    return NSS_OK;
+}
+
 int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");

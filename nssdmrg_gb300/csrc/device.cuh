@@ -138,6 +138,10 @@ struct DevRdm {
     int64_t cap_htab = 0;
     double *hu = nullptr;            // pinned staging of the compact kept columns
     int64_t cap_hu = 0;
+    double *big = nullptr;           // blocked library reductions: block copies + workspaces
+    int64_t cap_big = 0;
+    int *big_info = nullptr;
+    int64_t cap_big_info = 0;
 };
 
 // Operator renormalisation on the device (k_renorm.cu): grow-only buffers
@@ -189,6 +193,10 @@ struct Ctx {
     // last nss_rdm: blocks on the own eigensolver, on the library, and own
     // blocks whose vectors were recomputed by the library
     int rdm_own_blocks = 0, rdm_lib_blocks = 0, rdm_fallback_blocks = 0;
+    // fallback reasons over the context's life: not positive definite, gap
+    // below 32 eps, Rayleigh iteration unsettled, Gram-Schmidt remainder,
+    // cluster too large
+    int64_t rdm_fail_why[5] = {0, 0, 0, 0, 0};
 };
 
 // Allocation through the context budget.
@@ -240,19 +248,26 @@ int batch_step(BatchEngine *e, int max_done, int *ndone, int *ids, double *energ
 int batch_inflight(const BatchEngine *e);
 void lanczos_release(Ctx &c);
 
-// k_syev.cu: FP64 eigensolver of the rho blocks (blocks up to SYEV_MAX)
+// k_syev.cu: FP64 eigensolver of the rho blocks.  Blocks up to SYEV_MAX
+// are reduced to tridiagonal form in one CTA (k_trd); larger ones, up to
+// SYEV_BIG_MAX, by the library's blocked reduction (k_big_prep adapts its
+// output); the eigenvalues and kept vectors of both come from k_bisect and
+// k_vec.
 constexpr int SYEV_MAX = 160;
+constexpr int SYEV_BIG_MAX = 2048;
 int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
              int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, cudaStream_t st);
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
                 const double *te, double *evals, double *ldd, double *ldl, double *bscale, double *bsig,
-                int *flags, int *sub, cudaStream_t st);
+                int *flags, int *sub, int nmax, cudaStream_t st);
+int syev_big_prep(const double *A, int n, int64_t roff, int eo, double *refl, double *te, double *tau, int *perm,
+                  cudaStream_t st);
 // kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions
 // start at nl): k_vec + the cluster Gram-Schmidt, two launches
 int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
              const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
              const double *ldd, const double *ldl, const double *bscale, const double *bsig, const double *tau,
-             const double *refl, const int *perm, int *flags, double *vec, cudaStream_t st);
+             const double *refl, const int *perm, int *flags, double *vec, int nmax, cudaStream_t st);
 int syev_eigs_per_cta();
 
 // k_rdm.cu

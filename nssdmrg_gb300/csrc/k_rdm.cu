@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(256) k_fbperm(const int *__restrict__ list, co
                                               const int *__restrict__ ev_off, const int64_t *__restrict__ rho_off,
                                               const double *__restrict__ evals, const double *__restrict__ src,
                                               double *__restrict__ dst) {
-    __shared__ int perm[SYEV_MAX];
+    extern __shared__ int perm[];
     const int q = list[blockIdx.x], n = dims[q];
     const double *ev = evals + ev_off[q];
     for (int col = threadIdx.x; col < n; col += blockDim.x) {
@@ -509,7 +509,7 @@ int ensure_n(Ctx &c, T **p, int64_t &cap, int64_t need) {
 void rdm_release(Ctx &c) {
     DevRdm &r = c.rdm;
     void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal, r.bat, r.bat_info,
-                    r.vec, r.syd, r.syi, r.tab};
+                    r.vec, r.syd, r.syi, r.tab, r.big, r.big_info};
     for (void *p : ptrs) ctx_free(c, p);
     if (r.htab) cudaFreeHost(r.htab);
     if (r.hu) cudaFreeHost(r.hu);
@@ -559,24 +559,32 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // eigensolver path of each block
     const bool own_path = rdm_own_eigensolver();
     const int jmax = jacobi_max();
-    std::vector<int> own, small, large;
-    int maxn_own = 1;
+    // own: reduced in one CTA (k_trd); big: by the library's blocked
+    // tridiagonal reduction; both then share bisection and vectors (the
+    // "own path"); small / large: the library eigensolvers throughout
+    std::vector<int> own, big, small, large;
+    int maxn_own = 1, maxn_path = 1;
     for (int q = 0; q < nblk; ++q) {
         if (own_path && dims[q] <= SYEV_MAX) {
             own.push_back(q);
             maxn_own = std::max(maxn_own, dims[q]);
+        } else if (own_path && dims[q] <= SYEV_BIG_MAX) {
+            big.push_back(q);
         } else if (dims[q] <= jmax) {
             small.push_back(q);
         } else {
             large.push_back(q);
         }
     }
+    std::vector<int> path(own);
+    path.insert(path.end(), big.begin(), big.end());
+    for (int q : path) maxn_path = std::max(maxn_path, dims[q]);
     std::vector<int2> bis;
     const int epc = syev_eigs_per_cta();
-    for (int q : own)
+    for (int q : path)
         for (int k0 = 0; k0 < dims[q]; k0 += epc) bis.push_back(make_int2(q, k0));
     std::vector<int> bmode(nblk, 1);
-    for (int q : own) bmode[q] = 0;
+    for (int q : path) bmode[q] = 0;
     std::vector<int> maps(s.ai), map_off(s.ai_off);
     for (int k = 1; k <= nsb; ++k) map_off.push_back((int)s.ai.size() + s.bi_off[k]);
     maps.insert(maps.end(), s.bi.begin(), s.bi.end());
@@ -605,7 +613,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     }
     // own eigensolver: reflectors (rho layout), T, tau, L D L^T (eigenvalue
     // layout), per-block scale and shift; per-block flags
-    const int64_t syd_need = own.empty() ? 1 : acc + 5 * (int64_t)eacc + 2 * nblk;
+    const int64_t syd_need = path.empty() ? 1 : acc + 5 * (int64_t)eacc + 2 * nblk;
     if ((rc = ensure_n(c, &r.syd, r.cap_syd, syd_need))) return rc;
     if ((rc = ensure_n(c, &r.syi, r.cap_syi, nblk + 3 * (int64_t)eacc))) return rc;
     double *refl = r.syd, *td = refl + acc, *te = td + eacc, *tau = te + eacc, *ldd = tau + eacc,
@@ -660,13 +668,81 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
     ++c.launches;
     k_symcheck<<<std::min(nblk, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, nblk, r.iscal + 7);
-    if (!own.empty()) {
-        NSS_CUDA_TRY(c, cudaMemsetAsync(flags, 0, nblk * sizeof(int), st));
-        c.launches += 2;
-        int e = syev_trd(r.rho, d_rho_off, d_dims, d_ev_off, d_own, (int)own.size(), maxn_own, refl, td, te, tau,
+    cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
+    auto make_side_streams = [&]() -> int {
+        if (!r.ev_fork) {
+            NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
+            for (int i = 0; i < DevRdm::NSIDE; ++i) {
+                NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&r.side[i], cudaStreamNonBlocking));
+                NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
+            }
+        }
+        return NSS_OK;
+    };
+    if (!path.empty()) NSS_CUDA_TRY(c, cudaMemsetAsync(flags, 0, nblk * sizeof(int), st));
+    if (!big.empty()) {
+        // blocked library reductions of the big blocks on the side streams
+        if ((rc = make_side_streams())) { cleanup(); return rc; }
+        std::vector<int64_t> aoff(big.size()), woff(big.size());
+        int64_t bneed = 0;
+        for (size_t b = 0; b < big.size(); ++b) {
+            const int q = big[b], n = dims[q];
+            int lw = 0;
+            if (cusolverDnDsytrd_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, r.rho, n, td, te, tau, &lw) !=
+                CUSOLVER_STATUS_SUCCESS) {
+                cleanup();
+                c.err = "nss_rdm: cusolverDnDsytrd_bufferSize failed";
+                return NSS_ERR_CUDA;
+            }
+            aoff[b] = bneed;
+            bneed += (int64_t)n * n;
+            woff[b] = bneed;
+            bneed += lw + 8;
+        }
+        if ((rc = ensure_n(c, &r.big, r.cap_big, bneed))) { cleanup(); return rc; }
+        if ((rc = ensure_n(c, &r.big_info, r.cap_big_info, (int64_t)big.size()))) { cleanup(); return rc; }
+        NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
+        for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
+        for (size_t b = 0; b < big.size(); ++b) {
+            const int q = big[b], n = dims[q], eo = ev_off[q];
+            cudaStream_t ss = r.side[b % DevRdm::NSIDE];
+            double *A = r.big + aoff[b];
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(A, r.rho + rho_off[q], (size_t)n * n * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, ss));
+            cusolverDnSetStream(h, ss);
+            const cusolverStatus_t cs =
+                cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, A, n, td + eo, te + eo, tau + eo, r.big + woff[b],
+                                 (int)(aoff.size() > b + 1 ? aoff[b + 1] - woff[b] - 8 : bneed - woff[b] - 8),
+                                 r.big_info + b);
+            cusolverDnSetStream(h, st);
+            if (cs != CUSOLVER_STATUS_SUCCESS) {
+                cleanup();
+                c.err = "nss_rdm: cusolverDnDsytrd failed";
+                return NSS_ERR_CUDA;
+            }
+            ++c.launches;
+            const int e = syev_big_prep(A, n, rho_off[q], eo, refl, te, tau, perm, ss);
+            if (e) {
+                cleanup();
+                c.err = std::string("nss_rdm: eigensolver launch failed: ") + cudaGetErrorString((cudaError_t)e);
+                return NSS_ERR_CUDA;
+            }
+        }
+        for (int i = 0; i < DevRdm::NSIDE; ++i) {
+            NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
+            NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
+        }
+    }
+    if (!path.empty()) {
+        int e = 0;
+        if (!own.empty()) {
+            ++c.launches;
+            e = syev_trd(r.rho, d_rho_off, d_dims, d_ev_off, d_own, (int)own.size(), maxn_own, refl, td, te, tau,
                          perm, st);
+        }
+        ++c.launches;
         if (!e) e = syev_bisect(d_dims, d_ev_off, d_bis, (int)bis.size(), td, te, r.evals, ldd, ldl, bscale, bsig,
-                                flags, sub, st);
+                                flags, sub, maxn_path, st);
         if (e) {
             cleanup();
             c.err = std::string("nss_rdm: eigensolver launch failed: ") + cudaGetErrorString((cudaError_t)e);
@@ -679,17 +755,10 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // eigensolve per padded size class N = 32*ceil(d/32) (each block embedded
     // in an N x N matrix whose extra diagonal lies below its spectrum), the
     // classes on side streams.
-    cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
     auto lib_eigh = [&](const std::vector<int> &sm, const std::vector<int> &lg, bool write_evals,
                         double *vec_out) -> int {
         if (sm.empty() && lg.empty()) return NSS_OK;
-        if (!r.ev_fork) {
-            NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
-            for (int i = 0; i < DevRdm::NSIDE; ++i) {
-                NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&r.side[i], cudaStreamNonBlocking));
-                NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&r.ev_join[i], cudaEventDisableTiming));
-            }
-        }
+        if ((rc = make_side_streams())) return rc;
         if (!r.params) {
             cusolverDnParams_t prm = nullptr;
             if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) {
@@ -781,7 +850,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         cleanup();
         return rc;
     }
-    c.rdm_own_blocks = (int)own.size();
+    c.rdm_own_blocks = (int)path.size();
     c.rdm_lib_blocks = (int)(small.size() + large.size());
     c.rdm_fallback_blocks = 0;
     ++c.launches;
@@ -794,7 +863,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         const int n = nside[side], base = side == 0 ? 0 : nl;
         ++c.launches;
         k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base,
-                                                own.empty() ? nullptr : rnk + base);
+                                                path.empty() ? nullptr : rnk + base);
         ++c.launches;
         k_truncate<<<1, 1024, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
                                      r.iscal + side);
@@ -830,11 +899,11 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     }
     // kept eigenvectors of the own path's blocks; marked blocks again
     // through the library
-    if (!own.empty() && (u_l || u_r || kl)) {
+    if (!path.empty() && (u_l || u_r || kl)) {
         const int msv[2] = {(u_l || kl) ? hi[0] : 0, (u_r || kl) ? hi[1] : 0};
-        c.launches += 2;
+        c.launches += 3;
         const int e = syev_vec(r.order, rnk, msv, nl, nsb, d_ev_off, d_dims, d_rho_off, d_bmode, sub, r.evals, ldd,
-                               ldl, bscale, bsig, tau, refl, perm, flags, r.vec, st);
+                               ldl, bscale, bsig, tau, refl, perm, flags, r.vec, maxn_path, st);
         if (e) {
             cleanup();
             c.err = std::string("nss_rdm: eigenvector launch failed: ") + cudaGetErrorString((cudaError_t)e);
@@ -844,8 +913,12 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         NSS_CUDA_TRY(c, cudaMemcpyAsync(hflags.data(), flags, nblk * sizeof(int), cudaMemcpyDeviceToHost, st));
         NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
         std::vector<int> fs, fl;
-        for (int q : own)
-            if (hflags[q] & 2) (dims[q] <= jmax ? fs : fl).push_back(q);
+        for (int q : path)
+            if (hflags[q] & 2) {
+                (dims[q] <= jmax ? fs : fl).push_back(q);
+                for (int b = 0; b < 5; ++b)
+                    if (hflags[q] & (4 << b)) ++c.rdm_fail_why[b];
+            }
         c.rdm_fallback_blocks = (int)(fs.size() + fl.size());
         if (c.rdm_fallback_blocks) {
             // library vectors into the blocks' rho slots (consumed by then),
@@ -861,7 +934,10 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             temps.push_back(d_fb);
             NSS_CUDA_TRY(c, cudaMemcpyAsync(d_fb, fb.data(), fb.size() * sizeof(int), cudaMemcpyHostToDevice, st));
             ++c.launches;
-            k_fbperm<<<(int)fb.size(), 256, 0, st>>>(d_fb, d_dims, d_ev_off, d_rho_off, r.evals, r.rho, r.vec);
+            int fbmax = 1;
+            for (int q : fb) fbmax = std::max(fbmax, dims[q]);
+            k_fbperm<<<(int)fb.size(), 256, fbmax * sizeof(int), st>>>(d_fb, d_dims, d_ev_off, d_rho_off, r.evals,
+                                                                        r.rho, r.vec);
             NSS_CUDA_TRY(c, cudaGetLastError());
         }
     }

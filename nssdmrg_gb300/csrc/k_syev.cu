@@ -46,6 +46,7 @@
 //             library eigensolver.
 #include "device.cuh"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -58,6 +59,7 @@ constexpr int BIS_EPC = 8;          // eigenvalues per CTA
 constexpr int BIS_THREADS = 160;    // 4 warps x 2 eigenvalues x 16 shifts, 1 warp for L D L^T
 constexpr int VEC_WARPS = 4;
 constexpr double RELGAP_MIN = 1e-2;
+constexpr int VEC_MAXCL = 16;       // kept members of one relative cluster
 constexpr double PIVMIN = 0x1p-900;
 
 __device__ __forceinline__ double wsum(double v) {
@@ -222,6 +224,32 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     }
 }
 
+// Blocks above SYEV_MAX are reduced by the library's blocked tridiagonal
+// reduction (LAPACK dsytrd layout, lower: T's diagonal and subdiagonal in
+// d and e, reflector k with v[k+1] = 1 implicit and v[k+2..] in column k of
+// A below the subdiagonal).  This copies the reflectors into the layout
+// k_vec reads (column k of the block's refl slot, v[k+1] = 1 explicit),
+// closes the T and tau arrays and sets the identity row order.
+__global__ void __launch_bounds__(256) k_big_prep(const double *__restrict__ A, int n, int64_t roff, int eo,
+                                                  double *__restrict__ refl, double *__restrict__ te,
+                                                  double *__restrict__ tau, int *__restrict__ perm) {
+    double *V = refl + roff;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n * n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(e / n), i = (int)(e - (int64_t)k * n);
+        double x = 0.0;
+        if (k + 2 < n) x = i == k + 1 ? 1.0 : (i > k + 1 ? A[e] : 0.0);
+        V[e] = x;
+    }
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) perm[eo + i] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        te[eo + n - 1] = 0.0;
+        tau[eo + n - 1] = 0.0;
+        if (n >= 2) tau[eo + n - 2] = 0.0;
+    }
+}
+
 // Number of eigenvalues of the scaled T below s (a: diagonal, bb[i] =
 // b_{i-1}^2, bb[0] = 0; the caller passes one unreduced block).  Sign changes of the leading minors; an exact zero
 // minor is replaced by -2^-100 times the previous one (a negative pivot, as
@@ -290,8 +318,10 @@ __global__ void __launch_bounds__(BIS_THREADS)
     k_bisect(const int *__restrict__ dims, const int *__restrict__ ev_off, const int2 *__restrict__ items,
              const double *__restrict__ td, const double *__restrict__ te, double *__restrict__ evals,
              double *__restrict__ ldd, double *__restrict__ ldl, double *__restrict__ bscale,
-             double *__restrict__ bsig, int *__restrict__ flags, int *__restrict__ sub) {
-    __shared__ double sa[SYEV_MAX], sbb[SYEV_MAX], sb[SYEV_MAX];
+             double *__restrict__ bsig, int *__restrict__ flags, int *__restrict__ sub, int nmax) {
+    extern __shared__ double bis_smem[];
+    double *sa = bis_smem, *sbb = sa + nmax, *sb = sbb + nmax;
+    float *fa = (float *)(sb + nmax), *fbb = fa + nmax;
     __shared__ double red[BIS_THREADS / 32];
     __shared__ double s_norm;
     const int2 it = items[blockIdx.x];
@@ -342,7 +372,6 @@ __global__ void __launch_bounds__(BIS_THREADS)
         // eigenvalues per warp.  Only brackets the eigenvalue: an FP32 count
         // is exact for a matrix within ~2^-21 of the scaled T, so the bracket
         // is widened by 2^-16 and checked with FP64 counts in phase B.
-        __shared__ float fa[SYEV_MAX], fbb[SYEV_MAX];
         __shared__ double blo[BIS_EPC], bhi[BIS_EPC];
         __shared__ int bk[BIS_EPC][3];               // r0, r1, exact (1 x 1 block)
         for (int i = tid; i < n; i += 128) {
@@ -524,14 +553,181 @@ __device__ __forceinline__ VecCluster vec_cluster(const VecArgs &a, int q, int c
     return c;
 }
 
+// Per-warp scratch of the vector kernels: seven arrays of n_max doubles.
+struct VecScratch {
+    double *dD, *dL, *lp, *um, *ss, *pp, *z;
+};
+
+__device__ __forceinline__ VecScratch vec_scratch(double *sw, int nmax) {
+    return VecScratch{sw, sw + nmax, sw + 2 * nmax, sw + 3 * nmax, sw + 4 * nmax, sw + 5 * nmax, sw + 6 * nmax};
+}
+
+// Stationary transform L+ D+ L+^T = L D L^T - lam over rows [r0, r1) on
+// lane 0: lp = L+, ss = the s_i of the differential form; dplus (may be
+// null) receives the pivots D+.
+__device__ __forceinline__ void dstqds_lane0(const VecScratch &w, int r0, int r1, double lam, double *dplus) {
+    double s = -lam;
+    for (int i = r0; i + 1 < r1; ++i) {
+        w.ss[i] = s;
+        double dp = w.dD[i] + s;
+        if (fabs(dp) < PIVMIN) dp = -PIVMIN;
+        if (dplus) dplus[i] = dp;
+        const double l = w.dD[i] * w.dL[i] * rcp_nr(dp);
+        w.lp[i] = l;
+        s = l * w.dL[i] * s - lam;
+    }
+    w.ss[r1 - 1] = s;
+    if (dplus) {
+        double dp = w.dD[r1 - 1] + s;
+        if (fabs(dp) < PIVMIN) dp = -PIVMIN;
+        dplus[r1 - 1] = dp;
+    }
+}
+
+// Twisted-factorisation eigenvector of L D L^T (rows [r0, r1) of the block,
+// zero elsewhere in z[0, n)) for the eigenvalue near lam0, with Rayleigh
+// corrections that stay within gap / 4; z comes out normalised.
+__device__ bool twisted_vector(const VecScratch &w, int lane, int n, int r0, int r1, double lam0, double gap) {
+    double lam = lam0, ztz = 1.0;
+    bool conv = false;
+    for (int itr = 0; itr < 8; ++itr) {
+        if (lane == 0) {
+            dstqds_lane0(w, r0, r1, lam, nullptr);
+        } else if (lane == 1) {                      // progressive: U- D- U-^T = L D L^T - lam
+            double p = w.dD[r1 - 1] - lam;
+            for (int i = r1 - 2; i >= r0; --i) {
+                w.pp[i + 1] = p;
+                double dm = w.dD[i] * w.dL[i] * w.dL[i] + p;
+                if (fabs(dm) < PIVMIN) dm = -PIVMIN;
+                const double t = w.dD[i] * rcp_nr(dm);
+                w.um[i] = w.dL[i] * t;
+                p = p * t - lam;
+            }
+            w.pp[r0] = p;
+        }
+        __syncwarp();
+        double best = INFINITY;
+        int bi = r1;
+        for (int k = r0 + lane; k < r1; k += 32) {
+            const double gk = fabs(w.ss[k] + w.pp[k] + lam);
+            if (gk < best) {
+                best = gk;
+                bi = k;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob < best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (bi >= r1) break;                         // every gamma NaN
+        const int r = bi;
+        const double gam = w.ss[r] + w.pp[r] + lam;
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) w.z[i] = 0.0;
+        __syncwarp();
+        if (lane == 0) {
+            double zz = 1.0;
+            w.z[r] = 1.0;
+            for (int i = r - 1; i >= r0; --i) {
+                zz = -w.lp[i] * zz;
+                w.z[i] = zz;
+            }
+        } else if (lane == 1) {
+            double zz = 1.0;
+            for (int i = r; i + 1 < r1; ++i) {
+                zz = -w.um[i] * zz;
+                w.z[i + 1] = zz;
+            }
+        }
+        __syncwarp();
+        double t2 = 0.0;
+        for (int k = r0 + lane; k < r1; k += 32) t2 = fma(w.z[k], w.z[k], t2);
+        ztz = wsum(t2);
+        const double corr = gam / ztz;
+        if (!isfinite(ztz) || !isfinite(corr)) break;
+        if (fabs(corr) <= 0x1p-49 * lam) {
+            conv = true;
+            break;
+        }
+        lam += corr;
+        if (!(fabs(lam - lam0) <= 0.25 * gap)) break;
+        __syncwarp();
+    }
+    if (conv) {
+        const double inv = 1.0 / sqrt(ztz);
+        for (int k = lane; k < n; k += 32) w.z[k] *= inv;
+    }
+    __syncwarp();
+    return conv;
+}
+
+// z <- z - sum_y (y . z) y over the vectors ys[0..ny) (length n, global),
+// then normalised; returns the norm after the projection.
+__device__ double project_out(double *z, int n, const double *const *ys, int ny, int lane) {
+    for (int t = 0; t < ny; ++t) {
+        const double *y = ys[t];
+        double d = 0.0;
+        for (int i = lane; i < n; i += 32) d = fma(y[i], z[i], d);
+        d = wsum(d);
+        for (int i = lane; i < n; i += 32) z[i] = fma(-d, y[i], z[i]);
+        __syncwarp();
+    }
+    double nz = 0.0;
+    for (int i = lane; i < n; i += 32) nz = fma(z[i], z[i], nz);
+    nz = sqrt(wsum(nz));
+    if (nz > 0.0) {
+        const double inv = 1.0 / nz;
+        for (int i = lane; i < n; i += 32) z[i] *= inv;
+    }
+    __syncwarp();
+    return nz;
+}
+
+// x = H_0 H_1 ... H_{n-3} z (z in shared memory, overwritten), then written
+// to column X in the block's own row order.
+__device__ void back_transform_store(const VecArgs &a, int q, int n, int eo, double *z, double *Xc, int lane) {
+    const double *Vq = a.refl + a.rho_off[q];
+    for (int k = n - 3; k >= 0; --k) {
+        const double t = a.tau[eo + k];
+        if (t == 0.0) continue;
+        const double *vk = Vq + (int64_t)k * n;
+        double d = 0.0;
+        for (int i = k + 1 + lane; i < n; i += 32) d = fma(vk[i], z[i], d);
+        d = t * wsum(d);
+        for (int i = k + 1 + lane; i < n; i += 32) z[i] = fma(-d, vk[i], z[i]);
+        __syncwarp();
+    }
+    for (int i = lane; i < n; i += 32) Xc[a.perm[eo + i]] = z[i];
+    __syncwarp();
+}
+
+// relative cluster with a pair closer than 32 eps (tight), counting the
+// neighbours just outside it in the unreduced block: those clusters are
+// done by k_vec_cl
+__device__ __forceinline__ bool cluster_tight(const VecArgs &a, int q, const VecCluster &cl) {
+    const int eo = a.ev_off[q];
+    const double scale = a.bscale[q];
+    for (int c = max(cl.c0 - 1, cl.r0); c <= min(cl.c1, cl.r1 - 2); ++c)
+        if (!(a.evals[eo + c + 1] * scale - a.evals[eo + c] * scale > 32.0 * 0x1p-52)) return true;
+    return false;
+}
+
 // One warp per kept eigenvalue (both sides in one launch).  Blocks of the
-// library path (bmode != 0) already hold their vectors.  The vector is
-// written to column col of the block's column-major slot in vec, rows in the
-// block's own order; failure sets bit 1 of flags[q].
-__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec(VecArgs a) {
-    __shared__ double sm[VEC_WARPS][7][SYEV_MAX];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int j = blockIdx.x * VEC_WARPS + warp;
+// library path (bmode != 0) already hold their vectors; kept eigenvalues of
+// tight clusters are left to k_vec_cl.  The vector is written to column col
+// of the block's column-major slot in vec, rows in the block's own order.
+// Failure sets bit 1 of flags[q] and a reason bit:
+// 4 = factorisation not positive definite, 8 = gap below 32 eps,
+// 16 = Rayleigh iteration not settled, 32 = Gram-Schmidt remainder < 1/2,
+// 64 = cluster larger than VEC_MAXCL.
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec(VecArgs a, int nmax) {
+    extern __shared__ double vec_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int j = blockIdx.x * nw + warp;
     int side, q, col;
     if (!vec_locate(a, j, side, q, col)) return;
     if (a.bmode[q] != 0) return;
@@ -541,120 +737,126 @@ __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec(VecArgs a) {
         if (lane == 0) X[0] = 1.0;
         return;
     }
-    double *dD = sm[warp][0], *dL = sm[warp][1], *lp = sm[warp][2], *um = sm[warp][3], *ss = sm[warp][4],
-           *pp = sm[warp][5], *z = sm[warp][6];
+    if (cluster_tight(a, q, vec_cluster(a, q, col))) return;
+    const VecScratch w = vec_scratch(vec_smem + (size_t)warp * 7 * nmax, nmax);
     const double scale = a.bscale[q], sig0 = a.bsig[q];
     const int sr = a.sub[eo + col], r0 = sr & 0xffff, r1 = sr >> 16;
     auto lamS = [&](int c) { return a.evals[eo + c] * scale - sig0; };
     const double lam0 = lamS(col);
     const double gap = fmin(col > r0 ? lam0 - lamS(col - 1) : INFINITY, col + 1 < r1 ? lamS(col + 1) - lam0 : INFINITY);
-    bool ok = (a.flags[q] & 1) == 0 && gap > 32.0 * 0x1p-52;
-    if (ok) {
+    int why = (a.flags[q] & 1) ? 4 : 0;
+    if (!why) {
         for (int i = lane; i < n; i += 32) {
-            dD[i] = a.ldd[eo + i];
-            dL[i] = a.ldl[eo + i];
+            w.dD[i] = a.ldd[eo + i];
+            w.dL[i] = a.ldl[eo + i];
         }
         __syncwarp();
-        double lam = lam0, ztz = 1.0;
-        bool conv = false;
-        for (int itr = 0; itr < 8; ++itr) {
-            if (lane == 0) {                         // stationary: L+ D+ L+^T = L D L^T - lam
-                double s = -lam;
-                for (int i = r0; i + 1 < r1; ++i) {
-                    ss[i] = s;
-                    double dp = dD[i] + s;
-                    if (fabs(dp) < PIVMIN) dp = -PIVMIN;
-                    const double l = dD[i] * dL[i] * rcp_nr(dp);
-                    lp[i] = l;
-                    s = l * dL[i] * s - lam;
-                }
-                ss[r1 - 1] = s;
-            } else if (lane == 1) {                  // progressive: U- D- U-^T = L D L^T - lam
-                double p = dD[r1 - 1] - lam;
-                for (int i = r1 - 2; i >= r0; --i) {
-                    pp[i + 1] = p;
-                    double dm = dD[i] * dL[i] * dL[i] + p;
-                    if (fabs(dm) < PIVMIN) dm = -PIVMIN;
-                    const double t = dD[i] * rcp_nr(dm);
-                    um[i] = dL[i] * t;
-                    p = p * t - lam;
-                }
-                pp[r0] = p;
-            }
-            __syncwarp();
-            double best = INFINITY;
-            int bi = r1;
-            for (int k = r0 + lane; k < r1; k += 32) {
-                const double gk = fabs(ss[k] + pp[k] + lam);
-                if (gk < best) {
-                    best = gk;
-                    bi = k;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob < best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (bi >= r1) break;                     // every gamma NaN
-            const int r = bi;
-            const double gam = ss[r] + pp[r] + lam;
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) z[i] = 0.0;
-            __syncwarp();
-            if (lane == 0) {
-                double zz = 1.0;
-                z[r] = 1.0;
-                for (int i = r - 1; i >= r0; --i) {
-                    zz = -lp[i] * zz;
-                    z[i] = zz;
-                }
-            } else if (lane == 1) {
-                double zz = 1.0;
-                for (int i = r; i + 1 < r1; ++i) {
-                    zz = -um[i] * zz;
-                    z[i + 1] = zz;
-                }
-            }
-            __syncwarp();
-            double t2 = 0.0;
-            for (int k = r0 + lane; k < r1; k += 32) t2 = fma(z[k], z[k], t2);
-            ztz = wsum(t2);
-            const double corr = gam / ztz;
-            if (!isfinite(ztz) || !isfinite(corr)) break;
-            if (fabs(corr) <= 0x1p-49 * lam) {
-                conv = true;
-                break;
-            }
-            lam += corr;
-            if (!(fabs(lam - lam0) <= 0.25 * gap)) break;
-            __syncwarp();
-        }
-        ok = conv;
-        if (ok) {
-            const double inv = 1.0 / sqrt(ztz);
-            for (int k = lane; k < n; k += 32) z[k] *= inv;
-            __syncwarp();
-            // x = H_0 H_1 ... H_{n-3} z
-            const double *Vq = a.refl + a.rho_off[q];
-            for (int k = n - 3; k >= 0; --k) {
-                const double t = a.tau[eo + k];
-                if (t == 0.0) continue;
-                const double *vk = Vq + (int64_t)k * n;
-                double d = 0.0;
-                for (int i = k + 1 + lane; i < n; i += 32) d = fma(vk[i], z[i], d);
-                d = t * wsum(d);
-                for (int i = k + 1 + lane; i < n; i += 32) z[i] = fma(-d, vk[i], z[i]);
-                __syncwarp();
-            }
-            double *Xc = X + (int64_t)col * n;
-            for (int i = lane; i < n; i += 32) Xc[a.perm[eo + i]] = z[i];
-        }
+        if (twisted_vector(w, lane, n, r0, r1, lam0, gap))
+            back_transform_store(a, q, n, eo, w.z, X + (int64_t)col * n, lane);
+        else
+            why |= 16;
     }
-    if (!ok && lane == 0) atomicOr(&a.flags[q], 2);
+    if (why && lane == 0) atomicOr(&a.flags[q], 2 | why);
+}
+
+// Tight clusters (a pair of kept or neighbouring eigenvalues closer than
+// 32 eps within one unreduced block): one warp, the cluster's first kept
+// member, computes all kept members in the tridiagonal basis: the twisted
+// vector where the member's own gap allows it, otherwise inverse iteration
+// with the stationary factorisation L+ D+ L+^T = L D L^T - lam from a
+// pseudo-random start, Gram-Schmidt against the members before it inside
+// every iteration (the classical remedy for clustered inverse iteration);
+// the orthonormal set is then back-transformed.
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_cl(VecArgs a, int nmax) {
+    extern __shared__ double vec_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int j = blockIdx.x * nw + warp;
+    int side, q, col;
+    if (!vec_locate(a, j, side, q, col)) return;
+    if (a.bmode[q] != 0) return;
+    const int n = a.dims[q], eo = a.ev_off[q];
+    if (n == 1) return;
+    const VecCluster cl = vec_cluster(a, q, col);
+    if (!cluster_tight(a, q, cl)) return;
+    const int ms = a.side[side].ms;
+    auto kept = [&](int c) { return a.rank[eo + c] < ms; };
+    for (int c = cl.c0; c < col; ++c)
+        if (kept(c)) return;                         // an earlier kept member leads
+    const VecScratch w = vec_scratch(vec_smem + (size_t)warp * 7 * nmax, nmax);
+    double *X = a.vec + a.rho_off[q];
+    const double scale = a.bscale[q], sig0 = a.bsig[q];
+    auto lamS = [&](int c) { return a.evals[eo + c] * scale - sig0; };
+    int why = (a.flags[q] & 1) ? 4 : 0;
+    int nm = 0;
+    for (int c = col; c <= cl.c1; ++c) nm += kept(c);
+    if (nm > VEC_MAXCL) why |= 64;
+    if (!why) {
+        for (int i = lane; i < n; i += 32) {
+            w.dD[i] = a.ldd[eo + i];
+            w.dL[i] = a.ldl[eo + i];
+        }
+        __syncwarp();
+    }
+    const double *prev[VEC_MAXCL];
+    int np = 0;
+    for (int c = col; !why && c <= cl.c1; ++c) {
+        if (!kept(c)) continue;
+        const int sr = a.sub[eo + c], r0 = sr & 0xffff, r1 = sr >> 16;
+        const double lam0 = lamS(c);
+        const double gap =
+            fmin(c > r0 ? lam0 - lamS(c - 1) : INFINITY, c + 1 < r1 ? lamS(c + 1) - lam0 : INFINITY);
+        bool done = gap > 32.0 * 0x1p-52 && twisted_vector(w, lane, n, r0, r1, lam0, gap);
+        if (done) {
+            if (!(project_out(w.z, n, prev, np, lane) >= 0.5)) why |= 32;
+        } else {
+            // inverse iteration at lam0 with in-loop Gram-Schmidt
+            if (lane == 0) dstqds_lane0(w, r0, r1, lam0, w.pp);
+            __syncwarp();
+            for (int i = lane; i < n; i += 32) {
+                unsigned hsh = (unsigned)(i + 1) * 2654435761u ^ (unsigned)(c + 7) * 40503u;
+                hsh ^= hsh >> 15;
+                hsh *= 2246822519u;
+                hsh ^= hsh >> 13;
+                w.z[i] = (i >= r0 && i < r1) ? ((double)(hsh & 0xffffu) / 32768.0 - 1.0) : 0.0;
+            }
+            __syncwarp();
+            project_out(w.z, n, prev, np, lane);
+            double nz = 0.0;
+            for (int it = 0; it < 3; ++it) {
+                if (lane == 0) {                     // L+ w = x
+                    for (int i = r0; i + 1 < r1; ++i) w.z[i + 1] -= w.lp[i] * w.z[i];
+                }
+                __syncwarp();
+                for (int i = r0 + lane; i < r1; i += 32) w.z[i] *= rcp_nr(w.pp[i]);   // D+^-1
+                __syncwarp();
+                if (lane == 0) {                     // L+^T y = w
+                    for (int i = r1 - 2; i >= r0; --i) w.z[i] -= w.lp[i] * w.z[i + 1];
+                }
+                __syncwarp();
+                double t2 = 0.0;
+                for (int i = lane; i < n; i += 32) t2 = fma(w.z[i], w.z[i], t2);
+                const double gz = sqrt(wsum(t2));
+                if (!(gz > 0.0) || !isfinite(gz)) break;
+                for (int i = lane; i < n; i += 32) w.z[i] *= 1.0 / gz;
+                __syncwarp();
+                nz = project_out(w.z, n, prev, np, lane);
+            }
+            if (!(nz >= 0.5)) why |= 32;
+        }
+        if (why) break;
+        // the tridiagonal-basis vector waits in its own column until the set is complete
+        double *Xc = X + (int64_t)c * n;
+        for (int i = lane; i < n; i += 32) Xc[i] = w.z[i];
+        __syncwarp();
+        prev[np++] = Xc;
+    }
+    for (int t = 0; !why && t < np; ++t) {
+        double *Xc = const_cast<double *>(prev[t]);
+        for (int i = lane; i < n; i += 32) w.z[i] = Xc[i];
+        __syncwarp();
+        back_transform_store(a, q, n, eo, w.z, Xc, lane);
+    }
+    if (why && lane == 0) atomicOr(&a.flags[q], 2 | why);
 }
 
 // Gram-Schmidt within relative clusters of kept eigenvalues: each member's
@@ -662,8 +864,6 @@ __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec(VecArgs a) {
 // eps / (gap to the rest), so orthogonalising the cluster's kept vectors in
 // ascending order gives an orthonormal basis of it.  One warp per kept
 // eigenvalue; the warp of the first kept member does the cluster.
-constexpr int VEC_MAXCL = 16;
-
 __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_gs(VecArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = blockIdx.x * VEC_WARPS + warp;
@@ -675,12 +875,14 @@ __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_gs(VecArgs a) {
     const int ms = a.side[side].ms;
     auto kept = [&](int c) { return a.rank[eo + c] < ms; };
     const VecCluster cl = vec_cluster(a, q, col);
+    if (cluster_tight(a, q, cl)) return;             // done by k_vec_cl
     for (int c = cl.c0; c < col; ++c)
         if (kept(c)) return;                         // an earlier kept member leads
     int nm = 0;
     for (int c = col; c <= cl.c1; ++c) nm += kept(c);
     if (nm < 2) return;
     bool ok = nm <= VEC_MAXCL;
+    int why = ok ? 0 : 64;
     double *X = a.vec + a.rho_off[q];
     for (int c = col + 1; ok && c <= cl.c1; ++c) {
         if (!kept(c)) continue;
@@ -699,13 +901,14 @@ __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_gs(VecArgs a) {
         nz = sqrt(wsum(nz));
         if (!(nz >= 0.5)) {
             ok = false;
+            why |= 32;
             break;
         }
         const double inv = 1.0 / nz;
         for (int i = lane; i < n; i += 32) Z[i] *= inv;
         __syncwarp();
     }
-    if (!ok && lane == 0) atomicOr(&a.flags[q], 2);
+    if (!ok && lane == 0) atomicOr(&a.flags[q], 2 | why);
 }
 
 }  // namespace
@@ -722,17 +925,27 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
 
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
                 const double *te, double *evals, double *ldd, double *ldl, double *bscale, double *bsig,
-                int *flags, int *sub, cudaStream_t st) {
+                int *flags, int *sub, int nmax, cudaStream_t st) {
     if (nitems <= 0) return 0;
-    k_bisect<<<nitems, BIS_THREADS, 0, st>>>(dims, ev_off, items, td, te, evals, ldd, ldl, bscale, bsig, flags,
-                                             sub);
+    const int smem = nmax * (3 * (int)sizeof(double) + 2 * (int)sizeof(float));
+    cudaError_t e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return (int)e;
+    k_bisect<<<nitems, BIS_THREADS, smem, st>>>(dims, ev_off, items, td, te, evals, ldd, ldl, bscale, bsig, flags,
+                                                sub, nmax);
+    return (int)cudaGetLastError();
+}
+
+int syev_big_prep(const double *A, int n, int64_t roff, int eo, double *refl, double *te, double *tau, int *perm,
+                  cudaStream_t st) {
+    const int grid = (int)std::min<int64_t>(((int64_t)n * n + 255) / 256, 304);
+    k_big_prep<<<grid, 256, 0, st>>>(A, n, roff, eo, refl, te, tau, perm);
     return (int)cudaGetLastError();
 }
 
 int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
              const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
              const double *ldd, const double *ldl, const double *bscale, const double *bsig, const double *tau,
-             const double *refl, const int *perm, int *flags, double *vec, cudaStream_t st) {
+             const double *refl, const int *perm, int *flags, double *vec, int nmax, cudaStream_t st) {
     VecArgs a;
     a.side[0] = VecSide{order, 0, ms[0], 0};
     a.side[1] = VecSide{order + nl, nl, ms[1], nsb};
@@ -755,9 +968,16 @@ int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb
     a.vec = vec;
     const int tot = ms[0] + ms[1];
     if (tot <= 0) return 0;
-    const int grid = (tot + VEC_WARPS - 1) / VEC_WARPS;
-    k_vec<<<grid, VEC_WARPS * 32, 0, st>>>(a);
-    k_vec_gs<<<grid, VEC_WARPS * 32, 0, st>>>(a);
+    // per warp 7 n_max doubles of shared memory: up to 4 warps a CTA within 200 KB
+    const int per_warp = 7 * nmax * (int)sizeof(double);
+    const int nw = std::max(1, std::min(VEC_WARPS, (200 * 1024) / per_warp));
+    cudaError_t e = cudaFuncSetAttribute(k_vec, cudaFuncAttributeMaxDynamicSharedMemorySize, nw * per_warp);
+    if (e != cudaSuccess) return (int)e;
+    k_vec<<<(tot + nw - 1) / nw, nw * 32, nw * per_warp, st>>>(a, nmax);
+    e = cudaFuncSetAttribute(k_vec_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, nw * per_warp);
+    if (e != cudaSuccess) return (int)e;
+    k_vec_cl<<<(tot + nw - 1) / nw, nw * 32, nw * per_warp, st>>>(a, nmax);
+    k_vec_gs<<<(tot + VEC_WARPS - 1) / VEC_WARPS, VEC_WARPS * 32, 0, st>>>(a);
     return (int)cudaGetLastError();
 }
 

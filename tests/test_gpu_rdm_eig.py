@@ -178,3 +178,27 @@ def test_qn_entropy_split_matches_oracle(nss, name):
         assert abs(res.s_number[side] - sn) <= 1e-11 * abs(sn) + 1e-14, (side, res.s_number[side], sn)
         assert abs(res.s_config[side] - sc) <= 1e-11 * abs(sc) + 1e-14, (side, res.s_config[side], sc)
         assert abs(res.s_number[side] + res.s_config[side] - res.entropy[side]) <= 1e-12
+
+
+def test_big_blocks_through_blocked_reduction(nss):
+    """Rho blocks above 160 states take the library's blocked tridiagonal
+    reduction and then the same bisection and twisted vectors: against the
+    library eigensolver on the spin-1 chain's last infinite step (L=32,
+    m=256, blocks up to ~190)."""
+    d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 16, 256, dmrg_qn=(0.0,), lanc_neigen=1, lanc_tolerance=1e-12)
+    d.prepare_last()
+    s = d.sb
+    desc = d.export_superblock()
+    assert max(desc.dls[k] for k in range(desc.nsb)) > 160
+    ev, vec, _ = s.sb_diag(neigen=1, nitermax=300, tol=1e-12, seed=5, want_vectors=True)
+    psi = np.ascontiguousarray(vec[:, 0])
+    # the cut at 64 states lies well above the rounding level of this
+    # spectrum (at 256 it falls among eigenvalues of 1e-15, where rounding
+    # decides the degeneracy extension)
+    own, st_own = _rdm(s, 64, psi, library=False)
+    lib, _ = _rdm(s, 64, psi, library=True)
+    assert st_own[0] > 0 and st_own[1] == 0, st_own
+    dls = np.array([desc.dls[k] for k in range(desc.nsb)])
+    drs = np.array([desc.drs[k] for k in range(desc.nsb)])
+    off = np.array([desc.offset[k] for k in range(desc.nsb)])
+    _check_against(own, lib, _blocks_of(psi, dls, drs, off))
