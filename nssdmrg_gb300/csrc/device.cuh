@@ -260,6 +260,12 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
                 const double *te, double *evals, double *ldd, double *ldl, double *bscale, double *bsig,
                 int *flags, int *sub, int nmax, cudaStream_t st);
+// clusters of 8 or 16 CTAs per block (k_trd_cl); the size and the largest
+// block it takes
+int syev_trd_cl_size(int *nmax);
+int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
+                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm,
+                cudaStream_t st);
 int syev_big_prep(const double *A, int n, int64_t roff, int eo, double *refl, double *te, double *tau, int *perm,
                   cudaStream_t st);
 // kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions

@@ -562,12 +562,25 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // own: reduced in one CTA (k_trd); big: by the library's blocked
     // tridiagonal reduction; both then share bisection and vectors (the
     // "own path"); small / large: the library eigensolvers throughout
-    std::vector<int> own, big, small, large;
-    int maxn_own = 1, maxn_path = 1;
+    // own: one CTA per block up to SYEV_MAX states (k_trd, with the
+    // component reordering; measured faster than a cluster at 120 states),
+    // clu: a thread-block cluster per block up to the size its shared memory
+    // holds (k_trd_cl; env NSS_TRD_CLUSTER=0 disables it), big: the
+    // library's blocked reduction
+    int cl_nmax = 0;
+    syev_trd_cl_size(&cl_nmax);
+    const char *tce = std::getenv("NSS_TRD_CLUSTER");
+    const bool use_cl = !(tce && std::string(tce) == "0");
+    const int cta_max = SYEV_MAX;
+    std::vector<int> own, clu, big, small, large;
+    int maxn_own = 1, maxn_clu = 1, maxn_path = 1;
     for (int q = 0; q < nblk; ++q) {
-        if (own_path && dims[q] <= SYEV_MAX) {
+        if (own_path && dims[q] <= cta_max) {
             own.push_back(q);
             maxn_own = std::max(maxn_own, dims[q]);
+        } else if (own_path && use_cl && dims[q] <= cl_nmax) {
+            clu.push_back(q);
+            maxn_clu = std::max(maxn_clu, dims[q]);
         } else if (own_path && dims[q] <= SYEV_BIG_MAX) {
             big.push_back(q);
         } else if (dims[q] <= jmax) {
@@ -577,6 +590,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         }
     }
     std::vector<int> path(own);
+    path.insert(path.end(), clu.begin(), clu.end());
     path.insert(path.end(), big.begin(), big.end());
     for (int q : path) maxn_path = std::max(maxn_path, dims[q]);
     std::vector<int2> bis;
@@ -629,7 +643,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     const size_t o_items = slot(items.size() * sizeof(RhoItem)), o_rho_off = slot(rho_off.size() * sizeof(int64_t)),
                  o_dims = slot(dims.size() * sizeof(int)), o_ev_off = slot(ev_off.size() * sizeof(int)),
                  o_maps = slot(maps.size() * sizeof(int)), o_map_off = slot(map_off.size() * sizeof(int)),
-                 o_own = slot(own.size() * sizeof(int)), o_bis = slot(bis.size() * sizeof(int2)),
+                 o_own = slot(own.size() * sizeof(int)), o_clu = slot(clu.size() * sizeof(int)),
+                 o_bis = slot(bis.size() * sizeof(int2)),
                  o_bmode = slot(bmode.size() * sizeof(int)), o_kept = slot(4 * (size_t)kmax * sizeof(int));
     if (!r.htab || r.cap_htab < (int64_t)tot) {
         if (r.htab) cudaFreeHost(r.htab);
@@ -648,6 +663,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     put(o_maps, maps);
     put(o_map_off, map_off);
     put(o_own, own);
+    put(o_clu, clu);
     put(o_bis, bis);
     put(o_bmode, bmode);
     NSS_CUDA_TRY(c, cudaMemcpyAsync(r.tab, r.htab, o_kept, cudaMemcpyHostToDevice, st));
@@ -655,7 +671,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     const int64_t *d_rho_off = (const int64_t *)(r.tab + o_rho_off);
     const int *d_dims = (const int *)(r.tab + o_dims), *d_ev_off = (const int *)(r.tab + o_ev_off),
               *d_maps = (const int *)(r.tab + o_maps), *d_map_off = (const int *)(r.tab + o_map_off),
-              *d_own = (const int *)(r.tab + o_own), *d_bmode = (const int *)(r.tab + o_bmode);
+              *d_own = (const int *)(r.tab + o_own), *d_bmode = (const int *)(r.tab + o_bmode),
+              *d_clu = (const int *)(r.tab + o_clu);
     const int2 *d_bis = (const int2 *)(r.tab + o_bis);
     int *d_kept = (int *)(r.tab + o_kept);
     std::vector<void *> temps;
@@ -739,6 +756,11 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             ++c.launches;
             e = syev_trd(r.rho, d_rho_off, d_dims, d_ev_off, d_own, (int)own.size(), maxn_own, refl, td, te, tau,
                          perm, st);
+        }
+        if (!e && !clu.empty()) {
+            ++c.launches;
+            e = syev_trd_cl(r.rho, d_rho_off, d_dims, d_ev_off, d_clu, (int)clu.size(), maxn_clu, refl, td, te, tau,
+                            perm, st);
         }
         ++c.launches;
         if (!e) e = syev_bisect(d_dims, d_ev_off, d_bis, (int)bis.size(), td, te, r.evals, ldd, ldl, bscale, bsig,

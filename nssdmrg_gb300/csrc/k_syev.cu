@@ -46,6 +46,8 @@
 //             library eigensolver.
 #include "device.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -222,6 +224,140 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         te[eo + n - 1] = 0.0;
         tau[eo + n - 1] = 0.0;
     }
+}
+
+// The same Householder reduction for mid-size blocks on a thread-block
+// cluster of C CTAs (C = 8 or 16, one cluster per block).  CTA r holds the
+// full columns j = r + C jj of the symmetric block in shared memory.  Step
+// k: the owner of column k forms the reflector and publishes v and tau in
+// its shared memory; cluster barrier; every CTA copies v through
+// distributed shared memory and forms p_j = tau A_j . v for its active
+// columns and its share of p . v; cluster barrier; every CTA gathers p and
+// the shares, w = p - (tau/2)(p.v) v, and applies the rank-2 update to its
+// columns.  Two cluster barriers a step, the FP64 work spread over C SMs.
+// The buffers that cross CTAs alternate with the parity of k, so a
+// barrier always separates a buffer's writes from the previous step's reads.
+__global__ void __launch_bounds__(TRD_THREADS, 1)
+    k_trd_cl(const double *__restrict__ rho, const int64_t *__restrict__ rho_off, const int *__restrict__ dims,
+             const int *__restrict__ ev_off, const int *__restrict__ blocks, double *__restrict__ refl,
+             double *__restrict__ td, double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    constexpr int NW = TRD_THREADS / 32;
+    const int C = (int)cl.num_blocks(), r = (int)cl.block_rank();
+    const int q = blocks[blockIdx.x / C];
+    const int n = dims[q], eo = ev_off[q];
+    const int ncmax = (n + C - 1) / C, ncol = r < n ? (n - r + C - 1) / C : 0;
+    extern __shared__ double trc_smem[];
+    double *A = trc_smem, *v = A + (size_t)ncmax * n, *w = v + n, *pbuf = w + n, *vbuf = pbuf + 2 * ncmax,
+           *sbuf = vbuf + 2 * n;
+    __shared__ double red[NW];
+    __shared__ double kk;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const double *R = rho + rho_off[q];
+    double *Vq = refl + rho_off[q];
+    for (int e = tid; e < ncol * n; e += TRD_THREADS) {
+        const int jj = e / n, i = e - jj * n;
+        A[(size_t)jj * n + i] = R[(int64_t)(r + C * jj) * n + i];     // column j = row j (symmetric)
+    }
+    if (r == 0)
+        for (int i = tid; i < n; i += TRD_THREADS) perm[eo + i] = i;
+    cl.sync();
+    for (int k = 0; k + 2 < n; ++k) {
+        const int m = n - k - 1, par = k & 1, o = k % C;
+        double *vb = vbuf + par * n, *pb = pbuf + par * ncmax, *sb = sbuf + par * 4;
+        if (r == o) {
+            const double *colk = A + (size_t)(k / C) * n;
+            if (warp == 0) {
+                double ss = 0.0;
+                for (int i = k + 2 + lane; i < n; i += 32) ss = fma(colk[i], colk[i], ss);
+                ss = wsum(ss);
+                if (lane == 0) {
+                    const double alpha = colk[k + 1];
+                    double t = 0.0, beta = alpha, scal = 0.0;
+                    if (ss > 0.0) {
+                        beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
+                        t = (beta - alpha) / beta;
+                        scal = 1.0 / (alpha - beta);
+                    }
+                    sb[0] = t;
+                    sb[1] = scal;
+                    td[eo + k] = colk[k];
+                    te[eo + k] = beta;
+                    tau[eo + k] = t;
+                }
+            }
+            __syncthreads();
+            const double scal = sb[1];
+            for (int i = tid; i < m; i += TRD_THREADS) {
+                const double x = (i == 0) ? 1.0 : colk[k + 1 + i] * scal;
+                vb[i] = x;
+                Vq[(int64_t)k * n + k + 1 + i] = x;
+            }
+        }
+        cl.sync();                                   // v and tau of step k published
+        const double t = cl.map_shared_rank(sb, o)[0];
+        const double *rv = cl.map_shared_rank(vb, o);
+        for (int i = tid; i < m; i += TRD_THREADS) v[i] = rv[i];
+        __syncthreads();
+        const int jj0 = k + 1 > r ? (k + 1 - r + C - 1) / C : 0;   // first column j = r + C jj > k
+        double sp = 0.0;
+        if (t != 0.0)
+            for (int jj = jj0 + warp; jj < ncol; jj += NW) {
+                const double *a = A + (size_t)jj * n + k + 1;
+                double a0 = 0.0, a1 = 0.0;
+                int i = lane;
+                for (; i + 32 < m; i += 64) {
+                    a0 = fma(a[i], v[i], a0);
+                    a1 = fma(a[i + 32], v[i + 32], a1);
+                }
+                if (i < m) a0 = fma(a[i], v[i], a0);
+                const double pj = t * wsum(a0 + a1);
+                if (lane == 0) pb[jj] = pj;
+                sp = fma(pj, v[r + C * jj - k - 1], sp);
+            }
+        if (lane == 0) red[warp] = sp;
+        __syncthreads();
+        if (tid == 0) {
+            double x = 0.0;
+            for (int u = 0; u < NW; ++u) x += red[u];
+            sb[2] = x;
+        }
+        cl.sync();                                   // p and the p.v shares published
+        if (warp == 0) {
+            double x = lane < C ? cl.map_shared_rank(sb, lane)[2] : 0.0;
+            x = wsum(x);
+            if (lane == 0) kk = -0.5 * t * x;
+        }
+        __syncthreads();
+        const double K = kk;
+        if (t != 0.0)
+            for (int i = tid; i < m; i += TRD_THREADS) {
+                const int g = k + 1 + i;
+                w[i] = fma(K, v[i], cl.map_shared_rank(pb, g % C)[g / C]);
+            }
+        __syncthreads();
+        if (t != 0.0)
+            for (int jj = jj0 + warp; jj < ncol; jj += NW) {
+                const int jc = r + C * jj - k - 1;
+                const double vj = v[jc], wj = w[jc];
+                double *a = A + (size_t)jj * n + k + 1;
+                for (int i = lane; i < m; i += 32) a[i] -= fma(v[i], wj, w[i] * vj);
+            }
+        __syncthreads();
+    }
+    if (n >= 2 && r == (n - 2) % C && tid == 0) {
+        const double *c2 = A + (size_t)((n - 2) / C) * n;
+        td[eo + n - 2] = c2[n - 2];
+        te[eo + n - 2] = c2[n - 1];
+        tau[eo + n - 2] = 0.0;
+    }
+    if (r == (n - 1) % C && tid == 0) {
+        td[eo + n - 1] = A[(size_t)((n - 1) / C) * n + n - 1];
+        te[eo + n - 1] = 0.0;
+        tau[eo + n - 1] = 0.0;
+    }
+    cl.sync();                                       // no CTA leaves while its memory may be read
 }
 
 // Blocks above SYEV_MAX are reduced by the library's blocked tridiagonal
@@ -921,6 +1057,68 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
     if (e != cudaSuccess) return (int)e;
     k_trd<<<nblocks, TRD_THREADS, smem, st>>>(rho, rho_off, dims, ev_off, blocks, refl, td, te, tau, perm);
     return (int)cudaGetLastError();
+}
+
+// cluster size for k_trd_cl (16 where the device allows non-portable
+// clusters of that size with this shared memory, else 8) and the largest
+// block it takes
+int syev_trd_cl_size(int *nmax_out) {
+    static int csize = 0, nmax = 0;
+    if (!csize) {
+        cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        const int smem = 200 * 1024;
+        cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(TRD_THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        csize = (cudaOccupancyMaxActiveClusters(&nc, k_trd_cl, &cfg) == cudaSuccess && nc > 0) ? 16 : 8;
+        cudaGetLastError();
+        // (ncmax + 4) n doubles within 200 KB
+        nmax = 64;
+        while (true) {
+            const int nn = nmax + 1, nc2 = (nn + csize - 1) / csize;
+            if ((size_t)((nc2 + 4) * (size_t)nn + 2 * nc2 + 8) * sizeof(double) > 200u * 1024u) break;
+            nmax = nn;
+        }
+    }
+    if (nmax_out) *nmax_out = nmax;
+    return csize;
+}
+
+int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
+                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm,
+                cudaStream_t st) {
+    if (nblocks <= 0) return 0;
+    int nmax = 0;
+    const int C = syev_trd_cl_size(&nmax);
+    if (maxn > nmax) return (int)cudaErrorInvalidValue;
+    const int ncmax = (maxn + C - 1) / C;
+    const size_t smem = ((size_t)(ncmax + 4) * maxn + 2 * ncmax + 8) * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(nblocks * C);
+    cfg.blockDim = dim3(TRD_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_trd_cl, rho, rho_off, dims, ev_off, blocks, refl, td, te, tau, perm);
+    return (int)e;
 }
 
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
