@@ -231,6 +231,8 @@ def measure_sweeps(nss, device, case=None, warm=True):
                                         "nnz_ops": statistics.mean(r["nnz_ops"] for r in fin),
                                         "rdm_fallback_blocks": sum(r["rdm_fallback_blocks"] for r in fin),
                                         "rdm_own_blocks": sum(r["rdm_own_blocks"] for r in fin),
+                                        "rdm_phases": [statistics.mean(r["rdm_phase_ms"][i] for r in fin)
+                                                       for i in range(6)],
                                         "numop": statistics.mean(r["numop"] for r in fin),
                                         "N_max": max(r["n"] for r in fin)}}
     out.update(res)

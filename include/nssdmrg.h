@@ -322,6 +322,11 @@ typedef struct {
     int32_t rdm_own_blocks;     /* rho blocks on the own eigensolver ... */
     int32_t rdm_fallback_blocks;/* ... and those whose kept vectors the library recomputed */
     double  sn_left, sc_left, sn_right, sc_right;   /* S_N, S_c per side (SN_ScVSblock.length) */
+    double  rdm_phase_ms[6];/* device time of the RDM phases: rho build, tridiagonal
+                               reductions, eigenvalues, truncation, kept vectors, U */
+    int32_t rdm_path_blocks[4]; /* rho blocks per eigensolver tier: one CTA, cluster,
+                                   blocked library reduction, library eigensolver */
+    int32_t rdm_max_block;      /* largest rho block */
 } nss_step_record;
 
 typedef struct nss_dmrg nss_dmrg;

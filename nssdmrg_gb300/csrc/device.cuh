@@ -138,10 +138,10 @@ struct DevRdm {
     int64_t cap_htab = 0;
     double *hu = nullptr;            // pinned staging of the compact kept columns
     int64_t cap_hu = 0;
-    double *big = nullptr;           // blocked library reductions: block copies + workspaces
+    static constexpr int NPH = 7;    // phase events of the last call (see rdm_phase_ms)
+    cudaEvent_t ph[NPH] = {};
+    double *big = nullptr;           // global copies of the blocks the cluster kernel reduces in place
     int64_t cap_big = 0;
-    int *big_info = nullptr;
-    int64_t cap_big_info = 0;
 };
 
 // Operator renormalisation on the device (k_renorm.cu): grow-only buffers
@@ -197,6 +197,14 @@ struct Ctx {
     // below 32 eps, Rayleigh iteration unsettled, Gram-Schmidt remainder,
     // cluster too large
     int64_t rdm_fail_why[5] = {0, 0, 0, 0, 0};
+    // device time of the last nss_rdm's phases: rho build + symmetry check,
+    // tridiagonal reductions, eigenvalues (+ library blocks), truncation,
+    // kept vectors (+ fallbacks), compact U
+    double rdm_phase_ms[6] = {0, 0, 0, 0, 0, 0};
+    // blocks per eigensolver tier (one CTA, cluster, blocked library
+    // reduction, library eigensolver) and the largest block, last call
+    int rdm_path_blocks[4] = {0, 0, 0, 0};
+    int rdm_max_block = 0;
 };
 
 // Allocation through the context budget.
@@ -250,11 +258,15 @@ void lanczos_release(Ctx &c);
 
 // k_syev.cu: FP64 eigensolver of the rho blocks.  Blocks up to SYEV_MAX
 // are reduced to tridiagonal form in one CTA (k_trd); larger ones, up to
-// SYEV_BIG_MAX, by the library's blocked reduction (k_big_prep adapts its
-// output); the eigenvalues and kept vectors of both come from k_bisect and
-// k_vec.
+// SYEV_BIG_MAX, by a thread-block cluster (k_trd_cl, the block in the
+// cluster's shared memory or in a global copy); the eigenvalues and kept
+// vectors of all come from k_bisect and k_vec.
 constexpr int SYEV_MAX = 160;
-constexpr int SYEV_BIG_MAX = 2048;
+// k_vec keeps 7 x n doubles per warp in shared memory.  (The cluster's 16
+// SMs bound the largest blocks, n^3/16 FP64 FMAs each: 0.5 s at n = 2645,
+// the noise-level truncation blocks of the spin-1 m=512 sweep; the
+// library's blocked solver measured 0.5-2.2 s there.)
+constexpr int SYEV_BIG_MAX = 3500;
 int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
              int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, cudaStream_t st);
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
@@ -263,11 +275,12 @@ int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitem
 // clusters of 8 or 16 CTAs per block (k_trd_cl); the size and the largest
 // block it takes
 int syev_trd_cl_size(int *nmax);
+// gA (may be null): global column-major scratch for blocks too large for the
+// cluster's shared memory, block b at gA + goff[b] (goff on the device)
 int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
-                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm,
-                cudaStream_t st);
-int syev_big_prep(const double *A, int n, int64_t roff, int eo, double *refl, double *te, double *tau, int *perm,
-                  cudaStream_t st);
+                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, double *gA,
+                const int64_t *goff, cudaStream_t st);
+
 // kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions
 // start at nl): k_vec + the cluster Gram-Schmidt, two launches
 int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,

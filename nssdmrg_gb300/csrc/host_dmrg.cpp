@@ -384,6 +384,9 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     cudaEventDestroy(em);
     rec.ms_solve = ms;
     rec.ms_eigh = ms_e;
+    for (int i = 0; i < 6; ++i) rec.rdm_phase_ms[i] = c.rdm_phase_ms[i];
+    for (int i = 0; i < 4; ++i) rec.rdm_path_blocks[i] = c.rdm_path_blocks[i];
+    rec.rdm_max_block = c.rdm_max_block;
     rec.rdm_own_blocks = c.rdm_own_blocks;
     rec.rdm_fallback_blocks = c.rdm_fallback_blocks;
     rec.numop = numop;

@@ -293,6 +293,11 @@ constexpr int JAC_DEFAULT = 32;
 
 // blocks up to this size take k_jacobi (env NSS_JACOBI_MAX, 0..JAC_MAX, default
 // 32; 0 sends every block to the batched library eigensolver)
+// padded size classes from this size on go one matrix at a time through the
+// library's blocked solver (all SMs) instead of its batched one (one CTA
+// per matrix, seconds at these sizes)
+constexpr int LIB_WHOLE_GPU_N = 1024;
+
 int jacobi_max() {
     static const int v = [] {
         const char *e = std::getenv("NSS_JACOBI_MAX");
@@ -509,7 +514,7 @@ int ensure_n(Ctx &c, T **p, int64_t &cap, int64_t need) {
 void rdm_release(Ctx &c) {
     DevRdm &r = c.rdm;
     void *ptrs[] = {r.rho, r.evals, r.sorted, r.order, r.u, r.work, r.info, r.scal, r.iscal, r.bat, r.bat_info,
-                    r.vec, r.syd, r.syi, r.tab, r.big, r.big_info};
+                    r.vec, r.syd, r.syi, r.tab, r.big};
     for (void *p : ptrs) ctx_free(c, p);
     if (r.htab) cudaFreeHost(r.htab);
     if (r.hu) cudaFreeHost(r.hu);
@@ -518,6 +523,8 @@ void rdm_release(Ctx &c) {
         if (r.ev_join[i]) cudaEventDestroy(r.ev_join[i]);
     }
     if (r.ev_fork) cudaEventDestroy(r.ev_fork);
+    for (int i = 0; i < DevRdm::NPH; ++i)
+        if (r.ph[i]) cudaEventDestroy(r.ph[i]);
     if (r.params) cusolverDnDestroyParams((cusolverDnParams_t)r.params);
     r = DevRdm{};
 }
@@ -565,10 +572,12 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // own: one CTA per block up to SYEV_MAX states (k_trd, with the
     // component reordering; measured faster than a cluster at 120 states),
     // clu: a thread-block cluster per block up to the size its shared memory
-    // holds (k_trd_cl; env NSS_TRD_CLUSTER=0 disables it), big: the
-    // library's blocked reduction
+    // holds (k_trd_cl; env NSS_TRD_CLUSTER=0 disables it), big: the same
+    // cluster kernel on a global (L2-resident) copy of the block, up to
+    // SYEV_BIG_MAX; larger blocks take the library eigensolver
     int cl_nmax = 0;
     syev_trd_cl_size(&cl_nmax);
+    if (const char *sm = std::getenv("NSS_TRD_CL_SHARED_MAX")) cl_nmax = std::min(cl_nmax, std::atoi(sm));
     const char *tce = std::getenv("NSS_TRD_CLUSTER");
     const bool use_cl = !(tce && std::string(tce) == "0");
     const int cta_max = SYEV_MAX;
@@ -581,8 +590,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         } else if (own_path && use_cl && dims[q] <= cl_nmax) {
             clu.push_back(q);
             maxn_clu = std::max(maxn_clu, dims[q]);
-        } else if (own_path && dims[q] <= SYEV_BIG_MAX) {
-            big.push_back(q);
+        } else if (own_path && use_cl && dims[q] <= SYEV_BIG_MAX) {
+            big.push_back(q);                        // the cluster kernel on a global copy
         } else if (dims[q] <= jmax) {
             small.push_back(q);
         } else {
@@ -644,6 +653,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
                  o_dims = slot(dims.size() * sizeof(int)), o_ev_off = slot(ev_off.size() * sizeof(int)),
                  o_maps = slot(maps.size() * sizeof(int)), o_map_off = slot(map_off.size() * sizeof(int)),
                  o_own = slot(own.size() * sizeof(int)), o_clu = slot(clu.size() * sizeof(int)),
+                 o_big = slot(big.size() * sizeof(int)), o_goff = slot(big.size() * sizeof(int64_t)),
                  o_bis = slot(bis.size() * sizeof(int2)),
                  o_bmode = slot(bmode.size() * sizeof(int)), o_kept = slot(4 * (size_t)kmax * sizeof(int));
     if (!r.htab || r.cap_htab < (int64_t)tot) {
@@ -664,6 +674,14 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     put(o_map_off, map_off);
     put(o_own, own);
     put(o_clu, clu);
+    put(o_big, big);
+    std::vector<int64_t> goff(big.size());
+    int64_t gneed = 0;
+    for (size_t b = 0; b < big.size(); ++b) {
+        goff[b] = gneed;
+        gneed += (int64_t)dims[big[b]] * dims[big[b]];
+    }
+    put(o_goff, goff);
     put(o_bis, bis);
     put(o_bmode, bmode);
     NSS_CUDA_TRY(c, cudaMemcpyAsync(r.tab, r.htab, o_kept, cudaMemcpyHostToDevice, st));
@@ -672,7 +690,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     const int *d_dims = (const int *)(r.tab + o_dims), *d_ev_off = (const int *)(r.tab + o_ev_off),
               *d_maps = (const int *)(r.tab + o_maps), *d_map_off = (const int *)(r.tab + o_map_off),
               *d_own = (const int *)(r.tab + o_own), *d_bmode = (const int *)(r.tab + o_bmode),
-              *d_clu = (const int *)(r.tab + o_clu);
+              *d_clu = (const int *)(r.tab + o_clu), *d_big = (const int *)(r.tab + o_big);
+    const int64_t *d_goff = (const int64_t *)(r.tab + o_goff);
     const int2 *d_bis = (const int2 *)(r.tab + o_bis);
     int *d_kept = (int *)(r.tab + o_kept);
     std::vector<void *> temps;
@@ -680,11 +699,15 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         cudaStreamSynchronize(st);
         for (void *p : temps) ctx_free(c, p);
     };
+    if (!r.ph[0])
+        for (int i = 0; i < DevRdm::NPH; ++i) NSS_CUDA_TRY(c, cudaEventCreate(&r.ph[i]));
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[0], st));
     ++c.launches;
     k_rho<<<(int)items.size(), 256, 0, st>>>(d_psi, d_items, s.d_dls, s.d_drs, s.d_off, d_rho_off, nsb, r.rho);
     NSS_CUDA_TRY(c, cudaMemsetAsync(r.iscal, 0, 8 * sizeof(int), st));
     ++c.launches;
     k_symcheck<<<std::min(nblk, 304), 256, 0, st>>>(r.rho, acc, d_rho_off, d_dims, nblk, r.iscal + 7);
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[1], st));
     cusolverDnHandle_t h = (cusolverDnHandle_t)c.solver;
     auto make_side_streams = [&]() -> int {
         if (!r.ev_fork) {
@@ -697,59 +720,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         return NSS_OK;
     };
     if (!path.empty()) NSS_CUDA_TRY(c, cudaMemsetAsync(flags, 0, nblk * sizeof(int), st));
-    if (!big.empty()) {
-        // blocked library reductions of the big blocks on the side streams
-        if ((rc = make_side_streams())) { cleanup(); return rc; }
-        std::vector<int64_t> aoff(big.size()), woff(big.size());
-        int64_t bneed = 0;
-        for (size_t b = 0; b < big.size(); ++b) {
-            const int q = big[b], n = dims[q];
-            int lw = 0;
-            if (cusolverDnDsytrd_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, r.rho, n, td, te, tau, &lw) !=
-                CUSOLVER_STATUS_SUCCESS) {
-                cleanup();
-                c.err = "nss_rdm: cusolverDnDsytrd_bufferSize failed";
-                return NSS_ERR_CUDA;
-            }
-            aoff[b] = bneed;
-            bneed += (int64_t)n * n;
-            woff[b] = bneed;
-            bneed += lw + 8;
-        }
-        if ((rc = ensure_n(c, &r.big, r.cap_big, bneed))) { cleanup(); return rc; }
-        if ((rc = ensure_n(c, &r.big_info, r.cap_big_info, (int64_t)big.size()))) { cleanup(); return rc; }
-        NSS_CUDA_TRY(c, cudaEventRecord(r.ev_fork, st));
-        for (int i = 0; i < DevRdm::NSIDE; ++i) NSS_CUDA_TRY(c, cudaStreamWaitEvent(r.side[i], r.ev_fork, 0));
-        for (size_t b = 0; b < big.size(); ++b) {
-            const int q = big[b], n = dims[q], eo = ev_off[q];
-            cudaStream_t ss = r.side[b % DevRdm::NSIDE];
-            double *A = r.big + aoff[b];
-            NSS_CUDA_TRY(c, cudaMemcpyAsync(A, r.rho + rho_off[q], (size_t)n * n * sizeof(double),
-                                            cudaMemcpyDeviceToDevice, ss));
-            cusolverDnSetStream(h, ss);
-            const cusolverStatus_t cs =
-                cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, A, n, td + eo, te + eo, tau + eo, r.big + woff[b],
-                                 (int)(aoff.size() > b + 1 ? aoff[b + 1] - woff[b] - 8 : bneed - woff[b] - 8),
-                                 r.big_info + b);
-            cusolverDnSetStream(h, st);
-            if (cs != CUSOLVER_STATUS_SUCCESS) {
-                cleanup();
-                c.err = "nss_rdm: cusolverDnDsytrd failed";
-                return NSS_ERR_CUDA;
-            }
-            ++c.launches;
-            const int e = syev_big_prep(A, n, rho_off[q], eo, refl, te, tau, perm, ss);
-            if (e) {
-                cleanup();
-                c.err = std::string("nss_rdm: eigensolver launch failed: ") + cudaGetErrorString((cudaError_t)e);
-                return NSS_ERR_CUDA;
-            }
-        }
-        for (int i = 0; i < DevRdm::NSIDE; ++i) {
-            NSS_CUDA_TRY(c, cudaEventRecord(r.ev_join[i], r.side[i]));
-            NSS_CUDA_TRY(c, cudaStreamWaitEvent(st, r.ev_join[i], 0));
-        }
-    }
+    if (!big.empty())
+        if ((rc = ensure_n(c, &r.big, r.cap_big, gneed))) { cleanup(); return rc; }
     if (!path.empty()) {
         int e = 0;
         if (!own.empty()) {
@@ -760,8 +732,16 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         if (!e && !clu.empty()) {
             ++c.launches;
             e = syev_trd_cl(r.rho, d_rho_off, d_dims, d_ev_off, d_clu, (int)clu.size(), maxn_clu, refl, td, te, tau,
-                            perm, st);
+                            perm, nullptr, nullptr, st);
         }
+        if (!e && !big.empty()) {
+            int maxn_big = 1;
+            for (int q : big) maxn_big = std::max(maxn_big, dims[q]);
+            ++c.launches;
+            e = syev_trd_cl(r.rho, d_rho_off, d_dims, d_ev_off, d_big, (int)big.size(), maxn_big, refl, td, te, tau,
+                            perm, r.big, d_goff, st);
+        }
+        if (!e) e = (int)cudaEventRecord(r.ph[2], st);
         ++c.launches;
         if (!e) e = syev_bisect(d_dims, d_ev_off, d_bis, (int)bis.size(), td, te, r.evals, ldd, ldl, bscale, bsig,
                                 flags, sub, maxn_path, st);
@@ -807,9 +787,19 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             cl.list_off = (int64_t)lists.size();
             lists.insert(lists.end(), kv.second.begin(), kv.second.end());
             size_t wd = 0, wh = 0;
-            if (cusolverDnXsyevBatched_bufferSize(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
-                                                  CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, r.rho, cl.N, CUDA_R_64F,
-                                                  r.evals, CUDA_R_64F, &wd, &wh, cl.batch) != CUSOLVER_STATUS_SUCCESS) {
+            if (cl.N >= LIB_WHOLE_GPU_N) {
+                // one matrix at a time through the blocked whole-GPU solver
+                int lw = 0;
+                if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, r.rho,
+                                                cl.N, r.evals, &lw) != CUSOLVER_STATUS_SUCCESS) {
+                    c.err = "nss_rdm: cusolverDnDsyevd_bufferSize failed";
+                    return NSS_ERR_CUDA;
+                }
+                wd = (size_t)lw * sizeof(double);
+            } else if (cusolverDnXsyevBatched_bufferSize(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
+                                                         CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, r.rho, cl.N,
+                                                         CUDA_R_64F, r.evals, CUDA_R_64F, &wd, &wh, cl.batch) !=
+                       CUSOLVER_STATUS_SUCCESS) {
                 c.err = "nss_rdm: cusolverDnXsyevBatched_bufferSize failed";
                 return NSS_ERR_CUDA;
             }
@@ -840,10 +830,18 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             c.launches += 2;
             k_pack<<<cl.batch, 256, 0, ss>>>(r.rho, d_rho_off, d_dims, d_list + cl.list_off, cl.N, A);
             cusolverDnSetStream(h, ss);
-            const cusolverStatus_t cs = cusolverDnXsyevBatched(
-                h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F,
-                A, cl.N, CUDA_R_64F, W, CUDA_R_64F, ws, cl.ws, cl.hws.data(), cl.hws.size() - 16,
-                r.bat_info + info_off, cl.batch);
+            cusolverStatus_t cs = CUSOLVER_STATUS_SUCCESS;
+            if (cl.N >= LIB_WHOLE_GPU_N) {
+                for (int b = 0; b < cl.batch && cs == CUSOLVER_STATUS_SUCCESS; ++b)
+                    cs = cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N,
+                                          A + (int64_t)b * cl.N * cl.N, cl.N, W + (int64_t)b * cl.N, ws,
+                                          (int)(cl.ws / sizeof(double)), r.bat_info + info_off + b);
+            } else {
+                cs = cusolverDnXsyevBatched(h, (cusolverDnParams_t)r.params, CUSOLVER_EIG_MODE_VECTOR,
+                                            CUBLAS_FILL_MODE_LOWER, cl.N, CUDA_R_64F, A, cl.N, CUDA_R_64F, W,
+                                            CUDA_R_64F, ws, cl.ws, cl.hws.data(), cl.hws.size() - 16,
+                                            r.bat_info + info_off, cl.batch);
+            }
             cusolverDnSetStream(h, st);
             if (cs != CUSOLVER_STATUS_SUCCESS) {
                 c.err = "nss_rdm: cusolverDnXsyevBatched failed";
@@ -868,11 +866,19 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         }
         return NSS_OK;
     };
+    if (path.empty()) NSS_CUDA_TRY(c, cudaEventRecord(r.ph[2], st));
     if ((rc = lib_eigh(small, large, true, r.vec))) {
         cleanup();
         return rc;
     }
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[3], st));
     c.rdm_own_blocks = (int)path.size();
+    c.rdm_path_blocks[0] = (int)own.size();
+    c.rdm_path_blocks[1] = (int)clu.size();
+    c.rdm_path_blocks[2] = (int)big.size();
+    c.rdm_path_blocks[3] = (int)(small.size() + large.size());
+    c.rdm_max_block = 0;
+    for (int d : dims) c.rdm_max_block = std::max(c.rdm_max_block, d);
     c.rdm_lib_blocks = (int)(small.size() + large.size());
     c.rdm_fallback_blocks = 0;
     ++c.launches;
@@ -891,6 +897,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
                                      r.iscal + side);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[4], st));
     double hs[8];
     int hi[8];
     NSS_CUDA_TRY(c, cudaMemcpyAsync(hs, r.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -963,6 +970,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             NSS_CUDA_TRY(c, cudaGetLastError());
         }
     }
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[5], st));
     // kept columns, compact (no zero rows) -> pinned staging -> the dense
     // m_block x m_s host matrices (zero rows outside each column's block)
     NSS_CUDA_TRY(c, cudaGetLastError());
@@ -1040,7 +1048,13 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             for (int p = 0; p < nq; ++p) dst[mp[p]] = src[p];
         }
     }
+    NSS_CUDA_TRY(c, cudaEventRecord(r.ph[6], st));
     cleanup();
+    for (int i = 0; i + 1 < DevRdm::NPH; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.ph[i], r.ph[i + 1]);
+        c.rdm_phase_ms[i] = ms;
+    }
     return NSS_OK;
 }
 

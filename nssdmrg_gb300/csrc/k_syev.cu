@@ -237,20 +237,30 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
 // columns.  Two cluster barriers a step, the FP64 work spread over C SMs.
 // The buffers that cross CTAs alternate with the parity of k, so a
 // barrier always separates a buffer's writes from the previous step's reads.
+// GLOBAL: the block's columns live in a global (L2-resident) copy instead
+// of the cluster's shared memory, for blocks too large for it; gA + goff[b]
+// is block b's n x n column-major scratch.
+template <bool GLOBAL>
 __global__ void __launch_bounds__(TRD_THREADS, 1)
     k_trd_cl(const double *__restrict__ rho, const int64_t *__restrict__ rho_off, const int *__restrict__ dims,
              const int *__restrict__ ev_off, const int *__restrict__ blocks, double *__restrict__ refl,
-             double *__restrict__ td, double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm) {
+             double *__restrict__ td, double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm,
+             double *__restrict__ gA, const int64_t *__restrict__ goff) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     constexpr int NW = TRD_THREADS / 32;
     const int C = (int)cl.num_blocks(), r = (int)cl.block_rank();
-    const int q = blocks[blockIdx.x / C];
+    const int bq = blockIdx.x / C;
+    const int q = blocks[bq];
     const int n = dims[q], eo = ev_off[q];
     const int ncmax = (n + C - 1) / C, ncol = r < n ? (n - r + C - 1) / C : 0;
     extern __shared__ double trc_smem[];
-    double *A = trc_smem, *v = A + (size_t)ncmax * n, *w = v + n, *pbuf = w + n, *vbuf = pbuf + 2 * ncmax,
-           *sbuf = vbuf + 2 * n;
+    double *const G = GLOBAL ? gA + goff[bq] : nullptr;
+    double *const As = trc_smem;
+    // local column jj = global column r + C jj
+    auto colp = [&](int jj) -> double * { return GLOBAL ? G + (int64_t)(r + C * jj) * n : As + (size_t)jj * n; };
+    double *v = GLOBAL ? trc_smem : As + (size_t)ncmax * n;
+    double *w = v + n, *pbuf = w + n, *vbuf = pbuf + 2 * ncmax, *sbuf = vbuf + 2 * n;
     __shared__ double red[NW];
     __shared__ double kk;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -258,8 +268,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     double *Vq = refl + rho_off[q];
     for (int e = tid; e < ncol * n; e += TRD_THREADS) {
         const int jj = e / n, i = e - jj * n;
-        A[(size_t)jj * n + i] = R[(int64_t)(r + C * jj) * n + i];     // column j = row j (symmetric)
+        colp(jj)[i] = R[(int64_t)(r + C * jj) * n + i];     // column j = row j (symmetric)
     }
+    if (GLOBAL) __threadfence_block();
     if (r == 0)
         for (int i = tid; i < n; i += TRD_THREADS) perm[eo + i] = i;
     cl.sync();
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         const int m = n - k - 1, par = k & 1, o = k % C;
         double *vb = vbuf + par * n, *pb = pbuf + par * ncmax, *sb = sbuf + par * 4;
         if (r == o) {
-            const double *colk = A + (size_t)(k / C) * n;
+            const double *colk = colp(k / C);
             if (warp == 0) {
                 double ss = 0.0;
                 for (int i = k + 2 + lane; i < n; i += 32) ss = fma(colk[i], colk[i], ss);
@@ -304,7 +315,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         double sp = 0.0;
         if (t != 0.0)
             for (int jj = jj0 + warp; jj < ncol; jj += NW) {
-                const double *a = A + (size_t)jj * n + k + 1;
+                const double *a = colp(jj) + k + 1;
                 double a0 = 0.0, a1 = 0.0;
                 int i = lane;
                 for (; i + 32 < m; i += 64) {
@@ -341,49 +352,23 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
             for (int jj = jj0 + warp; jj < ncol; jj += NW) {
                 const int jc = r + C * jj - k - 1;
                 const double vj = v[jc], wj = w[jc];
-                double *a = A + (size_t)jj * n + k + 1;
+                double *a = colp(jj) + k + 1;
                 for (int i = lane; i < m; i += 32) a[i] -= fma(v[i], wj, w[i] * vj);
             }
         __syncthreads();
     }
     if (n >= 2 && r == (n - 2) % C && tid == 0) {
-        const double *c2 = A + (size_t)((n - 2) / C) * n;
+        const double *c2 = colp((n - 2) / C);
         td[eo + n - 2] = c2[n - 2];
         te[eo + n - 2] = c2[n - 1];
         tau[eo + n - 2] = 0.0;
     }
     if (r == (n - 1) % C && tid == 0) {
-        td[eo + n - 1] = A[(size_t)((n - 1) / C) * n + n - 1];
+        td[eo + n - 1] = colp((n - 1) / C)[n - 1];
         te[eo + n - 1] = 0.0;
         tau[eo + n - 1] = 0.0;
     }
     cl.sync();                                       // no CTA leaves while its memory may be read
-}
-
-// Blocks above SYEV_MAX are reduced by the library's blocked tridiagonal
-// reduction (LAPACK dsytrd layout, lower: T's diagonal and subdiagonal in
-// d and e, reflector k with v[k+1] = 1 implicit and v[k+2..] in column k of
-// A below the subdiagonal).  This copies the reflectors into the layout
-// k_vec reads (column k of the block's refl slot, v[k+1] = 1 explicit),
-// closes the T and tau arrays and sets the identity row order.
-__global__ void __launch_bounds__(256) k_big_prep(const double *__restrict__ A, int n, int64_t roff, int eo,
-                                                  double *__restrict__ refl, double *__restrict__ te,
-                                                  double *__restrict__ tau, int *__restrict__ perm) {
-    double *V = refl + roff;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n * n;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(e / n), i = (int)(e - (int64_t)k * n);
-        double x = 0.0;
-        if (k + 2 < n) x = i == k + 1 ? 1.0 : (i > k + 1 ? A[e] : 0.0);
-        V[e] = x;
-    }
-    if (blockIdx.x == 0)
-        for (int i = threadIdx.x; i < n; i += blockDim.x) perm[eo + i] = i;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        te[eo + n - 1] = 0.0;
-        tau[eo + n - 1] = 0.0;
-        if (n >= 2) tau[eo + n - 2] = 0.0;
-    }
 }
 
 // Number of eigenvalues of the scaled T below s (a: diagonal, bb[i] =
@@ -1065,9 +1050,10 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
 int syev_trd_cl_size(int *nmax_out) {
     static int csize = 0, nmax = 0;
     if (!csize) {
-        cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_trd_cl<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(k_trd_cl<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         const int smem = 200 * 1024;
-        cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(k_trd_cl<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1080,7 +1066,7 @@ int syev_trd_cl_size(int *nmax_out) {
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int nc = 0;
-        csize = (cudaOccupancyMaxActiveClusters(&nc, k_trd_cl, &cfg) == cudaSuccess && nc > 0) ? 16 : 8;
+        csize = (cudaOccupancyMaxActiveClusters(&nc, k_trd_cl<false>, &cfg) == cudaSuccess && nc > 0) ? 16 : 8;
         cudaGetLastError();
         // (ncmax + 4) n doubles within 200 KB
         nmax = 64;
@@ -1095,15 +1081,17 @@ int syev_trd_cl_size(int *nmax_out) {
 }
 
 int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
-                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm,
-                cudaStream_t st) {
+                int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, double *gA,
+                const int64_t *goff, cudaStream_t st) {
     if (nblocks <= 0) return 0;
     int nmax = 0;
     const int C = syev_trd_cl_size(&nmax);
-    if (maxn > nmax) return (int)cudaErrorInvalidValue;
+    const bool glob = gA != nullptr;
+    if (!glob && maxn > nmax) return (int)cudaErrorInvalidValue;
     const int ncmax = (maxn + C - 1) / C;
-    const size_t smem = ((size_t)(ncmax + 4) * maxn + 2 * ncmax + 8) * sizeof(double);
-    cudaError_t e = cudaFuncSetAttribute(k_trd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = ((size_t)(glob ? 4 : ncmax + 4) * maxn + 2 * ncmax + 8) * sizeof(double);
+    auto kern = glob ? k_trd_cl<true> : k_trd_cl<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
@@ -1117,7 +1105,7 @@ int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, cons
     cfg.stream = st;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, k_trd_cl, rho, rho_off, dims, ev_off, blocks, refl, td, te, tau, perm);
+    e = cudaLaunchKernelEx(&cfg, kern, rho, rho_off, dims, ev_off, blocks, refl, td, te, tau, perm, gA, goff);
     return (int)e;
 }
 
@@ -1133,12 +1121,6 @@ int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitem
     return (int)cudaGetLastError();
 }
 
-int syev_big_prep(const double *A, int n, int64_t roff, int eo, double *refl, double *te, double *tau, int *perm,
-                  cudaStream_t st) {
-    const int grid = (int)std::min<int64_t>(((int64_t)n * n + 255) / 256, 304);
-    k_big_prep<<<grid, 256, 0, st>>>(A, n, roff, eo, refl, te, tau, perm);
-    return (int)cudaGetLastError();
-}
 
 int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
              const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
