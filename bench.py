@@ -233,6 +233,11 @@ def measure_sweeps(nss, device, case=None, warm=True):
                                         "rdm_own_blocks": sum(r["rdm_own_blocks"] for r in fin),
                                         "rdm_phases": [statistics.mean(r["rdm_phase_ms"][i] for r in fin)
                                                        for i in range(6)],
+                                        "host_phases": dict(zip(
+                                            ("enlarge", "sb_build", "upload", "renorm_extract",
+                                             "renorm_device_wait", "renorm_assemble"),
+                                            (statistics.mean(r["host_phase_ms"][i] for r in fin)
+                                             for i in range(6)))),
                                         "numop": statistics.mean(r["numop"] for r in fin),
                                         "N_max": max(r["n"] for r in fin)}}
     out.update(res)

@@ -327,6 +327,11 @@ typedef struct {
     int32_t rdm_path_blocks[4]; /* rho blocks per eigensolver tier: one CTA, cluster,
                                    blocked library reduction, library eigensolver */
     int32_t rdm_max_block;      /* largest rho block */
+    double  host_phase_ms[6];   /* host wall time of: the two block enlargements,
+                                   the superblock build, the superblock view and
+                                   upload, the renormalisation's block scan and
+                                   extraction, its wait for the device GEMMs, and
+                                   its CSR assembly of the new operators */
 } nss_step_record;
 
 typedef struct nss_dmrg nss_dmrg;

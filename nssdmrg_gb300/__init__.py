@@ -90,7 +90,8 @@ class StepRecord(C.Structure):
                 ("nnz_u", C.c_int64), ("nnz_ops", C.c_int64), ("rdm_own_blocks", C.c_int32),
                 ("rdm_fallback_blocks", C.c_int32), ("sn_left", C.c_double), ("sc_left", C.c_double),
                 ("sn_right", C.c_double), ("sc_right", C.c_double), ("rdm_phase_ms", C.c_double * 6),
-                ("rdm_path_blocks", C.c_int32 * 4), ("rdm_max_block", C.c_int32)]
+                ("rdm_path_blocks", C.c_int32 * 4), ("rdm_max_block", C.c_int32),
+                ("host_phase_ms", C.c_double * 6)]
 
 
 _lib = None
@@ -574,6 +575,6 @@ class DMRG:
         L.nss_dmrg_records(self._d, arr, n)
         out = []
         for r in arr[:n]:
-            out.append({k: (list(getattr(r, k)) if k in ("energy", "rdm_phase_ms", "rdm_path_blocks") else getattr(r, k))
+            out.append({k: (list(getattr(r, k)) if k in ("energy", "rdm_phase_ms", "rdm_path_blocks", "host_phase_ms") else getattr(r, k))
                         for k, _ in StepRecord._fields_})
         return out

@@ -104,7 +104,7 @@ void nss_destroy(nss_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->c.device);
     cudaStreamSynchronize(ctx->c.stream);
-    nss::sb_release(ctx->c);
+    nss::sb_release(ctx->c, true);
     nss::lanczos_release(ctx->c);
     nss::rdm_release(ctx->c);
     nss::renorm_release(ctx->c);
@@ -131,7 +131,7 @@ int nss_sb_free(nss_ctx *ctx) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     cudaSetDevice(ctx->c.device);
     cudaStreamSynchronize(ctx->c.stream);
-    nss::sb_release(ctx->c);
+    nss::sb_release(ctx->c, true);
     ctx->sbhost.reset();
     return NSS_OK;
 }

@@ -146,7 +146,6 @@ struct DevRdm {
 
 // Operator renormalisation on the device (k_renorm.cu): grow-only buffers
 struct DevRenorm {
-    void *blas = nullptr;        // cublasHandle_t
     double *ublk = nullptr, *dblk = nullptr, *tbuf = nullptr, *rbuf = nullptr;
     int64_t cap_ublk = 0, cap_dblk = 0, cap_tbuf = 0, cap_rbuf = 0;
     int *itab = nullptr;
@@ -205,6 +204,9 @@ struct Ctx {
     // reduction, library eigensolver) and the largest block, last call
     int rdm_path_blocks[4] = {0, 0, 0, 0};
     int rdm_max_block = 0;
+    char *sb_arena = nullptr, *sb_stage = nullptr;   // superblock pool: device arena, pinned staging
+    size_t sb_arena_cap = 0, sb_stage_cap = 0;
+    double renorm_phase_ms[3] = {0, 0, 0};   // host: scan+extract, device wait, CSR assembly (summed over calls)
 };
 
 // Allocation through the context budget.
@@ -224,7 +226,9 @@ void ctx_free(Ctx &c, void *p);
 
 // k_matvec.cu
 int sb_upload(Ctx &c, const nss_sb_desc *d);
-void sb_release(Ctx &c);
+// Drop the pool; free_arena also returns its device arena and pinned
+// staging buffer (otherwise kept for the next upload).
+void sb_release(Ctx &c, bool free_arena);
 // `stop` (may be null): a device flag; the kernels return at once when set
 int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop = nullptr);
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
@@ -299,7 +303,9 @@ void rdm_release(Ctx &c);
 // k_renorm.cu: blk's operators <- U^T O U for the kept columns kl, blk's
 // basis <- kept_qn (one QN tuple per kept column)
 struct Block;
-int renorm_device(Ctx &c, const KeptLayout &kl, Block &blk, const std::vector<std::vector<double>> &kept_qn);
+// Both blocks of a step at once: blk[s] is renormalised with the kept
+// columns kl[s] and gets the basis kept_qn[s].
+int renorm_device(Ctx &c, const KeptLayout kl[2], Block *blk[2], const std::vector<std::vector<double>> *kept_qn[2]);
 void renorm_release(Ctx &c);
 
 }  // namespace nss

@@ -121,7 +121,15 @@ std::vector<double> outsum(const std::vector<double> &a, int na, const std::vect
 
 Block enlarge_block(const Block &blk, const Block &dot, char label, const double *hij) {
     const int m = blk.dim, d = dot.dim;
-    Block out = blk;
+    // the block's metadata and operator list without its matrices, which
+    // are all replaced below
+    Block out;
+    out.length = blk.length;
+    out.dim = blk.dim;
+    out.qdim = blk.qdim;
+    out.fermion = blk.fermion;
+    out.ops.reserve(blk.ops.size());
+    for (const Op &o : blk.ops) out.ops.push_back({o.key, Csr{}, o.type});
     Csr hb, hd, h2;
     if (label == 'l') {
         hb = csr_kron(blk.op("H"), csr_identity(d));
@@ -134,18 +142,21 @@ Block enlarge_block(const Block &blk, const Block &dot, char label, const double
     }
     out.op("H") = csr_add(csr_add(hb, hd), h2);
     // other operators in list order; P is read from the list being updated
-    // exactly as the reference loop does (src/DMRG_CONNECT.f90:117-146)
+    // exactly as the reference loop does (src/DMRG_CONNECT.f90:117-146):
+    // the enlarged P once its own entry has been passed, the block's before
+    const int ip = blk.find_op("P_n");
+    auto p_now = [&](size_t i) -> const Csr & {
+        if (ip < 0) throw std::runtime_error("block operator not found: P_n");
+        return (size_t)ip < i ? out.ops[ip].m : blk.ops[ip].m;
+    };
     for (size_t i = 0; i < blk.ops.size(); ++i) {
         const Op &o = blk.ops[i];
         if (o.key == "H") continue;
         const char t = o.type.empty() ? 'b' : o.type[0];
-        Csr eo;
         if (label == 'l') {
-            eo = (t == 'b') ? csr_identity(m) : out.op("P_n");
-            out.ops[i].m = csr_kron(eo, dot.op(o.key));
+            out.ops[i].m = (t == 'b') ? csr_kron(csr_identity(m), dot.op(o.key)) : csr_kron(p_now(i), dot.op(o.key));
         } else {
-            eo = (t == 'p') ? out.op("P_n") : csr_identity(m);
-            out.ops[i].m = csr_kron(dot.op(o.key), eo);
+            out.ops[i].m = (t == 'p') ? csr_kron(dot.op(o.key), p_now(i)) : csr_kron(dot.op(o.key), csr_identity(m));
         }
     }
     out.length = blk.length + 1;
@@ -224,13 +235,19 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
 int Driver::step(int type, int label, int sweep) {
     const auto t_step = std::chrono::steady_clock::now();
     const int mstates = (type == 0) ? p.mdmrg : msweep.at(sweep - 1);
-    left = enlarge_block(left, dot, 'l', hij);
-    right = enlarge_block(right, dot, 'r', hij);
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    // the two enlargements are independent
+    run_pair([&] { left = enlarge_block(left, dot, 'l', hij); },
+             [&] { right = enlarge_block(right, dot, 'r', hij); });
+    const double ms_enlarge = ms_since(t_step);
     const int current_l = left.length + right.length;
     // sb_set_current_qn, QNtype local: int(target_qn * L * Norb), truncated
     Qn target(left.qdim);
     for (int i = 0; i < left.qdim; ++i) target[i] = std::trunc(p.dmrg_qn[i] * current_l * 1.0);
+    const auto t_sb = clk::now();
     SbHost sb = sb_build(left, right, target, hij);
+    const double ms_sb = ms_since(t_sb);
     bool renorm;
     if (type == 0) renorm = left.length != p.ldmrg;
     else renorm = !(left.length == p.ldmrg + 1 && label == 1);
@@ -249,7 +266,9 @@ int Driver::step(int type, int label, int sweep) {
         stopped = true;
         return rc;
     }
-    rec.ms_build = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
+    rec.ms_build = ms_since(t_step);
+    rec.host_phase_ms[0] = ms_enlarge;
+    rec.host_phase_ms[1] = ms_sb;
     int rc = nss_solve_step(*ctx, sb, p, mstates, renorm, left, right, rec);
     if (rc) return rc;
     rec.ms_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
@@ -336,10 +355,12 @@ void renormalize(Block &blk, const Csr &u, const std::vector<Qn> &kept_qn) {
 
 int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, bool renorm, Block &left,
                    Block &right, nss_step_record &rec) {
+    const auto t_up = std::chrono::steady_clock::now();
     SbView v;
     sb_view(sb, v);
     int rc = sb_upload(c, &v.desc);
     if (rc) return rc;
+    rec.host_phase_ms[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_up).count();
     const int64_t n = sb.n();
     const int neigen = (int)std::min<int64_t>(n, p.lanc_neigen);
     const int nitermax = (int)std::min<int64_t>(n, p.lanc_niter);
@@ -354,13 +375,6 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     if (rc) return rc;
     cudaEventRecord(em, c.stream);
     nss_rdm_side side[2];
-    std::vector<double> u_l, u_r;
-    std::vector<int32_t> k_l, k_r;
-    // m_s is known only after the truncation kernel: size for the maximum
-    u_l.resize((size_t)sb.m_left * sb.m_left);
-    u_r.resize((size_t)sb.m_right * sb.m_right);
-    k_l.resize(sb.m_left);
-    k_r.resize(sb.m_right);
     // operator renormalisation: QN-block GEMMs on the device for blocks of
     // at least 256 states (below that the host's sparse products are as
     // fast as the transfers); env NSS_RENORM=host / device forces one
@@ -368,6 +382,16 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     const bool force_host = rh && std::string(rh) == "host", force_dev = rh && std::string(rh) == "device";
     const bool dev_renorm =
         renorm && !force_host && (force_dev || std::max(sb.m_left, sb.m_right) >= 256);
+    std::vector<double> u_l, u_r;
+    std::vector<int32_t> k_l, k_r;
+    // m_s is known only after the truncation kernel: size for the maximum
+    // (the dense U only for the host renormalisation)
+    if (renorm && !dev_renorm) {
+        u_l.resize((size_t)sb.m_left * sb.m_left);
+        u_r.resize((size_t)sb.m_right * sb.m_right);
+    }
+    k_l.resize(sb.m_left);
+    k_r.resize(sb.m_right);
     KeptLayout kl[2];
     rc = rdm_run(c, c.lz.evecs, mstates, p.deg_evals_threshold, side, nullptr, nullptr,
                  renorm ? k_l.data() : nullptr, renorm ? k_r.data() : nullptr,
@@ -408,8 +432,11 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             qr.push_back(q);
         }
         const auto t_r = std::chrono::steady_clock::now();
+        for (double &x : c.renorm_phase_ms) x = 0.0;
         if (dev_renorm) {
-            if ((rc = renorm_device(c, kl[0], left, ql)) || (rc = renorm_device(c, kl[1], right, qr))) return rc;
+            Block *bl[2] = {&left, &right};
+            const std::vector<Qn> *kq[2] = {&ql, &qr};
+            if ((rc = renorm_device(c, kl, bl, kq))) return rc;
             rec.nnz_u = 0;
             for (int s2 = 0; s2 < 2; ++s2)
                 for (int j = 0; j < kl[s2].ms; ++j) rec.nnz_u += kl[s2].dims[kl[s2].q[j]];
@@ -423,6 +450,7 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
         for (const auto &o : left.ops) rec.nnz_ops += o.m.nnz();
         for (const auto &o : right.ops) rec.nnz_ops += o.m.nnz();
         rec.ms_renorm = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_r).count();
+        for (int i = 0; i < 3; ++i) rec.host_phase_ms[3 + i] = c.renorm_phase_ms[i];
         rec.trunc_left = side[0].trunc_err;
         rec.trunc_right = side[1].trunc_err;
         rec.m_left = left.dim;

@@ -54,10 +54,10 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
     for (int k = 0; k < nsb; ++k) index.emplace(sb.qns[k], k);
 
     const Csr &hl = left.op("H"), &hr = right.op("H");
-    for (int k = 0; k < nsb; ++k) {
-        sb.hleft.push_back(csr_filter(hl, sb.ai[k], sb.ai[k]));
-        sb.hright.push_back(csr_filter(hr, sb.bi[k], sb.bi[k]));
-    }
+    sb.hleft.resize(nsb);
+    sb.hright.resize(nsb);
+    run_pair([&] { for (int k = 0; k < nsb; ++k) sb.hleft[k] = csr_filter(hl, sb.ai[k], sb.ai[k]); },
+             [&] { for (int k = 0; k < nsb; ++k) sb.hright[k] = csr_filter(hr, sb.bi[k], sb.bi[k]); });
 
     auto set_term = [&](int it, int k, int jsb, int hc, Csr a, Csr b, int64_t ro, int64_t co) {
         int idx = it + sb.tnso * k;

@@ -8,11 +8,36 @@
 #pragma once
 
 #include <cstdint>
+#include <exception>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace nss {
+
+// f0 on the calling thread and f1 on a second one (the two sides of a DMRG
+// step are independent); an exception of either is rethrown after both
+// have finished, f0's first.
+template <class F0, class F1>
+void run_pair(F0 &&f0, F1 &&f1) {
+    std::exception_ptr e0, e1;
+    std::thread th([&] {
+        try {
+            f1();
+        } catch (...) {
+            e1 = std::current_exception();
+        }
+    });
+    try {
+        f0();
+    } catch (...) {
+        e0 = std::current_exception();
+    }
+    th.join();
+    if (e0) std::rethrow_exception(e0);
+    if (e1) std::rethrow_exception(e1);
+}
 
 // CSR matrix, 0-based.  Explicit zeros that arise from arithmetic are kept,
 // as in the reference's sparse algebra.

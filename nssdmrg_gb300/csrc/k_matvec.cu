@@ -8,6 +8,7 @@
 // (:808-857, regrouped by output sector so each tile has one writer).
 #include "device.cuh"
 #include "hv_tile.cuh"
+#include "host_sparse.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -34,15 +35,18 @@ void ctx_free(Ctx &c, void *p) {
     cudaFree(p);
 }
 
-void sb_release(Ctx &c) {
-    DevSb &s = c.sb;
-    void *ptrs[] = {s.d_dls, s.d_drs, s.d_off, s.d_hl_off, s.d_hr_off, s.d_hl, s.d_hr,
-                    s.d_term_ptr, s.d_terms, s.d_ab_rowptr, s.d_ab_col, s.d_ab_val,
-                    s.d_tiles, s.d_hl32, s.d_hr32, s.d_ab_val32, s.d_tiles32, s.d_tiles_tc, s.d_tc_err,
-                    s.d_ab_rowptr32, s.d_ab_col32, s.d_terms32, s.d_items32, s.d_item_ell, s.d_ell,
-                    s.d_term_hdr};
-    for (void *p : ptrs) ctx_free(c, p);
-    s = DevSb{};
+// The pool's device arrays are sections of one device arena, filled from
+// one pinned staging buffer by one copy; both grow only and are kept from
+// one upload to the next (a DMRG run uploads a new pool every step).
+void sb_release(Ctx &c, bool free_arena) {
+    c.sb = DevSb{};
+    if (free_arena) {
+        ctx_free(c, c.sb_arena);
+        if (c.sb_stage) cudaFreeHost(c.sb_stage);
+        c.sb_arena = nullptr;
+        c.sb_stage = nullptr;
+        c.sb_arena_cap = c.sb_stage_cap = 0;
+    }
 }
 
 namespace {
@@ -51,13 +55,52 @@ constexpr int TILE = 16;
 constexpr int TILE32 = 32;
 constexpr int TC_ROWS = 128, TC_COLS = 64;   // k_hv_tc tile
 
-template <class T>
-int upload_vec(Ctx &c, T **dst, const std::vector<T> &src) {
-    NSS_CUDA_TRY(c, ctx_alloc(c, dst, src.size()));
-    c.sb.h2d_bytes += (int64_t)(src.size() * sizeof(T));
-    if (!src.empty())
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T),
-                                        cudaMemcpyHostToDevice, c.stream));
+// Sections of the pool's arena: each array at a 256-byte boundary (at least
+// 16 bytes, so that every pointer is distinct and valid).
+struct Stager {
+    struct Item {
+        void **dst;
+        const void *src;
+        size_t bytes, off;
+    };
+    std::vector<Item> items;
+    size_t total = 0;
+    template <class T>
+    void add(T **dst, const std::vector<T> &v) {
+        const size_t bytes = v.size() * sizeof(T);
+        items.push_back({(void **)dst, (const void *)v.data(), bytes, total});
+        total += (std::max<size_t>(bytes, 16) + 255) / 256 * 256;
+    }
+};
+
+int stage_commit(Ctx &c, Stager &sg) {
+    if (c.sb_arena_cap < sg.total) {
+        ctx_free(c, c.sb_arena);
+        c.sb_arena = nullptr;
+        c.sb_arena_cap = 0;
+        const size_t cap = sg.total + sg.total / 4;   // headroom: the pool size varies from step to step
+        NSS_CUDA_TRY(c, ctx_alloc(c, &c.sb_arena, cap));
+        c.sb_arena_cap = cap;
+    }
+    if (c.sb_stage_cap < sg.total) {
+        if (c.sb_stage) cudaFreeHost(c.sb_stage);
+        c.sb_stage = nullptr;
+        c.sb_stage_cap = 0;
+        const size_t cap = sg.total + sg.total / 4;
+        NSS_CUDA_TRY(c, cudaHostAlloc((void **)&c.sb_stage, cap, cudaHostAllocDefault));
+        c.sb_stage_cap = cap;
+    }
+    const size_t half = sg.items.size() / 2;
+    auto fill = [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i)
+            if (sg.items[i].bytes) std::memcpy(c.sb_stage + sg.items[i].off, sg.items[i].src, sg.items[i].bytes);
+    };
+    run_pair([&] { fill(0, half); }, [&] { fill(half, sg.items.size()); });
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(c.sb_arena, c.sb_stage, sg.total, cudaMemcpyHostToDevice, c.stream));
+    for (const auto &it : sg.items) {
+        *it.dst = (void *)(c.sb_arena + it.off);
+        c.sb.h2d_bytes += (int64_t)it.bytes;
+    }
     return NSS_OK;
 }
 
@@ -84,7 +127,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
         c.err = "nss_sb_upload: incomplete descriptor";
         return NSS_ERR_INVALID;
     }
-    sb_release(c);
+    // kernels of the previous pool may still be reading the arena (a
+    // batch runs several contexts' solves on one stream)
+    NSS_CUDA_TRY(c, cudaDeviceSynchronize());
+    sb_release(c, false);
     DevSb &s = c.sb;
     s.nsb = d->nsb;
     s.tnso = d->tnso;
@@ -338,23 +384,35 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     s.ntiles_tc = (int)tiles_tc.size();
     std::vector<int> tc_err(1, 0);
 
+    Stager sg;
+    sg.add(&s.d_hl32, hl32);
+    sg.add(&s.d_hr32, hr32);
+    sg.add(&s.d_ab_val32, val32);
+    sg.add(&s.d_ab_rowptr32, rowptr32);
+    sg.add(&s.d_ab_col32, col32);
+    sg.add(&s.d_terms32, terms32);
+    sg.add(&s.d_tiles32, tiles32);
+    sg.add(&s.d_items32, recs);
+    sg.add(&s.d_item_ell, item_ell);
+    sg.add(&s.d_ell, ell);
+    sg.add(&s.d_term_hdr, term_hdr);
+    sg.add(&s.d_tiles_tc, tiles_tc);
+    sg.add(&s.d_tc_err, tc_err);
+    sg.add(&s.d_dls, s.dls);
+    sg.add(&s.d_drs, s.drs);
+    sg.add(&s.d_off, s.off);
+    sg.add(&s.d_hl_off, s.hl_off);
+    sg.add(&s.d_hr_off, s.hr_off);
+    sg.add(&s.d_hl, hl);
+    sg.add(&s.d_hr, hr);
+    sg.add(&s.d_term_ptr, s.term_ptr);
+    sg.add(&s.d_terms, s.terms);
+    sg.add(&s.d_ab_rowptr, rowptr);
+    sg.add(&s.d_ab_col, col);
+    sg.add(&s.d_ab_val, val);
+    sg.add(&s.d_tiles, tiles);
     int rc;
-    if ((rc = upload_vec(c, &s.d_hl32, hl32)) || (rc = upload_vec(c, &s.d_hr32, hr32)) ||
-        (rc = upload_vec(c, &s.d_ab_val32, val32)) || (rc = upload_vec(c, &s.d_ab_rowptr32, rowptr32)) ||
-        (rc = upload_vec(c, &s.d_ab_col32, col32)) || (rc = upload_vec(c, &s.d_terms32, terms32)) ||
-        (rc = upload_vec(c, &s.d_tiles32, tiles32)) || (rc = upload_vec(c, &s.d_items32, recs)) ||
-        (rc = upload_vec(c, &s.d_item_ell, item_ell)) || (rc = upload_vec(c, &s.d_ell, ell)) ||
-        (rc = upload_vec(c, &s.d_term_hdr, term_hdr)) ||
-        (rc = upload_vec(c, &s.d_tiles_tc, tiles_tc)) || (rc = upload_vec(c, &s.d_tc_err, tc_err)))
-        return rc;
-    if ((rc = upload_vec(c, &s.d_dls, s.dls)) || (rc = upload_vec(c, &s.d_drs, s.drs)) ||
-        (rc = upload_vec(c, &s.d_off, s.off)) || (rc = upload_vec(c, &s.d_hl_off, s.hl_off)) ||
-        (rc = upload_vec(c, &s.d_hr_off, s.hr_off)) || (rc = upload_vec(c, &s.d_hl, hl)) ||
-        (rc = upload_vec(c, &s.d_hr, hr)) || (rc = upload_vec(c, &s.d_term_ptr, s.term_ptr)) ||
-        (rc = upload_vec(c, &s.d_terms, s.terms)) || (rc = upload_vec(c, &s.d_ab_rowptr, rowptr)) ||
-        (rc = upload_vec(c, &s.d_ab_col, col)) || (rc = upload_vec(c, &s.d_ab_val, val)) ||
-        (rc = upload_vec(c, &s.d_tiles, tiles)))
-        return rc;
+    if ((rc = stage_commit(c, sg))) return rc;
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
     s.valid = true;
     return NSS_OK;

@@ -1,4 +1,4 @@
-// Operator renormalisation O' = U^T O U of one block on the GPU
+// Operator renormalisation O' = U^T O U of the two blocks on the GPU
 // (operators_renormalization, src/DMRG_RDM.f90:355-404).
 //
 // U is block-sparse by construction: kept column j is the eigenvector of
@@ -7,32 +7,115 @@
 //     O'[j, j'] = (U_q^T  O_{q q'}  U_q')[loc(j), loc(j')],
 // q = q_j, q' = q_j', with U_q the n_q x k_q matrix of block q's kept
 // columns and O_{q q'} the dense n_q x n_q' block of O between the two
-// blocks' states.  Every nonzero block pair of every operator becomes two
-// FP64 GEMMs (cuBLAS DGEMM: T = O_{q q'} U_q', O'_{q q'} = U_q^T T); the
-// operators stay sparse on the host between steps as in the reference, and
-// only their nonzero blocks travel.  The kept columns come from the RDM
-// step in compact form (no zero rows) and stay on the device.
+// blocks' states.  Every nonzero block pair of every operator of both blocks
+// becomes two FP64 products (T = O_{q q'} U_q', O'_{q q'} = U_q^T T), all of
+// one kind in one launch of a batched tile kernel: the pairs are a few
+// hundred states wide, so one library GEMM per pair would occupy a dozen
+// SMs at a time.  The operators stay sparse on the host between steps as in
+// the reference, and only their nonzero blocks travel; the two blocks'
+// host-side scan, extraction and CSR assembly run on two threads.  The kept
+// columns come from the RDM step in compact form (no zero rows) and stay on
+// the device.
 #include "device.cuh"
 #include "host_sparse.hpp"
 
-#include <cublas_v2.h>
-
 #include <algorithm>
+#include <chrono>
 #include <cstring>
+#include <exception>
+#include <thread>
 
 namespace nss {
 
 namespace {
 
 // U_q blocks: column j of the compact buffer (length n_q) -> column loc of
-// the n_q x k_q column-major matrix at uoff[j] in ublk.
+// the n_q x k_q column-major matrix at dst_off[j] in ublk.
 __global__ void __launch_bounds__(128) k_gather_u(const double *__restrict__ comp, const int *__restrict__ src_off,
-                                                 const int *__restrict__ dst_off, const int *__restrict__ len,
+                                                 const int64_t *__restrict__ dst_off, const int *__restrict__ len,
                                                  double *__restrict__ ublk) {
     const int j = blockIdx.x;
     const double *s = comp + src_off[j];
     double *d = ublk + dst_off[j];
     for (int p = threadIdx.x; p < len[j]; p += blockDim.x) d[p] = s[p];
+}
+
+// One product C (m x n, column-major, ldc) = op(A) B, B column-major k x n
+// (ldb); op(A) = A (m x k, lda) or A^T (A stored k x m, lda).  Its 64 x 64
+// output tiles are blocks tile0 .. tile0 + tiles_m * ceil(n/64) - 1.
+struct RnJob {
+    const double *a;
+    const double *b;
+    double *c;
+    int m, n, k, lda, ldb, ldc, transa, tiles_m, tile0, pad;
+};
+
+constexpr int RN_TILE = 64, RN_K = 16;
+
+// Batched FP64 tile product: one CTA per 64 x 64 output tile of any job,
+// 256 threads with 4 x 4 outputs each (rows tm + 16 i, columns tn + 16 j),
+// K in steps of 16 through shared memory, zero-filled at the edges.
+__global__ void __launch_bounds__(256) k_rn_gemm(const RnJob *__restrict__ jobs, const int *__restrict__ tile_job) {
+    __shared__ double As[RN_K][RN_TILE + 1];
+    __shared__ double Bs[RN_K][RN_TILE + 1];
+    const RnJob jb = jobs[tile_job[blockIdx.x]];
+    const int local = blockIdx.x - jb.tile0;
+    const int m0 = (local % jb.tiles_m) * RN_TILE, n0 = (local / jb.tiles_m) * RN_TILE;
+    const int tid = threadIdx.x, tm = tid & 15, tn = tid >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int k0 = 0; k0 < jb.k; k0 += RN_K) {
+        if (!jb.transa) {
+            const int m = tid & 63, gm = m0 + m;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int kk = (tid >> 6) + 4 * r, gk = k0 + kk;
+                As[kk][m] = (gm < jb.m && gk < jb.k) ? jb.a[(int64_t)gk * jb.lda + gm] : 0.0;
+            }
+        } else {
+            const int kk = tid & 15, gk = k0 + kk;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int m = (tid >> 4) + 16 * r, gm = m0 + m;
+                As[kk][m] = (gm < jb.m && gk < jb.k) ? jb.a[(int64_t)gm * jb.lda + gk] : 0.0;
+            }
+        }
+        {
+            const int kk = tid & 15, gk = k0 + kk;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int n = (tid >> 4) + 16 * r, gn = n0 + n;
+                Bs[kk][n] = (gn < jb.n && gk < jb.k) ? jb.b[(int64_t)gn * jb.ldb + gk] : 0.0;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < RN_K; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][tm + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tn + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int gn = n0 + tn + 16 * j;
+        if (gn >= jb.n) continue;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int gm = m0 + tm + 16 * i;
+            if (gm < jb.m) jb.c[(int64_t)gn * jb.ldc + gm] = acc[i][j];
+        }
+    }
 }
 
 template <class T>
@@ -55,154 +138,119 @@ int grow_host(Ctx &c, T **p, int64_t &cap, int64_t need) {
     return NSS_OK;
 }
 
-}  // namespace
+struct Pair {
+    int op, qr, qc;
+    int64_t o_off, t_off, r_off;   // offsets into the side's O, T and R shares
+};
 
-void renorm_release(Ctx &c) {
-    DevRenorm &w = c.ren;
-    void *ptrs[] = {w.ublk, w.dblk, w.tbuf, w.rbuf, w.itab};
-    for (void *p : ptrs) ctx_free(c, p);
-    if (w.hblk) cudaFreeHost(w.hblk);
-    if (w.hres) cudaFreeHost(w.hres);
-    if (w.hitab) cudaFreeHost(w.hitab);
-    if (w.blas) cublasDestroy((cublasHandle_t)w.blas);
-    w = DevRenorm{};
-}
+// One block's share of the work.
+struct Side {
+    const KeptLayout *kl = nullptr;
+    Block *blk = nullptr;
+    const std::vector<Qn> *kept_qn = nullptr;
+    int nb = 0, ms = 0;
+    std::vector<int> kq, loc;
+    std::vector<int64_t> uoff;            // U_q blocks, offsets into the side's U share
+    std::vector<int> bof, lof;            // enlarged-block state -> (block, local row)
+    std::vector<Pair> pairs;
+    std::vector<std::vector<int>> pidx;   // [op][qr * nb + qc] -> pair or -1
+    int64_t o_tot = 0, t_tot = 0, r_tot = 0, u_tot = 0;
+};
 
-int renorm_device(Ctx &c, const KeptLayout &kl, Block &blk, const std::vector<Qn> &kept_qn) {
-    DevRenorm &w = c.ren;
-    cudaStream_t st = c.stream;
-    const int ms = kl.ms, nb = (int)kl.dims.size();
-    if (!w.blas) {
-        cublasHandle_t h = nullptr;
-        if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) {
-            c.err = "renormalisation: cublasCreate failed";
-            return NSS_ERR_CUDA;
-        }
-        w.blas = h;
-    }
-    cublasHandle_t h = (cublasHandle_t)w.blas;
-    if (cublasSetStream(h, st) != CUBLAS_STATUS_SUCCESS) {
-        c.err = "renormalisation: cublasSetStream failed";
-        return NSS_ERR_CUDA;
-    }
-    // kept columns per block, in ascending j
-    std::vector<int> kq(nb, 0), loc(ms);
-    for (int j = 0; j < ms; ++j) loc[j] = kq[kl.q[j]]++;
-    std::vector<int64_t> uoff(nb + 1, 0);
-    for (int q = 0; q < nb; ++q) uoff[q + 1] = uoff[q] + (int64_t)kl.dims[q] * kq[q];
-    // enlarged-block state -> (block, local row)
+// kept columns per block, state maps and the nonzero block pairs of every
+// operator (both blocks with kept columns)
+void scan_side(Side &s) {
+    const KeptLayout &kl = *s.kl;
+    const Block &blk = *s.blk;
+    s.ms = kl.ms;
+    s.nb = (int)kl.dims.size();
+    const int nb = s.nb;
+    s.kq.assign(nb, 0);
+    s.loc.resize(s.ms);
+    for (int j = 0; j < s.ms; ++j) s.loc[j] = s.kq[kl.q[j]]++;
+    s.uoff.assign(nb + 1, 0);
+    for (int q = 0; q < nb; ++q) s.uoff[q + 1] = s.uoff[q] + (int64_t)kl.dims[q] * s.kq[q];
+    s.u_tot = s.uoff[nb];
     const int mblock = blk.dim;
-    std::vector<int> bof(mblock, -1), lof(mblock, -1);
+    s.bof.assign(mblock, -1);
+    s.lof.assign(mblock, -1);
     for (int q = 0; q < nb; ++q)
         for (int p = 0; p < kl.dims[q]; ++p) {
-            const int s = kl.maps[kl.map_off[q] + p];
-            if (s >= 0 && s < mblock) {
-                bof[s] = q;
-                lof[s] = p;
+            const int st = kl.maps[kl.map_off[q] + p];
+            if (st >= 0 && st < mblock) {
+                s.bof[st] = q;
+                s.lof[st] = p;
             }
         }
-    // nonzero block pairs of every operator (both blocks with kept columns)
-    struct Pair {
-        int op, qr, qc;
-        int64_t o_off, t_off, r_off;
-    };
-    std::vector<Pair> pairs;
-    std::vector<std::vector<int>> pidx(blk.ops.size(), std::vector<int>((size_t)nb * nb, -1));
-    int64_t o_tot = 0, t_tot = 0, r_tot = 0;
+    s.pidx.assign(blk.ops.size(), std::vector<int>((size_t)nb * nb, -1));
     for (size_t io = 0; io < blk.ops.size(); ++io) {
         const Csr &m = blk.ops[io].m;
         for (int r = 0; r < m.nrow; ++r) {
-            const int qr = r < mblock ? bof[r] : -1;
-            if (qr < 0 || !kq[qr]) continue;
+            const int qr = r < mblock ? s.bof[r] : -1;
+            if (qr < 0 || !s.kq[qr]) continue;
             for (int e = m.rowptr[r]; e < m.rowptr[r + 1]; ++e) {
                 const int cc = m.col[e];
-                const int qc = cc < mblock ? bof[cc] : -1;
-                if (qc < 0 || !kq[qc]) continue;
+                const int qc = cc < mblock ? s.bof[cc] : -1;
+                if (qc < 0 || !s.kq[qc]) continue;
                 const int key = qr * nb + qc;
-                if (pidx[io][key] >= 0) continue;
-                Pair pr{(int)io, qr, qc, o_tot, t_tot, r_tot};
-                o_tot += (int64_t)kl.dims[qr] * kl.dims[qc];
-                t_tot += (int64_t)kl.dims[qr] * kq[qc];
-                r_tot += (int64_t)kq[qr] * kq[qc];
-                pidx[io][key] = (int)pairs.size();
-                pairs.push_back(pr);
+                if (s.pidx[io][key] >= 0) continue;
+                s.pidx[io][key] = (int)s.pairs.size();
+                s.pairs.push_back({(int)io, qr, qc, s.o_tot, s.t_tot, s.r_tot});
+                s.o_tot += (int64_t)kl.dims[qr] * kl.dims[qc];
+                s.t_tot += (int64_t)kl.dims[qr] * s.kq[qc];
+                s.r_tot += (int64_t)s.kq[qr] * s.kq[qc];
             }
         }
     }
-    int rc;
-    if ((rc = grow_host(c, &w.hblk, w.cap_hblk, o_tot))) return rc;
-    if ((rc = grow_host(c, &w.hres, w.cap_hres, r_tot))) return rc;
-    if ((rc = grow_dev(c, &w.dblk, w.cap_dblk, o_tot))) return rc;
-    if ((rc = grow_dev(c, &w.tbuf, w.cap_tbuf, t_tot))) return rc;
-    if ((rc = grow_dev(c, &w.rbuf, w.cap_rbuf, r_tot))) return rc;
-    if ((rc = grow_dev(c, &w.ublk, w.cap_ublk, uoff[nb]))) return rc;
-    // dense blocks of the operators (column-major n_qr x n_qc)
-    std::memset(w.hblk, 0, (size_t)o_tot * sizeof(double));
+}
+
+// dense blocks of the operators (column-major n_qr x n_qc) into hblk, the
+// side's share of the staging buffer
+void extract_side(const Side &s, double *hblk) {
+    const KeptLayout &kl = *s.kl;
+    const Block &blk = *s.blk;
+    const int nb = s.nb, mblock = blk.dim;
+    std::memset(hblk, 0, (size_t)s.o_tot * sizeof(double));
     for (size_t io = 0; io < blk.ops.size(); ++io) {
         const Csr &m = blk.ops[io].m;
+        const std::vector<int> &pi = s.pidx[io];
         for (int r = 0; r < m.nrow; ++r) {
-            const int qr = r < mblock ? bof[r] : -1;
-            if (qr < 0 || !kq[qr]) continue;
+            const int qr = r < mblock ? s.bof[r] : -1;
+            if (qr < 0 || !s.kq[qr]) continue;
+            const int64_t rowbase = s.lof[r];
             for (int e = m.rowptr[r]; e < m.rowptr[r + 1]; ++e) {
                 const int cc = m.col[e];
-                const int qc = cc < mblock ? bof[cc] : -1;
-                if (qc < 0 || !kq[qc]) continue;
-                const Pair &pr = pairs[pidx[io][qr * nb + qc]];
-                w.hblk[pr.o_off + (int64_t)lof[cc] * kl.dims[qr] + lof[r]] = m.val[e];
+                const int qc = cc < mblock ? s.bof[cc] : -1;
+                if (qc < 0 || !s.kq[qc]) continue;
+                const Pair &pr = s.pairs[pi[qr * nb + qc]];
+                hblk[pr.o_off + (int64_t)s.lof[cc] * kl.dims[qr] + rowbase] = m.val[e];
             }
         }
     }
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.dblk, w.hblk, (size_t)o_tot * sizeof(double), cudaMemcpyHostToDevice, st));
-    // U_q from the compact kept columns
-    if (ms > 0) {
-        if ((rc = grow_host(c, &w.hitab, w.cap_hitab, 3 * (int64_t)ms))) return rc;
-        if ((rc = grow_dev(c, &w.itab, w.cap_itab, 3 * (int64_t)ms))) return rc;
-        int *src = w.hitab, *dst = src + ms, *len = dst + ms;
-        for (int j = 0; j < ms; ++j) {
-            const int q = kl.q[j];
-            src[j] = kl.off[j];
-            dst[j] = (int)(uoff[q] + (int64_t)loc[j] * kl.dims[q]);
-            len[j] = kl.dims[q];
-        }
-        NSS_CUDA_TRY(c, cudaMemcpyAsync(w.itab, w.hitab, 3 * (size_t)ms * sizeof(int), cudaMemcpyHostToDevice, st));
-        ++c.launches;
-        k_gather_u<<<ms, 128, 0, st>>>(kl.dcomp, w.itab, w.itab + ms, w.itab + 2 * ms, w.ublk);
-        NSS_CUDA_TRY(c, cudaGetLastError());
-    }
-    // two GEMMs per block pair
-    const double one = 1.0, zero = 0.0;
-    for (const Pair &pr : pairs) {
-        const int nr = kl.dims[pr.qr], nc = kl.dims[pr.qc], kr = kq[pr.qr], kc = kq[pr.qc];
-        const double *O = w.dblk + pr.o_off, *Ur = w.ublk + uoff[pr.qr], *Uc = w.ublk + uoff[pr.qc];
-        double *T = w.tbuf + pr.t_off, *R = w.rbuf + pr.r_off;
-        if (cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nr, kc, nc, &one, O, nr, Uc, nc, &zero, T, nr) !=
-                CUBLAS_STATUS_SUCCESS ||
-            cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, kr, kc, nr, &one, Ur, nr, T, nr, &zero, R, kr) !=
-                CUBLAS_STATUS_SUCCESS) {
-            c.err = "renormalisation: cublasDgemm failed";
-            return NSS_ERR_CUDA;
-        }
-        c.launches += 2;
-    }
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.hres, w.rbuf, (size_t)r_tot * sizeof(double), cudaMemcpyDeviceToHost, st));
-    NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-    // O' in CSR, rows and columns in kept order, exact zeros dropped
+}
+
+// O' in CSR, rows and columns in kept order, exact zeros dropped; hres is
+// the side's share of the result staging buffer
+void assemble_side(Side &s, const double *hres) {
+    const KeptLayout &kl = *s.kl;
+    Block &blk = *s.blk;
+    const int nb = s.nb, ms = s.ms;
     std::vector<std::vector<int>> jof(nb);
     for (int j = 0; j < ms; ++j) jof[kl.q[j]].push_back(j);
+    std::vector<std::pair<int, double>> row;
     for (size_t io = 0; io < blk.ops.size(); ++io) {
-        std::vector<std::vector<int>> prow(nb);       // pairs of this operator by row block
+        std::vector<std::vector<int>> prow(nb);   // pairs of this operator by row block
         for (int key = 0; key < nb * nb; ++key)
-            if (pidx[io][key] >= 0) prow[key / nb].push_back(pidx[io][key]);
+            if (s.pidx[io][key] >= 0) prow[key / nb].push_back(s.pidx[io][key]);
         Csr out;
         out.init(ms, ms);
-        std::vector<std::pair<int, double>> row;
         for (int j = 0; j < ms; ++j) {
-            const int qr = kl.q[j], a = loc[j];
+            const int qr = kl.q[j], a = s.loc[j];
             row.clear();
             for (int pi : prow[qr]) {
-                const Pair &pr = pairs[pi];
-                const int kr = kq[qr];
-                const double *R = w.hres + pr.r_off;
+                const Pair &pr = s.pairs[pi];
+                const int kr = s.kq[qr];
+                const double *R = hres + pr.r_off;
                 const std::vector<int> &cols = jof[pr.qc];
                 for (size_t b = 0; b < cols.size(); ++b) {
                     const double v = R[(int64_t)b * kr + a];
@@ -220,7 +268,138 @@ int renorm_device(Ctx &c, const KeptLayout &kl, Block &blk, const std::vector<Qn
     }
     blk.dim = ms;
     blk.basis.clear();
-    for (const Qn &q : kept_qn) blk.basis.insert(blk.basis.end(), q.begin(), q.end());
+    for (const Qn &q : *s.kept_qn) blk.basis.insert(blk.basis.end(), q.begin(), q.end());
+}
+
+}  // namespace
+
+void renorm_release(Ctx &c) {
+    DevRenorm &w = c.ren;
+    void *ptrs[] = {w.ublk, w.dblk, w.tbuf, w.rbuf, w.itab};
+    for (void *p : ptrs) ctx_free(c, p);
+    if (w.hblk) cudaFreeHost(w.hblk);
+    if (w.hres) cudaFreeHost(w.hres);
+    if (w.hitab) cudaFreeHost(w.hitab);
+    w = DevRenorm{};
+}
+
+int renorm_device(Ctx &c, const KeptLayout kl[2], Block *blk[2], const std::vector<Qn> *kept_qn[2]) {
+    DevRenorm &w = c.ren;
+    cudaStream_t st = c.stream;
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
+    const auto t0 = clk::now();
+    Side sd[2];
+    for (int s = 0; s < 2; ++s) {
+        sd[s].kl = &kl[s];
+        sd[s].blk = blk[s];
+        sd[s].kept_qn = kept_qn[s];
+    }
+    run_pair([&] { scan_side(sd[0]); }, [&] { scan_side(sd[1]); });
+    // shared buffers: side 1's share after side 0's
+    const int64_t o_tot = sd[0].o_tot + sd[1].o_tot, t_tot = sd[0].t_tot + sd[1].t_tot,
+                  r_tot = sd[0].r_tot + sd[1].r_tot, u_tot = sd[0].u_tot + sd[1].u_tot;
+    const int ms_tot = sd[0].ms + sd[1].ms;
+    const int npairs = (int)(sd[0].pairs.size() + sd[1].pairs.size());
+    int rc;
+    if ((rc = grow_host(c, &w.hblk, w.cap_hblk, o_tot))) return rc;
+    if ((rc = grow_host(c, &w.hres, w.cap_hres, r_tot))) return rc;
+    if ((rc = grow_dev(c, &w.dblk, w.cap_dblk, o_tot))) return rc;
+    if ((rc = grow_dev(c, &w.tbuf, w.cap_tbuf, t_tot))) return rc;
+    if ((rc = grow_dev(c, &w.rbuf, w.cap_rbuf, r_tot))) return rc;
+    if ((rc = grow_dev(c, &w.ublk, w.cap_ublk, u_tot))) return rc;
+    run_pair([&] { extract_side(sd[0], w.hblk); }, [&] { extract_side(sd[1], w.hblk + sd[0].o_tot); });
+    c.renorm_phase_ms[0] += ms_since(t0);
+    const auto t1 = clk::now();
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.dblk, w.hblk, (size_t)o_tot * sizeof(double), cudaMemcpyHostToDevice, st));
+    // product jobs of both sides: pass 0 T = O U_qc, pass 1 R = U_qr^T T
+    int ntiles[2] = {0, 0};
+    std::vector<RnJob> jobs[2];
+    for (int pass = 0; pass < 2; ++pass) jobs[pass].reserve(npairs);
+    for (int s = 0; s < 2; ++s) {
+        const Side &S = sd[s];
+        const int64_t ob = s ? sd[0].o_tot : 0, tb = s ? sd[0].t_tot : 0, rb = s ? sd[0].r_tot : 0,
+                      ub = s ? sd[0].u_tot : 0;
+        for (const Pair &pr : S.pairs) {
+            const int nr = S.kl->dims[pr.qr], nc = S.kl->dims[pr.qc], kr = S.kq[pr.qr], kc = S.kq[pr.qc];
+            double *T = w.tbuf + tb + pr.t_off;
+            const int tn = (kc + RN_TILE - 1) / RN_TILE;
+            RnJob a{w.dblk + ob + pr.o_off, w.ublk + ub + S.uoff[pr.qc], T, nr, kc, nc, nr, nc, nr, 0,
+                    (nr + RN_TILE - 1) / RN_TILE, ntiles[0], 0};
+            ntiles[0] += a.tiles_m * tn;
+            jobs[0].push_back(a);
+            RnJob b{w.ublk + ub + S.uoff[pr.qr], T, w.rbuf + rb + pr.r_off, kr, kc, nr, nr, nr, kr, 1,
+                    (kr + RN_TILE - 1) / RN_TILE, ntiles[1], 0};
+            ntiles[1] += b.tiles_m * tn;
+            jobs[1].push_back(b);
+        }
+    }
+    // index staging, 16-byte aligned sections: kept-column gather tables of
+    // both sides (src offsets, lengths, 64-bit dst offsets), the jobs of the
+    // two passes, and their tile -> job maps
+    auto al16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    const size_t b_src = 0, b_len = al16(b_src + sizeof(int) * (size_t)ms_tot);
+    const size_t b_dst = al16(b_len + sizeof(int) * (size_t)ms_tot);
+    const size_t b_jobs = al16(b_dst + sizeof(int64_t) * (size_t)ms_tot);
+    const size_t b_tj = al16(b_jobs + sizeof(RnJob) * (size_t)npairs * 2);
+    const size_t b_end = b_tj + sizeof(int) * (size_t)(ntiles[0] + ntiles[1]);
+    const int64_t words = (int64_t)((b_end + sizeof(int) - 1) / sizeof(int));
+    if ((rc = grow_host(c, &w.hitab, w.cap_hitab, words))) return rc;
+    if ((rc = grow_dev(c, &w.itab, w.cap_itab, words))) return rc;
+    char *hb = (char *)w.hitab;
+    {
+        int *src = (int *)(hb + b_src), *len = (int *)(hb + b_len);
+        int64_t *dst = (int64_t *)(hb + b_dst);
+        int at = 0;
+        for (int s = 0; s < 2; ++s) {
+            const Side &S = sd[s];
+            const int64_t ub = s ? sd[0].u_tot : 0;
+            for (int j = 0; j < S.ms; ++j, ++at) {
+                const int q = S.kl->q[j];
+                src[at] = S.kl->off[j];
+                dst[at] = ub + S.uoff[q] + (int64_t)S.loc[j] * S.kl->dims[q];
+                len[at] = S.kl->dims[q];
+            }
+        }
+        RnJob *hj = (RnJob *)(hb + b_jobs);
+        std::copy(jobs[0].begin(), jobs[0].end(), hj);
+        std::copy(jobs[1].begin(), jobs[1].end(), hj + npairs);
+        int *tj = (int *)(hb + b_tj);
+        for (int pass = 0; pass < 2; ++pass) {
+            int *t = tj + (pass ? ntiles[0] : 0);
+            for (int i = 0; i < npairs; ++i) {
+                const RnJob &jb = jobs[pass][i];
+                const int nt = jb.tiles_m * ((jb.n + RN_TILE - 1) / RN_TILE);
+                for (int k = 0; k < nt; ++k) t[jb.tile0 + k] = i + (pass ? npairs : 0);
+            }
+        }
+    }
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.itab, w.hitab, b_end, cudaMemcpyHostToDevice, st));
+    const char *db = (const char *)w.itab;
+    // U_q from the compact kept columns (each side's columns live in its
+    // own compact buffer)
+    for (int s = 0, at = 0; s < 2; at += sd[s].ms, ++s) {
+        if (sd[s].ms == 0) continue;
+        ++c.launches;
+        k_gather_u<<<sd[s].ms, 128, 0, st>>>(kl[s].dcomp, (const int *)(db + b_src) + at,
+                                             (const int64_t *)(db + b_dst) + at, (const int *)(db + b_len) + at,
+                                             w.ublk);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
+    const RnJob *dj = (const RnJob *)(db + b_jobs);
+    const int *dtj = (const int *)(db + b_tj);
+    for (int pass = 0; pass < 2; ++pass) {
+        if (ntiles[pass] == 0) continue;
+        ++c.launches;
+        k_rn_gemm<<<ntiles[pass], 256, 0, st>>>(dj, dtj + (pass ? ntiles[0] : 0));
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.hres, w.rbuf, (size_t)r_tot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+    c.renorm_phase_ms[1] += ms_since(t1);
+    const auto t2 = clk::now();
+    run_pair([&] { assemble_side(sd[0], w.hres); }, [&] { assemble_side(sd[1], w.hres + sd[0].r_tot); });
+    c.renorm_phase_ms[2] += ms_since(t2);
     return NSS_OK;
 }
 
