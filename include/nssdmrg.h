@@ -186,6 +186,21 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
             int32_t *kept_left, int32_t *kept_right,
             double *u_left, double *u_right);
 
+/* OdotV_direct (src/DMRG_MEASURE.f90:653-705): ov = (O x 1) v for label
+ * 'l' (or 's') and ov = (1 x O) v for 'r' (or 'e') on the uploaded
+ * superblock, where ops[k] (k < nsb) is the block operator filtered to
+ * sector k's left / right states (Dl_k x Dl_k or Dr_k x Dr_k, 0-based CSR)
+ * and v, ov are host arrays of length nss_sb_dim. */
+int nss_odotv(nss_ctx *ctx, char label, const nss_csr *ops, const double *v, double *ov);
+
+/* Average_Op_dmrg (src/DMRG_MEASURE.f90:595-646): <psi| O |psi> for a whole
+ * block operator O (m_left x m_left for label 'l', m_right x m_right for
+ * 'r', 0-based CSR).  O is filtered to every sector's states with the sector
+ * maps of the uploaded descriptor (ai / bi, the reference's LI / RI) and
+ * applied on the device.  psi: host vector of length nss_sb_dim, or NULL
+ * for the ground state of the last nss_eigh. */
+int nss_average_op(nss_ctx *ctx, char label, const nss_csr *op, const double *psi, double *val);
+
 /* Eigensolver statistics of the last nss_rdm: rho blocks diagonalised by the
  * library's own FP64 eigensolver (Householder tridiagonalisation, bisection,
  * twisted-factorisation vectors of the kept states), blocks sent to the
@@ -298,6 +313,9 @@ typedef struct {
     double  deg_evals_threshold; /* default 0.1 */
     uint64_t seed;
     int32_t precision;      /* NSS_PREC_* */
+    int32_t save_umat;      /* keep every renormalisation's rotation matrix
+                               on the host (SAVE_UMAT with STORE_UMAT='b'),
+                               which nss_dmrg_measure needs */
 } nss_dmrg_params;
 
 typedef struct {
@@ -348,6 +366,14 @@ int       nss_dmrg_prepare_last(nss_dmrg *d);
  * the next call on d). */
 int       nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out);
 int       nss_dmrg_nrecords(const nss_dmrg *d);
+/* Measure_DMRG_scalar (src/DMRG_MEASURE.f90:148-220, 288-486, 595-705) after
+ * a run with save_umat: for each position pos[i] (1-based along the chain,
+ * OBC) the site operator op (dot basis, d x d, 0-based CSR) is placed at
+ * that site of the block holding it (Build_Op_dmrg), carried to the last
+ * step's block by the stored rotations and enlargements (Advance_Op_dmrg)
+ * on the host, and averaged in the last step's ground state on the device
+ * (Average_Op_dmrg / OdotV_direct).  out[i] = <gs| O(pos[i]) |gs>. */
+int       nss_dmrg_measure(nss_dmrg *d, const nss_csr *op, const int32_t *pos, int npos, double *out);
 int       nss_dmrg_records(const nss_dmrg *d, nss_step_record *out, int max);
 
 #ifdef __cplusplus

@@ -77,7 +77,8 @@ class DmrgParams(C.Structure):
                 ("u", C.c_double), ("hfmode", C.c_int32), ("dmrg_qn", C.c_double * 2), ("ldmrg", C.c_int32),
                 ("mdmrg", C.c_int32), ("nsweep", C.c_int32), ("msweep", C.POINTER(C.c_int32)),
                 ("lanc_neigen", C.c_int32), ("lanc_niter", C.c_int32), ("lanc_tolerance", C.c_double),
-                ("deg_evals_threshold", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int32)]
+                ("deg_evals_threshold", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int32),
+                ("save_umat", C.c_int32)]
 
 
 class StepRecord(C.Structure):
@@ -147,6 +148,9 @@ def lib():
         "nss_rdm_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "nss_rdm_fallback_reasons": (C.c_int, [P, C.POINTER(C.c_int64)]),
         "nss_dmrg_nrecords": (C.c_int, [P]),
+        "nss_dmrg_measure": (C.c_int, [P, C.POINTER(Csr), C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_double)]),
+        "nss_odotv": (C.c_int, [P, C.c_char, C.POINTER(Csr), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "nss_average_op": (C.c_int, [P, C.c_char, C.POINTER(Csr), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "nss_dmrg_records": (C.c_int, [P, C.POINTER(StepRecord), C.c_int]),
     }
     for name, (res, args) in sig.items():
@@ -384,6 +388,27 @@ class Superblock:
         self._check(lib().nss_chunk_stats(self._ctx, C.byref(ms), C.byref(nl), C.byref(it), C.byref(cols)))
         return ms.value, nl.value, it.value, cols.value
 
+    def odotv(self, label, ops, v):
+        """OdotV_direct: (O x 1) v for label 'l', (1 x O) v for 'r'; ops[k]
+        is the block operator filtered to sector k's states (scipy sparse)."""
+        keep = _Keep()
+        arr = (Csr * len(ops))(*[keep.csr(m) for m in ops])
+        v = keep.arr(v, np.float64)
+        ov = np.empty_like(v)
+        self._check(lib().nss_odotv(self._ctx, label.encode()[:1], arr, _p(v, C.c_double), _p(ov, C.c_double)))
+        return ov
+
+    def average_op(self, label, op, psi=None):
+        """Average_Op_dmrg: <psi| O |psi> for a whole block operator O (scipy
+        sparse, m_block x m_block) on side 'l' or 'r'; psi None = the ground
+        state of the last sb_diag."""
+        keep = _Keep()
+        c = keep.csr(op)
+        pp = _p(keep.arr(psi, np.float64), C.c_double) if psi is not None else None
+        val = C.c_double()
+        self._check(lib().nss_average_op(self._ctx, label.encode()[:1], C.byref(c), pp, C.byref(val)))
+        return val.value
+
     def rdm_stats(self):
         """(own-eigensolver blocks, library blocks, own blocks recomputed by
         the library) of the last sb_get_rdm."""
@@ -524,7 +549,8 @@ class DMRG:
 
     def __init__(self, model, ldmrg, mdmrg, msweep=(), jz=1.0, jxy=1.0, t=1.0, u=0.0, hfmode=True,
                  dmrg_qn=(0.0, 0.0), lanc_neigen=1, lanc_niter=512, lanc_tolerance=1e-12,
-                 deg_evals_threshold=0.1, seed=1234, precision=NSS_PREC_FP64, device=0, sb=None):
+                 deg_evals_threshold=0.1, seed=1234, precision=NSS_PREC_FP64, device=0, sb=None,
+                 save_umat=False):
         self.sb = sb or Superblock(device)
         p = DmrgParams()
         p.model, p.jz, p.jxy, p.t, p.u, p.hfmode = model, jz, jxy, t, u, int(hfmode)
@@ -536,6 +562,7 @@ class DMRG:
         p.msweep = _p(self._ms, C.c_int32)
         p.lanc_neigen, p.lanc_niter, p.lanc_tolerance = lanc_neigen, lanc_niter, lanc_tolerance
         p.deg_evals_threshold, p.seed, p.precision = deg_evals_threshold, seed, precision
+        p.save_umat = int(save_umat)
         self._p = p
         self._d = lib().nss_dmrg_create(self.sb._ctx, C.byref(p))
         if not self._d:
@@ -562,6 +589,19 @@ class DMRG:
 
     def prepare_last(self):
         self.sb._check(lib().nss_dmrg_prepare_last(self._d))
+
+    def measure(self, op, pos):
+        """Measure_DMRG for one site operator op (d x d, dense or scipy
+        sparse, dot basis) at the 1-based chain positions pos, after a run
+        with save_umat=True: <gs|O(pos)|gs> per position."""
+        import scipy.sparse as sp
+        keep = _Keep()
+        c = keep.csr(sp.csr_matrix(np.asarray(op.todense() if hasattr(op, "todense") else op, np.float64)))
+        pos = keep.arr(pos, np.int32)
+        out = np.empty(len(pos))
+        self.sb._check(lib().nss_dmrg_measure(self._d, C.byref(c), _p(pos, C.c_int32), len(pos),
+                                              _p(out, C.c_double)))
+        return out
 
     def export_superblock(self) -> SbDesc:
         d = SbDesc()

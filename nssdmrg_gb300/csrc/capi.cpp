@@ -108,6 +108,7 @@ void nss_destroy(nss_ctx *ctx) {
     nss::lanczos_release(ctx->c);
     nss::rdm_release(ctx->c);
     nss::renorm_release(ctx->c);
+    nss::measure_release(ctx->c);
     nss::ctx_free(ctx->c, ctx->d_v);
     nss::ctx_free(ctx->c, ctx->d_hv);
     nss::ctx_free(ctx->c, ctx->d_psi);
@@ -253,6 +254,95 @@ int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     NSS_CUDA_TRY(c, cudaMemcpyAsync(hv, ctx->d_hv, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
     return NSS_OK;
+}
+
+namespace {
+
+// 'l'/'s' -> 0 (left, system), 'r'/'e' -> 1 (right, environment), else -1
+int side_of(char label) {
+    switch (label) {
+    case 'l': case 'L': case 's': case 'S': return 0;
+    case 'r': case 'R': case 'e': case 'E': return 1;
+    default: return -1;
+    }
+}
+
+}  // namespace
+
+int nss_odotv(nss_ctx *ctx, char label, const nss_csr *ops, const double *v, double *ov) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_odotv: no superblock uploaded");
+    const int side = side_of(label);
+    if (side < 0) return fail(ctx, NSS_ERR_INVALID, "nss_odotv: label not [l,r]");
+    if (!ops || !v || !ov) return fail(ctx, NSS_ERR_INVALID, "nss_odotv: null argument");
+    cudaSetDevice(ctx->c.device);
+    return guarded(ctx, [&] {
+        nss::Ctx &c = ctx->c;
+        const int64_t n = c.sb.n;
+        int rc = ensure_tmp(ctx, n);
+        if (rc) return rc;
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, v, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        if ((rc = nss::odotv_device(c, side, ops, ctx->d_v, ctx->d_hv, nullptr))) return rc;
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(ov, ctx->d_hv, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+        return NSS_OK;
+    });
+}
+
+int nss_average_op(nss_ctx *ctx, char label, const nss_csr *op, const double *psi, double *val) {
+    if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
+    if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_average_op: no superblock uploaded");
+    const int side = side_of(label);
+    if (side < 0) return fail(ctx, NSS_ERR_INVALID, "Average_op_dmrg error: label not [l,r]");
+    if (!op || !val) return fail(ctx, NSS_ERR_INVALID, "nss_average_op: null argument");
+    cudaSetDevice(ctx->c.device);
+    return guarded(ctx, [&] {
+        nss::Ctx &c = ctx->c;
+        const nss::DevSb &s = c.sb;
+        const std::vector<int> &maps = side ? s.bi : s.ai;
+        const std::vector<int> &moff = side ? s.bi_off : s.ai_off;
+        if (maps.empty()) return fail(ctx, NSS_ERR_STATE, "nss_average_op: the descriptor carried no sector maps (ai/bi)");
+        const int mb = side ? s.m_right : s.m_left;
+        if (op->nrow != mb || op->ncol != mb || !op->rowptr || (op->rowptr[mb] > 0 && (!op->colidx || !op->vals)))
+            return fail(ctx, NSS_ERR_INVALID, "nss_average_op: operator is not m_block x m_block");
+        for (int i = 0; i < mb; ++i)
+            if (op->rowptr[i + 1] < op->rowptr[i]) return fail(ctx, NSS_ERR_INVALID, "nss_average_op: bad row pointers");
+        // sp_filter(Oi, LI(isb)%states) per sector (:617-625)
+        std::vector<int> local(mb, -1);
+        std::vector<std::vector<int>> rp(s.nsb), cl(s.nsb);
+        std::vector<std::vector<double>> vl(s.nsb);
+        std::vector<nss_csr> ops(s.nsb);
+        for (int k = 0; k < s.nsb; ++k) {
+            const int a = moff[k], b = moff[k + 1];
+            for (int p = a; p < b; ++p) local[maps[p]] = p - a;
+            rp[k].assign(1, 0);
+            for (int p = a; p < b; ++p) {
+                const int i = maps[p];
+                for (int e = op->rowptr[i]; e < op->rowptr[i + 1]; ++e) {
+                    const int j = op->colidx[e];
+                    if (j < 0 || j >= mb) return fail(ctx, NSS_ERR_INVALID, "nss_average_op: column out of range");
+                    if (local[j] < 0) continue;
+                    cl[k].push_back(local[j]);
+                    vl[k].push_back(op->vals[e]);
+                }
+                rp[k].push_back((int)cl[k].size());
+            }
+            for (int p = a; p < b; ++p) local[maps[p]] = -1;
+            ops[k] = nss_csr{b - a, b - a, rp[k].data(), cl[k].data(), vl[k].data()};
+        }
+        const double *d_psi = nullptr;
+        if (psi) {
+            int rc = ensure_tmp(ctx, s.n);
+            if (rc) return rc;
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, psi, s.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+            d_psi = ctx->d_v;
+        } else {
+            if (c.lz.neigen_done < 1 || c.lz.n != s.n)
+                return fail(ctx, NSS_ERR_STATE, "nss_average_op: no ground state (call nss_eigh or pass psi)");
+            d_psi = c.lz.evecs;
+        }
+        return nss::odotv_device(c, side, ops.data(), d_psi, nullptr, val);
+    });
 }
 
 int nss_eigh(nss_ctx *ctx, int neigen, int nitermax, int ncv, double tol, uint64_t seed, int precision,
@@ -451,6 +541,36 @@ int nss_dmrg_finite(nss_dmrg *d) {
     if (!d) return NSS_ERR_INVALID;
     cudaSetDevice(d->ctx->c.device);
     return guarded(d->ctx, [&] { return d->drv.finite(); });
+}
+
+int nss_dmrg_measure(nss_dmrg *d, const nss_csr *op, const int32_t *pos, int npos, double *out) {
+    if (!d) return NSS_ERR_INVALID;
+    if (!op || (npos > 0 && (!pos || !out)) || npos < 0) return fail(d->ctx, NSS_ERR_INVALID, "nss_dmrg_measure: bad arguments");
+    cudaSetDevice(d->ctx->c.device);
+    return guarded(d->ctx, [&] {
+        const int dd = d->drv.dot.dim;
+        if (op->nrow != dd || op->ncol != dd || !op->rowptr)
+            return fail(d->ctx, NSS_ERR_INVALID, "nss_dmrg_measure: operator is not d x d");
+        nss::Csr o;
+        o.init(dd, dd);
+        for (int i = 0; i < dd; ++i) {
+            for (int e = op->rowptr[i]; e < op->rowptr[i + 1]; ++e) {
+                if (op->colidx[e] < 0 || op->colidx[e] >= dd)
+                    return fail(d->ctx, NSS_ERR_INVALID, "nss_dmrg_measure: column out of range");
+                o.col.push_back(op->colidx[e]);
+                o.val.push_back(op->vals[e]);
+            }
+            o.rowptr[i + 1] = (int)o.col.size();
+        }
+        for (int k = 0; k < npos; ++k) {
+            int side = 0;
+            const nss::Csr oi = d->drv.site_op_on_block(o, pos[k], &side);
+            const nss_csr view{oi.nrow, oi.ncol, oi.rowptr.data(), oi.col.data(), oi.val.data()};
+            int rc = nss_average_op(d->ctx, side ? 'r' : 'l', &view, nullptr, &out[k]);
+            if (rc) return rc;
+        }
+        return NSS_OK;
+    });
 }
 
 int nss_dmrg_prepare_last(nss_dmrg *d) {

@@ -206,7 +206,9 @@ struct Ctx {
     int rdm_max_block = 0;
     char *sb_arena = nullptr, *sb_stage = nullptr;   // superblock pool: device arena, pinned staging
     size_t sb_arena_cap = 0, sb_stage_cap = 0;
-    double renorm_phase_ms[3] = {0, 0, 0};   // host: scan+extract, device wait, CSR assembly (summed over calls)
+    double renorm_phase_ms[3] = {0, 0, 0};
+    char *ms_dev = nullptr, *ms_host = nullptr;   // OdotV tables: device, pinned staging
+    size_t ms_cap = 0;   // host: scan+extract, device wait, CSR assembly (summed over calls)
 };
 
 // Allocation through the context budget.
@@ -303,10 +305,21 @@ void rdm_release(Ctx &c);
 // k_renorm.cu: blk's operators <- U^T O U for the kept columns kl, blk's
 // basis <- kept_qn (one QN tuple per kept column)
 struct Block;
+struct Csr;
 // Both blocks of a step at once: blk[s] is renormalised with the kept
 // columns kl[s] and gets the basis kept_qn[s].
 int renorm_device(Ctx &c, const KeptLayout kl[2], Block *blk[2], const std::vector<std::vector<double>> *kept_qn[2]);
 void renorm_release(Ctx &c);
+// The rotation matrix U (m_block x m_s, CSR, exact zeros dropped) of one
+// side from its kept columns, for the stored rotations of measurements.
+int kept_u_csr(Ctx &c, const KeptLayout &kl, int mblock, Csr &u);
+
+// k_measure.cu: OdotV_direct / Average_Op_dmrg on the uploaded superblock.
+// ops[k] (k < nsb): the block operator filtered to sector k's left
+// (label 0) or right (label 1) states; d_ov (may be null) receives O v and
+// *val (may be null) v . O v.
+int odotv_device(Ctx &c, int label, const nss_csr *ops, const double *d_v, double *d_ov, double *val);
+void measure_release(Ctx &c);
 
 }  // namespace nss
 

@@ -128,6 +128,7 @@ Block enlarge_block(const Block &blk, const Block &dot, char label, const double
     out.dim = blk.dim;
     out.qdim = blk.qdim;
     out.fermion = blk.fermion;
+    out.omats = blk.omats;
     out.ops.reserve(blk.ops.size());
     for (const Op &o : blk.ops) out.ops.push_back({o.key, Csr{}, o.type});
     Csr hb, hd, h2;
@@ -223,6 +224,9 @@ int Driver::init(Ctx *c, const nss_dmrg_params &params) {
     } else {
         hij[0] = p.jz; hij[1] = 0; hij[2] = 0; hij[3] = p.jxy / 2.0;   // Hlr = diag(Jp, Jx/2)
     }
+    // the site block's rotation list starts with the identity
+    // (constructor_from_site, src/BLOCKS/BLOCKS.f90:140-142)
+    dot.omats = {std::make_shared<const Csr>(csr_identity(dot.dim))};
     left = dot;
     right = dot;
     return NSS_OK;
@@ -274,6 +278,36 @@ int Driver::step(int type, int label, int sweep) {
     rec.ms_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     records.push_back(rec);
     return NSS_OK;
+}
+
+// Build_Op_dmrg (src/DMRG_MEASURE.f90:288-386) and Advance_Op_dmrg
+// (:398-486), OBC: the site sits at index i of the block holding it (i = pos
+// on the left, N+1-pos on the right); it enters as Id(D) x Op on the left
+// (Op x Id(D) on the right) of the enlarged length-i block, D the states of
+// the length-(i-1) block, and is rotated with omat(i), ..., omat(Lside-1)
+// and enlarged by the site after each rotation.
+Csr Driver::site_op_on_block(const Csr &op, int pos, int *side) const {
+    const int L = left.length, R = right.length, N = L + R;
+    if (pos < 1 || pos > N) throw std::runtime_error("Build_op_dmrg error: Pos not in [1,Ldmrg]");
+    const bool rgt = pos > L;
+    const Block &b = rgt ? right : left;
+    const int i = rgt ? N + 1 - pos : pos, iend = (rgt ? R : L) - 1;
+    if ((int)b.omats.size() < std::max(iend, i - 1))
+        throw std::runtime_error("Init_Measure_DMRG: No rotation matrices are present (run with save_umat)");
+    if (op.nrow != dot.dim || op.ncol != dot.dim) throw std::runtime_error("measure: operator is not d x d");
+    Csr oi = op;
+    if (i > 1) {
+        const int D = b.omats[i - 2]->ncol;
+        oi = rgt ? csr_kron(op, csr_identity(D)) : csr_kron(csr_identity(D), op);
+    }
+    for (int it = i; it <= iend; ++it) {
+        const Csr &u = *b.omats[it - 1];
+        if (u.nrow != oi.nrow) throw std::runtime_error("Advance_Op_DMRG: rotation does not match the operator");
+        oi = csr_matmul(csr_matmul(csr_transpose(u), oi), u);
+        oi = rgt ? csr_kron(csr_identity(dot.dim), oi) : csr_kron(oi, csr_identity(dot.dim));
+    }
+    *side = rgt ? 1 : 0;
+    return oi;
 }
 
 int Driver::infinite() {
@@ -434,6 +468,13 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
         const auto t_r = std::chrono::steady_clock::now();
         for (double &x : c.renorm_phase_ms) x = 0.0;
         if (dev_renorm) {
+            if (p.save_umat) {
+                // put_omat(str(length), trRho) (src/DMRG_RDM.f90:225, :298)
+                Csr ul, ur;
+                if ((rc = kept_u_csr(c, kl[0], left.dim, ul)) || (rc = kept_u_csr(c, kl[1], right.dim, ur))) return rc;
+                left.omats.push_back(std::make_shared<const Csr>(std::move(ul)));
+                right.omats.push_back(std::make_shared<const Csr>(std::move(ur)));
+            }
             Block *bl[2] = {&left, &right};
             const std::vector<Qn> *kq[2] = {&ql, &qr};
             if ((rc = renorm_device(c, kl, bl, kq))) return rc;
@@ -445,6 +486,10 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             renormalize(left, cul, ql);
             renormalize(right, cur, qr);
             rec.nnz_u = cul.nnz() + cur.nnz();
+            if (p.save_umat) {
+                left.omats.push_back(std::make_shared<const Csr>(cul));
+                right.omats.push_back(std::make_shared<const Csr>(cur));
+            }
         }
         rec.nnz_ops = 0;
         for (const auto &o : left.ops) rec.nnz_ops += o.m.nnz();

@@ -38,6 +38,10 @@ struct Driver {
     int step(int type, int label, int sweep);
     int infinite();
     int finite();
+    // Build_Op_dmrg + Advance_Op_dmrg: the site operator op (dot basis) at
+    // chain position pos, on the last step's enlarged block holding it;
+    // *side = 0 (left) or 1 (right)
+    Csr site_op_on_block(const Csr &op, int pos, int *side) const;
 };
 
 }  // namespace nss

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <exception>
 #include <map>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -93,6 +94,11 @@ struct Block {
     bool fermion = false;
     std::vector<double> basis;   // dim*qdim
     std::vector<Op> ops;         // ordered as the reference's operators_list
+    // rotation matrices of the renormalisations that built the block
+    // (omatrices, src/BLOCKS/BLOCKS.f90:21): omats[i] belongs to length i+1,
+    // omats[0] is the site's identity; shared, since the finite algorithm
+    // copies blocks and never changes a stored rotation
+    std::vector<std::shared_ptr<const Csr>> omats;
 
     Csr &op(const std::string &key);
     const Csr &op(const std::string &key) const;

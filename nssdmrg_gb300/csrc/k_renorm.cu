@@ -403,4 +403,29 @@ int renorm_device(Ctx &c, const KeptLayout kl[2], Block *blk[2], const std::vect
     return NSS_OK;
 }
 
+int kept_u_csr(Ctx &c, const KeptLayout &kl, int mblock, Csr &u) {
+    int64_t tot = 0;
+    for (int j = 0; j < kl.ms; ++j) tot = std::max<int64_t>(tot, (int64_t)kl.off[j] + kl.dims[kl.q[j]]);
+    std::vector<double> h((size_t)tot);
+    if (tot) NSS_CUDA_TRY(c, cudaMemcpy(h.data(), kl.dcomp, (size_t)tot * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<std::vector<std::pair<int, double>>> rows(mblock);
+    for (int j = 0; j < kl.ms; ++j) {
+        const int q = kl.q[j];
+        for (int p = 0; p < kl.dims[q]; ++p) {
+            const int st = kl.maps[kl.map_off[q] + p];
+            const double v = h[(size_t)kl.off[j] + p];
+            if (st >= 0 && st < mblock && v != 0.0) rows[st].push_back({j, v});
+        }
+    }
+    u.init(mblock, kl.ms);
+    for (int i = 0; i < mblock; ++i) {
+        for (const auto &e : rows[i]) {
+            u.col.push_back(e.first);
+            u.val.push_back(e.second);
+        }
+        u.rowptr[i + 1] = (int)u.col.size();
+    }
+    return NSS_OK;
+}
+
 }  // namespace nss

@@ -113,13 +113,16 @@ class Block:
     sitetype: str                      # "spin" | "fermion"
     basis: np.ndarray                  # [dim, qdim] float64 QN per state
     ops: dict = field(default_factory=dict)   # key -> (csr, type), ordered
+    # omatrices (src/BLOCKS/BLOCKS.f90:21): omats[i] is the rotation of the
+    # block of length i+1; a site block starts with its identity (:140-142)
+    omats: list = field(default_factory=list)
 
     def op(self, key):
         return self.ops[key][0]
 
     def copy(self):
         return Block(self.length, self.dim, self.sitetype, self.basis.copy(),
-                     {k: (v[0].copy(), v[1]) for k, v in self.ops.items()})
+                     {k: (v[0].copy(), v[1]) for k, v in self.ops.items()}, list(self.omats))
 
     def sectors(self) -> Sectors:
         return Sectors(self.basis)
@@ -617,14 +620,62 @@ def kept_qns(rho: RhoBlocks, m: int) -> np.ndarray:
 
 
 def renormalize(blk: Block, u: sp.csr_matrix, qns: np.ndarray) -> Block:
-    """operators_renormalization (src/DMRG_RDM.f90:355-404): O <- U^T O U."""
+    """operators_renormalization (src/DMRG_RDM.f90:355-404): O <- U^T O U;
+    the rotation is stored as put_omat(str(length), trRho) does (:225, :298)."""
     out = blk.copy()
     ut = u.T.tocsr()
     for key, (o, t) in blk.ops.items():
         out.ops[key] = ((ut @ o @ u).tocsr(), t)
     out.dim = u.shape[1]
     out.basis = np.asarray(qns, dtype=np.float64).reshape(out.dim, -1)
+    out.omats = list(blk.omats) + [u.tocsr()]
     return out
+
+
+def odotv_direct(ops, v, label, sb: "Superblock"):
+    """OdotV_direct (src/DMRG_MEASURE.f90:653-705), loop for loop: ops[k] is
+    the block operator filtered to sector k's left ('l') or right ('r')
+    states; sector k of v is Psi[il, ir] at ir + il*Drs + Offset (0-based)."""
+    ov = np.zeros_like(v)
+    for k in range(len(sb.Dls)):
+        dl, dr, off = int(sb.Dls[k]), int(sb.Drs[k]), int(sb.Offset[k])
+        o = sp.csr_matrix(ops[k])
+        if label == "l":
+            for ir in range(dr):
+                for il in range(dl):
+                    i = ir + il * dr + off
+                    for p in range(o.indptr[il], o.indptr[il + 1]):
+                        ov[i] += o.data[p] * v[ir + o.indices[p] * dr + off]
+        else:
+            for il in range(dl):
+                for ir in range(dr):
+                    i = ir + il * dr + off
+                    for p in range(o.indptr[ir], o.indptr[ir + 1]):
+                        ov[i] += o.data[p] * v[o.indices[p] + il * dr + off]
+    return ov
+
+
+def odotv_vectorised(ops, v, label, sb: "Superblock"):
+    """The same product per sector as a matrix product (O Psi or Psi O^T)."""
+    ov = np.zeros_like(v)
+    for k in range(len(sb.Dls)):
+        dl, dr, off = int(sb.Dls[k]), int(sb.Drs[k]), int(sb.Offset[k])
+        psi = v[off:off + dl * dr].reshape(dl, dr)
+        o = sp.csr_matrix(ops[k])
+        ov[off:off + dl * dr] = (o @ psi if label == "l" else (o @ psi.T).T).ravel()
+    return ov
+
+
+def filter_sectors(oi, label, sb: "Superblock"):
+    """sp_filter(Oi, LI(isb)%states) / RI per sector (src/DMRG_MEASURE.f90:617-625)."""
+    oi = sp.csr_matrix(oi)
+    maps = sb.AI if label == "l" else sb.BI
+    return [oi[np.asarray(m)][:, np.asarray(m)].tocsr() for m in maps]
+
+
+def average_op(oi, label, sb: "Superblock", psi):
+    """Average_Op_dmrg (src/DMRG_MEASURE.f90:595-646): psi . OdotV(filtered Oi)."""
+    return float(np.dot(psi, odotv_vectorised(filter_sectors(oi, label, sb), psi, label, sb)))
 
 
 def entropy(lam: np.ndarray) -> float:
@@ -680,6 +731,8 @@ class DMRG:
         self.hij = np.asarray(hij, dtype=np.float64)
         self.dot = dot
         self.p = p
+        if not dot.omats:
+            dot.omats = [sp.identity(dot.dim, format="csr")]
         self.left = (left or dot).copy()
         self.right = (right or dot).copy()
         self.records: list[StepRecord] = []
@@ -703,6 +756,7 @@ class DMRG:
         ev, evec, solver = sb_diag(self.left, self.right, sb, ds, p, self.hij, p.norb, self.rng)
         if self.keep_setups:
             self.setups.append((self.left.copy(), self.right.copy(), sb, ds, ev, evec))
+        self.last_sb, self.last_psi = sb, evec[:, 0].copy()
         lsec, rsec = self.left.sectors(), self.right.sectors()
         lblocks, rblocks = build_density_matrices(sb, evec[:, 0], lsec, rsec)
         rho_l, rho_r = eigh_blocks(lblocks), eigh_blocks(rblocks)
@@ -727,6 +781,39 @@ class DMRG:
                     self.right, rec.trunc_right, rec.m_right = nb, eps, m_s
         self.records.append(rec)
         return rec
+
+    def site_op(self, op, pos):
+        """Build_Op_dmrg + Advance_Op_dmrg, OBC (src/DMRG_MEASURE.f90:288-486):
+        the site operator op at chain position pos (1-based) on the last
+        step's enlarged block holding it; returns (operator, 'l' | 'r')."""
+        L, R = self.left.length, self.right.length
+        n = L + R
+        if pos < 1 or pos > n:
+            raise ValueError("Build_op_dmrg error: Pos not in [1,Ldmrg]")
+        label = "r" if pos > L else "l"
+        blk = self.right if label == "r" else self.left
+        i = n + 1 - pos if label == "r" else pos
+        iend = (R if label == "r" else L) - 1
+        d = self.dot.dim
+        oi = sp.csr_matrix(op)
+        if i > 1:
+            big_d = blk.omats[i - 2].shape[1]
+            oi = kron(oi, eye(big_d)) if label == "r" else kron(eye(big_d), oi)
+        for it in range(i, iend + 1):
+            u = blk.omats[it - 1]
+            oi = (u.T @ oi @ u).tocsr()
+            oi = kron(eye(d), oi) if label == "r" else kron(oi, eye(d))
+        return oi, label
+
+    def measure(self, op, positions):
+        """Measure_DMRG_scalar (src/DMRG_MEASURE.f90:172-220) in the ground
+        state of the last step."""
+        sb, psi = self.last_sb, self.last_psi
+        out = []
+        for pos in positions:
+            oi, label = self.site_op(op, pos)
+            out.append(average_op(oi, label, sb, psi))
+        return np.array(out)
 
     def infinite(self):
         while self.left.length < self.p.Ldmrg:

@@ -84,6 +84,9 @@ def trajectories(ref: Path):
                            "dmrg_qn": [0.0], "left_length": e[:, 0].astype(int).tolist(),
                            "energy": e[:, 1:3].tolist(), "entropy": s.tolist(),
                            "source": "test/src/Spin1d_SU2/L40.energy.check, L40.Sentropy.check"}
+    # Measure_DMRG of S_z at sites 1..40 after that run (spinSU2_1d.f90:41, asserted at 1e-8)
+    out["spin_L40_M20"]["measure"] = {"sz": np.loadtxt(t / "Spin1d_SU2" / "sz.check").tolist(),
+                                      "source": "test/src/Spin1d_SU2/sz.check"}
     e = np.loadtxt(t / "Hubbard1d" / "L40.energy.check")
     s = np.loadtxt(t / "Hubbard1d" / "L40.Sentropy.check")
     out["hubbard_L40_M40"] = {"model": "hubbard", "ldmrg": 40, "mdmrg": 40, "neigen": 1, "u": 0.0,
@@ -91,6 +94,11 @@ def trajectories(ref: Path):
                               "left_length": list(range(2, 41)), "energy": e[:, None].tolist(),
                               "entropy": s.tolist(),
                               "source": "test/src/Hubbard1d/L40.energy.check, L40.Sentropy.check"}
+    # Measure_DMRG of n, n_up n_dw and (n_up - n_dw)^2 at sites 1..40 (hm_1d.f90:62-76,
+    # asserted at 1e-6)
+    out["hubbard_L40_M40"]["measure"] = {k: np.loadtxt(t / "Hubbard1d" / f"{k}.check").tolist()
+                                         for k in ("n", "d", "s2z")}
+    out["hubbard_L40_M40"]["measure"]["source"] = "test/src/Hubbard1d/{n,d,s2z}.check"
     e = np.loadtxt(pl / "Hubbard" / "U2" / "energyVSleft.length_L100_M50_iDMRG.dmrg")
     s = np.loadtxt(pl / "Hubbard" / "U2" / "SentropyVSleft.length_L100_M50_iDMRG.dmrg")
     # This published run used deg_evals_threshold = 0.01 (its DMRG.conf does
@@ -146,6 +154,28 @@ def oracle_runs():
     (OUT / "oracle_runs.json").write_text(json.dumps(res))
 
 
+def measure_runs():
+    """Oracle measurements (Measure_DMRG, src/DMRG_MEASURE.f90:148-705) where
+    the values are not fixed by symmetry: Hubbard U=4, HFMODE=F, L=20, M=64,
+    whose open ends make n_up n_dw vary along the chain, at every site (the
+    right half through the right block's rotations)."""
+    p = O.Params(Ldmrg=10, Mdmrg=64, lanc_neigen=1, dmrg_qn=(0.5, 0.5))
+    run = O.DMRG(O.hubbard_hij(1.0), O.electron_site(4.0, False), p)
+    run.infinite()
+    dot = run.dot
+    nup = (dot.op("C_l1_s1_n").T @ dot.op("C_l1_s1_n")).toarray()
+    ndw = (dot.op("C_l1_s2_n").T @ dot.op("C_l1_s2_n")).toarray()
+    ops = {"n": nup + ndw, "d": nup @ ndw, "s2z": (nup - ndw) @ (nup - ndw)}
+    pos = list(range(1, 21))
+    res = {"hubbard_U4_L20_M64": {"model": "hubbard", "ldmrg": 10, "mdmrg": 64, "u": 4.0, "hfmode": False,
+                                  "dmrg_qn": [0.5, 0.5], "neigen": 1, "pos": pos,
+                                  "energy_last": run.records[-1].energies.tolist(),
+                                  "ops": {k: v.tolist() for k, v in ops.items()},
+                                  "measure": {k: run.measure(v, pos).tolist() for k, v in ops.items()}}}
+    (OUT / "measure_runs.json").write_text(json.dumps(res))
+    print("measure runs", {k: v["measure"]["d"][:3] for k, v in res.items()})
+
+
 def c2_small():
     """A U=4, HFMODE=F Hubbard superblock (L=24, M=96) with oracle outputs."""
     p = O.Params(Ldmrg=12, Mdmrg=96, lanc_neigen=1, dmrg_qn=(0.5, 0.5))
@@ -169,8 +199,15 @@ def c2_small():
 
 if __name__ == "__main__":
     ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    kat(ref, "spin")
-    kat(ref, "hubbard")
-    trajectories(ref)
-    c2_small()
-    oracle_runs()
+    parts = set(sys.argv[2:]) or {"kat", "trajectories", "c2_small", "oracle_runs", "measure_runs"}
+    if "kat" in parts:
+        kat(ref, "spin")
+        kat(ref, "hubbard")
+    if "trajectories" in parts:
+        trajectories(ref)
+    if "c2_small" in parts:
+        c2_small()
+    if "oracle_runs" in parts:
+        oracle_runs()
+    if "measure_runs" in parts:
+        measure_runs()

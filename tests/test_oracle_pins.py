@@ -78,18 +78,41 @@ def test_loop_order_restatement_matches_vectorised():
     np.testing.assert_allclose(a, b, rtol=0, atol=1e-13 * np.abs(b).max())
 
 
+_L40_RUNS = {}
+
+
+def _l40_run(trajectories, key):
+    if key not in _L40_RUNS:
+        t = trajectories[key]
+        if t["model"] == "heisenberg_half":
+            p = O.Params(Ldmrg=t["ldmrg"], Mdmrg=t["mdmrg"], lanc_neigen=2, lanc_ncv_factor=5,
+                         lanc_dim_threshold=128, dmrg_qn=(0.0,))
+            run = O.DMRG(O.heisenberg_hij(), O.spin_site(2), p)
+        else:
+            p = O.Params(Ldmrg=t["ldmrg"], Mdmrg=t["mdmrg"], lanc_neigen=1, lanc_ncv_factor=10,
+                         lanc_dim_threshold=128, dmrg_qn=(0.5, 0.5))
+            run = O.DMRG(O.hubbard_hij(), O.electron_site(t["u"], t["hfmode"]), p)
+        run.infinite()
+        _L40_RUNS[key] = run
+    return _L40_RUNS[key]
+
+
+def measure_ops(model):
+    """The site operators the reference's test drivers measure: S_z
+    (spinSU2_1d.f90:41), and n, n_up n_dw, (n_up - n_dw)^2 built from the
+    dot's C operators as N_s = C_s^+ C_s (hm_1d.f90:62-76)."""
+    if model == "heisenberg_half":
+        return {"sz": np.diag([0.5, -0.5])}
+    dot = O.electron_site(0.0, True)
+    nup = (dot.op("C_l1_s1_n").T @ dot.op("C_l1_s1_n")).toarray()
+    ndw = (dot.op("C_l1_s2_n").T @ dot.op("C_l1_s2_n")).toarray()
+    return {"n": nup + ndw, "d": nup @ ndw, "s2z": (nup - ndw) @ (nup - ndw)}
+
+
 @pytest.mark.parametrize("key", ["spin_L40_M20", "hubbard_L40_M40"])
 def test_l40_trajectory(trajectories, key):
     t = trajectories[key]
-    if t["model"] == "heisenberg_half":
-        p = O.Params(Ldmrg=t["ldmrg"], Mdmrg=t["mdmrg"], lanc_neigen=2, lanc_ncv_factor=5,
-                     lanc_dim_threshold=128, dmrg_qn=(0.0,))
-        run = O.DMRG(O.heisenberg_hij(), O.spin_site(2), p)
-    else:
-        p = O.Params(Ldmrg=t["ldmrg"], Mdmrg=t["mdmrg"], lanc_neigen=1, lanc_ncv_factor=10,
-                     lanc_dim_threshold=128, dmrg_qn=(0.5, 0.5))
-        run = O.DMRG(O.hubbard_hij(), O.electron_site(t["u"], t["hfmode"]), p)
-    run.infinite()
+    run = _l40_run(trajectories, key)
     e = np.array([r.energies for r in run.records])
     ref = np.array(t["energy"])
     np.testing.assert_allclose(e, ref, rtol=1e-11, atol=0)
@@ -206,3 +229,33 @@ def test_qn_entropy_split_adds_up(name):
     one = O.eigh_blocks([((0,), np.arange(4), np.diag([0.5, 0.3, 0.2, 0.0]))])
     sn1, sc1 = O.qn_entropies(one)
     assert abs(sn1) < 1e-15 and abs(sc1 - O.entropy(one.evalues)) < 1e-15
+
+
+@pytest.mark.parametrize("key", ["spin_L40_M20", "hubbard_L40_M40"])
+def test_l40_measurements_match_checks(trajectories, key):
+    """Measure_DMRG (Build_Op, Advance_Op, Average_Op, OdotV_direct) after the
+    L=40 runs against sz.check (asserted at 1e-8 by spinSU2_1d.f90:60) and
+    n / d / s2z.check (1e-6, hm_1d.f90:139-147)."""
+    t = trajectories[key]
+    run = _l40_run(trajectories, key)
+    tol = 1e-8 if t["model"] == "heisenberg_half" else 1e-6
+    for name, op in measure_ops(t["model"]).items():
+        got = run.measure(op, range(1, t["ldmrg"] + 1))
+        ref = np.array(t["measure"][name])
+        assert got.shape == ref.shape
+        np.testing.assert_allclose(got, ref, rtol=0, atol=tol, err_msg=name)
+
+
+def test_odotv_loop_restatement_matches_vectorised():
+    """OdotV_direct's loop nest against the per-sector matrix product, both
+    sides, random sparse sector operators on the spin KAT superblock."""
+    z, run, rec = _kat_run("spin")
+    left, right, sb, ds, ev, evec = run.setups[-1]
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(sb.N)
+    for label in ("l", "r"):
+        dims = sb.Dls if label == "l" else sb.Drs
+        ops = [sp.random(int(d), int(d), density=0.3, random_state=rng, format="csr") for d in dims]
+        a = O.odotv_direct(ops, v, label, sb)
+        b = O.odotv_vectorised(ops, v, label, sb)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-13 * np.abs(b).max())
