@@ -366,6 +366,18 @@ int       nss_dmrg_prepare_last(nss_dmrg *d);
  * the next call on d). */
 int       nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out);
 int       nss_dmrg_nrecords(const nss_dmrg *d);
+/* Block restart files in the reference's text format (write_block /
+ * read_block, src/BLOCKS/BLOCKS.f90:418-537; sector, operator and rotation
+ * lists and sparse matrices as src/LIST/LIST_SECTORS.f90:639-705,
+ * src/LIST/LIST_OPERATORS.f90:602-667, src/MATRIX/MATRIX_SPARSE.f90:703-770).
+ * save writes the driver's current left / right block (either path may be
+ * NULL), with its rotation matrices when the run keeps them; load replaces
+ * them (load_block), e.g. to continue from the reference's own restart files
+ * (older operator names such as "S_z" or "P" are mapped to "S_z_n", "P_n").
+ * A loaded block must match the driver's model (site type, QN length and
+ * operator keys). */
+int       nss_dmrg_save_blocks(nss_dmrg *d, const char *left_path, const char *right_path);
+int       nss_dmrg_load_blocks(nss_dmrg *d, const char *left_path, const char *right_path);
 /* Measure_DMRG_scalar (src/DMRG_MEASURE.f90:148-220, 288-486, 595-705) after
  * a run with save_umat: for each position pos[i] (1-based along the chain,
  * OBC) the site operator op (dot basis, d x d, 0-based CSR) is placed at

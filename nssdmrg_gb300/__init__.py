@@ -149,6 +149,8 @@ def lib():
         "nss_rdm_fallback_reasons": (C.c_int, [P, C.POINTER(C.c_int64)]),
         "nss_dmrg_nrecords": (C.c_int, [P]),
         "nss_dmrg_measure": (C.c_int, [P, C.POINTER(Csr), C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_double)]),
+        "nss_dmrg_save_blocks": (C.c_int, [P, C.c_char_p, C.c_char_p]),
+        "nss_dmrg_load_blocks": (C.c_int, [P, C.c_char_p, C.c_char_p]),
         "nss_odotv": (C.c_int, [P, C.c_char, C.POINTER(Csr), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "nss_average_op": (C.c_int, [P, C.c_char, C.POINTER(Csr), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "nss_dmrg_records": (C.c_int, [P, C.POINTER(StepRecord), C.c_int]),
@@ -589,6 +591,17 @@ class DMRG:
 
     def prepare_last(self):
         self.sb._check(lib().nss_dmrg_prepare_last(self._d))
+
+    def save_blocks(self, left=None, right=None):
+        """write_block of the current left / right block to restart files."""
+        enc = lambda x: None if x is None else str(x).encode()
+        self.sb._check(lib().nss_dmrg_save_blocks(self._d, enc(left), enc(right)))
+
+    def load_blocks(self, left=None, right=None):
+        """load_block: replace the current left / right block from restart
+        files (the reference's own, older operator names included)."""
+        enc = lambda x: None if x is None else str(x).encode()
+        self.sb._check(lib().nss_dmrg_load_blocks(self._d, enc(left), enc(right)))
 
     def measure(self, op, pos):
         """Measure_DMRG for one site operator op (d x d, dense or scipy

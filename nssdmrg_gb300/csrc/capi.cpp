@@ -10,6 +10,7 @@
 
 #include "device.cuh"
 #include "host_dmrg.hpp"
+#include "host_restart.hpp"
 #include "host_tridiag.hpp"
 
 struct nss_ctx {
@@ -541,6 +542,42 @@ int nss_dmrg_finite(nss_dmrg *d) {
     if (!d) return NSS_ERR_INVALID;
     cudaSetDevice(d->ctx->c.device);
     return guarded(d->ctx, [&] { return d->drv.finite(); });
+}
+
+int nss_dmrg_save_blocks(nss_dmrg *d, const char *left_path, const char *right_path) {
+    if (!d) return NSS_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        if (left_path) nss::save_block_file(left_path, d->drv.left);
+        if (right_path) nss::save_block_file(right_path, d->drv.right);
+        return NSS_OK;
+    });
+}
+
+int nss_dmrg_load_blocks(nss_dmrg *d, const char *left_path, const char *right_path) {
+    if (!d) return NSS_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        const nss::Block &dot = d->drv.dot;
+        auto check = [&](const nss::Block &b, const char *path) -> int {
+            if (b.fermion != dot.fermion || b.qdim != dot.qdim)
+                return fail(d->ctx, NSS_ERR_INVALID, std::string("load_block: ") + path + " is not a block of this model");
+            for (const nss::Op &o : dot.ops)
+                if (b.find_op(o.key) < 0)
+                    return fail(d->ctx, NSS_ERR_INVALID, std::string("load_block: ") + path + " lacks operator " + o.key);
+            return NSS_OK;
+        };
+        nss::Block l = d->drv.left, r = d->drv.right;
+        if (left_path) {
+            l = nss::load_block_file(left_path);
+            if (int rc = check(l, left_path)) return rc;
+        }
+        if (right_path) {
+            r = nss::load_block_file(right_path);
+            if (int rc = check(r, right_path)) return rc;
+        }
+        d->drv.left = std::move(l);
+        d->drv.right = std::move(r);
+        return NSS_OK;
+    });
 }
 
 int nss_dmrg_measure(nss_dmrg *d, const nss_csr *op, const int32_t *pos, int npos, double *out) {
