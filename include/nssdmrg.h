@@ -210,6 +210,15 @@ int nss_average_op(nss_ctx *ctx, char label, const nss_csr *op, const double *ps
  * reference (LAPACK dsyev per block, src/MATRIX/MATRIX_BLOCKS.f90:589-657). */
 int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int *fallback_blocks);
 
+/* The mixed method's refinement in the last nss_eigh: the passes it took
+ * (each anchors every refined vector in FP64 and corrects it with FP32
+ * Lanczos), the size of the refined cluster (the wanted vectors plus
+ * near-degenerate partners, resolved by an FP64 Rayleigh-Ritz step before
+ * every later pass), and how many mixed solves of the context's life were
+ * redone in FP64 because the refinement did not reach the tolerance.  No
+ * counterpart in the reference (ARPACK in FP64). */
+int nss_refine_stats(const nss_ctx *ctx, int *passes, int *cluster, int64_t *fp64_fallbacks);
+
 /* Why blocks fell back to the library path, counted over the context's life:
  * out[0] L D L^T not positive definite, out[1] a kept eigenvalue within 32 eps
  * of a neighbour, out[2] the Rayleigh iteration did not settle, out[3] a

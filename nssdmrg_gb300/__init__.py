@@ -147,6 +147,7 @@ def lib():
         "nss_dmrg_export_superblock": (C.c_int, [P, C.POINTER(SbDesc)]),
         "nss_rdm_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "nss_rdm_fallback_reasons": (C.c_int, [P, C.POINTER(C.c_int64)]),
+        "nss_refine_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
         "nss_dmrg_nrecords": (C.c_int, [P]),
         "nss_dmrg_measure": (C.c_int, [P, C.POINTER(Csr), C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_double)]),
         "nss_dmrg_save_blocks": (C.c_int, [P, C.c_char_p, C.c_char_p]),
@@ -417,6 +418,13 @@ class Superblock:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         self._check(lib().nss_rdm_stats(self._ctx, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def refine_stats(self):
+        """(passes, cluster size, FP64 fallbacks so far) of the mixed
+        method's refinement in the last sb_diag."""
+        a, b, f = C.c_int(), C.c_int(), C.c_int64()
+        self._check(lib().nss_refine_stats(self._ctx, C.byref(a), C.byref(b), C.byref(f)))
+        return a.value, b.value, f.value
 
     def rdm_fallback_reasons(self):
         """Counts of own-path blocks sent back to the library, by reason:

@@ -226,6 +226,14 @@ int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iter
     return NSS_OK;
 }
 
+int nss_refine_stats(const nss_ctx *ctx, int *passes, int *cluster, int64_t *fp64_fallbacks) {
+    if (!ctx) return NSS_ERR_INVALID;
+    if (passes) *passes = ctx->c.refine_passes;
+    if (cluster) *cluster = ctx->c.refine_cluster;
+    if (fp64_fallbacks) *fp64_fallbacks = ctx->c.mixed_fallbacks;
+    return NSS_OK;
+}
+
 int nss_rdm_stats(const nss_ctx *ctx, int *own_blocks, int *library_blocks, int *fallback_blocks) {
     if (!ctx) return NSS_ERR_INVALID;
     if (own_blocks) *own_blocks = ctx->c.rdm_own_blocks;

@@ -84,6 +84,7 @@ struct DevLanczos {
     double last_resid[4] = {0, 0, 0, 0};   // FP64 residual norms of the last solve
     int last_iters = 0;
     double *evecs = nullptr;     // [neigen][n] Ritz vectors (last solve)
+    double *rrw = nullptr;       // [4][n] H U of the mixed refinement's Rayleigh-Ritz step
     int neigen_done = 0;
     double *scal = nullptr;      // device scalars (see k_lanczos.cu)
     double *part = nullptr;      // per-CTA partial sums
@@ -179,7 +180,7 @@ struct Ctx {
     DevRdm rdm;
     DevRenorm ren;
     int64_t launches = 0;        // kernels of this library launched
-    int tc_min_dl = 256;         // tensor-core sector threshold (see tc_min_dl_default)
+    int tc_min_dl = 1024;        // tensor-core sector threshold (see tc_min_dl_default)
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
@@ -207,6 +208,8 @@ struct Ctx {
     char *sb_arena = nullptr, *sb_stage = nullptr;   // superblock pool: device arena, pinned staging
     size_t sb_arena_cap = 0, sb_stage_cap = 0;
     double renorm_phase_ms[3] = {0, 0, 0};
+    int refine_passes = 0, refine_cluster = 0;   // mixed refinement of the last solve
+    int64_t mixed_fallbacks = 0;                 // mixed solves redone in FP64 (context life)
     char *ms_dev = nullptr, *ms_host = nullptr;   // OdotV tables: device, pinned staging
     size_t ms_cap = 0;   // host: scan+extract, device wait, CSR assembly (summed over calls)
 };
@@ -239,7 +242,9 @@ struct Hv32Ops;
 Hv32Ops hv32_ops(const DevSb &s);
 // sectors with at least this many left states take the tensor-core kernel
 // in the mixed path; a context takes env NSS_TC_MIN_DL at creation (default
-// 256: below that the FP32 CUDA-core tiles are faster on GB300; 0 disables)
+// 1024: up to a few hundred states the persistent CUDA-core path is faster
+// on GB300, 20-25 ms against 29-37 ms per solve of the spin-1 L=64 m=512
+// superblock, whose sectors reach 350 states; 0 disables)
 int tc_min_dl_default();
 
 // k_noalloc.cu

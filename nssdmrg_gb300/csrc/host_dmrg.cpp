@@ -2,6 +2,8 @@
 #include "host_dmrg.hpp"
 
 #include <chrono>
+#include <deque>
+#include <thread>
 #include <cstdlib>
 #include <cmath>
 #include <stdexcept>
@@ -78,35 +80,35 @@ Block electron_site(double uloc, bool hfmode) {
 
 namespace {
 
-// connect_spin_blocks (src/DMRG_CONNECT.f90:394-454), link 'n'
-Csr connect_spin(const Block &l, const Block &r, const double *hij) {
-    const Csr &szl = l.op("S_z_n"), &spl = l.op("S_p_n");
-    const Csr &szr = r.op("S_z_n"), &spr = r.op("S_p_n");
-    Csr h2 = csr_scale(csr_kron(szl, szr), hij[0]);
-    h2 = csr_add(h2, csr_scale(csr_kron(spl, csr_transpose(spr)), hij[3]));
-    h2 = csr_add(h2, csr_scale(csr_kron(csr_transpose(spl), spr), hij[3]));
-    return h2;
-}
-
-// connect_fermion_blocks (src/DMRG_CONNECT.f90:296-389), real, Norb=1
-Csr connect_fermion(const Block &l, const Block &r, const double *hij) {
+// The coupling terms of connect_spin_blocks (src/DMRG_CONNECT.f90:394-454)
+// and connect_fermion_blocks (:296-389, real, Norb=1), link 'n', as
+// coef * kron(X from l, Y from r); transposes and products land in tmp.
+void connect_terms(const Block &l, const Block &r, const double *hij, std::deque<Csr> &tmp,
+                   std::vector<KronTerm> &terms) {
+    if (!l.fermion) {
+        const Csr &szl = l.op("S_z_n"), &spl = l.op("S_p_n");
+        const Csr &szr = r.op("S_z_n"), &spr = r.op("S_p_n");
+        terms.push_back({&szl, &szr, hij[0]});
+        tmp.push_back(csr_transpose(spr));
+        terms.push_back({&spl, &tmp.back(), hij[3]});
+        tmp.push_back(csr_transpose(spl));
+        terms.push_back({&tmp.back(), &spr, hij[3]});
+        return;
+    }
     const Csr &pl = l.op("P_n");
     const char *key[2] = {"C_l1_s1_n", "C_l1_s2_n"};
-    Csr h2;
-    h2.init(l.dim * r.dim, l.dim * r.dim);
     for (int io = 0; io < 2; ++io)
         for (int jo = 0; jo < 2; ++jo) {
             const double t = hij[io * 2 + jo];
             if (t == 0.0) continue;
             const Csr &cl = l.op(key[io]), &cr = r.op(key[jo]);
-            h2 = csr_add(h2, csr_scale(csr_kron(csr_matmul(csr_transpose(cl), pl), cr), t));
-            h2 = csr_add(h2, csr_scale(csr_kron(csr_matmul(pl, cl), csr_transpose(cr)), t));
+            tmp.push_back(csr_matmul(csr_transpose(cl), pl));
+            terms.push_back({&tmp.back(), &cr, t});
+            tmp.push_back(csr_matmul(pl, cl));
+            const Csr *a2 = &tmp.back();
+            tmp.push_back(csr_transpose(cr));
+            terms.push_back({a2, &tmp.back(), t});
         }
-    return h2;
-}
-
-Csr connect(const Block &l, const Block &r, const double *hij) {
-    return l.fermion ? connect_fermion(l, r, hij) : connect_spin(l, r, hij);
 }
 
 std::vector<double> outsum(const std::vector<double> &a, int na, const std::vector<double> &b, int nb, int q) {
@@ -131,17 +133,24 @@ Block enlarge_block(const Block &blk, const Block &dot, char label, const double
     out.omats = blk.omats;
     out.ops.reserve(blk.ops.size());
     for (const Op &o : blk.ops) out.ops.push_back({o.key, Csr{}, o.type});
-    Csr hb, hd, h2;
+    // H = H_block x 1 + 1 x H_dot + the coupling terms (left; mirrored on the
+    // right), summed in one pass over the output rows
+    std::deque<Csr> tmp;
+    const Csr id_m = csr_identity(m), id_d = csr_identity(d);
+    std::vector<KronTerm> terms;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nth = (int)std::max(1u, std::min(4u, hw / 2));
     if (label == 'l') {
-        hb = csr_kron(blk.op("H"), csr_identity(d));
-        hd = csr_kron(csr_identity(m), dot.op("H"));
-        h2 = connect(blk, dot, hij);
+        terms.push_back({&blk.op("H"), &id_d, 1.0});
+        terms.push_back({&id_m, &dot.op("H"), 1.0});
+        connect_terms(blk, dot, hij, tmp, terms);
+        out.op("H") = csr_kron_sum(m, d, terms, nth);
     } else {
-        hb = csr_kron(csr_identity(d), blk.op("H"));
-        hd = csr_kron(dot.op("H"), csr_identity(m));
-        h2 = connect(dot, blk, hij);
+        terms.push_back({&id_d, &blk.op("H"), 1.0});
+        terms.push_back({&dot.op("H"), &id_m, 1.0});
+        connect_terms(dot, blk, hij, tmp, terms);
+        out.op("H") = csr_kron_sum(d, m, terms, nth);
     }
-    out.op("H") = csr_add(csr_add(hb, hd), h2);
     // other operators in list order; P is read from the list being updated
     // exactly as the reference loop does (src/DMRG_CONNECT.f90:117-146):
     // the enlarged P once its own entry has been passed, the block's before

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <stdexcept>
+#include <thread>
 
 namespace nss {
 
@@ -85,6 +86,69 @@ Csr csr_kron(const Csr &a, const Csr &b) {
                 }
             c.rowptr[i * b.nrow + k + 1] = (int)c.col.size();
         }
+    return c;
+}
+
+Csr csr_kron_sum(int na, int nb, const std::vector<KronTerm> &terms, int nthreads) {
+    for (const KronTerm &t : terms)
+        if (t.a->nrow != na || t.a->ncol != na || t.b->nrow != nb || t.b->ncol != nb)
+            throw std::runtime_error("csr_kron_sum: term shape mismatch");
+    const int n = na * nb;
+    nthreads = std::max(1, std::min(nthreads, na));
+    struct Part {
+        std::vector<int> rowlen, col;
+        std::vector<double> val;
+    };
+    std::vector<Part> parts(nthreads);
+    auto work = [&](int ti) {
+        Part &P = parts[ti];
+        const int i0 = (int)((int64_t)na * ti / nthreads), i1 = (int)((int64_t)na * (ti + 1) / nthreads);
+        std::vector<int> pos(n, -1);
+        P.rowlen.reserve((size_t)(i1 - i0) * nb);
+        for (int i = i0; i < i1; ++i)
+            for (int k = 0; k < nb; ++k) {
+                const int start = (int)P.col.size();
+                for (const KronTerm &t : terms) {
+                    const Csr &a = *t.a, &b = *t.b;
+                    for (int ia = a.rowptr[i]; ia < a.rowptr[i + 1]; ++ia) {
+                        const int cbase = a.col[ia] * nb;
+                        const double av = a.val[ia];
+                        for (int kb = b.rowptr[k]; kb < b.rowptr[k + 1]; ++kb) {
+                            const int j = cbase + b.col[kb];
+                            const double v = (av * b.val[kb]) * t.coef;
+                            if (pos[j] < 0) {
+                                pos[j] = (int)P.col.size();
+                                P.col.push_back(j);
+                                P.val.push_back(v);
+                            } else {
+                                P.val[pos[j]] += v;
+                            }
+                        }
+                    }
+                }
+                for (int jj = start; jj < (int)P.col.size(); ++jj) pos[P.col[jj]] = -1;
+                P.rowlen.push_back((int)P.col.size() - start);
+            }
+    };
+    std::vector<std::thread> th;
+    for (int ti = 1; ti < nthreads; ++ti) th.emplace_back(work, ti);
+    work(0);
+    for (auto &t : th) t.join();
+    Csr c;
+    c.init(n, n);
+    size_t nnz = 0;
+    for (const Part &P : parts) nnz += P.col.size();
+    c.col.reserve(nnz);
+    c.val.reserve(nnz);
+    int r = 0;
+    for (const Part &P : parts) {
+        for (int len : P.rowlen) {
+            c.rowptr[r + 1] = c.rowptr[r] + len;
+            ++r;
+        }
+        c.col.insert(c.col.end(), P.col.begin(), P.col.end());
+        c.val.insert(c.val.end(), P.val.begin(), P.val.end());
+    }
     return c;
 }
 

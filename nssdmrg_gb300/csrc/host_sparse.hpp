@@ -61,6 +61,15 @@ Csr csr_from_dense(int nrow, int ncol, const double *a /* row-major */);
 Csr csr_scale(const Csr &a, double s);
 Csr csr_add(const Csr &a, const Csr &b);           // a + b
 Csr csr_kron(const Csr &a, const Csr &b);           // sp_kron_matrix
+// sum_t coef_t * kron(a_t, b_t) in one pass, every a_t na x na and b_t
+// nb x nb: the sparse sum of the terms' Kronecker products as csr_add would
+// form it (entries touched by any term are kept, also when they cancel),
+// rows split over nthreads threads
+struct KronTerm {
+    const Csr *a, *b;
+    double coef;
+};
+Csr csr_kron_sum(int na, int nb, const std::vector<KronTerm> &terms, int nthreads);
 Csr csr_transpose(const Csr &a);                    // sp_dgr_matrix (real)
 Csr csr_matmul(const Csr &a, const Csr &b);         // sp_matmul_matrix
 // sp_filter_matrix_2: rows `rows`, columns `cols` (0-based state lists).

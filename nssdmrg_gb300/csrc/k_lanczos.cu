@@ -1304,6 +1304,118 @@ __global__ void __launch_bounds__(256) k_anchor_r(const double *__restrict__ psi
     *counter = 0u;
 }
 
+// Gram matrix of k <= 4 FP64 vectors against k others: r[i*k+j] = U_i . W_j
+// (grid reduction; part holds k*k columns of gridDim.x partials)
+__global__ void __launch_bounds__(256) k_gram(const double *__restrict__ U, const double *__restrict__ W, int k,
+                                              int64_t n, double *__restrict__ part, double *__restrict__ r,
+                                              unsigned *counter) {
+    const int tid = threadIdx.x;
+    double acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + tid; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double u[4], w[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            u[a] = a < k ? U[(int64_t)a * n + i] : 0.0;
+            w[a] = a < k ? W[(int64_t)a * n + i] : 0.0;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a * 4 + b] = fma(u[a], w[b], acc[a * 4 + b]);
+    }
+    __shared__ double red[16][8];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const double v = warp_sum<double>(acc[q]);
+        if ((tid & 31) == 0) red[q][tid >> 5] = v;
+    }
+    __syncthreads();
+    if (tid < k * k) {
+        const int a = tid / k, b = tid % k;
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += red[a * 4 + b][q];
+        part[(int64_t)tid * gridDim.x + blockIdx.x] = t;
+    }
+    if (!last_block(counter)) return;
+    for (int q = 0; q < k * k; ++q) {
+        const double t = lastblock_sum(part + (int64_t)q * gridDim.x, gridDim.x);
+        if (tid == 0) r[q] = t;
+    }
+    if (tid == 0) *counter = 0u;
+}
+
+// X <- X Q for k <= 4 FP64 vectors (Q column-major k x k)
+struct Rot4 {
+    double q[16];
+};
+__global__ void __launch_bounds__(256) k_rot(double *__restrict__ X, int k, int64_t n, Rot4 Q) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) x[a] = a < k ? X[(int64_t)a * n + i] : 0.0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            double t = 0.0;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) t = fma(x[a], Q.q[b * 4 + a], t);
+            y[b] = t;
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            if (b < k) X[(int64_t)b * n + i] = y[b];
+    }
+}
+
+// Eigenvalues (ascending) and orthonormal eigenvectors (columns of q,
+// column-major k x k) of a symmetric k x k matrix a (row-major, destroyed),
+// k <= 4, by cyclic Jacobi rotations.
+void sym_eig_small(int k, double *a, double *lam, double *q) {
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) q[j * k + i] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) {
+                tot += a[i * k + j] * a[i * k + j];
+                if (i != j) off += a[i * k + j] * a[i * k + j];
+            }
+        if (off <= 1e-34 * tot) break;
+        for (int p = 0; p < k; ++p)
+            for (int r = p + 1; r < k; ++r) {
+                const double apr = a[p * k + r];
+                if (apr == 0.0) continue;
+                const double tau = (a[r * k + r] - a[p * k + p]) / (2.0 * apr);
+                const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / std::sqrt(1.0 + t * t), sn = t * cs;
+                for (int i = 0; i < k; ++i) {   // columns p, r
+                    const double x = a[i * k + p], y = a[i * k + r];
+                    a[i * k + p] = cs * x - sn * y;
+                    a[i * k + r] = sn * x + cs * y;
+                }
+                for (int j = 0; j < k; ++j) {   // rows p, r
+                    const double x = a[p * k + j], y = a[r * k + j];
+                    a[p * k + j] = cs * x - sn * y;
+                    a[r * k + j] = sn * x + cs * y;
+                }
+                for (int i = 0; i < k; ++i) {
+                    const double x = q[p * k + i], y = q[r * k + i];
+                    q[p * k + i] = cs * x - sn * y;
+                    q[r * k + i] = sn * x + cs * y;
+                }
+            }
+    }
+    int ord[4] = {0, 1, 2, 3};
+    std::sort(ord, ord + k, [&](int x, int y) { return a[x * k + x] < a[y * k + y]; });
+    double qs[16];
+    for (int j = 0; j < k; ++j) {
+        lam[j] = a[ord[j] * k + ord[j]];
+        for (int i = 0; i < k; ++i) qs[j * k + i] = q[ord[j] * k + i];
+    }
+    for (int t = 0; t < k * k; ++t) q[t] = qs[t];
+}
+
 // out = (float)(x * s)
 __global__ void k_to32(float *__restrict__ out, const double *__restrict__ x, double s, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1393,6 +1505,14 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     return NSS_OK;
 }
 
+// the FP64 scratch of the mixed refinement's Rayleigh-Ritz step (4 vectors)
+int ensure_rrw(Ctx &c, int64_t n) {
+    DevLanczos &z = c.lz;
+    if (z.rrw) return NSS_OK;
+    NSS_CUDA_TRY(c, ctx_alloc(c, &z.rrw, (size_t)4 * n));
+    return NSS_OK;
+}
+
 template <class T>
 int hv_t(Ctx &c, const T *v, T *hv, const int *stop);
 template <>
@@ -1429,9 +1549,15 @@ __global__ void __launch_bounds__(256) k_ritz_anchor(const T *__restrict__ V, in
 // The Lanczos iterations on a basis of type T; leaves theta (Ritz values),
 // svec (their T_m eigenvectors, stride m) and the Ritz vectors (FP64) in c.lz.
 // With `anc` it runs the anchored refinement instead (one eigenvector).
+// cluster_max > neigen (mixed first phase): the Ritz pairs just above the
+// wanted ones whose values lie within CLUSTER_GAP (relative) of their lower
+// neighbour are returned as well, up to cluster_max in all; *ne_out gets the
+// number of Ritz vectors left in evecs.
+constexpr double CLUSTER_GAP = 1e-4;
 template <class T>
 int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t seed, int *numop_out,
-                int *m_out, const AnchorSpec *anc = nullptr) {
+                int *m_out, const AnchorSpec *anc = nullptr, int cluster_max = 0, int *ne_out = nullptr,
+                const double *start = nullptr) {
     DevLanczos &z = c.lz;
     const int64_t n = c.sb.n;
     const int cap = z.cap;
@@ -1452,7 +1578,10 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         neigen = 1;
     } else {
         ++c.launches;
-        k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
+        if (start && sizeof(T) == sizeof(float))   // a given FP64 start vector (mixed refinement)
+            k_to32<<<vb, 256, 0, st>>>((float *)(void *)V, start, 1.0, n);
+        else
+            k_random<T><<<vb, 256, 0, st>>>(V, n, seed, restarts);
         ++c.launches;
         normalize_dev<T>(z, V, n, st, c.launches);
     }
@@ -1678,6 +1807,25 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         z.last_anchor_theta = theta[0];
         return NSS_OK;
     }
+    if (cluster_max > ne_done && m_done > ne_done && (int64_t)cluster_max * cluster_max <= cap + 2) {
+        // near-degenerate partners of the wanted pairs (see cluster_max)
+        const int ntry = std::min(cluster_max, m_done);
+        std::vector<double> th2(ntry), sv2((size_t)ntry * m_done), rs2(ntry);
+        tridiag_lowest(ha, hb, m_done, ntry, hb[m_done - 1], th2.data(), sv2.data(), rs2.data(), nullptr, work);
+        double scale = 0.0;
+        for (int e = 0; e < ntry; ++e) scale = std::max(scale, std::fabs(th2[e]));
+        int k = ne_done;
+        while (k < ntry && th2[k] - th2[k - 1] <= CLUSTER_GAP * scale) ++k;
+        if (k > ne_done) {
+            for (int e = 0; e < k; ++e) {
+                theta[e] = th2[e];
+                resid[e] = rs2[e];
+            }
+            svec.assign(sv2.begin(), sv2.begin() + (size_t)k * m_done);
+            ne_done = k;
+        }
+    }
+    if (ne_out) *ne_out = ne_done;
     const int ne = ne_done;
     NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta, theta.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
     NSS_CUDA_TRY(c, cudaMemcpyAsync(z.resid, resid.data(), ne * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1699,7 +1847,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
-    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.slot32, z.evecs, z.scal, z.part, z.counter,
+    void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.slot32, z.evecs, z.rrw, z.scal, z.part, z.counter,
                     z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags, z.pitem};
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
@@ -1731,20 +1879,32 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    int numop_ = 0, m_done = 0;
+    int numop_ = 0, m_done = 0, kcl = 1;
     if (!mixed) {
         rc = run_lanczos<double>(c, z.V, z.w, neigen, mmax, tol, seed, &numop_, &m_done);
     } else {
-        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done);
+        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done,
+                                nullptr, std::min(4, neigen + 2), &kcl);
     }
     const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
     if (!rc && mixed) {
-        // Anchored refinement of each Ritz vector: FP64 anchor u (deflated
-        // against the vectors already refined), r = H u - theta0 u in FP64,
-        // then FP32 Lanczos on the complement of u started from r/|r|, with
-        // the couplings u.H.v = r.v in FP64; the small matrix is solved on the
-        // host.  The FP32 errors then only touch the correction (|r|/gap), so
-        // the vector comes out at FP64 quality.
+        // Iterative refinement of the FP32 Ritz vectors to FP64 quality.  Each
+        // pass takes every vector u (deflated against the ones before it) as
+        // an FP64 anchor: theta0 = u.H.u and r = H u - theta0 u in FP64; a
+        // vector with ||r|| <= tol |theta0| is final, any other gets an FP32
+        // Lanczos run on the complement of u started from r/|r|, with the
+        // couplings u.H.v = r.v in FP64, solved on the host.  The FP32 errors
+        // then only touch the correction, which shrinks by about
+        // eps32 ||H|| / gap per pass, gap the distance to the nearest other
+        // eigenvalue.  Near-degenerate partners (within CLUSTER_GAP of the
+        // wanted pairs, e.g. the singlet and Sz=0 triplet of a spin-1
+        // chain's edge spins, split by ~1e-7 relative) would make that factor
+        // ~1: they are refined along, and before every later pass an FP64
+        // Rayleigh-Ritz step on the cluster resolves the mixing among them
+        // exactly, so only the gap to the rest of the spectrum matters.  The
+        // passes end when every wanted vector meets the FP64 residual test;
+        // after MAX_PASSES without that the solve is redone in FP64.
+        constexpr int MAX_PASSES = 8;
         double *r = z.scal + S_NSCAL + 4 * (z.cap + 2);   // 8 refinement slots
         double *h1 = z.scal + S_NSCAL;
         double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
@@ -1754,7 +1914,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             cudaFuncSetAttribute(k_dots<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
         if (upd_smem > 48 * 1024)
             cudaFuncSetAttribute(k_update<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
-        // w -= Y (Y^T w) against the e vectors already refined; returns via scal[S_BB]
+        // w -= Y (Y^T w) against the e vectors before it; returns via scal[S_BB]
         auto deflate = [&](double *vec, int e) -> int {
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.scal + S_ALPHA, 0, sizeof(double), st));
@@ -1765,14 +1925,18 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
                                                           rs_alpha, rs_beta, 0);
             return NSS_OK;
         };
-        for (int e = 0; e < ne && !rc; ++e) {
+        double th[4] = {0, 0, 0, 0}, res[4] = {0, 0, 0, 0};
+        // FP64 check of wanted vector e (deflated against the ones before it
+        // and normalised): th[e] = u.H.u, res[e] = ||H u - th u||; leaves
+        // r = H u - th u in z.w (deflated for e > 0) and its norm in *beta0
+        auto check = [&](int e, double *beta0) -> int {
             double *u = z.evecs + (int64_t)e * n;
             if (e > 0) {
-                if ((rc = deflate(u, e))) break;
+                if (int rc2 = deflate(u, e)) return rc2;
                 ++c.launches;
                 normalize_dev<double>(z, u, n, st, c.launches);
             }
-            if ((rc = hv_device(c, u, z.w))) break;
+            if (int rc2 = hv_device(c, u, z.w)) return rc2;
             ++numop_;
             c.launches += 2;
             k_rq<<<NBLK, 256, 0, st>>>(u, z.w, n, z.part, r, z.counter);
@@ -1780,46 +1944,130 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             double hr[8];
             NSS_CUDA_TRY(c, cudaMemcpyAsync(hr, r, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
             NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-            const double theta0 = hr[0] / hr[2];
+            th[e] = hr[0] / hr[2];
+            res[e] = std::sqrt(std::max(hr[4], 0.0));
             double rr = hr[4];
             if (e > 0) {
-                if ((rc = deflate(z.w, e))) break;
+                if (int rc2 = deflate(z.w, e)) return rc2;
                 NSS_CUDA_TRY(c, cudaMemcpyAsync(&rr, z.scal + S_BB, sizeof(double), cudaMemcpyDeviceToHost, st));
                 NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
             }
-            const double beta0 = std::sqrt(std::max(rr, 0.0));
-            if (!(beta0 > tol * std::fabs(theta0))) continue;   // the anchor is converged already
-            // FP32 start vector r/|r| and FP32 copies of u, r and the deflation set
+            *beta0 = std::sqrt(std::max(rr, 0.0));
+            return NSS_OK;
+        };
+        // anchored FP32 correction of wanted vector e, right after check(e)
+        auto refine = [&](int e, double beta0) -> int {
+            double *u = z.evecs + (int64_t)e * n;
             float *u32 = z.anc32, *r32 = z.anc32 + n, *y32 = z.anc32 + 2 * n;
             c.launches += 3 + e;
             k_to32<<<608, 256, 0, st>>>(z.V32, z.w, 1.0 / beta0, n);
             k_to32<<<608, 256, 0, st>>>(u32, u, 1.0, n);
             k_to32<<<608, 256, 0, st>>>(r32, z.w, 1.0, n);
-            for (int f = 0; f < e; ++f) k_to32<<<608, 256, 0, st>>>(y32 + (int64_t)f * n, z.evecs + (int64_t)f * n, 1.0, n);
-            AnchorSpec as{u, u32, r32, y32, e, theta0, u};
+            for (int f = 0; f < e; ++f)
+                k_to32<<<608, 256, 0, st>>>(y32 + (int64_t)f * n, z.evecs + (int64_t)f * n, 1.0, n);
+            AnchorSpec as{u, u32, r32, y32, e, th[e], u};
             int it2 = 0, m2 = 0;
-            rc = run_lanczos<float>(c, z.V32, z.w32, 1, mmax, tol, seed, &it2, &m2, &as);
+            // a pass gains at most ~1e4 (the FP32 floor of the correction):
+            // the anchored problem is solved to 1e-4 of the vector's residual
+            const double tol_pass = std::max(tol, 1e-4 * beta0 / std::max(std::fabs(th[e]), 1e-300));
+            if (int rc2 = run_lanczos<float>(c, z.V32, z.w32, 1, mmax, tol_pass, seed, &it2, &m2, &as)) return rc2;
             numop_ += it2;
-        }
-    }
-    if (!rc && mixed) {
-        // FP64 energy of each eigenvector: theta = psi.H.psi / psi.psi with
-        // the FP64 H*psi, and the FP64 residual ||H psi - theta psi||.
-        double *r = z.scal + S_NSCAL + 4 * (z.cap + 2);   // 8 refinement slots
-        for (int e = 0; e < ne; ++e) {
-            const double *psi = z.evecs + (int64_t)e * n;
-            rc = hv_device(c, psi, z.w);
-            ++numop_;
-            if (rc) break;
-            c.launches += 2;
-            k_rq<<<NBLK, 256, 0, st>>>(psi, z.w, n, z.part, r, z.counter);
-            k_resid<<<NBLK, 256, 0, st>>>(psi, z.w, n, z.part, r, z.counter);
-            double hr[4];
-            NSS_CUDA_TRY(c, cudaMemcpyAsync(hr, r, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            return NSS_OK;
+        };
+        // FP64 Rayleigh-Ritz on the k cluster vectors: orthonormalise them,
+        // W = H U (into the FP64 scratch), G = U^T W, U <- U Q with G's
+        // eigenvectors Q in ascending order
+        auto rayleigh_ritz = [&](int k) -> int {
+            ++c.launches;
+            normalize_dev<double>(z, z.evecs, n, st, c.launches);
+            for (int e = 1; e < k; ++e) {
+                double *u = z.evecs + (int64_t)e * n;
+                if (int rc2 = deflate(u, e)) return rc2;
+                ++c.launches;
+                normalize_dev<double>(z, u, n, st, c.launches);
+            }
+            for (int e = 0; e < k; ++e) {
+                if (int rc2 = hv_device(c, z.evecs + (int64_t)e * n, z.rrw + (int64_t)e * n)) return rc2;
+                ++numop_;
+            }
+            ++c.launches;
+            k_gram<<<NBLK, 256, 0, st>>>(z.evecs, z.rrw, k, n, z.part, h1, z.counter);
+            double g[16];
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(g, h1, (size_t)k * k * sizeof(double), cudaMemcpyDeviceToHost, st));
             NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-            const double th = hr[0] / hr[2];
-            z.last_resid[e] = std::sqrt(std::max(hr[3], 0.0));
-            NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta + e, &th, sizeof(double), cudaMemcpyHostToDevice, st));
+            double a[16], q[16], lam[4];
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) a[i * k + j] = 0.5 * (g[i * k + j] + g[j * k + i]);
+            sym_eig_small(k, a, lam, q);
+            Rot4 R{};
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) R.q[j * 4 + i] = q[j * k + i];
+            ++c.launches;
+            k_rot<<<608, 256, 0, st>>>(z.evecs, k, n, R);
+            NSS_CUDA_TRY(c, cudaGetLastError());
+            return NSS_OK;
+        };
+        // k: the cluster (wanted vectors and partners); the passes
+        int k = kcl;
+        if (!rc) rc = ensure_rrw(c, n);
+        bool done = false, rr_due = k > ne, rerun = false;
+        double prev[4] = {0, 0, 0, 0};
+        int passes = 0;
+        for (; passes < MAX_PASSES && !rc && !done; ++passes) {
+            if (rr_due && (rc = rayleigh_ritz(k))) break;
+            const bool rr_now = rr_due;
+            rr_due = false;
+            bool all = true, redo = false;
+            for (int e = 0; e < ne && !rc; ++e) {
+                double beta0 = 0.0;
+                if ((rc = check(e, &beta0))) break;
+                if (res[e] <= tol * std::fabs(th[e])) continue;
+                all = false;
+                // a correction that gained less than 20x: the vector is mixed
+                // with a near-degenerate state the cluster lacks or resolves
+                // no longer
+                const bool stalled = passes > 0 && !rr_now && res[e] > 0.05 * prev[e];
+                if (stalled && k > ne) {
+                    rr_due = redo = true;
+                    break;
+                }
+                if (stalled && ne == 1 && !rerun) {
+                    // the FP32 phase stopped before it resolved the pair: a
+                    // short FP32 Lanczos run from the vector, which lies
+                    // almost inside the pair's plane, finds both states
+                    rerun = true;
+                    int it3 = 0, m3 = 0, k3 = 2;
+                    const int rc3 = run_lanczos<float>(c, z.V32, z.w32, 2, std::min(mmax, 160), std::max(tol, mixed_tol()),
+                                                       seed, &it3, &m3, nullptr, 4, &k3, z.evecs);
+                    numop_ += it3;
+                    if (rc3 == NSS_ERR_NOCONV) break;   // left to the passes' limit
+                    if ((rc = rc3)) break;
+                    k = std::max(k3, 2);
+                    rr_due = redo = true;
+                    break;
+                }
+                if (!(beta0 > 0.0)) continue;
+                if ((rc = refine(e, beta0))) break;
+            }
+            if (rc) break;
+            if (all) done = true;
+            else if (!redo)
+                for (int e = 0; e < ne; ++e) prev[e] = res[e];
+        }
+        c.refine_passes = passes;
+        c.refine_cluster = k;
+        if (!rc && done) {
+            for (int e = 0; e < ne; ++e) z.last_resid[e] = res[e];
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta, th, ne * sizeof(double), cudaMemcpyHostToDevice, st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        } else if (!rc) {
+            // the FP32 corrections did not reach tol: the plain FP64 method
+            ++c.mixed_fallbacks;
+            if ((rc = ensure_lanczos(c, n, mmax + 1, false)) == NSS_OK) {
+                int it64 = 0;
+                rc = run_lanczos<double>(c, c.lz.V, c.lz.w, neigen, mmax, tol, seed, &it64, &m_done);
+                numop_ += it64;
+            }
         }
     }
     cudaEventRecord(e1, st);

@@ -20,7 +20,7 @@ namespace nss {
 
 int tc_min_dl_default() {
     const char *e = std::getenv("NSS_TC_MIN_DL");
-    if (!e) return 256;
+    if (!e) return 1024;
     const int x = std::atoi(e);
     return x < 0 ? 0 : x;
 }
