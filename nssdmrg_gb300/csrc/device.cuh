@@ -143,6 +143,8 @@ struct DevRdm {
     cudaEvent_t ph[NPH] = {};
     double *big = nullptr;           // global copies of the blocks the cluster kernel reduces in place
     int64_t cap_big = 0;
+    double *tg = nullptr;            // k_trd_grid exchange buffers, barrier and error word
+    int64_t cap_tg = 0;
 };
 
 // Operator renormalisation on the device (k_renorm.cu): grow-only buffers
@@ -291,6 +293,13 @@ int syev_trd_cl_size(int *nmax);
 int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
                 int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, double *gA,
                 const int64_t *goff, cudaStream_t st);
+// k_trd_grid: the same reduction of each block in `blocks` (dims nb) by the
+// whole GPU, one cooperative launch per block, for blocks far beyond a
+// cluster's reach; *err (device) is set if a grid barrier timed out.
+int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off,
+                  const std::vector<int> &blocks, const std::vector<int> &nb, double *refl, double *td, double *te,
+                  double *tau, int *perm, double *gA, const std::vector<int64_t> &goff_h, double *comm,
+                  unsigned *bar, int *err, cudaStream_t st);
 
 // kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions
 // start at nl): k_vec + the cluster Gram-Schmidt, two launches

@@ -371,6 +371,166 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     cl.sync();                                       // no CTA leaves while its memory may be read
 }
 
+// Bounded grid barrier of k_trd_grid (cooperative launch, all CTAs
+// resident): barrier e of a launch waits for e * G arrivals on bar[0]; a
+// wait that runs past TG_SPIN polls sets *err, and every later barrier
+// returns false at once, so the kernel always ends.  bar[0] and *err are
+// zero at launch.
+constexpr uint32_t TG_SPIN = 1u << 22;
+__device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned &epoch, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int good = 1;
+        epoch += gridDim.x;
+        __threadfence();
+        atomicAdd(bar, 1u);
+        uint32_t it = 0;
+        while (true) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+            if (v >= epoch) break;
+            if ((++it & 255u) == 0) {
+                if (*(volatile int *)err) { good = 0; break; }
+                if (it > TG_SPIN) { atomicExch(err, 1); good = 0; break; }
+            }
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// The Householder reduction of one very large block by the whole GPU (a
+// cooperative launch of one CTA per SM): k_trd_cl's step with the CTAs of
+// the grid in place of a cluster's, so the n^3 FP64 FMAs spread over every
+// SM instead of 16.  CTA r holds columns j = r + G jj of the block's global
+// (L2-resident) copy gA; the reflector, the p_j and the partial sums p.v
+// cross CTAs through global buffers (comm: v [2][n], p [2][n], t [2],
+// partials [2][G]) that alternate with the parity of k, between two grid
+// barriers a step.
+__global__ void __launch_bounds__(TRD_THREADS, 1)
+    k_trd_grid(const double *__restrict__ rho, const int64_t *__restrict__ rho_off, const int *__restrict__ dims,
+               const int *__restrict__ ev_off, int q, double *__restrict__ refl, double *__restrict__ td,
+               double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm, double *__restrict__ gA,
+               double *__restrict__ comm, unsigned *bar, int *err) {
+    constexpr int NW = TRD_THREADS / 32;
+    const int G = gridDim.x, r = blockIdx.x;
+    const int n = dims[q], eo = ev_off[q];
+    const int ncol = r < n ? (n - r + G - 1) / G : 0;
+    extern __shared__ double tg_smem[];
+    double *v = tg_smem, *w = v + n;
+    __shared__ double red[NW];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const double *R = rho + rho_off[q];
+    double *Vq = refl + rho_off[q];
+    double *gv = comm, *gp = comm + 2 * (int64_t)n, *gt = comm + 4 * (int64_t)n, *gs = gt + 2;
+    auto colp = [&](int jj) -> double * { return gA + (int64_t)(r + G * jj) * n; };
+    for (int e = tid; e < ncol * n; e += TRD_THREADS) {
+        const int jj = e / n, i = e - jj * n;
+        colp(jj)[i] = R[(int64_t)(r + G * jj) * n + i];   // column j = row j (symmetric)
+    }
+    if (r == 0)
+        for (int i = tid; i < n; i += TRD_THREADS) perm[eo + i] = i;
+    unsigned epoch = 0;
+    bool alive = tg_sync(bar, epoch, err);
+    for (int k = 0; alive && k + 2 < n; ++k) {
+        const int m = n - k - 1, par = k & 1, o = k % G;
+        double *vb = gv + par * (int64_t)n, *pb = gp + par * (int64_t)n, *sb = gs + par * G;
+        if (r == o) {
+            const double *colk = colp(k / G);
+            __shared__ double hs[2];
+            if (warp == 0) {
+                double ss = 0.0;
+                for (int i = k + 2 + lane; i < n; i += 32) ss = fma(colk[i], colk[i], ss);
+                ss = wsum(ss);
+                if (lane == 0) {
+                    const double alpha = colk[k + 1];
+                    double t = 0.0, beta = alpha, scal = 0.0;
+                    if (ss > 0.0) {
+                        beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
+                        t = (beta - alpha) / beta;
+                        scal = 1.0 / (alpha - beta);
+                    }
+                    hs[0] = t;
+                    hs[1] = scal;
+                    gt[par] = t;
+                    td[eo + k] = colk[k];
+                    te[eo + k] = beta;
+                    tau[eo + k] = t;
+                }
+            }
+            __syncthreads();
+            const double scal = hs[1];
+            for (int i = tid; i < m; i += TRD_THREADS) {
+                const double x = (i == 0) ? 1.0 : colk[k + 1 + i] * scal;
+                vb[i] = x;
+                Vq[(int64_t)k * n + k + 1 + i] = x;
+            }
+        }
+        if (!(alive = tg_sync(bar, epoch, err))) break;   // v and t of step k published
+        const double t = *(volatile double *)(gt + par);
+        for (int i = tid; i < m; i += TRD_THREADS) v[i] = ((volatile double *)vb)[i];
+        __syncthreads();
+        const int jj0 = k + 1 > r ? (k + 1 - r + G - 1) / G : 0;   // first own column j > k
+        double sp = 0.0;
+        if (t != 0.0)
+            for (int jj = jj0 + warp; jj < ncol; jj += NW) {
+                const double *a = colp(jj) + k + 1;
+                double a0 = 0.0, a1 = 0.0;
+                int i = lane;
+                for (; i + 32 < m; i += 64) {
+                    a0 = fma(a[i], v[i], a0);
+                    a1 = fma(a[i + 32], v[i + 32], a1);
+                }
+                if (i < m) a0 = fma(a[i], v[i], a0);
+                const int jc = r + G * jj - k - 1;
+                const double pj = t * wsum(a0 + a1);
+                if (lane == 0) pb[jc] = pj;
+                sp = fma(pj, v[jc], sp);
+            }
+        if (lane == 0) red[warp] = sp;
+        __syncthreads();
+        if (tid == 0) {
+            double x = 0.0;
+            for (int u = 0; u < NW; ++u) x += red[u];
+            sb[r] = x;
+        }
+        if (!(alive = tg_sync(bar, epoch, err))) break;   // p and the p.v shares published
+        __shared__ double kk;
+        if (warp == 0) {
+            double x = 0.0;
+            for (int u = lane; u < G; u += 32) x += ((volatile double *)sb)[u];
+            x = wsum(x);
+            if (lane == 0) kk = -0.5 * t * x;
+        }
+        __syncthreads();
+        const double K = kk;
+        if (t != 0.0) {
+            for (int i = tid; i < m; i += TRD_THREADS) w[i] = fma(K, v[i], ((volatile double *)pb)[i]);
+            __syncthreads();
+            for (int jj = jj0 + warp; jj < ncol; jj += NW) {
+                const int jc = r + G * jj - k - 1;
+                const double vj = v[jc], wj = w[jc];
+                double *a = colp(jj) + k + 1;
+                for (int i = lane; i < m; i += 32) a[i] -= fma(v[i], wj, w[i] * vj);
+            }
+        }
+        __syncthreads();
+    }
+    if (alive && n >= 2 && r == (n - 2) % G && tid == 0) {
+        const double *c2 = colp((n - 2) / G);
+        td[eo + n - 2] = c2[n - 2];
+        te[eo + n - 2] = c2[n - 1];
+        tau[eo + n - 2] = 0.0;
+    }
+    if (alive && r == (n - 1) % G && tid == 0) {
+        td[eo + n - 1] = colp((n - 1) / G)[n - 1];
+        te[eo + n - 1] = 0.0;
+        tau[eo + n - 1] = 0.0;
+    }
+}
+
 // Number of eigenvalues of the scaled T below s (a: diagonal, bb[i] =
 // b_{i-1}^2, bb[0] = 0; the caller passes one unreduced block).  Sign changes of the leading minors; an exact zero
 // minor is replaced by -2^-100 times the previous one (a negative pivot, as
@@ -1107,6 +1267,41 @@ int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, cons
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, kern, rho, rho_off, dims, ev_off, blocks, refl, td, te, tau, perm, gA, goff);
     return (int)e;
+}
+
+// One cooperative launch of k_trd_grid per block of `blocks` (host list):
+// gA + goff_h[b] is block b's n x n scratch, comm at least 4 maxn + 2 + 2 G
+// doubles, bar two unsigned and err one int of device memory (zeroed here).
+int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off,
+                  const std::vector<int> &blocks, const std::vector<int> &nb, double *refl, double *td, double *te,
+                  double *tau, int *perm, double *gA, const std::vector<int64_t> &goff_h, double *comm,
+                  unsigned *bar, int *err, cudaStream_t st) {
+    if (blocks.empty()) return 0;
+    int dev = 0, nsm = 0, maxn = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    for (int x : nb) maxn = std::max(maxn, x);
+    const size_t smem = 2 * (size_t)maxn * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_trd_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trd_grid, TRD_THREADS, smem);
+    if (e != cudaSuccess) return (int)e;
+    if (occ < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
+    e = cudaMemsetAsync(err, 0, sizeof(int), st);
+    if (e != cudaSuccess) return (int)e;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+        e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st);
+        if (e != cudaSuccess) return (int)e;
+        int q = blocks[b];
+        double *g = gA + goff_h[b];
+        void *args[] = {(void *)&rho, (void *)&rho_off, (void *)&dims, (void *)&ev_off, (void *)&q, (void *)&refl,
+                        (void *)&td, (void *)&te, (void *)&tau, (void *)&perm, (void *)&g, (void *)&comm,
+                        (void *)&bar, (void *)&err};
+        e = cudaLaunchCooperativeKernel((const void *)k_trd_grid, dim3(nsm), dim3(TRD_THREADS), args, smem, st);
+        if (e != cudaSuccess) return (int)e;
+    }
+    return 0;
 }
 
 int syev_bisect(const int *dims, const int *ev_off, const int2 *items, int nitems, const double *td,
