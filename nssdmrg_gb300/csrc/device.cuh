@@ -293,9 +293,12 @@ int syev_trd_cl_size(int *nmax);
 int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
                 int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, double *gA,
                 const int64_t *goff, cudaStream_t st);
-// k_trd_grid: the same reduction of each block in `blocks` (dims nb) by the
-// whole GPU, one cooperative launch per block, for blocks far beyond a
-// cluster's reach; *err (device) is set if a grid barrier timed out.
+// k_trd_grid: the same reduction of the blocks in `blocks` (dims nb) by the
+// whole GPU, up to 8 blocks a cooperative launch on CTA groups sized by
+// n^3, for blocks far beyond a cluster's reach; comm needs
+// syev_trd_grid_comm(nb, SMs) doubles, bar 8 unsigned; *err (device) is set
+// if a barrier timed out.
+int64_t syev_trd_grid_comm(const std::vector<int> &nb, int nsm);
 int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off,
                   const std::vector<int> &blocks, const std::vector<int> &nb, double *refl, double *td, double *te,
                   double *tau, int *perm, double *gA, const std::vector<int64_t> &goff_h, double *comm,

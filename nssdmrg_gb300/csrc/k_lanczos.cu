@@ -1967,9 +1967,10 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
                 k_to32<<<608, 256, 0, st>>>(y32 + (int64_t)f * n, z.evecs + (int64_t)f * n, 1.0, n);
             AnchorSpec as{u, u32, r32, y32, e, th[e], u};
             int it2 = 0, m2 = 0;
-            // a pass gains at most ~1e4 (the FP32 floor of the correction):
-            // the anchored problem is solved to 1e-4 of the vector's residual
-            const double tol_pass = std::max(tol, 1e-4 * beta0 / std::max(std::fabs(th[e]), 1e-300));
+            // the anchored problem is solved to 1e-6 of the vector's residual
+            // (from the FP32 phase's 1e-7 that is the final tolerance: one
+            // pass; a stalled pass cannot gain more than its FP32 floor)
+            const double tol_pass = std::max(tol, 1e-6 * beta0 / std::max(std::fabs(th[e]), 1e-300));
             if (int rc2 = run_lanczos<float>(c, z.V32, z.w32, 1, mmax, tol_pass, seed, &it2, &m2, &as)) return rc2;
             numop_ += it2;
             return NSS_OK;

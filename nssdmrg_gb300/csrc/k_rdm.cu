@@ -765,11 +765,11 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             }
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            const int64_t ncomm = 4 * (int64_t)maxn_g + 2 + 2 * (int64_t)nsm;
-            if ((rc = ensure_n(c, &r.tg, r.cap_tg, ncomm + 2))) { cleanup(); return rc; }
-            unsigned *bar = (unsigned *)(r.tg + ncomm);
-            int *gerr = (int *)(r.tg + ncomm + 1);
-            c.launches += (int64_t)gb.size();
+            const int64_t ncomm = syev_trd_grid_comm(gn, nsm);
+            if ((rc = ensure_n(c, &r.tg, r.cap_tg, ncomm + 8))) { cleanup(); return rc; }
+            unsigned *bar = (unsigned *)(r.tg + ncomm);          // 8 counters
+            int *gerr = (int *)(r.tg + ncomm + 4);
+            c.launches += (int64_t)(gb.size() + 7) / 8;
             e = syev_trd_grid(r.rho, d_rho_off, d_dims, d_ev_off, gb, gn, refl, td, te, tau, perm, r.big, gofs,
                               r.tg, bar, gerr, st);
             if (!e) {

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
             const double vi = v[i], wi = w[i];
             for (int j = lane; j <= i; j += 32) {
                 const int c = k + 1 + j;
-                A[r * ld + c] -= fma(vi, w[j], wi * v[j]);
+                A[r * ld + c] = fma(-vi, w[j], fma(-wi, v[j], A[r * ld + c]));   // two FMAs
             }
         }
         __syncthreads();
@@ -353,7 +353,8 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 const int jc = r + C * jj - k - 1;
                 const double vj = v[jc], wj = w[jc];
                 double *a = colp(jj) + k + 1;
-                for (int i = lane; i < m; i += 32) a[i] -= fma(v[i], wj, w[i] * vj);
+                const double nvj = -vj, nwj = -wj;
+                for (int i = lane; i < m; i += 32) a[i] = fma(v[i], nwj, fma(w[i], nvj, a[i]));   // two FMAs
             }
         __syncthreads();
     }
@@ -371,18 +372,18 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     cl.sync();                                       // no CTA leaves while its memory may be read
 }
 
-// Bounded grid barrier of k_trd_grid (cooperative launch, all CTAs
-// resident): barrier e of a launch waits for e * G arrivals on bar[0]; a
-// wait that runs past TG_SPIN polls sets *err, and every later barrier
-// returns false at once, so the kernel always ends.  bar[0] and *err are
-// zero at launch.
+// Bounded barrier of one CTA group of k_trd_grid (cooperative launch, all
+// CTAs resident): barrier e of a launch waits for e * G arrivals on *bar, G
+// the group's CTAs; a wait that runs past TG_SPIN polls sets *err, and every
+// later barrier (of any group) returns false at once, so the kernel always
+// ends.  The counters and *err are zero at launch.
 constexpr uint32_t TG_SPIN = 1u << 22;
-__device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned &epoch, int *err) {
+__device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned G, unsigned &epoch, int *err) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int good = 1;
-        epoch += gridDim.x;
+        epoch += G;
         __threadfence();
         atomicAdd(bar, 1u);
         uint32_t it = 0;
@@ -401,26 +402,46 @@ __device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned &epoch, int *err
     return ok != 0;
 }
 
-// The Householder reduction of one very large block by the whole GPU (a
-// cooperative launch of one CTA per SM): k_trd_cl's step with the CTAs of
-// the grid in place of a cluster's, so the n^3 FP64 FMAs spread over every
-// SM instead of 16.  CTA r holds columns j = r + G jj of the block's global
-// (L2-resident) copy gA; the reflector, the p_j and the partial sums p.v
-// cross CTAs through global buffers (comm: v [2][n], p [2][n], t [2],
-// partials [2][G]) that alternate with the parity of k, between two grid
-// barriers a step.
+// Blocks of one k_trd_grid launch: group g (CTAs c0[g] .. c0[g+1]-1)
+// reduces block q[g], whose copy is gA + goff[g] and whose exchange buffers
+// are comm + coff[g]; its barrier counter is bars[g].
+constexpr int TG_MAXG = 8;
+struct TgGroups {
+    int ng;
+    int q[TG_MAXG];
+    int c0[TG_MAXG + 1];
+    int64_t goff[TG_MAXG], coff[TG_MAXG];
+};
+
+// The Householder reduction of very large blocks by the whole GPU (a
+// cooperative launch of one CTA per SM, split into one CTA group per block
+// in proportion to the blocks' n^3): k_trd_cl's step with a group's CTAs in
+// place of a cluster's, so the FP64 FMAs spread over every SM instead of 16
+// per block.  CTA r of a group holds columns j = r + G jj of its block's
+// global (L2-resident) copy; the reflector, the p_j and the partial sums p.v
+// cross CTAs through global buffers (v [2][n], p [2][n], t [2], partials
+// [2][G]) that alternate with the parity of k, between two group barriers a
+// step.
 __global__ void __launch_bounds__(TRD_THREADS, 1)
     k_trd_grid(const double *__restrict__ rho, const int64_t *__restrict__ rho_off, const int *__restrict__ dims,
-               const int *__restrict__ ev_off, int q, double *__restrict__ refl, double *__restrict__ td,
-               double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm, double *__restrict__ gA,
-               double *__restrict__ comm, unsigned *bar, int *err) {
+               const int *__restrict__ ev_off, TgGroups grp, double *__restrict__ refl, double *__restrict__ td,
+               double *__restrict__ te, double *__restrict__ tau, int *__restrict__ perm, double *__restrict__ gA0,
+               double *__restrict__ comm0, unsigned *bars, int *err) {
     constexpr int NW = TRD_THREADS / 32;
-    const int G = gridDim.x, r = blockIdx.x;
+    int g = 0;
+    while (g + 1 < grp.ng && (int)blockIdx.x >= grp.c0[g + 1]) ++g;
+    const int G = grp.c0[g + 1] - grp.c0[g], r = (int)blockIdx.x - grp.c0[g];
+    const int q = grp.q[g];
+    double *const gA = gA0 + grp.goff[g];
+    double *const comm = comm0 + grp.coff[g];
+    unsigned *const bar = bars + g;
     const int n = dims[q], eo = ev_off[q];
     const int ncol = r < n ? (n - r + G - 1) / G : 0;
     extern __shared__ double tg_smem[];
     double *v = tg_smem, *w = v + n;
     __shared__ double red[NW];
+    __shared__ double hs[2];
+    __shared__ double kk;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const double *R = rho + rho_off[q];
     double *Vq = refl + rho_off[q];
@@ -433,32 +454,33 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     if (r == 0)
         for (int i = tid; i < n; i += TRD_THREADS) perm[eo + i] = i;
     unsigned epoch = 0;
-    bool alive = tg_sync(bar, epoch, err);
+    bool alive = tg_sync(bar, G, epoch, err);
     for (int k = 0; alive && k + 2 < n; ++k) {
         const int m = n - k - 1, par = k & 1, o = k % G;
         double *vb = gv + par * (int64_t)n, *pb = gp + par * (int64_t)n, *sb = gs + par * G;
         if (r == o) {
             const double *colk = colp(k / G);
-            __shared__ double hs[2];
-            if (warp == 0) {
-                double ss = 0.0;
-                for (int i = k + 2 + lane; i < n; i += 32) ss = fma(colk[i], colk[i], ss);
-                ss = wsum(ss);
-                if (lane == 0) {
-                    const double alpha = colk[k + 1];
-                    double t = 0.0, beta = alpha, scal = 0.0;
-                    if (ss > 0.0) {
-                        beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
-                        t = (beta - alpha) / beta;
-                        scal = 1.0 / (alpha - beta);
-                    }
-                    hs[0] = t;
-                    hs[1] = scal;
-                    gt[par] = t;
-                    td[eo + k] = colk[k];
-                    te[eo + k] = beta;
-                    tau[eo + k] = t;
+            double ss = 0.0;                         // sum of squares below the subdiagonal, all warps
+            for (int i = k + 2 + tid; i < n; i += TRD_THREADS) ss = fma(colk[i], colk[i], ss);
+            ss = wsum(ss);
+            if (lane == 0) red[warp] = ss;
+            __syncthreads();
+            if (tid == 0) {
+                double x = 0.0;
+                for (int u = 0; u < NW; ++u) x += red[u];
+                const double alpha = colk[k + 1];
+                double t = 0.0, beta = alpha, scal = 0.0;
+                if (x > 0.0) {
+                    beta = -copysign(sqrt(fma(alpha, alpha, x)), alpha);
+                    t = (beta - alpha) / beta;
+                    scal = 1.0 / (alpha - beta);
                 }
+                hs[0] = t;
+                hs[1] = scal;
+                gt[par] = t;
+                td[eo + k] = colk[k];
+                te[eo + k] = beta;
+                tau[eo + k] = t;
             }
             __syncthreads();
             const double scal = hs[1];
@@ -468,7 +490,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 Vq[(int64_t)k * n + k + 1 + i] = x;
             }
         }
-        if (!(alive = tg_sync(bar, epoch, err))) break;   // v and t of step k published
+        if (!(alive = tg_sync(bar, G, epoch, err))) break;   // v and t of step k published
         const double t = *(volatile double *)(gt + par);
         for (int i = tid; i < m; i += TRD_THREADS) v[i] = ((volatile double *)vb)[i];
         __syncthreads();
@@ -477,15 +499,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         if (t != 0.0)
             for (int jj = jj0 + warp; jj < ncol; jj += NW) {
                 const double *a = colp(jj) + k + 1;
-                double a0 = 0.0, a1 = 0.0;
+                double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
                 int i = lane;
-                for (; i + 32 < m; i += 64) {
+                for (; i + 96 < m; i += 128) {
                     a0 = fma(a[i], v[i], a0);
                     a1 = fma(a[i + 32], v[i + 32], a1);
+                    a2 = fma(a[i + 64], v[i + 64], a2);
+                    a3 = fma(a[i + 96], v[i + 96], a3);
                 }
-                if (i < m) a0 = fma(a[i], v[i], a0);
+                for (; i < m; i += 32) a0 = fma(a[i], v[i], a0);
                 const int jc = r + G * jj - k - 1;
-                const double pj = t * wsum(a0 + a1);
+                const double pj = t * wsum((a0 + a1) + (a2 + a3));
                 if (lane == 0) pb[jc] = pj;
                 sp = fma(pj, v[jc], sp);
             }
@@ -496,8 +520,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
             for (int u = 0; u < NW; ++u) x += red[u];
             sb[r] = x;
         }
-        if (!(alive = tg_sync(bar, epoch, err))) break;   // p and the p.v shares published
-        __shared__ double kk;
+        if (!(alive = tg_sync(bar, G, epoch, err))) break;   // p and the p.v shares published
         if (warp == 0) {
             double x = 0.0;
             for (int u = lane; u < G; u += 32) x += ((volatile double *)sb)[u];
@@ -513,7 +536,8 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 const int jc = r + G * jj - k - 1;
                 const double vj = v[jc], wj = w[jc];
                 double *a = colp(jj) + k + 1;
-                for (int i = lane; i < m; i += 32) a[i] -= fma(v[i], wj, w[i] * vj);
+                const double nvj = -vj, nwj = -wj;
+                for (int i = lane; i < m; i += 32) a[i] = fma(v[i], nwj, fma(w[i], nvj, a[i]));   // two FMAs
             }
         }
         __syncthreads();
@@ -1269,9 +1293,17 @@ int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, cons
     return (int)e;
 }
 
-// One cooperative launch of k_trd_grid per block of `blocks` (host list):
-// gA + goff_h[b] is block b's n x n scratch, comm at least 4 maxn + 2 + 2 G
-// doubles, bar two unsigned and err one int of device memory (zeroed here).
+// k_trd_grid launches for the blocks of `blocks` (host list, sizes nb): up
+// to TG_MAXG blocks a launch, the SMs split among them in proportion to n^3
+// (at least 8 each).  gA + goff_h[b] is block b's n x n scratch; comm holds
+// 4 n + 2 + 2 nsm doubles per block of a launch (syev_trd_grid_comm), bar
+// TG_MAXG unsigned and err one int of device memory (zeroed here).
+int64_t syev_trd_grid_comm(const std::vector<int> &nb, int nsm) {
+    int64_t tot = 0;
+    for (int x : nb) tot += 4 * (int64_t)x + 2 + 2 * (int64_t)nsm;
+    return tot;
+}
+
 int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off,
                   const std::vector<int> &blocks, const std::vector<int> &nb, double *refl, double *td, double *te,
                   double *tau, int *perm, double *gA, const std::vector<int64_t> &goff_h, double *comm,
@@ -1290,13 +1322,36 @@ int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, co
     if (occ < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
     e = cudaMemsetAsync(err, 0, sizeof(int), st);
     if (e != cudaSuccess) return (int)e;
-    for (size_t b = 0; b < blocks.size(); ++b) {
-        e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st);
+    const int per = std::max(1, std::min(TG_MAXG, nsm / 8));
+    for (size_t b0 = 0; b0 < blocks.size(); b0 += per) {
+        const int ng = (int)std::min<size_t>(per, blocks.size() - b0);
+        TgGroups grp{};
+        grp.ng = ng;
+        double w3[TG_MAXG], wsum3 = 0.0;
+        for (int g = 0; g < ng; ++g) {
+            const double x = nb[b0 + g];
+            w3[g] = x * x * x;
+            wsum3 += w3[g];
+        }
+        // CTAs in proportion to n^3, at least 8 a group, all nsm used
+        int cnt[TG_MAXG], left = nsm - 8 * ng;
+        for (int g = 0; g < ng; ++g) cnt[g] = 8 + (int)std::floor(left * (w3[g] / wsum3));
+        int used = 0;
+        for (int g = 0; g < ng; ++g) used += cnt[g];
+        for (int g = 0; used < nsm; g = (g + 1) % ng, ++used) ++cnt[g];
+        int64_t coff = 0;
+        grp.c0[0] = 0;
+        for (int g = 0; g < ng; ++g) {
+            grp.q[g] = blocks[b0 + g];
+            grp.c0[g + 1] = grp.c0[g] + cnt[g];
+            grp.goff[g] = goff_h[b0 + g];
+            grp.coff[g] = coff;
+            coff += 4 * (int64_t)nb[b0 + g] + 2 + 2 * (int64_t)nsm;
+        }
+        e = cudaMemsetAsync(bar, 0, TG_MAXG * sizeof(unsigned), st);
         if (e != cudaSuccess) return (int)e;
-        int q = blocks[b];
-        double *g = gA + goff_h[b];
-        void *args[] = {(void *)&rho, (void *)&rho_off, (void *)&dims, (void *)&ev_off, (void *)&q, (void *)&refl,
-                        (void *)&td, (void *)&te, (void *)&tau, (void *)&perm, (void *)&g, (void *)&comm,
+        void *args[] = {(void *)&rho, (void *)&rho_off, (void *)&dims, (void *)&ev_off, (void *)&grp, (void *)&refl,
+                        (void *)&td, (void *)&te, (void *)&tau, (void *)&perm, (void *)&gA, (void *)&comm,
                         (void *)&bar, (void *)&err};
         e = cudaLaunchCooperativeKernel((const void *)k_trd_grid, dim3(nsm), dim3(TRD_THREADS), args, smem, st);
         if (e != cudaSuccess) return (int)e;
