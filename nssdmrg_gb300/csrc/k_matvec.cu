@@ -71,7 +71,46 @@ struct Stager {
         items.push_back({(void **)dst, (const void *)v.data(), bytes, total});
         total += (std::max<size_t>(bytes, 16) + 255) / 256 * 256;
     }
+    // a section the device fills (no host source, not copied)
+    template <class T>
+    void add_dev(T **dst, size_t count) {
+        const size_t bytes = count * sizeof(T);
+        items.push_back({(void **)dst, nullptr, bytes, total});
+        total += (std::max<size_t>(bytes, 16) + 255) / 256 * 256;
+    }
 };
+
+// Dense sector operators from their CSR rows: one thread per row of one
+// sector's H_L or H_R (rows of both sides in one launch), duplicates summed
+// as the host build did; the blocks are zeroed beforehand.  FP32 copies
+// follow in k_dense32.
+struct DenseRows {
+    const int *rowptr;      // per side: all sectors' rows, global entry offsets
+    const int *col;
+    const double *val;
+    const int *row_sec;     // sector of each row (global row index)
+    const int64_t *row_first;   // first global row of each sector
+};
+__global__ void __launch_bounds__(256) k_densify(DenseRows L, DenseRows R, int nrow_l, int nrow_r,
+                                                  const int *__restrict__ dls, const int *__restrict__ drs,
+                                                  const int64_t *__restrict__ hl_off, const int64_t *__restrict__ hr_off,
+                                                  double *__restrict__ hl, double *__restrict__ hr) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nrow_l + nrow_r) return;
+    const bool right = t >= nrow_l;
+    const DenseRows &D = right ? R : L;
+    const int g = (int)(right ? t - nrow_l : t);
+    const int k = D.row_sec[g];
+    const int d = right ? drs[k] : dls[k];
+    const int i = (int)(g - D.row_first[k]);
+    double *row = (right ? hr + hr_off[k] : hl + hl_off[k]) + (int64_t)i * d;
+    for (int p = D.rowptr[g]; p < D.rowptr[g + 1]; ++p) row[D.col[p]] += D.val[p];
+}
+
+__global__ void __launch_bounds__(256) k_dense32(const double *__restrict__ x, float *__restrict__ y, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (float)x[i];
+}
 
 int stage_commit(Ctx &c, Stager &sg) {
     if (c.sb_arena_cap < sg.total) {
@@ -93,13 +132,14 @@ int stage_commit(Ctx &c, Stager &sg) {
     const size_t half = sg.items.size() / 2;
     auto fill = [&](size_t i0, size_t i1) {
         for (size_t i = i0; i < i1; ++i)
-            if (sg.items[i].bytes) std::memcpy(c.sb_stage + sg.items[i].off, sg.items[i].src, sg.items[i].bytes);
+            if (sg.items[i].bytes && sg.items[i].src)
+                std::memcpy(c.sb_stage + sg.items[i].off, sg.items[i].src, sg.items[i].bytes);
     };
     run_pair([&] { fill(0, half); }, [&] { fill(half, sg.items.size()); });
     NSS_CUDA_TRY(c, cudaMemcpyAsync(c.sb_arena, c.sb_stage, sg.total, cudaMemcpyHostToDevice, c.stream));
     for (const auto &it : sg.items) {
         *it.dst = (void *)(c.sb_arena + it.off);
-        c.sb.h2d_bytes += (int64_t)it.bytes;
+        if (it.src) c.sb.h2d_bytes += (int64_t)it.bytes;
     }
     return NSS_OK;
 }
@@ -169,28 +209,74 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
             if (x < 0 || x >= d->m_right) { c.err = "nss_sb_upload: bi out of range"; return NSS_ERR_INVALID; }
     }
 
-    // dense sector operators
-    std::vector<double> hl, hr;
+    // dense sector operators: their CSR rows travel and the device scatters
+    // them into zeroed row-major blocks (k_densify), FP32 copies after
+    int64_t hl_tot = 0, hr_tot = 0, nnz_l = 0, nnz_r = 0, nrow_l = 0, nrow_r = 0;
     for (int k = 0; k < s.nsb; ++k) {
         const int dl = s.dls[k], dr = s.drs[k];
         if (!csr_ok(d->hleft[k], dl, dl) || !csr_ok(d->hright[k], dr, dr)) {
             c.err = "nss_sb_upload: Hleft/Hright shape or index error at sector " + std::to_string(k);
             return NSS_ERR_INVALID;
         }
-        s.hl_off.push_back((int64_t)hl.size());
-        s.hr_off.push_back((int64_t)hr.size());
-        size_t bl = hl.size(), br = hr.size();
-        hl.resize(bl + (size_t)dl * dl, 0.0);
-        hr.resize(br + (size_t)dr * dr, 0.0);
-        const nss_csr &L = d->hleft[k], &R = d->hright[k];
-        for (int i = 0; i < dl; ++i)
-            for (int jj = L.rowptr[i]; jj < L.rowptr[i + 1]; ++jj) hl[bl + (size_t)i * dl + L.colidx[jj]] += L.vals[jj];
-        for (int i = 0; i < dr; ++i)
-            for (int jj = R.rowptr[i]; jj < R.rowptr[i + 1]; ++jj) hr[br + (size_t)i * dr + R.colidx[jj]] += R.vals[jj];
+        s.hl_off.push_back(hl_tot);
+        s.hr_off.push_back(hr_tot);
+        hl_tot += (int64_t)dl * dl;
+        hr_tot += (int64_t)dr * dr;
+        nnz_l += d->hleft[k].rowptr[dl];
+        nnz_r += d->hright[k].rowptr[dr];
+        nrow_l += dl;
+        nrow_r += dr;
         s.flops_dense += 2.0 * dl * dr * ((double)dl + dr);
     }
-    s.hl_off.push_back((int64_t)hl.size());
-    s.hr_off.push_back((int64_t)hr.size());
+    s.hl_off.push_back(hl_tot);
+    s.hr_off.push_back(hr_tot);
+    if (nnz_l > INT32_MAX || nnz_r > INT32_MAX) {
+        c.err = "nss_sb_upload: more than 2^31 entries in the sector operators";
+        return NSS_ERR_INVALID;
+    }
+    struct PackedRows {
+        std::vector<int> rowptr, col, row_sec;
+        std::vector<double> val;
+        std::vector<int64_t> row_first;
+    } pk[2];
+    run_pair(
+        [&] {
+            for (int side = 0; side < 2; ++side) {
+                PackedRows &P = pk[side];
+                P.rowptr.reserve((size_t)(side ? nrow_r : nrow_l) + 1);
+                P.rowptr.push_back(0);
+                P.row_first.reserve(s.nsb);
+                P.row_sec.reserve((size_t)(side ? nrow_r : nrow_l));
+                int64_t rows = 0;
+                for (int k = 0; k < s.nsb; ++k) {
+                    const nss_csr &M = side ? d->hright[k] : d->hleft[k];
+                    const int base = P.rowptr.back();
+                    P.row_first.push_back(rows);
+                    for (int i = 0; i < M.nrow; ++i) {
+                        P.rowptr.push_back(base + M.rowptr[i + 1]);
+                        P.row_sec.push_back(k);
+                    }
+                    rows += M.nrow;
+                }
+            }
+        },
+        [&] {
+            for (int side = 0; side < 2; ++side) {
+                PackedRows &P = pk[side];
+                P.col.resize((size_t)(side ? nnz_r : nnz_l));
+                P.val.resize((size_t)(side ? nnz_r : nnz_l));
+                int64_t at = 0;
+                for (int k = 0; k < s.nsb; ++k) {
+                    const nss_csr &M = side ? d->hright[k] : d->hleft[k];
+                    const int nz = M.rowptr[M.nrow];
+                    if (nz) {
+                        std::memcpy(P.col.data() + at, M.colidx, sizeof(int) * (size_t)nz);
+                        std::memcpy(P.val.data() + at, M.vals, sizeof(double) * (size_t)nz);
+                    }
+                    at += nz;
+                }
+            }
+        });
 
     // A x B terms, regrouped by output sector
     std::vector<std::vector<DevTerm>> by_out(s.nsb);
@@ -250,7 +336,6 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     // entries (up to 33 per row at m=256) whose contribution (~1e-17 of the
     // result) is far below FP32 rounding, while each of them costs a gather.
     // The FP64 pool keeps every entry, as the reference does.
-    std::vector<float> hl32(hl.begin(), hl.end()), hr32(hr.begin(), hr.end());
     std::vector<int> rowptr32, col32;
     std::vector<float> val32;
     std::vector<DevTerm> terms32 = s.terms;
@@ -385,8 +470,8 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     std::vector<int> tc_err(1, 0);
 
     Stager sg;
-    sg.add(&s.d_hl32, hl32);
-    sg.add(&s.d_hr32, hr32);
+    sg.add_dev(&s.d_hl32, (size_t)hl_tot);
+    sg.add_dev(&s.d_hr32, (size_t)hr_tot);
     sg.add(&s.d_ab_val32, val32);
     sg.add(&s.d_ab_rowptr32, rowptr32);
     sg.add(&s.d_ab_col32, col32);
@@ -403,8 +488,16 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     sg.add(&s.d_off, s.off);
     sg.add(&s.d_hl_off, s.hl_off);
     sg.add(&s.d_hr_off, s.hr_off);
-    sg.add(&s.d_hl, hl);
-    sg.add(&s.d_hr, hr);
+    sg.add_dev(&s.d_hl, (size_t)hl_tot);
+    sg.add_dev(&s.d_hr, (size_t)hr_tot);
+    DenseRows dr_dev[2];
+    for (int side = 0; side < 2; ++side) {
+        sg.add((int **)&dr_dev[side].rowptr, pk[side].rowptr);
+        sg.add((int **)&dr_dev[side].col, pk[side].col);
+        sg.add((double **)&dr_dev[side].val, pk[side].val);
+        sg.add((int **)&dr_dev[side].row_sec, pk[side].row_sec);
+        sg.add((int64_t **)&dr_dev[side].row_first, pk[side].row_first);
+    }
     sg.add(&s.d_term_ptr, s.term_ptr);
     sg.add(&s.d_terms, s.terms);
     sg.add(&s.d_ab_rowptr, rowptr);
@@ -413,6 +506,18 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
     sg.add(&s.d_tiles, tiles);
     int rc;
     if ((rc = stage_commit(c, sg))) return rc;
+    NSS_CUDA_TRY(c, cudaMemsetAsync(s.d_hl, 0, (size_t)hl_tot * sizeof(double), c.stream));
+    NSS_CUDA_TRY(c, cudaMemsetAsync(s.d_hr, 0, (size_t)hr_tot * sizeof(double), c.stream));
+    {
+        const int64_t nr = nrow_l + nrow_r;
+        c.launches += 3;
+        k_densify<<<(unsigned)((nr + 255) / 256), 256, 0, c.stream>>>(dr_dev[0], dr_dev[1], (int)nrow_l, (int)nrow_r,
+                                                                      s.d_dls, s.d_drs, s.d_hl_off, s.d_hr_off,
+                                                                      s.d_hl, s.d_hr);
+        k_dense32<<<608, 256, 0, c.stream>>>(s.d_hl, s.d_hl32, hl_tot);
+        k_dense32<<<608, 256, 0, c.stream>>>(s.d_hr, s.d_hr32, hr_tot);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
     s.valid = true;
     return NSS_OK;
