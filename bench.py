@@ -56,6 +56,10 @@ def parse():
                     help="finite sweeps timed on the spin-1 L=64 m=512 chain (0 skips it)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--profile-case", choices=["renorm", "trd-grid"], default=None,
+                    help="for profiler captures of single kernels: run one small workload and exit "
+                         "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
+                         "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -381,6 +385,34 @@ def measure_serving(nss, device):
     return out
 
 
+def run_profile_case(case):
+    """Small single-kernel workloads for ncu captures (see --profile-case)."""
+    import numpy as np
+    import scipy.sparse as sp
+    import torch
+    torch.cuda.set_device(0)
+    import nssdmrg_gb300 as nss
+    if case == "renorm":
+        d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 12, 256, dmrg_qn=(0.0, 0.0), lanc_neigen=1, lanc_niter=200,
+                     lanc_tolerance=1e-12, precision=nss.NSS_PREC_MIXED)
+        recs = d.infinite()
+        print(json.dumps({"profile_case": case, "steps": len(recs), "m_last": recs[-1]["m_left"],
+                          "ms_renorm_last": [round(r["ms_renorm"], 3) for r in recs[-4:]]}))
+        return
+    nbig = 1000
+    rng = np.random.default_rng(1)
+    dls, drs = [nbig, 40], [24, 40]
+    off = [0, nbig * 24]
+    s = nss.Superblock()
+    s.upload(dls, drs, off, [sp.identity(x, format="csr") for x in dls], [sp.identity(x, format="csr") for x in drs],
+             [], 0, nbig + 40, 64, [np.arange(nbig), np.arange(nbig, nbig + 40)], [np.arange(24), np.arange(24, 64)])
+    psi = rng.standard_normal(off[1] + 1600)
+    psi /= np.linalg.norm(psi)
+    os.environ["NSS_TRD_GRID_MIN"] = "900"
+    res = s.sb_get_rdm(64, 0.1, psi=psi, want_u=False)
+    print(json.dumps({"profile_case": case, "block": nbig, "m_s": list(res.m_s), "lambda0": res.lambdas[0][0]}))
+
+
 def run_gpu(args):
     import torch
 
@@ -685,7 +717,9 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.profile_case:
+        run_profile_case(a.profile_case)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_gpu(a)
