@@ -211,6 +211,8 @@ struct Ctx {
     size_t sb_arena_cap = 0, sb_stage_cap = 0;
     double renorm_phase_ms[3] = {0, 0, 0};
     int refine_passes = 0, refine_cluster = 0;   // mixed refinement of the last solve
+    int rdm_refined_blocks = 0;                  // flagged blocks redone by k_vec_fb in the last nss_rdm
+    int rdm_ql_blocks = 0;                       // ... and of those, blocks finished by host QL
     int64_t mixed_fallbacks = 0;                 // mixed solves redone in FP64 (context life)
     char *ms_dev = nullptr, *ms_host = nullptr;   // OdotV tables: device, pinned staging
     size_t ms_cap = 0;   // host: scan+extract, device wait, CSR assembly (summed over calls)
@@ -306,6 +308,19 @@ int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, co
 
 // kept eigenvectors of both sides (ms[0] left, ms[1] right; right positions
 // start at nl): k_vec + the cluster Gram-Schmidt, two launches
+// Back-transformation (Householder reflectors of the tridiagonal reduction,
+// then the block's row order) of the columns cols[t] = (block, column) of
+// vec, which hold tridiagonal-basis vectors.
+int syev_backtr(const int *dims, const int *ev_off, const int64_t *rho_off, const double *tau, const double *refl,
+                const int *perm, double *vec, const int2 *cols, int ncols, int nmax, cudaStream_t st);
+// Kept vectors of the flagged blocks in `blocks` (device list of nb) again,
+// by inverse iteration with Gram-Schmidt inside near clusters (k_vec_fb);
+// blocks it cannot do keep bit 1 of their flags.
+int syev_vec_fallback(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
+                      const int *dims, const int64_t *rho_off, const int *sub, const double *evals, const double *ldd,
+                      const double *ldl, const double *bscale, const double *bsig, const double *tau,
+                      const double *refl, const int *perm, int *flags, double *vec, const int *blocks, int nb,
+                      int nmax, cudaStream_t st);
 int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
              const int *dims, const int64_t *rho_off, const int *bmode, const int *sub, const double *evals,
              const double *ldd, const double *ldl, const double *bscale, const double *bsig, const double *tau,

@@ -10,6 +10,8 @@
 // vector), Gram-Schmidt against the vectors already found in the same
 // cluster.
 #include "host_tridiag.hpp"
+#include <vector>
+#include <limits>
 
 #include <algorithm>
 #include <cfloat>
@@ -325,6 +327,78 @@ bool arrow_lowest(double theta0, const double *m, const double *a, const double 
     for (int i = 0; i < k; ++i) c[i + 1] = -y[i] * inv;
     *lam = x;
     *resid = std::fabs(b_last * c[k]);
+    return true;
+}
+
+// Implicit QL with Wilkinson shifts for a symmetric tridiagonal matrix
+// (Bowdler, Martin, Reinsch and Wilkinson, "The QR and QL algorithms for
+// symmetric matrices", Numer. Math. 11 (1968)).  Work is O(n^2) for the
+// eigenvalues and O(n^3) for the accumulated rotations; each rotation
+// touches two contiguous columns of Z.
+bool tridiag_ql(int n, double *d, double *e, double *Z) {
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) Z[(size_t)j * n + i] = i == j ? 1.0 : 0.0;
+    if (n <= 1) return true;
+    std::vector<double> off(n, 0.0);
+    for (int i = 0; i + 1 < n; ++i) off[i] = e[i];
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (int l = 0; l < n; ++l) {
+        for (int iter = 0;; ++iter) {
+            int m = l;
+            for (; m + 1 < n; ++m) {                 // a negligible coupling splits the matrix at m
+                const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+                if (std::fabs(off[m]) <= eps * dd) break;
+            }
+            if (m == l) break;
+            if (iter == 60) return false;
+            // shift: the eigenvalue of the leading 2x2 block nearer d[l]
+            double g = (d[l + 1] - d[l]) / (2.0 * off[l]);
+            double r = std::hypot(g, 1.0);
+            g = d[m] - d[l] + off[l] / (g + std::copysign(r, g));
+            double s = 1.0, c = 1.0, p = 0.0;
+            int i = m - 1;
+            bool split = false;
+            for (; i >= l; --i) {                    // chase the bulge from m up to l
+                const double f = s * off[i], b = c * off[i];
+                r = std::hypot(f, g);
+                off[i + 1] = r;
+                if (r == 0.0) {                      // exact underflow: deflate and restart
+                    d[i + 1] -= p;
+                    off[m] = 0.0;
+                    split = true;
+                    break;
+                }
+                s = f / r;
+                c = g / r;
+                g = d[i + 1] - p;
+                r = (d[i] - g) * s + 2.0 * c * b;
+                p = s * r;
+                d[i + 1] = g + p;
+                g = c * r - b;
+                double *zi = Z + (size_t)i * n, *zj = Z + (size_t)(i + 1) * n;
+                for (int k = 0; k < n; ++k) {
+                    const double t = zj[k];
+                    zj[k] = s * zi[k] + c * t;
+                    zi[k] = c * zi[k] - s * t;
+                }
+            }
+            if (split) continue;
+            d[l] -= p;
+            off[l] = g;
+            off[m] = 0.0;
+        }
+    }
+    // ascending order, vectors along
+    std::vector<int> ord(n);
+    for (int j = 0; j < n; ++j) ord[j] = j;
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return d[x] < d[y]; });
+    std::vector<double> ds(n), Zs((size_t)n * n);
+    for (int j = 0; j < n; ++j) {
+        ds[j] = d[ord[j]];
+        std::copy(Z + (size_t)ord[j] * n, Z + (size_t)(ord[j] + 1) * n, Zs.begin() + (size_t)j * n);
+    }
+    std::copy(ds.begin(), ds.end(), d);
+    std::copy(Zs.begin(), Zs.end(), Z);
     return true;
 }
 

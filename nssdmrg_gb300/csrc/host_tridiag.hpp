@@ -39,4 +39,12 @@ void tridiag_lowest(const double *a, const double *b, int m, int ne, double b_la
 bool arrow_lowest(double theta0, const double *m, const double *a, const double *b, int k, double b_last,
                   double *lam, double *c, double *resid, std::vector<double> &work);
 
+// All eigenpairs of the symmetric tridiagonal matrix with diagonal d[0..n)
+// and off-diagonal e[0..n-1) (e[i] couples i and i+1): implicit QL
+// iterations with Wilkinson shifts, the rotations accumulated into Z
+// (column-major n x n, initialised to the identity here).  On return d
+// holds the eigenvalues ascending and column j of Z the eigenvector of
+// d[j].  Returns false if an eigenvalue takes more than 60 iterations.
+bool tridiag_ql(int n, double *d, double *e, double *Z);
+
 }  // namespace nss

@@ -17,6 +17,7 @@
 // The block eigensolve is cuSOLVER dsyevd, one call per block on the
 // context stream (a library call; the sector blocks are small, < 600).
 #include "device.cuh"
+#include "host_tridiag.hpp"
 
 #include <cstdlib>
 #include <cstring>
@@ -24,6 +25,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <functional>
 #include <map>
 #include <cfloat>
@@ -297,6 +299,8 @@ constexpr int JAC_DEFAULT = 32;
 // library's blocked solver (all SMs) instead of its batched one (one CTA
 // per matrix, seconds at these sizes)
 constexpr int LIB_WHOLE_GPU_N = 1024;
+constexpr int LIB_FALLBACK_WHOLE_N = 128;   // the same for the own path's flagged blocks
+constexpr int QL_HOST_MAX = 800;             // flagged blocks up to this size: host QL on their tridiagonal matrix
 
 int jacobi_max() {
     static const int v = [] {
@@ -800,7 +804,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     // in an N x N matrix whose extra diagonal lies below its spectrum), the
     // classes on side streams.
     auto lib_eigh = [&](const std::vector<int> &sm, const std::vector<int> &lg, bool write_evals,
-                        double *vec_out) -> int {
+                        double *vec_out, int whole_min) -> int {
         if (sm.empty() && lg.empty()) return NSS_OK;
         if ((rc = make_side_streams())) return rc;
         if (!r.params) {
@@ -829,7 +833,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             cl.list_off = (int64_t)lists.size();
             lists.insert(lists.end(), kv.second.begin(), kv.second.end());
             size_t wd = 0, wh = 0;
-            if (cl.N >= LIB_WHOLE_GPU_N) {
+            if (cl.N >= whole_min) {
                 // one matrix at a time through the blocked whole-GPU solver
                 int lw = 0;
                 if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N, r.rho,
@@ -873,7 +877,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
             k_pack<<<cl.batch, 256, 0, ss>>>(r.rho, d_rho_off, d_dims, d_list + cl.list_off, cl.N, A);
             cusolverDnSetStream(h, ss);
             cusolverStatus_t cs = CUSOLVER_STATUS_SUCCESS;
-            if (cl.N >= LIB_WHOLE_GPU_N) {
+            if (cl.N >= whole_min) {
                 for (int b = 0; b < cl.batch && cs == CUSOLVER_STATUS_SUCCESS; ++b)
                     cs = cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, cl.N,
                                           A + (int64_t)b * cl.N * cl.N, cl.N, W + (int64_t)b * cl.N, ws,
@@ -909,7 +913,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         return NSS_OK;
     };
     if (path.empty()) NSS_CUDA_TRY(c, cudaEventRecord(r.ph[2], st));
-    if ((rc = lib_eigh(small, large, true, r.vec))) {
+    if ((rc = lib_eigh(small, large, true, r.vec, LIB_WHOLE_GPU_N))) {
         cleanup();
         return rc;
     }
@@ -923,6 +927,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
     for (int d : dims) c.rdm_max_block = std::max(c.rdm_max_block, d);
     c.rdm_lib_blocks = (int)(small.size() + large.size());
     c.rdm_fallback_blocks = 0;
+    c.rdm_refined_blocks = 0;
     ++c.launches;
     k_clamp<<<8, 256, 0, st>>>(r.evals, eacc);
     ++c.launches;
@@ -983,18 +988,112 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         std::vector<int> hflags(nblk);
         NSS_CUDA_TRY(c, cudaMemcpyAsync(hflags.data(), flags, nblk * sizeof(int), cudaMemcpyDeviceToHost, st));
         NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
-        std::vector<int> fs, fl;
+        // flagged blocks: first inverse iteration with Gram-Schmidt in near
+        // clusters (k_vec_fb), then the library for what that cannot do
+        std::vector<int> fb_own;
+        // env NSS_RDM_REDO_ALL=1 sends every own-path block through k_vec_fb
+        // (to check that path against the others)
+        const char *redo = std::getenv("NSS_RDM_REDO_ALL");
+        if (redo && std::string(redo) == "1")
+            for (int q : path) hflags[q] |= 2;
         for (int q : path)
             if (hflags[q] & 2) {
-                (dims[q] <= jmax ? fs : fl).push_back(q);
+                fb_own.push_back(q);
                 for (int b = 0; b < 5; ++b)
                     if (hflags[q] & (4 << b)) ++c.rdm_fail_why[b];
+                hflags[q] &= 1;                      // keep only "no positive definite L D L^T"
             }
+        c.rdm_refined_blocks = (int)fb_own.size();
+        if (!fb_own.empty()) {
+            int *d_fo = nullptr;
+            NSS_CUDA_TRY(c, ctx_alloc(c, &d_fo, fb_own.size()));
+            temps.push_back(d_fo);
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(d_fo, fb_own.data(), fb_own.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(flags, hflags.data(), nblk * sizeof(int), cudaMemcpyHostToDevice, st));
+            ++c.launches;
+            const int e2 = syev_vec_fallback(r.order, rnk, msv, nl, nsb, d_ev_off, d_dims, d_rho_off, sub, r.evals, ldd,
+                                             ldl, bscale, bsig, tau, refl, perm, flags, r.vec, d_fo,
+                                             (int)fb_own.size(), maxn_path, st);
+            if (e2) {
+                cleanup();
+                c.err = std::string("nss_rdm: eigenvector launch failed: ") + cudaGetErrorString((cudaError_t)e2);
+                return NSS_ERR_CUDA;
+            }
+            NSS_CUDA_TRY(c, cudaMemcpyAsync(hflags.data(), flags, nblk * sizeof(int), cudaMemcpyDeviceToHost, st));
+            NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+        }
+        // still flagged: blocks of up to QL_HOST_MAX states get all
+        // eigenvectors of their tridiagonal matrix from implicit QL on the
+        // host, written into their vec slot and back-transformed on the
+        // device (cuSOLVER measured 0.9 s for a lone 305-state block); larger
+        // ones go to the library
+        std::vector<int> fs, fl, fq;
+        // env NSS_RDM_QL_ALL=1 sends every flagged block to host QL (to check
+        // that path; with NSS_RDM_REDO_ALL=1, every block)
+        const char *qla = std::getenv("NSS_RDM_QL_ALL");
+        const bool ql_all = qla && std::string(qla) == "1";
+        for (int q : fb_own)
+            if ((hflags[q] & 2) || ql_all) (dims[q] <= QL_HOST_MAX ? fq : (dims[q] <= jmax ? fs : fl)).push_back(q);
+        if (!fq.empty()) {
+            std::vector<int2> cols;
+            int qmax = 1;
+            for (int q : fq) {
+                const int nq = dims[q];
+                qmax = std::max(qmax, nq);
+                std::vector<double> d(nq), e(nq), Z((size_t)nq * nq, 0.0);
+                std::vector<int> sr(nq);
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(d.data(), td + ev_off[q], nq * sizeof(double), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(e.data(), te + ev_off[q], nq * sizeof(double), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(sr.data(), sub + ev_off[q], nq * sizeof(int), cudaMemcpyDeviceToHost, st));
+                NSS_CUDA_TRY(c, cudaStreamSynchronize(st));
+                // the own path's columns: the eigenvalues of each unreduced
+                // block [r0, r1) of T ascending in columns r0 .. r1-1, so QL
+                // runs on each of those blocks
+                bool ql_ok = true;
+                for (int r0 = 0; r0 < nq && ql_ok;) {
+                    const int r1 = sr[r0] >> 16, nb = r1 - r0;
+                    if ((sr[r0] & 0xffff) != r0 || r1 <= r0 || r1 > nq) { ql_ok = false; break; }
+                    std::vector<double> db(d.begin() + r0, d.begin() + r1), eb(nb, 0.0), Zb((size_t)nb * nb);
+                    for (int i = 0; i + 1 < nb; ++i) eb[i] = e[r0 + i];
+                    if (!tridiag_ql(nb, db.data(), eb.data(), Zb.data())) { ql_ok = false; break; }
+                    for (int j = 0; j < nb; ++j)
+                        std::copy(Zb.begin() + (size_t)j * nb, Zb.begin() + (size_t)(j + 1) * nb,
+                                  Z.begin() + (size_t)(r0 + j) * nq + r0);
+                    r0 = r1;
+                }
+                if (!ql_ok) {
+                    (nq <= jmax ? fs : fl).push_back(q);
+                    continue;
+                }
+                NSS_CUDA_TRY(c, cudaMemcpy(r.vec + rho_off[q], Z.data(), Z.size() * sizeof(double),
+                                           cudaMemcpyHostToDevice));
+                for (int col = 0; col < nq; ++col) cols.push_back(make_int2(q, col));
+            }
+            c.rdm_ql_blocks += (int)(fq.size());
+            if (!cols.empty()) {
+                int2 *d_cols = nullptr;
+                NSS_CUDA_TRY(c, ctx_alloc(c, &d_cols, cols.size()));
+                temps.push_back(d_cols);
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(d_cols, cols.data(), cols.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                                st));
+                ++c.launches;
+                const int e3 = syev_backtr(d_dims, d_ev_off, d_rho_off, tau, refl, perm, r.vec, d_cols, (int)cols.size(),
+                                           qmax, st);
+                if (e3) {
+                    cleanup();
+                    c.err = std::string("nss_rdm: back-transformation launch failed: ") +
+                            cudaGetErrorString((cudaError_t)e3);
+                    return NSS_ERR_CUDA;
+                }
+            }
+        }
         c.rdm_fallback_blocks = (int)(fs.size() + fl.size());
         if (c.rdm_fallback_blocks) {
             // library vectors into the blocks' rho slots (consumed by then),
             // then matched to the own path's eigenvalue order in r.vec
-            if ((rc = lib_eigh(fs, fl, false, r.rho))) {
+            // a handful of blocks: the whole-GPU solver from 128 states on
+            // (the batched one measured 3.1 s for a lone 356-state block)
+            if ((rc = lib_eigh(fs, fl, false, r.rho, LIB_FALLBACK_WHOLE_N))) {
                 cleanup();
                 return rc;
             }

@@ -1216,7 +1216,224 @@ __global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_gs(VecArgs a) {
     if (!ok && lane == 0) atomicOr(&a.flags[q], 2 | why);
 }
 
+// Flagged blocks (k_vec / k_vec_cl / k_vec_gs could not certify their kept
+// vectors, e.g. a relative cluster whose twisted vectors came out nearly
+// dependent): one warp per block recomputes every kept vector of the block
+// by inverse iteration with the stationary factorisation at its eigenvalue
+// from a pseudo-random start, with Gram-Schmidt inside every iteration
+// against the kept vectors before it in the same unreduced block whose
+// eigenvalues lie within FB_ORTOL of it (scaled units; the
+// reorthogonalisation rule of LAPACK's inverse-iteration routine), then
+// back-transforms the set.  Members of a cluster tighter than the
+// eigenvalues' own accuracy have no individual vectors: inverse iteration
+// from a random start then returns some vector of the cluster's subspace,
+// and Gram-Schmidt against the members before it leaves a remainder of
+// about sqrt(left / size) of it.  So a remainder down to FB_KEEP is kept:
+// two projections make it orthogonal to the others to eps whatever its
+// size, and a residual test on L D L^T then decides whether it is an
+// eigenvector; a smaller remainder is retried from another start.  A block
+// whose L D L^T is not positive definite, or whose vectors fail, keeps bit 1
+// of flags[q] for the library eigensolver.
+constexpr double FB_ORTOL = 1e-3;
+constexpr double FB_KEEP = 1e-3;
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_vec_fb(VecArgs a, const int *__restrict__ blocks, int nb,
+                                                            int nmax) {
+    extern __shared__ double vec_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int b = blockIdx.x * nw + warp;
+    if (b >= nb) return;
+    const int q = blocks[b];
+    const int side = q < a.side[1].o ? 0 : 1;
+    const int ms = a.side[side].ms;
+    const int n = a.dims[q], eo = a.ev_off[q];
+    if (n < 2) return;
+    double *X = a.vec + a.rho_off[q];
+    auto kept = [&](int c) { return a.rank[eo + c] < ms; };
+    if (a.flags[q] & 1) {                            // no positive definite root representation
+        if (lane == 0) atomicOr(&a.flags[q], 2);
+        return;
+    }
+    const VecScratch w = vec_scratch(vec_smem + (size_t)warp * 7 * nmax, nmax);
+    const double scale = a.bscale[q], sig0 = a.bsig[q];
+    auto lamS = [&](int c) { return a.evals[eo + c] * scale - sig0; };
+    for (int i = lane; i < n; i += 32) {
+        w.dD[i] = a.ldd[eo + i];
+        w.dL[i] = a.ldl[eo + i];
+    }
+    __syncwarp();
+    // z -= sum over earlier kept columns of the same unreduced block within
+    // FB_ORTOL of lam0 (tridiagonal basis), then normalised; returns |z|
+    auto reorth = [&](int c, int r0, double lam0) -> double {
+        for (int cp = c - 1; cp >= r0; --cp) {
+            if (!(lam0 - lamS(cp) < FB_ORTOL)) break;
+            if (!kept(cp)) continue;
+            const double *Y = X + (int64_t)cp * n;
+            double d = 0.0;
+            for (int i = lane; i < n; i += 32) d = fma(Y[i], w.z[i], d);
+            d = wsum(d);
+            for (int i = lane; i < n; i += 32) w.z[i] = fma(-d, Y[i], w.z[i]);
+            __syncwarp();
+        }
+        double nz = 0.0;
+        for (int i = lane; i < n; i += 32) nz = fma(w.z[i], w.z[i], nz);
+        nz = sqrt(wsum(nz));
+        if (nz > 0.0) {
+            const double inv = 1.0 / nz;
+            for (int i = lane; i < n; i += 32) w.z[i] *= inv;
+        }
+        __syncwarp();
+        return nz;
+    };
+    // number of eigenvalues of L D L^T (rows [r0, r1)) below sig: negative
+    // pivots of the stationary transform L D L^T - sig = L+ D+ L+^T, whose
+    // relative accuracy carries over to small eigenvalues (the bisection
+    // that found the eigenvalues counted on T, with absolute accuracy only)
+    auto ldl_count = [&](int r0, int r1, double sig) -> int {
+        double sv = -sig;
+        int cnt = 0;
+        for (int i = r0; i + 1 < r1; ++i) {
+            double dp = w.dD[i] + sv;
+            if (fabs(dp) < PIVMIN) dp = -PIVMIN;
+            cnt += dp < 0.0;
+            sv = w.dD[i] * w.dL[i] * rcp_nr(dp) * w.dL[i] * sv - sig;
+        }
+        double dp = w.dD[r1 - 1] + sv;
+        if (fabs(dp) < PIVMIN) dp = -PIVMIN;
+        return cnt + (dp < 0.0);
+    };
+    bool ok = true;
+    for (int c = 0; ok && c < n; ++c) {
+        if (!kept(c)) continue;
+        const int sr = a.sub[eo + c], r0 = sr & 0xffff, r1 = sr >> 16;
+        // the eigenvalue's index inside its unreduced block, refined to the
+        // relative accuracy of L D L^T by 32-way multisection on the counts
+        int idx = 0;
+        for (int cp = 0; cp < c; ++cp) idx += a.sub[eo + cp] == sr;
+        double lam0 = lamS(c);
+        {
+            double w0 = fmax(fabs(lam0) * 1e-6, 1e-30), lo = lam0 - w0, hi = lam0 + w0;
+            for (int grow = 0; grow < 100; ++grow) {     // bracket: count(lo) <= idx < count(hi)
+                const int cl = ldl_count(r0, r1, lo), ch = ldl_count(r0, r1, hi);
+                if (cl <= idx && ch > idx) break;
+                w0 *= 4.0;
+                if (cl > idx) lo = lam0 - w0;
+                if (ch <= idx) hi = lam0 + w0;
+            }
+            for (int round = 0; round < 12 && hi - lo > 4e-16 * fmax(fabs(lo), fabs(hi)); ++round) {
+                const double x = lo + (hi - lo) * (lane + 1) / 33.0;
+                const int below = ldl_count(r0, r1, x) > idx ? 1 : 0;
+                const unsigned m = __ballot_sync(0xffffffffu, below);
+                const int first = m ? __ffs(m) - 1 : 32;   // first lane whose shift lies above
+                const double nlo = first > 0 ? lo + (hi - lo) * first / 33.0 : lo;
+                const double nhi = first < 32 ? lo + (hi - lo) * (first + 1) / 33.0 : hi;
+                lo = nlo;
+                hi = nhi;
+            }
+            lam0 = 0.5 * (lo + hi);
+        }
+        if (lane == 0) dstqds_lane0(w, r0, r1, lam0, w.pp);
+        __syncwarp();
+        double nz = 0.0;
+        for (int attempt = 0; attempt < 3 && !(nz >= FB_KEEP); ++attempt) {
+        for (int i = lane; i < n; i += 32) {
+            unsigned hsh = (unsigned)(i + 1) * 2654435761u ^ (unsigned)(c + 7 + 7919 * attempt) * 40503u;
+            hsh ^= hsh >> 15;
+            hsh *= 2246822519u;
+            hsh ^= hsh >> 13;
+            w.z[i] = (i >= r0 && i < r1) ? ((double)(hsh & 0xffffu) / 32768.0 - 1.0) : 0.0;
+        }
+        __syncwarp();
+        reorth(c, r0, lam0);
+        nz = 0.0;
+        for (int it = 0; it < 3; ++it) {
+            if (lane == 0) {                         // L+ w = x
+                for (int i = r0; i + 1 < r1; ++i) w.z[i + 1] -= w.lp[i] * w.z[i];
+            }
+            __syncwarp();
+            for (int i = r0 + lane; i < r1; i += 32) w.z[i] *= rcp_nr(w.pp[i]);   // D+^-1
+            __syncwarp();
+            if (lane == 0) {                         // L+^T y = w
+                for (int i = r1 - 2; i >= r0; --i) w.z[i] -= w.lp[i] * w.z[i + 1];
+            }
+            __syncwarp();
+            double t2 = 0.0;
+            for (int i = lane; i < n; i += 32) t2 = fma(w.z[i], w.z[i], t2);
+            const double gz = sqrt(wsum(t2));
+            if (!(gz > 0.0) || !isfinite(gz)) break;
+            for (int i = lane; i < n; i += 32) w.z[i] *= 1.0 / gz;
+            __syncwarp();
+            nz = reorth(c, r0, lam0);
+        }
+        }
+        if (!(nz >= FB_KEEP)) ok = false;
+        else if (nz < 0.5) nz = reorth(c, r0, lam0);   // a second projection for a small remainder
+        if (ok) {
+            // residual ||L D L^T z - lam0 z|| (scaled units, ~1 the norm of
+            // the block): a vector that did not settle goes to the library
+            for (int i = r0 + lane; i < r1; i += 32)
+                w.um[i] = w.dD[i] * (w.z[i] + (i + 1 < r1 ? w.dL[i] * w.z[i + 1] : 0.0));
+            __syncwarp();
+            double rr = 0.0;
+            for (int i = r0 + lane; i < r1; i += 32) {
+                const double y = w.um[i] + (i > r0 ? w.dL[i - 1] * w.um[i - 1] : 0.0) - lam0 * w.z[i];
+                rr = fma(y, y, rr);
+            }
+            rr = wsum(rr);
+            __syncwarp();
+            if (!(sqrt(rr) <= 1e-11)) ok = false;
+        }
+        double *Xc = X + (int64_t)c * n;             // tridiagonal basis until the set is complete
+        for (int i = lane; i < n; i += 32) Xc[i] = w.z[i];
+        __syncwarp();
+    }
+    for (int c = 0; ok && c < n; ++c) {
+        if (!kept(c)) continue;
+        double *Xc = X + (int64_t)c * n;
+        for (int i = lane; i < n; i += 32) w.z[i] = Xc[i];
+        __syncwarp();
+        back_transform_store(a, q, n, eo, w.z, Xc, lane);
+    }
+    if (!ok && lane == 0) atomicOr(&a.flags[q], 2 | 32);
+}
+
+// Kept columns of the blocks in `blocks`, already in their tridiagonal
+// basis in vec (the host QL fallback puts them there): back-transformed in
+// place, one warp per column.
+__global__ void __launch_bounds__(VEC_WARPS * 32) k_backtr(VecArgs a, const int2 *__restrict__ cols, int ncols,
+                                                            int nmax) {
+    extern __shared__ double vec_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int t = blockIdx.x * nw + warp;
+    if (t >= ncols) return;
+    const int q = cols[t].x, c = cols[t].y;
+    const int n = a.dims[q], eo = a.ev_off[q];
+    double *z = vec_smem + (size_t)warp * nmax;
+    double *Xc = a.vec + a.rho_off[q] + (int64_t)c * n;
+    for (int i = lane; i < n; i += 32) z[i] = Xc[i];
+    __syncwarp();
+    back_transform_store(a, q, n, eo, z, Xc, lane);
+}
+
 }  // namespace
+
+int syev_backtr(const int *dims, const int *ev_off, const int64_t *rho_off, const double *tau, const double *refl,
+                const int *perm, double *vec, const int2 *cols, int ncols, int nmax, cudaStream_t st) {
+    if (ncols <= 0) return 0;
+    VecArgs a{};
+    a.dims = dims;
+    a.ev_off = ev_off;
+    a.rho_off = rho_off;
+    a.tau = tau;
+    a.refl = refl;
+    a.perm = perm;
+    a.vec = vec;
+    const int nw = VEC_WARPS;
+    const size_t smem = (size_t)nw * nmax * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_backtr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    k_backtr<<<(ncols + nw - 1) / nw, nw * 32, smem, st>>>(a, cols, ncols, nmax);
+    return (int)cudaGetLastError();
+}
 
 int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,
              int nblocks, int maxn, double *refl, double *td, double *te, double *tau, int *perm, cudaStream_t st) {
@@ -1408,6 +1625,39 @@ int syev_vec(const int *order, const int *rank, const int ms[2], int nl, int nsb
     if (e != cudaSuccess) return (int)e;
     k_vec_cl<<<(tot + nw - 1) / nw, nw * 32, nw * per_warp, st>>>(a, nmax);
     k_vec_gs<<<(tot + VEC_WARPS - 1) / VEC_WARPS, VEC_WARPS * 32, 0, st>>>(a);
+    return (int)cudaGetLastError();
+}
+
+int syev_vec_fallback(const int *order, const int *rank, const int ms[2], int nl, int nsb, const int *ev_off,
+                      const int *dims, const int64_t *rho_off, const int *sub, const double *evals, const double *ldd,
+                      const double *ldl, const double *bscale, const double *bsig, const double *tau,
+                      const double *refl, const int *perm, int *flags, double *vec, const int *blocks, int nb,
+                      int nmax, cudaStream_t st) {
+    if (nb <= 0) return 0;
+    VecArgs a{};
+    a.side[0] = VecSide{order, 0, ms[0], 0};
+    a.side[1] = VecSide{order + nl, nl, ms[1], nsb};
+    a.nsb = nsb;
+    a.rank = rank;
+    a.ev_off = ev_off;
+    a.dims = dims;
+    a.sub = sub;
+    a.perm = perm;
+    a.rho_off = rho_off;
+    a.evals = evals;
+    a.ldd = ldd;
+    a.ldl = ldl;
+    a.bscale = bscale;
+    a.bsig = bsig;
+    a.tau = tau;
+    a.refl = refl;
+    a.flags = flags;
+    a.vec = vec;
+    const int per_warp = 7 * nmax * (int)sizeof(double);
+    const int nw = std::max(1, std::min(VEC_WARPS, (200 * 1024) / per_warp));
+    cudaError_t e = cudaFuncSetAttribute(k_vec_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, nw * per_warp);
+    if (e != cudaSuccess) return (int)e;
+    k_vec_fb<<<(nb + nw - 1) / nw, nw * 32, nw * per_warp, st>>>(a, blocks, nb, nmax);
     return (int)cudaGetLastError();
 }
 

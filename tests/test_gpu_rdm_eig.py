@@ -216,3 +216,29 @@ def test_big_blocks_through_blocked_reduction(nss, cluster_mem):
     drs = np.array([desc.drs[k] for k in range(desc.nsb)])
     off = np.array([desc.offset[k] for k in range(desc.nsb)])
     _check_against(own, lib, _blocks_of(psi, dls, drs, off))
+
+
+@pytest.mark.parametrize("mode", ["inverse_iteration", "host_ql"])
+@pytest.mark.parametrize("name", ["kat_hubbard.npz", "c2_small.npz"])
+def test_flagged_block_paths_match_library(nss, name, mode):
+    """The in-house fallbacks for flagged blocks, forced onto every block:
+    inverse iteration with Gram-Schmidt inside near clusters (k_vec_fb,
+    NSS_RDM_REDO_ALL=1), and implicit QL of the block's tridiagonal matrix on
+    the host with the device back-transformation (NSS_RDM_QL_ALL=1), against
+    the library path on the same blocks."""
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    mst = int(z["params"][1]) if "params" in z else 128
+    os.environ["NSS_RDM_REDO_ALL"] = "1"
+    if mode == "host_ql":
+        os.environ["NSS_RDM_QL_ALL"] = "1"
+    try:
+        own, st_own = _rdm(s, mst, z["psi"], library=False)
+    finally:
+        os.environ.pop("NSS_RDM_REDO_ALL", None)
+        os.environ.pop("NSS_RDM_QL_ALL", None)
+    lib, _ = _rdm(s, mst, z["psi"], library=True)
+    assert st_own[2] == 0, st_own           # none left to the library
+    _check_against(own, lib, _blocks_of(z["psi"], z["sb_dls"], z["sb_drs"], z["sb_offset"]))
