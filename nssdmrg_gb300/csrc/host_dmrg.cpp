@@ -139,7 +139,7 @@ Block enlarge_block(const Block &blk, const Block &dot, char label, const double
     const Csr id_m = csr_identity(m), id_d = csr_identity(d);
     std::vector<KronTerm> terms;
     const unsigned hw = std::thread::hardware_concurrency();
-    const int nth = (int)std::max(1u, std::min(4u, hw / 2));
+    const int nth = blk.op("H").nnz() > 20000 ? (int)std::max(1u, std::min(4u, hw / 2)) : 1;
     if (label == 'l') {
         terms.push_back({&blk.op("H"), &id_d, 1.0});
         terms.push_back({&id_m, &dot.op("H"), 1.0});
@@ -252,7 +252,8 @@ int Driver::step(int type, int label, int sweep) {
     auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
     // the two enlargements are independent
     run_pair([&] { left = enlarge_block(left, dot, 'l', hij); },
-             [&] { right = enlarge_block(right, dot, 'r', hij); });
+             [&] { right = enlarge_block(right, dot, 'r', hij); },
+             (int64_t)left.op("H").nnz() + right.op("H").nnz() > 20000);
     const double ms_enlarge = ms_since(t_step);
     const int current_l = left.length + right.length;
     // sb_set_current_qn, QNtype local: int(target_qn * L * Norb), truncated
@@ -491,9 +492,18 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             for (int s2 = 0; s2 < 2; ++s2)
                 for (int j = 0; j < kl[s2].ms; ++j) rec.nnz_u += kl[s2].dims[kl[s2].q[j]];
         } else {
-            const Csr cul = u_to_csr(u_l, sb.m_left, side[0].m_s), cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
-            renormalize(left, cul, ql);
-            renormalize(right, cur, qr);
+            Csr cul, cur;
+            // the two blocks are independent (a thread pays off from ~10^4 entries)
+            run_pair(
+                [&] {
+                    cul = u_to_csr(u_l, sb.m_left, side[0].m_s);
+                    renormalize(left, cul, ql);
+                },
+                [&] {
+                    cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
+                    renormalize(right, cur, qr);
+                },
+                (int64_t)sb.m_left * side[0].m_s + (int64_t)sb.m_right * side[1].m_s > 8000);
             rec.nnz_u = cul.nnz() + cur.nnz();
             if (p.save_umat) {
                 left.omats.push_back(std::make_shared<const Csr>(cul));

@@ -57,7 +57,8 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
     sb.hleft.resize(nsb);
     sb.hright.resize(nsb);
     run_pair([&] { for (int k = 0; k < nsb; ++k) sb.hleft[k] = csr_filter(hl, sb.ai[k], sb.ai[k]); },
-             [&] { for (int k = 0; k < nsb; ++k) sb.hright[k] = csr_filter(hr, sb.bi[k], sb.bi[k]); });
+             [&] { for (int k = 0; k < nsb; ++k) sb.hright[k] = csr_filter(hr, sb.bi[k], sb.bi[k]); },
+             hl.nnz() + hr.nnz() > 40000);
 
     auto set_term = [&](int it, int k, int jsb, int hc, Csr a, Csr b, int64_t ro, int64_t co) {
         int idx = it + sb.tnso * k;

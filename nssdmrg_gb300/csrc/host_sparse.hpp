@@ -19,9 +19,15 @@ namespace nss {
 
 // f0 on the calling thread and f1 on a second one (the two sides of a DMRG
 // step are independent); an exception of either is rethrown after both
-// have finished, f0's first.
+// have finished, f0's first.  With parallel false (work too small to pay
+// for a thread, ~20 us) both run here, f0 first.
 template <class F0, class F1>
-void run_pair(F0 &&f0, F1 &&f1) {
+void run_pair(F0 &&f0, F1 &&f1, bool parallel = true) {
+    if (!parallel) {
+        f0();
+        f1();
+        return;
+    }
     std::exception_ptr e0, e1;
     std::thread th([&] {
         try {

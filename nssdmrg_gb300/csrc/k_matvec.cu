@@ -135,7 +135,7 @@ int stage_commit(Ctx &c, Stager &sg) {
             if (sg.items[i].bytes && sg.items[i].src)
                 std::memcpy(c.sb_stage + sg.items[i].off, sg.items[i].src, sg.items[i].bytes);
     };
-    run_pair([&] { fill(0, half); }, [&] { fill(half, sg.items.size()); });
+    run_pair([&] { fill(0, half); }, [&] { fill(half, sg.items.size()); }, sg.total > ((size_t)4 << 20));
     NSS_CUDA_TRY(c, cudaMemcpyAsync(c.sb_arena, c.sb_stage, sg.total, cudaMemcpyHostToDevice, c.stream));
     for (const auto &it : sg.items) {
         *it.dst = (void *)(c.sb_arena + it.off);
@@ -239,6 +239,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
         std::vector<double> val;
         std::vector<int64_t> row_first;
     } pk[2];
+    const bool big_pool = nnz_l + nnz_r > 100000;
     run_pair(
         [&] {
             for (int side = 0; side < 2; ++side) {
@@ -276,7 +277,8 @@ int sb_upload(Ctx &c, const nss_sb_desc *d) {
                     at += nz;
                 }
             }
-        });
+        },
+        big_pool);
 
     // A x B terms, regrouped by output sector
     std::vector<std::vector<DevTerm>> by_out(s.nsb);
