@@ -40,6 +40,17 @@ __global__ void __launch_bounds__(128) k_gather_u(const double *__restrict__ com
     for (int p = threadIdx.x; p < len[j]; p += blockDim.x) d[p] = s[p];
 }
 
+// The operators' nonzero entries into their zeroed dense block pairs:
+// (position in the O buffer, value) pairs from the host.
+struct RnEntry {
+    int64_t at;
+    double val;
+};
+__global__ void __launch_bounds__(256) k_rn_scatter(const RnEntry *__restrict__ e, int64_t n, double *__restrict__ o) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        o[e[i].at] = e[i].val;
+}
+
 // One product C (m x n, column-major, ldc) = op(A) B, B column-major k x n
 // (ldb); op(A) = A (m x k, lda) or A^T (A stored k x m, lda).  Its 64 x 64
 // output tiles are blocks tile0 .. tile0 + tiles_m * ceil(n/64) - 1.
@@ -155,6 +166,7 @@ struct Side {
     std::vector<Pair> pairs;
     std::vector<std::vector<int>> pidx;   // [op][qr * nb + qc] -> pair or -1
     int64_t o_tot = 0, t_tot = 0, r_tot = 0, u_tot = 0;
+    int64_t nent = 0;                     // operator entries inside kept block pairs
 };
 
 // kept columns per block, state maps and the nonzero block pairs of every
@@ -192,6 +204,7 @@ void scan_side(Side &s) {
                 const int cc = m.col[e];
                 const int qc = cc < mblock ? s.bof[cc] : -1;
                 if (qc < 0 || !s.kq[qc]) continue;
+                ++s.nent;
                 const int key = qr * nb + qc;
                 if (s.pidx[io][key] >= 0) continue;
                 s.pidx[io][key] = (int)s.pairs.size();
@@ -204,13 +217,14 @@ void scan_side(Side &s) {
     }
 }
 
-// dense blocks of the operators (column-major n_qr x n_qc) into hblk, the
-// side's share of the staging buffer
-void extract_side(const Side &s, double *hblk) {
+// the operators' entries inside kept block pairs as (position in the
+// column-major n_qr x n_qc block of their pair, offset by ob, value) into
+// ent, the side's share of the staging buffer; the device scatters them
+void extract_side(const Side &s, RnEntry *ent, int64_t ob) {
     const KeptLayout &kl = *s.kl;
     const Block &blk = *s.blk;
     const int nb = s.nb, mblock = blk.dim;
-    std::memset(hblk, 0, (size_t)s.o_tot * sizeof(double));
+    int64_t at = 0;
     for (size_t io = 0; io < blk.ops.size(); ++io) {
         const Csr &m = blk.ops[io].m;
         const std::vector<int> &pi = s.pidx[io];
@@ -223,7 +237,7 @@ void extract_side(const Side &s, double *hblk) {
                 const int qc = cc < mblock ? s.bof[cc] : -1;
                 if (qc < 0 || !s.kq[qc]) continue;
                 const Pair &pr = s.pairs[pi[qr * nb + qc]];
-                hblk[pr.o_off + (int64_t)s.lof[cc] * kl.dims[qr] + rowbase] = m.val[e];
+                ent[at++] = RnEntry{ob + pr.o_off + (int64_t)s.lof[cc] * kl.dims[qr] + rowbase, m.val[e]};
             }
         }
     }
@@ -302,16 +316,27 @@ int renorm_device(Ctx &c, const KeptLayout kl[2], Block *blk[2], const std::vect
     const int ms_tot = sd[0].ms + sd[1].ms;
     const int npairs = (int)(sd[0].pairs.size() + sd[1].pairs.size());
     int rc;
-    if ((rc = grow_host(c, &w.hblk, w.cap_hblk, o_tot))) return rc;
+    const int64_t nent = sd[0].nent + sd[1].nent;
+    if ((rc = grow_host(c, &w.hblk, w.cap_hblk, 2 * nent))) return rc;   // RnEntry = two doubles
     if ((rc = grow_host(c, &w.hres, w.cap_hres, r_tot))) return rc;
     if ((rc = grow_dev(c, &w.dblk, w.cap_dblk, o_tot))) return rc;
-    if ((rc = grow_dev(c, &w.tbuf, w.cap_tbuf, t_tot))) return rc;
     if ((rc = grow_dev(c, &w.rbuf, w.cap_rbuf, r_tot))) return rc;
     if ((rc = grow_dev(c, &w.ublk, w.cap_ublk, u_tot))) return rc;
-    run_pair([&] { extract_side(sd[0], w.hblk); }, [&] { extract_side(sd[1], w.hblk + sd[0].o_tot); });
+    RnEntry *hent = (RnEntry *)w.hblk;
+    run_pair([&] { extract_side(sd[0], hent, 0); }, [&] { extract_side(sd[1], hent + sd[0].nent, sd[0].o_tot); });
     c.renorm_phase_ms[0] += ms_since(t0);
     const auto t1 = clk::now();
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(w.dblk, w.hblk, (size_t)o_tot * sizeof(double), cudaMemcpyHostToDevice, st));
+    // the entries go to the device as pairs and land in the zeroed blocks
+    // there (the T buffer holds them until the first product overwrites it)
+    if ((rc = grow_dev(c, &w.tbuf, w.cap_tbuf, std::max<int64_t>(t_tot, 2 * nent)))) return rc;
+    NSS_CUDA_TRY(c, cudaMemsetAsync(w.dblk, 0, (size_t)o_tot * sizeof(double), st));
+    if (nent > 0) {
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(w.tbuf, w.hblk, (size_t)nent * sizeof(RnEntry), cudaMemcpyHostToDevice, st));
+        ++c.launches;
+        k_rn_scatter<<<(unsigned)std::min<int64_t>((nent + 255) / 256, 4 * 152), 256, 0, st>>>(
+            (const RnEntry *)w.tbuf, nent, w.dblk);
+        NSS_CUDA_TRY(c, cudaGetLastError());
+    }
     // product jobs of both sides: pass 0 T = O U_qc, pass 1 R = U_qr^T T
     int ntiles[2] = {0, 0};
     std::vector<RnJob> jobs[2];
