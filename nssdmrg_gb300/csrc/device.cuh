@@ -211,6 +211,7 @@ struct Ctx {
     size_t sb_arena_cap = 0, sb_stage_cap = 0;
     double renorm_phase_ms[3] = {0, 0, 0};
     int refine_passes = 0, refine_cluster = 0;   // mixed refinement of the last solve
+    bool last_pair = false;                      // ... needed a near-degenerate partner
     int rdm_refined_blocks = 0;                  // flagged blocks redone by k_vec_fb in the last nss_rdm
     int rdm_ql_blocks = 0;                       // ... and of those, blocks finished by host QL
     int64_t mixed_fallbacks = 0;                 // mixed solves redone in FP64 (context life)

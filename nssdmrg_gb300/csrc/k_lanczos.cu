@@ -1883,8 +1883,12 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     if (!mixed) {
         rc = run_lanczos<double>(c, z.V, z.w, neigen, mmax, tol, seed, &numop_, &m_done);
     } else {
-        rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done,
-                                nullptr, std::min(4, neigen + 2), &kcl);
+        // after a solve that needed a near-degenerate partner (consecutive
+        // DMRG steps have alike spectra) the FP32 phase also converges the
+        // next Ritz pair, so that the pair is resolved when it stops
+        const int want32 = std::min(4, neigen + (c.last_pair ? 1 : 0));
+        rc = run_lanczos<float>(c, z.V32, z.w32, want32, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done,
+                                nullptr, std::min(4, want32 + 2), &kcl);
     }
     const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
     if (!rc && mixed) {
@@ -1978,6 +1982,8 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         // FP64 Rayleigh-Ritz on the k cluster vectors: orthonormalise them,
         // W = H U (into the FP64 scratch), G = U^T W, U <- U Q with G's
         // eigenvectors Q in ascending order
+        double rr_lam[4] = {0, 0, 0, 0};
+        int rr_k = 0;                                // cluster size of the last Rayleigh-Ritz step
         auto rayleigh_ritz = [&](int k) -> int {
             ++c.launches;
             normalize_dev<double>(z, z.evecs, n, st, c.launches);
@@ -2000,6 +2006,8 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             for (int i = 0; i < k; ++i)
                 for (int j = 0; j < k; ++j) a[i * k + j] = 0.5 * (g[i * k + j] + g[j * k + i]);
             sym_eig_small(k, a, lam, q);
+            for (int e = 0; e < k; ++e) rr_lam[e] = lam[e];
+            rr_k = k;
             Rot4 R{};
             for (int i = 0; i < k; ++i)
                 for (int j = 0; j < k; ++j) R.q[j * 4 + i] = q[j * k + i];
@@ -2057,6 +2065,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         }
         c.refine_passes = passes;
         c.refine_cluster = k;
+        c.last_pair = rr_k > ne && rr_lam[ne] - rr_lam[ne - 1] <= CLUSTER_GAP * std::fabs(rr_lam[0]);
         if (!rc && done) {
             for (int e = 0; e < ne; ++e) z.last_resid[e] = res[e];
             NSS_CUDA_TRY(c, cudaMemcpyAsync(z.theta, th, ne * sizeof(double), cudaMemcpyHostToDevice, st));
