@@ -1933,6 +1933,9 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         // FP64 check of wanted vector e (deflated against the ones before it
         // and normalised): th[e] = u.H.u, res[e] = ||H u - th u||; leaves
         // r = H u - th u in z.w (deflated for e > 0) and its norm in *beta0
+        double rr_lam[4] = {0, 0, 0, 0};
+        int rr_k = 0;                                // cluster size of the last Rayleigh-Ritz step
+        bool rr_fresh = false;                       // rrw holds H U of the current U
         auto check = [&](int e, double *beta0) -> int {
             double *u = z.evecs + (int64_t)e * n;
             if (e > 0) {
@@ -1940,8 +1943,14 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
                 ++c.launches;
                 normalize_dev<double>(z, u, n, st, c.launches);
             }
-            if (int rc2 = hv_device(c, u, z.w)) return rc2;
-            ++numop_;
+            if (e == 0 && rr_fresh) {
+                // right after a Rayleigh-Ritz step H u_0 is known
+                NSS_CUDA_TRY(c, cudaMemcpyAsync(z.w, z.rrw, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            } else {
+                if (int rc2 = hv_device(c, u, z.w)) return rc2;
+                ++numop_;
+            }
+            rr_fresh = false;
             c.launches += 2;
             k_rq<<<NBLK, 256, 0, st>>>(u, z.w, n, z.part, r, z.counter);
             k_anchor_r<<<NBLK, 256, 0, st>>>(u, z.w, n, z.part, r, z.counter);
@@ -1982,8 +1991,6 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         // FP64 Rayleigh-Ritz on the k cluster vectors: orthonormalise them,
         // W = H U (into the FP64 scratch), G = U^T W, U <- U Q with G's
         // eigenvectors Q in ascending order
-        double rr_lam[4] = {0, 0, 0, 0};
-        int rr_k = 0;                                // cluster size of the last Rayleigh-Ritz step
         auto rayleigh_ritz = [&](int k) -> int {
             ++c.launches;
             normalize_dev<double>(z, z.evecs, n, st, c.launches);
@@ -2011,9 +2018,11 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
             Rot4 R{};
             for (int i = 0; i < k; ++i)
                 for (int j = 0; j < k; ++j) R.q[j * 4 + i] = q[j * k + i];
-            ++c.launches;
+            c.launches += 2;
             k_rot<<<608, 256, 0, st>>>(z.evecs, k, n, R);
+            k_rot<<<608, 256, 0, st>>>(z.rrw, k, n, R);   // H U along, for the next check
             NSS_CUDA_TRY(c, cudaGetLastError());
+            rr_fresh = true;
             return NSS_OK;
         };
         // k: the cluster (wanted vectors and partners); the passes
