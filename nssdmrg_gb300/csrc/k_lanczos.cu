@@ -1889,6 +1889,13 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         const int want32 = std::min(4, neigen + (c.last_pair ? 1 : 0));
         rc = run_lanczos<float>(c, z.V32, z.w32, want32, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done,
                                 nullptr, std::min(4, want32 + 2), &kcl);
+        if (rc == NSS_ERR_NOCONV && want32 > neigen) {
+            // the extra pair did not converge within nitermax: the wanted ones alone
+            int it0 = numop_;
+            rc = run_lanczos<float>(c, z.V32, z.w32, neigen, mmax, std::max(tol, mixed_tol()), seed, &numop_, &m_done,
+                                    nullptr, std::min(4, neigen + 2), &kcl);
+            numop_ += it0;
+        }
     }
     const int ne = (int)std::min<int64_t>(neigen, std::max(m_done, 1));
     if (!rc && mixed) {
