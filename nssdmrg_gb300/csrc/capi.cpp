@@ -492,7 +492,7 @@ int nss_sb_setup(nss_ctx *ctx, int site_type, const nss_block_desc *left, const 
         auto sb = std::make_unique<nss::SbHost>(nss::sb_build(l, r, t, hij));
         nss::SbView v;
         nss::sb_view(*sb, v);
-        int rc = nss::sb_upload(ctx->c, &v.desc);
+        int rc = nss::sb_upload(ctx->c, &v.desc, true);
         if (rc) return rc;
         ctx->sbhost = std::move(sb);
         return NSS_OK;

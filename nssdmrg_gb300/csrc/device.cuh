@@ -235,7 +235,9 @@ cudaError_t ctx_alloc(Ctx &c, T **p, size_t count) {
 void ctx_free(Ctx &c, void *p);
 
 // k_matvec.cu
-int sb_upload(Ctx &c, const nss_sb_desc *d);
+// trusted: the descriptor comes from this library's own setup (its column
+// indices are not re-checked entry by entry)
+int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted = false);
 // Drop the pool; free_arena also returns its device arena and pinned
 // staging buffer (otherwise kept for the next upload).
 void sb_release(Ctx &c, bool free_arena);

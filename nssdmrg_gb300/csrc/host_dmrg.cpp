@@ -276,7 +276,7 @@ int Driver::step(int type, int label, int sweep) {
         last_sb = std::make_shared<SbHost>(std::move(sb));
         SbView v;
         sb_view(*last_sb, v);
-        int rc = sb_upload(*ctx, &v.desc);
+        int rc = sb_upload(*ctx, &v.desc, true);
         stopped = true;
         return rc;
     }
@@ -402,7 +402,7 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     const auto t_up = std::chrono::steady_clock::now();
     SbView v;
     sb_view(sb, v);
-    int rc = sb_upload(c, &v.desc);
+    int rc = sb_upload(c, &v.desc, true);
     if (rc) return rc;
     rec.host_phase_ms[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_up).count();
     const int64_t n = sb.n();

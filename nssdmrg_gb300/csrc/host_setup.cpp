@@ -31,6 +31,14 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
     // order, each with its matching right sector target - q; inside a sector
     // the left state is the slow index.
     int64_t pos = 0;
+    {
+        int64_t tot = 0;
+        for (size_t ql = 0; ql < lsec.qns.size(); ++ql) {
+            const int rk = rsec.find(qn_sub(target, lsec.qns[ql]));
+            if (rk >= 0) tot += (int64_t)lsec.maps[ql].size() * rsec.maps[rk].size();
+        }
+        sb.sb_states.reserve((size_t)tot);
+    }
     for (size_t ql = 0; ql < lsec.qns.size(); ++ql) {
         const Qn rq = qn_sub(target, lsec.qns[ql]);
         int rk = rsec.find(rq);
