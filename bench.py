@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -85,7 +86,10 @@ class Clocks:
         self.device = device
         self.enabled = enabled
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        # the samples go next to the run's other outputs when NSS_CLOCKS_DIR
+        # names a folder, else to the system's temporary folder
+        out_dir = os.environ.get("NSS_CLOCKS_DIR")
+        self.path = Path(out_dir or tempfile.gettempdir()) / f"clocks_bench_{os.getpid()}.csv"
 
     def __enter__(self):
         if not self.enabled:
