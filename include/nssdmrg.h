@@ -263,6 +263,12 @@ int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b
  * precision runs after its FP32 phase (no counterpart in the reference,
  * whose Lanczos is FP64 throughout).  Outputs *lam, c[k+1] (unit norm,
  * c[0] > 0) and *resid = |b_last * c[k]|.  Needs no context and no GPU. */
+/* All eigenpairs of the symmetric tridiagonal matrix (diagonal d[n],
+ * off-diagonal e[n-1]) by implicit QL with Wilkinson shifts: evals[n]
+ * ascending, Z[n*n] column-major with column j the eigenvector of evals[j].
+ * The host solver the RDM uses for flagged rho blocks (their tridiagonal
+ * matrices after the device reduction); needs no context and no GPU. */
+int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, double *Z);
 int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, const double *b, double b_last,
                      double *lam, double *c, double *resid);
 

@@ -126,6 +126,7 @@ def lib():
         "nss_sb_energy_noalloc": (C.c_int, [P, I64, P, C.POINTER(D)]),
         "nss_tridiag_lowest": (C.c_int, [C.c_int, P, P, C.c_int, D, P, P, P]),
         "nss_arrow_lowest": (C.c_int, [C.c_int, D, P, P, P, D, C.POINTER(D), P, C.POINTER(D)]),
+        "nss_tridiag_eig": (C.c_int, [C.c_int, P, P, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
@@ -187,6 +188,20 @@ def tridiag_lowest(a, b, ne: int = 1, b_last: float = 0.0):
     if rc != 0:
         raise NssError(rc, lib().nss_last_error(None).decode())
     return theta, s, resid
+
+
+def tridiag_eig(d, e):
+    """All eigenpairs of a symmetric tridiagonal matrix (host implicit QL):
+    (evals ascending, Z with Z[:, j] the eigenvector of evals[j])."""
+    d = np.ascontiguousarray(d, np.float64)
+    e = np.ascontiguousarray(e, np.float64)
+    n = d.size
+    ev = np.empty(n)
+    Z = np.empty((n, n))   # filled column-major: Z.T[j] is column j
+    rc = lib().nss_tridiag_eig(n, _ptr(d), _ptr(e) if n > 1 else None, _ptr(ev), _ptr(Z))
+    if rc:
+        raise NssError(rc, lib().nss_last_error(None).decode())
+    return ev, Z.T.copy()
 
 
 def arrow_lowest(theta0: float, m, a, b, b_last: float = 0.0):

@@ -197,6 +197,21 @@ int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b
     return NSS_OK;
 }
 
+int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, double *Z) {
+    if (n <= 0 || !d || (n > 1 && !e) || !evals || !Z) {
+        g_err = "nss_tridiag_eig: need n > 0 and non-NULL arrays";
+        return NSS_ERR_INVALID;
+    }
+    std::vector<double> dd(d, d + n), ee(n, 0.0);
+    for (int i = 0; i + 1 < n; ++i) ee[i] = e[i];
+    if (!nss::tridiag_ql(n, dd.data(), ee.data(), Z)) {
+        g_err = "nss_tridiag_eig: an eigenvalue did not converge in 60 QL iterations";
+        return NSS_ERR_NOCONV;
+    }
+    std::copy(dd.begin(), dd.end(), evals);
+    return NSS_OK;
+}
+
 int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, const double *b, double b_last,
                      double *lam, double *c, double *resid) {
     if (k < 0 || (k > 0 && (!m || !a || (k > 1 && !b))) || !lam || !c || !resid) {
