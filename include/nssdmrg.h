@@ -392,6 +392,11 @@ int       nss_dmrg_nrecords(const nss_dmrg *d);
  * A loaded block must match the driver's model (site type, QN length and
  * operator keys). */
 int       nss_dmrg_save_blocks(nss_dmrg *d, const char *left_path, const char *right_path);
+/* Read one restart file and write it back in the current layout (operator
+ * names with the link suffix, P typed "psign", 17 significant digits);
+ * needs no context and no GPU.  Returns 0 or a negative code
+ * (nss_last_error(NULL) has the message). */
+int       nss_restart_rewrite(const char *in_path, const char *out_path);
 int       nss_dmrg_load_blocks(nss_dmrg *d, const char *left_path, const char *right_path);
 /* Measure_DMRG_scalar (src/DMRG_MEASURE.f90:148-220, 288-486, 595-705) after
  * a run with save_umat: for each position pos[i] (1-based along the chain,

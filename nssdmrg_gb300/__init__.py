@@ -127,6 +127,7 @@ def lib():
         "nss_tridiag_lowest": (C.c_int, [C.c_int, P, P, C.c_int, D, P, P, P]),
         "nss_arrow_lowest": (C.c_int, [C.c_int, D, P, P, P, D, C.POINTER(D), P, C.POINTER(D)]),
         "nss_tridiag_eig": (C.c_int, [C.c_int, P, P, P, P]),
+        "nss_restart_rewrite": (C.c_int, [C.c_char_p, C.c_char_p]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
@@ -188,6 +189,14 @@ def tridiag_lowest(a, b, ne: int = 1, b_last: float = 0.0):
     if rc != 0:
         raise NssError(rc, lib().nss_last_error(None).decode())
     return theta, s, resid
+
+
+def restart_rewrite(in_path, out_path):
+    """Read a block restart file (older operator names included) and write it
+    in the current layout; no GPU needed."""
+    rc = lib().nss_restart_rewrite(str(in_path).encode(), str(out_path).encode())
+    if rc:
+        raise NssError(rc, lib().nss_last_error(None).decode())
 
 
 def tridiag_eig(d, e):

@@ -567,6 +567,20 @@ int nss_dmrg_finite(nss_dmrg *d) {
     return guarded(d->ctx, [&] { return d->drv.finite(); });
 }
 
+int nss_restart_rewrite(const char *in_path, const char *out_path) {
+    if (!in_path || !out_path) {
+        g_err = "nss_restart_rewrite: null path";
+        return NSS_ERR_INVALID;
+    }
+    try {
+        nss::save_block_file(out_path, nss::load_block_file(in_path));
+    } catch (const std::exception &ex) {
+        g_err = ex.what();
+        return NSS_ERR_INVALID;
+    }
+    return NSS_OK;
+}
+
 int nss_dmrg_save_blocks(nss_dmrg *d, const char *left_path, const char *right_path) {
     if (!d) return NSS_ERR_INVALID;
     return guarded(d->ctx, [&] {
