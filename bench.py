@@ -57,10 +57,11 @@ def parse():
                     help="finite sweeps timed on the spin-1 L=64 m=512 chain (0 skips it)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
-    ap.add_argument("--profile-case", choices=["renorm", "trd-grid"], default=None,
+    ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large"], default=None,
                     help="for profiler captures of single kernels: run one small workload and exit "
                          "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
-                         "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction)")
+                         "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction; "
+                         "sweep-large: the mixed-precision finite sweep of the spin-1 L=64 m=512 chain)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -402,6 +403,14 @@ def run_profile_case(case):
         recs = d.infinite()
         print(json.dumps({"profile_case": case, "steps": len(recs), "m_last": recs[-1]["m_left"],
                           "ms_renorm_last": [round(r["ms_renorm"], 3) for r in recs[-4:]]}))
+        return
+    if case == "sweep-large":
+        d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, msweep=[512], dmrg_qn=(0.0, 0.0), lanc_neigen=1,
+                     lanc_niter=200, lanc_tolerance=1e-12, precision=nss.NSS_PREC_MIXED)
+        recs = d.finite()
+        fin = [r for r in recs if r["type"] != 0]
+        print(json.dumps({"profile_case": case, "steps": len(recs), "s_finite": sum(r["ms_step"] for r in fin) / 1e3,
+                          "energy_final": recs[-1]["energy"][0]}))
         return
     nbig = 1000
     rng = np.random.default_rng(1)
