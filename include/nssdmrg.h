@@ -269,6 +269,16 @@ int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b
  * The host solver the RDM uses for flagged rho blocks (their tridiagonal
  * matrices after the device reduction); needs no context and no GPU. */
 int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, double *Z);
+/* The Kronecker sums of enlarge_block, H = Hb + Hd + H2
+ * (src/DMRG_CONNECT.f90:75-107 with connect_spin_blocks :437-439 and
+ * connect_fermion_blocks :370-371; sp_kron_matrix,
+ * src/MATRIX/MATRIX_SPARSE.f90:832-876): out = sum_t coef[t] * (a[t] x b[t]),
+ * row i*nb+k, column j*nb+l, each a[t] na x na and b[t] nb x nb.  Host
+ * only, no context.  Entries appear in the order of their first term and
+ * stay when they cancel, like sp_sum.  With colidx or vals NULL only *nnz is
+ * returned; otherwise cap must hold it.  nthreads <= 0 uses every core. */
+int nss_kron_sum(int32_t na, int32_t nb, int32_t nterms, const double *coef, const nss_csr *a, const nss_csr *b,
+                 int nthreads, int64_t cap, int64_t *nnz, int32_t *rowptr, int32_t *colidx, double *vals);
 int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, const double *b, double b_last,
                      double *lam, double *c, double *resid);
 

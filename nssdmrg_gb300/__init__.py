@@ -128,6 +128,8 @@ def lib():
         "nss_arrow_lowest": (C.c_int, [C.c_int, D, P, P, P, D, C.POINTER(D), P, C.POINTER(D)]),
         "nss_tridiag_eig": (C.c_int, [C.c_int, P, P, P, P]),
         "nss_restart_rewrite": (C.c_int, [C.c_char_p, C.c_char_p]),
+        "nss_kron_sum": (C.c_int, [I32, I32, I32, P, C.POINTER(Csr), C.POINTER(Csr), C.c_int, I64,
+                                   C.POINTER(I64), P, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
@@ -211,6 +213,31 @@ def tridiag_eig(d, e):
     if rc:
         raise NssError(rc, lib().nss_last_error(None).decode())
     return ev, Z.T.copy()
+
+
+def kron_sum(terms, nthreads: int = 0):
+    """sum_t coef_t * kron(A_t, B_t) on the host, as enlarge_block builds the
+    enlarged H; terms = [(coef, A, B), ...] with scipy sparse A (na x na) and
+    B (nb x nb).  Returns (indptr, indices, data) of the na*nb square CSR."""
+    if not terms:
+        raise ValueError("kron_sum: no terms")
+    na, nb = terms[0][1].shape[0], terms[0][2].shape[0]
+    keep = _Keep()
+    coef = keep.arr([t[0] for t in terms], np.float64)
+    ca = (Csr * len(terms))(*[keep.csr(t[1]) for t in terms])
+    cb = (Csr * len(terms))(*[keep.csr(t[2]) for t in terms])
+    nnz = C.c_int64()
+    args = (na, nb, len(terms), _ptr(coef), ca, cb, nthreads)
+    rc = lib().nss_kron_sum(*args, 0, C.byref(nnz), None, None, None)
+    if rc:
+        raise NssError(rc, lib().nss_last_error(None).decode())
+    rp = np.empty(na * nb + 1, np.int32)
+    ci = np.empty(nnz.value, np.int32)
+    va = np.empty(nnz.value, np.float64)
+    rc = lib().nss_kron_sum(*args, nnz.value, C.byref(nnz), _ptr(rp), _ptr(ci), _ptr(va))
+    if rc:
+        raise NssError(rc, lib().nss_last_error(None).decode())
+    return rp, ci, va
 
 
 def arrow_lowest(theta0: float, m, a, b, b_last: float = 0.0):

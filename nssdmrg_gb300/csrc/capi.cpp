@@ -3,9 +3,12 @@
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
+#include <algorithm>
+#include <climits>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "device.cuh"
@@ -209,6 +212,55 @@ int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, doub
         return NSS_ERR_NOCONV;
     }
     std::copy(dd.begin(), dd.end(), evals);
+    return NSS_OK;
+}
+
+int nss_kron_sum(int32_t na, int32_t nb, int32_t nterms, const double *coef, const nss_csr *a, const nss_csr *b,
+                 int nthreads, int64_t cap, int64_t *nnz, int32_t *rowptr, int32_t *colidx, double *vals) {
+    if (na <= 0 || nb <= 0 || nterms < 0 || (nterms > 0 && (!coef || !a || !b)) || !nnz ||
+        (int64_t)na * nb > INT32_MAX - 1) {
+        g_err = "nss_kron_sum: need na, nb > 0, na*nb < 2^31 and non-NULL arrays";
+        return NSS_ERR_INVALID;
+    }
+    auto load = [](const nss_csr &c, int n, nss::Csr &m) {
+        if (c.nrow != n || c.ncol != n || !c.rowptr || c.rowptr[0] != 0) return false;
+        m.init(n, n);
+        for (int i = 0; i < n; ++i) {
+            if (c.rowptr[i + 1] < c.rowptr[i]) return false;
+            for (int e = c.rowptr[i]; e < c.rowptr[i + 1]; ++e) {
+                if (!c.colidx || !c.vals || c.colidx[e] < 0 || c.colidx[e] >= n) return false;
+                m.col.push_back(c.colidx[e]);
+                m.val.push_back(c.vals[e]);
+            }
+            m.rowptr[i + 1] = (int)m.col.size();
+        }
+        return true;
+    };
+    std::vector<nss::Csr> ma(nterms), mb(nterms);
+    std::vector<nss::KronTerm> terms;
+    for (int t = 0; t < nterms; ++t) {
+        if (!load(a[t], na, ma[t]) || !load(b[t], nb, mb[t])) {
+            g_err = "nss_kron_sum: term " + std::to_string(t) + " has a wrong shape or a malformed CSR";
+            return NSS_ERR_INVALID;
+        }
+        terms.push_back({&ma[t], &mb[t], coef[t]});
+    }
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    try {
+        const nss::Csr c = nss::csr_kron_sum(na, nb, terms, nthreads);
+        *nnz = (int64_t)c.col.size();
+        if (!colidx || !vals) return NSS_OK;
+        if (!rowptr || cap < *nnz) {
+            g_err = "nss_kron_sum: rowptr missing or cap below nnz";
+            return NSS_ERR_INVALID;
+        }
+        std::copy(c.rowptr.begin(), c.rowptr.end(), rowptr);
+        std::copy(c.col.begin(), c.col.end(), colidx);
+        std::copy(c.val.begin(), c.val.end(), vals);
+    } catch (const std::exception &ex) {
+        g_err = std::string("nss_kron_sum: ") + ex.what();
+        return NSS_ERR_INVALID;
+    }
     return NSS_OK;
 }
 
