@@ -61,7 +61,7 @@ def parse():
                     help="for profiler captures of single kernels: run one small workload and exit "
                          "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
                          "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction; "
-                         "sweep-large: the mixed-precision finite sweep of the spin-1 L=64 m=512 chain)")
+                         "sweep-large: the finite sweep of the spin-1 L=64 m=512 chain in --precision)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -390,7 +390,7 @@ def measure_serving(nss, device):
     return out
 
 
-def run_profile_case(case):
+def run_profile_case(case, precision="mixed"):
     """Small single-kernel workloads for ncu captures (see --profile-case)."""
     import numpy as np
     import scipy.sparse as sp
@@ -406,10 +406,11 @@ def run_profile_case(case):
         return
     if case == "sweep-large":
         d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, msweep=[512], dmrg_qn=(0.0, 0.0), lanc_neigen=1,
-                     lanc_niter=200, lanc_tolerance=1e-12, precision=nss.NSS_PREC_MIXED)
+                     lanc_niter=200, lanc_tolerance=1e-12,
+                     precision=nss.NSS_PREC_FP64 if precision == "fp64" else nss.NSS_PREC_MIXED)
         recs = d.finite()
         fin = [r for r in recs if r["type"] != 0]
-        print(json.dumps({"profile_case": case, "steps": len(recs), "s_finite": sum(r["ms_step"] for r in fin) / 1e3,
+        print(json.dumps({"profile_case": case, "precision": precision, "steps": len(recs), "s_finite": sum(r["ms_step"] for r in fin) / 1e3,
                           "energy_final": recs[-1]["energy"][0]}))
         return
     nbig = 1000
@@ -731,7 +732,7 @@ def run_reference(args):
 if __name__ == "__main__":
     a = parse()
     if a.profile_case:
-        run_profile_case(a.profile_case)
+        run_profile_case(a.profile_case, a.precision)
     elif a.impl == "reference":
         run_reference(a)
     else:

@@ -504,10 +504,14 @@ bool rdm_own_eigensolver() {
 }
 
 // blocks from this many states on are reduced by the whole GPU (env
-// NSS_TRD_GRID_MIN; 0 keeps every big block on one cluster)
+// NSS_TRD_GRID_MIN; 0 keeps every big block on one cluster).  Alone, a
+// 1000-state block is faster on the whole GPU (17.5 against 39.5 ms); in a
+// sweep the cluster tier runs several such blocks side by side, and the
+// spin-1 L=64 M=512 finite sweep took 6.59-6.67 s with 1400 (three runs)
+// against 6.73-6.81 s with 900 and 6.77 s with 600.
 int trd_grid_min() {
     const char *e = std::getenv("NSS_TRD_GRID_MIN");
-    return e ? std::atoi(e) : 900;
+    return e ? std::atoi(e) : 1400;
 }
 
 template <class T>
