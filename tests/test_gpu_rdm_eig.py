@@ -185,7 +185,7 @@ def test_big_blocks_through_blocked_reduction(nss, cluster_mem):
     """Rho blocks above 160 states are reduced by a thread-block cluster,
     with the block in the cluster's shared memory or (env
     NSS_TRD_CL_SHARED_MAX=0, as for blocks too large for it) in a global
-    copy, or (NSS_TRD_GRID_MIN, as for blocks of ~900 states and more) by
+    copy, or (NSS_TRD_GRID_MIN, as for blocks of 1400 states and more) by
     the whole GPU, then the same bisection and twisted vectors: against the
     library eigensolver on the spin-1 chain's last infinite step (L=32,
     m=256, blocks up to ~190)."""
