@@ -240,11 +240,13 @@ int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iter
  * allocating any memory.  No counterpart in the reference: it is for callers
  * that cannot allocate device memory when they need an energy (a host code
  * whose device heap belongs to another allocator, a context whose HBM budget
- * is spent, code about to be captured into a CUDA graph).  Its scratch is a
- * static device array of 32768 16x16-tile partial sums (512 KiB per GPU that
- * loads the library, held until exit); larger superblocks are rejected with
- * NSS_ERR_INVALID.  The first call on a device looks up that array and must
- * come before any stream capture; calls that overlap on the GPU race. */
+ * is spent).  Its scratch is a static device array of 32768 16x16-tile
+ * partial sums (512 KiB per GPU that loads the library, held until exit);
+ * larger superblocks are rejected with NSS_ERR_INVALID, and so is a psi of
+ * zero norm.  The first call on each context looks up that array's device
+ * address and should come before any stream capture.  Each call waits for
+ * its kernel and copies the energy into host memory before it returns;
+ * calls that overlap on the GPU race on the shared array. */
 int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy);
 
 /* Lowest ne eigenpairs of the symmetric tridiagonal matrix with diagonal

@@ -51,6 +51,23 @@ int guarded(nss_ctx *ctx, F &&f) {
     }
 }
 
+// Makes the context's device current for the duration of one entry point
+// and gives the caller back the device that was current before, so that a
+// host code with its own device binding keeps it.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 int ensure_tmp(nss_ctx *ctx, int64_t n) {
     if (ctx->tmp_n >= n && ctx->d_v) return NSS_OK;
     nss::ctx_free(ctx->c, ctx->d_v);
@@ -76,8 +93,10 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
         g_err = "nss_create: device index out of range";
         return nullptr;
     }
-    if (cudaSetDevice(device) != cudaSuccess) {
-        g_err = "nss_create: cudaSetDevice failed";
+    DeviceScope dscope(device);
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != device) {
+        g_err = "nss_create: cannot make the device current";
         return nullptr;
     }
     auto *ctx = new (std::nothrow) nss_ctx;
@@ -106,7 +125,7 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
 
 void nss_destroy(nss_ctx *ctx) {
     if (!ctx) return;
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     cudaStreamSynchronize(ctx->c.stream);
     nss::sb_release(ctx->c, true);
     nss::lanczos_release(ctx->c);
@@ -126,7 +145,7 @@ const char *nss_last_error(const nss_ctx *ctx) { return ctx ? ctx->c.err.c_str()
 int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     return guarded(ctx, [&] {
-        cudaSetDevice(ctx->c.device);
+        DeviceScope dscope(ctx->c.device);
         ctx->sbhost.reset();
         return nss::sb_upload(ctx->c, desc);
     });
@@ -134,7 +153,7 @@ int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc) {
 
 int nss_sb_free(nss_ctx *ctx) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     cudaStreamSynchronize(ctx->c.stream);
     nss::sb_release(ctx->c, true);
     ctx->sbhost.reset();
@@ -170,7 +189,7 @@ int nss_hv_device(nss_ctx *ctx, int64_t n, const double *d_v, double *d_hv) {
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
     if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
     if (!d_v || !d_hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return nss::hv_device(ctx->c, d_v, d_hv);
 }
 
@@ -179,13 +198,13 @@ int nss_hv_device_f32(nss_ctx *ctx, int64_t n, const float *d_v, float *d_hv) {
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
     if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
     if (!d_v || !d_hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return nss::hv_device_fp32(ctx->c, d_v, d_hv);
 }
 
 int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return nss::sb_energy_noalloc(ctx->c, n, d_psi, energy);
 }
 
@@ -320,7 +339,7 @@ int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (!ctx->c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_hv: no superblock uploaded");
     if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
     if (!v || !hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     int rc = ensure_tmp(ctx, n);
     if (rc) return rc;
     nss::Ctx &c = ctx->c;
@@ -351,7 +370,7 @@ int nss_odotv(nss_ctx *ctx, char label, const nss_csr *ops, const double *v, dou
     const int side = side_of(label);
     if (side < 0) return fail(ctx, NSS_ERR_INVALID, "nss_odotv: label not [l,r]");
     if (!ops || !v || !ov) return fail(ctx, NSS_ERR_INVALID, "nss_odotv: null argument");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return guarded(ctx, [&] {
         nss::Ctx &c = ctx->c;
         const int64_t n = c.sb.n;
@@ -371,7 +390,7 @@ int nss_average_op(nss_ctx *ctx, char label, const nss_csr *op, const double *ps
     const int side = side_of(label);
     if (side < 0) return fail(ctx, NSS_ERR_INVALID, "Average_op_dmrg error: label not [l,r]");
     if (!op || !val) return fail(ctx, NSS_ERR_INVALID, "nss_average_op: null argument");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return guarded(ctx, [&] {
         nss::Ctx &c = ctx->c;
         const nss::DevSb &s = c.sb;
@@ -428,7 +447,7 @@ int nss_eigh(nss_ctx *ctx, int neigen, int nitermax, int ncv, double tol, uint64
     if (!evals) return fail(ctx, NSS_ERR_INVALID, "nss_eigh: evals is NULL");
     if (precision != NSS_PREC_FP64 && precision != NSS_PREC_MIXED)
         return fail(ctx, NSS_ERR_INVALID, "nss_eigh: unknown precision mode");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return guarded(ctx, [&] {
         int rc = nss::lanczos_eigh(ctx->c, neigen, nitermax, tol, seed, precision, evals, numop);
         if (rc) return rc;
@@ -456,7 +475,7 @@ int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const
         }
     nss_ctx *c0 = ctxs[0];
     return guarded(c0, [&] {
-        cudaSetDevice(c0->c.device);
+        DeviceScope dscope(c0->c.device);
         std::vector<nss::Ctx *> cs((size_t)nb);
         for (int b = 0; b < nb; ++b) cs[b] = &ctxs[b]->c;
         return nss::lanczos_eigh_batch(cs.data(), nb, nitermax, tol, seeds, evals, numops);
@@ -474,7 +493,7 @@ nss_batch *nss_batch_create(nss_ctx *host) {
         return nullptr;
     }
     try {
-        cudaSetDevice(host->c.device);
+        DeviceScope dscope(host->c.device);
         nss::BatchEngine *e = nss::batch_create(host->c);
         if (!e) return nullptr;
         nss_batch *b = new nss_batch();
@@ -493,7 +512,7 @@ int nss_batch_add(nss_batch *b, nss_ctx *ctx, uint64_t seed, int nitermax, doubl
         return NSS_ERR_INVALID;
     }
     return guarded(b->host, [&] {
-        cudaSetDevice(b->host->c.device);
+        DeviceScope dscope(b->host->c.device);
         return nss::batch_add(b->eng, ctx->c, seed, nitermax, tol, id);
     });
 }
@@ -504,7 +523,7 @@ int nss_batch_step(nss_batch *b, int max_done, int *ndone, int *ids, double *ene
         return NSS_ERR_INVALID;
     }
     return guarded(b->host, [&] {
-        cudaSetDevice(b->host->c.device);
+        DeviceScope dscope(b->host->c.device);
         return nss::batch_step(b->eng, max_done, ndone, ids, energies, numops);
     });
 }
@@ -513,7 +532,7 @@ int nss_batch_inflight(const nss_batch *b) { return b ? nss::batch_inflight(b->e
 
 void nss_batch_destroy(nss_batch *b) {
     if (!b) return;
-    cudaSetDevice(b->host->c.device);
+    DeviceScope dscope(b->host->c.device);
     nss::batch_destroy(b->eng);
     delete b;
 }
@@ -523,7 +542,7 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rd
             double *u_right) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!out) return fail(ctx, NSS_ERR_INVALID, "nss_rdm: out is NULL");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return guarded(ctx, [&] {
         nss::Ctx &c = ctx->c;
         if (!c.sb.valid) return fail(ctx, NSS_ERR_STATE, "nss_rdm: no superblock uploaded");
@@ -551,7 +570,7 @@ int nss_sb_setup(nss_ctx *ctx, int site_type, const nss_block_desc *left, const 
     if (!left || !right || !target || !hij) return fail(ctx, NSS_ERR_INVALID, "nss_sb_setup: null argument");
     if (site_type != NSS_SITE_SPIN && site_type != NSS_SITE_FERMION)
         return fail(ctx, NSS_ERR_INVALID, "nss_sb_setup: unknown site type");
-    cudaSetDevice(ctx->c.device);
+    DeviceScope dscope(ctx->c.device);
     return guarded(ctx, [&] {
         const bool f = site_type == NSS_SITE_FERMION;
         nss::Block l = nss::block_from_desc(*left, f), r = nss::block_from_desc(*right, f);
@@ -609,13 +628,13 @@ void nss_dmrg_destroy(nss_dmrg *d) { delete d; }
 
 int nss_dmrg_infinite(nss_dmrg *d) {
     if (!d) return NSS_ERR_INVALID;
-    cudaSetDevice(d->ctx->c.device);
+    DeviceScope dscope(d->ctx->c.device);
     return guarded(d->ctx, [&] { return d->drv.infinite(); });
 }
 
 int nss_dmrg_finite(nss_dmrg *d) {
     if (!d) return NSS_ERR_INVALID;
-    cudaSetDevice(d->ctx->c.device);
+    DeviceScope dscope(d->ctx->c.device);
     return guarded(d->ctx, [&] { return d->drv.finite(); });
 }
 
@@ -672,7 +691,7 @@ int nss_dmrg_load_blocks(nss_dmrg *d, const char *left_path, const char *right_p
 int nss_dmrg_measure(nss_dmrg *d, const nss_csr *op, const int32_t *pos, int npos, double *out) {
     if (!d) return NSS_ERR_INVALID;
     if (!op || (npos > 0 && (!pos || !out)) || npos < 0) return fail(d->ctx, NSS_ERR_INVALID, "nss_dmrg_measure: bad arguments");
-    cudaSetDevice(d->ctx->c.device);
+    DeviceScope dscope(d->ctx->c.device);
     return guarded(d->ctx, [&] {
         const int dd = d->drv.dot.dim;
         if (op->nrow != dd || op->ncol != dd || !op->rowptr)
@@ -701,7 +720,7 @@ int nss_dmrg_measure(nss_dmrg *d, const nss_csr *op, const int32_t *pos, int npo
 
 int nss_dmrg_prepare_last(nss_dmrg *d) {
     if (!d) return NSS_ERR_INVALID;
-    cudaSetDevice(d->ctx->c.device);
+    DeviceScope dscope(d->ctx->c.device);
     return guarded(d->ctx, [&] {
         d->drv.stop_before_last_solve = true;
         int rc = d->drv.infinite();

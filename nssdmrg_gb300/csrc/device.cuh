@@ -217,6 +217,7 @@ struct Ctx {
     int64_t mixed_fallbacks = 0;                 // mixed solves redone in FP64 (context life)
     char *ms_dev = nullptr, *ms_host = nullptr;   // OdotV tables: device, pinned staging
     size_t ms_cap = 0;   // host: scan+extract, device wait, CSR assembly (summed over calls)
+    double *noalloc_scratch = nullptr;   // device address of k_noalloc.cu's static scratch, looked up on first use
 };
 
 // Allocation through the context budget.

@@ -2,10 +2,10 @@
 //
 // Some callers of this library cannot allocate device memory at the moment
 // they need an energy: a Fortran driver whose device heap is owned by
-// another pool allocator, a code that has already given the whole HBM
-// budget of its context to the Krylov basis, or one that is about to run
-// inside a captured stream, where an allocation would either fail or
-// break the capture.  nss_sb_energy_noalloc serves them: it evaluates
+// another pool allocator, or a code that has already given the whole HBM
+// budget of its context to the Krylov basis, where one more cudaMalloc would
+// fail or fragment a pool that is not this library's.  nss_sb_energy_noalloc
+// serves them: it evaluates
 //     E = <psi|H|psi> / <psi|psi>
 // on the superblock already uploaded with nss_sb_upload / nss_sb_setup,
 // without allocating anything.  (The reference computes the same number in a
@@ -16,9 +16,11 @@
 // per-tile partial sums and the last-CTA counter live in the file-scope
 // device array g_noalloc_scratch below, NOALLOC_MAX_TILES tiles at most
 // (512 KiB + 256 B; every GPU that loads the library keeps it until the
-// process exits).  The host code obtains its address with
-// cudaGetSymbolAddress the first time it is called on a device, with that
-// device current, so that first call must come before any stream capture.
+// process exits).  In host code the array's name is only a host-side stand-in,
+// so the first call on each context looks up its device address with
+// cudaGetSymbolAddress, with the context's device current, and keeps it in
+// the context; that first call should come before any stream capture.  Each
+// call waits for its kernel and copies E into host memory before it returns.
 // All calls on a device share the array and each one clears the counter it
 // needs: two calls whose kernels overlap on the GPU race with each other.
 #include "device.cuh"
@@ -31,13 +33,10 @@ namespace {
 
 constexpr int NA_TILE = 16;
 constexpr int NOALLOC_MAX_TILES = 32768;
-constexpr int NA_MAX_DEVICES = 64;
 
 // partials: [0, MAX) psi.Hpsi per tile, [MAX, 2 MAX) psi.psi per tile,
 // then one 32-double slot for the counter and the results
 __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_MAX_TILES + 32];
-
-double *g_scratch_ptr[NA_MAX_DEVICES] = {};
 
 __global__ void __launch_bounds__(256) k_energy_noalloc(
     const double *__restrict__ v, const int4 *__restrict__ tiles, const int *__restrict__ dls,
@@ -156,19 +155,19 @@ int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy) {
                 std::to_string(NOALLOC_MAX_TILES) + " its static scratch holds; use nss_hv instead";
         return NSS_ERR_INVALID;
     }
-    if (c.device < 0 || c.device >= NA_MAX_DEVICES) {
-        c.err = "nss_sb_energy_noalloc: device index beyond the supported range";
+    if (s.ntiles <= 0) {
+        c.err = "nss_sb_energy_noalloc: the uploaded superblock has no tiles";
         return NSS_ERR_INVALID;
     }
-    double *scratch = g_scratch_ptr[c.device];
+    double *scratch = c.noalloc_scratch;
     if (!scratch) {
-        // once per device, with that device current (the caller's context)
+        // once per context, with its device current (the entry point made it so)
         cudaError_t e = cudaGetSymbolAddress((void **)&scratch, g_noalloc_scratch);
         if (e != cudaSuccess || !scratch) {
             c.err = std::string("nss_sb_energy_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
             return NSS_ERR_CUDA;
         }
-        g_scratch_ptr[c.device] = scratch;
+        c.noalloc_scratch = scratch;
     }
     // the last-CTA counter must start at zero
     NSS_CUDA_TRY(c, cudaMemsetAsync(scratch + 2 * NOALLOC_MAX_TILES, 0, 8 * sizeof(double), c.stream));
@@ -177,9 +176,15 @@ int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy) {
                                                      s.d_ab_rowptr, s.d_ab_col, s.d_ab_val, scratch);
     c.launches += 1;
     NSS_CUDA_TRY(c, cudaGetLastError());
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(energy, scratch + 2 * NOALLOC_MAX_TILES + 8, sizeof(double),
-                                    cudaMemcpyDeviceToHost, c.stream));
+    double res[3] = {0.0, 0.0, 0.0};   // E, <psi|H|psi>, <psi|psi>
+    NSS_CUDA_TRY(c, cudaMemcpyAsync(res, scratch + 2 * NOALLOC_MAX_TILES + 8, sizeof(res), cudaMemcpyDeviceToHost,
+                                    c.stream));
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    if (!(res[2] > 0.0)) {
+        c.err = "nss_sb_energy_noalloc: psi has zero norm";
+        return NSS_ERR_INVALID;
+    }
+    *energy = res[0];
     return NSS_OK;
 }
 

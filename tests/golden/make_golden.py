@@ -198,7 +198,9 @@ def c2_small():
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference checkout> [kat] [trajectories] [c2_small] [oracle_runs] [measure_runs]")
+    ref = Path(sys.argv[1])
     parts = set(sys.argv[2:]) or {"kat", "trajectories", "c2_small", "oracle_runs", "measure_runs"}
     if "kat" in parts:
         kat(ref, "spin")

@@ -191,7 +191,7 @@ def c2_superblock(nss):
     """Last infinite step of the Hubbard L=32, U=4, M=256 chain (the
     benchmark superblock: N=65 900, sectors up to 120 x 120).  Its context
     sends sectors with Dl >= 64 to the tensor-core kernel (the default
-    threshold, 256, would leave it unused at this size)."""
+    threshold would leave it unused at this size)."""
     import os
     old = os.environ.get("NSS_TC_MIN_DL")
     os.environ["NSS_TC_MIN_DL"] = "64"
