@@ -149,7 +149,8 @@ def measure_core_peaks():
         exe = build_peaks()
         line = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.strip().splitlines()[-1]
         j = json.loads(line)
-        CORE_PROBE.update({k: j[k] for k in ("dfma_gflops", "dmma_gflops", "ffma_gflops", "dfma_chain_cycles",
+        CORE_PROBE.update({k: j[k] for k in ("dfma_gflops", "dmma_gflops", "ffma_gflops", "tf32_tc_gflops",
+                                             "dfma_chain_cycles",
                                              "ddiv_chain_cycles", "ffma_chain_cycles", "chain_lanes") if k in j})
         return j["dfma_gflops"] / 1e3, j["ffma_gflops"] / 1e3, \
             "DFMA / FFMA rates measured in this run by nssdmrg_gb300/peaks.cu (whole GPU)"

@@ -88,7 +88,10 @@ const char *nss_last_error(const nss_ctx *ctx);
 /* Upload the superblock operator pool; replaces the Setup_SuperBlock_Direct
  * -> spHtimesV_p assignment (src/DMRG_SUPERBLOCK.f90:553-573,
  * src/DMRG_SUPERBLOCK_SETUP.f90:113-136).  Copies everything: the caller
- * may free its arrays on return.  Replaces any previous superblock. */
+ * may free its arrays on return.  Replaces any previous superblock.
+ * Inconsistent sizes, out-of-range indices and non-finite operator values
+ * are refused with NSS_ERR_INVALID; a context over its hbm_budget returns
+ * NSS_ERR_NOMEM. */
 int nss_sb_upload(nss_ctx *ctx, const nss_sb_desc *desc);
 /* Free the device superblock (sb_delete_Hv, src/DMRG_SUPERBLOCK.f90:582-620). */
 int nss_sb_free(nss_ctx *ctx);
@@ -185,6 +188,19 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr,
             nss_rdm_side out[2], double *lambda_left, double *lambda_right,
             int32_t *kept_left, int32_t *kept_right,
             double *u_left, double *u_right);
+
+/* nss_rdm with the reference's second truncation rule: renormalize_block's
+ * (Mstates, Estates) pair (src/DMRG_RDM.f90:204-211, right side :277-284).
+ * mstates != 0 keeps min(mstates, m_block, nevals) states as nss_rdm does;
+ * mstates == 0 with estates != 0 keeps the m_s that minimises
+ * |1 - sum(lambda(1:m_s)) - estates| (the first such m_s), i.e. the
+ * discarded weight closest to the threshold Edmrg; both are then extended
+ * over degenerate eigenvalues.  mstates == 0 with estates == 0 is refused
+ * with NSS_ERR_INVALID, as the reference stops there. */
+int nss_rdm_estates(nss_ctx *ctx, const double *psi, int mstates, double estates, double deg_thr,
+                    nss_rdm_side out[2], double *lambda_left, double *lambda_right,
+                    int32_t *kept_left, int32_t *kept_right,
+                    double *u_left, double *u_right);
 
 /* OdotV_direct (src/DMRG_MEASURE.f90:653-705): ov = (O x 1) v for label
  * 'l' (or 's') and ov = (1 x O) v for 'r' (or 'e') on the uploaded
@@ -308,8 +324,9 @@ typedef struct {
 int nss_sb_setup(nss_ctx *ctx, int site_type, const nss_block_desc *left,
                  const nss_block_desc *right, const double *target,
                  const double *hij);
-/* Sector tables of the current superblock: nsb, sector QNs (left QN, qdim
- * each), Dls, Drs, Offset and sb_states (left*m_right + right, 0-based).
+/* Sector tables of the current superblock (built by nss_sb_setup, or by the
+ * driver's nss_dmrg_prepare_last on this context): nsb, sector QNs (left QN,
+ * qdim each), Dls, Drs, Offset and sb_states (left*m_right + right, 0-based).
  * Pass NULL for anything not wanted; sizes from nss_sb_counts. */
 int nss_sb_counts(const nss_ctx *ctx, int32_t *nsb, int32_t *qdim, int64_t *n);
 int nss_sb_tables(const nss_ctx *ctx, double *qns, int32_t *dls, int32_t *drs,
@@ -343,6 +360,10 @@ typedef struct {
     int32_t save_umat;      /* keep every renormalisation's rotation matrix
                                on the host (SAVE_UMAT with STORE_UMAT='b'),
                                which nss_dmrg_measure needs */
+    double  edmrg;          /* Edmrg: truncation threshold used when mdmrg == 0
+                               (src/INPUT_VARS.f90:16-19) */
+    const double *esweep;   /* [nsweep] Esweep, used where msweep is 0; NULL:
+                               edmrg for every sweep */
 } nss_dmrg_params;
 
 typedef struct {

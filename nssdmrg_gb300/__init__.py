@@ -78,7 +78,7 @@ class DmrgParams(C.Structure):
                 ("mdmrg", C.c_int32), ("nsweep", C.c_int32), ("msweep", C.POINTER(C.c_int32)),
                 ("lanc_neigen", C.c_int32), ("lanc_niter", C.c_int32), ("lanc_tolerance", C.c_double),
                 ("deg_evals_threshold", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int32),
-                ("save_umat", C.c_int32)]
+                ("save_umat", C.c_int32), ("edmrg", C.c_double), ("esweep", C.POINTER(C.c_double))]
 
 
 class StepRecord(C.Structure):
@@ -132,6 +132,7 @@ def lib():
                                    C.POINTER(I64), P, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
+        "nss_rdm_estates": (C.c_int, [P, P, C.c_int, D, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
         "nss_time_chunks": (C.c_int, [P, C.c_int]),
         "nss_chunk_stats": (C.c_int, [P, C.POINTER(D), C.POINTER(C.c_int), C.POINTER(I64), C.POINTER(D)]),
@@ -583,7 +584,9 @@ class Superblock:
         ne = min(neigen, n)
         return ev[:ne], (vec[:ne].T if vec is not None else None), numop.value
 
-    def sb_get_rdm(self, mstates, deg_thr=0.1, psi=None, want_u=True) -> RdmResult:
+    def sb_get_rdm(self, mstates, deg_thr=0.1, psi=None, want_u=True, estates=0.0) -> RdmResult:
+        """sb_get_rdm + eigh + the truncation choice; mstates=0 with
+        estates != 0 selects the error-threshold rule (Edmrg)."""
         out = (RdmSide * 2)()
         _, ml, mr, n = self.shape()     # output buffers sized from the uploaded superblock
         if psi is not None and np.asarray(psi).size != n:
@@ -593,7 +596,7 @@ class Superblock:
         ul = np.zeros(ml * ml) if want_u else None
         ur = np.zeros(mr * mr) if want_u else None
         p = np.ascontiguousarray(psi, np.float64) if psi is not None else None
-        self._check(lib().nss_rdm(self._ctx, _ptr(p) if p is not None else None, mstates, deg_thr, out,
+        self._check(lib().nss_rdm_estates(self._ctx, _ptr(p) if p is not None else None, mstates, estates, deg_thr, out,
                                   _ptr(lam_l), _ptr(lam_r), _ptr(kl), _ptr(kr),
                                   _ptr(ul) if want_u else None, _ptr(ur) if want_u else None))
         ms = (out[0].m_s, out[1].m_s)
@@ -611,7 +614,7 @@ class DMRG:
     def __init__(self, model, ldmrg, mdmrg, msweep=(), jz=1.0, jxy=1.0, t=1.0, u=0.0, hfmode=True,
                  dmrg_qn=(0.0, 0.0), lanc_neigen=1, lanc_niter=512, lanc_tolerance=1e-12,
                  deg_evals_threshold=0.1, seed=1234, precision=NSS_PREC_FP64, device=0, sb=None,
-                 save_umat=False):
+                 save_umat=False, edmrg=0.0, esweep=()):
         self.sb = sb or Superblock(device)
         p = DmrgParams()
         p.model, p.jz, p.jxy, p.t, p.u, p.hfmode = model, jz, jxy, t, u, int(hfmode)
@@ -624,6 +627,12 @@ class DMRG:
         p.lanc_neigen, p.lanc_niter, p.lanc_tolerance = lanc_neigen, lanc_niter, lanc_tolerance
         p.deg_evals_threshold, p.seed, p.precision = deg_evals_threshold, seed, precision
         p.save_umat = int(save_umat)
+        p.edmrg = edmrg
+        self._es = np.ascontiguousarray(esweep, np.float64) if len(esweep) else None
+        if self._es is not None:
+            if len(self._es) != len(msweep):
+                raise NssError(NSS_ERR_INVALID, "esweep needs one entry per sweep")
+            p.esweep = _p(self._es, C.c_double)
         self._p = p
         self._d = lib().nss_dmrg_create(self.sb._ctx, C.byref(p))
         if not self._d:

@@ -18,7 +18,9 @@
 
 struct nss_ctx {
     nss::Ctx c;
-    std::unique_ptr<nss::SbHost> sbhost;   // set by nss_sb_setup
+    // host tables of the superblock built here: by nss_sb_setup, or the
+    // driver's superblock after nss_dmrg_prepare_last
+    std::shared_ptr<const nss::SbHost> sbhost;
     double *d_v = nullptr, *d_hv = nullptr, *d_psi = nullptr;
     int64_t tmp_n = 0;
 };
@@ -106,6 +108,8 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
     }
     ctx->c.device = device;
     ctx->c.tc_min_dl = nss::tc_min_dl_default();
+    nss::mma_tile_default(&ctx->c.mma_bn, &ctx->c.mma_split);
+    ctx->c.mma_lolo = nss::mma_lolo_default();
     ctx->c.budget = hbm_budget;
     if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_err = "nss_create: stream creation failed";
@@ -540,6 +544,13 @@ void nss_batch_destroy(nss_batch *b) {
 int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rdm_side out[2],
             double *lambda_left, double *lambda_right, int32_t *kept_left, int32_t *kept_right, double *u_left,
             double *u_right) {
+    return nss_rdm_estates(ctx, psi, mstates, 0.0, deg_thr, out, lambda_left, lambda_right, kept_left, kept_right,
+                           u_left, u_right);
+}
+
+int nss_rdm_estates(nss_ctx *ctx, const double *psi, int mstates, double estates, double deg_thr,
+                    nss_rdm_side out[2], double *lambda_left, double *lambda_right, int32_t *kept_left,
+                    int32_t *kept_right, double *u_left, double *u_right) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");
     if (!out) return fail(ctx, NSS_ERR_INVALID, "nss_rdm: out is NULL");
     DeviceScope dscope(ctx->c.device);
@@ -559,7 +570,7 @@ int nss_rdm(nss_ctx *ctx, const double *psi, int mstates, double deg_thr, nss_rd
                 return fail(ctx, NSS_ERR_STATE, "nss_rdm: no ground state (call nss_eigh or pass psi)");
             d_psi = c.lz.evecs;
         }
-        return nss::rdm_run(c, d_psi, mstates, deg_thr, out, lambda_left, lambda_right, kept_left, kept_right,
+        return nss::rdm_run(c, d_psi, mstates, estates, deg_thr, out, lambda_left, lambda_right, kept_left, kept_right,
                             u_left, u_right);
     });
 }
@@ -727,6 +738,7 @@ int nss_dmrg_prepare_last(nss_dmrg *d) {
         d->drv.stop_before_last_solve = false;
         if (rc) return rc;
         if (!d->drv.stopped) return fail(d->ctx, NSS_ERR_STATE, "nss_dmrg_prepare_last: infinite run already done");
+        d->ctx->sbhost = d->drv.last_sb;
         return NSS_OK;
     });
 }

@@ -66,9 +66,18 @@ struct DevSb {
     int *d_item_ell = nullptr;         // per item: offset of its A x B table (-1: CSR loop)
     int2 *d_ell = nullptr;             // the tables
     int4 *d_term_hdr = nullptr;        // per FP32 term: input-sector offset (lo, hi), its Dr
-    int4 *d_tiles_tc = nullptr;        // tensor-core tiles (sectors with Dl >= TC_MIN_DL)
-    int ntiles_tc = 0;
-    int *d_tc_err = nullptr;           // set when a tensor-core wait ran out
+    int *d_tc_err = nullptr;           // set when a tensor-core pipeline wait ran out
+    // tensor-core sector GEMM (k_sector_mma.cu), sections of the upload arena:
+    // operand pool [2 planes][rows][32] FP32 (hi, lo), output planes [2][n],
+    // work items, 32x32 W tiles and their per-sector pack records; the two
+    // tensor maps (128-row and BN-row boxes) over the pool
+    float *d_mma_pool = nullptr, *d_mma_out = nullptr;
+    struct MmaItem *d_mma_items = nullptr;
+    int4 *d_mma_wt = nullptr;
+    struct PackSec *d_mma_sec = nullptr;
+    int mma_nitems = 0, mma_nwt = 0, mma_plane_rows = 0, mma_bn = 64;
+    bool mma_split = true;
+    alignas(64) unsigned char mma_map_a[128] = {}, mma_map_b[128] = {};
 };
 
 // Device-side Lanczos state, kept resident between nss_eigh and nss_rdm.
@@ -183,6 +192,9 @@ struct Ctx {
     DevRenorm ren;
     int64_t launches = 0;        // kernels of this library launched
     int tc_min_dl = 1024;        // tensor-core sector threshold (see tc_min_dl_default)
+    int mma_bn = 64;             // tensor-core tile width (64 or 128) and K-loop split
+    bool mma_split = true;
+    bool mma_lolo = false;       // fourth product lo.lo in the split-TF32 GEMM
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
@@ -245,7 +257,9 @@ void sb_release(Ctx &c, bool free_arena);
 // `stop` (may be null): a device flag; the kernels return at once when set
 int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop = nullptr);
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
-int hv_device_tc(Ctx &c, const float *d_v, float *d_hv, const int *stop = nullptr);
+// k_sector_mma.cu: the dense sector products of the routed sectors into the
+// two output planes (the "terms only" tiles of k_hv_fp32 add them)
+int hv_device_mma(Ctx &c, const float *d_v, const int *stop = nullptr);
 struct Hv32Ops;
 Hv32Ops hv32_ops(const DevSb &s);
 // sectors with at least this many left states take the tensor-core kernel
@@ -254,6 +268,17 @@ Hv32Ops hv32_ops(const DevSb &s);
 // on GB300, 20-25 ms against 29-37 ms per solve of the spin-1 L=64 m=512
 // superblock, whose sectors reach 350 states; 0 disables)
 int tc_min_dl_default();
+// tensor-core tile width and K-loop split of a new context: env NSS_TC_BN
+// (64 or 128, default 64) and NSS_TC_SPLIT (0 or 1, default 1)
+void mma_tile_default(int *bn, bool *split);
+// the split-TF32 GEMM's fourth product lo.lo: env NSS_TC_LOLO (default off)
+bool mma_lolo_default();
+// Poll limit of every bounded device wait (the grid barriers of the
+// cooperative Lanczos and tridiagonalisation kernels): env NSS_WAIT_LIMIT,
+// default 2^22 polls (about 2 s).  A wait that runs out makes its kernel
+// return and the entry point report NSS_ERR_CUDA; the tests shorten the
+// limit to exercise that path.
+uint32_t wait_limit();
 
 // k_noalloc.cu
 int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy);
@@ -333,7 +358,8 @@ int syev_eigs_per_cta();
 
 // k_rdm.cu
 // kl (may be null): per side, the kept columns left on the device
-int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2],
+// mstates = 0 with estates != 0 selects the Edmrg (error threshold) rule
+int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg_thr, nss_rdm_side out[2],
             double *lam_l, double *lam_r, int32_t *kept_l, int32_t *kept_r,
             double *u_l, double *u_r, KeptLayout *kl = nullptr);
 void rdm_release(Ctx &c);

@@ -210,6 +210,13 @@ int Driver::init(Ctx *c, const nss_dmrg_params &params) {
     p = params;
     if (p.msweep && p.nsweep > 0) msweep.assign(p.msweep, p.msweep + p.nsweep);
     p.msweep = nullptr;
+    // Esweep defaults to Edmrg for every sweep (src/INPUT_VARS.f90:203-205)
+    esweep.assign(msweep.size(), p.edmrg);
+    if (p.esweep && p.nsweep > 0) esweep.assign(p.esweep, p.esweep + p.nsweep);
+    p.esweep = nullptr;
+    if (p.mdmrg < 0) throw std::invalid_argument("nss_dmrg_create: Mdmrg must not be negative");
+    if (p.mdmrg == 0 && !(p.edmrg != 0.0))
+        throw std::invalid_argument("Mdmrg=Edmrg=0 can not fix a threshold for the RDM");
     if (p.lanc_neigen <= 0) p.lanc_neigen = 2;
     if (p.lanc_niter <= 0) p.lanc_niter = 512;
     if (p.lanc_tolerance <= 0) p.lanc_tolerance = 1e-12;
@@ -241,13 +248,16 @@ int Driver::init(Ctx *c, const nss_dmrg_params &params) {
     return NSS_OK;
 }
 
-int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, bool renormalize,
-                   Block &left, Block &right, nss_step_record &rec);
+int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, double estates,
+                   bool renormalize, Block &left, Block &right, nss_step_record &rec);
 
 // step_dmrg (src/DMRG_MAIN.f90:262-433), OBC link 'n'
 int Driver::step(int type, int label, int sweep) {
     const auto t_step = std::chrono::steady_clock::now();
+    // Mstates/Estates of step_dmrg (src/DMRG_MAIN.f90:288-295): Mdmrg/Edmrg
+    // while growing, Msweep/Esweep of the sweep afterwards
     const int mstates = (type == 0) ? p.mdmrg : msweep.at(sweep - 1);
+    const double estates = (type == 0) ? p.edmrg : esweep.at(sweep - 1);
     using clk = std::chrono::steady_clock;
     auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
     // the two enlargements are independent
@@ -283,7 +293,7 @@ int Driver::step(int type, int label, int sweep) {
     rec.ms_build = ms_since(t_step);
     rec.host_phase_ms[0] = ms_enlarge;
     rec.host_phase_ms[1] = ms_sb;
-    int rc = nss_solve_step(*ctx, sb, p, mstates, renorm, left, right, rec);
+    int rc = nss_solve_step(*ctx, sb, p, mstates, estates, renorm, left, right, rec);
     if (rc) return rc;
     rec.ms_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     records.push_back(rec);
@@ -397,7 +407,7 @@ void renormalize(Block &blk, const Csr &u, const std::vector<Qn> &kept_qn) {
 
 }  // namespace
 
-int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, bool renorm, Block &left,
+int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, double estates, bool renorm, Block &left,
                    Block &right, nss_step_record &rec) {
     const auto t_up = std::chrono::steady_clock::now();
     SbView v;
@@ -437,7 +447,7 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     k_l.resize(sb.m_left);
     k_r.resize(sb.m_right);
     KeptLayout kl[2];
-    rc = rdm_run(c, c.lz.evecs, mstates, p.deg_evals_threshold, side, nullptr, nullptr,
+    rc = rdm_run(c, c.lz.evecs, mstates, estates, p.deg_evals_threshold, side, nullptr, nullptr,
                  renorm ? k_l.data() : nullptr, renorm ? k_r.data() : nullptr,
                  (renorm && !dev_renorm) ? u_l.data() : nullptr, (renorm && !dev_renorm) ? u_r.data() : nullptr,
                  dev_renorm ? kl : nullptr);

@@ -26,6 +26,7 @@ struct Driver {
     Ctx *ctx = nullptr;
     nss_dmrg_params p{};
     std::vector<int32_t> msweep;
+    std::vector<double> esweep;   // Esweep (default Edmrg for every sweep)
     double hij[4] = {0, 0, 0, 0};
     Block dot, left, right;
     std::vector<nss_step_record> records;

@@ -133,11 +133,15 @@ struct Hv32Ops {
     const int *item_ell;
     const int2 *ell;             // (column, value bits) of A rows / B columns
     const int4 *term_hdr;        // per term: offset of its input sector (lo, hi), its Dr
+    // output planes of the tensor-core sector GEMM (null when it has no
+    // sectors): a "terms only" tile adds both to its A x B terms
+    const float *tc0, *tc1;
 };
 
 // One 32x32 FP32 output tile t = (sector, row0, col0, flags) by 256 threads
 // (lt = thread index in the group), each owning rows {ty, ty+16} x columns
-// {tx, tx+16}.  A "terms only" tile (t.w & 1) skips the two dense products.
+// {tx, tx+16}.  A "terms only" tile (t.w & 1) skips the two dense products
+// and adds them from the tensor-core output planes op.tc0 / op.tc1 instead.
 // The outputs, multiplied by `scale`, go to hv; returns this thread's share
 // of sum_i v[i] * out[i] * scale^2 over its outputs (the Lanczos alpha of a
 // unit vector v * scale), meaningful for whole tiles (t.w == 0).
@@ -230,7 +234,8 @@ __device__ __forceinline__ float hv32_tile(int4 t, const float *__restrict__ v, 
             const int il = row0 + ty + 16 * rr, ir = col0 + tx + 16 * cc;
             if (il < dl && ir < dr) {
                 const int64_t idx = (int64_t)il * dr + ir;
-                const float y = acc[rr][cc] * scale;
+                float y = acc[rr][cc] * scale;
+                if ((t.w & 1) && op.tc0) y += op.tc0[o + idx] + op.tc1[o + idx];
                 hv[o + idx] = y;
                 part = fmaf(W[idx] * scale, y, part);
             }

@@ -80,7 +80,6 @@ double mixed_tol() {
 }
 constexpr int ORTH_THREADS = 512;
 constexpr int ORTH_WARPS = ORTH_THREADS / 32;
-constexpr uint32_t BAR_SPIN = 1u << 22;   // grid-barrier poll limit (~2 s of L2 round trips)
 
 // device scalar slots (Ctx::lz.scal)
 enum { S_WW = 0, S_BB = 1, S_ALPHA = 2, S_NRM = 3, S_NSCAL = 4 };
@@ -305,6 +304,7 @@ struct OrthArgs {
     const void *anc_u, *anc_r, *defl;
     int ndefl;
     double *h_m;
+    uint32_t spin;               // poll limit of the grid barriers (wait_limit)
 };
 
 constexpr int PA_COLS = 8;       // per-CTA values of the first phase (alpha, u.w, r.v, y_k.w)
@@ -321,7 +321,7 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     return v;
 }
 
-__device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned &epoch, int *err) {
+__device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned &epoch, int *err, uint32_t spin) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -331,10 +331,8 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned &epoch, int *e
         atomicAdd(bar, 1u);
         uint32_t it = 0;
         while (ld_acquire_u32(bar) < epoch) {
-            if ((++it & 255u) == 0) {
-                if (*(volatile int *)err) { good = 0; break; }
-                if (it > BAR_SPIN) { atomicExch(err, 1); good = 0; break; }
-            }
+            if (++it > spin) { atomicExch(err, 1); good = 0; break; }
+            if ((it & 255u) == 0 && *(volatile int *)err) { good = 0; break; }
         }
         ok = good;
     }
@@ -352,6 +350,16 @@ __device__ __forceinline__ void grid_exit(unsigned *bar) {
             atomicExch(bar + 1, 0u);
         }
     }
+}
+
+// leaving after a barrier that failed: the host learns of it through the
+// mapped flag mirror at its next check, before it reads any result
+__device__ __forceinline__ void fail_exit(unsigned *bar, int *h_flags) {
+    if (threadIdx.x == 0) {
+        h_flags[F_ERR] = 1;
+        __threadfence_system();
+    }
+    grid_exit(bar);
 }
 
 // CTA sums of NV values at once (512 threads), valid in thread 0
@@ -569,7 +577,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         if (tid == 0) pA[blk] = a1[0];
     }
     if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
-    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
+    if (!grid_sync(a.bar, epoch, err, a.spin)) { fail_exit(a.bar, a.h_flags); return; }
     if (__ldcg(&flags[F_HOST])) {
         if (blk == 0 && tid == 0) flags[F_STOP] = 1;
         grid_exit(a.bar);
@@ -603,7 +611,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         __syncthreads();
         cta_dots<T, CW>(V, m, w, n, i0, i1, true, red, pH + blk, G);
     }
-    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
+    if (!grid_sync(a.bar, epoch, err, a.spin)) { fail_exit(a.bar, a.h_flags); return; }
     grid_columns<T>(pH, G, m + 1, hs);
     __syncthreads();
     const T ww = hs[m];
@@ -613,19 +621,19 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         block_sums<T, 1>(s1, scr);
         if (tid == 0) pB[blk] = s1[0];
     }
-    if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
+    if (!grid_sync(a.bar, epoch, err, a.spin)) { fail_exit(a.bar, a.h_flags); return; }
     T bb[1];
     grid_totals<T, 1>(pB, G, bc + 8, bb);
     if (bb[0] < (T)0.5 * ww) {   // second projection (same decision in every CTA)
         cta_dots<T, CW>(V, m, w, n, i0, i1, false, red, pH2 + blk, G);
-        if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
+        if (!grid_sync(a.bar, epoch, err, a.spin)) { fail_exit(a.bar, a.h_flags); return; }
         grid_columns<T>(pH2, G, m, hs);
         __syncthreads();
         hj += hs[j];
         T s1[1] = {cta_update<T>(V, m, w, n, i0, i1, hs)};
         block_sums<T, 1>(s1, scr);
         if (tid == 0) pB2[blk] = s1[0];
-        if (!grid_sync(a.bar, epoch, err)) { grid_exit(a.bar); return; }
+        if (!grid_sync(a.bar, epoch, err, a.spin)) { fail_exit(a.bar, a.h_flags); return; }
         grid_totals<T, 1>(pB2, G, bc + 9, bb);
     }
     const T alpha_j = alpha0 + hj;
@@ -730,6 +738,10 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
     int done = 0, brk_m = 0;
     // CTA 0 publishes the completed iterations (device arrays, host mirrors)
     auto publish = [&]() {
+        if (tid == 0 && *(volatile int *)err) {
+            a.o.h_flags[F_ERR] = 1;
+            __threadfence_system();
+        }
         if (blk == 0 && tid == 0) {
             for (int q = 0; q < done; ++q) {
                 const int j = a.j0 + q;
@@ -767,7 +779,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             if (tid == 0) pA[blk] = a1[0];
         }
         if (blk == 0 && tid == 0) flags[F_HOST] = host_stop;
-        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
+        if (!grid_sync(a.o.bar, epoch, err, a.o.spin)) { publish(); return; }
         if (__ldcg(&flags[F_HOST])) {
             if (blk == 0 && tid == 0) flags[F_STOP] = 1;
             publish();
@@ -814,7 +826,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
                     if (k < nd) pH[(int64_t)(m + 3 + k) * G + blk] = ex[2 + k];
             }
         }
-        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
+        if (!grid_sync(a.o.bar, epoch, err, a.o.spin)) { publish(); return; }
         grid_columns<float>(pH, G, m + 1 + nx, hs);
         __syncthreads();
         const float ww = hs[m];
@@ -841,7 +853,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             block_sums<float, 1>(s1, scr);
             if (tid == 0) pB[blk] = s1[0];
         }
-        if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
+        if (!grid_sync(a.o.bar, epoch, err, a.o.spin)) { publish(); return; }
         float bb;
         {
             float t1[1];
@@ -869,14 +881,14 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
                         if (k < nd) pH2[(int64_t)(m + 2 + k) * G + blk] = ex[2 + k];
                 }
             }
-            if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
+            if (!grid_sync(a.o.bar, epoch, err, a.o.spin)) { publish(); return; }
             grid_columns<float>(pH2, G, m + (anc ? 2 + nd : 0), hs);
             __syncthreads();
             hj += hs[jj];
             float s1[1] = {update(m)};
             block_sums<float, 1>(s1, scr);
             if (tid == 0) pB2[blk] = s1[0];
-            if (!grid_sync(a.o.bar, epoch, err)) { publish(); return; }
+            if (!grid_sync(a.o.bar, epoch, err, a.o.spin)) { publish(); return; }
             float t1[1];
             grid_totals<float, 1>(pB2, G, bc + 9, t1);
             bb = t1[0];
@@ -934,6 +946,7 @@ struct BatchArgs {
     unsigned *bar;               // global barrier
     int *err;
     int steps;                   // iterations of this launch
+    uint32_t spin;               // poll limit of the grid barriers (wait_limit)
 };
 
 constexpr int BATCH_MAX = 160;   // solves per launch (each needs a CTA)
@@ -1007,7 +1020,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
             }
             GroupSync{1 + grp}();
         }
-        if (!grid_sync(B.bar, epoch, B.err)) break;
+        if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
         const bool run = me >= 0 && alive[me] && Mp->c.j0 + step < Mp->c.jend;
         const int jj = Mp ? Mp->c.j0 + step : 0, m = jj + 1;
         const bool first = run && jj == Mp->c.j0 && Mp->c.first_from_v;
@@ -1059,7 +1072,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
                 }
             }
         }
-        if (!grid_sync(B.bar, epoch, B.err)) break;
+        if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
         float hj = 0.f, mj = 0.f;
         auto update = [&](int xoff) -> float {
             float ss = 0.f;
@@ -1090,7 +1103,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
             block_sums<float, 1>(s1, scr);
             if (tid == 0) pB[lb] = s1[0];
         }
-        if (!grid_sync(B.bar, epoch, B.err)) break;
+        if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
         // every CTA: beta^2 and the second-projection decision of every solve
         if (tid == 0) any_p2 = 0;
         __syncthreads();
@@ -1133,7 +1146,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
                     }
                 }
             }
-            if (!grid_sync(B.bar, epoch, B.err)) break;
+            if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
             if (mine) {
                 grid_columns<float>(pH2, Gs, m + (anc ? 2 + nd : 0), hs);
                 __syncthreads();
@@ -1142,7 +1155,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
                 block_sums<float, 1>(s1, scr);
                 if (tid == 0) pB2[lb] = s1[0];
             }
-            if (!grid_sync(B.bar, epoch, B.err)) break;
+            if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
             for (int s = tid; s < ns; s += ORTH_THREADS) {
                 if (!p2[s]) continue;
                 const BatchSolve &S = B.s[s];
@@ -1612,6 +1625,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     oa.defl = anc ? (const void *)anc->defl32 : nullptr;
     oa.ndefl = anc ? anc->ndefl : 0;
     oa.h_m = z.d_h_ab + 2 * (cap + 1);
+    oa.spin = wait_limit();
     const double *hm = z.h_ab + 2 * (cap + 1);
     std::vector<double> cvec;
     // Chunks of CHECK iterations, each ending with an event; the host checks
@@ -1620,7 +1634,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     cudaEventCreateWithFlags(&evs[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&evs[1], cudaEventDisableTiming);
     // mixed method without tensor-core sectors: one persistent launch per chunk
-    const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.ntiles_tc == 0;
+    const bool use_chunk = sizeof(T) == sizeof(float) && z.chunk_ok && c.sb.mma_nitems == 0;
     struct ChunkTiming {
         cudaEvent_t a, b;
         int j0, jend;
@@ -1694,6 +1708,11 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         if (next_end == -1) { rc = NSS_ERR_CUDA; break; }
         cudaError_t ce = cudaEventSynchronize(evs[slot]);
         if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); rc = NSS_ERR_CUDA; break; }
+        if (hf[F_ERR]) {   // a bounded barrier wait ran out: nothing of this solve is trusted
+            c.err = "nss_eigh: a grid barrier of the orthogonalisation kernel timed out (results discarded)";
+            rc = NSS_ERR_CUDA;
+            break;
+        }
         // a breakdown inside this chunk ends it early; one flagged by the
         // chunk running ahead belongs to the next check
         int m = pend_end;
@@ -2213,7 +2232,7 @@ int engine_add(BatchEngine &E, Ctx &c, uint64_t seed, int nitermax, double tol, 
     }
     if (c.device != c0.device) { c0.err = "nss_batch_add: the context is on another device"; return NSS_ERR_INVALID; }
     if (!c.sb.valid) { c0.err = "nss_batch_add: the context has no superblock"; return NSS_ERR_STATE; }
-    if (c.sb.ntiles_tc != 0) {
+    if (c.sb.mma_nitems != 0) {
         c0.err = "nss_batch_add: superblocks with tensor-core sectors are solved one by one (nss_eigh)";
         return NSS_ERR_INVALID;
     }
@@ -2312,6 +2331,7 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
             oa.h_beta = z.d_h_ab + (z.cap + 1);
             oa.h_flags = z.d_h_flags;
             oa.h_m = z.d_h_ab + 2 * (z.cap + 1);
+            oa.spin = wait_limit();
             const bool anc = B.phase == 2;
             oa.anc_u = anc ? (const void *)B.as.u32 : nullptr;
             oa.anc_r = anc ? (const void *)B.as.r32 : nullptr;
@@ -2357,6 +2377,7 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
         ba.bar = c0.lz.counter + 2;
         ba.err = c0.lz.flags + F_ERR;
         ba.steps = CHECK;
+        ba.spin = wait_limit();
         void *args[] = {&ba};
         cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_batch32, dim3(G), dim3(ORTH_THREADS), args,
                                                     E.smem_set, st);

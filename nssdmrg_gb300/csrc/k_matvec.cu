@@ -9,6 +9,7 @@
 #include "device.cuh"
 #include "hv_tile.cuh"
 #include "host_sparse.hpp"
+#include "sector_mma.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -23,6 +24,25 @@ int tc_min_dl_default() {
     if (!e) return 1024;
     const int x = std::atoi(e);
     return x < 0 ? 0 : x;
+}
+
+void mma_tile_default(int *bn, bool *split) {
+    const char *b = std::getenv("NSS_TC_BN");
+    *bn = (b && std::atoi(b) == 128) ? 128 : 64;
+    const char *sp = std::getenv("NSS_TC_SPLIT");
+    *split = !(sp && std::atoi(sp) == 0);
+}
+
+bool mma_lolo_default() {
+    const char *e = std::getenv("NSS_TC_LOLO");
+    return e && std::atoi(e) != 0;
+}
+
+uint32_t wait_limit() {
+    const char *e = std::getenv("NSS_WAIT_LIMIT");
+    if (!e) return 1u << 22;
+    const long x = std::atol(e);
+    return x < 0 ? 0u : (uint32_t)std::min<long>(x, 1l << 30);
 }
 
 void ctx_free(Ctx &c, void *p) {
@@ -53,7 +73,6 @@ namespace {
 
 constexpr int TILE = 16;
 constexpr int TILE32 = 32;
-constexpr int TC_ROWS = 128, TC_COLS = 64;   // k_hv_tc tile
 
 // Sections of the pool's arena: each array at a 256-byte boundary (at least
 // 16 bytes, so that every pointer is distinct and valid).
@@ -160,6 +179,15 @@ bool csr_ok(const nss_csr &m, int nrow, int ncol, bool cols_known = false) {
     return true;
 }
 
+// every stored value finite (a NaN or Inf operator entry would poison every
+// H*psi and the Lanczos scalars without any other sign)
+bool csr_finite(const nss_csr &m) {
+    const int nnz = m.nrow > 0 ? m.rowptr[m.nrow] : 0;
+    for (int j = 0; j < nnz; ++j)
+        if (!std::isfinite(m.vals[j])) return false;
+    return true;
+}
+
 }  // namespace
 
 // Validate and copy the operator pool.  Errors mirror the reference's stop
@@ -219,6 +247,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
         const int dl = s.dls[k], dr = s.drs[k];
         if (!csr_ok(d->hleft[k], dl, dl, trusted) || !csr_ok(d->hright[k], dr, dr, trusted)) {
             c.err = "nss_sb_upload: Hleft/Hright shape or index error at sector " + std::to_string(k);
+            return NSS_ERR_INVALID;
+        }
+        if (!trusted && (!csr_finite(d->hleft[k]) || !csr_finite(d->hright[k]))) {
+            c.err = "nss_sb_upload: non-finite value in Hleft/Hright at sector " + std::to_string(k);
             return NSS_ERR_INVALID;
         }
         s.hl_off.push_back(hl_tot);
@@ -312,6 +344,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
             c.err = "nss_sb_upload: A/B shape or index error (term " + std::to_string(idx) + ")";
             return NSS_ERR_INVALID;
         }
+        if (!trusted && (!csr_finite(A) || !csr_finite(B))) {
+            c.err = "nss_sb_upload: non-finite value in A/B (term " + std::to_string(idx) + ")";
+            return NSS_ERR_INVALID;
+        }
         DevTerm t;
         t.out_sec = o;
         t.in_sec = q;
@@ -364,26 +400,22 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
             else t.b_rp = at;
         }
     }
-    // Sectors on the tensor-core kernel get their A x B terms from "terms
-    // only" CUDA-core tiles (w = 1), listed first: k_hv_fp32 writes those
-    // terms to H psi and k_hv_tc, launched after it, adds its dense products.
-    std::vector<int4> tiles32, tiles_tc;
-    for (int k = 0; k < s.nsb; ++k) {
-        if (c.tc_min_dl > 0 && s.dls[k] >= c.tc_min_dl) {
-            for (int r = 0; r < s.dls[k]; r += TC_ROWS)
-                for (int cc = 0; cc < s.drs[k]; cc += TC_COLS) tiles_tc.push_back(make_int4(k, r, cc, 0));
+    // Sectors on the tensor-core GEMM (k_sector_mma.cu) get their A x B
+    // terms from "terms only" CUDA-core tiles (w = 1), listed first, which
+    // k_hv_fp32 runs after the GEMM and which add its two output planes.
+    MmaPlan plan;
+    mma_layout(s, c.tc_min_dl, c.mma_bn, c.mma_split, plan);
+    std::vector<char> on_tc(s.nsb, 0);
+    for (int k : plan.sectors) on_tc[k] = 1;
+    std::vector<int4> tiles32;
+    for (int k = 0; k < s.nsb; ++k)
+        if (on_tc[k])
             for (int r = 0; r < s.dls[k]; r += TILE32)
                 for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 1));
-        }
-    }
-    for (int k = 0; k < s.nsb; ++k) {
-        if (c.tc_min_dl > 0 && s.dls[k] >= c.tc_min_dl) {
-            continue;
-        } else {
+    for (int k = 0; k < s.nsb; ++k)
+        if (!on_tc[k])
             for (int r = 0; r < s.dls[k]; r += TILE32)
                 for (int cc = 0; cc < s.drs[k]; cc += TILE32) tiles32.push_back(make_int4(k, r, cc, 0));
-        }
-    }
     // work items of the persistent kernel: 32x32 tiles of every sector,
     // split into H_L, H_R and A x B parts when a K loop is long
     std::vector<int4> items32;
@@ -471,7 +503,6 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
         s.item_cost[ii] = t.w == HV_LEFT ? dl : (t.w == HV_RIGHT ? dr : (t.w == HV_TERMS ? 48 : dl + dr + 48));
     }
     s.ntiles32 = (int)tiles32.size();
-    s.ntiles_tc = (int)tiles_tc.size();
     std::vector<int> tc_err(1, 0);
 
     Stager sg;
@@ -486,8 +517,12 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
     sg.add(&s.d_item_ell, item_ell);
     sg.add(&s.d_ell, ell);
     sg.add(&s.d_term_hdr, term_hdr);
-    sg.add(&s.d_tiles_tc, tiles_tc);
     sg.add(&s.d_tc_err, tc_err);
+    sg.add_dev(&s.d_mma_pool, (size_t)(plan.items.empty() ? 0 : 2 * plan.plane_rows * MM_KC));
+    sg.add_dev(&s.d_mma_out, (size_t)(plan.items.empty() ? 0 : 2 * s.n));
+    sg.add(&s.d_mma_items, plan.items);
+    sg.add(&s.d_mma_wt, plan.wt);
+    sg.add(&s.d_mma_sec, plan.ps);
     sg.add(&s.d_dls, s.dls);
     sg.add(&s.d_drs, s.drs);
     sg.add(&s.d_off, s.off);
@@ -523,6 +558,7 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
         k_dense32<<<608, 256, 0, c.stream>>>(s.d_hr, s.d_hr32, hr_tot);
         NSS_CUDA_TRY(c, cudaGetLastError());
     }
+    if ((rc = mma_finish(c, plan))) return rc;
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
     s.valid = true;
     return NSS_OK;
@@ -638,6 +674,8 @@ Hv32Ops hv32_ops(const DevSb &s) {
     op.item_ell = s.d_item_ell;
     op.ell = s.d_ell;
     op.term_hdr = s.d_term_hdr;
+    op.tc0 = s.mma_nitems ? s.d_mma_out : nullptr;
+    op.tc1 = s.mma_nitems ? s.d_mma_out + s.n : nullptr;
     return op;
 }
 
@@ -647,12 +685,14 @@ int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
         c.err = "nss_hv: no superblock uploaded";
         return NSS_ERR_STATE;
     }
+    // the tensor-core sectors' dense products first: the terms-only tiles add them
+    if (int rc = hv_device_mma(c, d_v, stop)) return rc;
     if (s.ntiles32 > 0) {
         k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, hv32_ops(s), stop);
         c.launches += 1;
         NSS_CUDA_TRY(c, cudaGetLastError());
     }
-    return hv_device_tc(c, d_v, d_hv, stop);
+    return NSS_OK;
 }
 
 int hv_device(Ctx &c, const double *d_v, double *d_hv, const int *stop) {

@@ -142,13 +142,76 @@ __global__ void __launch_bounds__(256) k_rank(const double *ev, int n, double *s
 // 1024 threads: the degeneracy extension is a count over the tail, the sums
 // are block reductions (the reference sums sequentially; the orders differ by
 // rounding only).
-__global__ void __launch_bounds__(1024) k_truncate(const double *sorted, int n, int mstates, int mblock, double thr,
+// Truncation choice of renormalize_block (src/DMRG_RDM.f90:204-221, right
+// side :277-294) on the descending eigenvalues (negatives read as 0):
+//   Mstates != 0 : m_s = min(Mstates, m_block, n)
+//   else         : m_s = the first minimum over i of |1 - sum(lambda(1:i)) - Estates|
+//                  (minloc of abs(1-cumulate(lambda)-Estates))
+// then extended over every later eigenvalue within deg_evals_threshold
+// (relative) of lambda(m_s); truncation error 1 - sum(lambda(1:m_s)) and the
+// entropy S = -sum lambda log(lambda + 1e-32) (src/DMRG_MAIN.f90:501-518).
+// The prefix sums of the Estates rule: each thread sums a contiguous chunk,
+// the chunk totals are scanned over the block, then every thread walks its
+// chunk again with its offset; ties keep the lowest index.
+__global__ void __launch_bounds__(1024) k_truncate(const double *sorted, int n, int mstates, double estates,
+                                                   int mblock, double thr,
                                                    double *out_d /*trunc, entropy*/, int *out_i /*m_s*/) {
     __shared__ double red_s[32], red_e[32];
     __shared__ int red_c[32];
     __shared__ int ms_s;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int ms = min(mstates, min(mblock, n));
+    if (mstates == 0) {
+        __shared__ double wsum[32];
+        __shared__ double best_v[32];
+        __shared__ int best_i[32];
+        const int per = (n + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int c0 = min(n, tid * per), c1 = min(n, c0 + per);
+        double loc = 0.0;
+        for (int i = c0; i < c1; ++i) loc += sorted[i] < 0.0 ? 0.0 : sorted[i];
+        // inclusive scan of the chunk totals: warps, then the warp totals
+        double inc = loc;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            double t = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0.0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            wsum[lane] = t;
+        }
+        __syncthreads();
+        double run = (warp > 0 ? wsum[warp - 1] : 0.0) + inc - loc;   // sum of all earlier chunks
+        double bv = 1e300;
+        int bi = n;
+        for (int i = c0; i < c1; ++i) {
+            run += sorted[i] < 0.0 ? 0.0 : sorted[i];
+            const double dv = fabs(1.0 - run - estates);
+            if (dv < bv) { bv = dv; bi = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (v2 < bv || (v2 == bv && i2 < bi)) { bv = v2; bi = i2; }
+        }
+        if (lane == 0) { best_v[warp] = bv; best_i[warp] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            double v = best_v[0];
+            int b = best_i[0];
+            for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+                if (best_v[q] < v || (best_v[q] == v && best_i[q] < b)) { v = best_v[q]; b = best_i[q]; }
+            ms_s = b + 1;
+        }
+        __syncthreads();
+        ms = ms_s;
+        __syncthreads();
+    }
     if (ms < 1) ms = 1;
     const double e_ = sorted[ms - 1] < 0.0 ? 0.0 : sorted[ms - 1];
     int cnt = 0;
@@ -544,12 +607,16 @@ void rdm_release(Ctx &c) {
     r = DevRdm{};
 }
 
-int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_side out[2], double *lam_l,
+int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg_thr, nss_rdm_side out[2], double *lam_l,
             double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r, KeptLayout *kl) {
     DevSb &s = c.sb;
     if (!s.valid) { c.err = "nss_rdm: no superblock uploaded"; return NSS_ERR_STATE; }
     if (s.ai.empty() || s.bi.empty()) { c.err = "nss_rdm: descriptor had no ai/bi state maps"; return NSS_ERR_INVALID; }
-    if (mstates < 1) { c.err = "nss_rdm: Mstates must be >= 1 (Edmrg mode is not supported)"; return NSS_ERR_INVALID; }
+    if (mstates < 0) { c.err = "nss_rdm: Mstates must not be negative"; return NSS_ERR_INVALID; }
+    if (mstates == 0 && !(estates != 0.0)) {
+        c.err = "Mdmrg=Edmrg=0 can not fix a threshold for the RDM";
+        return NSS_ERR_INVALID;
+    }
     cudaStream_t st = c.stream;
     DevRdm &r = c.rdm;
     const int nsb = s.nsb, nblk = 2 * nsb;
@@ -944,7 +1011,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double deg_thr, nss_rdm_si
         k_rank<<<(n + 255) / 256, 256, 0, st>>>(r.evals + base, n, r.sorted + base, r.order + base,
                                                 path.empty() ? nullptr : rnk + base);
         ++c.launches;
-        k_truncate<<<1, 1024, 0, st>>>(r.sorted + base, n, mstates, mblk[side], deg_thr, r.scal + 2 * side,
+        k_truncate<<<1, 1024, 0, st>>>(r.sorted + base, n, mstates, estates, mblk[side], deg_thr, r.scal + 2 * side,
                                      r.iscal + side);
     }
     NSS_CUDA_TRY(c, cudaGetLastError());

@@ -1,0 +1,552 @@
+// Tensor-core sector product of the mixed-precision path (tcgen05 + TMA).
+//
+// For every sector k routed here (Dl or Dr at least the context's threshold)
+// it computes the dense part of the direct superblock product
+// (src/DMRG_SUPERBLOCK_SETUP.f90:767-796)
+//     D_k = H_L(k) W_k + W_k H_R(k)^T ,   W_k = psi_k as row-major [Dl x Dr],
+// as a grouped GEMM over work items (sector, 128-row tile of il, BN-column
+// tile of ir, part): part 0 runs both K loops into one accumulator, parts 1
+// and 2 split them (H_L W and W H_R^T) over two CTAs for more parallelism.
+// The A x B terms of these sectors stay on CUDA cores (k_hv_fp32 "terms
+// only" tiles, launched after this kernel), which add D_k from the two
+// output planes this kernel writes.
+//
+// Precision: split TF32.  Every FP32 operand x is split into hi = x rounded
+// to TF32 and lo = (x - hi) rounded to TF32 (so the tensor core's reading of
+// a TF32 operand drops nothing); each K step issues hi.hi + hi.lo + lo.hi
+// (and lo.lo with the context's lolo option) as tcgen05.mma kind::tf32
+// (M=128, N=BN, K=8) into an FP32 accumulator in TMEM: FP32-class products.  H_L and H_R are split once per upload;
+// only W is split per call (k_pack_w).
+//
+// Operand layout for TMA: every operand is stored "K-chunked": for a block X
+// with R rows contracted over K, chunk c (K columns 32c..32c+31) is an
+// [R x 32] FP32 slab (128-byte rows, K beyond the block zero), slabs one
+// after the other.  All slabs of all sectors, hi and lo planes, constant
+// operators and the per-call W planes live in one [rows x 32] FP32 pool, so
+// ONE 2-D tensor map (box 32 x 128 or 32 x BN rows, 128-byte swizzle) loads
+// every tile: the swizzled box is exactly the canonical K-major SW128 layout
+// the UMMA descriptors read.  Rows of a box that run past a block belong to
+// the next slab (finite values) and only reach output rows / columns beyond
+// the block, which the epilogue drops; K padding is zero in every operand.
+//   phase 0 (H_L W):    A = H_L rows il, K = j     B = W^T rows ir, K = il
+//   phase 1 (W H_R^T):  A = W rows il, K = ir       B = H_R rows ir, K = j
+//
+// Kernel: persistent, one CTA per SM, 6 warps.  Warp 0 (one lane) issues the
+// TMA loads into a ring of shared-memory stages (mbarrier full/empty pairs);
+// warp 1 (one lane) issues the MMAs of each 32-wide K slab into a fresh TMEM
+// accumulator and commits the stage back to the producer and the slab's
+// partial product to the epilogue; warps 2-5 read the partials out of TMEM
+// (tcgen05.ld, each warp its 32 lanes) and sum them in FP32 registers, then
+// store the item's tile.  Two TMEM buffers alternate, so draining one slab
+// overlaps the MMAs of the next.  The per-slab promotion matters: the
+// tensor core's FP32 accumulation does not round to nearest, and over a
+// whole K loop of ~350 its error grew to 5x that of an FP32 FMA chain
+// (measured RMS 1.8e-6 against 3.6e-7), enough to cost the mixed solver a
+// third more iterations; over one slab it stays below the FMA chain's.  Every wait is bounded (wait_limit):
+// a wait that runs out sets the error word, every role stops, the producer
+// waits for the copies it issued, the MMA lane for its MMAs, and the CTA
+// frees its TMEM and returns.
+#include "sector_mma.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace nss {
+
+namespace {
+
+constexpr int MM_THREADS = 192;            // 6 warps
+constexpr int MM_SMEM_BUDGET = 200 * 1024; // operand stages
+
+// instruction descriptor, kind::tf32: D FP32, A and B TF32, both K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int bn) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(MM_M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), start address in 16-byte units
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;                 // LBO (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;       // SBO
+    d |= (uint64_t)1 << 46;                 // descriptor version
+    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// bounded wait for the phase of the given parity; false when it ran out or
+// when another role has already given up (*abort)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t spin, volatile int *abort) {
+    for (uint32_t it = 0; it <= spin; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((it & 63u) == 63u && *abort) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+}  // namespace
+
+// Pack one operator block X [d x d] (row-major FP32) into its K-chunked hi
+// and lo slabs: slab c row r = X[r][32c .. 32c+31] (zero beyond d).
+// One thread per (slab row, K column) element.
+__global__ void __launch_bounds__(256) k_pack_h(const float *__restrict__ x, int d, float *__restrict__ hi,
+                                                float *__restrict__ lo) {
+    const int nch = (d + MM_KC - 1) / MM_KC;
+    const int64_t total = (int64_t)nch * d * MM_KC;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int kk = (int)(e % MM_KC);
+        const int64_t rr = e / MM_KC;
+        const int r = (int)(rr % d), c = (int)(rr / d);
+        const int j = c * MM_KC + kk;
+        const float v = j < d ? x[(int64_t)r * d + j] : 0.f;
+        const float h = tf32_hi(v);
+        hi[e] = h;
+        lo[e] = tf32_hi(v - h);
+    }
+}
+
+// Per call: W of every routed sector into its two K-chunked operands, hi and
+// lo.  One CTA per 32 x 32 tile of W_k (tile list `wt`: sector, il0, ir0):
+//   W1 (phase 1 A): slab c = ir0/32, row il:  W[il][ir0..ir0+31]
+//   W0 (phase 0 B): slab c = il0/32, row ir:  W[il0..il0+31][ir]   (transposed through shared memory)
+// with zeros beyond the block on the K side.  `scale` multiplies W.
+__global__ void __launch_bounds__(256) k_pack_w(const float *__restrict__ v, float scale,
+                                                const int4 *__restrict__ wt, const PackSec *__restrict__ sec,
+                                                float *__restrict__ pool, int64_t plane, const int *stop) {
+    if (stop && *stop) return;
+    __shared__ float t[32][33];
+    const int4 w = wt[blockIdx.x];
+    const PackSec s = sec[w.x];
+    const int il0 = w.y, ir0 = w.z;
+    const float *W = v + s.off;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 32 lanes
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int il = il0 + ty + 8 * q, ir = ir0 + tx;
+        const float x = (il < s.dl && ir < s.dr) ? W[(int64_t)il * s.dr + ir] * scale : 0.f;
+        t[ty + 8 * q][tx] = x;
+        if (il < s.dl) {   // W1 row il of slab ir0/32, K column tx (zero beyond Dr)
+            const int64_t p = ((int64_t)s.w1_row + (int64_t)(ir0 / MM_KC) * s.dl + il) * MM_KC + tx;
+            const float h = tf32_hi(x);
+            pool[p] = h;
+            pool[p + plane] = tf32_hi(x - h);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ir = ir0 + ty + 8 * q;
+        if (ir < s.dr) {   // W0 row ir of slab il0/32, K column tx = il - il0 (zero beyond Dl)
+            const float x = t[tx][ty + 8 * q];
+            const int64_t p = ((int64_t)s.w0_row + (int64_t)(il0 / MM_KC) * s.dr + ir) * MM_KC + tx;
+            const float h = tf32_hi(x);
+            pool[p] = h;
+            pool[p + plane] = tf32_hi(x - h);
+        }
+    }
+}
+
+template <int BN>
+struct MmaCfg {
+    static constexpr int A_BYTES = MM_M * 128;                 // one plane of an A box
+    static constexpr int B_BYTES = BN * 128;
+    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;    // hi and lo of A and B
+    static constexpr int STAGES = MM_SMEM_BUDGET / STAGE;
+    static constexpr int SMEM = STAGES * STAGE + 1024;         // + alignment slack
+    static constexpr uint32_t TCOLS = 2 * BN;                  // two accumulators
+};
+
+template <int BN>
+__global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_constant__ CUtensorMap map_a,
+                                                               const __grid_constant__ CUtensorMap map_b,
+                                                               const MmaItem *__restrict__ items, int nitems,
+                                                               int plane_rows, float *__restrict__ out0,
+                                                               float *__restrict__ out1, int lolo, uint32_t spin,
+                                                               int *err, const int *stop) {
+    using C = MmaCfg<BN>;
+    constexpr int S = C::STAGES;
+    if (stop && *stop) return;   // before any TMEM allocation: uniform exit
+    extern __shared__ uint8_t mm_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)mm_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(smem_u32(&tfull[a]), 1);
+            mbar_init(smem_u32(&tempty[a]), 4);   // one arrival per epilogue warp
+        }
+        mbar_init(smem_u32(&drain), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_a) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_b) : "memory");
+        abort_s = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(C::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    volatile int *abort = &abort_s;
+    auto give_up = [&]() {
+        *abort = 1;
+        atomicExch(err, 1);
+    };
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        int it = 0;                   // stage fills issued so far
+        int last_par[S];
+        bool inflight[S];
+        for (int s = 0; s < S; ++s) inflight[s] = false;
+        for (int i = blockIdx.x; i < nitems && !*abort; i += gridDim.x) {
+            const MmaItem m = items[i];
+            const int nk = m.nk0 + m.nk1;
+            for (int c = 0; c < nk; ++c, ++it) {
+                const int s = it % S;
+                const uint32_t par = (uint32_t)(it / S) & 1u;
+                if (!mbar_wait(smem_u32(&empty[s]), par ^ 1u, spin, abort)) { give_up(); break; }
+                const bool p0 = c < m.nk0;
+                const int cc = p0 ? c : c - m.nk0;
+                const int ar = (p0 ? m.a_row0 : m.a_row1) + cc * m.a_step + m.m0;
+                const int br = (p0 ? m.b_row0 : m.b_row1) + cc * m.b_step + m.n0;
+                uint8_t *st = smem + (size_t)s * C::STAGE;
+                const uint32_t fb = smem_u32(&full[s]);
+                mbar_expect_tx(fb, (uint32_t)C::STAGE);
+                tma_load_2d(smem_u32(st), &map_a, 0, ar, fb);
+                tma_load_2d(smem_u32(st + C::A_BYTES), &map_a, 0, ar + plane_rows, fb);
+                tma_load_2d(smem_u32(st + 2 * C::A_BYTES), &map_b, 0, br, fb);
+                tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), &map_b, 0, br + plane_rows, fb);
+                inflight[s] = true;
+                last_par[s] = (int)par;
+            }
+        }
+        // no copy of this CTA may still be landing when it leaves (bounded,
+        // and not cut short by the abort flag)
+        volatile int never = 0;
+        for (int s = 0; s < S; ++s)
+            if (inflight[s] && !mbar_wait(smem_u32(&full[s]), (uint32_t)last_par[s], spin, &never)) atomicExch(err, 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer: every slab into a fresh accumulator buffer (two
+        // alternate), which the epilogue drains into FP32 registers
+        constexpr uint32_t IDESC = idesc_tf32(BN);
+        int it = 0;                   // slabs issued (= stage fills consumed, = accumulator uses)
+        bool issued = false;
+        for (int i = blockIdx.x; i < nitems && !*abort; i += gridDim.x) {
+            const MmaItem m = items[i];
+            const int nk = m.nk0 + m.nk1;
+            bool ok = true;
+            for (int c = 0; c < nk; ++c, ++it) {
+                const int s = it % S, acc = it & 1;
+                const uint32_t par = (uint32_t)(it / S) & 1u;
+                const uint32_t tacc = tmem + (uint32_t)(acc * BN);
+                // the epilogue has drained this buffer (its use two slabs ago)
+                if (!mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(it >> 1) & 1u) ^ 1u, spin, abort) ||
+                    !mbar_wait(smem_u32(&full[s]), par, spin, abort)) {
+                    give_up();
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a_hi = smem_u32(smem + (size_t)s * C::STAGE), a_lo = a_hi + C::A_BYTES;
+                const uint32_t b_hi = a_hi + 2 * C::A_BYTES, b_lo = b_hi + C::B_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < MM_KC / 8; ++kk) {
+                    const uint32_t o = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzled row
+                    mma_tf32(tacc, desc_sw128(a_hi + o), desc_sw128(b_hi + o), IDESC, kk > 0 ? 1u : 0u);
+                    mma_tf32(tacc, desc_sw128(a_hi + o), desc_sw128(b_lo + o), IDESC, 1u);
+                    mma_tf32(tacc, desc_sw128(a_lo + o), desc_sw128(b_hi + o), IDESC, 1u);
+                    if (lolo) mma_tf32(tacc, desc_sw128(a_lo + o), desc_sw128(b_lo + o), IDESC, 1u);
+                }
+                issued = true;
+                mma_commit(smem_u32(&empty[s]));     // the stage is free once these MMAs have read it
+                mma_commit(smem_u32(&tfull[acc]));   // ... and the slab's partial product is ready
+            }
+            if (!ok) break;
+        }
+        if (issued) {   // every MMA of this lane done before the CTA frees its TMEM
+            mma_commit(smem_u32(&drain));
+            volatile int never = 0;
+            if (!mbar_wait(smem_u32(&drain), 0u, spin, &never)) atomicExch(err, 1);
+        }
+    } else if (warp >= 2) {
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows)
+        // and sums the slab partials of an item in FP32 registers; the
+        // tensor core's own accumulation then spans one slab only (12 or 16
+        // MMAs), which keeps the product as accurate as FP32 FMA chains
+        const int q = warp & 3;
+        int it = 0;
+        for (int i = blockIdx.x; i < nitems && !*abort; i += gridDim.x) {
+            const MmaItem m = items[i];
+            const int nk = m.nk0 + m.nk1;
+            float sum[BN];
+#pragma unroll
+            for (int j = 0; j < BN; ++j) sum[j] = 0.f;
+            bool ok = true;
+            for (int c = 0; c < nk; ++c, ++it) {
+                const int acc = it & 1;
+                bool got = true;
+                if (lane == 0) got = mbar_wait(smem_u32(&tfull[acc]), (uint32_t)(it >> 1) & 1u, spin, abort);
+                if (__shfl_sync(0xffffffffu, got ? 1 : 0, 0) == 0) {
+                    if (lane == 0) give_up();
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                for (int c0 = 0; c0 < BN; c0 += 16) {
+                    uint32_t r[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15])
+                        : "r"(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * BN + c0)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) sum[c0 + j] += __uint_as_float(r[j]);
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&tempty[acc]));
+            }
+            if (!ok) break;
+            const int il = m.m0 + 32 * q + lane;
+            if (il < m.dl) {
+                float *dst = (m.out ? out1 : out0) + m.off + (int64_t)il * m.dr;
+#pragma unroll
+                for (int j = 0; j < BN; ++j)
+                    if (m.n0 + j < m.dr) dst[m.n0 + j] = sum[j];
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TCOLS));
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+template <int BN>
+int set_smem_attr(Ctx &c) {
+    static bool done = false;
+    if (!done) {
+        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_sector_mma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             MmaCfg<BN>::SMEM));
+        done = true;
+    }
+    return NSS_OK;
+}
+
+}  // namespace
+
+void mma_layout(const DevSb &s, int tc_min_dl, int bn, bool split, MmaPlan &p) {
+    p = MmaPlan{};
+    p.bn = bn == 128 ? 128 : 64;
+    p.split = split;
+    for (int k = 0; k < s.nsb; ++k)
+        if (tc_min_dl > 0 && s.dls[k] >= tc_min_dl) p.sectors.push_back(k);
+    if (p.sectors.empty()) return;
+    // pool rows, per plane: [H_L slabs | H_R slabs | W0 slabs | W1 slabs] of
+    // every routed sector; lo planes follow the hi planes at +plane_rows
+    auto slabs = [](int d) { return (d + MM_KC - 1) / MM_KC; };
+    int64_t r = 0;
+    for (size_t i = 0; i < p.sectors.size(); ++i) {
+        const int k = p.sectors[i], dl = s.dls[k], dr = s.drs[k];
+        PackSec ps{dl, dr, 0, 0, s.off[k]};
+        p.hl_row.push_back((int)r); r += (int64_t)slabs(dl) * dl;
+        p.hr_row.push_back((int)r); r += (int64_t)slabs(dr) * dr;
+        ps.w0_row = (int)r; r += (int64_t)slabs(dl) * dr;
+        ps.w1_row = (int)r; r += (int64_t)slabs(dr) * dl;
+        p.ps.push_back(ps);
+        for (int a = 0; a < dl; a += 32)
+            for (int b = 0; b < dr; b += 32) p.wt.push_back(make_int4((int)i, a, b, 0));
+    }
+    r += MM_M;   // a box that starts near the end of a plane stays inside it
+    p.plane_rows = r;
+    for (size_t i = 0; i < p.sectors.size(); ++i) {
+        const int k = p.sectors[i], dl = s.dls[k], dr = s.drs[k];
+        for (int m0 = 0; m0 < dl; m0 += MM_M)
+            for (int n0 = 0; n0 < dr; n0 += p.bn) {
+                MmaItem m{};
+                m.a_row0 = p.hl_row[i];
+                m.b_row0 = p.ps[i].w0_row;
+                m.a_row1 = p.ps[i].w1_row;
+                m.b_row1 = p.hr_row[i];
+                m.a_step = dl;
+                m.b_step = dr;
+                m.dl = dl; m.dr = dr; m.m0 = m0; m.n0 = n0; m.off = s.off[k];
+                if (split) {
+                    m.nk0 = slabs(dl); m.nk1 = 0; m.out = 0;
+                    p.items.push_back(m);
+                    m.nk0 = 0; m.nk1 = slabs(dr); m.out = 1;
+                    p.items.push_back(m);
+                } else {
+                    m.nk0 = slabs(dl); m.nk1 = slabs(dr); m.out = 0;
+                    p.items.push_back(m);
+                }
+            }
+    }
+    // longest first: with the static round-robin over CTAs the long items start at once
+    std::stable_sort(p.items.begin(), p.items.end(),
+                     [](const MmaItem &a, const MmaItem &b) { return a.nk0 + a.nk1 > b.nk0 + b.nk1; });
+}
+
+int mma_finish(Ctx &c, const MmaPlan &p) {
+    DevSb &s = c.sb;
+    if (p.items.empty()) return NSS_OK;
+    const int64_t pl = p.plane_rows * MM_KC;
+    NSS_CUDA_TRY(c, cudaMemsetAsync(s.d_mma_pool, 0, (size_t)(2 * pl) * sizeof(float), c.stream));
+    NSS_CUDA_TRY(c, cudaMemsetAsync(s.d_mma_out, 0, (size_t)(2 * s.n) * sizeof(float), c.stream));
+    auto slabs = [](int d) { return (d + MM_KC - 1) / MM_KC; };
+    for (size_t i = 0; i < p.sectors.size(); ++i) {
+        const int k = p.sectors[i], dl = s.dls[k], dr = s.drs[k];
+        float *q = s.d_mma_pool;
+        k_pack_h<<<(unsigned)std::min<int64_t>(1024, ((int64_t)slabs(dl) * dl * MM_KC + 255) / 256), 256, 0,
+                   c.stream>>>(s.d_hl32 + s.hl_off[k], dl, q + (int64_t)p.hl_row[i] * MM_KC,
+                               q + pl + (int64_t)p.hl_row[i] * MM_KC);
+        k_pack_h<<<(unsigned)std::min<int64_t>(1024, ((int64_t)slabs(dr) * dr * MM_KC + 255) / 256), 256, 0,
+                   c.stream>>>(s.d_hr32 + s.hr_off[k], dr, q + (int64_t)p.hr_row[i] * MM_KC,
+                               q + pl + (int64_t)p.hr_row[i] * MM_KC);
+        c.launches += 2;
+    }
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    s.mma_nitems = (int)p.items.size();
+    s.mma_nwt = (int)p.wt.size();
+    s.mma_plane_rows = (int)p.plane_rows;
+    s.mma_bn = p.bn;
+    s.mma_split = p.split;
+    // two tensor maps over the whole pool, [2 plane rows] x 32 FP32 with
+    // 128-byte rows and the 128-byte swizzle: boxes of 128 rows (A) and of
+    // BN rows (B)
+    auto enc = encode_fn();
+    if (!enc) {
+        c.err = "nss_sb_upload: cuTensorMapEncodeTiled is not available from the driver";
+        return NSS_ERR_CUDA;
+    }
+    const cuuint64_t gdim[2] = {(cuuint64_t)MM_KC, (cuuint64_t)(2 * p.plane_rows)};
+    const cuuint64_t gstride[1] = {(cuuint64_t)MM_KC * sizeof(float)};
+    const cuuint32_t estr[2] = {1, 1};
+    for (int which = 0; which < 2; ++which) {
+        alignas(64) CUtensorMap map;
+        const cuuint32_t box[2] = {(cuuint32_t)MM_KC, (cuuint32_t)(which == 0 ? MM_M : p.bn)};
+        const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)s.d_mma_pool, gdim, gstride, box,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS) {
+            c.err = "nss_sb_upload: cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")";
+            return NSS_ERR_CUDA;
+        }
+        static_assert(sizeof(CUtensorMap) == sizeof(s.mma_map_a), "tensor map storage");
+        std::memcpy(which == 0 ? s.mma_map_a : s.mma_map_b, &map, sizeof(map));
+    }
+    return NSS_OK;
+}
+
+// D_k of every routed sector into the two output planes (d_mma_out, d_mma_out
+// + n): pack W, then the persistent GEMM.  The caller's "terms only" tiles
+// add the planes to their A x B terms.
+int hv_device_mma(Ctx &c, const float *d_v, const int *stop) {
+    DevSb &s = c.sb;
+    if (s.mma_nitems == 0) return NSS_OK;
+    int nsm = 0;
+    NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    const int64_t pl = (int64_t)s.mma_plane_rows * MM_KC;
+    k_pack_w<<<s.mma_nwt, 256, 0, c.stream>>>(d_v, 1.0f, s.d_mma_wt, s.d_mma_sec, s.d_mma_pool, pl, stop);
+    const int grid = std::min(s.mma_nitems, nsm);
+    const uint32_t spin = wait_limit();
+    float *o0 = s.d_mma_out, *o1 = s.d_mma_out + s.n;
+    alignas(64) CUtensorMap ma, mb;
+    std::memcpy(&ma, s.mma_map_a, sizeof(ma));
+    std::memcpy(&mb, s.mma_map_b, sizeof(mb));
+    if (s.mma_bn == 128) {
+        if (int rc = set_smem_attr<128>(c)) return rc;
+        k_sector_mma<128><<<grid, MM_THREADS, MmaCfg<128>::SMEM, c.stream>>>(
+            ma, mb, s.d_mma_items, s.mma_nitems, s.mma_plane_rows, o0, o1, c.mma_lolo ? 1 : 0, spin, s.d_tc_err, stop);
+    } else {
+        if (int rc = set_smem_attr<64>(c)) return rc;
+        k_sector_mma<64><<<grid, MM_THREADS, MmaCfg<64>::SMEM, c.stream>>>(
+            ma, mb, s.d_mma_items, s.mma_nitems, s.mma_plane_rows, o0, o1, c.mma_lolo ? 1 : 0, spin, s.d_tc_err, stop);
+    }
+    c.launches += 2;
+    NSS_CUDA_TRY(c, cudaGetLastError());
+    return NSS_OK;
+}
+
+}  // namespace nss

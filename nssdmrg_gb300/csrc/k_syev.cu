@@ -374,11 +374,10 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
 
 // Bounded barrier of one CTA group of k_trd_grid (cooperative launch, all
 // CTAs resident): barrier e of a launch waits for e * G arrivals on *bar, G
-// the group's CTAs; a wait that runs past TG_SPIN polls sets *err, and every
+// the group's CTAs; a wait that runs past `spin` polls sets *err, and every
 // later barrier (of any group) returns false at once, so the kernel always
 // ends.  The counters and *err are zero at launch.
-constexpr uint32_t TG_SPIN = 1u << 22;
-__device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned G, unsigned &epoch, int *err) {
+__device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned G, unsigned &epoch, int *err, uint32_t spin) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -391,10 +390,8 @@ __device__ __forceinline__ bool tg_sync(unsigned *bar, unsigned G, unsigned &epo
             unsigned v;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
             if (v >= epoch) break;
-            if ((++it & 255u) == 0) {
-                if (*(volatile int *)err) { good = 0; break; }
-                if (it > TG_SPIN) { atomicExch(err, 1); good = 0; break; }
-            }
+            if (++it > spin) { atomicExch(err, 1); good = 0; break; }
+            if ((it & 255u) == 0 && *(volatile int *)err) { good = 0; break; }
         }
         ok = good;
     }
@@ -411,6 +408,7 @@ struct TgGroups {
     int q[TG_MAXG];
     int c0[TG_MAXG + 1];
     int64_t goff[TG_MAXG], coff[TG_MAXG];
+    uint32_t spin;               // poll limit of the group barriers (wait_limit)
 };
 
 // The Householder reduction of very large blocks by the whole GPU (a
@@ -454,7 +452,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
     if (r == 0)
         for (int i = tid; i < n; i += TRD_THREADS) perm[eo + i] = i;
     unsigned epoch = 0;
-    bool alive = tg_sync(bar, G, epoch, err);
+    bool alive = tg_sync(bar, G, epoch, err, grp.spin);
     for (int k = 0; alive && k + 2 < n; ++k) {
         const int m = n - k - 1, par = k & 1, o = k % G;
         double *vb = gv + par * (int64_t)n, *pb = gp + par * (int64_t)n, *sb = gs + par * G;
@@ -490,7 +488,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 Vq[(int64_t)k * n + k + 1 + i] = x;
             }
         }
-        if (!(alive = tg_sync(bar, G, epoch, err))) break;   // v and t of step k published
+        if (!(alive = tg_sync(bar, G, epoch, err, grp.spin))) break;   // v and t of step k published
         const double t = *(volatile double *)(gt + par);
         for (int i = tid; i < m; i += TRD_THREADS) v[i] = ((volatile double *)vb)[i];
         __syncthreads();
@@ -520,7 +518,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
             for (int u = 0; u < NW; ++u) x += red[u];
             sb[r] = x;
         }
-        if (!(alive = tg_sync(bar, G, epoch, err))) break;   // p and the p.v shares published
+        if (!(alive = tg_sync(bar, G, epoch, err, grp.spin))) break;   // p and the p.v shares published
         if (warp == 0) {
             double x = 0.0;
             for (int u = lane; u < G; u += 32) x += ((volatile double *)sb)[u];
@@ -1544,6 +1542,7 @@ int syev_trd_grid(const double *rho, const int64_t *rho_off, const int *dims, co
         const int ng = (int)std::min<size_t>(per, blocks.size() - b0);
         TgGroups grp{};
         grp.ng = ng;
+        grp.spin = wait_limit();
         double w3[TG_MAXG], wsum3 = 0.0;
         for (int g = 0; g < ng; ++g) {
             const double x = nb[b0 + g];

@@ -42,6 +42,9 @@ def lib():
         L.ref_lanczos.argtypes = [C.POINTER(_Desc), C.c_int, C.c_int, C.c_double, C.c_uint64, C.c_int,
                                   C.c_void_p, C.POINTER(C.c_int)]
         L.ref_lanczos.restype = C.c_int
+        L.ref_lanczos_vec.argtypes = [C.POINTER(_Desc), C.c_int, C.c_int, C.c_double, C.c_uint64, C.c_int,
+                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
+        L.ref_lanczos_vec.restype = C.c_int
         L.ref_max_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -120,3 +123,12 @@ class RefSuperblock:
         rc = lib().ref_lanczos(C.byref(self.desc), neigen, nitermax, tol, seed, nthreads, ev.ctypes.data,
                                C.byref(numop))
         return ev[:neigen], numop.value, rc
+
+    def lanczos_vectors(self, neigen=1, nitermax=512, tol=1e-12, seed=1234, nthreads=1):
+        """As lanczos, plus the unit Ritz vectors as the columns of an n x neigen array."""
+        ev = np.zeros(max(1, neigen))
+        vec = np.zeros((max(1, neigen), self.n))
+        numop = C.c_int()
+        rc = lib().ref_lanczos_vec(C.byref(self.desc), neigen, nitermax, tol, seed, nthreads, ev.ctypes.data,
+                                   vec.ctypes.data, C.byref(numop))
+        return ev[:neigen], vec[:neigen].T.copy(), numop.value, rc

@@ -42,6 +42,8 @@ class Params:
     Ldmrg: int = 10
     Mdmrg: int = 64
     Msweep: tuple = ()
+    Edmrg: float = 0.0                 # INPUT_VARS.f90:18, used when Mdmrg == 0
+    Esweep: tuple = ()                 # :35, default Edmrg per sweep
     dmrg_qn: tuple = (0.0,)            # DMRG_QN, QNtype=local
     norb: int = 1
     lanc_neigen: int = 2               # INPUT_VARS.f90:275
@@ -582,12 +584,20 @@ def eigh_blocks(blocks) -> RhoBlocks:
     return RhoBlocks(qns, maps, evals, evecs, evalues, eorder)
 
 
-def truncation(rho: RhoBlocks, mstates: int, m_block: int, deg_thr: float):
-    """renormalize_block selection (src/DMRG_RDM.f90:204-221): m_s=min(M,m,#λ),
-    extended over every later λ within deg_thr (relative) of λ(m_s);
-    truncation error 1 - sum(λ(1:m_s)).  λ<0 clipped to 0 (:88,:97)."""
+def truncation(rho: RhoBlocks, mstates: int, m_block: int, deg_thr: float, estates: float = 0.0):
+    """renormalize_block selection (src/DMRG_RDM.f90:204-221): m_s=min(M,m,#λ)
+    when Mstates != 0, else (Estates != 0) the first minimum of
+    |1 - cumulate(λ)(i) - Estates| (:206-208, cumulate_D in
+    src/AUX_FUNCS.f90:133-143: running sums left to right); then extended
+    over every later λ within deg_thr (relative) of λ(m_s); truncation error
+    1 - sum(λ(1:m_s)).  λ<0 clipped to 0 (:88,:97)."""
     lam = np.where(rho.evalues < 0.0, 0.0, rho.evalues)
-    m_s = min(mstates, m_block, lam.size)
+    if mstates != 0:
+        m_s = min(mstates, m_block, lam.size)
+    elif estates != 0.0:
+        m_s = int(np.argmin(np.abs(1.0 - np.cumsum(lam) - estates))) + 1
+    else:
+        raise ValueError("Mdmrg=Edmrg=0 can not fix a threshold for the RDM")
     e_ = lam[m_s - 1]
     ext = 0
     with np.errstate(divide="ignore", invalid="ignore"):
@@ -743,9 +753,10 @@ class DMRG:
     def step(self, kind="i", label=0, sweep=None):
         p = self.p
         if kind == "i":
-            mstates = p.Mdmrg
+            mstates, estates = p.Mdmrg, p.Edmrg
         else:
             mstates = (p.Msweep or (p.Mdmrg,))[sweep - 1]
+            estates = (p.Esweep or (p.Edmrg,) * max(1, len(p.Msweep)))[sweep - 1]
         m_left0, m_right0 = self.left.dim, self.right.dim
         self.left = enlarge_block(self.left, self.dot, "l", self.hij, p.norb)
         self.right = enlarge_block(self.right, self.dot, "r", self.hij, p.norb)
@@ -772,7 +783,7 @@ class DMRG:
             for side in ("l", "r"):
                 blk = self.left if side == "l" else self.right
                 rho = rho_l if side == "l" else rho_r
-                m_s, eps = truncation(rho, mstates, blk.dim, p.deg_evals_threshold)
+                m_s, eps = truncation(rho, mstates, blk.dim, p.deg_evals_threshold, estates)
                 u = rotation_matrix(rho, blk.dim, m_s)
                 nb = renormalize(blk, u, kept_qns(rho, m_s))
                 if side == "l":

@@ -190,8 +190,10 @@ static double tri_eig(const double *a, const double *b, int m, int e, double *s,
 /* Lowest `neigen` eigenvalues of the superblock H; returns 0 when converged,
  * 1 when nitermax was reached.  The matvec is ref_hv_omp (nthreads > 1) or
  * ref_hv_serial; the numop and the time split are reported to the caller. */
-int ref_lanczos(const nss_sb_desc *d, int neigen, int nitermax, double tol, uint64_t seed, int nthreads,
-                double *evals, int *numop) {
+/* ref_lanczos_vec: as ref_lanczos, and when evecs is not NULL it also
+ * receives the neigen Ritz vectors (row e = vector e, unit norm). */
+int ref_lanczos_vec(const nss_sb_desc *d, int neigen, int nitermax, double tol, uint64_t seed, int nthreads,
+                    double *evals, double *evecs, int *numop) {
     const int64_t n = sb_n(d);
     int mmax = nitermax < n ? nitermax : (int)n;
     double *V = (double *)malloc(sizeof(double) * n * (size_t)(mmax + 1));
@@ -271,10 +273,29 @@ int ref_lanczos(const nss_sb_desc *d, int neigen, int nitermax, double tol, uint
 #pragma omp parallel for num_threads(nthreads)
         for (int64_t i = 0; i < n; ++i) vn[i] = w[i] * inv;
     }
-    for (int e = 0; e < neigen && e < m; ++e) evals[e] = tri_eig(alpha, beta, m, e, s, work);
+    for (int e = 0; e < neigen && e < m; ++e) {
+        evals[e] = tri_eig(alpha, beta, m, e, s, work);
+        if (!evecs) continue;
+        double *x = evecs + (size_t)e * n, nx = 0.0;
+#pragma omp parallel for num_threads(nthreads) reduction(+ : nx)
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int l = 0; l < m; ++l) acc += s[l] * V[(size_t)l * n + i];
+            x[i] = acc;
+            nx += acc * acc;
+        }
+        nx = 1.0 / sqrt(nx);
+#pragma omp parallel for num_threads(nthreads)
+        for (int64_t i = 0; i < n; ++i) x[i] *= nx;
+    }
     if (numop) *numop = ops;
     free(V); free(w); free(h); free(alpha); free(beta); free(s); free(work);
     return conv >= neigen ? 0 : 1;
+}
+
+int ref_lanczos(const nss_sb_desc *d, int neigen, int nitermax, double tol, uint64_t seed, int nthreads,
+                double *evals, int *numop) {
+    return ref_lanczos_vec(d, neigen, nitermax, tol, seed, nthreads, evals, NULL, numop);
 }
 
 int ref_max_threads(void) {

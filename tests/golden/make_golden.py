@@ -151,6 +151,27 @@ def oracle_runs():
         "energy": [r.energies.tolist() for r in run.records],
         "entropy": [r.entropy_left for r in run.records], "N": [r.N for r in run.records],
         "trunc": [r.trunc_left for r in run.records]}
+    # the error-threshold truncation (Mdmrg = 0, Edmrg != 0; src/DMRG_RDM.f90:206-208):
+    # spin-1 L=20 grown at Edmrg=1e-6, then one finite sweep at Esweep=1e-7
+    p = O.Params(Ldmrg=10, Mdmrg=0, Edmrg=1e-6, Msweep=(0,), Esweep=(1e-7,), lanc_neigen=1, dmrg_qn=(0.0,))
+    run = O.DMRG(O.heisenberg_hij(), O.spin_site(3), p)
+    run.finite()
+    res["spin1_L20_E1e-6_sweep_E1e-7"] = {
+        "model": "heisenberg_one", "ldmrg": 10, "mdmrg": 0, "edmrg": 1e-6, "msweep": [0], "esweep": [1e-7],
+        "neigen": 1, "dmrg_qn": [0.0],
+        "kind": [r.kind for r in run.records], "left_length": [r.left_length for r in run.records],
+        "energy": [r.energies.tolist() for r in run.records],
+        "entropy": [r.entropy_left for r in run.records], "N": [r.N for r in run.records],
+        "trunc": [r.trunc_left for r in run.records], "m_left": [r.m_left for r in run.records]}
+    p = O.Params(Ldmrg=8, Mdmrg=0, Edmrg=1e-5, lanc_neigen=1, dmrg_qn=(0.5, 0.5))
+    run = O.DMRG(O.hubbard_hij(1.0), O.electron_site(4.0, False), p)
+    run.infinite()
+    res["hubbard_U4_L16_E1e-5"] = {
+        "model": "hubbard", "ldmrg": 8, "mdmrg": 0, "edmrg": 1e-5, "neigen": 1, "u": 4.0, "hfmode": False,
+        "dmrg_qn": [0.5, 0.5], "left_length": [r.left_length for r in run.records],
+        "energy": [r.energies.tolist() for r in run.records],
+        "entropy": [r.entropy_left for r in run.records], "N": [r.N for r in run.records],
+        "trunc": [r.trunc_left for r in run.records], "m_left": [r.m_left for r in run.records]}
     (OUT / "oracle_runs.json").write_text(json.dumps(res))
 
 

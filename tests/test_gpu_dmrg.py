@@ -21,7 +21,8 @@ def _run(nss, t, finite=False):
                  u=t.get("u", 0.0), hfmode=t.get("hfmode", True),
                  dmrg_qn=tuple(t["dmrg_qn"]) + ((0.0,) if len(t["dmrg_qn"]) == 1 else ()),
                  lanc_neigen=t["neigen"], lanc_tolerance=1e-12,
-                 deg_evals_threshold=t.get("deg_evals_threshold", 0.1))
+                 deg_evals_threshold=t.get("deg_evals_threshold", 0.1),
+                 edmrg=t.get("edmrg", 0.0), esweep=t.get("esweep", ()))
     recs = d.finite() if finite else d.infinite()
     return recs
 
@@ -50,6 +51,21 @@ def test_oracle_trajectory(nss, oracle_runs, key):
     np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-9, atol=0)
     assert [r["n"] for r in recs] == t["N"]
     np.testing.assert_allclose([r["trunc_left"] for r in recs], t["trunc"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("key,finite", [("hubbard_U4_L16_E1e-5", False), ("spin1_L20_E1e-6_sweep_E1e-7", True)])
+def test_error_threshold_trajectory(nss, oracle_runs, key, finite):
+    """Whole runs with the Edmrg truncation (Mdmrg = 0; src/DMRG_RDM.f90:
+    206-208): the kept dimensions chosen by the error threshold, the energies
+    and the truncation errors against the oracle's run."""
+    t = oracle_runs[key]
+    recs = _run(nss, t, finite=finite)
+    assert [r["left_length"] for r in recs] == t["left_length"]
+    assert [r["m_left"] for r in recs] == t["m_left"]
+    assert [r["n"] for r in recs] == t["N"]
+    e = np.array([r["energy"][0] for r in recs])
+    np.testing.assert_allclose(e, np.array(t["energy"])[:, 0], rtol=1e-10, atol=0)
+    np.testing.assert_allclose([r["trunc_left"] for r in recs], t["trunc"], rtol=1e-8, atol=1e-13)
 
 
 def test_finite_sweeps_c1(nss, oracle_runs):

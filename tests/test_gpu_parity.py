@@ -231,6 +231,52 @@ def test_fp32_and_tensor_core_products_match_fp64(nss, c2_superblock):
     assert abs(emx[0] - e64[0]) <= 1e-10 * abs(e64[0])
 
 
+@pytest.fixture(scope="module")
+def spin1_superblock_desc(nss):
+    """Last infinite step of the spin-1 chain L=32, m=256 (sectors up to ~190
+    states: two 128-row tiles per sector on the tensor cores)."""
+    d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 16, 256, dmrg_qn=(0.0, 0.0), lanc_neigen=1)
+    d.prepare_last()
+    yield d.export_superblock()
+    d.close()
+
+
+@pytest.mark.parametrize("bn,split", [(64, 1), (64, 0), (128, 1), (128, 0)])
+@pytest.mark.parametrize("case", ["hubbard_L32_M256", "spin1_L32_M256"])
+def test_tensor_core_tiles_match_fp64(nss, c2_superblock, spin1_superblock_desc, monkeypatch, case, bn, split):
+    """The TMA-fed tcgen05 sector GEMM (3xTF32, every sector with Dl >= 32
+    routed to it) for each tile width and K-loop split, against the FP64
+    product on the same superblock: FP32-class accuracy, 4e-6 of the largest
+    entry (few-hundred-term FP32 sums with cancellation)."""
+    import torch
+    desc = c2_superblock.export_superblock() if case.startswith("hubbard") else spin1_superblock_desc
+    monkeypatch.setenv("NSS_TC_MIN_DL", "32")
+    monkeypatch.setenv("NSS_TC_BN", str(bn))
+    monkeypatch.setenv("NSS_TC_SPLIT", str(split))
+    s = nss.Superblock()
+    s.upload_desc(desc)
+    ref = nss.Superblock()
+    monkeypatch.setenv("NSS_TC_MIN_DL", "0")
+    ref.upload_desc(desc)
+    n = s.n
+    g = torch.Generator(device="cuda").manual_seed(7)
+    for call in range(2):
+        v64 = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        v32 = v64.float()
+        h64 = torch.empty_like(v64)
+        h32 = torch.empty_like(v32)
+        c32 = torch.empty_like(v32)
+        s.hv_device(v64.data_ptr(), h64.data_ptr())
+        s.hv_device_f32(v32.data_ptr(), h32.data_ptr())
+        ref.hv_device_f32(v32.data_ptr(), c32.data_ptr())
+        torch.cuda.synchronize()
+        scale = h64.abs().max().item()
+        err = (h32.double() - h64).abs().max().item() / scale
+        err_cc = (c32.double() - h64).abs().max().item() / scale
+        print(f"{case} bn={bn} split={split}: tensor-core {err:.2e}, CUDA-core {err_cc:.2e}")
+        assert err <= 4e-6, err
+
+
 def test_precision_modes_alternate_on_one_context(nss):
     """FP64 and mixed solves share a context's buffers; switching back and
     forth must re-shape them (the FP64 basis is larger than the mixed
@@ -243,3 +289,39 @@ def test_precision_modes_alternate_on_one_context(nss):
     for prec in (nss.NSS_PREC_MIXED, nss.NSS_PREC_FP64, nss.NSS_PREC_MIXED, nss.NSS_PREC_FP64):
         ev, _, _ = s.sb_diag(neigen=1, tol=1e-12, want_vectors=False, precision=prec)
         assert abs(ev[0] - ref) <= 1e-10 * abs(ref)
+
+
+@pytest.mark.parametrize("name", ["kat_spin.npz", "kat_hubbard.npz", "c2_small.npz"])
+@pytest.mark.parametrize("estates", [1e-3, 1e-5, 1e-8])
+def test_rdm_error_threshold_rule_matches_oracle(nss, name, estates):
+    """The Edmrg rule (Mstates = 0, Estates != 0; src/DMRG_RDM.f90:206-208 and
+    :279-281): m_s is the first minimum of |1 - cumulate(lambda) - Estates|,
+    then the degeneracy extension.  On a given state against the oracle's
+    restatement: m_s exact, truncation error to 1e-13."""
+    z = load_npz(name)
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    psi = z["psi"]
+    res = s.sb_get_rdm(0, 0.1, psi=psi, want_u=True, estates=estates)
+    lb, rb = O.build_density_matrices(sb, psi, l.sectors(), r.sectors())
+    for side, blocks, dim in ((0, lb, l.dim), (1, rb, r.dim)):
+        rho = O.eigh_blocks(blocks)
+        m_s, eps = O.truncation(rho, 0, dim, 0.1, estates)
+        assert res.m_s[side] == m_s, (side, res.m_s[side], m_s)
+        assert abs(res.trunc_err[side] - eps) <= 1e-13, (side, res.trunc_err[side], eps)
+        u = res.u[side]
+        assert u.shape == (dim, m_s)
+        assert np.allclose(u.T @ u, np.eye(m_s), atol=1e-12)
+
+
+def test_rdm_without_threshold_is_refused(nss):
+    """Mstates = Estates = 0 stops the reference ("Mdmrg=Edmrg=0 can not fix
+    a threshold for the RDM"); here it is NSS_ERR_INVALID."""
+    z = load_npz("kat_spin.npz")
+    l, r, sb, ds = _setup(z)
+    s = nss.Superblock()
+    _upload(nss, s, l, r, ds)
+    with pytest.raises(nss.NssError) as ei:
+        s.sb_get_rdm(0, 0.1, psi=z["psi"], estates=0.0)
+    assert ei.value.code == nss.NSS_ERR_INVALID and "Edmrg" in str(ei.value)

@@ -277,3 +277,19 @@ def test_restart_text_writer_round_trips_through_the_reader(name, legacy):
         for k in b.ops:
             assert r.ops[k][1] == b.ops[k][1]
             assert (r.op(k) != b.op(k)).nnz == 0
+
+
+def test_error_threshold_rule_by_hand():
+    """The Edmrg rule of renormalize_block (src/DMRG_RDM.f90:206-208) on a
+    small spectrum worked out by hand: 1 - cumulate(lambda) = .5, .2, .05,
+    .01, .001, 0; closest to Estates = 0.012 is the fourth (|.01 - .012|);
+    no eigenvalue after it lies within 10 % of 0.04."""
+    from oracle import dmrg_oracle as O
+    lam = np.array([0.5, 0.3, 0.15, 0.04, 0.009, 0.001])
+    rho = O.RhoBlocks([(0.0,)], [np.arange(6)], [lam[::-1].copy()], [np.eye(6)], lam.copy(), np.arange(6)[::-1])
+    m_s, eps = O.truncation(rho, 0, 6, 0.1, 0.012)
+    assert m_s == 4 and abs(eps - 0.01) < 1e-15
+    # Mstates != 0 ignores Estates; both zero is the reference's stop
+    assert O.truncation(rho, 2, 6, 0.1, 0.012)[0] == 2
+    with pytest.raises(ValueError):
+        O.truncation(rho, 0, 6, 0.1, 0.0)
