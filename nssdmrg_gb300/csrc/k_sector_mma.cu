@@ -15,8 +15,8 @@
 // to TF32 and lo = (x - hi) rounded to TF32 (so the tensor core's reading of
 // a TF32 operand drops nothing); each K step issues hi.hi + hi.lo + lo.hi
 // (and lo.lo with the context's lolo option) as tcgen05.mma kind::tf32
-// (M=128, N=BN, K=8) into an FP32 accumulator in TMEM: FP32-class products.  H_L and H_R are split once per upload;
-// only W is split per call (k_pack_w).
+// (M=128, N=BN, K=8) into an FP32 accumulator in TMEM: FP32-class products.
+// H_L and H_R are split once per upload; only W is split per call (k_pack_w).
 //
 // Operand layout for TMA: every operand is stored "K-chunked": for a block X
 // with R rows contracted over K, chunk c (K columns 32c..32c+31) is an
@@ -37,15 +37,16 @@
 // accumulator and commits the stage back to the producer and the slab's
 // partial product to the epilogue; warps 2-5 read the partials out of TMEM
 // (tcgen05.ld, each warp its 32 lanes) and sum them in FP32 registers, then
-// store the item's tile.  Two TMEM buffers alternate, so draining one slab
-// overlaps the MMAs of the next.  The per-slab promotion matters: the
-// tensor core's FP32 accumulation does not round to nearest, and over a
-// whole K loop of ~350 its error grew to 5x that of an FP32 FMA chain
-// (measured RMS 1.8e-6 against 3.6e-7), enough to cost the mixed solver a
-// third more iterations; over one slab it stays below the FMA chain's.  Every wait is bounded (wait_limit):
-// a wait that runs out sets the error word, every role stops, the producer
-// waits for the copies it issued, the MMA lane for its MMAs, and the CTA
-// frees its TMEM and returns.
+// store the item's tile (staged in shared memory for whole-segment writes).
+// Four TMEM buffers rotate, so the MMAs run up to three slabs ahead of the
+// draining.  The per-slab promotion matters: the tensor core's FP32
+// accumulation does not round to nearest, and over a whole K loop of ~350
+// its error grew to 5x that of an FP32 FMA chain (measured RMS 1.8e-6
+// against 3.6e-7), enough to cost the mixed solver a third more iterations;
+// over one slab it stays below the FMA chain's.  Every wait is bounded
+// (wait_limit): a wait that runs out sets the error word, every role stops,
+// the producer waits for the copies it issued, the MMA lane for its MMAs,
+// and the CTA frees its TMEM and returns.
 #include "sector_mma.cuh"
 
 #include <cuda.h>
@@ -60,7 +61,7 @@ namespace nss {
 namespace {
 
 constexpr int MM_THREADS = 192;            // 6 warps
-constexpr int MM_SMEM_BUDGET = 200 * 1024; // operand stages
+constexpr int MM_SMEM_LIMIT = 232448;       // dynamic shared memory of one CTA
 
 // instruction descriptor, kind::tf32: D FP32, A and B TF32, both K-major
 __host__ __device__ constexpr uint32_t idesc_tf32(int bn) {
@@ -202,9 +203,14 @@ struct MmaCfg {
     static constexpr int A_BYTES = MM_M * 128;                 // one plane of an A box
     static constexpr int B_BYTES = BN * 128;
     static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;    // hi and lo of A and B
-    static constexpr int STAGES = MM_SMEM_BUDGET / STAGE;
-    static constexpr int SMEM = STAGES * STAGE + 1024;         // + alignment slack
-    static constexpr uint32_t TCOLS = 2 * BN;                  // two accumulators
+    static constexpr int OUT_LD = BN + 1;                      // staging row stride (conflict-free)
+    static constexpr int OUT_BYTES = MM_M * OUT_LD * 4;        // one output tile
+    // as many operand stages as fit beside the epilogue's staging
+    static constexpr int STAGES = (MM_SMEM_LIMIT - OUT_BYTES - 1024) / STAGE;
+    static constexpr int SMEM = STAGES * STAGE + OUT_BYTES + 1024;   // + alignment slack
+    static_assert(STAGES >= 2 && SMEM <= MM_SMEM_LIMIT, "shared memory plan");
+    static constexpr int NBUF = 4;                             // TMEM slab accumulators in flight
+    static constexpr uint32_t TCOLS = NBUF * BN;
 };
 
 template <int BN>
@@ -219,7 +225,8 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
     if (stop && *stop) return;   // before any TMEM allocation: uniform exit
     extern __shared__ uint8_t mm_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)mm_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], drain;
+    constexpr int NB = C::NBUF;
+    __shared__ __align__(8) uint64_t full[S], empty[S], tfull[NB], tempty[NB], drain;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_s;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -228,7 +235,7 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
         }
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < NB; ++a) {
             mbar_init(smem_u32(&tfull[a]), 1);
             mbar_init(smem_u32(&tempty[a]), 4);   // one arrival per epilogue warp
         }
@@ -296,11 +303,11 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
             const int nk = m.nk0 + m.nk1;
             bool ok = true;
             for (int c = 0; c < nk; ++c, ++it) {
-                const int s = it % S, acc = it & 1;
+                const int s = it % S, acc = it % NB;
                 const uint32_t par = (uint32_t)(it / S) & 1u;
                 const uint32_t tacc = tmem + (uint32_t)(acc * BN);
-                // the epilogue has drained this buffer (its use two slabs ago)
-                if (!mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(it >> 1) & 1u) ^ 1u, spin, abort) ||
+                // the epilogue has drained this buffer (its use NB slabs ago)
+                if (!mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(it / NB) & 1u) ^ 1u, spin, abort) ||
                     !mbar_wait(smem_u32(&full[s]), par, spin, abort)) {
                     give_up();
                     ok = false;
@@ -343,9 +350,9 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
             for (int j = 0; j < BN; ++j) sum[j] = 0.f;
             bool ok = true;
             for (int c = 0; c < nk; ++c, ++it) {
-                const int acc = it & 1;
+                const int acc = it % NB;
                 bool got = true;
-                if (lane == 0) got = mbar_wait(smem_u32(&tfull[acc]), (uint32_t)(it >> 1) & 1u, spin, abort);
+                if (lane == 0) got = mbar_wait(smem_u32(&tfull[acc]), (uint32_t)(it / NB) & 1u, spin, abort);
                 if (__shfl_sync(0xffffffffu, got ? 1 : 0, 0) == 0) {
                     if (lane == 0) give_up();
                     ok = false;
@@ -353,31 +360,38 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-                for (int c0 = 0; c0 < BN; c0 += 16) {
-                    uint32_t r[16];
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                        "[%16];"
-                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                          "=r"(r[14]), "=r"(r[15])
-                        : "r"(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * BN + c0)));
+                for (int c0 = 0; c0 < BN; c0 += 64) {   // 64 columns per load, one wait
+                    uint32_t r[64];
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+                                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+                                 : "r"(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * BN + c0)));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) sum[c0 + j] += __uint_as_float(r[j]);
+                    for (int j = 0; j < 64; ++j) sum[c0 + j] += __uint_as_float(r[j]);
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(&tempty[acc]));
             }
             if (!ok) break;
-            const int il = m.m0 + 32 * q + lane;
-            if (il < m.dl) {
-                float *dst = (m.out ? out1 : out0) + m.off + (int64_t)il * m.dr;
+            // the warp's 32 rows through shared memory, then row by row with
+            // the lanes along the columns: whole 128-byte segments per store
+            // (a lane writing its own row touched 32 sectors per store, 16x
+            // the output's own sectors in the measured L2 write traffic)
+            float *stg = (float *)(smem + (size_t)S * C::STAGE) + (size_t)(32 * q) * C::OUT_LD;
 #pragma unroll
-                for (int j = 0; j < BN; ++j)
-                    if (m.n0 + j < m.dr) dst[m.n0 + j] = sum[j];
+            for (int j = 0; j < BN; ++j) stg[lane * C::OUT_LD + j] = sum[j];
+            __syncwarp();
+            float *base = (m.out ? out1 : out0) + m.off;
+            for (int r = 0; r < 32; ++r) {
+                const int il = m.m0 + 32 * q + r;
+                if (il >= m.dl) break;
+                float *dst = base + (int64_t)il * m.dr + m.n0;
+#pragma unroll
+                for (int c = lane; c < BN; c += 32)
+                    if (m.n0 + c < m.dr) dst[c] = stg[r * C::OUT_LD + c];
             }
+            __syncwarp();
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
