@@ -251,6 +251,19 @@ int nss_rdm_fallback_reasons(const nss_ctx *ctx, int64_t out[5]);
 int nss_time_chunks(nss_ctx *ctx, int enable);
 int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iters, double *cols);
 
+/* The mixed path's plan for the uploaded superblock, as the tile tuner chose
+ * it: candidate 0 puts every sector on CUDA cores (the persistent Lanczos
+ * kernel), 1 and 2 the sectors with Dl >= 32 on the tensor-core GEMM with
+ * 64- or 128-column tiles (-1: the tuner is off, NSS_TC_MIN_DL or
+ * NSS_TC_AUTO=0).  The tuner keys superblocks by N and their largest left
+ * sector (quarter-octave bins), plans the first ones of a class with each
+ * candidate once, records each converged mixed solve's device time per H*psi
+ * product, and then keeps the fastest.  ms_per_hv[3] / solves[3] give the
+ * class's measurements so far (-1 / 0: not tried).  nss_tune_reset forgets
+ * every class.  No counterpart in the reference. */
+int nss_tune_info(const nss_ctx *ctx, int *candidate, double *ms_per_hv, int *solves);
+void nss_tune_reset(void);
+
 /* Energy <psi|H|psi> / <psi|psi> of a device vector d_psi (length n =
  * nss_sb_dim) on the uploaded superblock, written to *energy (host), without
  * allocating any memory.  No counterpart in the reference: it is for callers

@@ -131,6 +131,8 @@ def lib():
         "nss_kron_sum": (C.c_int, [I32, I32, I32, P, C.POINTER(Csr), C.POINTER(Csr), C.c_int, I64,
                                    C.POINTER(I64), P, P, P]),
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
+        "nss_tune_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+        "nss_tune_reset": (None, []),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_rdm_estates": (C.c_int, [P, P, C.c_int, D, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
@@ -554,6 +556,15 @@ class Superblock:
     def hv_device(self, d_v: int, d_hv: int):
         """H*v on device pointers (e.g. torch tensors' data_ptr())."""
         self._check(lib().nss_hv_device(self._ctx, self.n, C.c_void_p(d_v), C.c_void_p(d_hv)))
+
+    def tune_info(self):
+        """(candidate, ms per H*psi of candidates 0..2, solves of each) of the
+        tile tuner for the uploaded superblock's shape class."""
+        cand = C.c_int()
+        ms = (C.c_double * 3)()
+        n = (C.c_int * 3)()
+        self._check(lib().nss_tune_info(self._ctx, C.byref(cand), ms, n))
+        return cand.value, list(ms), list(n)
 
     def energy_noalloc(self, d_psi: int) -> float:
         """<psi|H|psi>/<psi|psi> of a device vector, allocating nothing (for

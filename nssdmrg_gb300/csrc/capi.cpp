@@ -108,6 +108,7 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
     }
     ctx->c.device = device;
     ctx->c.tc_min_dl = nss::tc_min_dl_default();
+    ctx->c.tc_auto = nss::tune_enabled();
     nss::mma_tile_default(&ctx->c.mma_bn, &ctx->c.mma_split);
     ctx->c.mma_lolo = nss::mma_lolo_default();
     ctx->c.budget = hbm_budget;
@@ -205,6 +206,21 @@ int nss_hv_device_f32(nss_ctx *ctx, int64_t n, const float *d_v, float *d_hv) {
     DeviceScope dscope(ctx->c.device);
     return nss::hv_device_fp32(ctx->c, d_v, d_hv);
 }
+
+int nss_tune_info(const nss_ctx *ctx, int *candidate, double *ms_per_hv, int *solves) {
+    if (!ctx || !ctx->c.sb.valid) return NSS_ERR_STATE;
+    if (candidate) *candidate = ctx->c.tune_cand;
+    double m[3] = {-1.0, -1.0, -1.0};
+    int n[3] = {0, 0, 0};
+    if (ctx->c.tune_cand >= 0) nss::tune_lookup(ctx->c.device, ctx->c.tune_class, m, n);
+    for (int k = 0; k < 3; ++k) {
+        if (ms_per_hv) ms_per_hv[k] = m[k];
+        if (solves) solves[k] = n[k];
+    }
+    return NSS_OK;
+}
+
+void nss_tune_reset(void) { nss::tune_reset(); }
 
 int nss_sb_energy_noalloc(nss_ctx *ctx, int64_t n, const double *d_psi, double *energy) {
     if (!ctx) return fail(ctx, NSS_ERR_INVALID, "null context");

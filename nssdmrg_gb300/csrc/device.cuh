@@ -192,6 +192,8 @@ struct Ctx {
     DevRenorm ren;
     int64_t launches = 0;        // kernels of this library launched
     int tc_min_dl = 1024;        // tensor-core sector threshold (see tc_min_dl_default)
+    bool tc_auto = true;         // the tile tuner picks the plan per upload (tile_tune.cpp)
+    int tune_class = 0, tune_cand = -1;   // the current superblock's shape class and candidate
     int mma_bn = 64;             // tensor-core tile width (64 or 128) and K-loop split
     bool mma_split = true;
     bool mma_lolo = false;       // fourth product lo.lo in the split-TF32 GEMM
@@ -279,6 +281,16 @@ bool mma_lolo_default();
 // return and the entry point report NSS_ERR_CUDA; the tests shorten the
 // limit to exercise that path.
 uint32_t wait_limit();
+
+// tile_tune.cpp: the mixed path's plan per shape class of superblock
+bool tune_enabled();
+// candidate for the superblock being uploaded (0 CUDA cores, 1 / 2 tensor
+// cores with 64 / 128-column tiles): sets *tc_min_dl and *bn for it
+int tune_choose(Ctx &c, const DevSb &s, int *tc_min_dl, int *bn);
+// a converged mixed solve on the current superblock took ms for numop products
+void tune_record(Ctx &c, double ms, int numop);
+int tune_lookup(int device, int cls, double *ms_per_hv, int *solves);
+void tune_reset();
 
 // k_noalloc.cu
 int sb_energy_noalloc(Ctx &c, int64_t n, const double *d_psi, double *energy);

@@ -1894,6 +1894,8 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     c.chunk_iters = 0;
     c.chunk_cols = 0.0;
     cudaStream_t st = c.stream;
+    // the tensor-core pipeline's error word belongs to this solve
+    if (mixed && s.d_tc_err) NSS_CUDA_TRY(c, cudaMemsetAsync(s.d_tc_err, 0, sizeof(int), st));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -2134,6 +2136,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     if (evals_host) NSS_CUDA_TRY(c, cudaMemcpy(evals_host, z.theta, ne * sizeof(double), cudaMemcpyDeviceToHost));
     c.last_ms_eigh = ms;
     c.last_numop = numop_;
+    if (mixed) tune_record(c, ms, numop_);
     z.last_iters = m_done;
     z.neigen_done = ne;
     if (numop) *numop = numop_;
@@ -2232,10 +2235,6 @@ int engine_add(BatchEngine &E, Ctx &c, uint64_t seed, int nitermax, double tol, 
     }
     if (c.device != c0.device) { c0.err = "nss_batch_add: the context is on another device"; return NSS_ERR_INVALID; }
     if (!c.sb.valid) { c0.err = "nss_batch_add: the context has no superblock"; return NSS_ERR_STATE; }
-    if (c.sb.mma_nitems != 0) {
-        c0.err = "nss_batch_add: superblocks with tensor-core sectors are solved one by one (nss_eigh)";
-        return NSS_ERR_INVALID;
-    }
     for (auto &S : E.solves)
         if (S.c == &c) { c0.err = "nss_batch_add: the context is already in the batch"; return NSS_ERR_INVALID; }
     if (tol <= 0.0) tol = 1e-15;

@@ -404,7 +404,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
     // terms from "terms only" CUDA-core tiles (w = 1), listed first, which
     // k_hv_fp32 runs after the GEMM and which add its two output planes.
     MmaPlan plan;
-    mma_layout(s, c.tc_min_dl, c.mma_bn, c.mma_split, plan);
+    int tc_thr = c.tc_min_dl, tc_bn = c.mma_bn;
+    c.tune_cand = -1;
+    if (c.tc_auto) tune_choose(c, s, &tc_thr, &tc_bn);
+    mma_layout(s, tc_thr, tc_bn, c.mma_split, plan);
     std::vector<char> on_tc(s.nsb, 0);
     for (int k : plan.sectors) on_tc[k] = 1;
     std::vector<int4> tiles32;

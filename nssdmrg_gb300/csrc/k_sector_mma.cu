@@ -254,6 +254,8 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
     volatile int *abort = &abort_s;
+    // waits for the CTA's own copies and MMAs before it leaves
+    const uint32_t drain_spin = spin > (1u << 22) ? spin : (1u << 22);
     auto give_up = [&]() {
         *abort = 1;
         atomicExch(err, 1);
@@ -287,11 +289,14 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
                 last_par[s] = (int)par;
             }
         }
-        // no copy of this CTA may still be landing when it leaves (bounded,
-        // and not cut short by the abort flag)
+        // no copy of this CTA may still be landing when it leaves: bounded, but
+        // by a limit of its own (the CTA's own copies complete whatever the
+        // other roles did; the configurable limit may be tiny in tests), and
+        // not cut short by the abort flag
         volatile int never = 0;
         for (int s = 0; s < S; ++s)
-            if (inflight[s] && !mbar_wait(smem_u32(&full[s]), (uint32_t)last_par[s], spin, &never)) atomicExch(err, 1);
+            if (inflight[s] && !mbar_wait(smem_u32(&full[s]), (uint32_t)last_par[s], drain_spin, &never))
+                atomicExch(err, 1);
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer: every slab into a fresh accumulator buffer (two
         // alternate), which the epilogue drains into FP32 registers
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
         if (issued) {   // every MMA of this lane done before the CTA frees its TMEM
             mma_commit(smem_u32(&drain));
             volatile int never = 0;
-            if (!mbar_wait(smem_u32(&drain), 0u, spin, &never)) atomicExch(err, 1);
+            if (!mbar_wait(smem_u32(&drain), 0u, drain_spin, &never)) atomicExch(err, 1);
         }
     } else if (warp >= 2) {
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows)

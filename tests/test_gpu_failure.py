@@ -125,3 +125,23 @@ def test_non_finite_operator_is_refused(nss, value):
     _upload(s, l, r, sb, ds)
     ev, _, _ = s.sb_diag(neigen=2, tol=1e-12)
     np.testing.assert_allclose(ev / (l.length + r.length), z["golden_energy"], rtol=1e-12, atol=0)
+
+
+def test_tensor_core_pipeline_wait_runs_out_then_recovers(nss, monkeypatch):
+    """The tensor-core sector GEMM's mbarrier waits with a poll limit of zero
+    (every sector of 32 left states or more routed to it): its roles give up,
+    the CTAs still wait for their own copies and MMAs and free their TMEM, the
+    solve reports the time-out, and the next solve on the context is right."""
+    z, l, r, sb, ds = _setup("c2_small.npz")
+    assert max(sb.Dls) >= 32
+    monkeypatch.setenv("NSS_TC_MIN_DL", "32")
+    s = nss.Superblock()
+    _upload(s, l, r, sb, ds)
+    monkeypatch.setenv("NSS_WAIT_LIMIT", "0")
+    with pytest.raises(nss.NssError) as ei:
+        s.sb_diag(neigen=1, tol=1e-12, precision=nss.NSS_PREC_MIXED, want_vectors=False)
+    assert ei.value.code == nss.NSS_ERR_CUDA and "timed out" in str(ei.value), str(ei.value)
+    monkeypatch.delenv("NSS_WAIT_LIMIT")
+    ev, _, _ = s.sb_diag(neigen=1, tol=1e-12, precision=nss.NSS_PREC_MIXED, want_vectors=False)
+    ref = z["oracle_gs_energy"][0]
+    assert abs(ev[0] - ref) <= 1e-10 * abs(ref)
