@@ -53,7 +53,7 @@ def parse():
                     help="headline path; the other one is timed alongside for comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweeps", action="store_true", help="skip the finite-sweep measurements")
-    ap.add_argument("--large-sweeps", type=int, default=1,
+    ap.add_argument("--large-sweeps", type=int, default=4,
                     help="finite sweeps timed on the spin-1 L=64 m=512 chain (0 skips it)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
@@ -150,7 +150,7 @@ def measure_core_peaks():
         line = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.strip().splitlines()[-1]
         j = json.loads(line)
         CORE_PROBE.update({k: j[k] for k in ("dfma_gflops", "dmma_gflops", "ffma_gflops", "tf32_tc_gflops",
-                                             "dfma_chain_cycles",
+                                             "l2_read_gbs", "dfma_chain_cycles",
                                              "ddiv_chain_cycles", "ffma_chain_cycles", "chain_lanes") if k in j})
         return j["dfma_gflops"] / 1e3, j["ffma_gflops"] / 1e3, \
             "DFMA / FFMA rates measured in this run by nssdmrg_gb300/peaks.cu (whole GPU)"
@@ -184,10 +184,17 @@ def cpu_baseline_leg(desc, n, flops_hv, budget_s=20.0):
     t0 = time.perf_counter()
     ev, numop, rc = ref.lanczos(neigen=1, nitermax=nit, tol=1e-12, seed=7, nthreads=cores)
     dt = time.perf_counter() - t0
+    # the serial loop nest on one core (the reference's serial build runs
+    # one rank on one core): a short Lanczos run, per H*psi
+    t1 = time.perf_counter()
+    _, nop1, _ = ref.lanczos(neigen=1, nitermax=4, tol=1e-12, seed=7, nthreads=1)
+    dt1 = (time.perf_counter() - t1) / max(nop1, 1)
     return {"value": flops_hv * numop / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
             "sample": f"one Lanczos solve of the same superblock (N={n}), {numop} H*psi products "
                       f"({'converged' if rc == 0 else 'iteration-capped'}), OpenMP over sectors, "
-                      f"{dt:.2f} s", "energy": float(ev[0])}
+                      f"{dt:.2f} s", "energy": float(ev[0]),
+            "serial_1core": {"value": flops_hv / dt1 / 1e12, "unit": "TFLOP/s", "cores": 1,
+                             "sample": f"{nop1} H*psi products of a Lanczos run on one core, {dt1 * 1e3:.1f} ms each"}}
 
 
 CHECK_ITERS = 4       # iterations per launch of the persistent kernel (the library's check period)
@@ -195,8 +202,8 @@ CHECK_ITERS = 4       # iterations per launch of the persistent kernel (the libr
 SWEEP_CASE = {"workload": "heisenberg_half_L20_M64_3sweeps", "model": "heisenberg_half", "L": 20, "ldmrg": 10,
               "mdmrg": 64, "msweep": [64, 64, 64], "lanc_tolerance": 1e-12, "lanc_niter": 200}
 
-# the third configuration: spin-1 chain L=64, m=512 (4 sweeps in the
-# configuration; `--large-sweeps` sets how many are timed, default 1)
+# the third configuration: spin-1 chain L=64, m=512, 4 finite sweeps
+# (`--large-sweeps` sets how many are timed, default 4)
 SWEEP_CASE_LARGE = {"workload": "heisenberg_one_L64_M512", "model": "heisenberg_one", "L": 64, "ldmrg": 32,
                     "mdmrg": 512, "lanc_tolerance": 1e-12, "lanc_niter": 200}
 
@@ -257,17 +264,17 @@ def measure_sweeps(nss, device, case=None, warm=True):
     return out
 
 
-BATCH_CASE = {"workload": "hubbard_batch_64", "instances": 64, "distinct": 8, "seed": 42, "U": [0.0, 8.0],
+BATCH_CASE = {"workload": "hubbard_batch_64", "instances": 64, "distinct": 64, "seed": 42, "U": [0.0, 8.0],
               "L": [16, 24, 32, 48], "m": [64, 128, 256, 384], "t": 1.0, "filling": "half",
               "lanc_tolerance": 1e-12, "lanc_niter": 256}
 
 
 def measure_batch(nss, device):
-    """Batched solves (the fourth benchmark configuration, scaled as noted):
-    Hubbard superblocks at the last infinite step, U ~ Uniform[0,8], L and m
-    drawn from the listed sets with a fixed seed; `distinct` superblocks are
-    generated and each is uploaded into instances/distinct contexts (every
-    instance is its own solve with its own start vector).  Solves/s of one
+    """Batched solves (the fourth benchmark configuration): 64 Hubbard
+    superblocks at the last infinite step, each drawn independently from the
+    seed (U ~ Uniform[0,8], L and m from the listed sets), each uploaded into
+    its own context (`distinct` = `instances`; a smaller `distinct` would
+    repeat superblocks, every repeat still its own solve).  Solves/s of one
     nss_eigh_batch call against the same solves one by one (mixed and FP64),
     and the largest |dE| between the batched and the single results."""
     rng = np.random.default_rng(BATCH_CASE["seed"])
@@ -441,6 +448,18 @@ def run_gpu(args):
     d, t_prep = build_product_workload(nss, local, prec)
     sb = d.sb
     n = sb.n
+    # the tile tuner settles during warm-up: one upload and mixed solve per
+    # candidate plan of this superblock's shape class, then the upload the
+    # timed steps use, planned with the class's fastest candidate
+    desc_w = d.export_superblock()
+    for _ in range(3):
+        sb.upload_desc(desc_w)
+        if sb.tune_info()[0] < 0:
+            break
+        sb.sb_diag(neigen=1, nitermax=WORKLOAD["lanc_niter"], tol=WORKLOAD["lanc_tolerance"], seed=77,
+                   precision=nss.NSS_PREC_MIXED, want_vectors=False)
+    sb.upload_desc(desc_w)
+    tune = sb.tune_info()
     fd, fab = sb.flops()
     f_hv = fd + fab
     ext = torch.cuda.ExternalStream(sb.stream)
@@ -532,9 +551,9 @@ def run_gpu(args):
     # the mixed method's dominant kernel is the persistent Lanczos kernel:
     # its launches timed with CUDA events on the library stream (3 solves)
     chunk = None
+    tms = tit = tcols = 0.0
     if mixed and not args.profile:
         sb.time_chunks(True)
-        tms = tit = tcols = 0.0
         tl = 0
         for r in range(3):
             flush.zero_()
@@ -546,6 +565,8 @@ def run_gpu(args):
             tit += it_
             tcols += cols_
         sb.time_chunks(False)
+    # (no launch timed: the tuner's plan runs the tensor-core path, not the persistent kernel)
+    if mixed and not args.profile and tit > 0:
         desc0 = d.export_superblock()
         op_bytes = 4 * sum(desc0.dls[k] ** 2 + desc0.drs[k] ** 2 for k in range(desc0.nsb))
         mbar = tcols / max(tit, 1)
@@ -606,6 +627,11 @@ def run_gpu(args):
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
             else {}
         fp64, fp32, peak_src = measure_core_peaks()
+        tf32_peak = (CORE_PROBE.get("tf32_tc_gflops") or 1.1e6) / 1e3
+        l2_peak = CORE_PROBE.get("l2_read_gbs") or 0.0
+        l2_src = "L2 read rate measured in this run by nssdmrg_gb300/peaks.cu (of measured)"
+        if not l2_peak:
+            l2_peak, l2_src = peaks.get("hbm_gbs", 6795.1), "no L2 measurement: MEASURED_PEAKS.json hbm_gbs"
         kname = "k_chunk32" if (mixed and chunk) else "k_hv_fp64"
         peak = fp32 if mixed else fp64
         traffic = None
@@ -623,6 +649,9 @@ def run_gpu(args):
                            l2="flushed between timed steps (512 MiB write)",
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
             "solves_per_s": head["solves_per_s"],
+            # time per solve (Lanczos to 1e-12 with the RDM step): the like-for-like figure, since the
+            # TFLOP/s counts every H*psi of the mixed method (FP32 phase, anchored phase, FP64 checks)
+            "ms_per_solve": head["ms_per_step"], "ms_per_solve_other_path": comp["ms_per_step"],
             "ms_eigensolve": head["ms_eigh"], "ms_rdm": head["ms_rdm"],
             "numop_mean": statistics.mean(numops[:args.steps]),
             ("fp64" if mixed else "mixed"): {"value": comp["value"], "ms_per_step": comp["ms_per_step"],
@@ -640,10 +669,16 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_times)},
             "roofline": ({"kernel": "k_chunk32 (persistent Lanczos: H*psi items + orthogonalisation, "
                                     f"{CHECK_ITERS} iterations per launch)",
-                          "bound": "hbm", "achieved": chunk["achieved_gbs"] * 1.0,
-                          "peak": peaks.get("hbm_gbs", 6795.1), "unit": "GB/s",
-                          "frac": chunk["achieved_gbs"] / peaks.get("hbm_gbs", 6795.1),
-                          "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                          # the working set stays in L2 (DRAM traffic per launch in `traffic`), and the
+                          # iteration is bound by its grid barriers: quoted against the measured L2 read
+                          # rate, with the HBM view beside it
+                          "bound": "l2", "achieved": chunk["achieved_gbs"] * 1.0,
+                          "peak": l2_peak, "unit": "GB/s",
+                          "frac": chunk["achieved_gbs"] / l2_peak,
+                          "traffic": traffic, "peak_source": l2_src,
+                          "hbm_view": {"peak_gbs": peaks.get("hbm_gbs", 6795.1),
+                                       "frac": chunk["achieved_gbs"] / peaks.get("hbm_gbs", 6795.1),
+                                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
                           "algorithmic_bytes_per_launch": chunk["bytes_per_iteration"] * chunk["iterations"]
                           / max(chunk["launches"], 1),
                           "ms_per_launch": chunk["ms_per_launch"], "detail": chunk,
@@ -652,6 +687,14 @@ def run_gpu(args):
                           "hv_alone": {"kernel": "k_hv_fp32", "ms_per_launch": t_hv * 1e3,
                                        "achieved_tflops": hv_achieved}}
                          if (mixed and chunk) else
+                         {"kernel": "k_sector_mma (split-TF32 tcgen05 sector GEMM, with its W packing and "
+                                    "the A x B terms kernel)", "bound": "tensor",
+                          "achieved": 3.0 * fd / t_hv / 1e12, "peak": tf32_peak, "unit": "TFLOP/s",
+                          "frac": 3.0 * fd / t_hv / 1e12 / tf32_peak, "traffic": traffic,
+                          "peak_source": "tcgen05 kind::tf32 rate measured in this run by nssdmrg_gb300/peaks.cu "
+                                         "(of measured); achieved counts the three TF32 products per FP32 product",
+                          "ms_per_launch": t_hv * 1e3}
+                         if mixed else
                          {"kernel": f"{kname} (sector H*psi)", "bound": "fp64",
                           "achieved": hv_achieved, "peak": peak, "unit": "TFLOP/s", "frac": hv_achieved / peak,
                           "traffic": traffic, "peak_source": peak_src + " (of measured DFMA rate)",
@@ -662,6 +705,9 @@ def run_gpu(args):
             "batch": batch,
             "serving": serving,
             "setup_s": t_prep,
+            "tile_tuner": {"candidate": tune[0], "ms_per_hv_by_candidate": tune[1], "solves_by_candidate": tune[2],
+                           "candidates": ["CUDA cores (persistent kernel)", "tensor cores, 64-column tiles",
+                                          "tensor cores, 128-column tiles"]},
         }
         if not args.no_cpu_baseline and world == 1:
             try:
@@ -709,11 +755,24 @@ def run_reference(args):
     nit = int(max(8, min(WORKLOAD["lanc_niter"], budget / max(per_it, 1e-9) / 2)))
     for w in range(args.warmup):
         ref.lanczos(neigen=1, nitermax=min(nit, 16), tol=1e-12, seed=w, nthreads=cores)
-    times, numops = [], []
+    lsec, rsec = run.left.sectors(), run.right.sectors()
+
+    def rdm(psi):
+        # sb_get_rdm + eigh + the truncation choice (src/DMRG_RDM.f90:18-221),
+        # as the oracle restates them: numpy's LAPACK eigh per rho block
+        lb, rb = O.build_density_matrices(sbo, psi, lsec, rsec)
+        for blocks, dim in ((lb, run.left.dim), (rb, run.right.dim)):
+            O.truncation(O.eigh_blocks(blocks), WORKLOAD["mdmrg"], dim, 0.1)
+
+    times, numops, t_rdm = [], [], []
     for s in range(args.steps):
         t0 = time.perf_counter()
-        ev, numop, rc = ref.lanczos(neigen=1, nitermax=nit, tol=1e-12, seed=1000 + s, nthreads=cores)
-        times.append(time.perf_counter() - t0)
+        ev, vec, numop, rc = ref.lanczos_vectors(neigen=1, nitermax=nit, tol=1e-12, seed=1000 + s, nthreads=cores)
+        t1 = time.perf_counter()
+        rdm(vec[:, 0])
+        t2 = time.perf_counter()
+        times.append(t2 - t0)
+        t_rdm.append(t2 - t1)
         numops.append(numop)
     value = f_hv * sum(numops) / sum(times) / 1e12
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
@@ -723,7 +782,9 @@ def run_reference(args):
            "config": dict(WORKLOAD, N=sbo.N, precision="fp64", l2="n/a (CPU)", parallelism="host cores"),
            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                             "sample": f"per step one Lanczos solve capped at {nit} H*psi products "
-                                      f"(oracle C restatement of spMatVec_direct_main + Lanczos, OpenMP)"},
+                                      f"(oracle C restatement of spMatVec_direct_main + Lanczos, OpenMP) "
+                                      f"and the RDM step (numpy LAPACK eigh of the rho blocks, truncation)"},
+           "ms_rdm": 1e3 * statistics.mean(t_rdm),
            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "gpu_launches": 0, "flops_per_hv": f_hv, "numop_mean": statistics.mean(numops), "setup_s": t_prep,
            "energy_per_site": float(ev[0]) / WORKLOAD["L"]}

@@ -96,6 +96,18 @@ __global__ void __launch_bounds__(128, 1) tf32mma_k(int rounds, int* err){
   if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" :: "r"(tbase));
 }
 
+// L2 read bandwidth: a 48 MiB buffer (L2-resident after the first pass) read
+// as float4 by every SM, reps times; the sum keeps the loads alive
+__global__ void l2read_k(const float4* __restrict__ x, size_t n4, int reps, float* out){
+  float acc = 0.f;
+  for (int r = 0; r < reps; ++r)
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+      const float4 v = __ldcg(x + i);
+      acc += v.x + v.y + v.z + v.w;
+    }
+  if (acc == 12345.f) out[0] = acc;
+}
+
 // dependent chains, one warp: cycles per operation
 #define LAT_N 2048
 __global__ void lat_k(double* dout, float* fout, long long* cyc, int active){
@@ -151,6 +163,20 @@ int main(){
     int herr = 0; cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
     if (herr) best_t = 0;
   }
+  // L2 read bandwidth
+  double best_l2 = 0;
+  {
+    const size_t bytes = (size_t)48 << 20, n4 = bytes / 16;
+    float4* buf; cudaMalloc(&buf, bytes); cudaMemset(buf, 0, bytes);
+    const int reps = 40;
+    l2read_k<<<nsm * 4, 512>>>(buf, n4, 2, fout); cudaDeviceSynchronize();
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0); l2read_k<<<nsm * 4, 512>>>(buf, n4, reps, fout); cudaEventRecord(e1); cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+      best_l2 = fmax(best_l2, (double)bytes * reps / ms / 1e6);
+    }
+    cudaFree(buf);
+  }
   long long* dcyc; cudaMalloc(&dcyc, 4*sizeof(long long)); long long hc[3] = {0, 0, 0}; double lat[2][3];
   for (int a = 0; a < 2; ++a) {
     for (int rep = 0; rep < 2; ++rep) lat_k<<<1, 32>>>(dout, fout, dcyc, a == 0 ? 1 : 32);
@@ -159,9 +185,9 @@ int main(){
   }
   cudaError_t e = cudaGetLastError();
   printf("{\"device\": \"%s\", \"sm\": \"%d.%d\", \"sms\": %d, \"dfma_gflops\": %.1f, \"dmma_gflops\": %.1f, "
-         "\"ffma_gflops\": %.1f, \"tf32_tc_gflops\": %.1f, \"dfma_chain_cycles\": [%.1f, %.1f], \"ddiv_chain_cycles\": [%.1f, %.1f], "
+         "\"ffma_gflops\": %.1f, \"tf32_tc_gflops\": %.1f, \"l2_read_gbs\": %.1f, \"dfma_chain_cycles\": [%.1f, %.1f], \"ddiv_chain_cycles\": [%.1f, %.1f], "
          "\"ffma_chain_cycles\": [%.1f, %.1f], \"chain_lanes\": [1, 32], \"status\": \"%s\"}\n",
-         pr.name, pr.major, pr.minor, nsm, best_d, best_m, best_f, best_t, lat[0][0], lat[1][0], lat[0][1], lat[1][1],
+         pr.name, pr.major, pr.minor, nsm, best_d, best_m, best_f, best_t, best_l2, lat[0][0], lat[1][0], lat[0][1], lat[1][1],
          lat[0][2], lat[1][2], cudaGetErrorString(e));
   return e == cudaSuccess ? 0 : 1;
 }
