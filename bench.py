@@ -57,6 +57,8 @@ def parse():
                     help="finite sweeps timed on the spin-1 L=64 m=512 chain (0 skips it)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-full", action="store_true",
+                    help="serve the fifth configuration's full size ranges (L up to 64, m up to 512) at low rates")
     ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large"], default=None,
                     help="for profiler captures of single kernels: run one small workload and exit "
                          "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
@@ -323,78 +325,95 @@ def measure_batch(nss, device):
             "dE_rel_batched_vs_fp64_max": de}
 
 
-SERVE_CASE = {"workload": "serving_mix", "rates": [20.0, 100.0, 400.0], "requests_per_rate": 150, "slots": 32,
-              "seed": 7, "templates": 8, "lanc_tolerance": 1e-12, "lanc_niter": 256}
+# the fifth configuration: a Poisson stream of whole finite-DMRG runs (2
+# sweeps each), half spin-1/2 Heisenberg (J ~ U[0.5, 1.5]), half Hubbard
+# (U ~ U[0, 8], half filling), L ~ U{16..64}, m ~ U{64..512}.  One such run
+# takes 0.2-16 s on the GPU (measured: Hubbard L=64 m=512 16.5 s mixed, 37.9 s
+# FP64), so the specified ~4000 requests at up to 200 req/s would take hours:
+# the default run scales down to L ~ U{16..32}, m ~ U{64..256}, 16 requests
+# at each of two rates (a few minutes for both precisions); --serve-full runs
+# the specified size ranges at rates the GPU can follow.
+SERVE_CASE = {"workload": "serving_dmrg_runs", "sweeps": 2, "L": [16, 32], "m": [64, 256],
+              "rates": [1.0, 4.0], "requests_per_rate": 16, "hbm_budget_gb": 96, "seed": 7,
+              "models": "50% heisenberg_half J~U[0.5,1.5], 50% hubbard U~U[0,8] half filling",
+              "lanc_tolerance": 1e-12, "lanc_niter": 512}
+SERVE_CASE_FULL = dict(SERVE_CASE, L=[16, 64], m=[64, 512], rates=[0.1, 0.3], requests_per_rate=12)
 
 
-def measure_serving(nss, device):
-    """Continuous batching under a Poisson request stream (the fifth
-    benchmark configuration, scaled as noted): each request is one
-    ground-state solve of a superblock drawn from a pool of templates, half
-    spin-1/2 Heisenberg (J ~ U[0.5, 1.5]) and half Hubbard (U ~ U[0, 8]),
-    L and m drawn per template; requests arrive at rate lambda, are
-    admitted into free context slots (superblock upload included in the
-    latency) and join the batch engine between rounds.  p50/p99 of
-    arrival-to-result latency and the completion rate per lambda; every
-    result is checked against the template's own FP64 solve."""
-    rng = np.random.default_rng(SERVE_CASE["seed"])
-    tol, nit = SERVE_CASE["lanc_tolerance"], SERVE_CASE["lanc_niter"]
-    templates, drivers = [], []
-    for k in range(SERVE_CASE["templates"]):
-        if k % 2 == 0:
-            jv = float(rng.uniform(0.5, 1.5))
-            L, m = int(rng.choice([16, 24, 32])), int(rng.choice([64, 128]))
-            d = nss.DMRG(nss.MODEL_HEISENBERG_HALF, L // 2, m, jz=jv, jxy=jv, dmrg_qn=(0.0,), lanc_neigen=1,
-                         device=device)
-            meta = {"model": "heisenberg_half", "J": round(jv, 4), "L": L, "m": m}
-        else:
-            u = float(rng.uniform(0.0, 8.0))
-            L, m = int(rng.choice([16, 24])), int(rng.choice([64, 128]))
-            d = nss.DMRG(nss.MODEL_HUBBARD, L // 2, m, u=u, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1,
-                         device=device)
-            meta = {"model": "hubbard", "U": round(u, 4), "L": L, "m": m}
-        d.prepare_last()
-        ev, _, _ = d.sb.sb_diag(neigen=1, nitermax=nit, tol=tol, want_vectors=False)
-        meta["N"] = int(d.sb.n)
-        drivers.append(d)
-        templates.append((d.export_superblock(), float(ev[0]), meta))
-    slots = [nss.Superblock(device) for _ in range(SERVE_CASE["slots"])]
-    eng = nss.BatchEngine(slots[0])
-    out = {"config": SERVE_CASE, "templates": [t[2] for t in templates], "rates": []}
-    for lam in SERVE_CASE["rates"]:
-        nreq = SERVE_CASE["requests_per_rate"]
+def measure_serving(nss, device, case=None):
+    """Serving (the fifth benchmark configuration): requests are whole
+    finite-DMRG runs arriving as a Poisson stream; the server
+    (nss_server_*) admits them by estimated HBM footprint within its budget,
+    runs each on its own context with its block state resident, and batches
+    the mixed ground-state solves of all running requests in one engine.  Per
+    rate and precision: p50/p99 of arrival-to-result latency, completed runs
+    and ground-state solves per second, and the admission figures; each
+    result is checked against the same run made alone."""
+    case = case or SERVE_CASE
+    rng = np.random.default_rng(case["seed"])
+    nreq = case["requests_per_rate"]
+    out = {"config": case, "rates": []}
+    alone = {}
+    for lam in case["rates"]:
         arrivals = np.cumsum(rng.exponential(1.0 / lam, nreq))
-        kinds = rng.integers(0, len(templates), nreq)
-        free = list(range(len(slots)))
-        inflight = {}          # engine id -> (request, slot)
-        lat, dev, occ = [], 0.0, []
-        nxt = 0
-        t0 = time.perf_counter()
-        while len(lat) < nreq:
-            now = time.perf_counter() - t0
-            while nxt < nreq and arrivals[nxt] <= now and free:
-                sl = free.pop()
-                desc, _, _ = templates[kinds[nxt]]
-                slots[sl].upload_desc(desc)
-                eid = eng.add(slots[sl], seed=1000 + nxt, nitermax=nit, tol=tol)
-                inflight[eid] = (nxt, sl)
-                nxt += 1
-            if eng.inflight:
-                occ.append(eng.inflight)
-                for eid, e, _ in eng.step():
-                    req, sl = inflight.pop(abs(eid))
-                    lat.append(time.perf_counter() - t0 - arrivals[req])
-                    ref = templates[kinds[req]][1]
-                    dev = max(dev, abs(e - ref) / abs(ref)) if eid > 0 else float("inf")
-                    free.append(sl)
-            elif nxt < nreq:
-                time.sleep(max(0.0, min(0.002, arrivals[nxt] - (time.perf_counter() - t0))))
-        span = time.perf_counter() - t0
-        lat = np.array(lat) * 1e3
-        out["rates"].append({"lambda_req_per_s": lam, "requests": nreq, "completed_per_s": nreq / span,
-                             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                             "mean_inflight": float(np.mean(occ)) if occ else 0.0, "dE_rel_max_vs_alone_fp64": dev})
-    eng.close()
+        reqs = []
+        for _ in range(nreq):
+            L = 2 * int(rng.integers(case["L"][0] // 2, case["L"][1] // 2 + 1))
+            m = int(rng.integers(case["m"][0], case["m"][1] + 1))
+            if rng.random() < 0.5:
+                jv = float(rng.uniform(0.5, 1.5))
+                kw = dict(model=nss.MODEL_HEISENBERG_HALF, ldmrg=L // 2, mdmrg=m, msweep=(m,) * case["sweeps"],
+                          jz=jv, jxy=jv, dmrg_qn=(0.0, 0.0))
+            else:
+                kw = dict(model=nss.MODEL_HUBBARD, ldmrg=L // 2, mdmrg=m, msweep=(m,) * case["sweeps"],
+                          u=float(rng.uniform(0.0, 8.0)), hfmode=False, dmrg_qn=(0.5, 0.5))
+            kw.update(lanc_neigen=1, lanc_niter=case["lanc_niter"], lanc_tolerance=case["lanc_tolerance"])
+            reqs.append(kw)
+        row = {"lambda_req_per_s": lam, "requests": nreq}
+        for name, prec in (("mixed", nss.NSS_PREC_MIXED), ("fp64", nss.NSS_PREC_FP64)):
+            srv = nss.Server(device, hbm_budget=int(case["hbm_budget_gb"] * 2**30))
+            ids, done, lat, steps = {}, {}, [], 0
+            t0 = time.perf_counter()
+            nxt = 0
+            while len(done) < nreq:
+                now = time.perf_counter() - t0
+                while nxt < nreq and arrivals[nxt] <= now:
+                    ids[srv.submit(precision=prec, **reqs[nxt])] = nxt
+                    nxt += 1
+                for r in srv.poll():
+                    k = ids[r["id"]]
+                    done[k] = r
+                    lat.append(time.perf_counter() - t0 - arrivals[k])
+                time.sleep(0.002)
+            span = time.perf_counter() - t0
+            srv.close()                      # every request done: the counters are final
+            st = srv.last_stats
+            bad = [k for k, r in done.items() if r["status"] != 0]
+            lat = np.array(lat) * 1e3
+            row[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                         "completed_per_s": nreq / span, "solves_per_s": st["solves"] / span, "span_s": span,
+                         "failed": len(bad), "failure_codes": sorted({done[k]["status"] for k in bad}),
+                         "mean_batch": st["mean_batch"], "engine_rounds": st["rounds"],
+                         "peak_admitted_gb": st["peak_in_use"] / 2**30,
+                         "peak_measured_over_estimate": max(r["peak_bytes"] / r["footprint_est"]
+                                                            for r in done.values()),
+                         "energies": {k: r["energy"] for k, r in done.items()}}
+        # a result in the mix against the same run alone (two requests per rate)
+        dev = 0.0
+        for k in list(range(nreq))[:2]:
+            kw = dict(reqs[k], precision=nss.NSS_PREC_MIXED)
+            key = repr(sorted(kw.items()))
+            if key not in alone:
+                d = nss.DMRG(device=device, **kw)
+                alone[key] = d.finite()[-1]["energy"][0]
+                d.close()
+            e = row["mixed"]["energies"][k]
+            dev = max(dev, abs(e - alone[key]) / abs(alone[key]))
+        for name in ("mixed", "fp64"):
+            row[name].pop("energies")
+        row["dE_rel_max_mix_vs_alone"] = dev
+        row["speedup_mixed_vs_fp64_completed"] = row["mixed"]["completed_per_s"] / row["fp64"]["completed_per_s"]
+        out["rates"].append(row)
     return out
 
 
@@ -620,7 +639,8 @@ def run_gpu(args):
         case["workload"] = f"heisenberg_one_L64_M512_{args.large_sweeps}sweeps"
         sweeps_large = measure_sweeps(nss, local, case, warm=False)
     batch = measure_batch(nss, local) if not args.no_batch else None
-    serving = measure_serving(nss, local) if not args.no_serving else None
+    serving = (measure_serving(nss, local, SERVE_CASE_FULL if args.serve_full else None)
+               if not args.no_serving else None)
 
     out = None
     if rank == 0:

@@ -427,6 +427,37 @@ int       nss_dmrg_prepare_last(nss_dmrg *d);
  * the next call on d). */
 int       nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out);
 int       nss_dmrg_nrecords(const nss_dmrg *d);
+/* Serving: whole DMRG runs (nss_dmrg_finite with the given parameters, one
+ * ground state per step) as requests.  The server admits queued requests,
+ * first come first served, while the sum of their estimated HBM footprints
+ * (nss_server_footprint: the Krylov basis of the largest superblock of the
+ * run, its work vectors, sector operators and rho blocks) stays within
+ * hbm_budget (one request always runs).  Each admitted request runs on a
+ * worker thread with its own context and its block state resident on the
+ * device; the mixed-precision ground-state solves of all running requests
+ * share one batch engine (the persistent multi-solve Lanczos kernel), joining
+ * it as they arrive; the requests' device phases take turns with the
+ * engine's rounds.  nss_server_poll returns finished requests (energy per
+ * site of the last step, seconds queued before admission and in service,
+ * the footprint estimate and the context's measured peak).
+ * nss_server_destroy waits for every submitted request.  No counterpart in
+ * the reference. */
+typedef struct nss_server nss_server;
+typedef struct {
+    int32_t id, status;
+    double  energy;
+    double  wait_s, service_s;
+    size_t  footprint_est, peak_bytes;
+} nss_served;
+nss_server *nss_server_create(int device, size_t hbm_budget);
+size_t      nss_server_footprint(const nss_dmrg_params *p);
+int         nss_server_submit(nss_server *s, const nss_dmrg_params *p, int *id);
+int         nss_server_poll(nss_server *s, int max, nss_served *out);
+int         nss_server_stats(nss_server *s, int *queued, int *running, size_t *in_use, size_t *peak_in_use,
+                             int64_t *rounds, double *mean_batch);
+int64_t     nss_server_solves(nss_server *s);   /* ground-state solves of served requests so far */
+void        nss_server_destroy(nss_server *s);
+
 /* Block restart files in the reference's text format (write_block /
  * read_block, src/BLOCKS/BLOCKS.f90:418-537; sector, operator and rotation
  * lists and sparse matrices as src/LIST/LIST_SECTORS.f90:639-705,

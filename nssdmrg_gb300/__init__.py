@@ -81,6 +81,11 @@ class DmrgParams(C.Structure):
                 ("save_umat", C.c_int32), ("edmrg", C.c_double), ("esweep", C.POINTER(C.c_double))]
 
 
+class Served(C.Structure):
+    _fields_ = [("id", C.c_int32), ("status", C.c_int32), ("energy", C.c_double), ("wait_s", C.c_double),
+                ("service_s", C.c_double), ("footprint_est", C.c_size_t), ("peak_bytes", C.c_size_t)]
+
+
 class StepRecord(C.Structure):
     _fields_ = [("type", C.c_int32), ("left_length", C.c_int32), ("right_length", C.c_int32),
                 ("current_l", C.c_int32), ("n", C.c_int64), ("nsb", C.c_int32), ("numop", C.c_int32),
@@ -133,6 +138,14 @@ def lib():
         "nss_eigh": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_int, P, P, C.POINTER(C.c_int)]),
         "nss_tune_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "nss_tune_reset": (None, []),
+        "nss_server_create": (P, [C.c_int, C.c_size_t]),
+        "nss_server_footprint": (C.c_size_t, [C.POINTER(DmrgParams)]),
+        "nss_server_submit": (C.c_int, [P, C.POINTER(DmrgParams), C.POINTER(C.c_int)]),
+        "nss_server_poll": (C.c_int, [P, C.c_int, C.POINTER(Served)]),
+        "nss_server_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_size_t),
+                                       C.POINTER(C.c_size_t), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+        "nss_server_destroy": (None, [P]),
+        "nss_server_solves": (C.c_int64, [P]),
         "nss_rdm": (C.c_int, [P, P, C.c_int, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_rdm_estates": (C.c_int, [P, P, C.c_int, D, D, C.POINTER(RdmSide), P, P, P, P, P, P]),
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
@@ -619,6 +632,82 @@ class Superblock:
                          (out[0].s_number, out[1].s_number), (out[0].s_config, out[1].s_config))
 
 
+def dmrg_params(model, ldmrg, mdmrg, msweep=(), jz=1.0, jxy=1.0, t=1.0, u=0.0, hfmode=True, dmrg_qn=(0.0, 0.0),
+                lanc_neigen=1, lanc_niter=512, lanc_tolerance=1e-12, deg_evals_threshold=0.1, seed=1234,
+                precision=NSS_PREC_FP64, save_umat=False, edmrg=0.0, esweep=()):
+    """nss_dmrg_params (and the arrays it points to, which must outlive it)."""
+    p = DmrgParams()
+    p.model, p.jz, p.jxy, p.t, p.u, p.hfmode = model, jz, jxy, t, u, int(hfmode)
+    p.dmrg_qn[0] = dmrg_qn[0]
+    p.dmrg_qn[1] = dmrg_qn[1] if len(dmrg_qn) > 1 else 0.0
+    p.ldmrg, p.mdmrg = ldmrg, mdmrg
+    ms = np.ascontiguousarray(msweep, np.int32) if len(msweep) else np.zeros(1, np.int32)
+    p.nsweep = len(msweep)
+    p.msweep = _p(ms, C.c_int32)
+    p.lanc_neigen, p.lanc_niter, p.lanc_tolerance = lanc_neigen, lanc_niter, lanc_tolerance
+    p.deg_evals_threshold, p.seed, p.precision = deg_evals_threshold, seed, precision
+    p.save_umat = int(save_umat)
+    p.edmrg = edmrg
+    es = np.ascontiguousarray(esweep, np.float64) if len(esweep) else None
+    if es is not None:
+        if len(es) != len(msweep):
+            raise NssError(NSS_ERR_INVALID, "esweep needs one entry per sweep")
+        p.esweep = _p(es, C.c_double)
+    return p, ms, es
+
+
+class Server:
+    """Whole DMRG runs served as requests (nss_server_*): admission by HBM
+    footprint, one worker context per running request, the mixed ground-state
+    solves of all running requests batched in one engine."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._s = lib().nss_server_create(device, hbm_budget)
+        if not self._s:
+            raise NssError(NSS_ERR_CUDA, lib().nss_last_error(None).decode())
+        self._keep = {}
+
+    @staticmethod
+    def footprint(**kw) -> int:
+        p, ms, es = dmrg_params(**kw)
+        return int(lib().nss_server_footprint(C.byref(p)))
+
+    def submit(self, **kw) -> int:
+        """Queue one run (keyword arguments as for DMRG); returns its id."""
+        p, ms, es = dmrg_params(**kw)
+        rid = C.c_int()
+        rc = lib().nss_server_submit(self._s, C.byref(p), C.byref(rid))
+        if rc != NSS_OK:
+            raise NssError(rc, "nss_server_submit: invalid request")
+        return rid.value
+
+    def poll(self, max_n: int = 256):
+        out = (Served * max_n)()
+        n = lib().nss_server_poll(self._s, max_n, out)
+        return [{k: getattr(r, k) for k, _ in Served._fields_} for r in out[:max(n, 0)]]
+
+    def stats(self):
+        q, r, iu, pk, rounds, mb = C.c_int(), C.c_int(), C.c_size_t(), C.c_size_t(), C.c_int64(), C.c_double()
+        lib().nss_server_stats(self._s, C.byref(q), C.byref(r), C.byref(iu), C.byref(pk), C.byref(rounds),
+                               C.byref(mb))
+        return {"queued": q.value, "running": r.value, "in_use": iu.value, "peak_in_use": pk.value,
+                "rounds": rounds.value, "mean_batch": mb.value, "solves": int(lib().nss_server_solves(self._s))}
+
+    def close(self):
+        """Wait for every submitted request and release the server; its last
+        counters stay in `last_stats`."""
+        if self._s:
+            self.last_stats = self.stats()
+            lib().nss_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class DMRG:
     """init_dmrg / run_DMRG with every superblock solve on the GPU."""
 
@@ -627,23 +716,9 @@ class DMRG:
                  deg_evals_threshold=0.1, seed=1234, precision=NSS_PREC_FP64, device=0, sb=None,
                  save_umat=False, edmrg=0.0, esweep=()):
         self.sb = sb or Superblock(device)
-        p = DmrgParams()
-        p.model, p.jz, p.jxy, p.t, p.u, p.hfmode = model, jz, jxy, t, u, int(hfmode)
-        p.dmrg_qn[0] = dmrg_qn[0]
-        p.dmrg_qn[1] = dmrg_qn[1] if len(dmrg_qn) > 1 else 0.0
-        p.ldmrg, p.mdmrg = ldmrg, mdmrg
-        self._ms = np.ascontiguousarray(msweep, np.int32) if len(msweep) else np.zeros(1, np.int32)
-        p.nsweep = len(msweep)
-        p.msweep = _p(self._ms, C.c_int32)
-        p.lanc_neigen, p.lanc_niter, p.lanc_tolerance = lanc_neigen, lanc_niter, lanc_tolerance
-        p.deg_evals_threshold, p.seed, p.precision = deg_evals_threshold, seed, precision
-        p.save_umat = int(save_umat)
-        p.edmrg = edmrg
-        self._es = np.ascontiguousarray(esweep, np.float64) if len(esweep) else None
-        if self._es is not None:
-            if len(self._es) != len(msweep):
-                raise NssError(NSS_ERR_INVALID, "esweep needs one entry per sweep")
-            p.esweep = _p(self._es, C.c_double)
+        p, self._ms, self._es = dmrg_params(model, ldmrg, mdmrg, msweep, jz, jxy, t, u, hfmode, dmrg_qn, lanc_neigen,
+                                            lanc_niter, lanc_tolerance, deg_evals_threshold, seed, precision,
+                                            save_umat, edmrg, esweep)
         self._p = p
         self._d = lib().nss_dmrg_create(self.sb._ctx, C.byref(p))
         if not self._d:

@@ -83,6 +83,8 @@ int ensure_tmp(nss_ctx *ctx, int64_t n) {
 
 }  // namespace
 
+nss::Ctx &nss::ctx_of(nss_ctx *ctx) { return ctx->c; }
+
 extern "C" {
 
 nss_ctx *nss_create(int device, size_t hbm_budget) {

@@ -232,6 +232,8 @@ struct Ctx {
     char *ms_dev = nullptr, *ms_host = nullptr;   // OdotV tables: device, pinned staging
     size_t ms_cap = 0;   // host: scan+extract, device wait, CSR assembly (summed over calls)
     double *noalloc_scratch = nullptr;   // device address of k_noalloc.cu's static scratch, looked up on first use
+    struct Server *serve = nullptr;      // the server running this context's requests (host_serve.cpp)
+    size_t peak_used = 0;                // largest `used` so far
 };
 
 // Allocation through the context budget.
@@ -243,6 +245,7 @@ cudaError_t ctx_alloc(Ctx &c, T **p, size_t count) {
     cudaError_t e = cudaMalloc((void **)p, bytes);
     if (e == cudaSuccess) {
         c.used += bytes;
+        c.peak_used = c.used > c.peak_used ? c.used : c.peak_used;
         c.sizes[(void *)*p] = bytes;
     }
     return e;
@@ -281,6 +284,21 @@ bool mma_lolo_default();
 // return and the entry point report NSS_ERR_CUDA; the tests shorten the
 // limit to exercise that path.
 uint32_t wait_limit();
+
+// host_serve.cpp: a served context's device phases take the server's device
+// lock (ServeLock is a no-op for other contexts), and its mixed ground-state
+// solves go to the server's batch engine
+struct Server;
+struct ServeLock {
+    Server *s;
+    explicit ServeLock(Ctx &c);
+    ~ServeLock();
+    void unlock();
+    ServeLock(const ServeLock &) = delete;
+    ServeLock &operator=(const ServeLock &) = delete;
+};
+int serve_solve(Ctx &c, int nitermax, double tol, uint64_t seed, double *energy, int *numop);
+void serve_count(Ctx &c);   // one more ground-state solve of a served request
 
 // tile_tune.cpp: the mixed path's plan per shape class of superblock
 bool tune_enabled();

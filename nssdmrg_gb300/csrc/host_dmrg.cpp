@@ -412,7 +412,11 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     const auto t_up = std::chrono::steady_clock::now();
     SbView v;
     sb_view(sb, v);
-    int rc = sb_upload(c, &v.desc, true);
+    int rc;
+    {
+        ServeLock g(c);   // a served request's device phases take turns with the others'
+        rc = sb_upload(c, &v.desc, true);
+    }
     if (rc) return rc;
     rec.host_phase_ms[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_up).count();
     const int64_t n = sb.n();
@@ -425,8 +429,16 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     cudaEventCreate(&e1);
     cudaEventCreate(&em);
     cudaEventRecord(e0, c.stream);
-    rc = lanczos_eigh(c, neigen, nitermax, p.lanc_tolerance, p.seed, p.precision, ev, &numop);
+    if (c.serve && p.precision == NSS_PREC_MIXED && neigen == 1) {
+        // served: the solve joins the server's batch engine with the other requests'
+        rc = serve_solve(c, nitermax, p.lanc_tolerance, p.seed, ev, &numop);
+    } else {
+        ServeLock g(c);
+        rc = lanczos_eigh(c, neigen, nitermax, p.lanc_tolerance, p.seed, p.precision, ev, &numop);
+    }
     if (rc) return rc;
+    serve_count(c);
+    ServeLock g_rdm(c);   // the RDM and the device renormalisation below
     cudaEventRecord(em, c.stream);
     nss_rdm_side side[2];
     // operator renormalisation: QN-block GEMMs on the device for blocks of

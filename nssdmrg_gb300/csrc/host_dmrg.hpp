@@ -12,6 +12,8 @@
 namespace nss {
 
 struct Ctx;
+// the library context behind a C ABI handle (capi.cpp)
+Ctx &ctx_of(nss_ctx *ctx);
 
 Block spin_site(int sun);
 Block electron_site(double uloc, bool hfmode);
