@@ -59,11 +59,13 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-full", action="store_true",
                     help="serve the fifth configuration's full size ranges (L up to 64, m up to 512) at low rates")
-    ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large"], default=None,
+    ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large", "tc-sector"], default=None,
                     help="for profiler captures of single kernels: run one small workload and exit "
                          "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
                          "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction; "
-                         "sweep-large: the finite sweep of the spin-1 L=64 m=512 chain in --precision)")
+                         "sweep-large: the finite sweep of the spin-1 L=64 m=512 chain in --precision; "
+                         "tc-sector: four FP32 H*psi of the spin-1 L=64 m=512 chain's last infinite "
+                         "superblock with every sector of >= 32 left states on the tensor-core GEMM)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -430,6 +432,23 @@ def run_profile_case(case, precision="mixed"):
         recs = d.infinite()
         print(json.dumps({"profile_case": case, "steps": len(recs), "m_last": recs[-1]["m_left"],
                           "ms_renorm_last": [round(r["ms_renorm"], 3) for r in recs[-4:]]}))
+        return
+    if case == "tc-sector":
+        import torch as _t
+        d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, dmrg_qn=(0.0, 0.0), lanc_neigen=1,
+                     precision=nss.NSS_PREC_MIXED)
+        d.prepare_last()
+        desc = d.export_superblock()
+        os.environ.update(NSS_TC_MIN_DL="32", NSS_TC_BN="64")
+        s = nss.Superblock(0)
+        s.upload_desc(desc)
+        v = _t.rand(s.n, device="cuda") * 2 - 1
+        hv = _t.empty_like(v)
+        for _ in range(4):
+            s.hv_device_f32(v.data_ptr(), hv.data_ptr())
+        _t.cuda.synchronize()
+        fd, _ = s.flops()
+        print(json.dumps({"profile_case": case, "N": s.n, "flops_dense": fd}))
         return
     if case == "sweep-large":
         d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, msweep=[512], dmrg_qn=(0.0, 0.0), lanc_neigen=1,
