@@ -68,14 +68,16 @@ struct DevSb {
     int4 *d_term_hdr = nullptr;        // per FP32 term: input-sector offset (lo, hi), its Dr
     int *d_tc_err = nullptr;           // set when a tensor-core pipeline wait ran out
     // tensor-core sector GEMM (k_sector_mma.cu), sections of the upload arena:
-    // operand pool [2 planes][rows][32] FP32 (hi, lo), output planes [2][n],
-    // work items, 32x32 W tiles and their per-sector pack records; the two
-    // tensor maps (128-row and BN-row boxes) over the pool
+    // operand pool [rows][32] FP32, output planes [nplanes][n], work items
+    // with their per-CTA ranges, 32x32 W tiles and their per-sector pack
+    // records; the two tensor maps (128-row and BN-row boxes) over the pool
     float *d_mma_pool = nullptr, *d_mma_out = nullptr;
     struct MmaItem *d_mma_items = nullptr;
+    int2 *d_mma_rng = nullptr;
     int4 *d_mma_wt = nullptr;
     struct PackSec *d_mma_sec = nullptr;
     int mma_nitems = 0, mma_nwt = 0, mma_plane_rows = 0, mma_bn = 64;
+    int mma_nplanes = 0, mma_grid = 0;
     bool mma_split = true;
     alignas(64) unsigned char mma_map_a[128] = {}, mma_map_b[128] = {};
 };
@@ -112,6 +114,9 @@ struct DevLanczos {
     float *slot32 = nullptr;     // [3][n] H*psi parts of the persistent chunk kernel
     size_t chunk_smem = 0;
     bool chunk_ok = false;       // the chunk kernel fits (one CTA per SM)
+    int chunk_vc = 0;            // basis vectors in its shared-memory row cache (0: no cache)
+    int chunk_cs = 0;            // cached floats per vector (rows of one CTA)
+    size_t chunk_smem_vc = 0;    // its dynamic shared memory with the row cache
     float *pitem = nullptr;      // per-item alpha partials of the batched kernel
     int cap_pitem = 0;
 };
@@ -389,9 +394,11 @@ int syev_eigs_per_cta();
 // k_rdm.cu
 // kl (may be null): per side, the kept columns left on the device
 // mstates = 0 with estates != 0 selects the Edmrg (error threshold) rule
+// vec_sides: bit s set = side s gets its kept vectors (U, kept indices, kl);
+// the other side only its spectrum, truncation, error and entropies
 int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg_thr, nss_rdm_side out[2],
             double *lam_l, double *lam_r, int32_t *kept_l, int32_t *kept_r,
-            double *u_l, double *u_r, KeptLayout *kl = nullptr);
+            double *u_l, double *u_r, KeptLayout *kl = nullptr, int vec_sides = 3);
 void rdm_release(Ctx &c);
 
 // k_renorm.cu: blk's operators <- U^T O U for the kept columns kl, blk's

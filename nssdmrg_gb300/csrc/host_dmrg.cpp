@@ -249,10 +249,13 @@ int Driver::init(Ctx *c, const nss_dmrg_params &params) {
 }
 
 int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, double estates,
-                   bool renormalize, Block &left, Block &right, nss_step_record &rec);
+                   bool renormalize, Block &left, Block &right, nss_step_record &rec, int keep_sides);
 
-// step_dmrg (src/DMRG_MAIN.f90:262-433), OBC link 'n'
-int Driver::step(int type, int label, int sweep) {
+// step_dmrg (src/DMRG_MAIN.f90:262-433), OBC link 'n'.  keep_sides: bit 0
+// left, bit 1 right; a side left out is not renormalised (its block is
+// replaced from the stored list before the next step uses it), its spectrum,
+// truncation error and entropies are still formed
+int Driver::step(int type, int label, int sweep, int keep_sides) {
     const auto t_step = std::chrono::steady_clock::now();
     // Mstates/Estates of step_dmrg (src/DMRG_MAIN.f90:288-295): Mdmrg/Edmrg
     // while growing, Msweep/Esweep of the sweep afterwards
@@ -293,7 +296,7 @@ int Driver::step(int type, int label, int sweep) {
     rec.ms_build = ms_since(t_step);
     rec.host_phase_ms[0] = ms_enlarge;
     rec.host_phase_ms[1] = ms_sb;
-    int rc = nss_solve_step(*ctx, sb, p, mstates, estates, renorm, left, right, rec);
+    int rc = nss_solve_step(*ctx, sb, p, mstates, estates, renorm, left, right, rec, keep_sides);
     if (rc) return rc;
     rec.ms_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     records.push_back(rec);
@@ -350,22 +353,27 @@ int Driver::finite() {
         lb[left.length] = left;
         rb[right.length] = right;
     }
-    for (int im = 1; im <= (int)msweep.size(); ++im) {
+    // the environment block of a step is loaded from the stored list; its
+    // renormalised copy is only used when the sweep turns on it (the last
+    // step of each half sweep) or when the run ends there
+    const int nsw = (int)msweep.size();
+    for (int im = 1; im <= nsw; ++im) {
         while (left.length < fN) {
             right = rb[fN - left.length];
-            int rc = step(1, 1, im);
+            int rc = step(1, 1, im, left.length + 1 < fN ? 1 : 3);
             if (rc) return rc;
             lb[left.length] = left;
         }
         while (right.length < fN) {
             left = lb[fN - right.length];
-            int rc = step(1, 2, im);
+            int rc = step(1, 2, im, right.length + 1 < fN ? 2 : 3);
             if (rc) return rc;
             rb[right.length] = right;
         }
         while (left.length <= p.ldmrg) {
             right = rb[fN - left.length];
-            int rc = step(1, 1, im);
+            const bool last = left.length + 1 > p.ldmrg && im == nsw;
+            int rc = step(1, 1, im, last ? 3 : 1);
             if (rc) return rc;
             lb[left.length] = left;
         }
@@ -408,7 +416,7 @@ void renormalize(Block &blk, const Csr &u, const std::vector<Qn> &kept_qn) {
 }  // namespace
 
 int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstates, double estates, bool renorm, Block &left,
-                   Block &right, nss_step_record &rec) {
+                   Block &right, nss_step_record &rec, int keep_sides) {
     const auto t_up = std::chrono::steady_clock::now();
     SbView v;
     sb_view(sb, v);
@@ -452,17 +460,18 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     std::vector<int32_t> k_l, k_r;
     // m_s is known only after the truncation kernel: size for the maximum
     // (the dense U only for the host renormalisation)
+    const bool ren_l = renorm && (keep_sides & 1), ren_r = renorm && (keep_sides & 2);
     if (renorm && !dev_renorm) {
-        u_l.resize((size_t)sb.m_left * sb.m_left);
-        u_r.resize((size_t)sb.m_right * sb.m_right);
+        if (ren_l) u_l.resize((size_t)sb.m_left * sb.m_left);
+        if (ren_r) u_r.resize((size_t)sb.m_right * sb.m_right);
     }
     k_l.resize(sb.m_left);
     k_r.resize(sb.m_right);
     KeptLayout kl[2];
     rc = rdm_run(c, c.lz.evecs, mstates, estates, p.deg_evals_threshold, side, nullptr, nullptr,
-                 renorm ? k_l.data() : nullptr, renorm ? k_r.data() : nullptr,
-                 (renorm && !dev_renorm) ? u_l.data() : nullptr, (renorm && !dev_renorm) ? u_r.data() : nullptr,
-                 dev_renorm ? kl : nullptr);
+                 ren_l ? k_l.data() : nullptr, ren_r ? k_r.data() : nullptr,
+                 (ren_l && !dev_renorm) ? u_l.data() : nullptr, (ren_r && !dev_renorm) ? u_r.data() : nullptr,
+                 dev_renorm ? kl : nullptr, renorm ? keep_sides : 3);
     if (rc) return rc;
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
@@ -491,23 +500,30 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
     rec.m_right = right.dim;
     if (renorm) {
         std::vector<Qn> ql, qr;
-        for (int j = 0; j < side[0].m_s; ++j) ql.push_back(sb.qns[k_l[j]]);
-        for (int j = 0; j < side[1].m_s; ++j) {
-            Qn q = sb.target;
-            for (size_t t = 0; t < q.size(); ++t) q[t] -= sb.qns[k_r[j]][t];
-            qr.push_back(q);
-        }
+        if (ren_l)
+            for (int j = 0; j < side[0].m_s; ++j) ql.push_back(sb.qns[k_l[j]]);
+        if (ren_r)
+            for (int j = 0; j < side[1].m_s; ++j) {
+                Qn q = sb.target;
+                for (size_t t = 0; t < q.size(); ++t) q[t] -= sb.qns[k_r[j]][t];
+                qr.push_back(q);
+            }
         const auto t_r = std::chrono::steady_clock::now();
         for (double &x : c.renorm_phase_ms) x = 0.0;
         if (dev_renorm) {
             if (p.save_umat) {
                 // put_omat(str(length), trRho) (src/DMRG_RDM.f90:225, :298)
                 Csr ul, ur;
-                if ((rc = kept_u_csr(c, kl[0], left.dim, ul)) || (rc = kept_u_csr(c, kl[1], right.dim, ur))) return rc;
-                left.omats.push_back(std::make_shared<const Csr>(std::move(ul)));
-                right.omats.push_back(std::make_shared<const Csr>(std::move(ur)));
+                if (ren_l) {
+                    if ((rc = kept_u_csr(c, kl[0], left.dim, ul))) return rc;
+                    left.omats.push_back(std::make_shared<const Csr>(std::move(ul)));
+                }
+                if (ren_r) {
+                    if ((rc = kept_u_csr(c, kl[1], right.dim, ur))) return rc;
+                    right.omats.push_back(std::make_shared<const Csr>(std::move(ur)));
+                }
             }
-            Block *bl[2] = {&left, &right};
+            Block *bl[2] = {ren_l ? &left : nullptr, ren_r ? &right : nullptr};
             const std::vector<Qn> *kq[2] = {&ql, &qr};
             if ((rc = renorm_device(c, kl, bl, kq))) return rc;
             rec.nnz_u = 0;
@@ -518,18 +534,20 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
             // the two blocks are independent (a thread pays off from ~10^4 entries)
             run_pair(
                 [&] {
+                    if (!ren_l) return;
                     cul = u_to_csr(u_l, sb.m_left, side[0].m_s);
                     renormalize(left, cul, ql);
                 },
                 [&] {
+                    if (!ren_r) return;
                     cur = u_to_csr(u_r, sb.m_right, side[1].m_s);
                     renormalize(right, cur, qr);
                 },
                 (int64_t)sb.m_left * side[0].m_s + (int64_t)sb.m_right * side[1].m_s > 8000);
-            rec.nnz_u = cul.nnz() + cur.nnz();
+            rec.nnz_u = (ren_l ? cul.nnz() : 0) + (ren_r ? cur.nnz() : 0);
             if (p.save_umat) {
-                left.omats.push_back(std::make_shared<const Csr>(cul));
-                right.omats.push_back(std::make_shared<const Csr>(cur));
+                if (ren_l) left.omats.push_back(std::make_shared<const Csr>(cul));
+                if (ren_r) right.omats.push_back(std::make_shared<const Csr>(cur));
             }
         }
         rec.nnz_ops = 0;
@@ -539,8 +557,9 @@ int nss_solve_step(Ctx &c, const SbHost &sb, const nss_dmrg_params &p, int mstat
         for (int i = 0; i < 3; ++i) rec.host_phase_ms[3 + i] = c.renorm_phase_ms[i];
         rec.trunc_left = side[0].trunc_err;
         rec.trunc_right = side[1].trunc_err;
-        rec.m_left = left.dim;
-        rec.m_right = right.dim;
+        // a side not renormalised reports the dimension it would have had
+        rec.m_left = ren_l ? left.dim : side[0].m_s;
+        rec.m_right = ren_r ? right.dim : side[1].m_s;
     }
     return NSS_OK;
 }

@@ -38,7 +38,7 @@ struct Driver {
     std::shared_ptr<SbHost> last_sb;   // superblock of the step stopped at
 
     int init(Ctx *c, const nss_dmrg_params &params);
-    int step(int type, int label, int sweep);
+    int step(int type, int label, int sweep, int keep_sides = 3);
     int infinite();
     int finite();
     // Build_Op_dmrg + Advance_Op_dmrg: the site operator op (dot basis) at

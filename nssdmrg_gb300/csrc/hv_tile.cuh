@@ -134,14 +134,17 @@ struct Hv32Ops {
     const int2 *ell;             // (column, value bits) of A rows / B columns
     const int4 *term_hdr;        // per term: offset of its input sector (lo, hi), its Dr
     // output planes of the tensor-core sector GEMM (null when it has no
-    // sectors): a "terms only" tile adds both to its A x B terms
-    const float *tc0, *tc1;
+    // sectors): a "terms only" tile adds them, plane 0 first, to its A x B
+    // terms; tcn planes, tcs floats apart
+    const float *tc;
+    int tcn;
+    int64_t tcs;
 };
 
 // One 32x32 FP32 output tile t = (sector, row0, col0, flags) by 256 threads
 // (lt = thread index in the group), each owning rows {ty, ty+16} x columns
 // {tx, tx+16}.  A "terms only" tile (t.w & 1) skips the two dense products
-// and adds them from the tensor-core output planes op.tc0 / op.tc1 instead.
+// and adds them from the tensor-core output planes op.tc instead.
 // The outputs, multiplied by `scale`, go to hv; returns this thread's share
 // of sum_i v[i] * out[i] * scale^2 over its outputs (the Lanczos alpha of a
 // unit vector v * scale), meaningful for whole tiles (t.w == 0).
@@ -235,7 +238,11 @@ __device__ __forceinline__ float hv32_tile(int4 t, const float *__restrict__ v, 
             if (il < dl && ir < dr) {
                 const int64_t idx = (int64_t)il * dr + ir;
                 float y = acc[rr][cc] * scale;
-                if ((t.w & 1) && op.tc0) y += op.tc0[o + idx] + op.tc1[o + idx];
+                if ((t.w & 1) && op.tc) {
+                    float d = op.tc[o + idx];
+                    for (int p = 1; p < op.tcn; ++p) d += op.tc[(int64_t)p * op.tcs + o + idx];
+                    y += d;
+                }
                 hv[o + idx] = y;
                 part = fmaf(W[idx] * scale, y, part);
             }

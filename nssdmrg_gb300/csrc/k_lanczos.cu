@@ -56,6 +56,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 namespace nss {
@@ -78,6 +80,24 @@ double mixed_tol() {
     }();
     return v;
 }
+// Raise a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`.  The attribute belongs to the kernel, shared by every
+// context of the process, so it only ever grows: a context sized for a
+// smaller basis must not take the room a larger one was set up with.
+inline cudaError_t allow_smem(const void *fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &cur = done[{dev, fn}];
+    if (bytes <= cur) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 constexpr int ORTH_THREADS = 512;
 constexpr int ORTH_WARPS = ORTH_THREADS / 32;
 
@@ -381,14 +401,33 @@ __device__ __forceinline__ void block_sums(R (&v)[NV], R *scr) {
     }
 }
 
+// p[i0] + p[i0 + stride] + ... (indices below end), added in that order;
+// the loads go out eight at a time, so a sum over the partials of a grid
+// costs one L2 round trip instead of one per term (an add waiting for its
+// load stalls the warp's next load: the loop form issued them one by one)
+template <class R>
+__device__ __forceinline__ R strided_sum(const R *p, int i0, int end, int stride) {
+    R t = (R)0;
+    for (int b0 = i0; b0 < end; b0 += 8 * stride) {
+        R v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int b = b0 + q * stride;
+            v[q] = b < end ? __ldcg(p + b) : (R)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) t += v[q];
+    }
+    return t;
+}
+
 // sums of the G per-CTA partials of NV columns p[q*G + b], same order in
 // every CTA; warp q reduces column q, results broadcast through bc[]
 template <class R, int NV>
 __device__ __forceinline__ void grid_totals(const R *p, int G, R *bc, R (&out)[NV]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp < NV) {
-        R t = (R)0;
-        for (int b = lane; b < G; b += 32) t += __ldcg(p + (int64_t)warp * G + b);
+        R t = strided_sum<R>(p + (int64_t)warp * G, lane, G, 32);
         t = warp_sum<R>(t);
         if (lane == 0) bc[warp] = t;
     }
@@ -397,17 +436,28 @@ __device__ __forceinline__ void grid_totals(const R *p, int G, R *bc, R (&out)[N
     for (int q = 0; q < NV; ++q) out[q] = bc[q];
 }
 
-// hs[l] = sum_b p[l*G + b] for l < ncol (four columns per warp in flight)
+// hs[l] = sum_b p[l*G + b] for l < ncol (four columns per warp in flight;
+// all their loads issued before the first add)
 template <class R>
 __device__ __forceinline__ void grid_columns(const R *p, int G, int ncol, R *hs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int l0 = warp; l0 < ncol; l0 += 4 * ORTH_WARPS) {
         R t[4] = {(R)0, (R)0, (R)0, (R)0};
+        for (int b0 = lane; b0 < G; b0 += 8 * 32) {
+            R v[4][8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int l = l0 + u * ORTH_WARPS;
-            if (l < ncol)
-                for (int b = lane; b < G; b += 32) t[u] += __ldcg(p + (int64_t)l * G + b);
+            for (int u = 0; u < 4; ++u) {
+                const int l = l0 + u * ORTH_WARPS;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int b = b0 + 32 * q;
+                    v[u][q] = (l < ncol && b < G) ? __ldcg(p + (int64_t)l * G + b) : (R)0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) t[u] += v[u][q];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -513,7 +563,7 @@ __host__ __device__ inline int orth_redsz(int pstride, int cw) {
 }
 
 // shared memory of k_orth, in elements of T: hs, red, scratch
-inline size_t orth_smem(int pstride, int cw, size_t tsize) {
+__host__ __device__ inline size_t orth_smem(int pstride, int cw, size_t tsize) {
     return (size_t)(pstride + orth_redsz(pstride, cw) + 8 * ORTH_WARPS + 16) * tsize;
 }
 
@@ -696,13 +746,92 @@ struct ChunkArgs {
     const ItemRec *items;
     int nitems;
     Hv32Ops op;
+    // shared-memory copy of the CTA's rows: basis vectors V[l < vc] and the
+    // work vector, `cs` floats per vector (0: everything from global memory)
+    int vc = 0, cs = 0;
 };
 
 constexpr int CHUNK_EXTRA = 8;   // extra partial columns of the anchored refinement
 constexpr int CHUNK_MAXIT = 16;  // iterations per launch (>= CHECK)
 
-inline size_t chunk_smem(int pstride) {
+__host__ __device__ inline size_t chunk_smem(int pstride) {
     return 2 * sizeof(Item32Smem) + orth_smem(pstride, OrthCW<float>::value, sizeof(float));
+}
+
+// offset of the row cache in k_chunk32's dynamic shared memory
+__host__ __device__ inline size_t chunk_cache_off(int pstride) { return (chunk_smem(pstride) + 15) & ~(size_t)15; }
+
+// dynamic shared memory k_chunk32 may take: the 227 KB of one CTA less room
+// for its static arrays
+constexpr size_t CHUNK_SMEM_MAX = 232448 - 2048;
+
+// NSS_CHUNK_CACHE=0 turns the row cache off (comparisons, experiments)
+inline bool chunk_cache_enabled() {
+    const char *e = std::getenv("NSS_CHUNK_CACHE");
+    return !(e && std::atoi(e) == 0);
+}
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// cta_dots on the row cache: the CTA's rows of V[l] (l < vc) at vs[l*cs + r]
+// and of w at ws[r] (r = row - i0); columns l >= vc come from V in global
+// memory.  Same items, rows and accumulation order as cta_dots.
+template <int CW>
+__device__ __forceinline__ void cta_dots_vc(const float *__restrict__ vs, int vc, int cs, const float *__restrict__ V,
+                                            int m, const float *__restrict__ ws, int64_t n, int64_t i0, int64_t i1,
+                                            bool ww, float *red, float *out, int G) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncol = m + (ww ? 1 : 0);
+    const int ng = (ncol + CW - 1) / CW;
+    const int nq = ng >= ORTH_WARPS ? 1 : ORTH_WARPS / ng;
+    const int rs = ng * CW;
+    const int len = (int)(i1 - i0), qlen = (len + nq - 1) / nq;
+    const float *Vg = V + i0;
+    for (int item = warp; item < ng * nq; item += ORTH_WARPS) {
+        const int g = item % ng, q = item / ng, l0 = g * CW;
+        const int r0 = q * qlen, r1 = min(len, r0 + qlen);
+        float acc[CW];
+#pragma unroll
+        for (int c = 0; c < CW; ++c) acc[c] = 0.f;
+        if (l0 + CW <= m && l0 + CW <= vc) {
+            const float *vr = vs + l0 * cs;
+            for (int r = r0 + lane; r < r1; r += 32) {
+                const float wv = ws[r];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) acc[c] += vr[c * cs + r] * wv;
+            }
+        } else if (l0 + CW <= m && l0 >= vc) {
+            const float *vr = Vg + (int64_t)l0 * n;
+            for (int r = r0 + lane; r < r1; r += 32) {
+                const float wv = ws[r];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) acc[c] += vr[(int64_t)c * n + r] * wv;
+            }
+        } else {
+            for (int r = r0 + lane; r < r1; r += 32) {
+                const float wv = ws[r];
+#pragma unroll
+                for (int c = 0; c < CW; ++c) {
+                    const int l = l0 + c;
+                    if (l < m) acc[c] += (l < vc ? vs[l * cs + r] : Vg[(int64_t)l * n + r]) * wv;
+                    else if (ww && l == m) acc[c] += wv * wv;
+                }
+            }
+        }
+        const float s = multi_reduce<float, CW>(acc, lane);
+        if (lane < CW && l0 + lane < ncol) red[q * rs + l0 + lane] = s;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < ncol; l += ORTH_THREADS) {
+        float s = 0.f;
+        for (int q = 0; q < nq; ++q) s += red[q * rs + l];
+        out[(int64_t)l * G] = s;
+    }
 }
 
 __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
@@ -734,6 +863,24 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
     const bool anc = au != nullptr;
     const int nd = anc ? a.o.ndefl : 0;
     const int nx = anc ? 3 + nd : 0;                 // extra columns: u.w, r.v_j, y_k.w
+    // row cache: the dots and updates of every iteration read the CTA's rows
+    // of V and of w from shared memory instead of L2 (a round of dependent
+    // loads less per phase); global V and w stay complete (other CTAs read
+    // w, the host-side steps read V).  The basis vectors of earlier launches
+    // are copied in asynchronously, behind the first H*psi items.
+    const bool yc = a.vc > 0;
+    const int vc = a.vc, cs = a.cs;
+    float *vcache = (float *)(chunk_raw + chunk_cache_off(ps));
+    float *ycache = vcache + (size_t)vc * cs;
+    if (yc) {
+        const int rows = (int)(i1 - i0);
+        const int npre = min(vc, a.first_from_v ? a.j0 + 1 : a.j0);
+        for (int e = tid; e < npre * rows; e += ORTH_THREADS) {
+            const int l = e / rows, r = e - l * rows;
+            cp_async4(vcache + l * cs + r, V + (int64_t)l * n + i0 + r);
+        }
+        cp_async_commit();
+    }
     float beta_prev = a.j0 > 0 ? (float)a.o.beta[a.j0 - 1] : 0.f;
     int done = 0, brk_m = 0;
     // CTA 0 publishes the completed iterations (device arrays, host mirrors)
@@ -773,6 +920,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         float ap = 0.f;
         for (int ti = 2 * blk + grp; ti < a.nitems; ti += 2 * G)
             ap += hv32_item(a.items[ti], x, a.slot, a.op, ism[grp], lt, GroupSync{1 + grp}, sc);
+        if (yc && jj == a.j0) cp_async_wait_all();   // the row cache (published by the barriers below)
         {
             float a1[1] = {ap};
             block_sums<float, 1>(a1, scr);
@@ -799,12 +947,18 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             float *vj = V + (int64_t)jj * n;
             const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
             const float *s0 = a.slot[0], *s1 = a.slot[1], *s2 = a.slot[2];
+            // own rows of x: the cached w of the previous iteration of this launch
+            const bool xc = yc && jj > a.j0;
+            const bool jc = jj < vc, jmc = jj > 0 && jj - 1 < vc;
             for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
-                const float v = x[i] * sc;
+                const int r = (int)(i - i0);
+                const float v = (xc ? ycache[r] : x[i]) * sc;
                 if (!first) vj[i] = v;
+                if (jc) vcache[jj * cs + r] = v;
                 float w = (s0[i] + s1[i] + s2[i]) - alpha0 * v;
-                if (jj > 0) w -= beta_prev * vjm[i];
+                if (jj > 0) w -= beta_prev * (jmc ? vcache[(jj - 1) * cs + r] : vjm[i]);
                 y[i] = w;
+                if (yc) ycache[r] = w;
                 if (anc) {
                     ex[0] += au[i] * w;
                     ex[1] += ar[i] * v;
@@ -815,7 +969,8 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             }
         }
         __syncthreads();
-        cta_dots<float, CW>(V, m, y, n, i0, i1, true, red, pH + blk, G);
+        if (yc) cta_dots_vc<CW>(vcache, vc, cs, V, m, ycache, n, i0, i1, true, red, pH + blk, G);
+        else cta_dots<float, CW>(V, m, y, n, i0, i1, true, red, pH + blk, G);
         if (anc) {
             block_sums<float, CHUNK_EXTRA>(ex, scr);
             if (tid == 0) {
@@ -835,15 +990,20 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         // w -= V h (+ the anchor and deflation components)
         auto update = [&](int xoff) -> float {
             float ss = 0.f;
+            const int mc = min(m, vc);
             for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
-                float w = y[i];
+                const int r = (int)(i - i0);
+                float w = yc ? ycache[r] : y[i];
+#pragma unroll 8
+                for (int l = 0; l < mc; ++l) w -= vcache[l * cs + r] * hs[l];
 #pragma unroll 32
-                for (int l = 0; l < m; ++l) w -= V[(int64_t)l * n + i] * hs[l];
+                for (int l = mc; l < m; ++l) w -= V[(int64_t)l * n + i] * hs[l];
                 if (anc) {
                     w -= hs[xoff] * au[i];
                     for (int k = 0; k < nd; ++k) w -= hs[xoff + 2 + k] * ay[(int64_t)k * n + i];
                 }
                 y[i] = w;
+                if (yc) ycache[r] = w;
                 ss += w * w;
             }
             return ss;
@@ -861,12 +1021,13 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             bb = t1[0];
         }
         if (bb < 0.5f * ww) {   // second projection (same decision in every CTA)
-            cta_dots<float, CW>(V, m, y, n, i0, i1, false, red, pH2 + blk, G);
+            if (yc) cta_dots_vc<CW>(vcache, vc, cs, V, m, ycache, n, i0, i1, false, red, pH2 + blk, G);
+            else cta_dots<float, CW>(V, m, y, n, i0, i1, false, red, pH2 + blk, G);
             if (anc) {
 #pragma unroll
                 for (int q = 0; q < CHUNK_EXTRA; ++q) ex[q] = 0.f;
                 for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
-                    const float w = y[i];
+                    const float w = yc ? ycache[i - i0] : y[i];
                     ex[0] += au[i] * w;
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
@@ -1035,7 +1196,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
             {   // alpha from the item partials, fixed order
                 float t = 0.f;
                 if (tid < 32) {
-                    for (int q = tid; q < Mp->c.nitems; q += 32) t += __ldcg(Mp->pitem + q);
+                    t = strided_sum<float>(Mp->pitem, tid, Mp->c.nitems, 32);
                     t = warp_sum<float>(t);
                     if (tid == 0) bc[0] = t;
                 }
@@ -1113,7 +1274,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
             if (!alive[s] || S.c.j0 + step >= S.c.jend) continue;
             const float *pBs = (const float *)S.c.o.part + (PA_COLS + (int64_t)S.c.o.pstride) * S.ncta;
             float t = 0.f;
-            for (int b = 0; b < S.ncta; ++b) t += __ldcg(pBs + b);
+            t = strided_sum<float>(pBs, 0, S.ncta, 1);
             bbb[s] = t;
             balpha[s] = __ldcg(B.st + 4 * s + 0);
             if (t < 0.5f * __ldcg(B.st + 4 * s + 1)) {
@@ -1161,7 +1322,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
                 const BatchSolve &S = B.s[s];
                 const float *pB2s = (const float *)S.c.o.part + (PA_COLS + 2 * (int64_t)S.c.o.pstride + 1) * S.ncta;
                 float t = 0.f;
-                for (int b = 0; b < S.ncta; ++b) t += __ldcg(pB2s + b);
+                t = strided_sum<float>(pB2s, 0, S.ncta, 1);
                 bbb[s] = t;
                 balpha[s] += __ldcg(B.st + 4 * s + 2);
             }
@@ -1472,7 +1633,7 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     const size_t smem = orth_smem(pstride, cw, mixed ? sizeof(float) : sizeof(double));
     const void *fn = mixed ? (const void *)k_orth<float, OrthCW<float>::value>
                            : (const void *)k_orth<double, OrthCW<double>::value>;
-    if (smem > 48 * 1024) NSS_CUDA_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NSS_CUDA_TRY(c, allow_smem(fn, smem));
     int occ = 0;
     NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, ORTH_THREADS, smem));
     if (occ < 1) {
@@ -1485,14 +1646,31 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
     if (mixed) {
         // the persistent chunk kernel of the mixed method
         const size_t csm = chunk_smem(pstride);
-        NSS_CUDA_TRY(c, cudaFuncSetAttribute((const void *)k_chunk32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)csm));
+        // the row cache takes what one CTA per SM leaves: the CTA's rows of
+        // the work vector and of as many basis vectors as fit
+        const int64_t rows = (n + nsm - 1) / nsm;
+        const int cs = (int)((rows + 3) & ~(int64_t)3);
+        const size_t coff = chunk_cache_off(pstride), vbytes = (size_t)cs * sizeof(float);
+        int vc = 0;
+        if (chunk_cache_enabled() && coff + 2 * vbytes <= CHUNK_SMEM_MAX)
+            vc = (int)std::min<int64_t>(cap + 1, (int64_t)((CHUNK_SMEM_MAX - coff - vbytes) / vbytes));
+        const size_t csm_vc = vc > 0 ? coff + (size_t)(vc + 1) * vbytes : csm;
+        NSS_CUDA_TRY(c, allow_smem((const void *)k_chunk32, std::max(csm, csm_vc)));
         int occ2 = 0;
-        NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS, csm));
+        NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS,
+                                                                      csm_vc));
+        if (occ2 < 1 && vc > 0) {   // no room for the cache after all: run without it
+            vc = 0;
+            NSS_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)k_chunk32, ORTH_THREADS,
+                                                                          csm));
+        }
         if (occ2 >= 1) {
             NSS_CUDA_TRY(c, ctx_alloc(c, &z.wbuf32, (size_t)2 * n));
             NSS_CUDA_TRY(c, ctx_alloc(c, &z.slot32, (size_t)3 * n));
             z.chunk_smem = csm;
+            z.chunk_vc = vc;
+            z.chunk_cs = vc > 0 ? cs : 0;
+            z.chunk_smem_vc = vc > 0 ? csm_vc : csm;
             z.chunk_ok = true;
         }
     }
@@ -1600,10 +1778,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     }
     const size_t dots_smem = (size_t)(cap + 2) * sizeof(double) + SUB * sizeof(T);
     const size_t upd_smem = (size_t)(cap + 2) * sizeof(double);
-    if (dots_smem > 48 * 1024)
-        cudaFuncSetAttribute(k_dots<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
-    if (upd_smem > 48 * 1024)
-        cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+    allow_smem((const void *)k_dots<T>, dots_smem);
+    allow_smem((const void *)k_update<T>, upd_smem);
     constexpr int CW = OrthCW<T>::value;
     OrthArgs oa;
     oa.V = V;
@@ -1659,6 +1835,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             ca.items = c.sb.d_items32;
             ca.nitems = c.sb.nitems32;
             ca.op = hv32_ops(c.sb);
+            ca.vc = z.chunk_vc;
+            ca.cs = z.chunk_cs;
             from_v = false;
             void *args[] = {&ca};
             ChunkTiming ct{nullptr, nullptr, j0, jend};
@@ -1668,7 +1846,7 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
                 cudaEventRecord(ct.a, st);
             }
             cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_chunk32, dim3(z.orth_grid),
-                                                        dim3(ORTH_THREADS), args, z.chunk_smem, st);
+                                                        dim3(ORTH_THREADS), args, z.chunk_smem_vc, st);
             if (c.time_chunks) {
                 cudaEventRecord(ct.b, st);
                 ctime.push_back(ct);
@@ -1942,10 +2120,8 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
         const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(double);
         const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
-        if (dots_smem > 48 * 1024)
-            cudaFuncSetAttribute(k_dots<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
-        if (upd_smem > 48 * 1024)
-            cudaFuncSetAttribute(k_update<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+        allow_smem((const void *)k_dots<double>, dots_smem);
+        allow_smem((const void *)k_update<double>, upd_smem);
         // w -= Y (Y^T w) against the e vectors before it; returns via scal[S_BB]
         auto deflate = [&](double *vec, int e) -> int {
             NSS_CUDA_TRY(c, cudaMemsetAsync(z.flags, 0, F_NFLAGS * sizeof(int), st));
@@ -2180,7 +2356,7 @@ struct BatchEngine {
     int cap_items = 0;
     float *d_st = nullptr;
     double *h_res = nullptr;     // [BATCH_MAX][8] pinned refinement results
-    size_t smem_set = 0;
+    size_t smem_set = 0;         // dynamic shared memory of its launches (the most any round needed)
     ~BatchEngine() {
         if (!c0) return;
         cudaStreamSynchronize(c0->stream);
@@ -2362,11 +2538,8 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
         NSS_CUDA_TRY(c0, cudaMemcpyAsync(E.d_solves, E.h_solves, sizeof(BatchSolve) * na, cudaMemcpyHostToDevice, st));
         NSS_CUDA_TRY(c0, cudaMemcpyAsync(E.d_gitems, E.h_gitems, sizeof(int2) * std::max(ng, 1), cudaMemcpyHostToDevice,
                                          st));
-        if (smem_max > E.smem_set) {
-            NSS_CUDA_TRY(c0, cudaFuncSetAttribute((const void *)k_batch32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)smem_max));
-            E.smem_set = smem_max;
-        }
+        NSS_CUDA_TRY(c0, allow_smem((const void *)k_batch32, smem_max));
+        E.smem_set = std::max(E.smem_set, smem_max);
         BatchArgs ba;
         ba.s = E.d_solves;
         ba.ns = na;
@@ -2431,10 +2604,8 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
                 float *vn = z.V32 + (int64_t)m * B.n;
                 const size_t dots_smem = (size_t)(z.cap + 2) * sizeof(double) + SUB * sizeof(float);
                 const size_t upd_smem = (size_t)(z.cap + 2) * sizeof(double);
-                if (dots_smem > 48 * 1024)
-                    cudaFuncSetAttribute(k_dots<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_smem);
-                if (upd_smem > 48 * 1024)
-                    cudaFuncSetAttribute(k_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem);
+                allow_smem((const void *)k_dots<float>, dots_smem);
+                allow_smem((const void *)k_update<float>, upd_smem);
                 double *h1 = z.scal + S_NSCAL;
                 double *rs_alpha = h1 + 2 * (z.cap + 2), *rs_beta = rs_alpha + (z.cap + 2);
                 c0.launches += 6;

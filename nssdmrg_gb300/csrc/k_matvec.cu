@@ -407,7 +407,9 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
     int tc_thr = c.tc_min_dl, tc_bn = c.mma_bn;
     c.tune_cand = -1;
     if (c.tc_auto) tune_choose(c, s, &tc_thr, &tc_bn);
-    mma_layout(s, tc_thr, tc_bn, c.mma_split, plan);
+    int nsm = 0;
+    NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    mma_layout(s, tc_thr, tc_bn, c.mma_split, nsm, plan);
     std::vector<char> on_tc(s.nsb, 0);
     for (int k : plan.sectors) on_tc[k] = 1;
     std::vector<int4> tiles32;
@@ -521,9 +523,10 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
     sg.add(&s.d_ell, ell);
     sg.add(&s.d_term_hdr, term_hdr);
     sg.add(&s.d_tc_err, tc_err);
-    sg.add_dev(&s.d_mma_pool, (size_t)(plan.items.empty() ? 0 : 2 * plan.plane_rows * MM_KC));
-    sg.add_dev(&s.d_mma_out, (size_t)(plan.items.empty() ? 0 : 2 * s.n));
+    sg.add_dev(&s.d_mma_pool, (size_t)(plan.items.empty() ? 0 : plan.plane_rows * MM_KC));
+    sg.add_dev(&s.d_mma_out, (size_t)(plan.items.empty() ? 0 : plan.nplanes * s.n));
     sg.add(&s.d_mma_items, plan.items);
+    sg.add(&s.d_mma_rng, plan.rng);
     sg.add(&s.d_mma_wt, plan.wt);
     sg.add(&s.d_mma_sec, plan.ps);
     sg.add(&s.d_dls, s.dls);
@@ -677,8 +680,9 @@ Hv32Ops hv32_ops(const DevSb &s) {
     op.item_ell = s.d_item_ell;
     op.ell = s.d_ell;
     op.term_hdr = s.d_term_hdr;
-    op.tc0 = s.mma_nitems ? s.d_mma_out : nullptr;
-    op.tc1 = s.mma_nitems ? s.d_mma_out + s.n : nullptr;
+    op.tc = s.mma_nitems ? s.d_mma_out : nullptr;
+    op.tcn = s.mma_nitems ? s.mma_nplanes : 0;
+    op.tcs = s.n;
     return op;
 }
 

@@ -608,7 +608,7 @@ void rdm_release(Ctx &c) {
 }
 
 int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg_thr, nss_rdm_side out[2], double *lam_l,
-            double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r, KeptLayout *kl) {
+            double *lam_r, int32_t *kept_l, int32_t *kept_r, double *u_l, double *u_r, KeptLayout *kl, int vec_sides) {
     DevSb &s = c.sb;
     if (!s.valid) { c.err = "nss_rdm: no superblock uploaded"; return NSS_ERR_STATE; }
     if (s.ai.empty() || s.bi.empty()) { c.err = "nss_rdm: descriptor had no ai/bi state maps"; return NSS_ERR_INVALID; }
@@ -1047,7 +1047,8 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     // kept eigenvectors of the own path's blocks; marked blocks again
     // through the library
     if (!path.empty() && (u_l || u_r || kl)) {
-        const int msv[2] = {(u_l || kl) ? hi[0] : 0, (u_r || kl) ? hi[1] : 0};
+        const int msv[2] = {((vec_sides & 1) && (u_l || kl)) ? hi[0] : 0,
+                            ((vec_sides & 2) && (u_r || kl)) ? hi[1] : 0};
         c.launches += 3;
         const int e = syev_vec(r.order, rnk, msv, nl, nsb, d_ev_off, d_dims, d_rho_off, d_bmode, sub, r.evals, ldd,
                                ldl, bscale, bsig, tau, refl, perm, flags, r.vec, maxn_path, st);
@@ -1214,7 +1215,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     for (int side = 0; side < 2; ++side) {
         const int base = side == 0 ? 0 : nl;
         const int ms = hi[side];
-        if (!(u_out[side] || kept_out[side] || kl)) continue;
+        if (!(u_out[side] || kept_out[side] || kl) || !(vec_sides & (1 << side))) continue;
         any = true;
         int *dk = d_kept + side * 2 * kmax, *doff = dk + kmax;
         double *du = r.u + (int64_t)side * kmax * maxd;
@@ -1232,6 +1233,10 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     if (kl)
         for (int side = 0; side < 2; ++side) {
             KeptLayout &L = kl[side];
+            if (!(vec_sides & (1 << side))) {   // no kept vectors computed for this side
+                L = KeptLayout{};
+                continue;
+            }
             const int ms = hi[side], o = side * nsb;
             L.ms = ms;
             L.q.assign(hkept[side], hkept[side] + ms);
@@ -1247,6 +1252,7 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
         }
     for (int side = 0; side < 2; ++side) {
         const int ms = hi[side];
+        if (!(vec_sides & (1 << side))) continue;
         if (kept_out[side])
             for (int j = 0; j < ms; ++j) kept_out[side][j] = hkept[side][j];
         if (!u_out[side]) continue;

@@ -172,6 +172,7 @@ struct Side {
 // kept columns per block, state maps and the nonzero block pairs of every
 // operator (both blocks with kept columns)
 void scan_side(Side &s) {
+    if (!s.blk) return;   // a side not renormalised: no columns, no pairs
     const KeptLayout &kl = *s.kl;
     const Block &blk = *s.blk;
     s.ms = kl.ms;
@@ -221,6 +222,7 @@ void scan_side(Side &s) {
 // column-major n_qr x n_qc block of their pair, offset by ob, value) into
 // ent, the side's share of the staging buffer; the device scatters them
 void extract_side(const Side &s, RnEntry *ent, int64_t ob) {
+    if (!s.blk) return;
     const KeptLayout &kl = *s.kl;
     const Block &blk = *s.blk;
     const int nb = s.nb, mblock = blk.dim;
@@ -246,6 +248,7 @@ void extract_side(const Side &s, RnEntry *ent, int64_t ob) {
 // O' in CSR, rows and columns in kept order, exact zeros dropped; hres is
 // the side's share of the result staging buffer
 void assemble_side(Side &s, const double *hres) {
+    if (!s.blk) return;
     const KeptLayout &kl = *s.kl;
     Block &blk = *s.blk;
     const int nb = s.nb, ms = s.ms;

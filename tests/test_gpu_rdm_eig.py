@@ -181,7 +181,7 @@ def test_qn_entropy_split_matches_oracle(nss, name):
 
 
 @pytest.mark.parametrize("cluster_mem", ["shared", "global", "grid"])
-def test_big_blocks_through_blocked_reduction(nss, cluster_mem):
+def test_big_blocks_through_blocked_reduction(nss, cluster_mem, monkeypatch):
     """Rho blocks above 160 states are reduced by a thread-block cluster,
     with the block in the cluster's shared memory or (env
     NSS_TRD_CL_SHARED_MAX=0, as for blocks too large for it) in a global
@@ -189,14 +189,13 @@ def test_big_blocks_through_blocked_reduction(nss, cluster_mem):
     the whole GPU, then the same bisection and twisted vectors: against the
     library eigensolver on the spin-1 chain's last infinite step (L=32,
     m=256, blocks up to ~190)."""
-    import os
-    os.environ.pop("NSS_TRD_GRID_MIN", None)
+    monkeypatch.delenv("NSS_TRD_GRID_MIN", raising=False)
     if cluster_mem in ("global", "grid"):
-        os.environ["NSS_TRD_CL_SHARED_MAX"] = "0"
+        monkeypatch.setenv("NSS_TRD_CL_SHARED_MAX", "0")
     else:
-        os.environ.pop("NSS_TRD_CL_SHARED_MAX", None)
+        monkeypatch.delenv("NSS_TRD_CL_SHARED_MAX", raising=False)
     if cluster_mem == "grid":
-        os.environ["NSS_TRD_GRID_MIN"] = "1"
+        monkeypatch.setenv("NSS_TRD_GRID_MIN", "1")
     d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 16, 256, dmrg_qn=(0.0,), lanc_neigen=1, lanc_tolerance=1e-12)
     d.prepare_last()
     s = d.sb
@@ -209,8 +208,8 @@ def test_big_blocks_through_blocked_reduction(nss, cluster_mem):
     # decides the degeneracy extension)
     own, st_own = _rdm(s, 64, psi, library=False)
     lib, _ = _rdm(s, 64, psi, library=True)
-    os.environ.pop("NSS_TRD_CL_SHARED_MAX", None)
-    os.environ.pop("NSS_TRD_GRID_MIN", None)
+    monkeypatch.delenv("NSS_TRD_CL_SHARED_MAX", raising=False)
+    monkeypatch.delenv("NSS_TRD_GRID_MIN", raising=False)
     assert st_own[0] > 0 and st_own[1] == 0, st_own
     dls = np.array([desc.dls[k] for k in range(desc.nsb)])
     drs = np.array([desc.drs[k] for k in range(desc.nsb)])
