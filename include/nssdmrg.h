@@ -251,6 +251,13 @@ int nss_rdm_fallback_reasons(const nss_ctx *ctx, int64_t out[5]);
 int nss_time_chunks(nss_ctx *ctx, int enable);
 int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iters, double *cols);
 
+/* The persistent kernel's shared-memory row cache in the context's Lanczos
+ * workspace (set up by the last mixed nss_eigh): how many basis vectors each
+ * CTA keeps of its rows, and the rows per CTA (0, 0: no cache; a basis that
+ * is too large for it, or NSS_CHUNK_CACHE=0).  No counterpart in the
+ * reference. */
+int nss_chunk_cache(const nss_ctx *ctx, int *vectors, int64_t *rows);
+
 /* The mixed path's plan for the uploaded superblock, as the tile tuner chose
  * it: candidate 0 puts every sector on CUDA cores (the persistent Lanczos
  * kernel), 1 and 2 the sectors with Dl >= 32 on the tensor-core GEMM with

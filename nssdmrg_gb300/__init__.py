@@ -151,6 +151,7 @@ def lib():
         "nss_eigh_batch": (C.c_int, [P, C.c_int, C.c_int, D, P, P, P]),
         "nss_time_chunks": (C.c_int, [P, C.c_int]),
         "nss_chunk_stats": (C.c_int, [P, C.POINTER(D), C.POINTER(C.c_int), C.POINTER(I64), C.POINTER(D)]),
+        "nss_chunk_cache": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(I64)]),
         "nss_batch_create": (P, [P]),
         "nss_batch_add": (C.c_int, [P, P, C.c_uint64, C.c_int, D, C.POINTER(C.c_int)]),
         "nss_batch_step": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P, P, P]),
@@ -457,6 +458,13 @@ class Superblock:
         ms, nl, it, cols = C.c_double(), C.c_int(), C.c_int64(), C.c_double()
         self._check(lib().nss_chunk_stats(self._ctx, C.byref(ms), C.byref(nl), C.byref(it), C.byref(cols)))
         return ms.value, nl.value, it.value, cols.value
+
+    def chunk_cache(self):
+        """(basis vectors cached per CTA, rows per CTA) of the persistent
+        kernel's shared-memory row cache in this context's workspace."""
+        vc, rows = C.c_int(), C.c_int64()
+        self._check(lib().nss_chunk_cache(self._ctx, C.byref(vc), C.byref(rows)))
+        return vc.value, rows.value
 
     def odotv(self, label, ops, v):
         """OdotV_direct: (O x 1) v for label 'l', (1 x O) v for 'r'; ops[k]

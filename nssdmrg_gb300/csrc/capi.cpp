@@ -325,6 +325,13 @@ int nss_time_chunks(nss_ctx *ctx, int enable) {
     return NSS_OK;
 }
 
+int nss_chunk_cache(const nss_ctx *ctx, int *vectors, int64_t *rows) {
+    if (!ctx) return NSS_ERR_INVALID;
+    if (vectors) *vectors = ctx->c.lz.chunk_vc;
+    if (rows) *rows = ctx->c.lz.chunk_cs;
+    return NSS_OK;
+}
+
 int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iters, double *cols) {
     if (!ctx) return NSS_ERR_INVALID;
     if (ms) *ms = ctx->c.chunk_ms;

@@ -779,33 +779,41 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // cta_dots on the row cache: the CTA's rows of V[l] (l < vc) at vs[l*cs + r]
-// and of w at ws[r] (r = row - i0); columns l >= vc come from V in global
-// memory.  Same items, rows and accumulation order as cta_dots.
+// and of w at ws[r] (r = row - i0).  Cached columns: one warp per column,
+// the lanes down the rows, one warp sum (shared-memory operands need no
+// loads in flight; the multi-column form below measured 3-5 us here against
+// 1.5 us).  Columns l >= vc stream from global memory in the multi-column
+// form of cta_dots (CW columns per lane, to keep enough loads in flight).
 template <int CW>
 __device__ __forceinline__ void cta_dots_vc(const float *__restrict__ vs, int vc, int cs, const float *__restrict__ V,
                                             int m, const float *__restrict__ ws, int64_t n, int64_t i0, int64_t i1,
                                             bool ww, float *red, float *out, int G) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ncol = m + (ww ? 1 : 0);
+    const int len = (int)(i1 - i0);
+    const int mc = min(m, vc);
+    const int n1 = mc + ((ww && m <= vc) ? 1 : 0);   // the w.w column here when nothing is left beyond the cache
+    for (int l = warp; l < n1; l += ORTH_WARPS) {
+        const float *src = l < mc ? vs + (int64_t)l * cs : ws;
+        float acc = 0.f;
+#pragma unroll 8
+        for (int r = lane; r < len; r += 32) acc += src[r] * ws[r];
+        acc = warp_sum<float>(acc);
+        if (lane == 0) out[(int64_t)l * G] = acc;
+    }
+    if (m <= vc) return;
+    const int ncol = m - vc + (ww ? 1 : 0);
     const int ng = (ncol + CW - 1) / CW;
     const int nq = ng >= ORTH_WARPS ? 1 : ORTH_WARPS / ng;
     const int rs = ng * CW;
-    const int len = (int)(i1 - i0), qlen = (len + nq - 1) / nq;
+    const int qlen = (len + nq - 1) / nq;
     const float *Vg = V + i0;
     for (int item = warp; item < ng * nq; item += ORTH_WARPS) {
-        const int g = item % ng, q = item / ng, l0 = g * CW;
+        const int g = item % ng, q = item / ng, l0 = vc + g * CW;
         const int r0 = q * qlen, r1 = min(len, r0 + qlen);
         float acc[CW];
 #pragma unroll
         for (int c = 0; c < CW; ++c) acc[c] = 0.f;
-        if (l0 + CW <= m && l0 + CW <= vc) {
-            const float *vr = vs + l0 * cs;
-            for (int r = r0 + lane; r < r1; r += 32) {
-                const float wv = ws[r];
-#pragma unroll
-                for (int c = 0; c < CW; ++c) acc[c] += vr[c * cs + r] * wv;
-            }
-        } else if (l0 + CW <= m && l0 >= vc) {
+        if (l0 + CW <= m) {
             const float *vr = Vg + (int64_t)l0 * n;
             for (int r = r0 + lane; r < r1; r += 32) {
                 const float wv = ws[r];
@@ -818,19 +826,19 @@ __device__ __forceinline__ void cta_dots_vc(const float *__restrict__ vs, int vc
 #pragma unroll
                 for (int c = 0; c < CW; ++c) {
                     const int l = l0 + c;
-                    if (l < m) acc[c] += (l < vc ? vs[l * cs + r] : Vg[(int64_t)l * n + r]) * wv;
+                    if (l < m) acc[c] += Vg[(int64_t)l * n + r] * wv;
                     else if (ww && l == m) acc[c] += wv * wv;
                 }
             }
         }
         const float s = multi_reduce<float, CW>(acc, lane);
-        if (lane < CW && l0 + lane < ncol) red[q * rs + l0 + lane] = s;
+        if (lane < CW && l0 - vc + lane < ncol) red[q * rs + l0 - vc + lane] = s;
     }
     __syncthreads();
     for (int l = threadIdx.x; l < ncol; l += ORTH_THREADS) {
         float s = 0.f;
         for (int q = 0; q < nq; ++q) s += red[q * rs + l];
-        out[(int64_t)l * G] = s;
+        out[(int64_t)(vc + l) * G] = s;
     }
 }
 
@@ -933,6 +941,12 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
             publish();
             return;
         }
+        const float *s0 = a.slot[0], *s1 = a.slot[1], *s2 = a.slot[2];
+        // the three-term step's H v_j of the thread's first row, loaded before
+        // the alpha total so that the two L2 round trips overlap
+        const int64_t if0 = i0 + tid;
+        float hv0 = 0.f;
+        if (if0 < i1) hv0 = s0[if0] + s1[if0] + s2[if0];
         float alpha0;
         {
             float t1[1];
@@ -946,16 +960,15 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_chunk32(ChunkArgs a) {
         {
             float *vj = V + (int64_t)jj * n;
             const float *vjm = V + (int64_t)(jj > 0 ? jj - 1 : 0) * n;
-            const float *s0 = a.slot[0], *s1 = a.slot[1], *s2 = a.slot[2];
             // own rows of x: the cached w of the previous iteration of this launch
             const bool xc = yc && jj > a.j0;
             const bool jc = jj < vc, jmc = jj > 0 && jj - 1 < vc;
-            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+            for (int64_t i = if0; i < i1; i += ORTH_THREADS) {
                 const int r = (int)(i - i0);
                 const float v = (xc ? ycache[r] : x[i]) * sc;
                 if (!first) vj[i] = v;
                 if (jc) vcache[jj * cs + r] = v;
-                float w = (s0[i] + s1[i] + s2[i]) - alpha0 * v;
+                float w = (i == if0 ? hv0 : (s0[i] + s1[i] + s2[i])) - alpha0 * v;
                 if (jj > 0) w -= beta_prev * (jmc ? vcache[(jj - 1) * cs + r] : vjm[i]);
                 y[i] = w;
                 if (yc) ycache[r] = w;

@@ -203,7 +203,7 @@ struct MmaCfg {
     static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;    // A hi, A lo, B hi, B lo (B hi, lo adjacent)
     static constexpr int TX = A_BYTES + B_BYTES;               // bytes the TMA lands per stage (FP32 A, B)
     static constexpr int HALF = BN / 2;                        // columns of one epilogue warp
-    static constexpr int OUT_LD = HALF + 1;                    // staging row stride (conflict-free)
+    static constexpr int OUT_LD = 33;                          // staging: 32 rows x 32 columns per pass
     static constexpr int OUT_BYTES = MM_NEPI * 32 * OUT_LD * 4;
     // as many operand stages as fit beside the epilogue's staging
     static constexpr int STAGES = (MM_SMEM_LIMIT - OUT_BYTES - 1024) / STAGE;
@@ -424,23 +424,24 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
                 if (lane == 0) mbar_arrive(smem_u32(&tempty[acc]));
             }
             if (!ok) break;
-            // the warp's 32 rows x BN/2 columns through shared memory, then row
-            // by row with the lanes along the columns: whole 128-byte segments
-            // per store (a lane writing its own row touched 32 sectors per store)
-#pragma unroll
-            for (int j = 0; j < C::HALF; ++j) stg[lane * C::OUT_LD + j] = sum[j];
-            __syncwarp();
+            // the warp's 32 rows through shared memory, 32 columns at a time,
+            // then row by row with the lanes along the columns: whole 128-byte
+            // segments per store (a lane writing its own row touched 32
+            // sectors per store)
             float *base = out + (int64_t)m.out * plane + m.off;
-            const int col0 = m.n0 + h * C::HALF;
-            for (int r = 0; r < 32; ++r) {
-                const int il = m.m0 + 32 * q + r;
-                if (il >= m.dl) break;
-                float *dst = base + (int64_t)il * m.dr + col0;
 #pragma unroll
-                for (int cc = lane; cc < C::HALF; cc += 32)
-                    if (col0 + cc < m.dr) dst[cc] = stg[r * C::OUT_LD + cc];
+            for (int c0 = 0; c0 < C::HALF; c0 += 32) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) stg[lane * C::OUT_LD + j] = sum[c0 + j];
+                __syncwarp();
+                const int col = m.n0 + h * C::HALF + c0 + lane;
+                for (int r = 0; r < 32; ++r) {
+                    const int il = m.m0 + 32 * q + r;
+                    if (il >= m.dl) break;
+                    if (col < m.dr) base[(int64_t)il * m.dr + col] = stg[r * C::OUT_LD + lane];
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

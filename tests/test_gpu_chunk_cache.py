@@ -2,13 +2,14 @@
 
 Each CTA keeps its rows of the work vector and of the first basis vectors
 in shared memory; columns beyond the cache come from global memory.  The
-cached path makes the same floating-point operations in the same order as
-the uncached one (NSS_CHUNK_CACHE=0), so a mixed solve gives bit-identical
-eigenvalues, vectors and product counts with and without it.  Two
-superblocks: the Hubbard L=32 m=256 benchmark superblock (434 rows per
-CTA: most of the basis cached, the last column group straddles the cache
-end) and the spin-1 L=64 m=512 one (2.6k rows per CTA: about a dozen
-vectors cached, the rest from global memory).
+cached dots run one warp per column (another summation order than the
+multi-column form of the uncached path), so a mixed solve with the cache
+(default) and without it (NSS_CHUNK_CACHE=0) agree to rounding: the same
+energy to 1e-12 relative, both within 1e-10 of the FP64 solve, product
+counts within 10 %.  Two superblocks: the Hubbard L=32 m=256 benchmark
+superblock (434 rows per CTA: the whole basis of a solve fits the cache)
+and the spin-1 L=64 m=512 one (2.6k rows per CTA: about a dozen vectors
+cached, the rest from global memory).
 """
 import numpy as np
 import pytest
@@ -33,7 +34,7 @@ def _desc(nss, case):
 
 
 @pytest.mark.parametrize("case", ["hubbard_L32_M256", "spin1_L64_M512"])
-def test_row_cache_is_bit_identical(nss, monkeypatch, case):
+def test_row_cache_matches_uncached(nss, monkeypatch, case):
     run = _desc(nss, case)
     desc = run.export_superblock()
     monkeypatch.setenv("NSS_TC_MIN_DL", "0")   # all sectors on CUDA cores: the persistent kernel runs
@@ -42,15 +43,21 @@ def test_row_cache_is_bit_identical(nss, monkeypatch, case):
         monkeypatch.setenv("NSS_CHUNK_CACHE", cache)
         s = nss.Superblock()
         s.upload_desc(desc)
-        ev, vec, numop = s.sb_diag(neigen=1, tol=1e-12, precision=nss.NSS_PREC_MIXED)
-        out[cache] = (ev.copy(), vec.copy(), numop)
+        ev, _, numop = s.sb_diag(neigen=1, tol=1e-12, precision=nss.NSS_PREC_MIXED, want_vectors=False)
+        out[cache] = (ev.copy(), numop, s.chunk_cache())
+        if cache == "1":
+            e64, _, _ = s.sb_diag(neigen=1, tol=1e-12, want_vectors=False)
         s.close()
     run.close()
-    (e0, v0, n0), (e1, v1, n1) = out["0"], out["1"]
-    print(f"{case}: E {e1[0]!r}, {n1} products")
-    assert n0 == n1
-    np.testing.assert_array_equal(e0, e1)
-    np.testing.assert_array_equal(v0, v1)
+    (e0, n0, c0), (e1, n1, c1) = out["0"], out["1"]
+    print(f"{case}: E {e1[0]!r} / {e0[0]!r}, products {n1} / {n0}, cache {c1} / {c0}")
+    assert c0 == (0, 0) and c1[0] > 0          # the cached run did use the cache
+    assert abs(e1[0] - e0[0]) <= 1e-12 * abs(e0[0])
+    for e in (e0, e1):
+        assert abs(e[0] - e64[0]) <= 1e-10 * abs(e64[0])
+    # the spin-1 superblock's end-spin pair makes the refinement's path (and
+    # its product count) follow rounding: measured 230 against 217
+    assert abs(n1 - n0) <= 0.1 * max(n0, n1)
 
 
 def test_contexts_of_different_sizes_interleave(nss, monkeypatch):
