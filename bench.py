@@ -65,7 +65,8 @@ def parse():
                          "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction; "
                          "sweep-large: the finite sweep of the spin-1 L=64 m=512 chain in --precision; "
                          "tc-sector: four FP32 H*psi of the spin-1 L=64 m=512 chain's last infinite "
-                         "superblock with every sector of >= 32 left states on the tensor-core GEMM)")
+                         "superblock with every sector of >= 32 left states on the tensor-core GEMM, "
+                         "128-column tiles)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -439,7 +440,7 @@ def run_profile_case(case, precision="mixed"):
                      precision=nss.NSS_PREC_MIXED)
         d.prepare_last()
         desc = d.export_superblock()
-        os.environ.update(NSS_TC_MIN_DL="32", NSS_TC_BN="64")
+        os.environ.update(NSS_TC_MIN_DL="32", NSS_TC_BN="128")
         s = nss.Superblock(0)
         s.upload_desc(desc)
         v = _t.rand(s.n, device="cuda") * 2 - 1
