@@ -436,6 +436,9 @@ def run_profile_case(case, precision="mixed"):
         return
     if case == "tc-sector":
         import torch as _t
+        # the chain is grown with the tuner off (CUDA-core products only), so
+        # that the only sector-GEMM launches are the four products below
+        os.environ.update(NSS_TC_AUTO="0", NSS_TC_MIN_DL="0")
         d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, dmrg_qn=(0.0, 0.0), lanc_neigen=1,
                      precision=nss.NSS_PREC_MIXED)
         d.prepare_last()

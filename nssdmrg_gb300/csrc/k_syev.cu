@@ -318,6 +318,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 const double *a = colp(jj) + k + 1;
                 double a0 = 0.0, a1 = 0.0;
                 int i = lane;
+                if (GLOBAL)   // columns in L2: eight rounds' loads out before the first FMA
+                    for (; i + 32 + 448 < m; i += 512) {
+                        double x[16];
+#pragma unroll
+                        for (int u = 0; u < 16; ++u) x[u] = a[i + 32 * u];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            a0 = fma(x[2 * u], v[i + 64 * u], a0);
+                            a1 = fma(x[2 * u + 1], v[i + 64 * u + 32], a1);
+                        }
+                    }
                 for (; i + 32 < m; i += 64) {
                     a0 = fma(a[i], v[i], a0);
                     a1 = fma(a[i + 32], v[i + 32], a1);
@@ -354,7 +365,23 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 const double vj = v[jc], wj = w[jc];
                 double *a = colp(jj) + k + 1;
                 const double nvj = -vj, nwj = -wj;
-                for (int i = lane; i < m; i += 32) a[i] = fma(v[i], nwj, fma(w[i], nvj, a[i]));   // two FMAs
+                if (GLOBAL) {   // two FMAs an element, eight loads in flight
+                    for (int i0 = lane; i0 < m; i0 += 256) {
+                        double x[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int i = i0 + 32 * u;
+                            x[u] = i < m ? a[i] : 0.0;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int i = i0 + 32 * u;
+                            if (i < m) a[i] = fma(v[i], nwj, fma(w[i], nvj, x[u]));
+                        }
+                    }
+                } else {
+                    for (int i = lane; i < m; i += 32) a[i] = fma(v[i], nwj, fma(w[i], nvj, a[i]));   // two FMAs
+                }
             }
         __syncthreads();
     }
@@ -459,7 +486,16 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         if (r == o) {
             const double *colk = colp(k / G);
             double ss = 0.0;                         // sum of squares below the subdiagonal, all warps
-            for (int i = k + 2 + tid; i < n; i += TRD_THREADS) ss = fma(colk[i], colk[i], ss);
+            for (int i0 = k + 2 + tid; i0 < n; i0 += 8 * TRD_THREADS) {   // eight loads in flight
+                double x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int i = i0 + u * TRD_THREADS;
+                    x[u] = i < n ? colk[i] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) ss = fma(x[u], x[u], ss);
+            }
             ss = wsum(ss);
             if (lane == 0) red[warp] = ss;
             __syncthreads();
@@ -490,7 +526,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         }
         if (!(alive = tg_sync(bar, G, epoch, err, grp.spin))) break;   // v and t of step k published
         const double t = *(volatile double *)(gt + par);
-        for (int i = tid; i < m; i += TRD_THREADS) v[i] = ((volatile double *)vb)[i];
+        for (int i0 = tid; i0 < m; i0 += 4 * TRD_THREADS) {   // written by another CTA: past L1
+            double x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * TRD_THREADS;
+                x[u] = i < m ? __ldcg(vb + i) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + u * TRD_THREADS < m) v[i0 + u * TRD_THREADS] = x[u];
+        }
         __syncthreads();
         const int jj0 = k + 1 > r ? (k + 1 - r + G - 1) / G : 0;   // first own column j > k
         double sp = 0.0;
@@ -499,6 +545,20 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
                 const double *a = colp(jj) + k + 1;
                 double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
                 int i = lane;
+                // four rounds of the four accumulators per batch: their sixteen
+                // loads go out before the first FMA
+                for (; i + 96 + 384 < m; i += 512) {
+                    double x[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) x[u] = a[i + 32 * u];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        a0 = fma(x[4 * u], v[i + 128 * u], a0);
+                        a1 = fma(x[4 * u + 1], v[i + 128 * u + 32], a1);
+                        a2 = fma(x[4 * u + 2], v[i + 128 * u + 64], a2);
+                        a3 = fma(x[4 * u + 3], v[i + 128 * u + 96], a3);
+                    }
+                }
                 for (; i + 96 < m; i += 128) {
                     a0 = fma(a[i], v[i], a0);
                     a1 = fma(a[i + 32], v[i + 32], a1);
@@ -528,14 +588,38 @@ __global__ void __launch_bounds__(TRD_THREADS, 1)
         __syncthreads();
         const double K = kk;
         if (t != 0.0) {
-            for (int i = tid; i < m; i += TRD_THREADS) w[i] = fma(K, v[i], ((volatile double *)pb)[i]);
+            for (int i0 = tid; i0 < m; i0 += 4 * TRD_THREADS) {
+                double x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * TRD_THREADS;
+                    x[u] = i < m ? __ldcg(pb + i) : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * TRD_THREADS;
+                    if (i < m) w[i] = fma(K, v[i], x[u]);
+                }
+            }
             __syncthreads();
             for (int jj = jj0 + warp; jj < ncol; jj += NW) {
                 const int jc = r + G * jj - k - 1;
                 const double vj = v[jc], wj = w[jc];
                 double *a = colp(jj) + k + 1;
                 const double nvj = -vj, nwj = -wj;
-                for (int i = lane; i < m; i += 32) a[i] = fma(v[i], nwj, fma(w[i], nvj, a[i]));   // two FMAs
+                for (int i0 = lane; i0 < m; i0 += 256) {   // two FMAs an element, eight loads in flight
+                    double x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = i0 + 32 * u;
+                        x[u] = i < m ? a[i] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = i0 + 32 * u;
+                        if (i < m) a[i] = fma(v[i], nwj, fma(w[i], nvj, x[u]));
+                    }
+                }
             }
         }
         __syncthreads();
