@@ -59,14 +59,15 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-full", action="store_true",
                     help="serve the fifth configuration's full size ranges (L up to 64, m up to 512) at low rates")
-    ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large", "tc-sector"], default=None,
+    ap.add_argument("--profile-case", choices=["renorm", "trd-grid", "sweep-large", "tc-sector", "batch"], default=None,
                     help="for profiler captures of single kernels: run one small workload and exit "
                          "(renorm: the spin-1 chain to L=24, m=256, whose last steps renormalise on the "
                          "device; trd-grid: one RDM of a 1000-state rho block on the whole-GPU reduction; "
                          "sweep-large: the finite sweep of the spin-1 L=64 m=512 chain in --precision; "
                          "tc-sector: four FP32 H*psi of the spin-1 L=64 m=512 chain's last infinite "
                          "superblock with every sector of >= 32 left states on the tensor-core GEMM, "
-                         "128-column tiles)")
+                         "128-column tiles; batch: the 64-superblock batched solve, its timed call in the "
+                         "NVTX range batch_timed)")
     ap.add_argument("--profile", action="store_true",
                     help="for profiler captures: time the headline path only, no clock sampler, no "
                          "compute-rate probe, no e2e, no CPU baseline (no child processes)")
@@ -453,6 +454,32 @@ def run_profile_case(case, precision="mixed"):
         _t.cuda.synchronize()
         fd, _ = s.flops()
         print(json.dumps({"profile_case": case, "N": s.n, "flops_dense": fd}))
+        return
+    if case == "batch":
+        import torch as _t
+        rng = np.random.default_rng(BATCH_CASE["seed"])
+        sbs = []
+        for k in range(BATCH_CASE["distinct"]):
+            L = int(rng.choice(BATCH_CASE["L"]))
+            m = int(rng.choice(BATCH_CASE["m"]))
+            u = float(rng.uniform(*BATCH_CASE["U"]))
+            d = nss.DMRG(nss.MODEL_HUBBARD, L // 2, m, u=u, hfmode=False, dmrg_qn=(0.5, 0.5), lanc_neigen=1)
+            d.prepare_last()
+            s = nss.Superblock()
+            s.upload_desc(d.export_superblock())
+            d.close()
+            sbs.append(s)
+        tol, nit = BATCH_CASE["lanc_tolerance"], BATCH_CASE["lanc_niter"]
+        seeds = np.arange(1, len(sbs) + 1, dtype=np.uint64)
+        nss.eigh_batch(sbs[:2], nitermax=nit, tol=tol)
+        _t.cuda.synchronize()
+        _t.cuda.nvtx.range_push("batch_timed")
+        t0 = time.perf_counter()
+        eb, nops = nss.eigh_batch(sbs, nitermax=nit, tol=tol, seeds=seeds)
+        t_batch = time.perf_counter() - t0
+        _t.cuda.nvtx.range_pop()
+        print(json.dumps({"profile_case": case, "solves": len(sbs), "s": t_batch, "matvecs_mean": float(np.mean(nops)),
+                          "N_sum": int(sum(s.n for s in sbs))}))
         return
     if case == "sweep-large":
         d = nss.DMRG(nss.MODEL_HEISENBERG_ONE, 32, 512, msweep=[512], dmrg_qn=(0.0, 0.0), lanc_neigen=1,

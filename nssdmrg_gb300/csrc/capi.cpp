@@ -113,6 +113,7 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
     ctx->c.tc_auto = nss::tune_enabled();
     nss::mma_tile_default(&ctx->c.mma_bn, &ctx->c.mma_split);
     ctx->c.mma_lolo = nss::mma_lolo_default();
+    ctx->c.mma_kps = nss::mma_kps_default();
     ctx->c.budget = hbm_budget;
     if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_err = "nss_create: stream creation failed";
@@ -143,6 +144,12 @@ void nss_destroy(nss_ctx *ctx) {
     nss::ctx_free(ctx->c, ctx->d_hv);
     nss::ctx_free(ctx->c, ctx->d_psi);
     if (ctx->c.solver) cusolverDnDestroy((cusolverDnHandle_t)ctx->c.solver);
+    if (ctx->c.hv_side) {
+        cudaStreamSynchronize(ctx->c.hv_side);
+        cudaStreamDestroy(ctx->c.hv_side);
+        cudaEventDestroy(ctx->c.hv_fork);
+        cudaEventDestroy(ctx->c.hv_join);
+    }
     cudaStreamDestroy(ctx->c.stream);
     delete ctx;
 }

@@ -190,6 +190,10 @@ struct Ctx {
     std::unordered_map<void *, size_t> sizes;   // live allocations
     std::string err;
     cudaStream_t stream = nullptr;
+    // the mixed product's side stream (CUDA-core tiles beside the tensor-core
+    // GEMM) and its fork / join events, made on first use
+    cudaStream_t hv_side = nullptr;
+    cudaEvent_t hv_fork = nullptr, hv_join = nullptr;
     void *solver = nullptr;      // cusolverDnHandle_t
     DevSb sb;
     DevLanczos lz;
@@ -202,6 +206,7 @@ struct Ctx {
     int mma_bn = 64;             // tensor-core tile width (64 or 128) and K-loop split
     bool mma_split = true;
     bool mma_lolo = false;       // fourth product lo.lo in the split-TF32 GEMM
+    int mma_kps = 1;             // K slabs (of 32) per tensor-memory accumulation before FP32 promotion
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
@@ -283,6 +288,9 @@ int tc_min_dl_default();
 void mma_tile_default(int *bn, bool *split);
 // the split-TF32 GEMM's fourth product lo.lo: env NSS_TC_LOLO (default off)
 bool mma_lolo_default();
+// NSS_TC_KPS (1 or 2, default 1): K slabs the tensor core accumulates before
+// the epilogue promotes the partial sum to FP32 registers
+int mma_kps_default();
 // Poll limit of every bounded device wait (the grid barriers of the
 // cooperative Lanczos and tridiagonalisation kernels): env NSS_WAIT_LIMIT,
 // default 2^22 polls (about 2 s).  A wait that runs out makes its kernel

@@ -33,6 +33,11 @@ void mma_tile_default(int *bn, bool *split) {
     *split = !(sp && std::atoi(sp) == 0);
 }
 
+int mma_kps_default() {
+    const char *e = std::getenv("NSS_TC_KPS");
+    return (e && std::atoi(e) == 2) ? 2 : 1;
+}
+
 bool mma_lolo_default() {
     const char *e = std::getenv("NSS_TC_LOLO");
     return e && std::atoi(e) != 0;
@@ -686,19 +691,57 @@ Hv32Ops hv32_ops(const DevSb &s) {
     return op;
 }
 
+// hv[i] += the tensor-core planes' sum at i (plane 0 first; zero outside the
+// tensor-core sectors)
+__global__ void __launch_bounds__(256) k_add_planes(float *__restrict__ hv, const float *__restrict__ planes,
+                                                    int64_t n, int np, const int *stop) {
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float d = planes[i];
+        for (int p = 1; p < np; ++p) d += planes[(int64_t)p * n + i];
+        hv[i] += d;
+    }
+}
+
 int hv_device_fp32(Ctx &c, const float *d_v, float *d_hv, const int *stop) {
     DevSb &s = c.sb;
     if (!s.valid) {
         c.err = "nss_hv: no superblock uploaded";
         return NSS_ERR_STATE;
     }
-    // the tensor-core sectors' dense products first: the terms-only tiles add them
-    if (int rc = hv_device_mma(c, d_v, stop)) return rc;
-    if (s.ntiles32 > 0) {
-        k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, hv32_ops(s), stop);
-        c.launches += 1;
-        NSS_CUDA_TRY(c, cudaGetLastError());
+    if (s.mma_nitems == 0) {
+        if (s.ntiles32 > 0) {
+            k_hv_fp32<<<s.ntiles32, 256, 0, c.stream>>>(d_v, d_hv, s.d_tiles32, hv32_ops(s), stop);
+            c.launches += 1;
+            NSS_CUDA_TRY(c, cudaGetLastError());
+        }
+        return NSS_OK;
     }
+    // tensor-core sectors: the CUDA-core tiles (their A x B terms, and the
+    // small sectors) run on a side stream beside the W packing and the GEMM;
+    // the GEMM's planes are added when both are done
+    if (!c.hv_side) {
+        NSS_CUDA_TRY(c, cudaStreamCreateWithFlags(&c.hv_side, cudaStreamNonBlocking));
+        NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&c.hv_fork, cudaEventDisableTiming));
+        NSS_CUDA_TRY(c, cudaEventCreateWithFlags(&c.hv_join, cudaEventDisableTiming));
+    }
+    NSS_CUDA_TRY(c, cudaEventRecord(c.hv_fork, c.stream));
+    NSS_CUDA_TRY(c, cudaStreamWaitEvent(c.hv_side, c.hv_fork, 0));
+    if (s.ntiles32 > 0) {
+        Hv32Ops op = hv32_ops(s);
+        op.tc = nullptr;   // the planes come afterwards
+        k_hv_fp32<<<s.ntiles32, 256, 0, c.hv_side>>>(d_v, d_hv, s.d_tiles32, op, stop);
+        c.launches += 1;
+    }
+    NSS_CUDA_TRY(c, cudaEventRecord(c.hv_join, c.hv_side));
+    if (int rc = hv_device_mma(c, d_v, stop)) return rc;
+    NSS_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.hv_join, 0));
+    int nsm = 0;
+    NSS_CUDA_TRY(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    k_add_planes<<<(unsigned)std::min<int64_t>(4 * nsm, (s.n + 255) / 256), 256, 0, c.stream>>>(
+        d_hv, s.d_mma_out, s.n, s.mma_nplanes, stop);
+    c.launches += 1;
+    NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;
 }
 

@@ -223,7 +223,7 @@ __device__ __forceinline__ void item_rows(const MmaItem &m, int c, int &ar, int 
     br = (p0 ? m.b_row0 : m.b_row1) + cc * m.b_step + m.n0;
 }
 
-template <int BN>
+template <int BN, int KPS>
 __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_constant__ CUtensorMap map_a,
                                                                const __grid_constant__ CUtensorMap map_b,
                                                                const MmaItem *__restrict__ items,
@@ -346,16 +346,18 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
         // [B_hi; B_lo] (N = 2 BN: hi.hi in the first BN columns, hi.lo in the
         // second), then A_lo x B_hi (and A_lo x B_lo) into the first BN.
         constexpr uint32_t IDESC2 = idesc_tf32(2 * BN), IDESC1 = idesc_tf32(BN);
-        int it = 0;                   // slabs issued (= stage fills consumed, = accumulator uses)
+        int it = 0;                   // slabs issued (= stage fills consumed)
+        int gq = 0;                   // accumulator groups (KPS slabs of one piece each)
         bool issued = false, ok = true;
         for (int i = rg.x; i < rg.y && ok && !*abort; ++i) {
             const int nk = items[i].nk;
             for (int c = 0; c < nk; ++c, ++it) {
-                const int s = it % S, acc = it % NB;
+                const int s = it % S, acc = gq % NB;
+                const bool gfirst = c % KPS == 0, glast = c % KPS == KPS - 1 || c == nk - 1;
                 const uint32_t par = (uint32_t)(it / S) & 1u;
                 const uint32_t tacc = tmem + (uint32_t)(acc * C::ACOLS);
-                // the epilogue has drained this buffer (its use NB slabs ago)
-                if (!mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(it / NB) & 1u) ^ 1u, spin, abort) ||
+                // the epilogue has drained this buffer (its use NB groups ago)
+                if ((gfirst && !mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(gq / NB) & 1u) ^ 1u, spin, abort)) ||
                     !mbar_wait(smem_u32(&conv[s]), par, spin, abort)) {
                     give_up();
                     ok = false;
@@ -367,13 +369,16 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
 #pragma unroll
                 for (int kk = 0; kk < MM_KC / 8; ++kk) {
                     const uint32_t o = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzled row
-                    mma_tf32(tacc, desc_sw128(a_hi + o), desc_sw128(b_hi + o), IDESC2, kk > 0 ? 1u : 0u);
+                    mma_tf32(tacc, desc_sw128(a_hi + o), desc_sw128(b_hi + o), IDESC2, (kk > 0 || !gfirst) ? 1u : 0u);
                     mma_tf32(tacc, desc_sw128(a_lo + o), desc_sw128(b_hi + o), IDESC1, 1u);
                     if (lolo) mma_tf32(tacc, desc_sw128(a_lo + o), desc_sw128(b_lo + o), IDESC1, 1u);
                 }
                 issued = true;
-                mma_commit(smem_u32(&empty[s]));     // the stage is free once these MMAs have read it
-                mma_commit(smem_u32(&tfull[acc]));   // ... and the slab's partial product is ready
+                mma_commit(smem_u32(&empty[s]));       // the stage is free once these MMAs have read it
+                if (glast) {
+                    mma_commit(smem_u32(&tfull[acc]));  // ... and the group's partial product is ready
+                    ++gq;
+                }
             }
         }
         if (issued) {   // every MMA of this lane done before the CTA frees its TMEM
@@ -389,17 +394,18 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
         // product as accurate as FP32 FMA chains
         const int q = warp & 3, h = (warp - MM_EPI0) >> 2;
         float *stg = (float *)(smem + (size_t)S * C::STAGE) + (size_t)(warp - MM_EPI0) * 32 * C::OUT_LD;
-        int it = 0;
+        int gq = 0;
         for (int i = rg.x; i < rg.y && !*abort; ++i) {
             const MmaItem m = items[i];
             float sum[C::HALF];
 #pragma unroll
             for (int j = 0; j < C::HALF; ++j) sum[j] = 0.f;
             bool ok = true;
-            for (int c = 0; c < m.nk; ++c, ++it) {
-                const int acc = it % NB;
+            const int ngr = (m.nk + KPS - 1) / KPS;
+            for (int c = 0; c < ngr; ++c, ++gq) {
+                const int acc = gq % NB;
                 bool got = true;
-                if (lane == 0) got = mbar_wait(smem_u32(&tfull[acc]), (uint32_t)(it / NB) & 1u, spin, abort);
+                if (lane == 0) got = mbar_wait(smem_u32(&tfull[acc]), (uint32_t)(gq / NB) & 1u, spin, abort);
                 if (__shfl_sync(0xffffffffu, got ? 1 : 0, 0) == 0) {
                     if (lane == 0) give_up();
                     ok = false;
@@ -467,14 +473,17 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-template <int BN>
-int set_smem_attr(Ctx &c) {
+template <int BN, int KPS>
+int launch_mma(Ctx &c, const CUtensorMap &ma, const CUtensorMap &mb, uint32_t spin, const int *stop) {
     static bool done = false;
     if (!done) {
-        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_sector_mma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_sector_mma<BN, KPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              MmaCfg<BN>::SMEM));
         done = true;
     }
+    DevSb &s = c.sb;
+    k_sector_mma<BN, KPS><<<s.mma_grid, MM_THREADS, MmaCfg<BN>::SMEM, c.stream>>>(
+        ma, mb, s.d_mma_items, s.d_mma_rng, s.d_mma_out, s.n, c.mma_lolo ? 1 : 0, spin, s.d_tc_err, stop);
     return NSS_OK;
 }
 
@@ -625,15 +634,12 @@ int hv_device_mma(Ctx &c, const float *d_v, const int *stop) {
     alignas(64) CUtensorMap ma, mb;
     std::memcpy(&ma, s.mma_map_a, sizeof(ma));
     std::memcpy(&mb, s.mma_map_b, sizeof(mb));
-    if (s.mma_bn == 128) {
-        if (int rc = set_smem_attr<128>(c)) return rc;
-        k_sector_mma<128><<<s.mma_grid, MM_THREADS, MmaCfg<128>::SMEM, c.stream>>>(
-            ma, mb, s.d_mma_items, s.d_mma_rng, s.d_mma_out, s.n, c.mma_lolo ? 1 : 0, spin, s.d_tc_err, stop);
-    } else {
-        if (int rc = set_smem_attr<64>(c)) return rc;
-        k_sector_mma<64><<<s.mma_grid, MM_THREADS, MmaCfg<64>::SMEM, c.stream>>>(
-            ma, mb, s.d_mma_items, s.d_mma_rng, s.d_mma_out, s.n, c.mma_lolo ? 1 : 0, spin, s.d_tc_err, stop);
-    }
+    int rc;
+    if (s.mma_bn == 128)
+        rc = c.mma_kps == 2 ? launch_mma<128, 2>(c, ma, mb, spin, stop) : launch_mma<128, 1>(c, ma, mb, spin, stop);
+    else
+        rc = c.mma_kps == 2 ? launch_mma<64, 2>(c, ma, mb, spin, stop) : launch_mma<64, 1>(c, ma, mb, spin, stop);
+    if (rc) return rc;
     c.launches += 2;
     NSS_CUDA_TRY(c, cudaGetLastError());
     return NSS_OK;
