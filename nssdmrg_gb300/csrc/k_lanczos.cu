@@ -1121,6 +1121,7 @@ struct BatchArgs {
     int *err;
     int steps;                   // iterations of this launch
     uint32_t spin;               // poll limit of the grid barriers (wait_limit)
+    unsigned *qcnt;              // [CHUNK_MAXIT] item queue heads, zero at launch
 };
 
 constexpr int BATCH_MAX = 160;   // solves per launch (each needs a CTA)
@@ -1134,6 +1135,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
     __shared__ float bprev[BATCH_MAX], balpha[BATCH_MAX], bbb[BATCH_MAX];
     __shared__ int alive[BATCH_MAX], p2[BATCH_MAX], brkm[BATCH_MAX];
     __shared__ int my_s, any_p2;
+    __shared__ int qn[2];
     const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x, grp = tid >> 8, lt = tid & 255;
     const int ns = B.ns;
     unsigned epoch = 0;
@@ -1173,26 +1175,36 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
     const int nx = anc ? 3 + nd : 0;
     int done = 0;
     for (int step = 0; step < B.steps; ++step) {
-        // ---- H*psi of every running solve, all items over all CTAs
-        for (int gi = 2 * blk + grp; gi < B.nitems; gi += 2 * G) {
+        // ---- H*psi of every running solve, all items over all CTAs: each
+        // thread group takes the next item off a global queue (longest
+        // first), fetching the index after next while it works on one
+        if (lt == 0) qn[grp] = (int)atomicAdd(B.qcnt + step, 1u);
+        GroupSync{1 + grp}();
+        for (int gi = qn[grp]; gi < B.nitems;) {
+            int nxt = 0;
+            if (lt == 0) nxt = (int)atomicAdd(B.qcnt + step, 1u);
             const int2 g = B.gitems[gi];
             const BatchSolve &S = B.s[g.x];
             const int tj = S.c.j0 + step;
-            if (!alive[g.x] || tj >= S.c.jend) continue;
-            const bool first = tj == S.c.j0 && S.c.first_from_v;
-            const float *x = first ? (const float *)S.c.o.V + (int64_t)tj * S.c.o.n : S.c.buf[tj & 1];
-            const float sc = first ? 1.f : 1.f / bprev[g.x];
-            float ap = hv32_item(S.c.items[g.y], x, S.c.slot, S.c.op, ism[grp], lt, GroupSync{1 + grp}, sc);
-            // group sum of the alpha partial (named barrier of the group)
-            ap = warp_sum<float>(ap);
-            if ((lt & 31) == 0) scr[grp * 8 + (lt >> 5)] = ap;
-            GroupSync{1 + grp}();
-            if (lt == 0) {
-                float t = 0.f;
-                for (int q = 0; q < 8; ++q) t += scr[grp * 8 + q];
-                S.pitem[g.y] = t;
+            if (alive[g.x] && tj < S.c.jend) {
+                const bool first = tj == S.c.j0 && S.c.first_from_v;
+                const float *x = first ? (const float *)S.c.o.V + (int64_t)tj * S.c.o.n : S.c.buf[tj & 1];
+                const float sc = first ? 1.f : 1.f / bprev[g.x];
+                float ap = hv32_item(S.c.items[g.y], x, S.c.slot, S.c.op, ism[grp], lt, GroupSync{1 + grp}, sc);
+                // group sum of the alpha partial (named barrier of the group)
+                ap = warp_sum<float>(ap);
+                if ((lt & 31) == 0) scr[grp * 8 + (lt >> 5)] = ap;
+                GroupSync{1 + grp}();
+                if (lt == 0) {
+                    float t = 0.f;
+                    for (int q = 0; q < 8; ++q) t += scr[grp * 8 + q];
+                    S.pitem[g.y] = t;
+                }
             }
             GroupSync{1 + grp}();
+            if (lt == 0) qn[grp] = nxt;
+            GroupSync{1 + grp}();
+            gi = qn[grp];
         }
         if (!grid_sync(B.bar, epoch, B.err, B.spin)) break;
         const bool run = me >= 0 && alive[me] && Mp->c.j0 + step < Mp->c.jend;
@@ -2368,6 +2380,7 @@ struct BatchEngine {
     int2 *d_gitems = nullptr, *h_gitems = nullptr;
     int cap_items = 0;
     float *d_st = nullptr;
+    unsigned *d_q = nullptr;     // item queue heads of a launch
     double *h_res = nullptr;     // [BATCH_MAX][8] pinned refinement results
     size_t smem_set = 0;         // dynamic shared memory of its launches (the most any round needed)
     ~BatchEngine() {
@@ -2376,6 +2389,7 @@ struct BatchEngine {
         ctx_free(*c0, d_solves);
         ctx_free(*c0, d_gitems);
         ctx_free(*c0, d_st);
+        ctx_free(*c0, d_q);
         if (h_solves) cudaFreeHost(h_solves);
         if (h_gitems) cudaFreeHost(h_gitems);
         if (h_res) cudaFreeHost(h_res);
@@ -2393,6 +2407,7 @@ int engine_init(BatchEngine &E, Ctx &c0) {
     }
     NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_solves, (size_t)BATCH_MAX));
     NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_st, (size_t)4 * BATCH_MAX));
+    NSS_CUDA_TRY(c0, ctx_alloc(c0, &E.d_q, (size_t)CHUNK_MAXIT));
     NSS_CUDA_TRY(c0, cudaMallocHost((void **)&E.h_solves, sizeof(BatchSolve) * BATCH_MAX));
     NSS_CUDA_TRY(c0, cudaMallocHost((void **)&E.h_res, sizeof(double) * 8 * BATCH_MAX));
     NSS_CUDA_TRY(c0, cudaMemsetAsync(c0.lz.counter, 0, 4 * sizeof(unsigned), c0.stream));
@@ -2474,12 +2489,30 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
     if (na > 0) {
         double ntot = 0.0;
         for (int b : act) ntot += (double)E.solves[b].n;
+        // CTAs per solve for its rows: one each, the rest in proportion to
+        // the orthogonalisation's work, rows x basis columns (largest
+        // remainders take the leftovers)
         std::vector<int> ncta(na, 1);
-        int left = G - na;
-        for (int q = 0; q < na && left > 0; ++q) {
-            const int extra = std::min(left, (int)((double)(G - na) * E.solves[act[q]].n / ntot));
-            ncta[q] += extra;
-            left -= extra;
+        {
+            std::vector<double> wgt(na);
+            double wtot = 0.0;
+            for (int q = 0; q < na; ++q) {
+                const BatchState &B = E.solves[act[q]];
+                wgt[q] = (double)B.n * (double)(B.j0 + CHECK + 16);
+                wtot += wgt[q];
+            }
+            int left = G - na;
+            std::vector<std::pair<double, int>> rem;
+            const int pool = left;
+            for (int q = 0; q < na && pool > 0; ++q) {
+                const double share = pool * wgt[q] / wtot;
+                const int whole = std::min(left, (int)share);
+                ncta[q] += whole;
+                left -= whole;
+                rem.push_back({share - whole, q});
+            }
+            std::stable_sort(rem.begin(), rem.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+            for (size_t r = 0; r < rem.size() && left > 0; ++r, --left) ++ncta[rem[r].second];
         }
         int tot_items = 0;
         for (int b : act) tot_items += E.solves[b].c->sb.nitems32;
@@ -2553,7 +2586,9 @@ int engine_step(BatchEngine &E, int max_done, int *ndone, int *ids, double *ener
                                          st));
         NSS_CUDA_TRY(c0, allow_smem((const void *)k_batch32, smem_max));
         E.smem_set = std::max(E.smem_set, smem_max);
+        NSS_CUDA_TRY(c0, cudaMemsetAsync(E.d_q, 0, CHUNK_MAXIT * sizeof(unsigned), st));
         BatchArgs ba;
+        ba.qcnt = E.d_q;
         ba.s = E.d_solves;
         ba.ns = na;
         ba.nitems = ng;
