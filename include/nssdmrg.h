@@ -258,6 +258,13 @@ int nss_chunk_stats(const nss_ctx *ctx, double *ms, int *launches, int64_t *iter
  * reference. */
 int nss_chunk_cache(const nss_ctx *ctx, int *vectors, int64_t *rows);
 
+/* CUDA graphs of the last nss_eigh: Lanczos chunks (four iterations of H*psi
+ * and orthogonalisation) that ran as one replayed graph, and graphs captured.
+ * They apply where an iteration is several launches (the FP64 method, the
+ * mixed method with tensor-core sectors); NSS_GRAPH=0 turns them off.  No
+ * counterpart in the reference. */
+int nss_graph_stats(const nss_ctx *ctx, int *replays, int *captures);
+
 /* The mixed path's plan for the uploaded superblock, as the tile tuner chose
  * it: candidate 0 puts every sector on CUDA cores (the persistent Lanczos
  * kernel), 1 and 2 the sectors with Dl >= 32 on the tensor-core GEMM with

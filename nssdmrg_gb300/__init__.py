@@ -152,6 +152,7 @@ def lib():
         "nss_time_chunks": (C.c_int, [P, C.c_int]),
         "nss_chunk_stats": (C.c_int, [P, C.POINTER(D), C.POINTER(C.c_int), C.POINTER(I64), C.POINTER(D)]),
         "nss_chunk_cache": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(I64)]),
+        "nss_graph_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "nss_batch_create": (P, [P]),
         "nss_batch_add": (C.c_int, [P, P, C.c_uint64, C.c_int, D, C.POINTER(C.c_int)]),
         "nss_batch_step": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), P, P, P]),
@@ -458,6 +459,12 @@ class Superblock:
         ms, nl, it, cols = C.c_double(), C.c_int(), C.c_int64(), C.c_double()
         self._check(lib().nss_chunk_stats(self._ctx, C.byref(ms), C.byref(nl), C.byref(it), C.byref(cols)))
         return ms.value, nl.value, it.value, cols.value
+
+    def graph_stats(self):
+        """(chunks replayed as CUDA graphs, graphs captured) in the last solve."""
+        r, cpt = C.c_int(), C.c_int()
+        self._check(lib().nss_graph_stats(self._ctx, C.byref(r), C.byref(cpt)))
+        return r.value, cpt.value
 
     def chunk_cache(self):
         """(basis vectors cached per CTA, rows per CTA) of the persistent

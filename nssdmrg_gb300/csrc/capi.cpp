@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -114,6 +115,10 @@ nss_ctx *nss_create(int device, size_t hbm_budget) {
     nss::mma_tile_default(&ctx->c.mma_bn, &ctx->c.mma_split);
     ctx->c.mma_lolo = nss::mma_lolo_default();
     ctx->c.mma_kps = nss::mma_kps_default();
+    {
+        const char *g = std::getenv("NSS_GRAPH");
+        ctx->c.use_graphs = !(g && std::atoi(g) == 0);
+    }
     ctx->c.budget = hbm_budget;
     if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_err = "nss_create: stream creation failed";
@@ -329,6 +334,13 @@ int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, con
 int nss_time_chunks(nss_ctx *ctx, int enable) {
     if (!ctx) return NSS_ERR_INVALID;
     ctx->c.time_chunks = enable != 0;
+    return NSS_OK;
+}
+
+int nss_graph_stats(const nss_ctx *ctx, int *replays, int *captures) {
+    if (!ctx) return NSS_ERR_INVALID;
+    if (replays) *replays = ctx->c.graph_replays;
+    if (captures) *captures = ctx->c.graph_captures;
     return NSS_OK;
 }
 

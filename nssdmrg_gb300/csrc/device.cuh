@@ -33,6 +33,7 @@ struct DevTerm {          // one A x B term, grouped by output sector
 
 struct DevSb {
     bool valid = false;
+    uint64_t gen = 0;                  // upload generation (process-wide count)
     int nsb = 0, tnso = 0, m_left = 0, m_right = 0;
     int64_t n = 0;
     // host mirrors of the small tables
@@ -119,6 +120,18 @@ struct DevLanczos {
     size_t chunk_smem_vc = 0;    // its dynamic shared memory with the row cache
     float *pitem = nullptr;      // per-item alpha partials of the batched kernel
     int cap_pitem = 0;
+    // CUDA-graph replay of the Lanczos chunks that run as separate launches
+    // (FP64 method, mixed method with tensor-core sectors): the fixed input
+    // vector of H*psi, the device step counter, and the instantiated graph
+    // of CHECK iterations with the key it was captured for
+    void *vcur = nullptr;        // [n] doubles' room
+    int *jdev = nullptr;
+    cudaGraphExec_t gx = nullptr;
+    uint64_t gx_gen = 0;
+    int gx_prec = -1, gx_mmax = 0, gx_ndefl = -1, gx_launches = 0;
+    uint32_t gx_spin = 0;        // the wait limit the graph's kernels were captured with
+    const void *gx_anc = nullptr;
+    bool gx_failed = false;      // capture failed once: this workspace runs without graphs
 };
 
 struct DevRdm {
@@ -207,6 +220,8 @@ struct Ctx {
     bool mma_split = true;
     bool mma_lolo = false;       // fourth product lo.lo in the split-TF32 GEMM
     int mma_kps = 1;             // K slabs (of 32) per tensor-memory accumulation before FP32 promotion
+    bool use_graphs = true;      // NSS_GRAPH=0: Lanczos chunks as separate launches, no CUDA graphs
+    int graph_replays = 0, graph_captures = 0;   // of the last nss_eigh
     // last nss_eigh statistics
     int last_numop = 0;
     double last_ms_eigh = 0.0;
@@ -437,5 +452,16 @@ void measure_release(Ctx &c);
             (c).err = std::string(#call) + " (" + __FILE__ + ":" + std::to_string(__LINE__) + "): " + \
                       cudaGetErrorString(_e);                                   \
             return _e == cudaErrorMemoryAllocation ? NSS_ERR_NOMEM : NSS_ERR_CUDA; \
+        }                                                                       \
+    } while (0)
+
+// the same inside a function that reports failure with its own value `fail`
+#define NSS_CUDA_TRY_R(c, call, fail)                                           \
+    do {                                                                        \
+        cudaError_t _e = (call);                                                \
+        if (_e != cudaSuccess) {                                                \
+            (c).err = std::string(#call) + " (" + __FILE__ + ":" + std::to_string(__LINE__) + "): " + \
+                      cudaGetErrorString(_e);                                   \
+            return (fail);                                                      \
         }                                                                       \
     } while (0)

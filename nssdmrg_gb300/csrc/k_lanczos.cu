@@ -121,6 +121,8 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 }
 
 // uniform(-1,1) start vector from a counter-based hash of (seed, stream, i)
+__global__ void k_seti(int *p, int v) { *p = v; }
+
 template <class T>
 __global__ void k_random(T *x, int64_t n, uint64_t seed, uint64_t stream) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -325,6 +327,11 @@ struct OrthArgs {
     int ndefl;
     double *h_m;
     uint32_t spin;               // poll limit of the grid barriers (wait_limit)
+    // replayed chunks (CUDA graph): the step is read from *jdev and advanced
+    // by the kernel, and the new Lanczos vector is also written to vcur, the
+    // fixed input of the next H*psi (null: step a.j, no copy)
+    int *jdev;
+    void *vcur;
 };
 
 constexpr int PA_COLS = 8;       // per-CTA values of the first phase (alpha, u.w, r.v, y_k.w)
@@ -587,7 +594,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
     const int64_t chunk = (n + G - 1) / G;
     const int64_t i0 = min(n, (int64_t)blk * chunk), i1 = min(n, i0 + chunk);
     T *V = (T *)a.V, *w = (T *)a.w;
-    const int j = a.j, m = j + 1;
+    const int j = a.jdev ? *(volatile const int *)a.jdev : a.j, m = j + 1;
     const T *vj = V + (int64_t)j * n;
     const T *vjm = V + (int64_t)(j > 0 ? j - 1 : 0) * n;
     T *pA = (T *)a.part, *pH = pA + PA_COLS * G, *pB = pH + (int64_t)ps * G, *pH2 = pB + G,
@@ -695,10 +702,16 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_orth(OrthArgs a) {
         if (!brk) {
             const T inv = (T)1 / beta_j;
             T *vn = V + (int64_t)m * n;
-            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) vn[i] = w[i] * inv;
+            T *vc = (T *)a.vcur;
+            for (int64_t i = i0 + tid; i < i1; i += ORTH_THREADS) {
+                const T x = w[i] * inv;
+                vn[i] = x;
+                if (vc) vc[i] = x;
+            }
         }
     }
     if (blk == 0 && tid == 0) {
+        if (a.jdev) *a.jdev = j + 1;   // every CTA read j before the first barrier
         a.alpha[j] = (double)alpha_j;
         a.beta[j] = (double)beta_j;
         a.h_alpha[j] = (double)alpha_j;
@@ -1700,6 +1713,12 @@ int ensure_lanczos(Ctx &c, int64_t n, int cap, bool mixed) {
         }
     }
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.w, (size_t)n));
+    {
+        double *vc = nullptr;
+        NSS_CUDA_TRY(c, ctx_alloc(c, &vc, (size_t)n));
+        z.vcur = vc;
+    }
+    NSS_CUDA_TRY(c, ctx_alloc(c, &z.jdev, 1));
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.evecs, (size_t)4 * n));
     // scalars, projection coefficients, restart scratch alpha/beta, refinement
     NSS_CUDA_TRY(c, ctx_alloc(c, &z.scal, (size_t)S_NSCAL + 4 * (cap + 2) + 8));
@@ -1827,6 +1846,10 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
     oa.ndefl = anc ? anc->ndefl : 0;
     oa.h_m = z.d_h_ab + 2 * (cap + 1);
     oa.spin = wait_limit();
+    oa.jdev = nullptr;
+    // the launched chunks keep vcur current too, so that a replayed chunk
+    // can follow one
+    oa.vcur = c.use_graphs ? z.vcur : nullptr;
     const double *hm = z.h_ab + 2 * (cap + 1);
     std::vector<double> cvec;
     // Chunks of CHECK iterations, each ending with an event; the host checks
@@ -1884,6 +1907,27 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
             cudaEventRecord(evs[slot], st);
             return jend;
         }
+        // a whole chunk of a plain (not anchored) Lanczos run replays the
+        // CUDA graph of CHECK iterations captured for this superblock,
+        // precision and iteration cap (the step and the input vector live on
+        // the device); the first chunk of a key runs as launches and captures
+        // the graph for the next ones
+        const int prec = sizeof(T) == sizeof(float) ? 1 : 0;
+        const bool key_ok = z.gx && z.gx_gen == c.sb.gen && z.gx_prec == prec && z.gx_mmax == mmax &&
+                            z.gx_anc == oa.anc_u && z.gx_ndefl == oa.ndefl && z.gx_spin == oa.spin;
+        const bool graphable = c.use_graphs && !z.gx_failed && jend - j0 == CHECK && oa.anc_u == nullptr;
+        if (graphable && key_ok) {
+            if (from_v)
+                NSS_CUDA_TRY_R(c, cudaMemcpyAsync(z.vcur, V + (int64_t)j0 * n, (size_t)n * sizeof(T),
+                                                  cudaMemcpyDeviceToDevice, st), -1);
+            k_seti<<<1, 1, 0, st>>>(z.jdev, j0);
+            NSS_CUDA_TRY_R(c, cudaGraphLaunch(z.gx, st), -1);
+            c.launches += 1 + z.gx_launches;
+            ++c.graph_replays;
+            from_v = false;
+            cudaEventRecord(evs[slot], st);
+            return jend;
+        }
         for (int jj = j0; jj < jend; ++jj) {
             if (hv_t<T>(c, V + (int64_t)jj * n, w, z.flags + F_STOP)) return -1;
             oa.j = jj;
@@ -1896,7 +1940,49 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
                 return -1;
             }
         }
+        from_v = false;
         cudaEventRecord(evs[slot], st);
+        if (graphable && !key_ok) {
+            // record (not run) the iterations of a chunk: H*psi of vcur, then
+            // k_orth stepping *jdev and writing the next vector to vcur
+            if (z.gx) {
+                cudaGraphExecDestroy(z.gx);
+                z.gx = nullptr;
+            }
+            OrthArgs og = oa;
+            og.jdev = z.jdev;
+            og.vcur = z.vcur;
+            const int64_t l0 = c.launches;
+            cudaGraph_t g = nullptr;
+            bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            for (int it = 0; ok && it < CHECK; ++it) {
+                if (hv_t<T>(c, (const T *)z.vcur, w, z.flags + F_STOP)) ok = false;
+                void *args[] = {&og};
+                if (ok && cudaLaunchCooperativeKernel((const void *)k_orth<T, CW>, dim3(z.orth_grid),
+                                                      dim3(ORTH_THREADS), args, z.orth_smem, st) != cudaSuccess)
+                    ok = false;
+            }
+            const cudaError_t ee = cudaStreamEndCapture(st, &g);
+            ok = ok && ee == cudaSuccess && g && cudaGraphInstantiate(&z.gx, g, 0) == cudaSuccess;
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();                      // a failed capture leaves nothing behind
+            if (ok) {
+                z.gx_gen = c.sb.gen;
+                z.gx_prec = prec;
+                z.gx_mmax = mmax;
+                z.gx_anc = oa.anc_u;
+                z.gx_ndefl = oa.ndefl;
+                z.gx_spin = oa.spin;
+                z.gx_launches = (int)(c.launches - l0);
+                ++c.graph_captures;
+            } else {
+                if (z.gx) cudaGraphExecDestroy(z.gx);
+                z.gx = nullptr;
+                z.gx_failed = true;
+                c.err.clear();
+            }
+            c.launches = l0;
+        }
         return jend;
     };
     std::vector<double> theta(4, 0.0), resid(4, 0.0), upper(4, 0.0), svec, work;
@@ -2001,6 +2087,10 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
         cudaEventDestroy(ct.a);
         cudaEventDestroy(ct.b);
     }
+    if ((rc || ce != cudaSuccess) && z.gx) {   // a failed run keeps no graph
+        cudaGraphExecDestroy(z.gx);
+        z.gx = nullptr;
+    }
     if (rc) return rc;
     if (ce != cudaSuccess) { c.err = cudaGetErrorString(ce); return NSS_ERR_CUDA; }
     int dflags[F_NFLAGS];
@@ -2070,7 +2160,8 @@ int run_lanczos(Ctx &c, T *V, T *w, int neigen, int mmax, double tol, uint64_t s
 void lanczos_release(Ctx &c) {
     DevLanczos &z = c.lz;
     void *ptrs[] = {z.V, z.w, z.V32, z.w32, z.anc32, z.wbuf32, z.slot32, z.evecs, z.rrw, z.scal, z.part, z.counter,
-                    z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags, z.pitem};
+                    z.alpha, z.beta, z.theta, z.resid, z.svec, z.flags, z.pitem, z.vcur, z.jdev};
+    if (z.gx) cudaGraphExecDestroy(z.gx);
     for (void *p : ptrs) ctx_free(c, p);
     if (z.h_flags) cudaFreeHost(z.h_flags);
     if (z.h_ab) cudaFreeHost(z.h_ab);
@@ -2093,6 +2184,8 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
     if (rc) return rc;
     DevLanczos &z = c.lz;
     c.chunk_ms = 0.0;
+    c.graph_replays = 0;
+    c.graph_captures = 0;
     c.chunk_launches = 0;
     c.chunk_iters = 0;
     c.chunk_cols = 0.0;

@@ -12,6 +12,7 @@
 #include "sector_mma.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -571,6 +572,8 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
     }
     if ((rc = mma_finish(c, plan))) return rc;
     NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    static std::atomic<uint64_t> g_gen{0};
+    s.gen = ++g_gen;
     s.valid = true;
     return NSS_OK;
 }
