@@ -23,6 +23,7 @@ same workload built by the CPU oracle; no GPU code runs on that arm.
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -785,7 +786,7 @@ def run_gpu(args):
             except Exception as e:   # the baseline must never break the GPU line
                 out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
         out["clocks"] = clk_summary
-        print(json.dumps(out))
+        print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out
@@ -862,6 +863,7 @@ def run_reference(args):
 
 
 if __name__ == "__main__":
+    faulthandler.enable(all_threads=True)   # a native crash leaves its Python stack on stderr
     a = parse()
     if a.profile_case:
         run_profile_case(a.profile_case, a.precision)

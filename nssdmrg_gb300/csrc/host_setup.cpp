@@ -31,21 +31,11 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
     // order, each with its matching right sector target - q; inside a sector
     // the left state is the slow index.
     int64_t pos = 0;
-    {
-        int64_t tot = 0;
-        for (size_t ql = 0; ql < lsec.qns.size(); ++ql) {
-            const int rk = rsec.find(qn_sub(target, lsec.qns[ql]));
-            if (rk >= 0) tot += (int64_t)lsec.maps[ql].size() * rsec.maps[rk].size();
-        }
-        sb.sb_states.reserve((size_t)tot);
-    }
     for (size_t ql = 0; ql < lsec.qns.size(); ++ql) {
         const Qn rq = qn_sub(target, lsec.qns[ql]);
         int rk = rsec.find(rq);
         if (rk < 0) continue;
         const std::vector<int> &lmap = lsec.maps[ql], &rmap = rsec.maps[rk];
-        for (int l : lmap)
-            for (int r : rmap) sb.sb_states.push_back((int64_t)l * right.dim + r);
         sb.qns.push_back(lsec.qns[ql]);
         sb.dls.push_back((int)lmap.size());
         sb.drs.push_back((int)rmap.size());
@@ -58,15 +48,24 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
     }
     if (pos == 0) throw std::runtime_error("sb_get_states ERROR: total_states=0. There are no SB states.");
     const int nsb = sb.nsb();
+    // the states of each sector at its offset (sectors fill in parallel)
+    sb.sb_states.resize((size_t)pos);
+    parallel_for(nsb, [&](int k) {
+        int64_t at = sb.offset[k];
+        for (int l : sb.ai[k])
+            for (int r : sb.bi[k]) sb.sb_states[(size_t)at++] = (int64_t)l * right.dim + r;
+    }, pos > 200000);
     std::map<Qn, int> index;
     for (int k = 0; k < nsb; ++k) index.emplace(sb.qns[k], k);
 
     const Csr &hl = left.op("H"), &hr = right.op("H");
     sb.hleft.resize(nsb);
     sb.hright.resize(nsb);
-    run_pair([&] { for (int k = 0; k < nsb; ++k) sb.hleft[k] = csr_filter(hl, sb.ai[k], sb.ai[k]); },
-             [&] { for (int k = 0; k < nsb; ++k) sb.hright[k] = csr_filter(hr, sb.bi[k], sb.bi[k]); },
-             hl.nnz() + hr.nnz() > 40000);
+    parallel_for(2 * nsb, [&](int t) {
+        const int k = t >> 1;
+        if (t & 1) sb.hright[k] = csr_filter(hr, sb.bi[k], sb.bi[k]);
+        else sb.hleft[k] = csr_filter(hl, sb.ai[k], sb.ai[k]);
+    }, hl.nnz() + hr.nnz() > 40000);
 
     auto set_term = [&](int it, int k, int jsb, int hc, Csr a, Csr b, int64_t ro, int64_t co) {
         int idx = it + sb.tnso * k;
@@ -93,20 +92,21 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
         const Csr &szl = left.op("S_z_n"), &spl = left.op("S_p_n");
         const Csr &szr = right.op("S_z_n");
         const Csr smr = csr_transpose(right.op("S_p_n"));
-        for (int k = 0; k < nsb; ++k) {
+        // each sector's terms in their own slots (sectors in parallel)
+        parallel_for(nsb, [&](int k) {
             set_term(0, k, k, 0, csr_scale(csr_filter(szl, sb.ai[k], sb.ai[k]), hij[0]),
                      csr_filter(szr, sb.bi[k], sb.bi[k]), sb.offset[k], sb.offset[k]);
             Qn qm = sb.qns[k];
             qm[0] -= 1.0;
             auto it = index.find(qm);
-            if (it == index.end()) continue;
+            if (it == index.end()) return;
             int j = it->second;
             Csr a2 = csr_scale(csr_filter(spl, sb.ai[k], sb.ai[j]), hij[3]);
             Csr b2 = csr_filter(smr, sb.bi[k], sb.bi[j]);
             Csr a3 = csr_transpose(a2), b3 = csr_transpose(b2);
             set_term(1, k, j, 0, std::move(a2), std::move(b2), sb.offset[k], sb.offset[j]);
             set_term(2, k, j, 1, std::move(a3), std::move(b3), sb.offset[j], sb.offset[k]);
-        }
+        }, szl.nnz() + spl.nnz() > 20000);
     } else {
         // Setup_SuperBlock_Fermion_Direct (src/DMRG_SUPERBLOCK_SETUP.f90:416-693),
         // Norb=1, OBC (fbc=2): tMap(i,io,jo) counts the non-zero couplings.
@@ -125,7 +125,8 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
             cldp[io] = csr_matmul(csr_transpose(left.op(ckey[io])), pl);
             cr[io] = right.op(ckey[io]);
         }
-        for (int k = 0; k < nsb; ++k) {
+        // each sector's terms in their own slots (sectors in parallel)
+        parallel_for(nsb, [&](int k) {
             for (int ispin = 0; ispin < 2; ++ispin) {
                 Qn qm = sb.qns[k];
                 qm[ispin] -= 1.0;   // qnup = [1,0], qndw = [0,1]
@@ -141,7 +142,7 @@ SbHost sb_build(const Block &left, const Block &right, const Qn &target, const d
                 set_term(tmap[1][io][jo], k, j, 0, std::move(a1), std::move(b1), sb.offset[k], sb.offset[j]);
                 set_term(tmap[2][io][jo], k, j, 1, std::move(a2), std::move(b2), sb.offset[j], sb.offset[k]);
             }
-        }
+        }, cldp[0].nnz() + cr[0].nnz() > 20000);
     }
     return sb;
 }

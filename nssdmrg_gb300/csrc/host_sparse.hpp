@@ -7,7 +7,10 @@
 // the superblock solve itself runs on the GPU.
 #pragma once
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <cstdlib>
 #include <exception>
 #include <map>
 #include <memory>
@@ -17,13 +20,25 @@
 
 namespace nss {
 
+// Host threads a parallel host loop may use, the caller's included:
+// NSS_HOST_THREADS if set to a positive number (1 runs every loop on the
+// calling thread), else no cap beyond each loop's own.  Read once.
+inline int host_threads_cap() {
+    static const int cap = [] {
+        const char *e = std::getenv("NSS_HOST_THREADS");
+        const int v = e ? std::atoi(e) : 0;
+        return v > 0 ? v : 1 << 20;
+    }();
+    return cap;
+}
+
 // f0 on the calling thread and f1 on a second one (the two sides of a DMRG
 // step are independent); an exception of either is rethrown after both
 // have finished, f0's first.  With parallel false (work too small to pay
 // for a thread, ~20 us) both run here, f0 first.
 template <class F0, class F1>
 void run_pair(F0 &&f0, F1 &&f1, bool parallel = true) {
-    if (!parallel) {
+    if (!parallel || host_threads_cap() < 2) {
         f0();
         f1();
         return;
@@ -44,6 +59,36 @@ void run_pair(F0 &&f0, F1 &&f1, bool parallel = true) {
     th.join();
     if (e0) std::rethrow_exception(e0);
     if (e1) std::rethrow_exception(e1);
+}
+
+// f(i) for i in [0, n) on up to `threads` threads (the caller's among them),
+// indices handed out one at a time; with parallel false, or n < 2, all run
+// here in order.  The first exception is rethrown after every thread ends.
+template <class F>
+void parallel_for(int n, F &&f, bool parallel = true, int threads = 8) {
+    threads = std::min(threads, host_threads_cap());
+    if (!parallel || n < 2 || threads < 2) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = std::min(std::min(n, threads), hw > 1 ? (int)hw : 2);
+    std::atomic<int> next{0};
+    std::vector<std::exception_ptr> errs(nt);
+    auto work = [&](int t) {
+        try {
+            for (int i; (i = next.fetch_add(1)) < n;) f(i);
+        } catch (...) {
+            errs[t] = std::current_exception();
+            next.store(n);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (std::thread &x : th) x.join();
+    for (const std::exception_ptr &e : errs)
+        if (e) std::rethrow_exception(e);
 }
 
 // CSR matrix, 0-based.  Explicit zeros that arise from arithmetic are kept,

@@ -154,13 +154,20 @@ int stage_commit(Ctx &c, Stager &sg) {
         NSS_CUDA_TRY(c, cudaHostAlloc((void **)&c.sb_stage, cap, cudaHostAllocDefault));
         c.sb_stage_cap = cap;
     }
-    const size_t half = sg.items.size() / 2;
-    auto fill = [&](size_t i0, size_t i1) {
-        for (size_t i = i0; i < i1; ++i)
-            if (sg.items[i].bytes && sg.items[i].src)
-                std::memcpy(c.sb_stage + sg.items[i].off, sg.items[i].src, sg.items[i].bytes);
+    // the staging copy in pieces of at most 1 MiB, spread over host threads
+    struct Piece {
+        char *dst;
+        const char *src;
+        size_t bytes;
     };
-    run_pair([&] { fill(0, half); }, [&] { fill(half, sg.items.size()); }, sg.total > ((size_t)4 << 20));
+    std::vector<Piece> pieces;
+    constexpr size_t PIECE = (size_t)1 << 20;
+    for (const auto &it : sg.items)
+        if (it.bytes && it.src)
+            for (size_t o = 0; o < it.bytes; o += PIECE)
+                pieces.push_back({c.sb_stage + it.off + o, (const char *)it.src + o, std::min(PIECE, it.bytes - o)});
+    parallel_for((int)pieces.size(), [&](int i) { std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes); },
+                 sg.total > ((size_t)4 << 20));
     NSS_CUDA_TRY(c, cudaMemcpyAsync(c.sb_arena, c.sb_stage, sg.total, cudaMemcpyHostToDevice, c.stream));
     for (const auto &it : sg.items) {
         *it.dst = (void *)(c.sb_arena + it.off);
@@ -303,21 +310,30 @@ int sb_upload(Ctx &c, const nss_sb_desc *d, bool trusted) {
             }
         },
         [&] {
+            std::vector<int64_t> at(2 * (size_t)s.nsb);
             for (int side = 0; side < 2; ++side) {
                 PackedRows &P = pk[side];
                 P.col.resize((size_t)(side ? nnz_r : nnz_l));
                 P.val.resize((size_t)(side ? nnz_r : nnz_l));
-                int64_t at = 0;
+                int64_t a = 0;
                 for (int k = 0; k < s.nsb; ++k) {
+                    at[(size_t)side * s.nsb + k] = a;
                     const nss_csr &M = side ? d->hright[k] : d->hleft[k];
-                    const int nz = M.rowptr[M.nrow];
-                    if (nz) {
-                        std::memcpy(P.col.data() + at, M.colidx, sizeof(int) * (size_t)nz);
-                        std::memcpy(P.val.data() + at, M.vals, sizeof(double) * (size_t)nz);
-                    }
-                    at += nz;
+                    a += M.rowptr[M.nrow];
                 }
             }
+            // the sectors' entries copied in parallel
+            parallel_for(2 * s.nsb, [&](int t) {
+                const int side = t / s.nsb, k = t % s.nsb;
+                PackedRows &P = pk[side];
+                const nss_csr &M = side ? d->hright[k] : d->hleft[k];
+                const int nz = M.rowptr[M.nrow];
+                const int64_t o = at[(size_t)t];
+                if (nz) {
+                    std::memcpy(P.col.data() + o, M.colidx, sizeof(int) * (size_t)nz);
+                    std::memcpy(P.val.data() + o, M.vals, sizeof(double) * (size_t)nz);
+                }
+            }, big_pool, 6);
         },
         big_pool);
 

@@ -167,6 +167,7 @@ struct Side {
     std::vector<std::vector<int>> pidx;   // [op][qr * nb + qc] -> pair or -1
     int64_t o_tot = 0, t_tot = 0, r_tot = 0, u_tot = 0;
     int64_t nent = 0;                     // operator entries inside kept block pairs
+    std::vector<int64_t> ent_first;       // per operator: its first entry (extract order)
 };
 
 // kept columns per block, state maps and the nonzero block pairs of every
@@ -196,7 +197,9 @@ void scan_side(Side &s) {
             }
         }
     s.pidx.assign(blk.ops.size(), std::vector<int>((size_t)nb * nb, -1));
+    s.ent_first.assign(blk.ops.size() + 1, 0);
     for (size_t io = 0; io < blk.ops.size(); ++io) {
+        s.ent_first[io] = s.nent;
         const Csr &m = blk.ops[io].m;
         for (int r = 0; r < m.nrow; ++r) {
             const int qr = r < mblock ? s.bof[r] : -1;
@@ -216,6 +219,7 @@ void scan_side(Side &s) {
             }
         }
     }
+    s.ent_first[blk.ops.size()] = s.nent;
 }
 
 // the operators' entries inside kept block pairs as (position in the
@@ -226,8 +230,9 @@ void extract_side(const Side &s, RnEntry *ent, int64_t ob) {
     const KeptLayout &kl = *s.kl;
     const Block &blk = *s.blk;
     const int nb = s.nb, mblock = blk.dim;
-    int64_t at = 0;
-    for (size_t io = 0; io < blk.ops.size(); ++io) {
+    // the operators in parallel, each from its first entry
+    parallel_for((int)blk.ops.size(), [&](int io) {
+        int64_t at = s.ent_first[io];
         const Csr &m = blk.ops[io].m;
         const std::vector<int> &pi = s.pidx[io];
         for (int r = 0; r < m.nrow; ++r) {
@@ -242,7 +247,7 @@ void extract_side(const Side &s, RnEntry *ent, int64_t ob) {
                 ent[at++] = RnEntry{ob + pr.o_off + (int64_t)s.lof[cc] * kl.dims[qr] + rowbase, m.val[e]};
             }
         }
-    }
+    }, s.nent > 50000);
 }
 
 // O' in CSR, rows and columns in kept order, exact zeros dropped; hres is
@@ -254,8 +259,9 @@ void assemble_side(Side &s, const double *hres) {
     const int nb = s.nb, ms = s.ms;
     std::vector<std::vector<int>> jof(nb);
     for (int j = 0; j < ms; ++j) jof[kl.q[j]].push_back(j);
-    std::vector<std::pair<int, double>> row;
-    for (size_t io = 0; io < blk.ops.size(); ++io) {
+    // the operators in parallel (each writes only its own matrix)
+    parallel_for((int)blk.ops.size(), [&](int io) {
+        std::vector<std::pair<int, double>> row;
         std::vector<std::vector<int>> prow(nb);   // pairs of this operator by row block
         for (int key = 0; key < nb * nb; ++key)
             if (s.pidx[io][key] >= 0) prow[key / nb].push_back(s.pidx[io][key]);
@@ -282,7 +288,7 @@ void assemble_side(Side &s, const double *hres) {
             out.rowptr[j + 1] = (int)out.col.size();
         }
         blk.ops[io].m = std::move(out);
-    }
+    }, s.r_tot > 50000);
     blk.dim = ms;
     blk.basis.clear();
     for (const Qn &q : *s.kept_qn) blk.basis.insert(blk.basis.end(), q.begin(), q.end());

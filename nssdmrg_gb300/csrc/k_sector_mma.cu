@@ -59,6 +59,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -460,26 +461,28 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_sector_mma(const __grid_const
 
 namespace {
 
+// the driver's tensor-map encoder, looked up once (thread-safe: contexts
+// of several host threads may plan at the same time)
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
 template <int BN, int KPS>
 int launch_mma(Ctx &c, const CUtensorMap &ma, const CUtensorMap &mb, uint32_t spin, const int *stop) {
-    static bool done = false;
-    if (!done) {
+    static std::atomic<bool> done{false};
+    if (!done.load()) {
         NSS_CUDA_TRY(c, cudaFuncSetAttribute(k_sector_mma<BN, KPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              MmaCfg<BN>::SMEM));
-        done = true;
+        done.store(true);
     }
     DevSb &s = c.sb;
     k_sector_mma<BN, KPS><<<s.mma_grid, MM_THREADS, MmaCfg<BN>::SMEM, c.stream>>>(
