@@ -165,8 +165,10 @@ int nss_eigh_batch(nss_ctx *const *ctxs, int nb, int nitermax, double tol, const
  * nss_batch_add returned, negative when that solve failed; energies[q] its
  * FP64 energy; the context keeps the ground state for nss_rdm).  `host`
  * provides the device, the stream and the barrier; it may also be one of
- * the solving contexts.  At most one batch per host context.  No
- * counterpart in the reference. */
+ * the solving contexts.  At most one batch per host context.  A round that
+ * fails (nss_batch_step returns non-zero) drops every solve in flight: their
+ * contexts leave the batch unsolved, may be solved alone or freed, and may
+ * join again.  No counterpart in the reference. */
 typedef struct nss_batch nss_batch;
 nss_batch *nss_batch_create(nss_ctx *host);
 int nss_batch_add(nss_batch *b, nss_ctx *ctx, uint64_t seed, int nitermax, double tol, int *id);

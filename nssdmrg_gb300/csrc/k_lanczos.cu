@@ -2894,7 +2894,18 @@ int batch_add(BatchEngine *E, Ctx &c, uint64_t seed, int nitermax, double tol, i
 }
 
 int batch_step(BatchEngine *E, int max_done, int *ndone, int *ids, double *energies, int *numops) {
-    return engine_step(*E, max_done, ndone, ids, energies, numops);
+    const int rc = engine_step(*E, max_done, ndone, ids, energies, numops);
+    if (rc) {
+        // a failed round drops every solve in flight, so that the engine
+        // holds no context its caller may now solve alone or release; the
+        // shared barrier and error word start the next round cleared
+        E->solves.clear();
+        if (ndone) *ndone = 0;
+        Ctx &c0 = *E->c0;
+        cudaMemsetAsync(c0.lz.counter, 0, 4 * sizeof(unsigned), c0.stream);
+        cudaMemsetAsync(c0.lz.flags, 0, F_NFLAGS * sizeof(int), c0.stream);
+    }
+    return rc;
 }
 
 int batch_inflight(const BatchEngine *E) { return (int)E->solves.size(); }

@@ -1531,8 +1531,12 @@ int syev_trd(const double *rho, const int64_t *rho_off, const int *dims, const i
 // clusters of that size with this shared memory, else 8) and the largest
 // block it takes
 int syev_trd_cl_size(int *nmax_out) {
-    static int csize = 0, nmax = 0;
-    if (!csize) {
+    struct Limits {
+        int csize, nmax;
+    };
+    // found once per process (thread-safe initialisation)
+    static const Limits lim = [] {
+        int csize = 0, nmax = 0;
         cudaFuncSetAttribute(k_trd_cl<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaFuncSetAttribute(k_trd_cl<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         const int smem = 200 * 1024;
@@ -1558,9 +1562,10 @@ int syev_trd_cl_size(int *nmax_out) {
             if ((size_t)((nc2 + 4) * (size_t)nn + 2 * nc2 + 8) * sizeof(double) > 200u * 1024u) break;
             nmax = nn;
         }
-    }
-    if (nmax_out) *nmax_out = nmax;
-    return csize;
+        return Limits{csize, nmax};
+    }();
+    if (nmax_out) *nmax_out = lim.nmax;
+    return lim.csize;
 }
 
 int syev_trd_cl(const double *rho, const int64_t *rho_off, const int *dims, const int *ev_off, const int *blocks,

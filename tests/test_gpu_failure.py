@@ -145,3 +145,35 @@ def test_tensor_core_pipeline_wait_runs_out_then_recovers(nss, monkeypatch):
     ev, _, _ = s.sb_diag(neigen=1, tol=1e-12, precision=nss.NSS_PREC_MIXED, want_vectors=False)
     ref = z["oracle_gs_energy"][0]
     assert abs(ev[0] - ref) <= 1e-10 * abs(ref)
+
+
+def test_batch_round_wait_runs_out_drops_solves(nss, monkeypatch):
+    """A continuous-batching round whose grid barrier gives up: the step
+    reports NSS_ERR_CUDA and the engine drops every solve in flight, so a
+    dropped context may be freed at once; the engine then solves a context
+    that joins again, to the oracle's energy."""
+    z, l, r, sb, ds = _setup("c2_small.npz")
+    host, other = nss.Superblock(), nss.Superblock()
+    _upload(host, l, r, sb, ds)
+    _upload(other, l, r, sb, ds)
+    eng = nss.BatchEngine(host)
+    eng.add(host, seed=1)
+    eng.add(other, seed=2)
+    monkeypatch.setenv("NSS_WAIT_LIMIT", "0")
+    with pytest.raises(nss.NssError) as ei:
+        eng.step()
+    assert ei.value.code == nss.NSS_ERR_CUDA and "timed out" in str(ei.value), str(ei.value)
+    assert eng.inflight == 0
+    monkeypatch.delenv("NSS_WAIT_LIMIT")
+    other.close()
+    eng.add(host, seed=3)
+    done = []
+    for _ in range(10000):
+        done += eng.step()
+        if eng.inflight == 0:
+            break
+    eng.close()
+    assert len(done) == 1 and done[0][0] > 0
+    ref = z["oracle_gs_energy"][0]
+    assert abs(done[0][1] - ref) <= 1e-10 * abs(ref)
+    host.close()
