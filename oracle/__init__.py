@@ -3,7 +3,8 @@
 Test infrastructure only: this package restates the reference library's
 algorithm on the CPU so that the CUDA path can be checked against it.  Only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import it, and only as the checker; nothing in the shipped
+``bench.py`` may import it, and only as the reference the results are
+compared with (or timed against); nothing in the shipped
 package ``nssdmrg_gb300`` imports, links or executes anything from here.
 
 Parity pins (checked by ``tests/test_oracle_pins.py``): the reference's own

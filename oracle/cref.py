@@ -1,7 +1,7 @@
 """ctypes view of the oracle's C restatement (libnss_oracle.so).
 
 Test infrastructure and the timed CPU baseline only.  Defines its own
-mirror of the nss_sb_desc layout of include/nssdmrg.h so that the checker
+mirror of the nss_sb_desc layout of include/nssdmrg.h so that the oracle
 does not depend on the shipped package.
 """
 from __future__ import annotations

@@ -1,8 +1,8 @@
 """Host thread helpers of the library (csrc/host_sparse.hpp): parallel_for
 and run_pair, with and without the NSS_HOST_THREADS cap.
 
-The header is compiled here with the host C++ compiler into a small
-checker program; no GPU and no CUDA toolkit are involved.  The program
+The header is compiled here with the host C++ compiler into a small test
+program; no GPU and no CUDA toolkit are involved.  The program
 prints one line per check; the test reads them back.
 """
 import os
@@ -82,7 +82,7 @@ int main() {
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def helper_exe(tmp_path_factory):
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no host C++ compiler")
@@ -105,8 +105,8 @@ def _run(exe, threads=None):
     return {ln.split()[0]: ln.split()[1:] for ln in out.stdout.splitlines()}
 
 
-def test_parallel_for_covers_every_index_once(checker):
-    res = _run(checker)
+def test_parallel_for_covers_every_index_once(helper_exe):
+    res = _run(helper_exe)
     bad, nthreads = int(res["cover"][0]), int(res["cover"][1])
     assert bad == 0
     if (os.cpu_count() or 1) > 1:
@@ -117,8 +117,8 @@ def test_parallel_for_covers_every_index_once(checker):
     assert res["cap"] == ["0"]
 
 
-def test_host_thread_cap_of_one_runs_on_the_caller(checker):
-    res = _run(checker, threads=1)
+def test_host_thread_cap_of_one_runs_on_the_caller(helper_exe):
+    res = _run(helper_exe, threads=1)
     assert res["cover"] == ["0", "1"]          # every index, one thread
     assert res["serial"] == ["0", "1", "2", "3", "10"]
     assert res["throw"][:2] == ["index", "700"]
