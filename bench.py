@@ -86,7 +86,7 @@ def dist_env():
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -94,6 +94,7 @@ class Clocks:
         self.device = device
         self.enabled = enabled
         self.proc = None
+        self.t_start = self.t_end = None
         # the samples go next to the run's other outputs when NSS_CLOCKS_DIR
         # names a folder, else to the system's temporary folder
         out_dir = os.environ.get("NSS_CLOCKS_DIR")
@@ -106,11 +107,23 @@ class Clocks:
             self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            # the sampler is running once its first line is out (up to 3 s)
+            for _ in range(300):
+                if self.path.stat().st_size > 0 or self.proc.poll() is not None:
+                    break
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
+
+    def mark_start(self):
+        """The timed region starts (host wall clock)."""
+        self.t_start = time.time()
+
+    def mark_end(self):
+        self.t_end = time.time()
 
     def __exit__(self, *a):
         if self.proc:
@@ -126,21 +139,44 @@ class Clocks:
             return None
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return self.summarize(self.path.read_text(), self.t_start, self.t_end)
+
+    @staticmethod
+    def summarize(text, t_start=None, t_end=None):
+        """Median SM clock, maximum clock and throttle reasons of the samples
+        taken inside [t_start, t_end] (host wall clock); when the region is
+        shorter than the sampling period and holds none, the samples within
+        0.25 s of it (the warm-up of the same workload)."""
+        from datetime import datetime
         rows = []
-        for line in self.path.read_text().splitlines():
+        for line in text.splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+                sm, smax = float(parts[2]), float(parts[3])
             except ValueError:
                 continue
+            try:
+                ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None                  # an unexpected stamp: the row still counts for the whole run
+            rows.append((ts, sm, smax, parts[6:10]))
+        window = "sampler run"
+        if rows and t_start is not None and t_end is not None and all(r[0] is not None for r in rows):
+            inside = [r for r in rows if t_start <= r[0] <= t_end]
+            if inside:
+                rows, window = inside, "timed region"
+            else:
+                near = [r for r in rows if t_start - 0.25 <= r[0] <= t_end + 0.25]
+                if near:
+                    rows, window = near, "within 0.25 s of the timed region"
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, r in rows for i, x in enumerate(r) if x.lower() == "active"})
-        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "samples": len(rows), "reasons": reasons}
+        reasons = sorted({names[i] for _, _, _, r in rows for i, x in enumerate(r) if x.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in rows), "sm_max_mhz": max(r[2] for r in rows),
+                "samples": len(rows), "window": window, "reasons": reasons}
 
 
 CORE_PROBE: dict = {}
@@ -546,15 +582,18 @@ def run_gpu(args):
         return ev, numop, res
 
     def time_path(p, steps, sample_clocks):
-        for w in range(args.warmup):
-            solve(100 + w, p)
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        l0 = sb.launches
-        times, numops, energies, ents, t_eigh = [], [], [], [], []
-        torch.cuda.nvtx.range_push("bench_timed")
+        # the clock sampler runs from before the warm-up; its summary keeps
+        # the samples of the timed region
         with Clocks(local, enabled=sample_clocks) as clk:
+            for w in range(args.warmup):
+                solve(100 + w, p)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            l0 = sb.launches
+            times, numops, energies, ents, t_eigh = [], [], [], [], []
+            torch.cuda.nvtx.range_push("bench_timed")
+            clk.mark_start()
             for s in range(steps):
                 flush.zero_()                      # evict L2 between timed steps
                 torch.cuda.synchronize()
@@ -570,7 +609,8 @@ def run_gpu(args):
                 numops.append(numop)
                 energies.append(float(ev[0]))
                 ents.append(res.entropy[0])
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            clk.mark_end()
         torch.cuda.nvtx.range_pop()
         t_total = sum(times)
         if world > 1:
