@@ -15,6 +15,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -35,22 +36,29 @@ inline int host_threads_cap() {
 // f0 on the calling thread and f1 on a second one (the two sides of a DMRG
 // step are independent); an exception of either is rethrown after both
 // have finished, f0's first.  With parallel false (work too small to pay
-// for a thread, ~20 us) both run here, f0 first.
+// for a thread, ~20 us), or when no thread can be started, both run here,
+// f0 first.
 template <class F0, class F1>
 void run_pair(F0 &&f0, F1 &&f1, bool parallel = true) {
-    if (!parallel || host_threads_cap() < 2) {
+    std::exception_ptr e0, e1;
+    std::thread th;
+    if (parallel && host_threads_cap() >= 2) {
+        try {
+            th = std::thread([&] {
+                try {
+                    f1();
+                } catch (...) {
+                    e1 = std::current_exception();
+                }
+            });
+        } catch (const std::system_error &) {
+        }
+    }
+    if (!th.joinable()) {
         f0();
         f1();
         return;
     }
-    std::exception_ptr e0, e1;
-    std::thread th([&] {
-        try {
-            f1();
-        } catch (...) {
-            e1 = std::current_exception();
-        }
-    });
     try {
         f0();
     } catch (...) {
@@ -63,7 +71,8 @@ void run_pair(F0 &&f0, F1 &&f1, bool parallel = true) {
 
 // f(i) for i in [0, n) on up to `threads` threads (the caller's among them),
 // indices handed out one at a time; with parallel false, or n < 2, all run
-// here in order.  The first exception is rethrown after every thread ends.
+// here in order.  If the system starts fewer threads, the ones running take
+// all indices.  The first exception is rethrown after every thread ends.
 template <class F>
 void parallel_for(int n, F &&f, bool parallel = true, int threads = 8) {
     threads = std::min(threads, host_threads_cap());
@@ -84,7 +93,13 @@ void parallel_for(int n, F &&f, bool parallel = true, int threads = 8) {
         }
     };
     std::vector<std::thread> th;
-    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    for (int t = 1; t < nt; ++t) {
+        try {
+            th.emplace_back(work, t);
+        } catch (const std::system_error &) {   // no more threads: those started share the rest
+            break;
+        }
+    }
     work(0);
     for (std::thread &x : th) x.join();
     for (const std::exception_ptr &e : errs)
