@@ -30,6 +30,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -136,10 +137,17 @@ void admit_loop(Server *S) {
         auto r = S->pending.front();
         S->pending.pop_front();
         r->t_admit = clk::now();
+        try {
+            S->workers.emplace_back(run_request, S, r);
+        } catch (const std::system_error &) {   // no thread for it: the request fails, the server goes on
+            r->status = NSS_ERR_NOMEM;
+            r->t_done = clk::now();
+            S->finished.push_back(r);
+            continue;
+        }
         S->in_use += r->footprint;
         S->peak_in_use = std::max(S->peak_in_use, S->in_use);
         ++S->running;
-        S->workers.emplace_back(run_request, S, r);
     }
 }
 

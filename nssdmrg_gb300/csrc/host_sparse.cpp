@@ -3,7 +3,6 @@
 
 #include <algorithm>
 #include <stdexcept>
-#include <thread>
 
 namespace nss {
 
@@ -130,10 +129,9 @@ Csr csr_kron_sum(int na, int nb, const std::vector<KronTerm> &terms, int nthread
                 P.rowlen.push_back((int)P.col.size() - start);
             }
     };
-    std::vector<std::thread> th;
-    for (int ti = 1; ti < nthreads; ++ti) th.emplace_back(work, ti);
-    work(0);
-    for (auto &t : th) t.join();
+    // the row ranges on threads (parallel_for: exceptions reach the caller,
+    // parts no thread takes run here); assembled below in row order
+    parallel_for(nthreads, work, nthreads > 1, nthreads);
     Csr c;
     c.init(n, n);
     size_t nnz = 0;
