@@ -30,6 +30,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <system_error>
 #include <thread>
 #include <vector>
@@ -285,14 +286,31 @@ nss_server *nss_server_create(int device, size_t hbm_budget) {
         delete S;
         return nullptr;
     }
-    S->eng = nss::batch_create(nss::ctx_of(S->host));
+    try {
+        S->eng = nss::batch_create(nss::ctx_of(S->host));
+    } catch (const std::exception &) {
+        S->eng = nullptr;
+    }
     if (!S->eng) {
         nss_destroy(S->host);
         delete S;
         return nullptr;
     }
-    S->admitter = std::thread(nss::admit_loop, S);
-    S->dispatcher = std::thread(nss::dispatch_loop, S);
+    try {
+        S->admitter = std::thread(nss::admit_loop, S);
+        S->dispatcher = std::thread(nss::dispatch_loop, S);
+    } catch (const std::system_error &) {   // no threads: no server (nothing was submitted yet)
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->stop = true;
+            S->cv.notify_all();
+        }
+        if (S->admitter.joinable()) S->admitter.join();
+        nss::batch_destroy(S->eng);
+        nss_destroy(S->host);
+        delete S;
+        return nullptr;
+    }
     return (nss_server *)S;
 }
 
@@ -304,18 +322,22 @@ int nss_server_submit(nss_server *sv, const nss_dmrg_params *p, int *id) {
     auto *S = (Server *)sv;
     if (!S || !p || !id) return NSS_ERR_INVALID;
     if (p->lanc_neigen > 1) return NSS_ERR_INVALID;   // the engine solves ground states
-    auto r = std::make_shared<nss::Request>();
-    r->p = *p;
-    if (p->msweep && p->nsweep > 0) r->msweep.assign(p->msweep, p->msweep + p->nsweep);
-    if (p->esweep && p->nsweep > 0) r->esweep.assign(p->esweep, p->esweep + p->nsweep);
-    r->p.lanc_neigen = 1;
-    r->footprint = nss::serve_footprint(*p, p->msweep, p->nsweep);
-    r->t_submit = nss::clk::now();
-    std::lock_guard<std::mutex> lk(S->mu);
-    r->id = S->next_id++;
-    *id = r->id;
-    S->pending.push_back(r);
-    S->cv.notify_all();
+    try {
+        auto r = std::make_shared<nss::Request>();
+        r->p = *p;
+        if (p->msweep && p->nsweep > 0) r->msweep.assign(p->msweep, p->msweep + p->nsweep);
+        if (p->esweep && p->nsweep > 0) r->esweep.assign(p->esweep, p->esweep + p->nsweep);
+        r->p.lanc_neigen = 1;
+        r->footprint = nss::serve_footprint(*p, p->msweep, p->nsweep);
+        r->t_submit = nss::clk::now();
+        std::lock_guard<std::mutex> lk(S->mu);
+        r->id = S->next_id++;
+        *id = r->id;
+        S->pending.push_back(r);
+        S->cv.notify_all();
+    } catch (const std::bad_alloc &) {
+        return NSS_ERR_NOMEM;
+    }
     return NSS_OK;
 }
 
