@@ -248,9 +248,11 @@ int nss_tridiag_lowest(int m, const double *a, const double *b, int ne, double b
         g_err = "nss_tridiag_lowest: need 0 < ne <= m and non-NULL arrays";
         return NSS_ERR_INVALID;
     }
-    std::vector<double> work;
-    nss::tridiag_lowest(a, b, m, ne, b_last, theta, s, resid, nullptr, work);
-    return NSS_OK;
+    return guarded(nullptr, [&] {
+        std::vector<double> work;
+        nss::tridiag_lowest(a, b, m, ne, b_last, theta, s, resid, nullptr, work);
+        return NSS_OK;
+    });
 }
 
 int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, double *Z) {
@@ -258,14 +260,16 @@ int nss_tridiag_eig(int n, const double *d, const double *e, double *evals, doub
         g_err = "nss_tridiag_eig: need n > 0 and non-NULL arrays";
         return NSS_ERR_INVALID;
     }
-    std::vector<double> dd(d, d + n), ee(n, 0.0);
-    for (int i = 0; i + 1 < n; ++i) ee[i] = e[i];
-    if (!nss::tridiag_ql(n, dd.data(), ee.data(), Z)) {
-        g_err = "nss_tridiag_eig: an eigenvalue did not converge in 60 QL iterations";
-        return NSS_ERR_NOCONV;
-    }
-    std::copy(dd.begin(), dd.end(), evals);
-    return NSS_OK;
+    return guarded(nullptr, [&] {
+        std::vector<double> dd(d, d + n), ee(n, 0.0);
+        for (int i = 0; i + 1 < n; ++i) ee[i] = e[i];
+        if (!nss::tridiag_ql(n, dd.data(), ee.data(), Z)) {
+            g_err = "nss_tridiag_eig: an eigenvalue did not converge in 60 QL iterations";
+            return NSS_ERR_NOCONV;
+        }
+        std::copy(dd.begin(), dd.end(), evals);
+        return NSS_OK;
+    });
 }
 
 int nss_kron_sum(int32_t na, int32_t nb, int32_t nterms, const double *coef, const nss_csr *a, const nss_csr *b,
@@ -323,12 +327,14 @@ int nss_arrow_lowest(int k, double theta0, const double *m, const double *a, con
         g_err = "nss_arrow_lowest: need k >= 0 and non-NULL arrays";
         return NSS_ERR_INVALID;
     }
-    std::vector<double> work;
-    if (!nss::arrow_lowest(theta0, m, a, b, k, b_last, lam, c, resid, work)) {
-        g_err = "nss_arrow_lowest: no root below the tridiagonal spectrum";
-        return NSS_ERR_NOCONV;
-    }
-    return NSS_OK;
+    return guarded(nullptr, [&] {
+        std::vector<double> work;
+        if (!nss::arrow_lowest(theta0, m, a, b, k, b_last, lam, c, resid, work)) {
+            g_err = "nss_arrow_lowest: no root below the tridiagonal spectrum";
+            return NSS_ERR_NOCONV;
+        }
+        return NSS_OK;
+    });
 }
 
 int nss_time_chunks(nss_ctx *ctx, int enable) {
@@ -388,15 +394,17 @@ int nss_hv(nss_ctx *ctx, int64_t n, const double *v, double *hv) {
     if (n != ctx->c.sb.n) return fail(ctx, NSS_ERR_INVALID, "nss_hv: Nloc != superblock dimension");
     if (!v || !hv) return fail(ctx, NSS_ERR_INVALID, "nss_hv: null vector");
     DeviceScope dscope(ctx->c.device);
-    int rc = ensure_tmp(ctx, n);
-    if (rc) return rc;
-    nss::Ctx &c = ctx->c;
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, v, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    rc = nss::hv_device(c, ctx->d_v, ctx->d_hv);
-    if (rc) return rc;
-    NSS_CUDA_TRY(c, cudaMemcpyAsync(hv, ctx->d_hv, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-    return NSS_OK;
+    return guarded(ctx, [&] {
+        int rc = ensure_tmp(ctx, n);
+        if (rc) return rc;
+        nss::Ctx &c = ctx->c;
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(ctx->d_v, v, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        rc = nss::hv_device(c, ctx->d_v, ctx->d_hv);
+        if (rc) return rc;
+        NSS_CUDA_TRY(c, cudaMemcpyAsync(hv, ctx->d_hv, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+        return NSS_OK;
+    });
 }
 
 namespace {
@@ -799,10 +807,12 @@ int nss_dmrg_records(const nss_dmrg *d, nss_step_record *out, int max) {
 int nss_dmrg_export_superblock(nss_dmrg *d, nss_sb_desc *out) {
     if (!d || !out) return NSS_ERR_INVALID;
     if (!d->drv.last_sb) return fail(d->ctx, NSS_ERR_STATE, "nss_dmrg_export_superblock: no superblock built yet");
-    d->last = std::make_unique<nss::SbHost>(*d->drv.last_sb);
-    nss::sb_view(*d->last, d->view);
-    *out = d->view.desc;
-    return NSS_OK;
+    return guarded(d->ctx, [&] {
+        d->last = std::make_unique<nss::SbHost>(*d->drv.last_sb);
+        nss::sb_view(*d->last, d->view);
+        *out = d->view.desc;
+        return NSS_OK;
+    });
 }
 
 }  // extern "C"
