@@ -38,14 +38,17 @@
 //
 // Precision modes.  The kernels are templates over the type T of the Krylov
 // vectors.  T = double is the plain method: FP64 everywhere.  T = float is
-// the mixed method: H*psi in FP32 (k_hv_fp32 / k_hv_tc), the basis and the
+// the mixed method: H*psi in FP32 (k_hv_fp32 on CUDA cores, and the
+// split-TF32 tensor-core sector GEMM k_sector_mma where the plan routes
+// large sectors to it), the basis and the
 // projections in FP32 with FP64 block partial sums, while alpha/beta, the
 // tridiagonal eigensolve and the Ritz vector stay FP64; it runs to a relative
 // residual of MIXED_TOL, and the energy is then refined in FP64 as the
 // Rayleigh quotient psi.H.psi of the FP64 Ritz vector with the FP64 H*psi
 // (error quadratic in the vector error: |dE|/|E| ~ 1e-13 at MIXED_TOL =
 // 1e-7), whose FP64 residual ||H psi - E psi|| is reported.  On GB300 the
-// FP64 pipe runs at 1/64 of the FP32 one, which is what the mixed method buys.
+// FP64 pipe runs at about 1/70 of the FP32 one (1.06 against 78 TFLOP/s
+// measured), which is what the mixed method buys.
 #include "device.cuh"
 #include "host_tridiag.hpp"
 #include "hv_tile.cuh"
