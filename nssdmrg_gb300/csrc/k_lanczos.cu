@@ -1152,7 +1152,7 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
     __shared__ int alive[BATCH_MAX], p2[BATCH_MAX], brkm[BATCH_MAX];
     __shared__ int my_s, any_p2;
     __shared__ int qn[2];
-    const int G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x, grp = tid >> 8, lt = tid & 255;
+    const int blk = blockIdx.x, tid = threadIdx.x, grp = tid >> 8, lt = tid & 255;
     const int ns = B.ns;
     unsigned epoch = 0;
     if (tid == 0) {
@@ -1416,8 +1416,6 @@ __global__ void __launch_bounds__(ORTH_THREADS, 1) k_batch32(BatchArgs B) {
     grid_exit(B.bar);
 }
 
-inline size_t batch_smem(int pstride_max) { return chunk_smem(pstride_max); }
-
 // Ritz vectors: out[e] = sum_l V[l] s_e[l]   (FP64 accumulation, FP64 out)
 template <class T>
 __global__ void __launch_bounds__(256) k_ritz(const T *__restrict__ V, int m, int64_t n,
@@ -1587,6 +1585,7 @@ __global__ void __launch_bounds__(256) k_rot(double *__restrict__ X, int k, int6
 // column-major k x k) of a symmetric k x k matrix a (row-major, destroyed),
 // k <= 4, by cyclic Jacobi rotations.
 void sym_eig_small(int k, double *a, double *lam, double *q) {
+    if (k < 1 || k > 4) return;   // callers pass 1..4
     for (int i = 0; i < k; ++i)
         for (int j = 0; j < k; ++j) q[j * k + i] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 50; ++sweep) {
@@ -1621,8 +1620,14 @@ void sym_eig_small(int k, double *a, double *lam, double *q) {
                 }
             }
     }
+    // ascending by the diagonal: insertion sort (equal values keep their order)
     int ord[4] = {0, 1, 2, 3};
-    std::sort(ord, ord + k, [&](int x, int y) { return a[x * k + x] < a[y * k + y]; });
+    for (int j = 1; j < k; ++j) {
+        const int x = ord[j];
+        int i = j;
+        for (; i > 0 && a[x * k + x] < a[ord[i - 1] * k + ord[i - 1]]; --i) ord[i] = ord[i - 1];
+        ord[i] = x;
+    }
     double qs[16];
     for (int j = 0; j < k; ++j) {
         lam[j] = a[ord[j] * k + ord[j]];
@@ -2317,6 +2322,7 @@ int lanczos_eigh(Ctx &c, int neigen, int nitermax, double tol, uint64_t seed, in
         // W = H U (into the FP64 scratch), G = U^T W, U <- U Q with G's
         // eigenvectors Q in ascending order
         auto rayleigh_ritz = [&](int k) -> int {
+            if (k < 1 || k > 4) { c.err = "nss_eigh: Rayleigh-Ritz over 1 to 4 vectors"; return NSS_ERR_INVALID; }
             ++c.launches;
             normalize_dev<double>(z, z.evecs, n, st, c.launches);
             for (int e = 1; e < k; ++e) {

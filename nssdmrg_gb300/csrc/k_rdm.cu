@@ -740,7 +740,6 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     };
     const size_t o_items = slot(items.size() * sizeof(RhoItem)), o_rho_off = slot(rho_off.size() * sizeof(int64_t)),
                  o_dims = slot(dims.size() * sizeof(int)), o_ev_off = slot(ev_off.size() * sizeof(int)),
-                 o_maps = slot(maps.size() * sizeof(int)), o_map_off = slot(map_off.size() * sizeof(int)),
                  o_own = slot(own.size() * sizeof(int)), o_clu = slot(clu.size() * sizeof(int)),
                  o_big = slot(big.size() * sizeof(int)), o_goff = slot(big.size() * sizeof(int64_t)),
                  o_bis = slot(bis.size() * sizeof(int2)),
@@ -759,8 +758,6 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     put(o_rho_off, rho_off);
     put(o_dims, dims);
     put(o_ev_off, ev_off);
-    put(o_maps, maps);
-    put(o_map_off, map_off);
     put(o_own, own);
     put(o_clu, clu);
     put(o_big, big);
@@ -777,7 +774,6 @@ int rdm_run(Ctx &c, const double *d_psi, int mstates, double estates, double deg
     const RhoItem *d_items = (const RhoItem *)(r.tab + o_items);
     const int64_t *d_rho_off = (const int64_t *)(r.tab + o_rho_off);
     const int *d_dims = (const int *)(r.tab + o_dims), *d_ev_off = (const int *)(r.tab + o_ev_off),
-              *d_maps = (const int *)(r.tab + o_maps), *d_map_off = (const int *)(r.tab + o_map_off),
               *d_own = (const int *)(r.tab + o_own), *d_bmode = (const int *)(r.tab + o_bmode),
               *d_clu = (const int *)(r.tab + o_clu), *d_big = (const int *)(r.tab + o_big);
     const int64_t *d_goff = (const int64_t *)(r.tab + o_goff);
