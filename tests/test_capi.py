@@ -58,3 +58,21 @@ def test_null_context_is_an_error_not_a_crash(libpath):
     L = nss.lib()
     assert L.nss_hv(None, 4, None, None) == nss.NSS_ERR_INVALID
     assert L.nss_sb_dim(None) == 0
+
+
+def test_server_and_batch_without_gpu_fail_cleanly(libpath):
+    """Without a device the server is not created (no threads are left
+    running), and the batch and server entry points refuse NULL handles."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import nssdmrg_gb300 as nss
+    L = nss.lib()
+    assert not L.nss_server_create(0, 1 << 30)
+    assert not L.nss_batch_create(None)
+    assert L.nss_batch_step(None, 1, None, None, None, None) == nss.NSS_ERR_INVALID
+    assert L.nss_batch_inflight(None) == 0
+    assert L.nss_server_submit(None, None, None) == nss.NSS_ERR_INVALID
+    assert L.nss_server_solves(None) == 0
+    L.nss_server_destroy(None)
+    L.nss_batch_destroy(None)
