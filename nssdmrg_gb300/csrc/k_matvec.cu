@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(256) k_dense32(const double *__restrict__ x, f
 }
 
 int stage_commit(Ctx &c, Stager &sg) {
+    // the previous upload's copy out of the staging buffer may still be in
+    // flight on the stream (two uploads with no solve between them)
+    NSS_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
     if (c.sb_arena_cap < sg.total) {
         ctx_free(c, c.sb_arena);
         c.sb_arena = nullptr;
